@@ -1,0 +1,204 @@
+/*
+ * tetemoko_gb300.h -- C ABI of the GB300 (sm_103a) per-level Godunov step of
+ * tetemoko's 2-D velocity-stress elasticity with fault boundaries.
+ *
+ * Every entry point is plain C: pointers, sizes and POD structs only.  A Chombo
+ * build calls these from thin shims that keep the reference's class names
+ * (LinElastLevelGodunov, LinElastPatchGodunov, LEPhysIBC/RSIBC/SWIBC,
+ * LinElastPhysics::plasticUpdate); the shims are shown in INTEGRATION.md.
+ *
+ * Data layout.  State arrays use Chombo's FArrayBox layout: structure of arrays,
+ * i fastest, then j, then component, over the allocated box (valid box grown by
+ * the ghost width).  The 22 state components are those of srcLinElast/LEINDEX.H:12-47
+ * (side 1: vx vy vz sxx syy szz sxy sxz syz lambda gamma; side 2 at +11).
+ * Fault ("boundary") data live on the row of y-lo faces of a patch, indexed by
+ * the face's i, with 11 components for rate-and-state (ibcLinElast/RSINDEX.H:12-22)
+ * and 9 for slip weakening (ibcLinElast/SWIBCF.ChF:32-72).
+ *
+ * Units follow the reference decks: km, km/s, g/cm^3, GPa (G), MPa (stress),
+ * m/s (particle and slip velocity), m (slip, L, Dc), s.
+ *
+ * Errors.  Every call returns a tmk_status code and never aborts the process.
+ * Device kernels never trap: they record the first problem in a device status
+ * word that the host reads after the step (tmk_level_status).
+ */
+#ifndef TETEMOKO_GB300_H
+#define TETEMOKO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TMK_ABI_VERSION 1
+
+#define TMK_NCOMP      22   /* state components, srcLinElast/LEINDEX.H:12-47 */
+#define TMK_NSIDE_COMP 11   /* IX_OFFSET, srcLinElast/LEINDEX.H:23 */
+#define TMK_RS_NBDRY   11   /* rate-and-state boundary components, ibcLinElast/RSINDEX.H */
+#define TMK_SW_NBDRY    9   /* slip-weakening boundary components, ibcLinElast/SWIBC.cpp:63 */
+#define TMK_NGHOST      4   /* m_numGhost for PPM, srcLinElast/LinElastLevelGodunov.cpp:108-115 */
+#define TMK_SW_MAX_PATCHES 8
+
+/* ---- status codes (the reference aborts through MayDay::Error / Fortran stop) ---- */
+typedef enum {
+  TMK_OK                = 0,
+  TMK_ERR_BAD_DESC      = 1,  /* inconsistent box / FAB descriptor or parameter */
+  TMK_ERR_NAN_STATE     = 2,  /* NaN state variable (ibcLinElast/RSIBCF.ChF:133-145 stops) */
+  TMK_ERR_TIMEOUT       = 3,  /* a bounded device wait ran out */
+  TMK_ERR_CUDA          = 4,  /* a CUDA runtime call failed */
+  TMK_ERR_UNSUPPORTED   = 5,  /* option the reference rejects or this build lacks */
+  TMK_ERR_ALLOC         = 6,  /* device allocation failed */
+  TMK_ERR_NO_DEVICE     = 7   /* no CUDA device visible */
+} tmk_status;
+
+/* boundary types of comp.x_boundary / y_boundary (execLinElast/amrGodunov.cpp:571-590) */
+enum { TMK_BC_OUTFLOW = 0, TMK_BC_FREE = 1, TMK_BC_FAULT = 2 };
+/* friction law plugged into the y-lo face (LEPhysIBC subclasses) */
+enum { TMK_FAULT_NONE = 0, TMK_FAULT_RS = 1, TMK_FAULT_SW = 2 };
+/* rate-and-state state evolution: the reference's slip law (ibcLinElast/RSIBCF.ChF:125-132)
+ * or the aging law, an extension absent from the reference */
+enum { TMK_RS_SLIP_LAW = 0, TMK_RS_AGING_LAW = 1 };
+/* slip-weakening side-2 component offset: the reference reads/writes side 2 at
+ * component 9 (ibcLinElast/SWIBCF.ChF:139-147,255-263); 11 is IX_OFFSET */
+enum { TMK_SW_LAYOUT_REFERENCE9 = 0, TMK_SW_LAYOUT_OFFSET11 = 1 };
+/* arithmetic of the volume stencil */
+enum { TMK_PREC_FP64 = 0, TMK_PREC_MIXED = 1 };
+
+/* LEPhysIBC::setFortranCommonLE -> LINELASTSETF (srcLinElast/LinElastPhysicsF.ChF:1149-1210) */
+typedef struct {
+  double cs, cp, G;                       /* G is overridden by rho*cs^2 when rho > 0 */
+  double rho;                             /* <= 0: derive from G (execLinElast/amrGodunov.cpp:206-215) */
+  double sxx0, syy0, szz0, sxy0, sxz0, syz0;
+} tmk_elastic_params;
+
+/* RSIBC constructor -> RSSETF (ibcLinElast/RSIBCF.ChF:8-55, ibcLinElast/RSIBC.cpp:17-51) */
+typedef struct {
+  double r0, x0, y0, nsig, ntime;         /* Gaussian nucleation: nsig*exp(-(x/r0)^2/2) */
+  double a, b, V0, f0, L, fw, Vw, fexp;
+  double ramp_x, ramp_w, ramp_a, ramp_Vw;
+  double rupture_threshold;
+  double psi_init;                        /* RSIBC::initializeBdry psi (ibcLinElast/RSIBC.cpp:158-160) */
+  int    state_law;                       /* TMK_RS_SLIP_LAW (reference) or TMK_RS_AGING_LAW */
+} tmk_rs_params;
+
+/* SWIBC constructor -> SWSETF (ibcLinElast/SWIBCF.ChF:6-27, ibcLinElast/SWIBC.cpp:16-52) */
+typedef struct {
+  double fs, fd, dw, smooth;
+  int    num_patches;
+  double xc[TMK_SW_MAX_PATCHES], xw[TMK_SW_MAX_PATCHES];
+  double zc[TMK_SW_MAX_PATCHES], zw[TMK_SW_MAX_PATCHES];
+  double tau[TMK_SW_MAX_PATCHES];
+  double fric_box_center[2], fric_box_width[2];
+  double outside_friction;
+  double rupture_threshold;
+  int    layout;                          /* TMK_SW_LAYOUT_* */
+} tmk_sw_params;
+
+/* setFortranCommonPlastic -> PLASTICSETF (srcLinElast/PlasticPhysicsF.ChF:6-25).
+ * b (cohesion term) and h (hardening) are hard-wired to 0 in the reference;
+ * non-zero values are an extension. */
+typedef struct { double mu, beta, eta, b, h; } tmk_plastic_params;
+
+/* AMRLevelLinElastFactory / LinElastPatchGodunov::define options */
+typedef struct {
+  int normal_pred_order;                  /* 0 CTU, 2 PPM (srcLinElast/LinElastPatchGodunov.cpp:272-287) */
+  int use_prim_limiting;
+  int use_char_limiting;
+  int boundary_type[6];                   /* x lo, x hi, y lo, y hi, z lo, z hi */
+  int fault_law;                          /* TMK_FAULT_* on the y-lo face when boundary_type[2]==2 */
+  int plasticity;                         /* apply PLASTICCORRECTION after the step */
+  int precision;                          /* TMK_PREC_* for level objects */
+} tmk_scheme;
+
+/* Chombo FArrayBox view: data[((c*(hi1-lo1+1)) + (j-lo1))*(hi0-lo0+1) + (i-lo0)] */
+typedef struct {
+  double* data;
+  int lo[2], hi[2];
+  int ncomp;
+} tmk_fab;
+
+typedef struct { int lo[2], hi[2]; } tmk_box;   /* cell-centred, inclusive */
+
+typedef struct tmk_context_s tmk_context;
+typedef struct tmk_level_s   tmk_level;
+
+/* ---------------------------------------------------------------------------
+ * Parameters (replaces the process-global Fortran COMMON blocks /IBC/, /rs/,
+ * /slipweak/, /PLASTIC/: srcLinElast/IBCCommon.fh:4-6, ibcLinElast/RSCommon.fh:4-5,
+ * ibcLinElast/SWCommon.fh:4-5, srcLinElast/PlasticCommon.fh:4-5).  Contexts are
+ * independent: several scenarios can coexist in one process.
+ * ------------------------------------------------------------------------- */
+int  tmk_abi_version(void);
+tmk_status tmk_context_create(const tmk_elastic_params* elastic,
+                              const tmk_scheme* scheme,
+                              const tmk_rs_params* rs,          /* NULL unless fault_law==RS */
+                              const tmk_sw_params* sw,          /* NULL unless fault_law==SW */
+                              const tmk_plastic_params* plastic,/* NULL unless plasticity */
+                              tmk_context** out);
+void tmk_context_destroy(tmk_context* ctx);
+/* Derived constants of LINELASTSETF: rho, lam, K, Zs, Zp (LinElastPhysicsF.ChF:1172-1176) */
+tmk_status tmk_context_constants(const tmk_context* ctx, double out[5]);
+
+/* ---------------------------------------------------------------------------
+ * Patch step on caller-owned DEVICE FABs (FP64).  Replaces
+ * LinElastPatchGodunov::setCurrentTime/setCurrentBox + LEPhysIBC::setBdryData +
+ * LinElastPatchGodunov::updateState (srcLinElast/LinElastPatchGodunov.H:63-83,
+ * srcLinElast/LinElastPatchGodunov.cpp:101-129).  U must hold 4 filled ghost
+ * cells around `valid` (cells outside `domain` are never read).  B is the
+ * patch's fault FAB (face row j=domain.lo[1], x ghosts filled) or NULL when the
+ * patch does not touch a fault.  F[0], F[1] (optional, may be NULL) receive
+ * the face fluxes of LinElastPhysics::computeUpdate for refluxing; each is a
+ * 22-component FAB over the x- or y-faces of `valid`.  Asynchronous on
+ * `stream` (a cudaStream_t, NULL = legacy default stream).
+ * ------------------------------------------------------------------------- */
+tmk_status tmk_patch_update_state(tmk_context* ctx,
+                                  const tmk_fab* U, const tmk_fab* B,
+                                  const tmk_fab* Fx, const tmk_fab* Fy,
+                                  const tmk_box* valid, const tmk_box* domain,
+                                  double dx, double time, double dt,
+                                  double* max_wave_speed, void* stream);
+
+/* LinElastPhysics::plasticUpdate -> PLASTICCORRECTION on device FAB U over box
+ * (srcLinElast/LinElastPhysics.cpp:544-554, srcLinElast/PlasticPhysicsF.ChF:30-69). */
+tmk_status tmk_plastic_update(tmk_context* ctx, const tmk_fab* U,
+                              const tmk_box* box, double dt, void* stream);
+
+/* LinElastPhysics::getMaxWaveSpeed -> MAXWAVESPEEDF (LinElastPhysicsF.ChF:10-21). */
+tmk_status tmk_max_wave_speed(const tmk_context* ctx, double* speed);
+
+/* ---------------------------------------------------------------------------
+ * Device-resident level (LinElastLevelGodunov::define/step/plasticUpdate,
+ * srcLinElast/LinElastLevelGodunov.cpp:45-398, 643-667).  The level owns the
+ * device mirrors of every patch's U (two buffers, swapped each step) and B.
+ * Precision follows scheme->precision: FP64 mirrors, or FP32 volume mirrors
+ * with FP64 fault data (mixed form).
+ * ------------------------------------------------------------------------- */
+tmk_status tmk_level_create(tmk_context* ctx, const tmk_box* domain, double dx,
+                            int npatch, const tmk_box* patches, tmk_level** out);
+void       tmk_level_destroy(tmk_level* lvl);
+/* Copy one patch's state in / out.  `host` selects host (1) or device (0)
+ * pointers.  U covers the valid box grown by TMK_NGHOST, 22 components (FP64);
+ * B covers the patch's fault row grown by TMK_NGHOST in x (NULL if none). */
+tmk_status tmk_level_set_patch(tmk_level* lvl, int patch, const double* U,
+                               const double* B, int host);
+tmk_status tmk_level_get_patch(tmk_level* lvl, int patch, double* U, double* B,
+                               int host);
+/* One level step at `time` by `dt`: same-level ghost exchange of U and B,
+ * fault solve, volume update of every patch in one launch, and (if the
+ * scheme has plasticity) the plastic correction.  *dt_new = dx / max wave
+ * speed (LinElastLevelGodunov.cpp:377-391).  Graph-capturable: no host sync. */
+tmk_status tmk_level_step(tmk_level* lvl, double time, double dt, void* stream,
+                          double* dt_new);
+/* Read and clear the device status word: returns the first recorded error and
+ * fills info[0]=code, info[1]=flat index of the first bad value,
+ * info[2]=Newton iterations that hit the limit (not an error in the reference). */
+tmk_status tmk_level_status(tmk_level* lvl, long long info[3]);
+/* Number of kernel launches one tmk_level_step issues. */
+int        tmk_level_launches_per_step(const tmk_level* lvl);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TETEMOKO_GB300_H */

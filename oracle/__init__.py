@@ -1,0 +1,191 @@
+"""CPU FP64 oracle of tetemoko's per-level Godunov step -- TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this
+package, and only as the checker: the CUDA product never imports or calls it.
+The C++ source (tmk_oracle.cpp) restates the reference's Fortran kernels and
+patch/level call order; its header lists the files it follows.
+
+Parity status: the reference kernels themselves (srcLinElast/*.ChF,
+ibcLinElast/*.ChF) cannot be compiled here (no Fortran compiler, no Chombo),
+and the reference ships no tests or golden vectors, so this restatement is
+pinned only by known-answer properties of the reference formulas
+(tests/test_oracle_kat.py) -- parity unpinned.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from tetemoko_gb300 import _capi as A
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "tmk_oracle.cpp")
+LIB = os.path.join(HERE, "libtmk_oracle.so")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (-O2, no FMA contraction, OpenMP)."""
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC",
+               "-o", LIB + ".tmp", SRC]
+        subprocess.run(cmd, check=True)
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        P = C.POINTER
+        dp, ip = P(C.c_double), P(C.c_int)
+        E, S, R, W, PL = (P(A.ElasticParams), P(A.Scheme), P(A.RSParams), P(A.SWParams),
+                          P(A.PlasticParams))
+        L.tmko_constants.argtypes = [E, dp]
+        L.tmko_charanalysis.argtypes = [E, dp, C.c_int]
+        L.tmko_charsynthesis.argtypes = [E, dp, C.c_int]
+        L.tmko_riemann.argtypes = [E, dp, dp, dp, C.c_int]
+        L.tmko_edgebc.argtypes = [E, dp, dp, C.c_int, C.c_int, C.c_int]
+        L.tmko_rsnewton.argtypes = [E, R, C.c_double, C.c_double, C.c_double, C.c_double, dp, dp]
+        L.tmko_rsfault.argtypes = [E, R, dp, dp, C.c_double, C.c_double]
+        L.tmko_swfault.argtypes = [E, W, dp, dp, dp, C.c_double]
+        L.tmko_plasticflow.argtypes = [E, PL, dp, C.c_double]
+        L.tmko_patch_update_state.argtypes = [E, S, R, W, dp, ip, ip, dp, C.c_int, C.c_int, dp, dp,
+                                              ip, ip, ip, ip, C.c_double, C.c_double, C.c_double]
+        L.tmko_plastic_correction.argtypes = [E, PL, dp, ip, ip, ip, ip, C.c_double]
+        L.tmko_level_step.argtypes = [E, S, R, W, PL, ip, ip, C.c_int, ip, dp, dp, C.c_double,
+                                      C.c_double, C.c_double, C.c_int]
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iv(*v):
+    return (C.c_int * len(v))(*v)
+
+
+def _ref(x):
+    return C.byref(x) if x is not None else None
+
+
+# ------------------------------------------------------------- pointwise --
+def constants(sc) -> dict:
+    out = np.zeros(5)
+    lib().tmko_constants(C.byref(sc.elastic), _dp(out))
+    return dict(rho=out[0], lam=out[1], K=out[2], Zs=out[3], Zp=out[4])
+
+
+def charanalysis(sc, w: np.ndarray, idir: int) -> np.ndarray:
+    w = np.ascontiguousarray(w, dtype=np.float64).copy()
+    lib().tmko_charanalysis(C.byref(sc.elastic), _dp(w), idir)
+    return w
+
+
+def charsynthesis(sc, w: np.ndarray, idir: int) -> np.ndarray:
+    w = np.ascontiguousarray(w, dtype=np.float64).copy()
+    lib().tmko_charsynthesis(C.byref(sc.elastic), _dp(w), idir)
+    return w
+
+
+def riemann(sc, wl, wr, idir: int) -> np.ndarray:
+    g = np.zeros(22)
+    wl = np.ascontiguousarray(wl, dtype=np.float64)
+    wr = np.ascontiguousarray(wr, dtype=np.float64)
+    lib().tmko_riemann(C.byref(sc.elastic), _dp(g), _dp(wl), _dp(wr), idir)
+    return g
+
+
+def edge_bc(sc, wi, lohisign: int, idir: int, outflow: bool) -> np.ndarray:
+    g = np.zeros(22)
+    wi = np.ascontiguousarray(wi, dtype=np.float64)
+    lib().tmko_edgebc(C.byref(sc.elastic), _dp(g), _dp(wi), lohisign, idir, int(outflow))
+    return g
+
+
+def rs_newton(sc, phi, psi, sn, a, V0guess):
+    V = C.c_double(V0guess)
+    tau = C.c_double(0.0)
+    it = lib().tmko_rsnewton(C.byref(sc.elastic), C.byref(sc.rs), phi, psi, sn, a, C.byref(V),
+                             C.byref(tau))
+    return V.value, tau.value, it
+
+
+def rs_fault(sc, wi, psi, x) -> np.ndarray:
+    g = np.zeros(22)
+    lib().tmko_rsfault(C.byref(sc.elastic), C.byref(sc.rs), _dp(g),
+                       _dp(np.ascontiguousarray(wi, dtype=np.float64)), psi, x)
+    return g
+
+
+def sw_fault(sc, wi, b, xcell, g0=None) -> np.ndarray:
+    g = np.zeros(22) if g0 is None else np.array(g0, dtype=np.float64)
+    lib().tmko_swfault(C.byref(sc.elastic), C.byref(sc.sw), _dp(g),
+                       _dp(np.ascontiguousarray(wi, dtype=np.float64)),
+                       _dp(np.ascontiguousarray(b, dtype=np.float64)), xcell)
+    return g
+
+
+def plastic_flow(sc, s6l2, dt) -> np.ndarray:
+    v = np.array(s6l2, dtype=np.float64)
+    lib().tmko_plasticflow(C.byref(sc.elastic), C.byref(sc.plastic), _dp(v), dt)
+    return v
+
+
+# ------------------------------------------------------------- patch/level --
+def patch_update_state(sc, U: np.ndarray, ulo, valid_lo, valid_hi, B: np.ndarray | None, bxlo: int,
+                       time: float, dt: float, with_flux: bool = False):
+    """LinElastPatchGodunov::updateState on a host FAB; U, B are updated in place.
+    Returns (rc, Fx, Fy)."""
+    assert U.shape[0] == 22
+    uhi = (ulo[0] + U.shape[2] - 1, ulo[1] + U.shape[1] - 1)
+    Fx = Fy = None
+    if with_flux:
+        nxv = valid_hi[0] - valid_lo[0] + 1
+        nyv = valid_hi[1] - valid_lo[1] + 1
+        Fx = np.zeros((22, nyv, nxv + 1))
+        Fy = np.zeros((22, nyv + 1, nxv))
+    bhi = bxlo + (B.shape[1] - 1 if B is not None else 0)
+    rc = lib().tmko_patch_update_state(
+        C.byref(sc.elastic), C.byref(sc.scheme), _ref(sc.rs), _ref(sc.sw), _dp(U), _iv(*ulo),
+        _iv(*uhi), _dp(B), bxlo, bhi, _dp(Fx), _dp(Fy), _iv(*valid_lo), _iv(*valid_hi), _iv(0, 0),
+        _iv(sc.nx - 1, sc.ny - 1), sc.dx, time, dt)
+    return rc, Fx, Fy
+
+
+def plastic_correction(sc, U: np.ndarray, ulo, blo, bhi, dt: float) -> None:
+    uhi = (ulo[0] + U.shape[2] - 1, ulo[1] + U.shape[1] - 1)
+    lib().tmko_plastic_correction(C.byref(sc.elastic), C.byref(sc.plastic), _dp(U), _iv(*ulo),
+                                  _iv(*uhi), _iv(*blo), _iv(*bhi), dt)
+
+
+def level_step(sc, Ug: np.ndarray, Bg: np.ndarray | None, boxes, time: float, dt: float,
+               nthreads: int = 1) -> int:
+    """LinElastLevelGodunov::step (+ plasticUpdate) for a single level whose
+    patches `boxes` [(lo0, lo1, hi0, hi1), ...] tile the domain.  Ug is
+    (22, ny+8, nx+8), Bg (nbdry, nx+8); both updated in place."""
+    flat = np.ascontiguousarray(np.array(boxes, dtype=np.int32).reshape(-1))
+    return lib().tmko_level_step(
+        C.byref(sc.elastic), C.byref(sc.scheme), _ref(sc.rs), _ref(sc.sw), _ref(sc.plastic),
+        _iv(0, 0), _iv(sc.nx - 1, sc.ny - 1), len(boxes), flat.ctypes.data_as(C.POINTER(C.c_int)),
+        _dp(Ug), _dp(Bg), sc.dx, time, dt, nthreads)
+
+
+def tile_boxes(nx: int, ny: int, max_grid: int):
+    """Cover [0,nx)x[0,ny) with boxes of at most max_grid cells per side."""
+    out = []
+    for j0 in range(0, ny, max_grid):
+        for i0 in range(0, nx, max_grid):
+            out.append((i0, j0, min(i0 + max_grid, nx) - 1, min(j0 + max_grid, ny) - 1))
+    return out

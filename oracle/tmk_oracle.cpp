@@ -1,0 +1,1179 @@
+// tmk_oracle.cpp -- CPU FP64 oracle of tetemoko's per-level Godunov step.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA path: the
+// tests, smoke() and bench.py's CPU baseline call it; the product never does.
+//
+// It restates, in the reference's own structure (array passes over Chombo-style
+// boxes, same operation order, FP64, built with -ffp-contract=off):
+//   srcLinElast/LinElastPhysicsF.ChF   (characteristics, Riemann, flux, BCs)
+//   ibcLinElast/RSIBCF.ChF            (rate-and-state fault solve + state update)
+//   ibcLinElast/SWIBCF.ChF            (slip-weakening fault solve + update)
+//   srcLinElast/PlasticPhysicsF.ChF   (Drucker-Prager correction)
+//   srcLinElast/LinElastPatchGodunov.cpp, LinElastPhysics.cpp, RSIBC.cpp,
+//   SWIBC.cpp, LinElastLevelGodunov.cpp (box algebra and call order).
+// The Chombo GodunovUtilities stages the reference calls (PPM face values,
+// PPM limiter, PPM normal predictor, van Leer slopes, FLUXDIFFF) are not in
+// the reference tree; they are restated from the published PPM method
+// (Colella & Woodward 1984, J. Comput. Phys. 54:174) and the Chombo design
+// description of the unsplit Godunov integrator.  Parity against Chombo itself
+// is therefore UNPINNED: no reference test or golden vector fixes those stages.
+//
+// Where the reference reads memory it never initialised (face states the
+// slip-weakening law leaves unwritten, slip-weakening boundary components 7
+// and 8 at start-up) this oracle uses zero, and 1e10 for rupture time.
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#include "../include/tetemoko_gb300.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ------------------------------------------------------------------ boxes --
+struct Box {
+  int lo[2], hi[2];
+  bool empty() const { return lo[0] > hi[0] || lo[1] > hi[1]; }
+  bool contains(int i, int j) const {
+    return i >= lo[0] && i <= hi[0] && j >= lo[1] && j <= hi[1];
+  }
+};
+Box mk(int l0, int l1, int h0, int h1) { Box b; b.lo[0]=l0; b.lo[1]=l1; b.hi[0]=h0; b.hi[1]=h1; return b; }
+Box grow(Box b, int n) { b.lo[0]-=n; b.lo[1]-=n; b.hi[0]+=n; b.hi[1]+=n; return b; }
+Box growd(Box b, int d, int n) { b.lo[d]-=n; b.hi[d]+=n; return b; }
+Box isect(Box a, const Box& b) {
+  for (int d = 0; d < 2; ++d) { a.lo[d] = std::max(a.lo[d], b.lo[d]); a.hi[d] = std::min(a.hi[d], b.hi[d]); }
+  return a;
+}
+// cell box -> box of the faces normal to d (face i is the lo face of cell i)
+Box surroundingNodes(Box b, int d) { b.hi[d] += 1; return b; }
+
+// ------------------------------------------------------------------- FABs --
+struct FAB {
+  Box b; int nc = 0; std::vector<double> v;
+  FAB() {}
+  FAB(Box bx, int n) { define(bx, n); }
+  void define(Box bx, int n) {
+    b = bx; nc = n;
+    size_t sz = (size_t)(b.hi[0]-b.lo[0]+1) * (size_t)(b.hi[1]-b.lo[1]+1) * (size_t)n;
+    v.assign(sz, 0.0);
+  }
+  size_t idx(int i, int j, int c) const {
+    return ((size_t)c * (size_t)(b.hi[1]-b.lo[1]+1) + (size_t)(j-b.lo[1])) * (size_t)(b.hi[0]-b.lo[0]+1)
+           + (size_t)(i-b.lo[0]);
+  }
+  double& operator()(int i, int j, int c) { return v[idx(i,j,c)]; }
+  double operator()(int i, int j, int c) const { return v[idx(i,j,c)]; }
+};
+
+// ----------------------------------------------------------- parameters ---
+struct Phys {
+  // COMMON /IBC/ (srcLinElast/IBCCommon.fh:4-6)
+  double cs, cp, G, rho, lam, K, Zp, Zs;
+  double background[22];
+  // COMMON /PLASTIC/
+  double p_mu, p_beta, p_eta, p_b, p_h;
+  tmk_scheme sch;
+  tmk_rs_params rs;
+  tmk_sw_params sw;
+};
+
+// LINELASTSETF (srcLinElast/LinElastPhysicsF.ChF:1149-1210)
+void linelastset(Phys& P, const tmk_elastic_params& e) {
+  P.cs = e.cs; P.cp = e.cp; P.G = e.G;
+  if (e.rho > 0) P.G = e.rho * e.cs * e.cs;   // execLinElast/amrGodunov.cpp:210-215
+  P.rho = P.G / (P.cs*P.cs);
+  P.lam = (P.cp*P.cp) * P.rho - 2.0 * P.G;
+  P.Zs = P.rho * P.cs;
+  P.Zp = P.rho * P.cp;
+  P.K = P.lam + 2.0*P.G/3.0;
+  double bg[11] = {0,0,0, e.sxx0, e.syy0, e.szz0, e.sxy0, e.sxz0, e.syz0, 0, 0};
+  for (int s = 0; s < 2; ++s) for (int c = 0; c < 11; ++c) P.background[11*s+c] = bg[c];
+}
+
+// index permutation shared by every directional routine of LinElastPhysicsF.ChF
+struct Perm { int cx, cy, cz, cxy, cxz, cyz; double rv; };
+Perm perm(int idir) {
+  Perm p; p.cx = idir; p.cy = (idir+1)%3; p.cz = (idir+2)%3;
+  if (idir == 0) { p.cxy = 6; p.cxz = 7; p.cyz = 8; p.rv = 1.0; }
+  else if (idir == 1) { p.cxy = 8; p.cxz = 6; p.cyz = 7; p.rv = -1.0; }
+  else { p.cxy = 7; p.cxz = 8; p.cyz = 6; p.rv = 1.0; }
+  return p;
+}
+
+// ------------------------------------------- pointwise physics (ChF) ------
+// CHARANALYSISF (LinElastPhysicsF.ChF:359-452), in place on 22 values
+void charanalysis(const Phys& P, double* dW, int idir) {
+  Perm q = perm(idir);
+  const int O = 11;
+  double vx1 = dW[q.cx], vy1 = dW[q.cy], vz1 = dW[q.cz];
+  double sxx1 = dW[q.cx+3], syy1 = dW[q.cy+3], szz1 = dW[q.cz+3];
+  double sxy1 = dW[q.cxy], sxz1 = dW[q.cxz], syz1 = dW[q.cyz];
+  double lam1 = dW[9], gam1 = dW[10];
+  double vx2 = q.rv*dW[O+q.cx], vy2 = q.rv*dW[O+q.cy], vz2 = q.rv*dW[O+q.cz];
+  double sxx2 = dW[O+q.cx+3], syy2 = dW[O+q.cy+3], szz2 = dW[O+q.cz+3];
+  double sxy2 = dW[O+q.cxy], sxz2 = dW[O+q.cxz], syz2 = dW[O+q.cyz];
+  double lam2 = dW[O+9], gam2 = dW[O+10];
+  const double lam = P.lam, G = P.G, Zp = P.Zp, Zs = P.Zs;
+  dW[2*0] = sxx1 + vx1 * Zp;
+  dW[2*1] = sxy1 + vy1 * Zs;
+  dW[2*2] = sxz1 + vz1 * Zs;
+  dW[2*3] = syy1 - sxx1 * lam / (2.0 * G + lam);
+  dW[2*4] = szz1 - sxx1 * lam / (2.0 * G + lam);
+  dW[2*5] = syz1;
+  dW[2*6] = lam1;
+  dW[2*7] = gam1;
+  dW[2*8] = sxz1 - vz1 * Zs;
+  dW[2*9] = sxy1 - vy1 * Zs;
+  dW[2*10] = sxx1 - vx1 * Zp;
+  dW[1+2*0] = sxx2 + vx2 * Zp;
+  dW[1+2*1] = sxy2 + vy2 * Zs;
+  dW[1+2*2] = sxz2 + vz2 * Zs;
+  dW[1+2*3] = syy2 - sxx2 * lam / (2.0 * G + lam);
+  dW[1+2*4] = szz2 - sxx2 * lam / (2.0 * G + lam);
+  dW[1+2*5] = syz2;
+  dW[1+2*6] = lam2;
+  dW[1+2*7] = gam2;
+  dW[1+2*8] = sxz2 - vz2 * Zs;
+  dW[1+2*9] = sxy2 - vy2 * Zs;
+  dW[1+2*10] = sxx2 - vx2 * Zp;
+}
+
+// CHARSYNTHESISF (LinElastPhysicsF.ChF:458-555)
+void charsynthesis(const Phys& P, double* dW, int idir) {
+  Perm q = perm(idir);
+  const int O = 11;
+  const double lam = P.lam, G = P.G, Zp = P.Zp, Zs = P.Zs;
+  double wxxm1 = dW[0], wxym1 = dW[2], wxzm1 = dW[4], wyy1 = dW[6], wzz1 = dW[8], wyz1 = dW[10];
+  double lam1 = dW[12], gam1 = dW[14], wxzp1 = dW[16], wxyp1 = dW[18], wxxp1 = dW[20];
+  double sxx1 = (wxxm1 + wxxp1) / 2.0;
+  double wxxm2 = dW[1], wxym2 = dW[3], wxzm2 = dW[5], wyy2 = dW[7], wzz2 = dW[9], wyz2 = dW[11];
+  double lam2 = dW[13], gam2 = dW[15], wxzp2 = dW[17], wxyp2 = dW[19], wxxp2 = dW[21];
+  double sxx2 = (wxxm2 + wxxp2) / 2.0;
+  dW[q.cx] = (wxxm1 - wxxp1) / 2.0 / Zp;
+  dW[q.cy] = (wxym1 - wxyp1) / 2.0 / Zs;
+  dW[q.cz] = (wxzm1 - wxzp1) / 2.0 / Zs;
+  dW[q.cx+3] = sxx1;
+  dW[q.cy+3] = wyy1 + sxx1 * lam / (2.0 * G + lam);
+  dW[q.cz+3] = wzz1 + sxx1 * lam / (2.0 * G + lam);
+  dW[q.cxy] = (wxym1 + wxyp1) / 2.0;
+  dW[q.cxz] = (wxzm1 + wxzp1) / 2.0;
+  dW[q.cyz] = wyz1;
+  dW[9] = lam1;
+  dW[10] = gam1;
+  dW[O+q.cx] = q.rv * (wxxm2 - wxxp2) / 2.0 / Zp;
+  dW[O+q.cy] = q.rv * (wxym2 - wxyp2) / 2.0 / Zs;
+  dW[O+q.cz] = q.rv * (wxzm2 - wxzp2) / 2.0 / Zs;
+  dW[O+q.cx+3] = sxx2;
+  dW[O+q.cy+3] = wyy2 + sxx2 * lam / (2.0 * G + lam);
+  dW[O+q.cz+3] = wzz2 + sxx2 * lam / (2.0 * G + lam);
+  dW[O+q.cxy] = (wxym2 + wxyp2) / 2.0;
+  dW[O+q.cxz] = (wxzm2 + wxzp2) / 2.0;
+  dW[O+q.cyz] = wyz2;
+  dW[O+9] = lam2;
+  dW[O+10] = gam2;
+}
+
+// CHARVALUESF (LinElastPhysicsF.ChF:561-595)
+void charvalues(const Phys& P, double* l) {
+  for (int k = 0; k < 22; ++k) l[k] = 0.0;
+  l[0] = l[1] = -P.cp;
+  l[2] = l[3] = l[4] = l[5] = -P.cs;
+  l[16] = l[17] = l[18] = l[19] = P.cs;
+  l[20] = l[21] = P.cp;
+}
+
+// RIEMANNF (LinElastPhysicsF.ChF:601-765) at one face
+void riemannpt(const Phys& P, double* Wg, const double* WL, const double* WR, int idir) {
+  Perm q = perm(idir);
+  const double lam = P.lam, G = P.G, Zp = P.Zp, Zs = P.Zs;
+  for (int s = 0; s < 2; ++s) {
+    const int O = 11*s;
+    const double rv = (s == 0) ? 1.0 : q.rv;
+    double Rvx = WR[O+q.cx], Rvy = WR[O+q.cy], Rvz = WR[O+q.cz];
+    double Rsxx = WR[O+q.cx+3], Rsyy = WR[O+q.cy+3], Rszz = WR[O+q.cz+3];
+    double Rsxy = WR[O+q.cxy], Rsxz = WR[O+q.cxz], Rsyz = WR[O+q.cyz];
+    double Rlam = WR[O+9], Rgam = WR[O+10];
+    double Lvx = WL[O+q.cx], Lvy = WL[O+q.cy], Lvz = WL[O+q.cz];
+    double Lsxx = WL[O+q.cx+3], Lsyy = WL[O+q.cy+3], Lszz = WL[O+q.cz+3];
+    double Lsxy = WL[O+q.cxy], Lsxz = WL[O+q.cxz], Lsyz = WL[O+q.cyz];
+    double Llam = WL[O+9], Lgam = WL[O+10];
+    double wxxp, wxyp, wxzp, wxxm, wxym, wxzm;
+    if (s == 0) {
+      wxxp = Lsxx - Zp * Lvx; wxyp = Lsxy - Zs * Lvy; wxzp = Lsxz - Zs * Lvz;
+      wxxm = Rsxx + Zp * Rvx; wxym = Rsxy + Zs * Rvy; wxzm = Rsxz + Zs * Rvz;
+    } else {
+      wxxp = Lsxx - rv*Zp * Lvx; wxyp = Lsxy - rv*Zs * Lvy; wxzp = Lsxz - rv*Zs * Lvz;
+      wxxm = Rsxx + rv*Zp * Rvx; wxym = Rsxy + rv*Zs * Rvy; wxzm = Rsxz + rv*Zs * Rvz;
+    }
+    double wyy = Rsyy - Rsxx * lam / (2.0 * G + lam);
+    double wzz = Rszz - Rsxx * lam / (2.0 * G + lam);
+    double wyz = Rsyz;
+    wyy = (wyy + Lsyy - Lsxx * lam / (2.0 * G + lam)) / 2.0;
+    wzz = (wzz + Lszz - Lsxx * lam / (2.0 * G + lam)) / 2.0;
+    wyz = (wyz + Lsyz) / 2.0;
+    double sxx = (wxxm + wxxp) / 2.0;
+    if (s == 0) {
+      Wg[O+q.cx] = (wxxm - wxxp) / 2.0 / Zp;
+      Wg[O+q.cy] = (wxym - wxyp) / 2.0 / Zs;
+      Wg[O+q.cz] = (wxzm - wxzp) / 2.0 / Zs;
+    } else {
+      Wg[O+q.cx] = rv*(wxxm - wxxp) / 2.0 / Zp;
+      Wg[O+q.cy] = rv*(wxym - wxyp) / 2.0 / Zs;
+      Wg[O+q.cz] = rv*(wxzm - wxzp) / 2.0 / Zs;
+    }
+    Wg[O+q.cx+3] = (wxxm + wxxp) / 2.0;
+    Wg[O+q.cy+3] = wyy + sxx * lam / (2.0 * G + lam);
+    Wg[O+q.cz+3] = wzz + sxx * lam / (2.0 * G + lam);
+    Wg[O+q.cxy] = (wxym + wxyp) / 2.0;
+    Wg[O+q.cxz] = (wxzm + wxzp) / 2.0;
+    Wg[O+q.cyz] = wyz;
+    Wg[O+9] = (Rlam + Llam) / 2.0;
+    Wg[O+10] = (Rgam + Lgam) / 2.0;
+  }
+}
+
+// GETFLUXF (LinElastPhysicsF.ChF:265-353) at one face
+void getfluxpt(const Phys& P, double* F, const double* Wg, int idir) {
+  Perm q = perm(idir);
+  const double lam = P.lam, G = P.G, rho = P.rho;
+  for (int s = 0; s < 2; ++s) {
+    const int O = 11*s;
+    double vx = Wg[O+q.cx], vy = Wg[O+q.cy], vz = Wg[O+q.cz];
+    double sxx = Wg[O+q.cx+3];
+    double sxy = Wg[O+q.cxy], sxz = Wg[O+q.cxz];
+    if (s == 0) {
+      F[O+q.cx] = -sxx / rho;
+      F[O+q.cy] = -sxy / rho;
+      F[O+q.cz] = -sxz / rho;
+      F[O+q.cx+3] = -vx * (lam + 2.0 * G);
+      F[O+q.cy+3] = -vx * lam;
+      F[O+q.cz+3] = -vx * lam;
+      F[O+q.cxy] = -vy * G;
+      F[O+q.cxz] = -vz * G;
+    } else {
+      const double rv = q.rv;
+      F[O+q.cx] = - rv * sxx / rho;
+      F[O+q.cy] = - rv * sxy / rho;
+      F[O+q.cz] = - rv * sxz / rho;
+      F[O+q.cx+3] = - rv * vx * (lam + 2.0 * G);
+      F[O+q.cy+3] = - rv * vx * lam;
+      F[O+q.cz+3] = - rv * vx * lam;
+      F[O+q.cxy] = - rv * vy * G;
+      F[O+q.cxz] = - rv * vz * G;
+    }
+    F[O+q.cyz] = 0.0;
+    F[O+9] = 0.0;
+    F[O+10] = 0.0;
+  }
+}
+
+// GETADWDXF (LinElastPhysicsF.ChF:791-901) at one cell: WHhi/WHlo are the
+// face states at the hi/lo faces of the cell in direction idir
+void getadwdxpt(const Phys& P, double* A, const double* WHhi, const double* WHlo,
+                double scale, int idir) {
+  Perm q = perm(idir);
+  const double lam = P.lam, G = P.G, rho = P.rho;
+  for (int s = 0; s < 2; ++s) {
+    const int O = 11*s;
+    double vx = WHhi[O+q.cx] - WHlo[O+q.cx];
+    double vy = WHhi[O+q.cy] - WHlo[O+q.cy];
+    double vz = WHhi[O+q.cz] - WHlo[O+q.cz];
+    double sxx = WHhi[O+q.cx+3] - WHlo[O+q.cx+3];
+    double sxy = WHhi[O+q.cxy] - WHlo[O+q.cxy];
+    double sxz = WHhi[O+q.cxz] - WHlo[O+q.cxz];
+    if (s == 0) {
+      A[O+q.cx] = -scale * sxx / rho;
+      A[O+q.cy] = -scale * sxy / rho;
+      A[O+q.cz] = -scale * sxz / rho;
+      A[O+q.cx+3] = -scale * vx * (lam + 2.0 * G);
+      A[O+q.cy+3] = -scale * vx * lam;
+      A[O+q.cz+3] = -scale * vx * lam;
+      A[O+q.cxy] = -scale * vy * G;
+      A[O+q.cxz] = -scale * vz * G;
+      A[O+q.cyz] = -scale * 0.0;
+      A[O+9] = -scale * 0.0;
+      A[O+10] = -scale * 0.0;
+    } else {
+      const double rv = q.rv;
+      A[O+q.cx] = -rv * scale * sxx / rho;
+      A[O+q.cy] = -rv * scale * sxy / rho;
+      A[O+q.cz] = -rv * scale * sxz / rho;
+      A[O+q.cx+3] = -rv * scale * vx * (lam + 2.0 * G);
+      A[O+q.cy+3] = -rv * scale * vx * lam;
+      A[O+q.cz+3] = -rv * scale * vx * lam;
+      A[O+q.cxy] = -rv * scale * vy * G;
+      A[O+q.cxz] = -rv * scale * vz * G;
+      A[O+q.cyz] = -rv * scale * 0.0;
+      A[O+9] = -rv * scale * 0.0;
+      A[O+10] = -rv * scale * 0.0;
+    }
+  }
+}
+
+// LINELASTFREEBCF (LinElastPhysicsF.ChF:906-1020) and LINELASTOUTBCF (:1025-1144)
+// at one boundary face.  Note that SHF is formed from the normal VELOCITY
+// WInside(cx) minus sxx, exactly as the reference writes it.
+void edgebcpt(const Phys& P, double* Wg, const double* Wi, int lohisign, int idir, bool outflow) {
+  Perm q = perm(idir);
+  const double lam = P.lam, G = P.G, Zp = P.Zp, Zs = P.Zs;
+  const double* bg = P.background;
+  for (int s = 0; s < 2; ++s) {
+    const int O = 11*s;
+    const double rv = (s == 0) ? 1.0 : q.rv;
+    double wpx, wpy, wpz, wmx, wmy, wmz;
+    if (outflow) {
+      wpx = bg[O+q.cx+3] - rv*Zp * bg[O+q.cx];
+      wpy = bg[O+q.cxy] - rv*Zs * bg[O+q.cy];
+      wpz = bg[O+q.cxz] - rv*Zs * bg[O+q.cz];
+      wmx = bg[O+q.cx+3] + rv*Zp * bg[O+q.cx];
+      wmy = bg[O+q.cxy] + rv*Zs * bg[O+q.cy];
+      wmz = bg[O+q.cxz] + rv*Zs * bg[O+q.cz];
+      if (s == 0) {  // side 1 has no rv factor in the source
+        wpx = bg[q.cx+3] - Zp * bg[q.cx];
+        wpy = bg[q.cxy] - Zs * bg[q.cy];
+        wpz = bg[q.cxz] - Zs * bg[q.cz];
+        wmx = bg[q.cx+3] + Zp * bg[q.cx];
+        wmy = bg[q.cxy] + Zs * bg[q.cy];
+        wmz = bg[q.cxz] + Zs * bg[q.cz];
+      }
+      if (lohisign == -1) {
+        if (s == 0) {
+          wmx = (Wi[q.cx+3] + Zp * Wi[q.cx]);
+          wmy = (Wi[q.cxy] + Zs * Wi[q.cy]);
+          wmz = (Wi[q.cxz] + Zs * Wi[q.cz]);
+        } else {
+          wmx = (Wi[O+q.cx+3] + rv*Zp * Wi[O+q.cx]);
+          wmy = (Wi[O+q.cxy] + rv*Zs * Wi[O+q.cy]);
+          wmz = (Wi[O+q.cxz] + rv*Zs * Wi[O+q.cz]);
+        }
+      } else {
+        if (s == 0) {
+          wpx = (Wi[q.cx+3] - Zp * Wi[q.cx]);
+          wpy = (Wi[q.cxy] - Zs * Wi[q.cy]);
+          wpz = (Wi[q.cxz] - Zs * Wi[q.cz]);
+        } else {
+          wpx = (Wi[O+q.cx+3] - rv*Zp * Wi[O+q.cx]);
+          wpy = (Wi[O+q.cxy] - rv*Zs * Wi[O+q.cy]);
+          wpz = (Wi[O+q.cxz] - rv*Zs * Wi[O+q.cz]);
+        }
+      }
+    } else {
+      if (lohisign == -1) {
+        if (s == 0) {
+          wmx = (Wi[q.cx+3] + Zp * Wi[q.cx]);
+          wmy = (Wi[q.cxy] + Zs * Wi[q.cy]);
+          wmz = (Wi[q.cxz] + Zs * Wi[q.cz]);
+        } else {
+          wmx = (Wi[O+q.cx+3] + rv*Zp * Wi[O+q.cx]);
+          wmy = (Wi[O+q.cxy] + rv*Zs * Wi[O+q.cy]);
+          wmz = (Wi[O+q.cxz] + rv*Zs * Wi[O+q.cz]);
+        }
+        wpx = -wmx; wpy = -wmy; wpz = -wmz;
+      } else {
+        if (s == 0) {
+          wpx = (Wi[q.cx+3] - Zp * Wi[q.cx]);
+          wpy = (Wi[q.cxy] - Zs * Wi[q.cy]);
+          wpz = (Wi[q.cxz] - Zs * Wi[q.cz]);
+        } else {
+          wpx = (Wi[O+q.cx+3] - rv*Zp * Wi[O+q.cx]);
+          wpy = (Wi[O+q.cxy] - rv*Zs * Wi[O+q.cy]);
+          wpz = (Wi[O+q.cxz] - rv*Zs * Wi[O+q.cz]);
+        }
+        wmx = -wpx; wmy = -wpy; wmz = -wpz;
+      }
+    }
+    double sxx = (wmx + wpx) / (2.0);
+    double SHF = -(Wi[O+q.cx] - sxx) * lam / (lam + 2.0 * G);
+    if (s == 0) {
+      Wg[O+q.cx] = (wmx - wpx) / (2.0 * Zp);
+      Wg[O+q.cy] = (wmy - wpy) / (2.0 * Zs);
+      Wg[O+q.cz] = (wmz - wpz) / (2.0 * Zs);
+    } else {
+      Wg[O+q.cx] = rv*(wmx - wpx) / (2.0 * Zp);
+      Wg[O+q.cy] = rv*(wmy - wpy) / (2.0 * Zs);
+      Wg[O+q.cz] = rv*(wmz - wpz) / (2.0 * Zs);
+    }
+    Wg[O+q.cx+3] = sxx;
+    Wg[O+q.cy+3] = Wi[O+q.cy+3] + SHF;
+    Wg[O+q.cz+3] = Wi[O+q.cz+3] + SHF;
+    Wg[O+q.cxy] = (wmy + wpy) / (2.0);
+    Wg[O+q.cxz] = (wmz + wpz) / (2.0);
+    Wg[O+q.cyz] = Wi[O+q.cyz];
+    Wg[O+9] = Wi[O+9];
+    Wg[O+10] = Wi[O+10];
+  }
+}
+
+// GAUSSIANFUNC / SMOOTHFUNC / BOXCARFUNC (LinElastPhysicsF.ChF:1291-1344)
+double gaussianfunc(double w, double r) { double q = r/w; return std::exp(-(0.5*(q*q))); }
+double smoothfunc(double w, double r) {
+  if (r >= w) return 0.0;
+  if (r <= 0) return 1.0;
+  return std::exp(r*r/(r*r - w*w));
+}
+double boxcarfunc(double w, double r) { return (r >= w) ? 0.0 : 1.0; }
+
+// RSNEWTON (ibcLinElast/RSIBCF.ChF:336-401); returns iterations used
+int rsnewton(const Phys& P, double phi, double psi, double sn, double c_rs_a, double& V, double& tau) {
+  const double rtolV = 0.0, atolV = 0.0;
+  const double atolG = 2.220446049250313e-16 * 1e4;   // epsilon(1d0)*1d4
+  const int IMAX = 100;
+  double Vmin = 0.0, Vmax = phi / P.Zs;
+  if (V < Vmin || V > Vmax) V = (Vmin + Vmax) / 2.0;
+  double alpha = sn * c_rs_a;
+  double beta = std::exp(psi / c_rs_a) / (2.0 * P.rs.V0);
+  double eta = 0.5 * P.Zs;
+  double fval = alpha * std::asinh(beta * V) + eta * V - phi;
+  int it;
+  for (it = 1; it <= IMAX; ++it) {
+    if (fval < 0) Vmin = V; else Vmax = V;
+    double dfval = alpha * beta / std::sqrt((beta*beta) * (V*V) + 1) + eta;
+    double dV = -fval / dfval;
+    V = V + dV;
+    if (V < Vmin || V > Vmax) V = (Vmin + Vmax) / 2.0;
+    fval = alpha * std::asinh(beta * V) + eta * V - phi;
+    if (std::fabs(fval) <= atolG) break;
+    if (std::fabs(dV) <= atolV + rtolV*(std::fabs(V)+std::fabs(dV))) break;
+  }
+  tau = alpha * std::asinh(beta * V);
+  return it;
+}
+
+// RSFAULTBCF (ibcLinElast/RSIBCF.ChF:158-323) at one fault face
+void rsfaultpt(const Phys& P, double* Wg, const double* Wi, double psi, double x) {
+  const double Zs = P.Zs, Zp = P.Zp, lam = P.lam, G = P.G;
+  double vx1 = Wi[0], vy1 = Wi[1], vz1 = Wi[2], sxx1 = Wi[3], syy1 = Wi[4], szz1 = Wi[5];
+  double sxy1 = Wi[6], sxz1 = Wi[7], syz1 = Wi[8];
+  double vx2 = Wi[11], vy2 = Wi[12], vz2 = Wi[13], sxx2 = Wi[14], syy2 = Wi[15], szz2 = Wi[16];
+  double sxy2 = Wi[17], sxz2 = Wi[18], syz2 = Wi[19];
+  (void)vy2; (void)syy2;
+  double wpxy1 = -sxy1 - Zs * vx1;
+  double wpyy1 = -syy1 - Zp * vy1;
+  double wpyz1 = -syz1 - Zs * vz1;
+  double wpxy2 = sxy2 - Zs * vx2;
+  double wpyy2 = syy2 - Zp * vy2;
+  double wpyz2 = syz2 - Zs * vz2;
+  wpyz1 = 0.0; wpyz2 = 0.0;
+  double tau_xy_0 = gaussianfunc(P.rs.r0, x);
+  tau_xy_0 = P.rs.nsig * tau_xy_0;
+  double tau_yz_0 = 0.0;
+  double phi_xy = 0.5*(wpxy2-wpxy1) + tau_xy_0;
+  double phi_yz = 0.5*(wpyz2-wpyz1) + tau_yz_0;
+  double phi = std::sqrt(phi_xy*phi_xy + phi_yz*phi_yz);
+  syy1 = -(wpyy1-wpyy2)/2.0;
+  syy2 = -(wpyy1-wpyy2)/2.0;
+  vy1 = -(wpyy1+wpyy2)/2.0/Zp;
+  vy2 = -(wpyy1+wpyy2)/2.0/Zp;
+  double V = std::sqrt((vx1-vx2)*(vx1-vx2) + (vz1-vz2)*(vz1-vz2));
+  double c_ramp = std::min(1.0, std::max(0.0, (x-P.rs.ramp_x)/P.rs.ramp_w));
+  double c_rs_a = P.rs.a + P.rs.ramp_a*c_ramp;
+  double tau;
+  rsnewton(P, phi, psi, -syy1, c_rs_a, V, tau);
+  sxy1 = (phi_xy/phi) * tau - tau_xy_0;
+  syz1 = (phi_yz/phi) * tau - tau_yz_0;
+  double Vx = (phi_xy/phi) * V;
+  double Vz = (phi_yz/phi) * V;
+  vx1 = -(sxy1 + wpxy1)/Zs;
+  vz1 = -(syz1 + wpyz1)/Zs;
+  double SHF = -(vy1 - syy1) * lam / (lam + 2.0 * G);
+  Wg[0] = vx1; Wg[1] = vy1; Wg[2] = vz1;
+  Wg[3] = sxx1 + SHF; Wg[4] = syy1; Wg[5] = szz1 + SHF;
+  Wg[6] = sxy1; Wg[7] = sxz1; Wg[8] = syz1;
+  Wg[10] = 0.0; Wg[9] = 0.0;
+  sxy2 = (phi_xy/phi) * tau - tau_xy_0;
+  syz2 = (phi_yz/phi) * tau - tau_yz_0;
+  vx2 = vx1 - Vx;
+  vz2 = vz1 - Vz;
+  SHF = -(vy2 - syy2) * lam / (lam + 2.0 * G);
+  Wg[11] = vx2; Wg[12] = vy2; Wg[13] = vz2;
+  Wg[14] = sxx2 + SHF; Wg[15] = syy2; Wg[16] = szz2 + SHF;
+  Wg[17] = sxy2; Wg[18] = sxz2; Wg[19] = syz2;
+  Wg[21] = 0.0; Wg[20] = 0.0;
+}
+
+// RSSETBND (ibcLinElast/RSIBCF.ChF:61-151) at one fault face; returns false on NaN psi
+bool rssetbndpt(const Phys& P, double* Bout, const double* Bin, const double* U,
+                double dt, double x, double time) {
+  const tmk_rs_params& r = P.rs;
+  double tau_xy_0 = gaussianfunc(r.r0, x);
+  tau_xy_0 = r.nsig*tau_xy_0;
+  double tau_yz_0 = 0.0;
+  double c_ramp = std::min(1.0, std::max(0.0, (x-r.ramp_x)/r.ramp_w));
+  double c_rs_a = r.a + r.ramp_a*c_ramp;
+  double c_rs_Vw = r.Vw + r.ramp_Vw*c_ramp;
+  double Vx = U[0] - U[11];
+  double Vz = U[2] - U[13];
+  double V = std::sqrt(Vx*Vx + Vz*Vz);
+  double Bin_rt = Bin[9], Bin_psi = Bin[10];
+  double Bin_dx = Bin[6], Bin_dz = Bin[7], Bin_dt = Bin[8];
+  Bout[0] = Vx;
+  Bout[1] = Vz;
+  Bout[2] = V;
+  Bout[3] = U[6] + tau_xy_0;
+  Bout[4] = U[8] + tau_yz_0;
+  Bout[6] = Bin_dx + dt*Vx;
+  Bout[7] = Bin_dz + dt*Vz;
+  Bout[8] = Bin_dt + dt*V;
+  if (Bin_rt > time && V > r.rupture_threshold) Bout[9] = time;
+  else if (Bin_rt > time) Bout[9] = 1e10;
+  Bout[5] = U[4];
+  double psi = Bin_psi;
+  double dPsi;
+  if (r.state_law == TMK_RS_AGING_LAW) {
+    // extension: aging law dpsi/dt = (b V0 / L) (exp((f0 - psi)/b) - V/V0),
+    // i.e. dtheta/dt = 1 - V theta / L for theta = (L/V0) exp((psi - f0)/b),
+    // advanced exactly at constant V over dt:
+    //   theta' = theta exp(-x) + dt (1 - exp(-x))/x,   x = V dt / L
+    double x = V * dt / r.L;
+    double phi1 = (x > 1e-12) ? -std::expm1(-x) / x : 1.0 - 0.5 * x;
+    double q = (psi - r.f0) / r.b - x;
+    dPsi = r.f0 + r.b * std::log(std::exp(q) + (r.V0 * dt / r.L) * phi1);
+  } else {
+    double f = c_rs_a*std::asinh(V*std::exp(psi/c_rs_a)/(2.0*r.V0));
+    double fss = r.f0 - (r.b - c_rs_a)*std::log(V / r.V0);
+    if (r.fexp > 0.0) {
+      double q = V/c_rs_Vw, q2 = q*q, q4 = q2*q2, q8 = q4*q4;
+      fss = r.fw + (fss - r.fw)/std::pow(1.0 + q8, 0.125);
+    }
+    dPsi = psi - dt * (V / r.L)*(f - fss);
+  }
+  Bout[10] = dPsi;
+  return !std::isnan(dPsi);
+}
+
+// SWFAULTBCF (ibcLinElast/SWIBCF.ChF:79-267) at one fault face.  `off` is the
+// side-2 component offset (9 in the reference source, 11 when corrected).
+void swfaultpt(const Phys& P, double* Wg, const double* Wi, const double* B, double xcell) {
+  const tmk_sw_params& w = P.sw;
+  const int off = (w.layout == TMK_SW_LAYOUT_OFFSET11) ? 11 : 9;
+  const double Zs = P.Zs, Zp = P.Zp, lam = P.lam, G = P.G;
+  double x = xcell - w.fric_box_center[0];
+  double vx1 = Wi[0], vy1 = Wi[1], vz1 = Wi[2], sxx1 = Wi[3], syy1 = Wi[4], szz1 = Wi[5];
+  double sxy1 = Wi[6], sxz1 = Wi[7], syz1 = Wi[8];
+  double vx2 = Wi[off+0], vy2 = Wi[off+1], vz2 = Wi[off+2], sxx2 = Wi[off+3], syy2 = Wi[off+4];
+  double szz2 = Wi[off+5], sxy2 = Wi[off+6], sxz2 = Wi[off+7], syz2 = Wi[off+8];
+  double wpxy1 = -sxy1 - Zs * vx1;
+  double wpyy1 = -syy1 - Zp * vy1;
+  double wpyz1 = -syz1 - Zs * vz1;
+  double wpxy2 = sxy2 - Zs * vx2;
+  double wpyy2 = syy2 - Zp * vy2;
+  double wpyz2 = syz2 - Zs * vz2;
+  double tau_0 = 0;
+  for (int ip = 0; ip < w.num_patches; ++ip) {
+    double valx = smoothfunc(w.smooth, std::fabs(x - w.xc[ip]) - w.xw[ip]);
+    tau_0 = tau_0 + w.tau[ip] * valx;
+  }
+  double a1 = 0.5*(wpxy2-wpxy1)+tau_0, a2 = 0.5*(wpyz2-wpyz1);
+  double tau_lock = std::sqrt(a1*a1 + a2*a2);
+  syy1 = -(wpyy1-wpyy2)/2.0;
+  syy2 = -(wpyy1-wpyy2)/2.0;
+  vy1 = -(wpyy1+wpyy2)/2.0/Zp;
+  vy2 = -(wpyy1+wpyy2)/2.0/Zp;
+  double valx = boxcarfunc(w.fric_box_width[0], std::fabs(x));
+  double fric = w.fs*valx + (1-valx)*w.outside_friction;
+  fric = fric-(fric-w.fd)*std::min(1.0, B[7]/w.dw);
+  double tau = std::min(tau_lock, -syy1*fric)-tau_0;
+  double phi_xy = 0.5*(wpxy2-wpxy1);
+  double phi_yz = 0.5*(wpyz2-wpyz1);
+  double phi = std::sqrt(phi_xy*phi_xy + phi_yz*phi_yz);
+  sxy1 = (phi_xy/phi) * tau;
+  syz1 = (phi_yz/phi) * tau;
+  vx1 = -(sxy1 + wpxy1)/Zs;
+  vz1 = -(syz1 + wpyz1)/Zs;
+  double SHF = -(vy1 - syy1) * lam / (lam + 2.0 * G);
+  Wg[0] = vx1; Wg[1] = vy1; Wg[2] = vz1;
+  Wg[3] = sxx1 + SHF; Wg[4] = syy1; Wg[5] = szz1 + SHF;
+  Wg[6] = sxy1; Wg[7] = sxz1; Wg[8] = syz1;
+  sxy2 = (phi_xy/phi) * tau;
+  syz2 = (phi_yz/phi) * tau;
+  vx2 = (sxy2 - wpxy2)/Zs;
+  vz2 = (syz2 - wpyz2)/Zs;
+  SHF = -(vy2 - syy2) * lam / (lam + 2.0 * G);
+  Wg[off+0] = vx2; Wg[off+1] = vy2; Wg[off+2] = vz2;
+  Wg[off+3] = sxx2 + SHF; Wg[off+4] = syy2; Wg[off+5] = szz2 + SHF;
+  Wg[off+6] = sxy2; Wg[off+7] = sxz2; Wg[off+8] = syz2;
+}
+
+// SWSETBND (ibcLinElast/SWIBCF.ChF:32-72) at one fault face (reference
+// layout: side 2 at component 9; corrected layout: 11)
+// When the update is in place (Bout and Bin the same FAB, as in the final
+// update of SWIBC::updateBoundary) the rupture test reads the V just written.
+void swsetbndpt(const Phys& P, double* Bout, const double* Bin, const double* U, double dt, double time,
+                bool inplace) {
+  const int off = (P.sw.layout == TMK_SW_LAYOUT_OFFSET11) ? 11 : 9;
+  double Bin4 = Bin[4], Bin5 = Bin[5], Bin6 = Bin[6], Bin7 = Bin[7], Bin8 = Bin[8];
+  Bout[0] = U[0] - U[off+0];
+  Bout[1] = U[2] - U[off+2];
+  Bout[2] = U[6];
+  Bout[3] = U[8];
+  Bout[4] = std::sqrt((Bout[0]*Bout[0] + Bout[1]*Bout[1]));
+  Bout[5] = Bin5 + dt*Bout[0];
+  Bout[6] = Bin6 + dt*Bout[1];
+  Bout[7] = Bin7 + dt*Bout[4];
+  double Vtest = inplace ? Bout[4] : Bin4;
+  if (Bin8 > time && Vtest > P.sw.rupture_threshold) Bout[8] = time;
+}
+
+// PLASTICFLOW + INVARIANTS + YIELD (srcLinElast/PlasticPhysicsF.ChF:74-181)
+void plasticflow(const Phys& P, double& sxx, double& syy, double& szz, double& sxy,
+                 double& sxz, double& syz, double& p_lam, double& p_gam, double dt) {
+  double sigma = (sxx + syy + szz) / 3.0;
+  double J2 = ((sxx-syy)*(sxx-syy)+(syy-szz)*(syy-szz)+(szz-sxx)*(szz-sxx))/6.0 +
+              sxy*sxy+sxz*sxz+syz*syz;
+  double tau = std::sqrt(J2);
+  double b = P.p_b + p_gam*P.p_h;
+  double Y = tau - std::max(-P.p_mu*sigma+b, 0.0);
+  if (Y <= 0.0) { p_lam = 0.0; return; }
+  p_lam = Y/(dt*(P.p_h+P.G+P.p_mu*P.p_beta*P.K)+P.p_eta);
+  p_gam = p_gam + dt*p_lam;
+  double sig_e = sigma;
+  tau = tau - dt * p_lam * P.G;
+  sigma = sigma - dt * p_lam * P.K * P.p_beta;
+  double factor = tau/(tau+dt*p_lam*P.G);
+  sxx = sigma + factor * (sxx - sig_e);
+  syy = sigma + factor * (syy - sig_e);
+  szz = sigma + factor * (szz - sig_e);
+  sxy = factor * sxy;
+  sxz = factor * sxz;
+  syz = factor * syz;
+}
+
+// PLASTICCORRECTION (srcLinElast/PlasticPhysicsF.ChF:30-69) over a box
+void plasticcorrection(const Phys& P, FAB& W, double dt, const Box& box) {
+  for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+    for (int i = box.lo[0]; i <= box.hi[0]; ++i)
+      for (int s = 0; s < 2; ++s) {
+        const int O = 11*s;
+        plasticflow(P, W(i,j,O+3), W(i,j,O+4), W(i,j,O+5), W(i,j,O+6), W(i,j,O+7),
+                    W(i,j,O+8), W(i,j,O+9), W(i,j,O+10), dt);
+      }
+}
+
+// ------------------------- Chombo GodunovUtilities stages (restated) -------
+// Second-order slopes with the van Leer limiter (Chombo vanLeerSlopes); one-sided
+// differences at cells adjacent to the domain boundary in direction d.
+void vanLeerSlopes(FAB& dW, const FAB& W, int nc, bool limit, int d, const Box& box, const Box& dom) {
+  int e0 = (d == 0), e1 = (d == 1);
+  for (int c = 0; c < nc; ++c)
+    for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+      for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+        int ii = d == 0 ? i : j;
+        bool hasL = ii-1 >= dom.lo[d], hasR = ii+1 <= dom.hi[d];
+        double dwc, dwl, dwr;
+        if (hasL && hasR) {
+          dwl = W(i,j,c) - W(i-e0,j-e1,c);
+          dwr = W(i+e0,j+e1,c) - W(i,j,c);
+          dwc = 0.5*(W(i+e0,j+e1,c) - W(i-e0,j-e1,c));
+        } else if (hasR) {
+          dwr = W(i+e0,j+e1,c) - W(i,j,c); dwl = dwr; dwc = dwr;
+        } else if (hasL) {
+          dwl = W(i,j,c) - W(i-e0,j-e1,c); dwr = dwl; dwc = dwl;
+        } else { dwl = dwr = dwc = 0.0; }
+        double s = dwc;
+        if (limit) {
+          if (dwl*dwr > 0.0) {
+            double m = std::min(std::fabs(dwc), std::min(2.0*std::fabs(dwl), 2.0*std::fabs(dwr)));
+            s = (dwc >= 0.0) ? m : -m;
+          } else s = 0.0;
+        }
+        dW(i,j,c) = s;
+      }
+}
+
+// PPM face values (Colella & Woodward 1984 eq. 1.6 on a uniform grid):
+//   W_{f} = (W_{f-1} + W_f)/2 - (dW_f - dW_{f-1})/6
+// at faces with both cells in the domain; at a domain-boundary face the value
+// is the linear extrapolation of the one-sided slope of the adjacent cell.
+void ppmFaceValues(FAB& WFace, const FAB& W, int nc, bool limit, int d, const Box& faceBox, const Box& dom) {
+  Box cells = faceBox; cells.hi[d] -= 1;      // enclosedCells
+  cells = growd(cells, d, 1);
+  cells = isect(cells, dom);
+  FAB dW(cells, nc);
+  vanLeerSlopes(dW, W, nc, limit, d, cells, dom);
+  int e0 = (d == 0), e1 = (d == 1);
+  for (int c = 0; c < nc; ++c)
+    for (int j = faceBox.lo[1]; j <= faceBox.hi[1]; ++j)
+      for (int i = faceBox.lo[0]; i <= faceBox.hi[0]; ++i) {
+        int ff = d == 0 ? i : j;
+        bool lowIn = ff-1 >= dom.lo[d], highIn = ff <= dom.hi[d];
+        double v;
+        if (lowIn && highIn)
+          v = 0.5*(W(i-e0,j-e1,c) + W(i,j,c)) - (dW(i,j,c) - dW(i-e0,j-e1,c))/6.0;
+        else if (highIn)
+          v = W(i,j,c) - 0.5*dW(i,j,c);
+        else
+          v = W(i-e0,j-e1,c) + 0.5*dW(i-e0,j-e1,c);
+        WFace(i,j,c) = v;
+      }
+}
+
+// PPM limiter on the face deltas (Colella & Woodward 1984 eq. 1.10)
+void ppmLimiter(FAB& dWm, FAB& dWp, int nc, const Box& box) {
+  for (int c = 0; c < nc; ++c)
+    for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+      for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+        double m = dWm(i,j,c), p = dWp(i,j,c);
+        if (m*p < 0.0) {
+          double am = std::min(std::fabs(m), 2.0*std::fabs(p));
+          double ap = std::min(std::fabs(p), 2.0*std::fabs(m));
+          dWm(i,j,c) = (m >= 0.0) ? am : -am;
+          dWp(i,j,c) = (p >= 0.0) ? ap : -ap;
+        } else { dWm(i,j,c) = 0.0; dWp(i,j,c) = 0.0; }
+      }
+}
+
+// PPM characteristic tracing (Colella & Woodward 1984 eq. 1.12): average of
+// the parabola over the domain of dependence |lambda| dt of the face the
+// characteristic moves towards; the other face keeps its limited value.
+void ppmNormalPred(FAB& dWm, FAB& dWp, const double* lambda, double dtbydx, int nc, const Box& box) {
+  for (int c = 0; c < nc; ++c) {
+    double sig = lambda[c] * dtbydx;
+    for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+      for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+        double m = dWm(i,j,c), p = dWp(i,j,c);
+        if (sig > 0.0) {
+          double s = sig;
+          dWp(i,j,c) = p - 0.5*s*((p - m) + 3.0*(1.0 - (2.0/3.0)*s)*(m + p));
+        } else if (sig < 0.0) {
+          double s = -sig;
+          dWm(i,j,c) = m + 0.5*s*(p - m) - 3.0*(m + p)*(0.5*s - s*s/3.0);
+        }
+      }
+  }
+}
+
+// ---------------------------------------------------------- the patch ----
+struct FaultData {
+  FAB* B = nullptr;       // persistent boundary data (m_bdryData)
+  FAB tmp;                // m_tmpBdryData
+  bool tmpSet = false;    // m_tmpBdryDataSet
+};
+
+struct Patch {
+  const Phys& P;
+  Box dom, cur;
+  double dx, time;
+  FaultData* fd;
+  Patch(const Phys& p) : P(p) {}
+
+  // LinElastPatchGodunov::PPMNormalPred (srcLinElast/LinElastPatchGodunov.cpp:603-702)
+  void PPMNormalPred(FAB& WM, FAB& WP, double dt, const FAB& W, int d, const Box& box) {
+    const int nc = 22;
+    Box faceBox = surroundingNodes(box, d);
+    FAB WFace(faceBox, nc);
+    bool limit = P.sch.use_char_limiting || P.sch.use_prim_limiting;
+    ppmFaceValues(WFace, W, nc, limit, d, faceBox, dom);
+    WM.define(box, nc); WP.define(box, nc);
+    int e0 = (d == 0), e1 = (d == 1);
+    for (int c = 0; c < nc; ++c)
+      for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+        for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+          WM(i,j,c) = (0.0 - W(i,j,c)) + WFace(i,j,c);
+          WP(i,j,c) = (0.0 - W(i,j,c)) + WFace(i+e0,j+e1,c);
+        }
+    double lambda[22]; charvalues(P, lambda);
+    std::vector<double> tmp(22);
+    auto analyse = [&](FAB& F) {
+      for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+        for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+          for (int c = 0; c < nc; ++c) tmp[c] = F(i,j,c);
+          charanalysis(P, tmp.data(), d);
+          for (int c = 0; c < nc; ++c) F(i,j,c) = tmp[c];
+        }
+    };
+    auto synth = [&](FAB& F) {
+      for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+        for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+          for (int c = 0; c < nc; ++c) tmp[c] = F(i,j,c);
+          charsynthesis(P, tmp.data(), d);
+          for (int c = 0; c < nc; ++c) F(i,j,c) = tmp[c];
+        }
+    };
+    if (P.sch.use_char_limiting) { analyse(WM); analyse(WP); }
+    if (P.sch.use_char_limiting || P.sch.use_prim_limiting) ppmLimiter(WM, WP, nc, box);
+    if (!P.sch.use_char_limiting) { analyse(WM); analyse(WP); }
+    ppmNormalPred(WM, WP, lambda, dt / dx, nc, box);
+    synth(WM); synth(WP);
+    for (int c = 0; c < nc; ++c)
+      for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+        for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+          WM(i,j,c) += W(i,j,c);
+          WP(i,j,c) += W(i,j,c);
+        }
+  }
+
+  // LEPhysIBC::primBC dispatch (ibcLinElast/RSIBC.cpp:179-273, SWIBC.cpp:161-271)
+  void primBC(FAB& Wg, const FAB& Wshift, const Box& WgBox, int d, int side /*-1 lo, +1 hi*/) {
+    // boundary faces of WgBox on `side` that lie on the domain boundary
+    int f = (side < 0) ? WgBox.lo[d] : WgBox.hi[d];
+    int domFace = (side < 0) ? dom.lo[d] : dom.hi[d] + 1;
+    if (f != domFace) return;
+    int t = 1 - d;
+    int tlo = std::max(WgBox.lo[t], dom.lo[t]), thi = std::min(WgBox.hi[t], dom.hi[t]);
+    double wg[22], wi[22];
+    for (int k = tlo; k <= thi; ++k) {
+      int i = d == 0 ? f : k, j = d == 0 ? k : f;
+      for (int c = 0; c < 22; ++c) { wi[c] = Wshift(i,j,c); wg[c] = Wg(i,j,c); }
+      if (side == -1 && d == 1 && P.sch.fault_law != TMK_FAULT_NONE) {
+        // RSIBC/SWIBC::primBC: the y-lo face is the fault whatever boundary_type says
+        FAB& src = fd->tmpSet ? fd->tmp : *fd->B;
+        double xc = (i + 0.5) * dx;
+        if (P.sch.fault_law == TMK_FAULT_RS) {
+          rsfaultpt(P, wg, wi, src(i, j, 10), xc - P.rs.x0);
+        } else {
+          double b[TMK_SW_NBDRY];
+          for (int c = 0; c < TMK_SW_NBDRY; ++c) b[c] = src(i, j, c);
+          swfaultpt(P, wg, wi, b, xc);
+        }
+      } else {
+        int bt = P.sch.boundary_type[d*2 + (side+1)/2];
+        edgebcpt(P, wg, wi, side, d, bt == TMK_BC_OUTFLOW);
+      }
+      for (int c = 0; c < 22; ++c) Wg(i,j,c) = wg[c];
+    }
+  }
+
+  // LinElastPhysics::riemann (srcLinElast/LinElastPhysics.cpp:301-359)
+  void riemann(FAB& Wg, const FAB& WLeftCells, const FAB& WRightCells, int d, const Box& faceBox) {
+    int e0 = (d == 0), e1 = (d == 1);
+    double wl[22], wr[22], wg[22];
+    for (int j = faceBox.lo[1]; j <= faceBox.hi[1]; ++j)
+      for (int i = faceBox.lo[0]; i <= faceBox.hi[0]; ++i) {
+        for (int c = 0; c < 22; ++c) { wl[c] = WLeftCells(i-e0,j-e1,c); wr[c] = WRightCells(i,j,c); }
+        riemannpt(P, wg, wl, wr, d);
+        for (int c = 0; c < 22; ++c) Wg(i,j,c) = wg[c];
+      }
+    // primBC(Hi) with the left states shifted onto the faces; primBC(Lo) with the right states
+    FAB shiftL(Wg.b, 22), shiftR(Wg.b, 22);
+    const Box& gb = Wg.b;
+    {
+      int f = gb.hi[d];
+      if (f == dom.hi[d]+1)
+        for (int k = gb.lo[1-d]; k <= gb.hi[1-d]; ++k) {
+          int i = d == 0 ? f : k, j = d == 0 ? k : f;
+          if (WLeftCells.b.contains(i-e0, j-e1))
+            for (int c = 0; c < 22; ++c) shiftL(i,j,c) = WLeftCells(i-e0,j-e1,c);
+        }
+      f = gb.lo[d];
+      if (f == dom.lo[d])
+        for (int k = gb.lo[1-d]; k <= gb.hi[1-d]; ++k) {
+          int i = d == 0 ? f : k, j = d == 0 ? k : f;
+          if (WRightCells.b.contains(i, j))
+            for (int c = 0; c < 22; ++c) shiftR(i,j,c) = WRightCells(i,j,c);
+        }
+    }
+    primBC(Wg, shiftL, gb, d, +1);
+    primBC(Wg, shiftR, gb, d, -1);
+  }
+
+  // LEPhysIBC::updateBoundary (ibcLinElast/RSIBC.cpp:295-336, SWIBC.cpp:293-331)
+  bool updateBoundary(const FAB& WH, int d, double dt, double t, bool final_) {
+    if (d != 1 || P.sch.fault_law == TMK_FAULT_NONE) return true;
+    if (WH.b.lo[1] != dom.lo[1]) return true;
+    if (WH.b.lo[0] < dom.lo[0] || WH.b.hi[0] > dom.hi[0]) return true;
+    const int j = dom.lo[1];
+    FAB& Bin = *fd->B;
+    FAB& Bout = final_ ? *fd->B : fd->tmp;
+    const int nb = Bin.nc;
+    bool ok = true;
+    double bin[TMK_RS_NBDRY], bout[TMK_RS_NBDRY], u[22];
+    for (int i = WH.b.lo[0]; i <= WH.b.hi[0]; ++i) {
+      for (int c = 0; c < nb; ++c) { bin[c] = Bin(i,j,c); bout[c] = Bout(i,j,c); }
+      for (int c = 0; c < 22; ++c) u[c] = WH(i,j,c);
+      if (P.sch.fault_law == TMK_FAULT_RS)
+        ok = rssetbndpt(P, bout, bin, u, dt, (i + 0.5)*dx - P.rs.x0, t) && ok;
+      else
+        swsetbndpt(P, bout, bin, u, dt, t, final_);
+      for (int c = 0; c < nb; ++c) Bout(i,j,c) = bout[c];
+    }
+    if (!final_) fd->tmpSet = true;
+    return ok;
+  }
+
+  // LinElastPatchGodunov::updateState + computeWHalf + computeUpdate
+  // (srcLinElast/LinElastPatchGodunov.cpp:101-129, 174-454, 456-469;
+  //  srcLinElast/LinElastPhysics.cpp:135-179)
+  bool updateState(FAB& U, FAB* Fout, double dt) {
+    bool ok = true;
+    if (fd && fd->B) { fd->tmp.define(fd->B->b, fd->B->nc); fd->tmpSet = false; }
+    Box faceBox[2], ccBox[2], fluxBox[2];
+    for (int d = 0; d < 2; ++d) {
+      Box fb = isect(grow(cur, 1), dom);
+      fb = growd(fb, d, -1);
+      faceBox[d] = surroundingNodes(fb, d);
+      Box cc = growd(grow(cur, 1), d, -1);
+      ccBox[d] = isect(cc, dom);
+      fluxBox[d] = surroundingNodes(ccBox[d], d);
+    }
+    Box WBox = isect(U.b, dom);
+    FAB W(WBox, 22);
+    for (int c = 0; c < 22; ++c)
+      for (int j = WBox.lo[1]; j <= WBox.hi[1]; ++j)
+        for (int i = WBox.lo[0]; i <= WBox.hi[0]; ++i) W(i,j,c) = U(i,j,c);
+    Box slopeBox = isect(grow(cur, 1), dom);
+    FAB WM[2], WP[2], WH1[2];
+    for (int d = 0; d < 2; ++d) {
+      if (P.sch.normal_pred_order == 2) {
+        PPMNormalPred(WM[d], WP[d], dt, W, d, slopeBox);
+      } else {   // CTUNormalPred: straight copy
+        WM[d].define(slopeBox, 22); WP[d].define(slopeBox, 22);
+        for (int c = 0; c < 22; ++c)
+          for (int j = slopeBox.lo[1]; j <= slopeBox.hi[1]; ++j)
+            for (int i = slopeBox.lo[0]; i <= slopeBox.hi[0]; ++i)
+              WM[d](i,j,c) = WP[d](i,j,c) = W(i,j,c);
+      }
+      WH1[d].define(fluxBox[d], 22);
+      riemann(WH1[d], WP[d], WM[d], d, faceBox[d]);
+    }
+    for (int d = 0; d < 2; ++d) {
+      Box fb = isect(growd(cur, d, 1), dom);
+      fb = growd(fb, d, -1);
+      faceBox[d] = surroundingNodes(fb, d);
+      fluxBox[d] = surroundingNodes(cur, d);
+    }
+    FAB WHalf[2];
+    for (int d = 0; d < 2; ++d) WHalf[d].define(fluxBox[d], 22);
+    double a[22], hi[22], lo[22];
+    for (int d1 = 0; d1 < 2; ++d1) {
+      int d2 = 1 - d1;
+      int e0 = (d2 == 0), e1 = (d2 == 1);
+      double scale = -(1.0/2.0) * dt / dx;
+      const Box& cb = ccBox[d2];
+      for (int pass = 0; pass < 2; ++pass) {
+        FAB& T = pass == 0 ? WM[d1] : WP[d1];
+        for (int j = cb.lo[1]; j <= cb.hi[1]; ++j)
+          for (int i = cb.lo[0]; i <= cb.hi[0]; ++i) {
+            for (int c = 0; c < 22; ++c) { hi[c] = WH1[d2](i+e0,j+e1,c); lo[c] = WH1[d2](i,j,c); }
+            getadwdxpt(P, a, hi, lo, scale, d2);
+            for (int c = 0; c < 22; ++c) T(i,j,c) += a[c];
+          }
+      }
+      ok = updateBoundary(WH1[d2], d2, (1.0/2.0)*dt, 0.0, false) && ok;
+      riemann(WHalf[d1], WP[d1], WM[d1], d1, faceBox[d1]);
+    }
+    // computeUpdate
+    FAB dU(U.b, 22);
+    double f[22];
+    for (int d = 0; d < 2; ++d) {
+      FAB F(fluxBox[d], 22);
+      const Box& fbx = fluxBox[d];
+      for (int j = fbx.lo[1]; j <= fbx.hi[1]; ++j)
+        for (int i = fbx.lo[0]; i <= fbx.hi[0]; ++i) {
+          for (int c = 0; c < 22; ++c) a[c] = WHalf[d](i,j,c);
+          getfluxpt(P, f, a, d);
+          for (int c = 0; c < 22; ++c) F(i,j,c) = f[c];
+        }
+      int e0 = (d == 0), e1 = (d == 1);
+      for (int c = 0; c < 22; ++c)
+        for (int j = cur.lo[1]; j <= cur.hi[1]; ++j)
+          for (int i = cur.lo[0]; i <= cur.hi[0]; ++i)
+            dU(i,j,c) += F(i+e0,j+e1,c) - F(i,j,c);
+      if (Fout) Fout[d] = F;
+      ok = updateBoundary(WHalf[d], d, dt, time + dt, true) && ok;
+    }
+    double sc = -dt / dx;
+    for (int c = 0; c < 22; ++c)
+      for (int j = cur.lo[1]; j <= cur.hi[1]; ++j)
+        for (int i = cur.lo[0]; i <= cur.hi[0]; ++i)
+          U(i,j,c) += dU(i,j,c) * sc;
+    return ok;
+  }
+};
+
+bool setup(Phys& P, const tmk_elastic_params* e, const tmk_scheme* s, const tmk_rs_params* rs,
+           const tmk_sw_params* sw, const tmk_plastic_params* pl) {
+  if (!e || !s) return false;
+  std::memset(&P, 0, sizeof(P));
+  linelastset(P, *e);
+  P.sch = *s;
+  if (rs) P.rs = *rs;
+  if (sw) P.sw = *sw;
+  if (pl) { P.p_mu = pl->mu; P.p_beta = pl->beta; P.p_eta = pl->eta; P.p_b = pl->b; P.p_h = pl->h; }
+  if (s->normal_pred_order != 0 && s->normal_pred_order != 2) return false;
+  if (s->use_char_limiting && s->use_prim_limiting) return false;
+  return true;
+}
+
+FAB wrap(const double* p, const int lo[2], const int hi[2], int nc) {
+  FAB f(mk(lo[0], lo[1], hi[0], hi[1]), nc);
+  std::memcpy(f.v.data(), p, f.v.size()*sizeof(double));
+  return f;
+}
+void unwrap(const FAB& f, double* p) { std::memcpy(p, f.v.data(), f.v.size()*sizeof(double)); }
+
+}  // namespace
+
+// ================================================================= C API ===
+extern "C" {
+
+// Derived constants: rho, lam, K, Zs, Zp
+int tmko_constants(const tmk_elastic_params* e, double out[5]) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  if (!setup(P, e, &s, nullptr, nullptr, nullptr)) return 1;
+  out[0] = P.rho; out[1] = P.lam; out[2] = P.K; out[3] = P.Zs; out[4] = P.Zp;
+  return 0;
+}
+
+// pointwise kernels for known-answer tests
+int tmko_charanalysis(const tmk_elastic_params* e, double* w, int idir) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  setup(P, e, &s, nullptr, nullptr, nullptr); charanalysis(P, w, idir); return 0;
+}
+int tmko_charsynthesis(const tmk_elastic_params* e, double* w, int idir) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  setup(P, e, &s, nullptr, nullptr, nullptr); charsynthesis(P, w, idir); return 0;
+}
+int tmko_riemann(const tmk_elastic_params* e, double* wg, const double* wl, const double* wr, int idir) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  setup(P, e, &s, nullptr, nullptr, nullptr); riemannpt(P, wg, wl, wr, idir); return 0;
+}
+int tmko_edgebc(const tmk_elastic_params* e, double* wg, const double* wi, int lohisign, int idir, int outflow) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  setup(P, e, &s, nullptr, nullptr, nullptr); edgebcpt(P, wg, wi, lohisign, idir, outflow != 0); return 0;
+}
+int tmko_rsnewton(const tmk_elastic_params* e, const tmk_rs_params* rs, double phi, double psi,
+                  double sn, double a, double* V, double* tau) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  setup(P, e, &s, rs, nullptr, nullptr);
+  return rsnewton(P, phi, psi, sn, a, *V, *tau);
+}
+int tmko_rsfault(const tmk_elastic_params* e, const tmk_rs_params* rs, double* wg, const double* wi,
+                 double psi, double x) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  setup(P, e, &s, rs, nullptr, nullptr); rsfaultpt(P, wg, wi, psi, x); return 0;
+}
+int tmko_swfault(const tmk_elastic_params* e, const tmk_sw_params* sw, double* wg, const double* wi,
+                 const double* b, double xcell) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  setup(P, e, &s, nullptr, sw, nullptr); swfaultpt(P, wg, wi, b, xcell); return 0;
+}
+int tmko_plasticflow(const tmk_elastic_params* e, const tmk_plastic_params* pl, double* s6l2, double dt) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  setup(P, e, &s, nullptr, nullptr, pl);
+  plasticflow(P, s6l2[0], s6l2[1], s6l2[2], s6l2[3], s6l2[4], s6l2[5], s6l2[6], s6l2[7], dt);
+  return 0;
+}
+
+// One LinElastPatchGodunov::updateState on a host FAB U (box ulo..uhi, 22 comps,
+// ghosts filled) with fault FAB B (box blo..bhi in x at j = domain lo, or NULL).
+// Fx/Fy (optional) receive the face fluxes over the faces of the valid box.
+// Returns 0, or 2 when RSSETBND produced a NaN state (the reference stops).
+int tmko_patch_update_state(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_rs_params* rs,
+                            const tmk_sw_params* sw, double* U, const int ulo[2], const int uhi[2],
+                            double* B, const int blo, const int bhi, double* Fx, double* Fy,
+                            const int vlo[2], const int vhi[2], const int dlo[2], const int dhi[2],
+                            double dx, double time, double dt) {
+  Phys P;
+  if (!setup(P, e, s, rs, sw, nullptr)) return 1;
+  FAB Uf = wrap(U, ulo, uhi, 22);
+  int nb = s->fault_law == TMK_FAULT_RS ? TMK_RS_NBDRY : TMK_SW_NBDRY;
+  FAB Bf;
+  FaultData fd;
+  if (s->fault_law != TMK_FAULT_NONE && vlo[1] == dlo[1] && !B) return 1;
+  if (B) {
+    int bl[2] = {blo, dlo[1]}, bh[2] = {bhi, dlo[1]};
+    Bf = wrap(B, bl, bh, nb);
+    fd.B = &Bf;
+  }
+  Patch pt(P);
+  pt.dom = mk(dlo[0], dlo[1], dhi[0], dhi[1]);
+  pt.cur = mk(vlo[0], vlo[1], vhi[0], vhi[1]);
+  pt.dx = dx; pt.time = time; pt.fd = B ? &fd : nullptr;
+  FAB F[2];
+  bool ok = pt.updateState(Uf, (Fx || Fy) ? F : nullptr, dt);
+  unwrap(Uf, U);
+  if (B) unwrap(Bf, B);
+  if (Fx) unwrap(F[0], Fx);
+  if (Fy) unwrap(F[1], Fy);
+  return ok ? 0 : 2;
+}
+
+// PLASTICCORRECTION over box on host FAB U
+int tmko_plastic_correction(const tmk_elastic_params* e, const tmk_plastic_params* pl, double* U,
+                            const int ulo[2], const int uhi[2], const int blo[2], const int bhi[2],
+                            double dt) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  setup(P, e, &s, nullptr, nullptr, pl);
+  FAB Uf = wrap(U, ulo, uhi, 22);
+  plasticcorrection(P, Uf, dt, mk(blo[0], blo[1], bhi[0], bhi[1]));
+  unwrap(Uf, U);
+  return 0;
+}
+
+// LinElastLevelGodunov::step for a single level (no coarser/finer level) whose
+// patches `boxes` tile the domain, followed by plasticUpdate when the scheme has
+// plasticity.  Ug is the level state over the domain grown by TMK_NGHOST (22
+// comps); Bg the fault row over x in [dom.lo-4, dom.hi+4] (or NULL).  The
+// same-level exchange is the copy of neighbour values into each patch's ghosts.
+// `nthreads` > 0 runs the patch loop with that many OpenMP threads.
+int tmko_level_step(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_rs_params* rs,
+                    const tmk_sw_params* sw, const tmk_plastic_params* pl,
+                    const int dlo[2], const int dhi[2], int npatch, const int* boxes /*npatch*4: lo0 lo1 hi0 hi1*/,
+                    double* Ug, double* Bg, double dx, double time, double dt, int nthreads) {
+  Phys P;
+  if (!setup(P, e, s, rs, sw, pl)) return 1;
+  Box dom = mk(dlo[0], dlo[1], dhi[0], dhi[1]);
+  Box gbox = grow(dom, TMK_NGHOST);
+  const int nb = s->fault_law == TMK_FAULT_RS ? TMK_RS_NBDRY : TMK_SW_NBDRY;
+  const bool fault = s->fault_law != TMK_FAULT_NONE;
+  if (fault && !Bg) return 1;
+  FAB Uold = wrap(Ug, gbox.lo, gbox.hi, 22);
+  FAB Unew = Uold;
+  Box bbox = mk(dom.lo[0]-TMK_NGHOST, dom.lo[1], dom.hi[0]+TMK_NGHOST, dom.lo[1]);
+  FAB Bold, Bnew;
+  if (fault) { Bold = wrap(Bg, bbox.lo, bbox.hi, nb); Bnew = Bold; }
+  int bad = 0;
+#ifdef _OPENMP
+  int nt = nthreads > 0 ? nthreads : 1;
+#pragma omp parallel for schedule(dynamic) num_threads(nt) reduction(|:bad)
+#endif
+  for (int p = 0; p < npatch; ++p) {
+    Box cur = mk(boxes[4*p], boxes[4*p+1], boxes[4*p+2], boxes[4*p+3]);
+    Box ub = grow(cur, TMK_NGHOST);
+    FAB U(ub, 22);
+    Box cp = isect(ub, gbox);
+    for (int c = 0; c < 22; ++c)
+      for (int j = cp.lo[1]; j <= cp.hi[1]; ++j)
+        for (int i = cp.lo[0]; i <= cp.hi[0]; ++i) U(i,j,c) = Uold(i,j,c);
+    FaultData fdt;
+    FAB B;
+    bool touches = fault && cur.lo[1] == dom.lo[1];
+    if (touches) {
+      Box bb = mk(cur.lo[0]-TMK_NGHOST, dom.lo[1], cur.hi[0]+TMK_NGHOST, dom.lo[1]);
+      B.define(bb, nb);
+      for (int c = 0; c < nb; ++c)
+        for (int i = std::max(bb.lo[0], bbox.lo[0]); i <= std::min(bb.hi[0], bbox.hi[0]); ++i)
+          B(i, dom.lo[1], c) = Bold(i, dom.lo[1], c);
+      fdt.B = &B;
+    }
+    Patch pt(P);
+    pt.dom = dom; pt.cur = cur; pt.dx = dx; pt.time = time; pt.fd = touches ? &fdt : nullptr;
+    if (!pt.updateState(U, nullptr, dt)) bad |= 1;
+    for (int c = 0; c < 22; ++c)
+      for (int j = cur.lo[1]; j <= cur.hi[1]; ++j)
+        for (int i = cur.lo[0]; i <= cur.hi[0]; ++i) Unew(i,j,c) = U(i,j,c);
+    if (touches)
+      for (int c = 0; c < nb; ++c)
+        for (int i = cur.lo[0]; i <= cur.hi[0]; ++i) Bnew(i, dom.lo[1], c) = B(i, dom.lo[1], c);
+  }
+  if (s->plasticity && pl) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+    for (int p = 0; p < npatch; ++p) {
+      Box cur = mk(boxes[4*p], boxes[4*p+1], boxes[4*p+2], boxes[4*p+3]);
+      plasticcorrection(P, Unew, dt, cur);
+    }
+  }
+  unwrap(Unew, Ug);
+  if (fault) unwrap(Bnew, Bg);
+  return bad ? 2 : 0;
+}
+
+}  // extern "C"

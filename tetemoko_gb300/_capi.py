@@ -1,0 +1,137 @@
+"""ctypes mirror of include/tetemoko_gb300.h and the loader of the CUDA library.
+
+The structs here are the C ABI's POD types; importing this module never loads
+the CUDA library.  `lib()` loads `libtetemoko_gb300.so` from this package
+directory and raises if it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+TMK_NCOMP = 22
+TMK_RS_NBDRY = 11
+TMK_SW_NBDRY = 9
+TMK_NGHOST = 4
+TMK_SW_MAX_PATCHES = 8
+
+TMK_OK = 0
+STATUS_NAMES = {
+    0: "TMK_OK", 1: "TMK_ERR_BAD_DESC", 2: "TMK_ERR_NAN_STATE", 3: "TMK_ERR_TIMEOUT",
+    4: "TMK_ERR_CUDA", 5: "TMK_ERR_UNSUPPORTED", 6: "TMK_ERR_ALLOC", 7: "TMK_ERR_NO_DEVICE",
+}
+
+TMK_BC_OUTFLOW, TMK_BC_FREE, TMK_BC_FAULT = 0, 1, 2
+TMK_FAULT_NONE, TMK_FAULT_RS, TMK_FAULT_SW = 0, 1, 2
+TMK_RS_SLIP_LAW, TMK_RS_AGING_LAW = 0, 1
+TMK_SW_LAYOUT_REFERENCE9, TMK_SW_LAYOUT_OFFSET11 = 0, 1
+TMK_PREC_FP64, TMK_PREC_MIXED = 0, 1
+
+
+class ElasticParams(C.Structure):
+    _fields_ = [("cs", C.c_double), ("cp", C.c_double), ("G", C.c_double), ("rho", C.c_double),
+                ("sxx0", C.c_double), ("syy0", C.c_double), ("szz0", C.c_double),
+                ("sxy0", C.c_double), ("sxz0", C.c_double), ("syz0", C.c_double)]
+
+
+class RSParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "r0", "x0", "y0", "nsig", "ntime", "a", "b", "V0", "f0", "L", "fw", "Vw", "fexp",
+        "ramp_x", "ramp_w", "ramp_a", "ramp_Vw", "rupture_threshold", "psi_init")] + [
+        ("state_law", C.c_int)]
+
+
+_P = TMK_SW_MAX_PATCHES
+
+
+class SWParams(C.Structure):
+    _fields_ = [("fs", C.c_double), ("fd", C.c_double), ("dw", C.c_double), ("smooth", C.c_double),
+                ("num_patches", C.c_int),
+                ("xc", C.c_double * _P), ("xw", C.c_double * _P), ("zc", C.c_double * _P),
+                ("zw", C.c_double * _P), ("tau", C.c_double * _P),
+                ("fric_box_center", C.c_double * 2), ("fric_box_width", C.c_double * 2),
+                ("outside_friction", C.c_double), ("rupture_threshold", C.c_double),
+                ("layout", C.c_int)]
+
+
+class PlasticParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("mu", "beta", "eta", "b", "h")]
+
+
+class Scheme(C.Structure):
+    _fields_ = [("normal_pred_order", C.c_int), ("use_prim_limiting", C.c_int),
+                ("use_char_limiting", C.c_int), ("boundary_type", C.c_int * 6),
+                ("fault_law", C.c_int), ("plasticity", C.c_int), ("precision", C.c_int)]
+
+
+class Fab(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("lo", C.c_int * 2), ("hi", C.c_int * 2), ("ncomp", C.c_int)]
+
+
+class Box(C.Structure):
+    _fields_ = [("lo", C.c_int * 2), ("hi", C.c_int * 2)]
+
+
+def box(lo0, lo1, hi0, hi1) -> Box:
+    b = Box()
+    b.lo[0], b.lo[1], b.hi[0], b.hi[1] = lo0, lo1, hi0, hi1
+    return b
+
+
+LIBNAME = "libtetemoko_gb300.so"
+_lib = None
+
+
+def lib_path() -> str:
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), LIBNAME)
+
+
+def lib() -> C.CDLL:
+    """Load the CUDA library (built in-tree by tetemoko_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{LIBNAME} is not built (expected at {path}); run "
+            "`python -c 'import __graft_entry__ as g; g.build()'`. There is no CPU fallback.")
+    L = C.CDLL(path)
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    L.tmk_abi_version.restype = C.c_int
+    L.tmk_context_create.argtypes = [C.POINTER(ElasticParams), C.POINTER(Scheme), C.POINTER(RSParams),
+                                     C.POINTER(SWParams), C.POINTER(PlasticParams), C.POINTER(vp)]
+    L.tmk_context_destroy.argtypes = [vp]
+    L.tmk_context_destroy.restype = None
+    L.tmk_context_constants.argtypes = [vp, dp]
+    L.tmk_patch_update_state.argtypes = [vp, C.POINTER(Fab), C.POINTER(Fab), C.POINTER(Fab), C.POINTER(Fab),
+                                         C.POINTER(Box), C.POINTER(Box), C.c_double, C.c_double, C.c_double,
+                                         dp, vp]
+    L.tmk_plastic_update.argtypes = [vp, C.POINTER(Fab), C.POINTER(Box), C.c_double, vp]
+    L.tmk_max_wave_speed.argtypes = [vp, dp]
+    L.tmk_level_create.argtypes = [vp, C.POINTER(Box), C.c_double, C.c_int, C.POINTER(Box), C.POINTER(vp)]
+    L.tmk_level_destroy.argtypes = [vp]
+    L.tmk_level_destroy.restype = None
+    L.tmk_level_set_patch.argtypes = [vp, C.c_int, vp, vp, C.c_int]
+    L.tmk_level_get_patch.argtypes = [vp, C.c_int, vp, vp, C.c_int]
+    L.tmk_level_step.argtypes = [vp, C.c_double, C.c_double, vp, dp]
+    L.tmk_level_status.argtypes = [vp, C.POINTER(C.c_longlong)]
+    L.tmk_level_launches_per_step.argtypes = [vp]
+    L.tmk_level_launches_per_step.restype = C.c_int
+    for name in ("tmk_context_create", "tmk_context_constants", "tmk_patch_update_state",
+                 "tmk_plastic_update", "tmk_max_wave_speed", "tmk_level_create", "tmk_level_set_patch",
+                 "tmk_level_get_patch", "tmk_level_step", "tmk_level_status"):
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+class TmkError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        super().__init__(f"{where}: {STATUS_NAMES.get(code, code)}")
+        self.code = code
+
+
+def check(code: int, where: str) -> None:
+    if code != TMK_OK:
+        raise TmkError(code, where)

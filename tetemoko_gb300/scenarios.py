@@ -1,0 +1,168 @@
+"""Rupture scenarios in the reference decks' units and their initial data.
+
+Each builder returns a `Scenario` holding the C-ABI parameter structs plus the
+grid (cells, dx).  Initial data follow the reference's initialisers:
+  * U = background stress on both sides, velocities and lambda, gamma zero
+    (LEINITF, srcLinElast/LinElastPhysicsF.ChF:1215-1263);
+  * rate-and-state B: zeros, rupture time 1e10, psi = psi_init
+    (RSIBC::initializeBdry, ibcLinElast/RSIBC.cpp:115-163);
+  * slip-weakening B: V, slip_x = 0 and slip_z = 100 as SWIBC::initializeBdry
+    sets (ibcLinElast/SWIBC.cpp:121-145); the components it leaves uninitialised
+    are set here to 0, with rupture time 1e10.
+Units: km, km/s, g/cm^3, GPa, MPa, m/s, m, s.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from . import _capi as A
+
+
+@dataclasses.dataclass
+class Scenario:
+    name: str
+    nx: int
+    ny: int
+    dx: float
+    cfl: float
+    elastic: A.ElasticParams
+    scheme: A.Scheme
+    rs: A.RSParams | None = None
+    sw: A.SWParams | None = None
+    plastic: A.PlasticParams | None = None
+
+    @property
+    def nbdry(self) -> int:
+        if self.scheme.fault_law == A.TMK_FAULT_RS:
+            return A.TMK_RS_NBDRY
+        if self.scheme.fault_law == A.TMK_FAULT_SW:
+            return A.TMK_SW_NBDRY
+        return 0
+
+    def constants(self) -> dict:
+        e = self.elastic
+        G = e.rho * e.cs * e.cs if e.rho > 0 else e.G
+        rho = G / (e.cs * e.cs)
+        lam = e.cp * e.cp * rho - 2.0 * G
+        return dict(G=G, rho=rho, lam=lam, Zs=rho * e.cs, Zp=rho * e.cp, K=lam + 2.0 * G / 3.0)
+
+    def dt(self) -> float:
+        """cfl * dx / max(cs, cp) (MAXWAVESPEEDF, AMRLevelLinElast::advance)."""
+        return self.cfl * self.dx / max(self.elastic.cs, self.elastic.cp)
+
+    def background(self) -> np.ndarray:
+        e = self.elastic
+        side = [0.0, 0.0, 0.0, e.sxx0, e.syy0, e.szz0, e.sxy0, e.sxz0, e.syz0, 0.0, 0.0]
+        return np.array(side + side, dtype=np.float64)
+
+    def initial_U(self, lo=(0, 0), hi=None, ghost=A.TMK_NGHOST) -> np.ndarray:
+        """State FAB (22, ny+2g, nx+2g) over [lo, hi] grown by `ghost`, set to background."""
+        if hi is None:
+            hi = (self.nx - 1, self.ny - 1)
+        ny = hi[1] - lo[1] + 1 + 2 * ghost
+        nx = hi[0] - lo[0] + 1 + 2 * ghost
+        U = np.empty((A.TMK_NCOMP, ny, nx), dtype=np.float64)
+        U[:] = self.background()[:, None, None]
+        return U
+
+    def initial_B(self, xlo=0, xhi=None, ghost=A.TMK_NGHOST) -> np.ndarray | None:
+        """Fault FAB (nbdry, nx+2g) over faces [xlo, xhi] grown by `ghost`."""
+        if self.scheme.fault_law == A.TMK_FAULT_NONE:
+            return None
+        if xhi is None:
+            xhi = self.nx - 1
+        n = xhi - xlo + 1 + 2 * ghost
+        if self.scheme.fault_law == A.TMK_FAULT_RS:
+            B = np.zeros((A.TMK_RS_NBDRY, n))
+            B[9] = 1e10
+            B[10] = self.rs.psi_init
+        else:
+            B = np.zeros((A.TMK_SW_NBDRY, n))
+            B[6] = 100.0
+            B[8] = 1e10
+        return B
+
+
+def _scheme(fault_law: int, precision: int = A.TMK_PREC_FP64, plasticity: int = 0,
+            prim: int = 1, char: int = 0, order: int = 2, bc=(0, 0, 2, 0, 0, 0)) -> A.Scheme:
+    s = A.Scheme()
+    s.normal_pred_order = order
+    s.use_prim_limiting = prim
+    s.use_char_limiting = char
+    for k in range(6):
+        s.boundary_type[k] = bc[k]
+    s.fault_law = fault_law
+    s.plasticity = plasticity
+    s.precision = precision
+    return s
+
+
+def _elastic(cs=3.464, cp=6.0, rho=2.670, sxx0=0.0, syy0=-120.0, szz0=0.0, sxy0=70.0, sxz0=0.0,
+             syz0=0.0) -> A.ElasticParams:
+    e = A.ElasticParams()
+    e.cs, e.cp, e.G, e.rho = cs, cp, 0.0, rho
+    e.sxx0, e.syy0, e.szz0, e.sxy0, e.sxz0, e.syz0 = sxx0, syy0, szz0, sxy0, sxz0, syz0
+    return e
+
+
+def psi_steady(tau: float, sn: float, V: float, a: float, V0: float, Zs: float) -> float:
+    """State psi at which slip rate V is steady under shear tau and normal stress sn:
+    tau - Zs/2 V = sn a asinh(V/(2 V0) exp(psi/a))."""
+    return a * math.log((2.0 * V0 / V) * math.sinh((tau - 0.5 * Zs * V) / (a * sn)))
+
+
+def slip_weakening(nx=512, ny=256, dx=0.1, precision=A.TMK_PREC_FP64,
+                   layout=A.TMK_SW_LAYOUT_OFFSET11, cfl=0.9, plasticity=False,
+                   nuc_tau=11.6, nuc_half_width=1.5) -> Scenario:
+    """Slip-weakening planar fault at y=0 (BASELINE configuration 1 at 512x256, dx=0.1 km):
+    mu_s=0.677, mu_d=0.525, Dc=0.4 m, sn=120 MPa, tau=70 MPa, a 3 km nucleation
+    window at 81.6 MPa (11.6 MPa excess), friction box covering the whole fault."""
+    sw = A.SWParams()
+    sw.fs, sw.fd, sw.dw, sw.smooth = 0.677, 0.525, 0.4, 0.0
+    sw.num_patches = 1
+    sw.xc[0], sw.xw[0], sw.zc[0], sw.zw[0], sw.tau[0] = 0.0, nuc_half_width, 0.0, nuc_half_width, nuc_tau
+    sw.fric_box_center[0], sw.fric_box_center[1] = nx * dx / 2.0, 0.0
+    sw.fric_box_width[0], sw.fric_box_width[1] = 1e3, 1e3
+    sw.outside_friction = 1e4
+    sw.rupture_threshold = 0.001
+    sw.layout = layout
+    pl = None
+    if plasticity:
+        pl = plastic_params()
+    return Scenario("slip_weakening", nx, ny, dx, cfl, _elastic(),
+                    _scheme(A.TMK_FAULT_SW, precision, int(plasticity)), sw=sw, plastic=pl)
+
+
+def rate_state(nx=2048, ny=1024, dx=0.1, precision=A.TMK_PREC_FP64,
+               state_law=A.TMK_RS_AGING_LAW, cfl=0.9, plasticity=False, V_init=1e-12) -> Scenario:
+    """Rate-and-state planar fault at y=0 (BASELINE configuration 2 at 2048x1024, dx=0.1 km):
+    a=0.008, b=0.012, L=0.02 m, f0=0.6, V0=1e-6 m/s, initial V=1e-12 m/s, Gaussian
+    shear nucleation of 25 MPa amplitude and 3 km width at the fault centre."""
+    e = _elastic()
+    sc = Scenario("rate_state", nx, ny, dx, cfl, e, _scheme(A.TMK_FAULT_RS, precision, int(plasticity)))
+    c = sc.constants()
+    rs = A.RSParams()
+    rs.r0, rs.x0, rs.y0, rs.nsig, rs.ntime = 3.0, nx * dx / 2.0, 0.0, 25.0, 0.0
+    rs.a, rs.b, rs.V0, rs.f0, rs.L = 0.008, 0.012, 1e-6, 0.6, 0.02
+    rs.fw, rs.Vw, rs.fexp = 0.1, 0.1, -1.0
+    rs.ramp_x, rs.ramp_w, rs.ramp_a, rs.ramp_Vw = 0.0, 1e40, 0.0, 0.0
+    rs.rupture_threshold = 0.001
+    rs.psi_init = psi_steady(e.sxy0, -e.syy0, V_init, rs.a, rs.V0, c["Zs"])
+    rs.state_law = state_law
+    sc.rs = rs
+    if plasticity:
+        sc.plastic = plastic_params()
+    return sc
+
+
+def plastic_params(mu=math.sin(0.75), eta_time=0.03, G=None) -> A.PlasticParams:
+    """Drucker-Prager: plas_mu, plas_beta = plas_mu/2 (execLinElast/amrGodunov.cpp:514),
+    plas_eta = eta_time * G (viscoplastic relaxation time eta/G)."""
+    if G is None:
+        G = 2.670 * 3.464 ** 2
+    p = A.PlasticParams()
+    p.mu, p.beta, p.eta, p.b, p.h = mu, mu / 2.0, eta_time * G, 0.0, 0.0
+    return p
