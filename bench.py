@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""Benchmark of the per-level Godunov step on the rate-and-state fault workload.
+
+Workload: planar rate-and-state fault on a uniform 2048 x 1024 grid, dx = 0.1 km
+(aging law, regularised sinh friction, Gaussian 25 MPa nucleation), one level,
+synthetic initial data as the reference's initialisers set it.  A step is one
+LinElastLevelGodunov::step of the whole level.
+
+Reported (one JSON line, rank 0):
+  value        mixed form (FP32 volume, FP64 fault) cell-updates/s, state resident in HBM
+  fp64_plain   the plain FP64 form on the same workload
+  roofline     volume kernel: algorithmic bytes (18 components read + written, 144 B per
+               cell in FP32) / average launch time from CUDA events on the launch stream
+  e2e          the same step through the C ABI with host (pinned) FP64 buffers copied in
+               and out every step
+  cpu_baseline the CPU oracle (a port of the reference) on the machine's host cores
+With --gpus N > 1 (torchrun) every rank runs an independent replica ("replicas
+only": the level step has no data-path collective on one GPU per box).
+`--impl reference` times the reference's CPU path (the oracle port) instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY = 2048, 1024
+METRIC = "cell-updates/s (rate-and-state level step, mixed FP32 volume / FP64 fault)"
+UNIT = "cell-updates/s"
+BYTES_PER_CELL_MIXED = 144   # 18 evolving components read + written, FP32
+BYTES_PER_CELL_FP64 = 288
+
+
+def workload_config(nx=NX, ny=NY):
+    return {
+        "workload": f"rate-and-state planar fault, uniform {nx}x{ny}, dx=0.1 km, aging law, "
+                    "Gaussian 25 MPa / 3 km nucleation, absorbing edges, PPM + prim limiting, CFL 0.9",
+        "cells": nx * ny,
+        "precision": "FP32 volume stencil, FP64 friction solve and fault accumulators",
+        "l2": "inputs larger than L2 (FP32 state 187 MB per buffer, two buffers)",
+        "parallelism": "replicas (one independent level per GPU)",
+    }
+
+
+def rank_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 10:
+                    rows.append(p)
+        os.unlink(self.path)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        sm, smax = [], None
+        for p in rows:
+            try:
+                util = float(p[4])
+                clk = float(p[1])
+                smax = float(p[2])
+            except ValueError:
+                continue
+            if util >= 50:
+                sm.append(clk)
+            for k, n in enumerate(names):
+                if p[6 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(rows), "samples_under_load": len(sm)}
+
+
+def cpu_sample(sc, max_seconds, nthreads, strip_rows=None):
+    """Time the oracle level step on the host cores; returns (cell-updates/s, sample description)."""
+    import numpy as np  # noqa: F401
+    import oracle as O
+    from tetemoko_gb300 import scenarios as S
+    rows = strip_rows or sc.ny
+    sub = S.rate_state(nx=sc.nx, ny=rows, dx=sc.dx)
+    boxes = O.tile_boxes(sub.nx, sub.ny, 128)
+    U = sub.initial_U()
+    B = sub.initial_B()
+    dt = sub.dt()
+    t = 0.0
+    O.level_step(sub, U, B, boxes, t, dt, nthreads=nthreads)   # warm-up
+    t += dt
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        O.level_step(sub, U, B, boxes, t, dt, nthreads=nthreads)
+        t += dt
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= max_seconds or n >= 1000:
+            break
+    rate = sub.nx * sub.ny * n / el
+    desc = (f"{n} level steps of a {sub.nx}x{sub.ny} strip of the workload (128x128 patches, OpenMP over "
+            f"patches, {nthreads} threads), {el:.1f} s")
+    return rate, desc
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args):
+    rank, world, _ = rank_env()
+    if rank != 0:
+        return 0
+    from tetemoko_gb300 import scenarios as S
+    nthreads = host_threads()
+    sc = S.rate_state(nx=NX, ny=NY)
+    # size the per-step sample so that warm-up + steps stay within about two minutes
+    probe_rate, _ = cpu_sample(sc, 2.0, nthreads, strip_rows=64)
+    budget = 120.0
+    steps = max(1, args.steps) + max(0, args.warmup)
+    rows = int(probe_rate * budget / steps / NX)
+    rows = max(16, min(NY, (rows // 8) * 8))
+    import oracle as O
+    sub = S.rate_state(nx=NX, ny=rows, dx=sc.dx)
+    boxes = O.tile_boxes(sub.nx, sub.ny, 128)
+    U, B = sub.initial_U(), sub.initial_B()
+    dt, t = sub.dt(), 0.0
+    for _ in range(args.warmup):
+        O.level_step(sub, U, B, boxes, t, dt, nthreads=nthreads)
+        t += dt
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.level_step(sub, U, B, boxes, t, dt, nthreads=nthreads)
+        t += dt
+    el = time.perf_counter() - t0
+    value = sub.nx * sub.ny * args.steps / el
+    sample = (f"each step: one level step of a {NX}x{rows} strip (fault row included) of the {NX}x{NY} "
+              f"workload, 128x128 patches, OpenMP over patches")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's Chombo/Fortran build cannot be compiled here (no Fortran compiler, no "
+                "Chombo); its path is timed through the FP64 C++ oracle that restates it",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--nx", type=int, default=NX)
+    ap.add_argument("--ny", type=int, default=NY)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from tetemoko_gb300 import _capi as A, scenarios as S
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+
+    rank, world, local = rank_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    nx, ny = args.nx, args.ny
+    cells = nx * ny
+    stream = torch.cuda.current_stream()
+
+    def make_level(prec):
+        sc = S.rate_state(nx=nx, ny=ny, precision=prec)
+        ctx = Context(sc)
+        lvl = LinElastLevelGodunov(ctx, [(0, 0, nx - 1, ny - 1)])
+        lvl.set_patch(0, sc.initial_U(), sc.initial_B())
+        return sc, ctx, lvl
+
+    def timed(lvl, sc, steps, warmup, profile=False, sampler=None):
+        dt = sc.dt()
+        t = 0.0
+        for _ in range(warmup):
+            lvl.step(t, dt, stream)
+            t += dt
+        if profile:
+            lvl.profile(True, steps)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.start()
+            time.sleep(0.4)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            lvl.step(t, dt, stream)
+            t += dt
+        e1.record(stream)
+        torch.cuda.synchronize()
+        clocks = sampler.stop() if sampler else None
+        barrier()
+        ms = e0.elapsed_time(e1)
+        prof = lvl.profile_read() if profile else None
+        if profile:
+            lvl.profile(False)
+        rc, info = lvl.status()
+        return ms, prof, clocks, (rc, info)
+
+    # ---- mixed form (headline)
+    sc, ctx, lvl = make_level(A.TMK_PREC_MIXED)
+    sampler = ClockSampler() if rank == 0 else None
+    ms, prof, clocks, st = timed(lvl, sc, args.steps, args.warmup, profile=True, sampler=sampler)
+    ms = max_over_ranks(ms)
+    launches = lvl.launches_per_step() * args.steps
+    value = world * cells * args.steps / (ms * 1e-3)
+    (ex_ms, fault_ms, vol_ms, step_ms), nprof = prof
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    achieved = BYTES_PER_CELL_MIXED * cells / (vol_ms * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "volume_kernel_mixed_2048x1024.traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "volume_kernel<float,32,8>",
+                "algorithmic_bytes_per_launch": BYTES_PER_CELL_MIXED * cells, "peak_source": peak_src,
+                "kernel_ms": vol_ms, "fault_kernel_ms": fault_ms, "step_ms_profiled": step_ms}
+
+    # ---- e2e through the C ABI with pinned host buffers
+    ushape, bshape = lvl.patch_shapes(0)
+    Uh = torch.empty(ushape, dtype=torch.float64).pin_memory()
+    Bh = torch.empty(bshape, dtype=torch.float64).pin_memory()
+    lvl.get_patch(0, Uh.numpy(), Bh.numpy())
+    dt = sc.dt()
+    t = 0.0
+    for _ in range(2):
+        lvl.set_patch(0, Uh.numpy(), Bh.numpy())
+        lvl.step(t, dt, stream)
+        lvl.get_patch(0, Uh.numpy(), Bh.numpy())
+        t += dt
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        lvl.set_patch(0, Uh.numpy(), Bh.numpy())
+        lvl.step(t, dt, stream)
+        lvl.get_patch(0, Uh.numpy(), Bh.numpy())
+        t += dt
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * cells * args.e2e_steps / e2e_s
+    h2d = Uh.numel() * 8 + Bh.numel() * 8
+    lvl.close()
+    ctx.close()
+
+    # ---- plain FP64 form on the same workload
+    sc64, ctx64, lvl64 = make_level(A.TMK_PREC_FP64)
+    n64 = max(1, args.fp64_steps)
+    ms64, prof64, _, st64 = timed(lvl64, sc64, n64, 3, profile=True)
+    ms64 = max_over_ranks(ms64)
+    value64 = world * cells * n64 / (ms64 * 1e-3)
+    vol64 = prof64[0][2]
+    lvl64.close()
+    ctx64.close()
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_seconds > 0:
+        nthreads = host_threads()
+        rate, desc = cpu_sample(S.rate_state(nx=nx, ny=ny), args.cpu_seconds, nthreads, strip_rows=min(ny, 256))
+        cpu = {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": workload_config(nx, ny),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                    "note": "per step: FP64 state copied host->device (pinned), level step, state copied back"},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_step": ms64 / n64, "steps": n64,
+                           "volume_kernel_ms": vol64,
+                           "volume_hbm_gbs": BYTES_PER_CELL_FP64 * cells / (vol64 * 1e-3) / 1e9},
+            "mixed_over_fp64": value / value64,
+            "device_status": {"mixed": st[1], "fp64": st64[1]},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -197,6 +197,13 @@ tmk_status tmk_level_step(tmk_level* lvl, double time, double dt, void* stream,
 tmk_status tmk_level_status(tmk_level* lvl, long long info[3]);
 /* Number of kernel launches one tmk_level_step issues. */
 int        tmk_level_launches_per_step(const tmk_level* lvl);
+/* Per-launch timing of tmk_level_step: with enable=1 the next (at most
+ * max_steps) steps record CUDA events on their stream around each launch
+ * (the work is unchanged); enable=0 stops recording. */
+tmk_status tmk_level_profile(tmk_level* lvl, int enable, int max_steps);
+/* Average milliseconds per recorded step of: out[0] ghost exchange,
+ * out[1] fault kernel, out[2] volume kernel, out[3] whole step. */
+tmk_status tmk_level_profile_read(tmk_level* lvl, double out[4], int* nsteps);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,147 @@
+"""FP64 GPU path == CPU oracle, through the C ABI (the parity tests proper).
+
+Tolerance: 1e-12 relative per component (tests/helpers.py RTOL_FP64); the
+FP64 kernels are built without FMA contraction and follow the reference's
+operation order, so the remaining differences are last-ulp differences of
+the transcendental functions in the friction solve.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from tetemoko_gb300 import _capi as A, scenarios as S
+from tests.helpers import RTOL_FP64, perturbed_state, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenarios():
+    out = []
+    sc = S.rate_state(nx=64, ny=32, dx=0.1, state_law=A.TMK_RS_SLIP_LAW)
+    sc.rs.L = 0.5
+    out.append(("rs_slip", sc))
+    out.append(("rs_aging", S.rate_state(nx=64, ny=32, dx=0.1)))
+    out.append(("sw_ref9", S.slip_weakening(nx=64, ny=32, dx=0.1, layout=A.TMK_SW_LAYOUT_REFERENCE9)))
+    out.append(("sw_off11", S.slip_weakening(nx=64, ny=32, dx=0.1, layout=A.TMK_SW_LAYOUT_OFFSET11)))
+    sc = S.slip_weakening(nx=64, ny=32, dx=0.1)
+    sc.scheme.use_prim_limiting, sc.scheme.use_char_limiting = 0, 1
+    out.append(("sw_charlim", sc))
+    sc = S.rate_state(nx=64, ny=32, dx=0.1)
+    for k, v in enumerate((1, 1, 2, 1, 0, 0)):
+        sc.scheme.boundary_type[k] = v
+    out.append(("rs_free_edges", sc))
+    sc = S.rate_state(nx=64, ny=32, dx=0.1)
+    sc.scheme.normal_pred_order = 0
+    out.append(("rs_ctu", sc))
+    sc = S.slip_weakening(nx=64, ny=32, dx=0.1)
+    sc.scheme.use_prim_limiting = 0
+    out.append(("sw_unlimited", sc))
+    return out
+
+
+SCEN = _scenarios()
+
+
+def _random_B(sc, rng, n):
+    B = sc.initial_B(xlo=0, xhi=n - 1 - 2 * A.TMK_NGHOST)
+    if sc.scheme.fault_law == A.TMK_FAULT_RS:
+        B[10] += 0.02 * rng.standard_normal(B.shape[1])
+        B[8] = np.abs(rng.standard_normal(B.shape[1]))
+    else:
+        B[7] = 0.3 * np.abs(rng.standard_normal(B.shape[1]))
+    return B
+
+
+@pytest.mark.parametrize("name,sc", SCEN, ids=[n for n, _ in SCEN])
+@pytest.mark.parametrize("valid", [(0, 0, 63, 31), (5, 0, 40, 13), (17, 9, 63, 31), (0, 3, 30, 31)],
+                         ids=["whole", "fault_edge", "corner_hi", "edge_lo"])
+def test_patch_update_state_matches_oracle(cuda_lib, name, sc, valid):
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov
+    rng = np.random.default_rng(1234)
+    g = A.TMK_NGHOST
+    ulo = (valid[0] - g, valid[1] - g)
+    U0 = perturbed_state(sc, rng, lo=valid[:2], hi=valid[2:])
+    touches = valid[1] == 0
+    B0 = _random_B(sc, rng, valid[2] - valid[0] + 1 + 2 * g) if touches else None
+    dt = sc.dt()
+    time = 1.25
+    # oracle
+    Ur, Br = U0.copy(), (B0.copy() if B0 is not None else None)
+    rc, Fxr, Fyr = O.patch_update_state(sc, Ur, ulo, valid[:2], valid[2:], Br, valid[0] - g, time, dt,
+                                        with_flux=True)
+    assert rc == 0
+    # GPU
+    ctx = Context(sc)
+    pg = LinElastPatchGodunov(ctx)
+    pg.set_current_box(valid)
+    pg.set_current_time(time)
+    Ud = torch.from_numpy(U0.copy()).cuda()
+    Bd = torch.from_numpy(B0.copy()).cuda() if B0 is not None else None
+    mws, Fx, Fy = pg.update_state(Ud, ulo, dt, B=Bd, bxlo=valid[0] - g, with_flux=True)
+    torch.cuda.synchronize()
+    assert mws == max(sc.elastic.cs, sc.elastic.cp)
+    Ug = Ud.cpu().numpy()
+    vs = (slice(None), slice(g, -g), slice(g, -g))
+    assert rel_err(Ug[vs], Ur[vs]) <= RTOL_FP64
+    # lambda, gamma and ghost cells are untouched
+    assert np.array_equal(Ug[[9, 10, 20, 21]], U0[[9, 10, 20, 21]])
+    assert np.array_equal(Ug[:, :g, :], U0[:, :g, :])
+    ev = [c for c in range(22) if c % 11 < 9]
+    assert rel_err(Fx.cpu().numpy()[ev], Fxr[ev]) <= RTOL_FP64
+    assert rel_err(Fy.cpu().numpy()[ev], Fyr[ev]) <= RTOL_FP64
+    if touches:
+        Bg = Bd.cpu().numpy()
+        bs = slice(g, -g)
+        assert rel_err(Bg[:, bs], Br[:, bs]) <= RTOL_FP64
+    ctx.close()
+
+
+@pytest.mark.parametrize("name,sc", SCEN[:4], ids=[n for n, _ in SCEN[:4]])
+def test_level_steps_match_oracle(cuda_lib, name, sc):
+    """Ten steps of a level of uneven patches (exchange, fault row split across patches)."""
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    rng = np.random.default_rng(99)
+    boxes = [(0, 0, 20, 9), (21, 0, 63, 9), (0, 10, 31, 31), (32, 10, 47, 20), (32, 21, 47, 31), (48, 10, 63, 31)]
+    Ug = perturbed_state(sc, rng, amp_v=0.05, amp_s=1.0)
+    Bg = sc.initial_B()
+    Ur, Br = Ug.copy(), Bg.copy()
+    ctx = Context(sc)
+    lvl = LinElastLevelGodunov(ctx, boxes)
+    lvl.set_level(Ug, Bg)
+    dt = sc.dt()
+    t = 0.0
+    for n in range(10):
+        assert O.level_step(sc, Ur, Br, boxes, t, dt) == 0
+        lvl.step(t, dt)
+        t += dt
+    Uo, Bo = Ug.copy(), Bg.copy()
+    lvl.get_level(Uo, Bo)
+    g = A.TMK_NGHOST
+    vs = (slice(None), slice(g, -g), slice(g, -g))
+    assert rel_err(Uo[vs], Ur[vs]) <= 1e-11
+    assert rel_err(Bo[:, g:-g], Br[:, g:-g]) <= 1e-11
+    rc, info = lvl.status()
+    assert rc == 0 and info[0] == 0
+    lvl.close()
+    ctx.close()
+
+
+def test_plastic_update_matches_oracle(cuda_lib):
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov
+    sc = S.slip_weakening(nx=32, ny=16, dx=0.1, plasticity=True)
+    rng = np.random.default_rng(7)
+    U0 = perturbed_state(sc, rng, amp_s=60.0)
+    U0[[10, 21]] = np.abs(rng.standard_normal((2,) + U0.shape[1:]))
+    g = A.TMK_NGHOST
+    Ur = U0.copy()
+    O.plastic_correction(sc, Ur, (-g, -g), (0, 0), (31, 15), sc.dt())
+    ctx = Context(sc)
+    pg = LinElastPatchGodunov(ctx)
+    Ud = torch.from_numpy(U0.copy()).cuda()
+    pg.plastic_update(Ud, (-g, -g), sc.dt(), box=(0, 0, 31, 15))
+    Ug = Ud.cpu().numpy()
+    assert (Ur[9] > 0).any(), "the test state must yield somewhere"
+    assert rel_err(Ug, Ur) <= RTOL_FP64
+    ctx.close()

@@ -118,9 +118,12 @@ def lib() -> C.CDLL:
     L.tmk_level_status.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.tmk_level_launches_per_step.argtypes = [vp]
     L.tmk_level_launches_per_step.restype = C.c_int
+    L.tmk_level_profile.argtypes = [vp, C.c_int, C.c_int]
+    L.tmk_level_profile_read.argtypes = [vp, dp, ip]
     for name in ("tmk_context_create", "tmk_context_constants", "tmk_patch_update_state",
                  "tmk_plastic_update", "tmk_max_wave_speed", "tmk_level_create", "tmk_level_set_patch",
-                 "tmk_level_get_patch", "tmk_level_step", "tmk_level_status"):
+                 "tmk_level_get_patch", "tmk_level_step", "tmk_level_status", "tmk_level_profile",
+                 "tmk_level_profile_read"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

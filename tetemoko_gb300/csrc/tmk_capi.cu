@@ -1,0 +1,602 @@
+// tmk_capi.cu -- the C ABI of include/tetemoko_gb300.h.
+//
+// Host-side objects:
+//   tmk_context  per-scenario parameters (the reference's COMMON blocks) with a
+//                device copy; scratch for the patch-level entry point.
+//   tmk_level    device mirrors of every patch of one level (two state buffers
+//                swapped each step, fault data, fault-face buffers), the tile
+//                work list of the volume kernel and the exchange lists.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/tetemoko_gb300.h"
+#include "tmk_kernels.cuh"
+#include "tmk_launch.h"
+
+using tmk::DevParams;
+using tmk::DevStatus;
+using tmk::PatchDev;
+using tmk::TileDev;
+using tmk::CopyDev;
+
+#define TMK_CU(call)                                   \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return TMK_ERR_CUDA;        \
+  } while (0)
+
+namespace {
+
+bool box_ok(const tmk_box& b) { return b.lo[0] <= b.hi[0] && b.lo[1] <= b.hi[1]; }
+bool box_contains(const tmk_box& a, const tmk_box& b) {
+  return a.lo[0] <= b.lo[0] && a.lo[1] <= b.lo[1] && a.hi[0] >= b.hi[0] && a.hi[1] >= b.hi[1];
+}
+tmk_box box_grow(tmk_box b, int n) { b.lo[0] -= n; b.lo[1] -= n; b.hi[0] += n; b.hi[1] += n; return b; }
+tmk_box box_isect(tmk_box a, const tmk_box& b) {
+  for (int d = 0; d < 2; ++d) { a.lo[d] = std::max(a.lo[d], b.lo[d]); a.hi[d] = std::min(a.hi[d], b.hi[d]); }
+  return a;
+}
+
+int device_ok() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return 0;
+  return 1;
+}
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) { return cudaMalloc((void**)p, n * sizeof(T) + 16); }
+
+}  // namespace
+
+struct tmk_context_s {
+  DevParams hp;
+  DevParams* dp = nullptr;
+  tmk_scheme scheme;
+  int nb = 0;
+  // patch-level scratch (grown on demand)
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  DevStatus* dstatus = nullptr;
+};
+
+extern "C" int tmk_abi_version(void) { return TMK_ABI_VERSION; }
+
+extern "C" tmk_status tmk_context_create(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_rs_params* rs,
+                                         const tmk_sw_params* sw, const tmk_plastic_params* pl,
+                                         tmk_context** out) {
+  if (!out) return TMK_ERR_BAD_DESC;
+  *out = nullptr;
+  if (!e || !s) return TMK_ERR_BAD_DESC;
+  if (s->normal_pred_order != 0 && s->normal_pred_order != 2) return TMK_ERR_UNSUPPORTED;
+  if (s->use_char_limiting && s->use_prim_limiting) return TMK_ERR_UNSUPPORTED;  // PPMNormalPred MayDay
+  for (int k = 0; k < 4; ++k)
+    if (s->boundary_type[k] < 0 || s->boundary_type[k] > 2) return TMK_ERR_BAD_DESC;  // "Invalid Boundary Type"
+  if (s->fault_law == TMK_FAULT_RS && !rs) return TMK_ERR_BAD_DESC;
+  if (s->fault_law == TMK_FAULT_SW && !sw) return TMK_ERR_BAD_DESC;
+  if (s->plasticity && !pl) return TMK_ERR_BAD_DESC;
+  if (s->fault_law < 0 || s->fault_law > 2) return TMK_ERR_BAD_DESC;
+  if (!(e->cs > 0) || !(e->cp >= e->cs)) return TMK_ERR_BAD_DESC;   // char transforms assume cp >= cs
+  if (sw && s->fault_law == TMK_FAULT_SW && (sw->num_patches < 0 || sw->num_patches > TMK_SW_MAX_PATCHES))
+    return TMK_ERR_BAD_DESC;
+  if (!device_ok()) return TMK_ERR_NO_DEVICE;
+  tmk_context* c = new (std::nothrow) tmk_context_s();
+  if (!c) return TMK_ERR_ALLOC;
+  DevParams& P = c->hp;
+  std::memset(&P, 0, sizeof(P));
+  // LINELASTSETF (srcLinElast/LinElastPhysicsF.ChF:1149-1210); rho > 0 overrides G
+  P.cs = e->cs; P.cp = e->cp; P.G = e->G;
+  if (e->rho > 0) P.G = e->rho * e->cs * e->cs;
+  P.rho = P.G / (P.cs * P.cs);
+  P.lam = (P.cp * P.cp) * P.rho - 2.0 * P.G;
+  P.Zs = P.rho * P.cs;
+  P.Zp = P.rho * P.cp;
+  P.K = P.lam + 2.0 * P.G / 3.0;
+  const double bg[11] = {0, 0, 0, e->sxx0, e->syy0, e->szz0, e->sxy0, e->sxz0, e->syz0, 0, 0};
+  for (int sd = 0; sd < 2; ++sd)
+    for (int k = 0; k < 11; ++k) P.bg[11 * sd + k] = bg[k];
+  P.order = s->normal_pred_order; P.prim_lim = s->use_prim_limiting; P.char_lim = s->use_char_limiting;
+  for (int k = 0; k < 6; ++k) P.bc[k] = s->boundary_type[k];
+  P.fault_law = s->fault_law;
+  P.plasticity = s->plasticity;
+  if (rs) {
+    P.rs_r0 = rs->r0; P.rs_x0 = rs->x0; P.rs_nsig = rs->nsig; P.rs_a = rs->a; P.rs_b = rs->b; P.rs_V0 = rs->V0;
+    P.rs_f0 = rs->f0; P.rs_L = rs->L; P.rs_fw = rs->fw; P.rs_Vw = rs->Vw; P.rs_fexp = rs->fexp;
+    P.ramp_x = rs->ramp_x; P.ramp_w = rs->ramp_w; P.ramp_a = rs->ramp_a; P.ramp_Vw = rs->ramp_Vw;
+    P.rs_thr = rs->rupture_threshold; P.state_law = rs->state_law;
+  }
+  if (sw) {
+    P.sw_fs = sw->fs; P.sw_fd = sw->fd; P.sw_dw = sw->dw; P.sw_smooth = sw->smooth; P.sw_np = sw->num_patches;
+    for (int k = 0; k < TMK_SW_MAX_PATCHES; ++k) { P.sw_xc[k] = sw->xc[k]; P.sw_xw[k] = sw->xw[k]; P.sw_tau[k] = sw->tau[k]; }
+    P.sw_fbc0 = sw->fric_box_center[0]; P.sw_fbw0 = sw->fric_box_width[0];
+    P.sw_outside = sw->outside_friction; P.sw_thr = sw->rupture_threshold;
+    P.sw_off = sw->layout == TMK_SW_LAYOUT_OFFSET11 ? 11 : 9;
+  }
+  if (pl) { P.p_mu = pl->mu; P.p_beta = pl->beta; P.p_eta = pl->eta; P.p_b = pl->b; P.p_h = pl->h; }
+  c->scheme = *s;
+  c->nb = s->fault_law == TMK_FAULT_RS ? TMK_RS_NBDRY : (s->fault_law == TMK_FAULT_SW ? TMK_SW_NBDRY : 0);
+  if (dalloc(&c->dp, 1) != cudaSuccess || dalloc(&c->dstatus, 1) != cudaSuccess) {
+    cudaFree(c->dp); cudaFree(c->dstatus); delete c; return TMK_ERR_ALLOC;
+  }
+  if (cudaMemcpy(c->dp, &P, sizeof(P), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(c->dstatus, 0, sizeof(DevStatus)) != cudaSuccess) {
+    cudaFree(c->dp); cudaFree(c->dstatus); delete c; return TMK_ERR_CUDA;
+  }
+  *out = c;
+  return TMK_OK;
+}
+
+extern "C" void tmk_context_destroy(tmk_context* c) {
+  if (!c) return;
+  cudaFree(c->dp);
+  cudaFree(c->dstatus);
+  cudaFree(c->scratch);
+  delete c;
+}
+
+extern "C" tmk_status tmk_context_constants(const tmk_context* c, double out[5]) {
+  if (!c || !out) return TMK_ERR_BAD_DESC;
+  out[0] = c->hp.rho; out[1] = c->hp.lam; out[2] = c->hp.K; out[3] = c->hp.Zs; out[4] = c->hp.Zp;
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_max_wave_speed(const tmk_context* c, double* speed) {
+  if (!c || !speed) return TMK_ERR_BAD_DESC;
+  *speed = std::max(c->hp.cs, c->hp.cp);   // MAXWAVESPEEDF
+  return TMK_OK;
+}
+
+namespace {
+
+// tiles of TX x TY over a valid box
+void make_tiles(std::vector<TileDev>& out, int patch, const tmk_box& v, int TX, int TY) {
+  for (int y0 = v.lo[1]; y0 <= v.hi[1]; y0 += TY)
+    for (int x0 = v.lo[0]; x0 <= v.hi[0]; x0 += TX) {
+      TileDev t;
+      t.patch = patch; t.x0 = x0; t.y0 = y0;
+      t.nx = std::min(TX, v.hi[0] - x0 + 1);
+      t.ny = std::min(TY, v.hi[1] - y0 + 1);
+      out.push_back(t);
+    }
+}
+
+size_t align_up(size_t n) { return (n + 255) & ~(size_t)255; }
+
+}  // namespace
+
+// ---------------------------------------------------------------- patch API
+extern "C" tmk_status tmk_patch_update_state(tmk_context* c, const tmk_fab* U, const tmk_fab* B, const tmk_fab* Fx,
+                                             const tmk_fab* Fy, const tmk_box* valid, const tmk_box* domain,
+                                             double dx, double time, double dt, double* max_wave_speed,
+                                             void* stream) {
+  if (!c || !U || !valid || !domain || !U->data) return TMK_ERR_BAD_DESC;
+  if (!box_ok(*valid) || !box_ok(*domain) || !box_contains(*domain, *valid)) return TMK_ERR_BAD_DESC;
+  if (U->ncomp != TMK_NCOMP || !(dx > 0) || !(dt > 0)) return TMK_ERR_BAD_DESC;
+  tmk_box ub; ub.lo[0] = U->lo[0]; ub.lo[1] = U->lo[1]; ub.hi[0] = U->hi[0]; ub.hi[1] = U->hi[1];
+  if (!box_contains(ub, box_isect(box_grow(*valid, 3), *domain))) return TMK_ERR_BAD_DESC;
+  const bool fault = c->scheme.fault_law != TMK_FAULT_NONE && valid->lo[1] == domain->lo[1];
+  if (fault) {
+    if (!B || !B->data || B->ncomp != c->nb) return TMK_ERR_BAD_DESC;
+    int need_lo = std::max(valid->lo[0] - 1, domain->lo[0]), need_hi = std::min(valid->hi[0] + 1, domain->hi[0]);
+    if (B->lo[0] > need_lo || B->hi[0] < need_hi) return TMK_ERR_BAD_DESC;
+  }
+  const int nvx = valid->hi[0] - valid->lo[0] + 1, nvy = valid->hi[1] - valid->lo[1] + 1;
+  if (Fx && (!Fx->data || Fx->ncomp != TMK_NCOMP || Fx->lo[0] != valid->lo[0] || Fx->hi[0] != valid->hi[0] + 1 ||
+             Fx->lo[1] != valid->lo[1] || Fx->hi[1] != valid->hi[1]))
+    return TMK_ERR_BAD_DESC;
+  if (Fy && (!Fy->data || Fy->ncomp != TMK_NCOMP || Fy->lo[0] != valid->lo[0] || Fy->hi[0] != valid->hi[0] ||
+             Fy->lo[1] != valid->lo[1] || Fy->hi[1] != valid->hi[1] + 1))
+    return TMK_ERR_BAD_DESC;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int anx = U->hi[0] - U->lo[0] + 1, any = U->hi[1] - U->lo[1] + 1;
+  const size_t ucount = (size_t)TMK_NCOMP * anx * any;
+  std::vector<TileDev> tiles;
+  make_tiles(tiles, 0, *valid, tmk::Launch<double>::TX, tmk::Launch<double>::TY);
+  const int nfirst = nvx + 2;
+  // scratch: Uout | first | ffault | PatchDev | tiles | fault patch index
+  size_t off_u = 0;
+  size_t off_first = align_up(off_u + ucount * sizeof(double));
+  size_t off_ff = align_up(off_first + (size_t)TMK_NCOMP * nfirst * sizeof(double));
+  size_t off_pd = align_up(off_ff + (size_t)TMK_NCOMP * nvx * sizeof(double));
+  size_t off_tl = align_up(off_pd + sizeof(PatchDev<double>));
+  size_t off_fp = align_up(off_tl + tiles.size() * sizeof(TileDev));
+  size_t total = align_up(off_fp + sizeof(int));
+  if (total > c->scratch_bytes) {
+    TMK_CU(cudaStreamSynchronize(s));
+    cudaFree(c->scratch);
+    c->scratch = nullptr; c->scratch_bytes = 0;
+    if (cudaMalloc(&c->scratch, total) != cudaSuccess) return TMK_ERR_ALLOC;
+    c->scratch_bytes = total;
+  }
+  char* base = (char*)c->scratch;
+  PatchDev<double> pd;
+  std::memset(&pd, 0, sizeof(pd));
+  pd.Uin = U->data;
+  pd.Uout = (double*)(base + off_u);
+  pd.alo0 = U->lo[0]; pd.alo1 = U->lo[1]; pd.anx = anx; pd.any = any;
+  pd.vlo0 = valid->lo[0]; pd.vlo1 = valid->lo[1]; pd.vhi0 = valid->hi[0]; pd.vhi1 = valid->hi[1];
+  pd.dlo0 = domain->lo[0]; pd.dlo1 = domain->lo[1]; pd.dhi0 = domain->hi[0]; pd.dhi1 = domain->hi[1];
+  pd.dx = dx; pd.dt = dt; pd.scen = 0;
+  pd.plastic = 0;   // LinElastLevelGodunov::plasticUpdate is a separate call (tmk_plastic_update)
+  pd.fault = fault ? 1 : 0;
+  if (fault) { pd.B = B->data; pd.blo0 = B->lo[0]; pd.bnx = B->hi[0] - B->lo[0] + 1; }
+  pd.first = (double*)(base + off_first);
+  pd.ffault = (double*)(base + off_ff);
+  pd.nfirst = nfirst;
+  pd.Fx = Fx ? Fx->data : nullptr;
+  pd.Fy = Fy ? Fy->data : nullptr;
+  const int zero = 0;
+  // descriptors are staged through pageable memory: synchronous with respect to the host
+  TMK_CU(cudaMemcpyAsync(base + off_pd, &pd, sizeof(pd), cudaMemcpyHostToDevice, s));
+  TMK_CU(cudaMemcpyAsync(base + off_tl, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice, s));
+  TMK_CU(cudaMemcpyAsync(base + off_fp, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+  if (Fx) TMK_CU(cudaMemsetAsync(Fx->data, 0, (size_t)TMK_NCOMP * (nvx + 1) * nvy * sizeof(double), s));
+  if (Fy) TMK_CU(cudaMemsetAsync(Fy->data, 0, (size_t)TMK_NCOMP * nvx * (nvy + 1) * sizeof(double), s));
+  const PatchDev<double>* dpd = (const PatchDev<double>*)(base + off_pd);
+  if (fault)
+    TMK_CU(tmk::Launch<double>::fault(dpd, (const int*)(base + off_fp), 1, nvx, c->dp, time, c->dstatus, s));
+  TMK_CU(tmk::Launch<double>::volume(dpd, (const TileDev*)(base + off_tl), (int)tiles.size(), c->dp, s));
+  // the volume kernel writes the nine evolving components of each side;
+  // lambda and gamma are left untouched, as updateState leaves them
+  for (int sd = 0; sd < 2; ++sd)
+    TMK_CU(tmk::copy_valid(pd.Uout, U->data, pd.alo0, pd.alo1, anx, any, pd.vlo0, pd.vlo1, pd.vhi0, pd.vhi1,
+                           11 * sd, tmk::NSIDE, s));
+  if (max_wave_speed) *max_wave_speed = std::max(c->hp.cs, c->hp.cp);
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_plastic_update(tmk_context* c, const tmk_fab* U, const tmk_box* box, double dt,
+                                         void* stream) {
+  if (!c || !U || !U->data || !box || U->ncomp != TMK_NCOMP || !box_ok(*box)) return TMK_ERR_BAD_DESC;
+  tmk_box ub; ub.lo[0] = U->lo[0]; ub.lo[1] = U->lo[1]; ub.hi[0] = U->hi[0]; ub.hi[1] = U->hi[1];
+  if (!box_contains(ub, *box)) return TMK_ERR_BAD_DESC;
+  const int anx = U->hi[0] - U->lo[0] + 1, any = U->hi[1] - U->lo[1] + 1;
+  TMK_CU(tmk::plastic_fab(U->data, U->lo[0], U->lo[1], anx, any, box->lo[0], box->lo[1], box->hi[0], box->hi[1],
+                          c->dp, dt, (cudaStream_t)stream));
+  return TMK_OK;
+}
+
+// ---------------------------------------------------------------- level API
+namespace {
+
+struct LevelPatch {
+  tmk_box valid, alloc;
+  int fault = 0;
+  void* U[2] = {nullptr, nullptr};
+  double* B = nullptr;
+  int blo = 0, bnx = 0;
+  double* first = nullptr;
+  double* ffault = nullptr;
+};
+
+}  // namespace
+
+struct tmk_level_s {
+  tmk_context* ctx = nullptr;
+  tmk_box domain;
+  double dx = 0;
+  int prec = TMK_PREC_FP64;
+  std::vector<LevelPatch> patches;
+  void* dpatch[2] = {nullptr, nullptr};   // PatchDev arrays, parity 0 (U0->U1) and 1 (U1->U0)
+  std::vector<char> hpatch[2];
+  TileDev* dtiles = nullptr;
+  int ntiles = 0;
+  int* dfault = nullptr;
+  int nfault = 0, max_faces = 0;
+  CopyDev* dcopies = nullptr;
+  int ncopies = 0;
+  CopyDev* dbcopies = nullptr;
+  int nbcopies = 0;
+  double** dbptr = nullptr;
+  int* dblo = nullptr;
+  int* dbnx = nullptr;
+  double* stage = nullptr;                 // FP64 staging for set/get of the mixed form
+  size_t stage_count = 0;
+  int parity = 0;
+  double cur_dt = -1.0;
+  std::vector<void*> allocs;
+  // per-launch timing (tmk_level_profile)
+  std::vector<cudaEvent_t> ev;            // 4 events per recorded step
+  int prof_on = 0, prof_max = 0, prof_n = 0;
+};
+
+namespace {
+
+template <typename Real>
+void fill_patchdev(tmk_level_s* L, int parity) {
+  L->hpatch[parity].assign(L->patches.size() * sizeof(PatchDev<Real>), 0);
+  PatchDev<Real>* hp = (PatchDev<Real>*)L->hpatch[parity].data();
+  for (size_t p = 0; p < L->patches.size(); ++p) {
+    const LevelPatch& lp = L->patches[p];
+    PatchDev<Real>& d = hp[p];
+    d.Uin = (const Real*)lp.U[parity];
+    d.Uout = (Real*)lp.U[1 - parity];
+    d.alo0 = lp.alloc.lo[0]; d.alo1 = lp.alloc.lo[1];
+    d.anx = lp.alloc.hi[0] - lp.alloc.lo[0] + 1; d.any = lp.alloc.hi[1] - lp.alloc.lo[1] + 1;
+    d.vlo0 = lp.valid.lo[0]; d.vlo1 = lp.valid.lo[1]; d.vhi0 = lp.valid.hi[0]; d.vhi1 = lp.valid.hi[1];
+    d.dlo0 = L->domain.lo[0]; d.dlo1 = L->domain.lo[1]; d.dhi0 = L->domain.hi[0]; d.dhi1 = L->domain.hi[1];
+    d.dx = L->dx; d.dt = L->cur_dt; d.scen = 0;
+    d.plastic = L->ctx->scheme.plasticity ? 1 : 0;
+    d.fault = lp.fault;
+    d.B = lp.B; d.blo0 = lp.blo; d.bnx = lp.bnx;
+    d.first = lp.first; d.ffault = lp.ffault;
+    d.nfirst = lp.valid.hi[0] - lp.valid.lo[0] + 3;
+    d.Fx = nullptr; d.Fy = nullptr;
+  }
+}
+
+size_t real_size(int prec) { return prec == TMK_PREC_MIXED ? sizeof(float) : sizeof(double); }
+
+tmk_status upload_patchdev(tmk_level_s* L, cudaStream_t s) {
+  for (int par = 0; par < 2; ++par) {
+    if (L->prec == TMK_PREC_MIXED) fill_patchdev<float>(L, par); else fill_patchdev<double>(L, par);
+    TMK_CU(cudaMemcpyAsync(L->dpatch[par], L->hpatch[par].data(), L->hpatch[par].size(), cudaMemcpyHostToDevice, s));
+  }
+  return TMK_OK;
+}
+
+}  // namespace
+
+extern "C" void tmk_level_destroy(tmk_level* L) {
+  if (!L) return;
+  cudaDeviceSynchronize();
+  for (void* p : L->allocs) cudaFree(p);
+  for (cudaEvent_t e : L->ev) cudaEventDestroy(e);
+  delete L;
+}
+
+extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, double dx, int npatch,
+                                       const tmk_box* boxes, tmk_level** out) {
+  if (!out) return TMK_ERR_BAD_DESC;
+  *out = nullptr;
+  if (!c || !domain || !boxes || npatch <= 0 || !(dx > 0) || !box_ok(*domain)) return TMK_ERR_BAD_DESC;
+  if (domain->hi[1] - domain->lo[1] < 2) return TMK_ERR_BAD_DESC;   // the fault stencil needs 3 rows
+  // patches must be valid, inside the domain and disjoint
+  for (int p = 0; p < npatch; ++p) {
+    if (!box_ok(boxes[p]) || !box_contains(*domain, boxes[p])) return TMK_ERR_BAD_DESC;
+    for (int q = 0; q < p; ++q) {
+      tmk_box x = box_isect(boxes[p], boxes[q]);
+      if (box_ok(x)) return TMK_ERR_BAD_DESC;
+    }
+  }
+  tmk_level_s* L = new (std::nothrow) tmk_level_s();
+  if (!L) return TMK_ERR_ALLOC;
+  L->ctx = c; L->domain = *domain; L->dx = dx; L->prec = c->scheme.precision;
+  L->patches.resize(npatch);
+  const size_t rs = real_size(L->prec);
+  const int nb = c->nb;
+  std::vector<TileDev> tiles;
+  std::vector<int> fault_idx;
+  const int TX = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::TX : tmk::Launch<double>::TX;
+  const int TY = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::TY : tmk::Launch<double>::TY;
+  auto fail = [&](tmk_status st) { tmk_level_destroy(L); return st; };
+  size_t max_count = 0;
+  for (int p = 0; p < npatch; ++p) {
+    LevelPatch& lp = L->patches[p];
+    lp.valid = boxes[p];
+    lp.alloc = box_grow(boxes[p], TMK_NGHOST);
+    const int anx = lp.alloc.hi[0] - lp.alloc.lo[0] + 1, any = lp.alloc.hi[1] - lp.alloc.lo[1] + 1;
+    const size_t count = (size_t)TMK_NCOMP * anx * any;
+    max_count = std::max(max_count, count);
+    for (int k = 0; k < 2; ++k) {
+      if (cudaMalloc(&lp.U[k], count * rs) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+      L->allocs.push_back(lp.U[k]);
+      if (cudaMemset(lp.U[k], 0, count * rs) != cudaSuccess) return fail(TMK_ERR_CUDA);
+    }
+    lp.fault = (c->scheme.fault_law != TMK_FAULT_NONE && boxes[p].lo[1] == domain->lo[1]) ? 1 : 0;
+    if (lp.fault) {
+      lp.blo = boxes[p].lo[0] - TMK_NGHOST;
+      lp.bnx = boxes[p].hi[0] - boxes[p].lo[0] + 1 + 2 * TMK_NGHOST;
+      const int nv = boxes[p].hi[0] - boxes[p].lo[0] + 1;
+      if (dalloc(&lp.B, (size_t)nb * lp.bnx) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+      L->allocs.push_back(lp.B);
+      if (dalloc(&lp.first, (size_t)TMK_NCOMP * (nv + 2)) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+      L->allocs.push_back(lp.first);
+      if (dalloc(&lp.ffault, (size_t)TMK_NCOMP * nv) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+      L->allocs.push_back(lp.ffault);
+      cudaMemset(lp.B, 0, (size_t)nb * lp.bnx * sizeof(double));
+      cudaMemset(lp.ffault, 0, (size_t)TMK_NCOMP * nv * sizeof(double));
+      fault_idx.push_back(p);
+      L->max_faces = std::max(L->max_faces, nv);
+    }
+    make_tiles(tiles, p, boxes[p], TX, TY);
+  }
+  // fault-row tiles first so that their CTAs start early
+  std::stable_sort(tiles.begin(), tiles.end(), [&](const TileDev& a, const TileDev& b) {
+    return (a.y0 == domain->lo[1]) > (b.y0 == domain->lo[1]);
+  });
+  // same-level exchange lists: ghost cells of p covered by valid cells of q
+  std::vector<CopyDev> copies, bcopies;
+  for (int p = 0; p < npatch; ++p)
+    for (int q = 0; q < npatch; ++q) {
+      if (p == q) continue;
+      tmk_box g = box_isect(box_isect(L->patches[p].alloc, boxes[q]), *domain);
+      if (box_ok(g)) {
+        CopyDev cd; cd.src = q; cd.dst = p; cd.lo0 = g.lo[0]; cd.lo1 = g.lo[1]; cd.hi0 = g.hi[0]; cd.hi1 = g.hi[1];
+        copies.push_back(cd);
+      }
+      if (L->patches[p].fault && L->patches[q].fault) {
+        int lo = std::max(L->patches[p].blo, boxes[q].lo[0]);
+        int hi = std::min(L->patches[p].blo + L->patches[p].bnx - 1, boxes[q].hi[0]);
+        if (lo <= hi) {
+          CopyDev cd; cd.src = q; cd.dst = p; cd.lo0 = lo; cd.hi0 = hi; cd.lo1 = cd.hi1 = domain->lo[1];
+          bcopies.push_back(cd);
+        }
+      }
+    }
+  L->ntiles = (int)tiles.size();
+  L->nfault = (int)fault_idx.size();
+  L->ncopies = (int)copies.size();
+  L->nbcopies = (int)bcopies.size();
+  size_t pds = L->prec == TMK_PREC_MIXED ? sizeof(PatchDev<float>) : sizeof(PatchDev<double>);
+  for (int k = 0; k < 2; ++k) {
+    if (cudaMalloc(&L->dpatch[k], pds * npatch) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+    L->allocs.push_back(L->dpatch[k]);
+  }
+  if (dalloc(&L->dtiles, tiles.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+  L->allocs.push_back(L->dtiles);
+  TMK_CU(cudaMemcpy(L->dtiles, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice));
+  if (L->nfault) {
+    if (dalloc(&L->dfault, fault_idx.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+    L->allocs.push_back(L->dfault);
+    TMK_CU(cudaMemcpy(L->dfault, fault_idx.data(), fault_idx.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  if (L->ncopies) {
+    if (dalloc(&L->dcopies, copies.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+    L->allocs.push_back(L->dcopies);
+    TMK_CU(cudaMemcpy(L->dcopies, copies.data(), copies.size() * sizeof(CopyDev), cudaMemcpyHostToDevice));
+  }
+  if (L->nbcopies) {
+    std::vector<double*> bp(npatch, nullptr);
+    std::vector<int> blo(npatch, 0), bnx(npatch, 0);
+    for (int p = 0; p < npatch; ++p) { bp[p] = L->patches[p].B; blo[p] = L->patches[p].blo; bnx[p] = L->patches[p].bnx; }
+    if (dalloc(&L->dbcopies, bcopies.size()) != cudaSuccess || dalloc(&L->dbptr, npatch) != cudaSuccess ||
+        dalloc(&L->dblo, npatch) != cudaSuccess || dalloc(&L->dbnx, npatch) != cudaSuccess)
+      return fail(TMK_ERR_ALLOC);
+    L->allocs.push_back(L->dbcopies); L->allocs.push_back(L->dbptr);
+    L->allocs.push_back(L->dblo); L->allocs.push_back(L->dbnx);
+    TMK_CU(cudaMemcpy(L->dbcopies, bcopies.data(), bcopies.size() * sizeof(CopyDev), cudaMemcpyHostToDevice));
+    TMK_CU(cudaMemcpy(L->dbptr, bp.data(), npatch * sizeof(double*), cudaMemcpyHostToDevice));
+    TMK_CU(cudaMemcpy(L->dblo, blo.data(), npatch * sizeof(int), cudaMemcpyHostToDevice));
+    TMK_CU(cudaMemcpy(L->dbnx, bnx.data(), npatch * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  if (L->prec == TMK_PREC_MIXED) {
+    if (dalloc(&L->stage, max_count) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+    L->allocs.push_back(L->stage);
+    L->stage_count = max_count;
+  }
+  if (upload_patchdev(L, 0) != TMK_OK) return fail(TMK_ERR_CUDA);
+  TMK_CU(cudaDeviceSynchronize());
+  *out = L;
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_set_patch(tmk_level* L, int p, const double* U, const double* B, int host) {
+  if (!L || p < 0 || p >= (int)L->patches.size() || !U) return TMK_ERR_BAD_DESC;
+  LevelPatch& lp = L->patches[p];
+  const size_t count = (size_t)TMK_NCOMP * (lp.alloc.hi[0] - lp.alloc.lo[0] + 1) * (lp.alloc.hi[1] - lp.alloc.lo[1] + 1);
+  const cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  const int k = L->parity;   // the buffer the next step reads
+  if (L->prec == TMK_PREC_MIXED) {
+    TMK_CU(cudaMemcpy(L->stage, U, count * sizeof(double), kind));
+    TMK_CU(tmk::convert_d2f(L->stage, (float*)lp.U[k], count, 0));
+  } else {
+    TMK_CU(cudaMemcpy(lp.U[k], U, count * sizeof(double), kind));
+  }
+  // lambda and gamma are the only planes a step without plasticity never
+  // rewrites: keep them identical in the other buffer
+  const size_t plane = count / TMK_NCOMP * real_size(L->prec);
+  for (int c : {9, 10, 20, 21})
+    TMK_CU(cudaMemcpy((char*)lp.U[1 - k] + c * plane, (char*)lp.U[k] + c * plane, plane, cudaMemcpyDeviceToDevice));
+  if (lp.fault) {
+    if (!B) return TMK_ERR_BAD_DESC;
+    TMK_CU(cudaMemcpy(lp.B, B, (size_t)L->ctx->nb * lp.bnx * sizeof(double), kind));
+  }
+  TMK_CU(cudaDeviceSynchronize());
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_get_patch(tmk_level* L, int p, double* U, double* B, int host) {
+  if (!L || p < 0 || p >= (int)L->patches.size()) return TMK_ERR_BAD_DESC;
+  LevelPatch& lp = L->patches[p];
+  const size_t count = (size_t)TMK_NCOMP * (lp.alloc.hi[0] - lp.alloc.lo[0] + 1) * (lp.alloc.hi[1] - lp.alloc.lo[1] + 1);
+  const cudaMemcpyKind kind = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  TMK_CU(cudaDeviceSynchronize());
+  if (U) {
+    if (L->prec == TMK_PREC_MIXED) {
+      TMK_CU(tmk::convert_f2d((const float*)lp.U[L->parity], L->stage, count, 0));
+      TMK_CU(cudaMemcpy(U, L->stage, count * sizeof(double), kind));
+    } else {
+      TMK_CU(cudaMemcpy(U, lp.U[L->parity], count * sizeof(double), kind));
+    }
+  }
+  if (B && lp.fault) TMK_CU(cudaMemcpy(B, lp.B, (size_t)L->ctx->nb * lp.bnx * sizeof(double), kind));
+  TMK_CU(cudaDeviceSynchronize());
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_step(tmk_level* L, double time, double dt, void* stream, double* dt_new) {
+  if (!L || !(dt > 0)) return TMK_ERR_BAD_DESC;
+  cudaStream_t s = (cudaStream_t)stream;
+  tmk_context* c = L->ctx;
+  if (dt != L->cur_dt) {
+    L->cur_dt = dt;
+    if (upload_patchdev(L, s) != TMK_OK) return TMK_ERR_CUDA;
+  }
+  const int par = L->parity;
+  cudaEvent_t* ev = nullptr;
+  if (L->prof_on && L->prof_n < L->prof_max) ev = &L->ev[4 * (size_t)L->prof_n++];
+  if (ev) TMK_CU(cudaEventRecord(ev[0], s));
+  if (L->prec == TMK_PREC_MIXED) {
+    const PatchDev<float>* pd = (const PatchDev<float>*)L->dpatch[par];
+    TMK_CU(tmk::Launch<float>::exchange(pd, L->dcopies, L->ncopies, 0, TMK_NCOMP, s));
+    TMK_CU(tmk::bexchange(L->dbptr, L->dblo, L->dbnx, L->dbcopies, L->nbcopies, c->nb, s));
+    if (ev) TMK_CU(cudaEventRecord(ev[1], s));
+    TMK_CU(tmk::Launch<float>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, s));
+    if (ev) TMK_CU(cudaEventRecord(ev[2], s));
+    TMK_CU(tmk::Launch<float>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
+  } else {
+    const PatchDev<double>* pd = (const PatchDev<double>*)L->dpatch[par];
+    TMK_CU(tmk::Launch<double>::exchange(pd, L->dcopies, L->ncopies, 0, TMK_NCOMP, s));
+    TMK_CU(tmk::bexchange(L->dbptr, L->dblo, L->dbnx, L->dbcopies, L->nbcopies, c->nb, s));
+    if (ev) TMK_CU(cudaEventRecord(ev[1], s));
+    TMK_CU(tmk::Launch<double>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, s));
+    if (ev) TMK_CU(cudaEventRecord(ev[2], s));
+    TMK_CU(tmk::Launch<double>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
+  }
+  if (ev) TMK_CU(cudaEventRecord(ev[3], s));
+  L->parity = 1 - par;
+  if (dt_new) *dt_new = L->dx / std::max(c->hp.cs, c->hp.cp);
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_profile(tmk_level* L, int enable, int max_steps) {
+  if (!L || (enable && max_steps <= 0)) return TMK_ERR_BAD_DESC;
+  if (!enable) { L->prof_on = 0; return TMK_OK; }
+  TMK_CU(cudaDeviceSynchronize());
+  const size_t need = 4 * (size_t)max_steps;
+  while (L->ev.size() < need) {
+    cudaEvent_t e;
+    TMK_CU(cudaEventCreate(&e));
+    L->ev.push_back(e);
+  }
+  L->prof_on = 1; L->prof_max = max_steps; L->prof_n = 0;
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_profile_read(tmk_level* L, double out[4], int* nsteps) {
+  if (!L || !out) return TMK_ERR_BAD_DESC;
+  TMK_CU(cudaDeviceSynchronize());
+  double acc[4] = {0, 0, 0, 0};
+  for (int k = 0; k < L->prof_n; ++k) {
+    cudaEvent_t* e = &L->ev[4 * (size_t)k];
+    float a, b, cc, d;
+    TMK_CU(cudaEventElapsedTime(&a, e[0], e[1]));
+    TMK_CU(cudaEventElapsedTime(&b, e[1], e[2]));
+    TMK_CU(cudaEventElapsedTime(&cc, e[2], e[3]));
+    TMK_CU(cudaEventElapsedTime(&d, e[0], e[3]));
+    acc[0] += a; acc[1] += b; acc[2] += cc; acc[3] += d;
+  }
+  for (int k = 0; k < 4; ++k) out[k] = L->prof_n ? acc[k] / L->prof_n : 0.0;
+  if (nsteps) *nsteps = L->prof_n;
+  return TMK_OK;
+}
+
+extern "C" int tmk_level_launches_per_step(const tmk_level* L) {
+  if (!L) return 0;
+  return (L->ncopies ? 1 : 0) + (L->nbcopies ? 1 : 0) + (L->nfault ? 1 : 0) + (L->ntiles ? 1 : 0);
+}
+
+extern "C" tmk_status tmk_level_status(tmk_level* L, long long info[3]) {
+  if (!L || !info) return TMK_ERR_BAD_DESC;
+  DevStatus h;
+  TMK_CU(cudaDeviceSynchronize());
+  TMK_CU(cudaMemcpy(&h, L->ctx->dstatus, sizeof(h), cudaMemcpyDeviceToHost));
+  TMK_CU(cudaMemset(L->ctx->dstatus, 0, sizeof(DevStatus)));
+  info[0] = h.code; info[1] = h.first_index; info[2] = (long long)h.newton_maxed;
+  return h.code == 0 ? TMK_OK : (tmk_status)h.code;
+}

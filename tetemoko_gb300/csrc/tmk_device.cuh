@@ -1,0 +1,403 @@
+// tmk_device.cuh -- per-point physics of the GB300 Godunov step.
+//
+// Every routine works on ONE side of the fault (9 state components, local order
+// vx vy vz sxx syy szz sxy sxz syz) in ONE direction D (0 = x, 1 = y).  The two
+// sides of the mirrored grid only meet at the fault face, and inside the
+// volume the reference's 22-component transforms are block-diagonal by side,
+// so the volume kernel runs one side per CTA.
+//
+// Two arithmetic policies share the code:
+//   * double: the reference's operation order (srcLinElast/LinElastPhysicsF.ChF),
+//     compiled without FMA contraction, so the FP64 path matches the CPU oracle
+//     to rounding;
+//   * float : the same formulas with divisions replaced by precomputed
+//     reciprocals, for the mixed-precision volume kernel.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <type_traits>
+
+#define TMK_HD __host__ __device__ __forceinline__
+#define TMK_D __device__ __forceinline__
+
+namespace tmk {
+
+constexpr int NC = 22;
+constexpr int NSIDE = 9;          // evolving components per side
+constexpr int NGHOST = 4;
+constexpr int SW_MAXP = 8;
+
+// Per-scenario parameters (the reference's COMMON blocks, precomputed on the host).
+struct DevParams {
+  // /IBC/ (LINELASTSETF)
+  double cs, cp, G, rho, lam, K, Zp, Zs;
+  double bg[22];
+  // scheme
+  int order, prim_lim, char_lim;
+  int bc[6];
+  int fault_law;            // 0 none, 1 RS, 2 SW
+  int plasticity;
+  // rate and state (RSSETF)
+  double rs_r0, rs_x0, rs_nsig, rs_a, rs_b, rs_V0, rs_f0, rs_L, rs_fw, rs_Vw, rs_fexp;
+  double ramp_x, ramp_w, ramp_a, ramp_Vw, rs_thr;
+  int state_law;
+  // slip weakening (SWSETF + SWIBC members)
+  double sw_fs, sw_fd, sw_dw, sw_smooth;
+  int sw_np;
+  double sw_xc[SW_MAXP], sw_xw[SW_MAXP], sw_tau[SW_MAXP];
+  double sw_fbc0, sw_fbw0, sw_outside, sw_thr;
+  int sw_off;               // side-2 component offset, 9 (reference) or 11
+  // plasticity (PLASTICSETF)
+  double p_mu, p_beta, p_eta, p_b, p_h;
+};
+
+// Constants of one arithmetic type.
+template <typename T>
+struct Consts {
+  T lam, G, rho, Zp, Zs, lam2G;           // lam2G = 2G + lam
+  T inv_rho, inv_Zp, inv_Zs, ratio;       // ratio = lam/(2G+lam)
+  T half_inv_Zp, half_inv_Zs, lamp2G;     // lamp2G = lam + 2G
+  T cs, cp;
+  TMK_D void load(const DevParams& p) {
+    lam = (T)p.lam; G = (T)p.G; rho = (T)p.rho; Zp = (T)p.Zp; Zs = (T)p.Zs;
+    lam2G = (T)(2.0 * p.G + p.lam);
+    lamp2G = (T)(p.lam + 2.0 * p.G);
+    inv_rho = (T)(1.0 / p.rho); inv_Zp = (T)(1.0 / p.Zp); inv_Zs = (T)(1.0 / p.Zs);
+    ratio = (T)(p.lam / (2.0 * p.G + p.lam));
+    half_inv_Zp = (T)(0.5 / p.Zp); half_inv_Zs = (T)(0.5 / p.Zs);
+    cs = (T)p.cs; cp = (T)p.cp;
+  }
+};
+
+template <typename T> constexpr bool kExact = std::is_same<T, double>::value;
+
+// Rotation of LinElastPhysicsF.ChF's directional routines (cx, cy, cz, cxy, cxz, cyz).
+template <int D> struct Rot;
+template <> struct Rot<0> { static constexpr int cx = 0, cy = 1, cz = 2, cxy = 6, cxz = 7, cyz = 8; };
+template <> struct Rot<1> { static constexpr int cx = 1, cy = 2, cz = 0, cxy = 8, cxz = 6, cyz = 7; };
+
+// lambda-ratio product  s*lam/(2G+lam)
+template <typename T> TMK_D T lratio(const Consts<T>& k, T s) {
+  if constexpr (kExact<T>) return s * k.lam / k.lam2G; else return s * k.ratio;
+}
+
+// ---------------------------------------------------------------- CHARANALYSISF
+// Output order of the nine characteristic variables of one side:
+//   0 sxx+Zp vx (-cp)  1 sxy+Zs vy (-cs)  2 sxz+Zs vz (-cs)  3 wyy (0)  4 wzz (0)
+//   5 wyz (0)  6 sxz-Zs vz (+cs)  7 sxy-Zs vy (+cs)  8 sxx-Zp vx (+cp)
+template <int D, typename T>
+TMK_D void char_analysis(const Consts<T>& k, T rv, const T* q, T* w) {
+  using R = Rot<D>;
+  T vx = rv * q[R::cx], vy = rv * q[R::cy], vz = rv * q[R::cz];
+  T sxx = q[R::cx + 3], syy = q[R::cy + 3], szz = q[R::cz + 3];
+  T sxy = q[R::cxy], sxz = q[R::cxz], syz = q[R::cyz];
+  w[0] = sxx + vx * k.Zp;
+  w[1] = sxy + vy * k.Zs;
+  w[2] = sxz + vz * k.Zs;
+  w[3] = syy - lratio(k, sxx);
+  w[4] = szz - lratio(k, sxx);
+  w[5] = syz;
+  w[6] = sxz - vz * k.Zs;
+  w[7] = sxy - vy * k.Zs;
+  w[8] = sxx - vx * k.Zp;
+}
+
+// ---------------------------------------------------------------- CHARSYNTHESISF
+template <int D, typename T>
+TMK_D void char_synthesis(const Consts<T>& k, T rv, const T* w, T* q) {
+  using R = Rot<D>;
+  T wxxm = w[0], wxym = w[1], wxzm = w[2], wyy = w[3], wzz = w[4], wyz = w[5];
+  T wxzp = w[6], wxyp = w[7], wxxp = w[8];
+  T sxx = (wxxm + wxxp) / T(2);
+  if constexpr (kExact<T>) {
+    q[R::cx] = rv * (wxxm - wxxp) / 2.0 / k.Zp;
+    q[R::cy] = rv * (wxym - wxyp) / 2.0 / k.Zs;
+    q[R::cz] = rv * (wxzm - wxzp) / 2.0 / k.Zs;
+  } else {
+    q[R::cx] = rv * (wxxm - wxxp) * k.half_inv_Zp;
+    q[R::cy] = rv * (wxym - wxyp) * k.half_inv_Zs;
+    q[R::cz] = rv * (wxzm - wxzp) * k.half_inv_Zs;
+  }
+  q[R::cx + 3] = sxx;
+  q[R::cy + 3] = wyy + lratio(k, sxx);
+  q[R::cz + 3] = wzz + lratio(k, sxx);
+  q[R::cxy] = (wxym + wxyp) / T(2);
+  q[R::cxz] = (wxzm + wxzp) / T(2);
+  q[R::cyz] = wyz;
+}
+
+// ---------------------------------------------------------------- RIEMANNF
+template <int D, typename T>
+TMK_D void riemann(const Consts<T>& k, T rv, const T* L, const T* Rr, T* g) {
+  using R = Rot<D>;
+  T wxxp = L[R::cx + 3] - rv * k.Zp * L[R::cx];
+  T wxyp = L[R::cxy] - rv * k.Zs * L[R::cy];
+  T wxzp = L[R::cxz] - rv * k.Zs * L[R::cz];
+  T wxxm = Rr[R::cx + 3] + rv * k.Zp * Rr[R::cx];
+  T wxym = Rr[R::cxy] + rv * k.Zs * Rr[R::cy];
+  T wxzm = Rr[R::cxz] + rv * k.Zs * Rr[R::cz];
+  T wyy = Rr[R::cy + 3] - lratio(k, Rr[R::cx + 3]);
+  T wzz = Rr[R::cz + 3] - lratio(k, Rr[R::cx + 3]);
+  T wyz = Rr[R::cyz];
+  wyy = (wyy + L[R::cy + 3] - lratio(k, L[R::cx + 3])) / T(2);
+  wzz = (wzz + L[R::cz + 3] - lratio(k, L[R::cx + 3])) / T(2);
+  wyz = (wyz + L[R::cyz]) / T(2);
+  T sxx = (wxxm + wxxp) / T(2);
+  if constexpr (kExact<T>) {
+    g[R::cx] = rv * (wxxm - wxxp) / 2.0 / k.Zp;
+    g[R::cy] = rv * (wxym - wxyp) / 2.0 / k.Zs;
+    g[R::cz] = rv * (wxzm - wxzp) / 2.0 / k.Zs;
+  } else {
+    g[R::cx] = rv * (wxxm - wxxp) * k.half_inv_Zp;
+    g[R::cy] = rv * (wxym - wxyp) * k.half_inv_Zs;
+    g[R::cz] = rv * (wxzm - wxzp) * k.half_inv_Zs;
+  }
+  g[R::cx + 3] = (wxxm + wxxp) / T(2);
+  g[R::cy + 3] = wyy + lratio(k, sxx);
+  g[R::cz + 3] = wzz + lratio(k, sxx);
+  g[R::cxy] = (wxym + wxyp) / T(2);
+  g[R::cxz] = (wxzm + wxzp) / T(2);
+  g[R::cyz] = wyz;
+}
+
+// ---------------------------------------------------------------- GETFLUXF
+template <int D, typename T>
+TMK_D void flux(const Consts<T>& k, T rv, const T* g, T* F) {
+  using R = Rot<D>;
+  T vx = g[R::cx], vy = g[R::cy], vz = g[R::cz];
+  T sxx = g[R::cx + 3], sxy = g[R::cxy], sxz = g[R::cxz];
+  if constexpr (kExact<T>) {
+    F[R::cx] = -rv * sxx / k.rho;
+    F[R::cy] = -rv * sxy / k.rho;
+    F[R::cz] = -rv * sxz / k.rho;
+    F[R::cx + 3] = -rv * vx * (k.lam + 2.0 * k.G);
+    F[R::cy + 3] = -rv * vx * k.lam;
+    F[R::cz + 3] = -rv * vx * k.lam;
+    F[R::cxy] = -rv * vy * k.G;
+    F[R::cxz] = -rv * vz * k.G;
+  } else {
+    T m = -rv;
+    F[R::cx] = m * sxx * k.inv_rho;
+    F[R::cy] = m * sxy * k.inv_rho;
+    F[R::cz] = m * sxz * k.inv_rho;
+    F[R::cx + 3] = m * vx * k.lamp2G;
+    F[R::cy + 3] = m * vx * k.lam;
+    F[R::cz + 3] = m * vx * k.lam;
+    F[R::cxy] = m * vy * k.G;
+    F[R::cxz] = m * vz * k.G;
+  }
+  F[R::cyz] = T(0);
+}
+
+// ---------------------------------------------------------------- GETADWDXF
+// increment of one cell from the face states at its hi (h) and lo (l) faces
+template <int D, typename T>
+TMK_D void adwdx_add(const Consts<T>& k, T rv, T scale, const T* h, const T* l, T* q) {
+  using R = Rot<D>;
+  T vx = h[R::cx] - l[R::cx];
+  T vy = h[R::cy] - l[R::cy];
+  T vz = h[R::cz] - l[R::cz];
+  T sxx = h[R::cx + 3] - l[R::cx + 3];
+  T sxy = h[R::cxy] - l[R::cxy];
+  T sxz = h[R::cxz] - l[R::cxz];
+  if constexpr (kExact<T>) {
+    q[R::cx] += -rv * scale * sxx / k.rho;
+    q[R::cy] += -rv * scale * sxy / k.rho;
+    q[R::cz] += -rv * scale * sxz / k.rho;
+    q[R::cx + 3] += -rv * scale * vx * (k.lam + 2.0 * k.G);
+    q[R::cy + 3] += -rv * scale * vx * k.lam;
+    q[R::cz + 3] += -rv * scale * vx * k.lam;
+    q[R::cxy] += -rv * scale * vy * k.G;
+    q[R::cxz] += -rv * scale * vz * k.G;
+    q[R::cyz] += -rv * scale * 0.0;
+  } else {
+    T m = -rv * scale;
+    q[R::cx] += m * sxx * k.inv_rho;
+    q[R::cy] += m * sxy * k.inv_rho;
+    q[R::cz] += m * sxz * k.inv_rho;
+    q[R::cx + 3] += m * vx * k.lamp2G;
+    q[R::cy + 3] += m * vx * k.lam;
+    q[R::cz + 3] += m * vx * k.lam;
+    q[R::cxy] += m * vy * k.G;
+    q[R::cxz] += m * vz * k.G;
+  }
+}
+
+// ------------------------------------------- LINELASTOUTBCF / LINELASTFREEBCF
+// Boundary Riemann state of one side at a domain edge.  `bg` is the side's
+// background (outflow only).  SHF is the normal VELOCITY minus sxx, as written
+// in the reference; it only reaches components no flux or transverse term reads.
+template <int D, typename T>
+TMK_D void edge_bc(const Consts<T>& k, T rv, int lohisign, bool outflow, const T* bg, const T* wi, T* g) {
+  using R = Rot<D>;
+  T wpx, wpy, wpz, wmx, wmy, wmz;
+  if (outflow) {
+    wpx = bg[R::cx + 3] - rv * k.Zp * bg[R::cx];
+    wpy = bg[R::cxy] - rv * k.Zs * bg[R::cy];
+    wpz = bg[R::cxz] - rv * k.Zs * bg[R::cz];
+    wmx = bg[R::cx + 3] + rv * k.Zp * bg[R::cx];
+    wmy = bg[R::cxy] + rv * k.Zs * bg[R::cy];
+    wmz = bg[R::cxz] + rv * k.Zs * bg[R::cz];
+    if (lohisign == -1) {
+      wmx = (wi[R::cx + 3] + rv * k.Zp * wi[R::cx]);
+      wmy = (wi[R::cxy] + rv * k.Zs * wi[R::cy]);
+      wmz = (wi[R::cxz] + rv * k.Zs * wi[R::cz]);
+    } else {
+      wpx = (wi[R::cx + 3] - rv * k.Zp * wi[R::cx]);
+      wpy = (wi[R::cxy] - rv * k.Zs * wi[R::cy]);
+      wpz = (wi[R::cxz] - rv * k.Zs * wi[R::cz]);
+    }
+  } else {
+    if (lohisign == -1) {
+      wmx = (wi[R::cx + 3] + rv * k.Zp * wi[R::cx]);
+      wmy = (wi[R::cxy] + rv * k.Zs * wi[R::cy]);
+      wmz = (wi[R::cxz] + rv * k.Zs * wi[R::cz]);
+      wpx = -wmx; wpy = -wmy; wpz = -wmz;
+    } else {
+      wpx = (wi[R::cx + 3] - rv * k.Zp * wi[R::cx]);
+      wpy = (wi[R::cxy] - rv * k.Zs * wi[R::cy]);
+      wpz = (wi[R::cxz] - rv * k.Zs * wi[R::cz]);
+      wmx = -wpx; wmy = -wpy; wmz = -wpz;
+    }
+  }
+  T sxx = (wmx + wpx) / T(2);
+  T SHF;
+  if constexpr (kExact<T>) {
+    SHF = -(wi[R::cx] - sxx) * k.lam / (k.lam + 2.0 * k.G);
+    g[R::cx] = rv * (wmx - wpx) / (2.0 * k.Zp);
+    g[R::cy] = rv * (wmy - wpy) / (2.0 * k.Zs);
+    g[R::cz] = rv * (wmz - wpz) / (2.0 * k.Zs);
+  } else {
+    SHF = -(wi[R::cx] - sxx) * k.ratio;
+    g[R::cx] = rv * (wmx - wpx) * k.half_inv_Zp;
+    g[R::cy] = rv * (wmy - wpy) * k.half_inv_Zs;
+    g[R::cz] = rv * (wmz - wpz) * k.half_inv_Zs;
+  }
+  g[R::cx + 3] = sxx;
+  g[R::cy + 3] = wi[R::cy + 3] + SHF;
+  g[R::cz + 3] = wi[R::cz + 3] + SHF;
+  g[R::cxy] = (wmy + wpy) / T(2);
+  g[R::cxz] = (wmz + wpz) / T(2);
+  g[R::cyz] = wi[R::cyz];
+}
+
+// ---------------------------------------------------------------- PPM stages
+// Van Leer limited slope of the middle value (one-sided where a neighbour is
+// outside the domain).
+template <typename T>
+TMK_D T vl_slope(T wm, T w0, T wp, bool hasL, bool hasR, bool limit) {
+  T dwl, dwr, dwc;
+  if (hasL && hasR) {
+    dwl = w0 - wm; dwr = wp - w0; dwc = T(0.5) * (wp - wm);
+  } else if (hasR) {
+    dwr = wp - w0; dwl = dwr; dwc = dwr;
+  } else if (hasL) {
+    dwl = w0 - wm; dwr = dwl; dwc = dwl;
+  } else {
+    return T(0);
+  }
+  if (!limit) return dwc;
+  if (dwl * dwr > T(0)) {
+    T m = fmin(fabs(dwc), fmin(T(2) * fabs(dwl), T(2) * fabs(dwr)));
+    return dwc >= T(0) ? m : -m;
+  }
+  return T(0);
+}
+
+// Face deltas (W_{lo face} - W, W_{hi face} - W) of the PPM parabola of the
+// middle cell from five values w[0..4] (cells -2..+2) with in[k] telling
+// whether cell k-2 lies in the domain (in[2] is always true).
+template <typename T>
+TMK_D void ppm_deltas(const T* w, const bool* in, bool limit, T& dm, T& dp) {
+  T sm = in[1] ? vl_slope(w[0], w[1], w[2], in[0], true, limit) : T(0);
+  T s0 = vl_slope(w[1], w[2], w[3], in[1], in[3], limit);
+  T sp = in[3] ? vl_slope(w[2], w[3], w[4], true, in[4], limit) : T(0);
+  T flo, fhi;
+  if (in[1]) flo = T(0.5) * (w[1] + w[2]) - (s0 - sm) / T(6);
+  else       flo = w[2] - T(0.5) * s0;
+  if (in[3]) fhi = T(0.5) * (w[2] + w[3]) - (sp - s0) / T(6);
+  else       fhi = w[2] + T(0.5) * s0;
+  dm = (T(0) - w[2]) + flo;
+  dp = (T(0) - w[2]) + fhi;
+}
+
+// PPM limiter (Colella & Woodward 1984 eq. 1.10) on one pair of deltas
+template <typename T>
+TMK_D void ppm_limit(T& m, T& p) {
+  if (m * p < T(0)) {
+    T am = fmin(fabs(m), T(2) * fabs(p));
+    T ap = fmin(fabs(p), T(2) * fabs(m));
+    m = m >= T(0) ? am : -am;
+    p = p >= T(0) ? ap : -ap;
+  } else {
+    m = T(0); p = T(0);
+  }
+}
+
+// PPM characteristic tracing (Colella & Woodward 1984 eq. 1.12) of one
+// characteristic with Courant number sig = lambda dt/dx
+template <typename T>
+TMK_D void ppm_trace(T sig, T& m, T& p) {
+  if (sig > T(0)) {
+    T s = sig;
+    p = p - T(0.5) * s * ((p - m) + T(3) * (T(1) - (T(2) / T(3)) * s) * (m + p));
+  } else if (sig < T(0)) {
+    T s = -sig;
+    m = m + T(0.5) * s * (p - m) - T(3) * (m + p) * (T(0.5) * s - s * s / T(3));
+  }
+}
+
+// Normal predictor of one side of one cell in direction D (order 2: PPM;
+// order 0: CTUNormalPred, a straight copy of the cell state to both faces,
+// srcLinElast/LinElastPatchGodunov.cpp:471-483).
+// Full PPM normal predictor of one side of one cell in direction D:
+// w5[c][k] holds component c at cells -2..+2.  Produces WM (lo face) and WP.
+// sig[9] are the characteristic Courant numbers (-cp,-cs,-cs,0,0,0,cs,cs,cp)*dt/dx.
+template <int D, typename T>
+TMK_D void ppm_predict(const Consts<T>& k, T rv, const T (*w5)[5], const bool* in, bool prim_lim,
+                       bool char_lim, const T* sig, T* WM, T* WP, int order = 2) {
+  if (order == 0) {
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) { WM[c] = w5[c][2]; WP[c] = w5[c][2]; }
+    return;
+  }
+  T dm[NSIDE], dp[NSIDE];
+  const bool limit = prim_lim || char_lim;
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) ppm_deltas(w5[c], in, limit, dm[c], dp[c]);
+  T cm[NSIDE], cpv[NSIDE];
+  if (char_lim) {
+    char_analysis<D>(k, rv, dm, cm);
+    char_analysis<D>(k, rv, dp, cpv);
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) ppm_limit(cm[c], cpv[c]);
+  } else {
+    if (prim_lim) {
+#pragma unroll
+      for (int c = 0; c < NSIDE; ++c) ppm_limit(dm[c], dp[c]);
+    }
+    char_analysis<D>(k, rv, dm, cm);
+    char_analysis<D>(k, rv, dp, cpv);
+  }
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) ppm_trace(sig[c], cm[c], cpv[c]);
+  char_synthesis<D>(k, rv, cm, WM);
+  char_synthesis<D>(k, rv, cpv, WP);
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) { WM[c] += w5[c][2]; WP[c] += w5[c][2]; }
+}
+
+// -------------------------------------------------------- status reporting
+enum : int { ST_OK = 0, ST_NAN = 2, ST_TIMEOUT = 3 };
+struct DevStatus {
+  int code;                 // first error code (0 = none)
+  int pad;
+  long long first_index;    // flat index of the first bad value
+  unsigned long long newton_maxed;   // Newton solves that used all IMAX iterations
+};
+
+TMK_D void report(DevStatus* st, int code, long long idx) {
+  if (atomicCAS(&st->code, 0, code) == 0) st->first_index = idx;
+}
+
+}  // namespace tmk

@@ -1,0 +1,253 @@
+// tmk_fault.cuh -- FP64 fault-face friction solves, boundary-data updates and
+// the Drucker-Prager return, one face (or cell) per thread.
+//
+// Friction laws follow ibcLinElast/RSIBCF.ChF (RSFAULTBCF, RSNEWTON, RSSETBND)
+// and ibcLinElast/SWIBCF.ChF (SWFAULTBCF, SWSETBND) with the reference's
+// operation order; plasticity follows srcLinElast/PlasticPhysicsF.ChF.
+#pragma once
+#include "tmk_device.cuh"
+
+namespace tmk {
+
+TMK_D double gaussian(double w, double r) { double q = r / w; return exp(-(0.5 * (q * q))); }
+TMK_D double smoothfn(double w, double r) {
+  if (r >= w) return 0.0;
+  if (r <= 0) return 1.0;
+  return exp(r * r / (r * r - w * w));
+}
+TMK_D double boxcar(double w, double r) { return (r >= w) ? 0.0 : 1.0; }
+
+constexpr int RS_IMAX = 100;
+
+// RSNEWTON (ibcLinElast/RSIBCF.ChF:336-401): bracketed Newton on the slip rate
+// for  sn a asinh(V exp(psi/a)/(2V0)) + Zs/2 V = phi  on (0, phi/Zs).  The loop
+// is bounded by IMAX; returns the iterations used.
+TMK_D int rs_newton(const DevParams& P, double phi, double psi, double sn, double c_rs_a, double& V,
+                    double& tau) {
+  const double atolG = 2.220446049250313e-16 * 1e4;
+  double Vmin = 0.0, Vmax = phi / P.Zs;
+  if (V < Vmin || V > Vmax) V = (Vmin + Vmax) / 2.0;
+  double alpha = sn * c_rs_a;
+  double beta = exp(psi / c_rs_a) / (2.0 * P.rs_V0);
+  double eta = 0.5 * P.Zs;
+  double fval = alpha * asinh(beta * V) + eta * V - phi;
+  int it;
+  for (it = 1; it <= RS_IMAX; ++it) {
+    if (fval < 0) Vmin = V; else Vmax = V;
+    double dfval = alpha * beta / sqrt((beta * beta) * (V * V) + 1) + eta;
+    double dV = -fval / dfval;
+    V = V + dV;
+    if (V < Vmin || V > Vmax) V = (Vmin + Vmax) / 2.0;
+    fval = alpha * asinh(beta * V) + eta * V - phi;
+    if (fabs(fval) <= atolG) break;
+    if (fabs(dV) <= 0.0) break;
+  }
+  tau = alpha * asinh(beta * V);
+  return it;
+}
+
+// RSFAULTBCF (ibcLinElast/RSIBCF.ChF:158-323) at one fault face; Wi, Wg: 22 comps.
+TMK_D int rs_fault(const DevParams& P, const double* Wi, double psi, double x, double* Wg) {
+  const double Zs = P.Zs, Zp = P.Zp, lam = P.lam, G = P.G;
+  double vx1 = Wi[0], vy1 = Wi[1], vz1 = Wi[2], sxx1 = Wi[3], syy1 = Wi[4], szz1 = Wi[5];
+  double sxy1 = Wi[6], sxz1 = Wi[7], syz1 = Wi[8];
+  double vx2 = Wi[11], vy2 = Wi[12], vz2 = Wi[13], sxx2 = Wi[14], syy2 = Wi[15], szz2 = Wi[16];
+  double sxy2 = Wi[17], sxz2 = Wi[18], syz2 = Wi[19];
+  double wpxy1 = -sxy1 - Zs * vx1;
+  double wpyy1 = -syy1 - Zp * vy1;
+  double wpxy2 = sxy2 - Zs * vx2;
+  double wpyy2 = syy2 - Zp * vy2;
+  double wpyz1 = 0.0, wpyz2 = 0.0;
+  (void)syz1; (void)syz2;
+  double tau_xy_0 = P.rs_nsig * gaussian(P.rs_r0, x);
+  double tau_yz_0 = 0.0;
+  double phi_xy = 0.5 * (wpxy2 - wpxy1) + tau_xy_0;
+  double phi_yz = 0.5 * (wpyz2 - wpyz1) + tau_yz_0;
+  double phi = sqrt(phi_xy * phi_xy + phi_yz * phi_yz);
+  syy1 = -(wpyy1 - wpyy2) / 2.0;
+  syy2 = -(wpyy1 - wpyy2) / 2.0;
+  vy1 = -(wpyy1 + wpyy2) / 2.0 / Zp;
+  vy2 = -(wpyy1 + wpyy2) / 2.0 / Zp;
+  double V = sqrt((vx1 - vx2) * (vx1 - vx2) + (vz1 - vz2) * (vz1 - vz2));
+  double c_ramp = fmin(1.0, fmax(0.0, (x - P.ramp_x) / P.ramp_w));
+  double c_rs_a = P.rs_a + P.ramp_a * c_ramp;
+  double tau;
+  int it = rs_newton(P, phi, psi, -syy1, c_rs_a, V, tau);
+  sxy1 = (phi_xy / phi) * tau - tau_xy_0;
+  syz1 = (phi_yz / phi) * tau - tau_yz_0;
+  double Vx = (phi_xy / phi) * V;
+  double Vz = (phi_yz / phi) * V;
+  vx1 = -(sxy1 + wpxy1) / Zs;
+  vz1 = -(syz1 + wpyz1) / Zs;
+  double SHF = -(vy1 - syy1) * lam / (lam + 2.0 * G);
+  Wg[0] = vx1; Wg[1] = vy1; Wg[2] = vz1;
+  Wg[3] = sxx1 + SHF; Wg[4] = syy1; Wg[5] = szz1 + SHF;
+  Wg[6] = sxy1; Wg[7] = sxz1; Wg[8] = syz1;
+  Wg[9] = 0.0; Wg[10] = 0.0;
+  sxy2 = (phi_xy / phi) * tau - tau_xy_0;
+  syz2 = (phi_yz / phi) * tau - tau_yz_0;
+  vx2 = vx1 - Vx;
+  vz2 = vz1 - Vz;
+  SHF = -(vy2 - syy2) * lam / (lam + 2.0 * G);
+  Wg[11] = vx2; Wg[12] = vy2; Wg[13] = vz2;
+  Wg[14] = sxx2 + SHF; Wg[15] = syy2; Wg[16] = szz2 + SHF;
+  Wg[17] = sxy2; Wg[18] = sxz2; Wg[19] = syz2;
+  Wg[20] = 0.0; Wg[21] = 0.0;
+  return it;
+}
+
+// RSSETBND (ibcLinElast/RSIBCF.ChF:61-151) for one face, B in/out (11 comps,
+// strided).  When `final_` is false only psi is produced (the predictor's
+// tmp data, of which the fault solve reads nothing else).  Returns the new
+// psi (NaN is reported by the caller; the reference stops there).
+TMK_D double rs_setbnd(const DevParams& P, const double* U, double* B, int bstride, double dt, double x,
+                       double time, bool final_) {
+  double tau_xy_0 = P.rs_nsig * gaussian(P.rs_r0, x);
+  double c_ramp = fmin(1.0, fmax(0.0, (x - P.ramp_x) / P.ramp_w));
+  double c_rs_a = P.rs_a + P.ramp_a * c_ramp;
+  double c_rs_Vw = P.rs_Vw + P.ramp_Vw * c_ramp;
+  double Vx = U[0] - U[11];
+  double Vz = U[2] - U[13];
+  double V = sqrt(Vx * Vx + Vz * Vz);
+  double psi = B[10 * bstride];
+  double dPsi;
+  if (P.state_law == 1) {
+    // aging law (extension), exact at constant V over dt:
+    // theta' = theta exp(-x) + dt (1-exp(-x))/x, x = V dt / L
+    double xx = V * dt / P.rs_L;
+    double phi1 = (xx > 1e-12) ? -expm1(-xx) / xx : 1.0 - 0.5 * xx;
+    double q = (psi - P.rs_f0) / P.rs_b - xx;
+    dPsi = P.rs_f0 + P.rs_b * log(exp(q) + (P.rs_V0 * dt / P.rs_L) * phi1);
+  } else {
+    double f = c_rs_a * asinh(V * exp(psi / c_rs_a) / (2.0 * P.rs_V0));
+    double fss = P.rs_f0 - (P.rs_b - c_rs_a) * log(V / P.rs_V0);
+    if (P.rs_fexp > 0.0) {
+      double q = V / c_rs_Vw, q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
+      fss = P.rs_fw + (fss - P.rs_fw) / pow(1.0 + q8, 0.125);
+    }
+    dPsi = psi - dt * (V / P.rs_L) * (f - fss);
+  }
+  if (final_) {
+    double rt = B[9 * bstride];
+    B[0] = Vx;
+    B[1 * bstride] = Vz;
+    B[2 * bstride] = V;
+    B[3 * bstride] = U[6] + tau_xy_0;
+    B[4 * bstride] = U[8] + 0.0;
+    B[6 * bstride] = B[6 * bstride] + dt * Vx;
+    B[7 * bstride] = B[7 * bstride] + dt * Vz;
+    B[8 * bstride] = B[8 * bstride] + dt * V;
+    if (rt > time && V > P.rs_thr) B[9 * bstride] = time;
+    else if (rt > time) B[9 * bstride] = 1e10;
+    B[5 * bstride] = U[4];
+    B[10 * bstride] = dPsi;
+  }
+  return dPsi;
+}
+
+// SWFAULTBCF (ibcLinElast/SWIBCF.ChF:79-267) at one fault face.  Side 2 is read
+// and written at component offset P.sw_off (9 as in the reference source).
+// Components the law does not write keep the values already in Wg.
+TMK_D void sw_fault(const DevParams& P, const double* Wi, double slip_total, double xcell, double* Wg) {
+  const int off = P.sw_off;
+  const double Zs = P.Zs, Zp = P.Zp, lam = P.lam, G = P.G;
+  double x = xcell - P.sw_fbc0;
+  double vx1 = Wi[0], vy1 = Wi[1], vz1 = Wi[2], sxx1 = Wi[3], syy1 = Wi[4], szz1 = Wi[5];
+  double sxy1 = Wi[6], sxz1 = Wi[7], syz1 = Wi[8];
+  double vx2 = Wi[off + 0], vy2 = Wi[off + 1], vz2 = Wi[off + 2], sxx2 = Wi[off + 3], syy2 = Wi[off + 4];
+  double szz2 = Wi[off + 5], sxy2 = Wi[off + 6], sxz2 = Wi[off + 7], syz2 = Wi[off + 8];
+  double wpxy1 = -sxy1 - Zs * vx1;
+  double wpyy1 = -syy1 - Zp * vy1;
+  double wpyz1 = -syz1 - Zs * vz1;
+  double wpxy2 = sxy2 - Zs * vx2;
+  double wpyy2 = syy2 - Zp * vy2;
+  double wpyz2 = syz2 - Zs * vz2;
+  double tau_0 = 0;
+  for (int ip = 0; ip < P.sw_np; ++ip) {
+    double valx = smoothfn(P.sw_smooth, fabs(x - P.sw_xc[ip]) - P.sw_xw[ip]);
+    tau_0 = tau_0 + P.sw_tau[ip] * valx;
+  }
+  double a1 = 0.5 * (wpxy2 - wpxy1) + tau_0, a2 = 0.5 * (wpyz2 - wpyz1);
+  double tau_lock = sqrt(a1 * a1 + a2 * a2);
+  syy1 = -(wpyy1 - wpyy2) / 2.0;
+  syy2 = -(wpyy1 - wpyy2) / 2.0;
+  vy1 = -(wpyy1 + wpyy2) / 2.0 / Zp;
+  vy2 = -(wpyy1 + wpyy2) / 2.0 / Zp;
+  double valx = boxcar(P.sw_fbw0, fabs(x));
+  double fric = P.sw_fs * valx + (1 - valx) * P.sw_outside;
+  fric = fric - (fric - P.sw_fd) * fmin(1.0, slip_total / P.sw_dw);
+  double tau = fmin(tau_lock, -syy1 * fric) - tau_0;
+  double phi_xy = 0.5 * (wpxy2 - wpxy1);
+  double phi_yz = 0.5 * (wpyz2 - wpyz1);
+  double phi = sqrt(phi_xy * phi_xy + phi_yz * phi_yz);
+  sxy1 = (phi_xy / phi) * tau;
+  syz1 = (phi_yz / phi) * tau;
+  vx1 = -(sxy1 + wpxy1) / Zs;
+  vz1 = -(syz1 + wpyz1) / Zs;
+  double SHF = -(vy1 - syy1) * lam / (lam + 2.0 * G);
+  Wg[0] = vx1; Wg[1] = vy1; Wg[2] = vz1;
+  Wg[3] = sxx1 + SHF; Wg[4] = syy1; Wg[5] = szz1 + SHF;
+  Wg[6] = sxy1; Wg[7] = sxz1; Wg[8] = syz1;
+  sxy2 = (phi_xy / phi) * tau;
+  syz2 = (phi_yz / phi) * tau;
+  vx2 = (sxy2 - wpxy2) / Zs;
+  vz2 = (syz2 - wpyz2) / Zs;
+  SHF = -(vy2 - syy2) * lam / (lam + 2.0 * G);
+  Wg[off + 0] = vx2; Wg[off + 1] = vy2; Wg[off + 2] = vz2;
+  Wg[off + 3] = sxx2 + SHF; Wg[off + 4] = syy2; Wg[off + 5] = szz2 + SHF;
+  Wg[off + 6] = sxy2; Wg[off + 7] = sxz2; Wg[off + 8] = syz2;
+}
+
+// SWSETBND (ibcLinElast/SWIBCF.ChF:32-72).  Predictor (final_=false): returns the
+// predicted slip_total only.  Final: updates B in place; as in the reference's
+// in-place call the rupture test reads the V just written.
+TMK_D double sw_setbnd(const DevParams& P, const double* U, double* B, int bstride, double dt, double time,
+                       bool final_) {
+  const int off = P.sw_off;
+  double vx = U[0] - U[off + 0];
+  double vz = U[2] - U[off + 2];
+  double V = sqrt((vx * vx + vz * vz));
+  double st = B[7 * bstride] + dt * V;
+  if (final_) {
+    double rt = B[8 * bstride];
+    B[0] = vx;
+    B[1 * bstride] = vz;
+    B[2 * bstride] = U[6];
+    B[3 * bstride] = U[8];
+    B[4 * bstride] = V;
+    B[5 * bstride] = B[5 * bstride] + dt * vx;
+    B[6 * bstride] = B[6 * bstride] + dt * vz;
+    B[7 * bstride] = st;
+    if (rt > time && V > P.sw_thr) B[8 * bstride] = time;
+  }
+  return st;
+}
+
+// PLASTICFLOW (srcLinElast/PlasticPhysicsF.ChF:74-181) on one side's stresses
+template <typename T>
+TMK_D void plastic_flow(const DevParams& P, T& sxx, T& syy, T& szz, T& sxy, T& sxz, T& syz, T& p_lam,
+                        T& p_gam, T dt) {
+  const T mu = (T)P.p_mu, beta = (T)P.p_beta, eta = (T)P.p_eta, pb = (T)P.p_b, ph = (T)P.p_h;
+  const T G = (T)P.G, K = (T)P.K;
+  T sigma = (sxx + syy + szz) / T(3);
+  T J2 = ((sxx - syy) * (sxx - syy) + (syy - szz) * (syy - szz) + (szz - sxx) * (szz - sxx)) / T(6) +
+         sxy * sxy + sxz * sxz + syz * syz;
+  T tau = sqrt(J2);
+  T b = pb + p_gam * ph;
+  T Y = tau - fmax(-mu * sigma + b, T(0));
+  if (Y <= T(0)) { p_lam = T(0); return; }
+  p_lam = Y / (dt * (ph + G + mu * beta * K) + eta);
+  p_gam = p_gam + dt * p_lam;
+  T sig_e = sigma;
+  tau = tau - dt * p_lam * G;
+  sigma = sigma - dt * p_lam * K * beta;
+  T factor = tau / (tau + dt * p_lam * G);
+  sxx = sigma + factor * (sxx - sig_e);
+  syy = sigma + factor * (syy - sig_e);
+  szz = sigma + factor * (szz - sig_e);
+  sxy = factor * sxy;
+  sxz = factor * sxz;
+  syz = factor * syz;
+}
+
+}  // namespace tmk

@@ -1,0 +1,95 @@
+// FP64 instantiation (plain form).  Compiled with --fmad=false so that every
+// product and sum rounds as in the reference's Fortran and the CPU oracle.
+#include "tmk_launch_impl.cuh"
+TMK_INSTANTIATE_LAUNCH(double, 16, 8, 256)
+
+namespace tmk {
+
+__global__ void plastic_fab_kernel(double* U, int alo0, int alo1, int anx, int any, int lo0, int lo1, int hi0,
+                                   int hi1, const DevParams* P, double dt) {
+  const int nx = hi0 - lo0 + 1, ny = hi1 - lo1 + 1;
+  const size_t plane = (size_t)anx * any;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nx * ny; idx += gridDim.x * blockDim.x) {
+    int i = lo0 + idx % nx, j = lo1 + idx / nx;
+    size_t o = (size_t)(j - alo1) * anx + (i - alo0);
+    for (int s = 0; s < 2; ++s) {
+      double* u = U + (size_t)(11 * s) * plane + o;
+      double sxx = u[3 * plane], syy = u[4 * plane], szz = u[5 * plane], sxy = u[6 * plane];
+      double sxz = u[7 * plane], syz = u[8 * plane], lam = u[9 * plane], gam = u[10 * plane];
+      plastic_flow<double>(*P, sxx, syy, szz, sxy, sxz, syz, lam, gam, dt);
+      u[3 * plane] = sxx; u[4 * plane] = syy; u[5 * plane] = szz; u[6 * plane] = sxy;
+      u[7 * plane] = sxz; u[8 * plane] = syz; u[9 * plane] = lam; u[10 * plane] = gam;
+    }
+  }
+}
+
+cudaError_t plastic_fab(double* U, int alo0, int alo1, int anx, int any, int lo0, int lo1, int hi0, int hi1,
+                        const DevParams* P, double dt, cudaStream_t s) {
+  int n = (hi0 - lo0 + 1) * (hi1 - lo1 + 1);
+  if (n <= 0) return cudaSuccess;
+  int blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  plastic_fab_kernel<<<blocks, 256, 0, s>>>(U, alo0, alo1, anx, any, lo0, lo1, hi0, hi1, P, dt);
+  return cudaGetLastError();
+}
+
+__global__ void copy_valid_kernel(const double* src, double* dst, int alo0, int alo1, int anx, int any, int vlo0,
+                                  int vlo1, int vhi0, int vhi1, int c0, int ncomp) {
+  const int nx = vhi0 - vlo0 + 1, ny = vhi1 - vlo1 + 1;
+  const size_t n = (size_t)ncomp * nx * ny;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    int c = c0 + (int)(idx / ((size_t)nx * ny)), j = vlo1 + (int)((idx / nx) % ny), i = vlo0 + (int)(idx % nx);
+    size_t o = ((size_t)c * any + (j - alo1)) * anx + (i - alo0);
+    dst[o] = src[o];
+  }
+}
+
+cudaError_t copy_valid(const double* src, double* dst, int alo0, int alo1, int anx, int any, int vlo0, int vlo1,
+                       int vhi0, int vhi1, int c0, int ncomp, cudaStream_t s) {
+  size_t n = (size_t)ncomp * (vhi0 - vlo0 + 1) * (vhi1 - vlo1 + 1);
+  if (n == 0) return cudaSuccess;
+  size_t blocks = (n + 255) / 256;
+  if (blocks > 8192) blocks = 8192;
+  copy_valid_kernel<<<(unsigned)blocks, 256, 0, s>>>(src, dst, alo0, alo1, anx, any, vlo0, vlo1, vhi0, vhi1, c0, ncomp);
+  return cudaGetLastError();
+}
+
+__global__ void d2f_kernel(const double* a, float* b, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+__global__ void f2d_kernel(const float* a, double* b, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+cudaError_t convert_d2f(const double* src, float* dst, size_t n, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  d2f_kernel<<<(unsigned)((n + 255) / 256 > 8192 ? 8192 : (n + 255) / 256), 256, 0, s>>>(src, dst, n);
+  return cudaGetLastError();
+}
+cudaError_t convert_f2d(const float* src, double* dst, size_t n, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  f2d_kernel<<<(unsigned)((n + 255) / 256 > 8192 ? 8192 : (n + 255) / 256), 256, 0, s>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
+// Fault-row exchange: copy boundary data faces [lo0, hi0] from src to dst patch.
+__global__ void bexchange_kernel(double* const* __restrict__ bptr, const int* __restrict__ blo,
+                                 const int* __restrict__ bnx, const CopyDev* __restrict__ copies, int nb) {
+  const CopyDev cp = copies[blockIdx.x];
+  const int n = cp.hi0 - cp.lo0 + 1;
+  for (int idx = threadIdx.x; idx < nb * n; idx += blockDim.x) {
+    int c = idx / n, i = cp.lo0 + idx % n;
+    bptr[cp.dst][(size_t)c * bnx[cp.dst] + (i - blo[cp.dst])] = bptr[cp.src][(size_t)c * bnx[cp.src] + (i - blo[cp.src])];
+  }
+}
+
+
+cudaError_t bexchange(double* const* bptr, const int* blo, const int* bnx, const CopyDev* copies, int ncopies,
+                      int nb, cudaStream_t s) {
+  if (ncopies <= 0) return cudaSuccess;
+  bexchange_kernel<<<ncopies, 128, 0, s>>>(bptr, blo, bnx, copies, nb);
+  return cudaGetLastError();
+}
+
+}  // namespace tmk

@@ -1,0 +1,435 @@
+// tmk_kernels.cuh -- the device kernels of one level step, templated on the
+// volume arithmetic type Real (double: plain FP64 form; float: mixed form).
+//
+//   fault_kernel   one thread per fault face (a warp per 32-face segment):
+//                  predicts the two states that meet at the fault (rows 0-2 of
+//                  the patch), runs the first-pass friction solve, the
+//                  half-step state predictor, the transverse-corrected final
+//                  solve and the boundary-data update, all friction work in FP64
+//                  (LinElastPatchGodunov::computeWHalf call order,
+//                  srcLinElast/LinElastPatchGodunov.cpp:289-452).
+//   volume_kernel  one CTA per (tile, side): PPM normal predictors in x and y,
+//                  first-pass Riemann, transverse corrections, final Riemann,
+//                  fluxes and the conservative update (and, with plasticity,
+//                  the Drucker-Prager return) of a TX x TY tile, every stage
+//                  in shared memory; the fault faces come from fault_kernel.
+//   exchange_kernel  same-level ghost copy between patches (LevelData::exchange).
+#pragma once
+#include "tmk_device.cuh"
+#include "tmk_fault.cuh"
+
+namespace tmk {
+
+// One patch of a level on the device.
+template <typename Real>
+struct PatchDev {
+  const Real* Uin;          // FAB over the allocated box, 22 component planes
+  Real* Uout;
+  int alo0, alo1, anx, any; // allocated box lo and extents
+  int vlo0, vlo1, vhi0, vhi1;
+  int dlo0, dlo1, dhi0, dhi1;
+  double dx, dt;
+  int scen;
+  int plastic;              // apply the Drucker-Prager return after the update
+  int fault;                // patch touches the y-lo fault
+  double* B;                // fault FAB: nb planes over x in [blo0, blo0+bnx)
+  int blo0, bnx;
+  double* first;            // first-pass fault states, 22 x nfirst, faces [vlo0-1, vhi0+1]
+  double* ffault;           // final fault-face fluxes, 22 x (vhi0-vlo0+1)
+  int nfirst;
+  Real* Fx;                 // optional reflux fluxes (22 comps over x faces of valid)
+  Real* Fy;
+};
+
+struct TileDev { int patch, x0, y0, nx, ny; };
+
+template <typename Real>
+TMK_D size_t fab_idx(const PatchDev<Real>& p, int c, int i, int j) {
+  return ((size_t)c * (size_t)p.any + (size_t)(j - p.alo1)) * (size_t)p.anx + (size_t)(i - p.alo0);
+}
+
+TMK_D void side_bg(const DevParams& P, int s, double* bg) {
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) bg[c] = P.bg[11 * s + c];
+}
+
+template <typename T>
+TMK_D void make_sig(const DevParams& P, double dtbydx, T* sig) {
+  const double l[9] = {-P.cp, -P.cs, -P.cs, 0.0, 0.0, 0.0, P.cs, P.cs, P.cp};
+#pragma unroll
+  for (int c = 0; c < 9; ++c) sig[c] = (T)(l[c] * dtbydx);
+}
+
+// =============================================================== fault kernel
+// Predicted state of one side's 11 components at (i, j0) in y, in arithmetic T
+// (lambda, gamma carry only their limited PPM delta: zero characteristic speed).
+template <typename Real, typename T>
+TMK_D void fault_ypred_side(const PatchDev<Real>& p, const DevParams& P, const Consts<T>& k, int s, int i,
+                            const T* sig, bool lim, double* out11) {
+  const int j0 = p.dlo1;
+  bool in[5] = {false, false, true, j0 + 1 <= p.dhi1, j0 + 2 <= p.dhi1};
+  T w5[NSIDE][5];
+  for (int c = 0; c < NSIDE; ++c)
+    for (int m = 0; m < 5; ++m) w5[c][m] = in[m] ? (T)p.Uin[fab_idx(p, 11 * s + c, i, j0 - 2 + m)] : T(0);
+  T WM[NSIDE], WP[NSIDE];
+  T rv = (s == 1) ? T(-1) : T(1);
+  ppm_predict<1, T>(k, rv, w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM, WP, P.order);
+  for (int c = 0; c < NSIDE; ++c) out11[c] = (double)WM[c];
+  for (int c = 9; c < 11; ++c) {
+    T w[5];
+    for (int m = 0; m < 5; ++m) w[m] = in[m] ? (T)p.Uin[fab_idx(p, 11 * s + c, i, j0 - 2 + m)] : T(0);
+    if (P.order == 0) { out11[c] = (double)w[2]; continue; }
+    T dm, dp;
+    ppm_deltas(w, in, lim, dm, dp);
+    if (lim) ppm_limit(dm, dp);
+    out11[c] = (double)(dm + w[2]);
+  }
+}
+
+// x-direction predicted states (WM, WP) of one side at cell (i, j0)
+template <typename Real, typename T>
+TMK_D void fault_xpred_side(const PatchDev<Real>& p, const DevParams& P, const Consts<T>& k, int s, int i,
+                            const T* sig, T* WM, T* WP) {
+  const int j0 = p.dlo1;
+  bool in[5];
+  for (int m = 0; m < 5; ++m) in[m] = (i - 2 + m >= p.dlo0) && (i - 2 + m <= p.dhi0);
+  T w5[NSIDE][5];
+  for (int c = 0; c < NSIDE; ++c)
+    for (int m = 0; m < 5; ++m) w5[c][m] = in[m] ? (T)p.Uin[fab_idx(p, 11 * s + c, i - 2 + m, j0)] : T(0);
+  ppm_predict<0, T>(k, T(1), w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM, WP, P.order);
+}
+
+// x face state (first pass) of one side at face f of row j0 from the cells
+// f-1 and f, or the domain-edge condition.
+template <typename T>
+TMK_D void xface_state(const DevParams& P, const Consts<T>& k, int f, int dlo0, int dhi0, const T* WPl,
+                       const T* WMr, const T* bg, T* g) {
+  if (f == dlo0) edge_bc<0, T>(k, T(1), -1, P.bc[0] == 0, bg, WMr, g);
+  else if (f == dhi0 + 1) edge_bc<0, T>(k, T(1), +1, P.bc[1] == 0, bg, WPl, g);
+  else riemann<0, T>(k, T(1), WPl, WMr, g);
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(128) fault_kernel(const PatchDev<Real>* __restrict__ patches,
+                                                    const int* __restrict__ fault_patches,
+                                                    const DevParams* __restrict__ params, double time,
+                                                    DevStatus* st) {
+  using T = Real;
+  const PatchDev<Real> p = patches[fault_patches[blockIdx.y]];
+  const DevParams& P = params[p.scen];
+  const int i = p.vlo0 - 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > p.vhi0 + 1 || i < p.dlo0 || i > p.dhi0) return;
+  Consts<T> k; k.load(P);
+  const double dt = p.dt, dx = p.dx;
+  T sigy[9], sigx[9];
+  make_sig(P, dt / dx, sigy);
+  make_sig(P, dt / dx, sigx);
+  const bool lim = P.prim_lim || P.char_lim;
+  const int bs = p.bnx;
+  double* Bi = p.B + (i - p.blo0);
+
+  // (1) predicted states entering the fault from both sides
+  double Wi[NC];
+  fault_ypred_side(p, P, k, 0, i, sigy, lim, Wi);
+  fault_ypred_side(p, P, k, 1, i, sigy, lim, Wi + 11);
+
+  // (2) first-pass friction solve with the persistent boundary data
+  const double xc = (i + 0.5) * dx;
+  double Wg[NC];
+  for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
+  int it = 0;
+  if (P.fault_law == 1) it = rs_fault(P, Wi, Bi[10 * bs], xc - P.rs_x0, Wg);
+  else sw_fault(P, Wi, Bi[7 * bs], xc, Wg);
+  if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
+  double* first = p.first + (i - (p.vlo0 - 1));
+  for (int c = 0; c < NC; ++c) first[c * p.nfirst] = Wg[c];
+
+  if (i < p.vlo0 || i > p.vhi0) return;
+
+  // (3) half-step predicted boundary data (RSIBC/SWIBC::updateBoundary, final=false)
+  double tmpv;
+  if (P.fault_law == 1) tmpv = rs_setbnd(P, Wg, Bi, bs, 0.5 * dt, xc - P.rs_x0, 0.0, false);
+  else tmpv = sw_setbnd(P, Wg, Bi, bs, 0.5 * dt, 0.0, false);
+
+  // (4) transverse correction of the predicted fault states by the x fluxes of row j0
+  const double scale = -(1.0 / 2.0) * dt / dx;
+  for (int s = 0; s < 2; ++s) {
+    double bgd[NSIDE]; side_bg(P, s, bgd);
+    T bg[NSIDE];
+    for (int c = 0; c < NSIDE; ++c) bg[c] = (T)bgd[c];
+    T WMl[NSIDE], WPl[NSIDE], WMc[NSIDE], WPc[NSIDE], WMr[NSIDE], WPr[NSIDE];
+    if (i - 1 >= p.dlo0) fault_xpred_side(p, P, k, s, i - 1, sigx, WMl, WPl);
+    fault_xpred_side(p, P, k, s, i, sigx, WMc, WPc);
+    if (i + 1 <= p.dhi0) fault_xpred_side(p, P, k, s, i + 1, sigx, WMr, WPr);
+    T glo[NSIDE], ghi[NSIDE];
+    xface_state<T>(P, k, i, p.dlo0, p.dhi0, WPl, WMc, bg, glo);
+    xface_state<T>(P, k, i + 1, p.dlo0, p.dhi0, WPc, WMr, bg, ghi);
+    T q[NSIDE];
+    for (int c = 0; c < NSIDE; ++c) q[c] = (T)Wi[11 * s + c];
+    adwdx_add<0, T>(k, T(1), (T)scale, ghi, glo, q);
+    for (int c = 0; c < NSIDE; ++c) Wi[11 * s + c] = (double)q[c];
+  }
+
+  // (5) final friction solve with the predicted boundary data
+  for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
+  it = 0;
+  if (P.fault_law == 1) it = rs_fault(P, Wi, tmpv, xc - P.rs_x0, Wg);
+  else sw_fault(P, Wi, tmpv, xc, Wg);
+  if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
+
+  // (6) y fluxes through the fault face (GETFLUXF, FP64)
+  Consts<double> kd; kd.load(P);
+  double F[NSIDE];
+  double* ff = p.ffault + (i - p.vlo0);
+  const int nv = p.vhi0 - p.vlo0 + 1;
+  flux<1, double>(kd, 1.0, Wg, F);
+  for (int c = 0; c < NSIDE; ++c) ff[c * nv] = F[c];
+  flux<1, double>(kd, -1.0, Wg + 11, F);
+  for (int c = 0; c < NSIDE; ++c) ff[(11 + c) * nv] = F[c];
+
+  // (7) boundary-data update with the final fault state (final=true, t+dt)
+  if (P.fault_law == 1) {
+    double np = rs_setbnd(P, Wg, Bi, bs, dt, xc - P.rs_x0, time + dt, true);
+    if (isnan(np)) report(st, ST_NAN, (long long)i);
+  } else {
+    sw_setbnd(P, Wg, Bi, bs, dt, time + dt, true);
+  }
+}
+
+// ============================================================== volume kernel
+template <typename Real, int TX, int TY>
+struct VolSmem {
+  static constexpr int RX = TX + 6, RY = TY + 6, PX = TX + 2, PY = TY + 2;
+  Real W[NSIDE][RY][RX];
+  Real WMx[NSIDE][PY][PX], WPx[NSIDE][PY][PX];
+  Real WMy[NSIDE][PY][PX], WPy[NSIDE][PY][PX];
+  Real H1x[NSIDE][PY][TX + 1];
+  Real H1y[NSIDE][TY + 1][PX];
+  Real Fx[NSIDE][TY][TX + 1];
+  Real Fy[NSIDE][TY + 1][TX];
+};
+
+template <typename Real, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __restrict__ patches,
+                                                    const TileDev* __restrict__ tiles,
+                                                    const DevParams* __restrict__ params) {
+  using T = Real;
+  using S = VolSmem<Real, TX, TY>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  S& sm = *reinterpret_cast<S*>(smem_raw);
+  const TileDev tl = tiles[blockIdx.x];
+  const int s = blockIdx.y;                // side
+  const PatchDev<Real>& pp = patches[tl.patch];
+  const PatchDev<Real> p = pp;
+  const DevParams& P = params[p.scen];
+  Consts<T> k; k.load(P);
+  const T rvy = (s == 1) ? T(-1) : T(1);
+  const int x0 = tl.x0, y0 = tl.y0, tnx = tl.nx, tny = tl.ny;
+  const double dt = p.dt, dx = p.dx;
+  const bool plim = P.prim_lim != 0, clim = P.char_lim != 0;
+  T sig[9]; make_sig(P, dt / dx, sig);
+  const T scale = (T)(-(1.0 / 2.0) * dt / dx);
+  const T sc = (T)(-dt / dx);
+  double bgd[NSIDE]; side_bg(P, s, bgd);
+  T bg[NSIDE];
+  for (int c = 0; c < NSIDE; ++c) bg[c] = (T)bgd[c];
+  const bool outx_lo = P.bc[0] == 0, outx_hi = P.bc[1] == 0;
+  const bool outy_lo = P.bc[2] == 0, outy_hi = P.bc[3] == 0;
+
+  // ---- load W over [x0-3, x0+TX+2] x [y0-3, y0+TY+2]
+  for (int idx = threadIdx.x; idx < NSIDE * S::RY * S::RX; idx += NT) {
+    int c = idx / (S::RY * S::RX), r = (idx / S::RX) % S::RY, q = idx % S::RX;
+    int x = x0 - 3 + q, y = y0 - 3 + r;
+    T v = T(0);
+    if (x >= p.dlo0 && x <= p.dhi0 && y >= p.dlo1 && y <= p.dhi1 && q < tnx + 6 && r < tny + 6)
+      v = p.Uin[fab_idx(p, 11 * s + c, x, y)];
+    sm.W[c][r][q] = v;
+  }
+  __syncthreads();
+
+  // ---- normal predictors on cells [x0-1, x0+nx] x [y0-1, y0+ny]
+  for (int idx = threadIdx.x; idx < (tny + 2) * (tnx + 2); idx += NT) {
+    int py = idx / (tnx + 2), px = idx % (tnx + 2);
+    int x = x0 - 1 + px, y = y0 - 1 + py;
+    if (x < p.dlo0 || x > p.dhi0 || y < p.dlo1 || y > p.dhi1) continue;
+    T w5[NSIDE][5], WM[NSIDE], WP[NSIDE];
+    bool in[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) in[m] = (x - 2 + m >= p.dlo0) && (x - 2 + m <= p.dhi0);
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c)
+#pragma unroll
+      for (int m = 0; m < 5; ++m) w5[c][m] = sm.W[c][py + 2][px + m];
+    ppm_predict<0, T>(k, T(1), w5, in, plim, clim, sig, WM, WP, P.order);
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) { sm.WMx[c][py][px] = WM[c]; sm.WPx[c][py][px] = WP[c]; }
+#pragma unroll
+    for (int m = 0; m < 5; ++m) in[m] = (y - 2 + m >= p.dlo1) && (y - 2 + m <= p.dhi1);
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c)
+#pragma unroll
+      for (int m = 0; m < 5; ++m) w5[c][m] = sm.W[c][py + m][px + 2];
+    ppm_predict<1, T>(k, rvy, w5, in, plim, clim, sig, WM, WP, P.order);
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) { sm.WMy[c][py][px] = WM[c]; sm.WPy[c][py][px] = WP[c]; }
+  }
+  __syncthreads();
+
+  // ---- first-pass Riemann: x faces [x0, x0+nx] on rows [y0-1, y0+ny]
+  for (int idx = threadIdx.x; idx < (tny + 2) * (tnx + 1); idx += NT) {
+    int ry = idx / (tnx + 1), fi = idx % (tnx + 1);
+    int f = x0 + fi, y = y0 - 1 + ry;
+    if (y < p.dlo1 || y > p.dhi1) continue;
+    T L[NSIDE], R[NSIDE], g[NSIDE];
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) { L[c] = sm.WPx[c][ry][fi]; R[c] = sm.WMx[c][ry][fi + 1]; }
+    if (f == p.dlo0) edge_bc<0, T>(k, T(1), -1, outx_lo, bg, R, g);
+    else if (f == p.dhi0 + 1) edge_bc<0, T>(k, T(1), +1, outx_hi, bg, L, g);
+    else riemann<0, T>(k, T(1), L, R, g);
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) sm.H1x[c][ry][fi] = g[c];
+  }
+  //      y faces [y0, y0+ny] on columns [x0-1, x0+nx]
+  for (int idx = threadIdx.x; idx < (tny + 1) * (tnx + 2); idx += NT) {
+    int gi = idx / (tnx + 2), cx = idx % (tnx + 2);
+    int gf = y0 + gi, x = x0 - 1 + cx;
+    if (x < p.dlo0 || x > p.dhi0) continue;
+    T g[NSIDE];
+    if (gf == p.dlo1 && p.fault) {
+      const double* fs = p.first + (x - (p.vlo0 - 1)) + (size_t)(11 * s) * p.nfirst;
+#pragma unroll
+      for (int c = 0; c < NSIDE; ++c) g[c] = (T)fs[c * p.nfirst];
+    } else {
+      T L[NSIDE], R[NSIDE];
+#pragma unroll
+      for (int c = 0; c < NSIDE; ++c) { L[c] = sm.WPy[c][gi][cx]; R[c] = sm.WMy[c][gi + 1][cx]; }
+      if (gf == p.dlo1) edge_bc<1, T>(k, rvy, -1, outy_lo, bg, R, g);
+      else if (gf == p.dhi1 + 1) edge_bc<1, T>(k, rvy, +1, outy_hi, bg, L, g);
+      else riemann<1, T>(k, rvy, L, R, g);
+    }
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) sm.H1y[c][gi][cx] = g[c];
+  }
+  __syncthreads();
+
+  // ---- transverse corrections (quasilinearUpdate with -(1/2) dt/dx)
+  for (int idx = threadIdx.x; idx < tny * (tnx + 2); idx += NT) {
+    int ry = idx / (tnx + 2), px = idx % (tnx + 2);
+    int x = x0 - 1 + px;
+    if (x < p.dlo0 || x > p.dhi0) continue;
+    T h[NSIDE], l[NSIDE], a[NSIDE];
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) { h[c] = sm.H1y[c][ry + 1][px]; l[c] = sm.H1y[c][ry][px]; a[c] = T(0); }
+    adwdx_add<1, T>(k, rvy, scale, h, l, a);
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) { sm.WMx[c][ry + 1][px] += a[c]; sm.WPx[c][ry + 1][px] += a[c]; }
+  }
+  for (int idx = threadIdx.x; idx < (tny + 2) * tnx; idx += NT) {
+    int py = idx / tnx, cx = idx % tnx;
+    int y = y0 - 1 + py;
+    if (y < p.dlo1 || y > p.dhi1) continue;
+    T h[NSIDE], l[NSIDE], a[NSIDE];
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) { h[c] = sm.H1x[c][py][cx + 1]; l[c] = sm.H1x[c][py][cx]; a[c] = T(0); }
+    adwdx_add<0, T>(k, T(1), scale, h, l, a);
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) { sm.WMy[c][py][cx + 1] += a[c]; sm.WPy[c][py][cx + 1] += a[c]; }
+  }
+  __syncthreads();
+
+  // ---- final Riemann + fluxes: x faces [x0, x0+nx] on rows [y0, y0+ny-1]
+  for (int idx = threadIdx.x; idx < tny * (tnx + 1); idx += NT) {
+    int ry = idx / (tnx + 1), fi = idx % (tnx + 1);
+    int f = x0 + fi;
+    T L[NSIDE], R[NSIDE], g[NSIDE], F[NSIDE];
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) { L[c] = sm.WPx[c][ry + 1][fi]; R[c] = sm.WMx[c][ry + 1][fi + 1]; }
+    if (f == p.dlo0) edge_bc<0, T>(k, T(1), -1, outx_lo, bg, R, g);
+    else if (f == p.dhi0 + 1) edge_bc<0, T>(k, T(1), +1, outx_hi, bg, L, g);
+    else riemann<0, T>(k, T(1), L, R, g);
+    flux<0, T>(k, T(1), g, F);
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) sm.Fx[c][ry][fi] = F[c];
+  }
+  //      y faces [y0, y0+ny] on columns [x0, x0+nx-1]
+  for (int idx = threadIdx.x; idx < (tny + 1) * tnx; idx += NT) {
+    int gi = idx / tnx, cx = idx % tnx;
+    int gf = y0 + gi, x = x0 + cx;
+    T F[NSIDE];
+    if (gf == p.dlo1 && p.fault) {
+      const int nv = p.vhi0 - p.vlo0 + 1;
+      const double* ff = p.ffault + (x - p.vlo0) + (size_t)(11 * s) * nv;
+#pragma unroll
+      for (int c = 0; c < NSIDE; ++c) F[c] = (T)ff[c * nv];
+    } else {
+      T L[NSIDE], R[NSIDE], g[NSIDE];
+#pragma unroll
+      for (int c = 0; c < NSIDE; ++c) { L[c] = sm.WPy[c][gi][cx + 1]; R[c] = sm.WMy[c][gi + 1][cx + 1]; }
+      if (gf == p.dlo1) edge_bc<1, T>(k, rvy, -1, outy_lo, bg, R, g);
+      else if (gf == p.dhi1 + 1) edge_bc<1, T>(k, rvy, +1, outy_hi, bg, L, g);
+      else riemann<1, T>(k, rvy, L, R, g);
+      flux<1, T>(k, rvy, g, F);
+    }
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) sm.Fy[c][gi][cx] = F[c];
+  }
+  __syncthreads();
+
+  // ---- conservative update (LinElastPhysics::computeUpdate) + plasticity
+  for (int idx = threadIdx.x; idx < tny * tnx; idx += NT) {
+    int ry = idx / tnx, cx = idx % tnx;
+    int x = x0 + cx, y = y0 + ry;
+    T u[NSIDE];
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) {
+      T du = (sm.Fx[c][ry][cx + 1] - sm.Fx[c][ry][cx]) + (sm.Fy[c][ry + 1][cx] - sm.Fy[c][ry][cx]);
+      u[c] = sm.W[c][ry + 3][cx + 3] + du * sc;
+    }
+    if (p.plastic) {
+      T lam = p.Uin[fab_idx(p, 11 * s + 9, x, y)];
+      T gam = p.Uin[fab_idx(p, 11 * s + 10, x, y)];
+      plastic_flow<T>(P, u[3], u[4], u[5], u[6], u[7], u[8], lam, gam, (T)dt);
+      p.Uout[fab_idx(p, 11 * s + 9, x, y)] = lam;
+      p.Uout[fab_idx(p, 11 * s + 10, x, y)] = gam;
+    }
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) p.Uout[fab_idx(p, 11 * s + c, x, y)] = u[c];
+  }
+  if (p.Fx) {
+    const int nvx = p.vhi0 - p.vlo0 + 2, nvy = p.vhi1 - p.vlo1 + 1;
+    for (int idx = threadIdx.x; idx < NSIDE * tny * (tnx + 1); idx += NT) {
+      int c = idx / (tny * (tnx + 1)), ry = (idx / (tnx + 1)) % tny, fi = idx % (tnx + 1);
+      size_t o = ((size_t)(11 * s + c) * nvy + (y0 + ry - p.vlo1)) * nvx + (x0 + fi - p.vlo0);
+      p.Fx[o] = sm.Fx[c][ry][fi];
+    }
+  }
+  if (p.Fy) {
+    const int nvx = p.vhi0 - p.vlo0 + 1, nvy = p.vhi1 - p.vlo1 + 2;
+    for (int idx = threadIdx.x; idx < NSIDE * (tny + 1) * tnx; idx += NT) {
+      int c = idx / ((tny + 1) * tnx), gi = (idx / tnx) % (tny + 1), cx = idx % tnx;
+      size_t o = ((size_t)(11 * s + c) * nvy + (y0 + gi - p.vlo1)) * nvx + (x0 + cx - p.vlo0);
+      p.Fy[o] = sm.Fy[c][gi][cx];
+    }
+  }
+}
+
+// =============================================================== exchange
+// Copy `ncomp` planes (first component c0) of box [lo, hi] from src to dst.
+struct CopyDev { int src, dst; int lo0, lo1, hi0, hi1; };
+
+template <typename Real>
+__global__ void exchange_kernel(const PatchDev<Real>* __restrict__ patches, const CopyDev* __restrict__ copies,
+                                int c0, int ncomp, int to_in) {
+  const CopyDev cp = copies[blockIdx.x];
+  const PatchDev<Real>& ps = patches[cp.src];
+  const PatchDev<Real>& pd = patches[cp.dst];
+  const int nx = cp.hi0 - cp.lo0 + 1, ny = cp.hi1 - cp.lo1 + 1;
+  const Real* src = to_in ? ps.Uout : ps.Uin;
+  Real* dst = to_in ? (Real*)pd.Uout : (Real*)pd.Uin;
+  for (int idx = threadIdx.x; idx < ncomp * nx * ny; idx += blockDim.x) {
+    int c = c0 + idx / (nx * ny), j = cp.lo1 + (idx / nx) % ny, i = cp.lo0 + idx % nx;
+    dst[fab_idx(pd, c, i, j)] = src[fab_idx(ps, c, i, j)];
+  }
+}
+
+}  // namespace tmk

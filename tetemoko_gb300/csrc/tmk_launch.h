@@ -1,0 +1,41 @@
+// tmk_launch.h -- launch wrappers, instantiated once per volume arithmetic type
+// (tmk_fp64.cu is compiled without FMA contraction for the parity form,
+// tmk_fp32.cu with it for the mixed form).
+#pragma once
+#include <cuda_runtime.h>
+#include "tmk_device.cuh"
+
+namespace tmk {
+
+template <typename Real> struct PatchDev;
+struct TileDev;
+struct CopyDev;
+
+template <typename Real>
+struct Launch {
+  static const int TX, TY;
+  // one thread per fault face of every fault patch
+  static cudaError_t fault(const PatchDev<Real>* patches, const int* fault_patches, int nfault, int max_faces,
+                           const DevParams* params, double time, DevStatus* st, cudaStream_t s);
+  // one CTA per (tile, side)
+  static cudaError_t volume(const PatchDev<Real>* patches, const TileDev* tiles, int ntiles,
+                            const DevParams* params, cudaStream_t s);
+  // same-level ghost exchange of components [c0, c0+ncomp) into the input buffers
+  static cudaError_t exchange(const PatchDev<Real>* patches, const CopyDev* copies, int ncopies, int c0,
+                              int ncomp, cudaStream_t s);
+  static size_t volume_smem();
+};
+
+// FP64 <-> Real conversion of a FAB on the device
+cudaError_t convert_d2f(const double* src, float* dst, size_t n, cudaStream_t s);
+cudaError_t convert_f2d(const float* src, double* dst, size_t n, cudaStream_t s);
+// copy components [c0, c0+ncomp) of the valid box of a FAB into another FAB of the same shape
+cudaError_t copy_valid(const double* src, double* dst, int alo0, int alo1, int anx, int any, int vlo0, int vlo1,
+                       int vhi0, int vhi1, int c0, int ncomp, cudaStream_t s);
+cudaError_t bexchange(double* const* bptr, const int* blo, const int* bnx, const CopyDev* copies, int ncopies,
+                      int nb, cudaStream_t s);
+// PLASTICCORRECTION over a box of an FP64 FAB
+cudaError_t plastic_fab(double* U, int alo0, int alo1, int anx, int any, int lo0, int lo1, int hi0, int hi1,
+                        const DevParams* P, double dt, cudaStream_t s);
+
+}  // namespace tmk

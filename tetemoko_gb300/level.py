@@ -1,0 +1,239 @@
+"""Host-side mirror of tetemoko's level/patch interfaces over the C ABI.
+
+Names and argument meaning follow the reference:
+  * LinElastPatchGodunov.update_state  -> LinElastPatchGodunov::updateState
+    (srcLinElast/LinElastPatchGodunov.cpp:101-129) on device FABs;
+  * LinElastPatchGodunov.plastic_update -> LinElastPhysics::plasticUpdate;
+  * LinElastLevelGodunov.step / plastic_update -> LinElastLevelGodunov::step /
+    plasticUpdate (srcLinElast/LinElastLevelGodunov.cpp:174-398, 643-667) on a
+    device-resident level.
+Device memory and streams come from PyTorch; every computation runs in the
+CUDA library (libtetemoko_gb300.so) and fails loudly when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi as A
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        torch = _torch()
+        return torch.cuda.current_stream().cuda_stream
+    return int(stream.cuda_stream) if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class Context:
+    """Per-scenario parameters on the device (replaces the COMMON blocks)."""
+
+    def __init__(self, sc):
+        self.sc = sc
+        self.lib = A.lib()
+        h = C.c_void_p()
+        rs = C.byref(sc.rs) if sc.rs is not None else None
+        sw = C.byref(sc.sw) if sc.sw is not None else None
+        pl = C.byref(sc.plastic) if sc.plastic is not None else None
+        A.check(self.lib.tmk_context_create(C.byref(sc.elastic), C.byref(sc.scheme), rs, sw, pl, C.byref(h)),
+                "tmk_context_create")
+        self.h = h
+
+    def constants(self) -> dict:
+        out = (C.c_double * 5)()
+        A.check(self.lib.tmk_context_constants(self.h, out), "tmk_context_constants")
+        return dict(rho=out[0], lam=out[1], K=out[2], Zs=out[3], Zp=out[4])
+
+    def close(self):
+        if self.h:
+            self.lib.tmk_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _fab(t, lo0, lo1) -> A.Fab:
+    """tmk_fab over a (ncomp, ny, nx) float64 CUDA tensor whose cell (0,0) is (lo0, lo1)."""
+    assert t.dtype == _torch().float64 and t.is_cuda and t.is_contiguous()
+    f = A.Fab()
+    f.data = t.data_ptr()
+    f.lo[0], f.lo[1] = lo0, lo1
+    f.hi[0], f.hi[1] = lo0 + t.shape[-1] - 1, lo1 + t.shape[-2] - 1
+    f.ncomp = t.shape[0]
+    return f
+
+
+class LinElastPatchGodunov:
+    """Patch integrator on caller-owned device FABs (FP64)."""
+
+    def __init__(self, ctx: Context, domain=None, dx: float | None = None):
+        self.ctx = ctx
+        sc = ctx.sc
+        self.domain = domain or (0, 0, sc.nx - 1, sc.ny - 1)
+        self.dx = sc.dx if dx is None else dx
+        self.time = 0.0
+        self.box = None
+
+    def set_current_time(self, t: float):
+        self.time = t
+
+    def set_current_box(self, box):
+        self.box = tuple(box)
+
+    def update_state(self, U, ulo, dt: float, B=None, bxlo: int = 0, with_flux: bool = False, stream=None):
+        """Advance the valid box of U (ncomp=22, FP64 CUDA tensor whose first
+        cell is `ulo`) by dt; B (fault row, cells from bxlo) updated in place.
+        Returns (max_wave_speed, Fx, Fy)."""
+        torch = _torch()
+        v = A.box(*self.box)
+        d = A.box(*self.domain)
+        Uf = _fab(U, *ulo)
+        Bf = None
+        if B is not None:
+            Bf = A.Fab()
+            Bf.data = B.data_ptr()
+            Bf.lo[0], Bf.lo[1] = bxlo, self.domain[1]
+            Bf.hi[0], Bf.hi[1] = bxlo + B.shape[-1] - 1, self.domain[1]
+            Bf.ncomp = B.shape[0]
+        Fx = Fy = None
+        Fxf = Fyf = None
+        if with_flux:
+            nx = self.box[2] - self.box[0] + 1
+            ny = self.box[3] - self.box[1] + 1
+            Fx = torch.empty((22, ny, nx + 1), dtype=torch.float64, device=U.device)
+            Fy = torch.empty((22, ny + 1, nx), dtype=torch.float64, device=U.device)
+            Fxf = _fab(Fx, self.box[0], self.box[1])
+            Fyf = _fab(Fy, self.box[0], self.box[1])
+        mws = C.c_double(0.0)
+        A.check(self.ctx.lib.tmk_patch_update_state(
+            self.ctx.h, C.byref(Uf), C.byref(Bf) if Bf is not None else None,
+            C.byref(Fxf) if Fxf is not None else None, C.byref(Fyf) if Fyf is not None else None,
+            C.byref(v), C.byref(d), self.dx, self.time, dt, C.byref(mws), _stream_ptr(stream)),
+            "tmk_patch_update_state")
+        return mws.value, Fx, Fy
+
+    def plastic_update(self, U, ulo, dt: float, box=None, stream=None):
+        b = A.box(*(box or self.box))
+        A.check(self.ctx.lib.tmk_plastic_update(self.ctx.h, C.byref(_fab(U, *ulo)), C.byref(b), dt,
+                                                _stream_ptr(stream)), "tmk_plastic_update")
+
+
+class LinElastLevelGodunov:
+    """Device-resident single level (all patches of the level in one launch)."""
+
+    def __init__(self, ctx: Context, boxes, domain=None, dx: float | None = None):
+        self.ctx = ctx
+        sc = ctx.sc
+        self.boxes = [tuple(b) for b in boxes]
+        self.domain = domain or (0, 0, sc.nx - 1, sc.ny - 1)
+        self.dx = sc.dx if dx is None else dx
+        self.lib = ctx.lib
+        arr = (A.Box * len(self.boxes))(*[A.box(*b) for b in self.boxes])
+        h = C.c_void_p()
+        A.check(self.lib.tmk_level_create(ctx.h, C.byref(A.box(*self.domain)), self.dx, len(self.boxes), arr,
+                                          C.byref(h)), "tmk_level_create")
+        self.h = h
+
+    def patch_shapes(self, p):
+        b = self.boxes[p]
+        g = A.TMK_NGHOST
+        ushape = (22, b[3] - b[1] + 1 + 2 * g, b[2] - b[0] + 1 + 2 * g)
+        bshape = (self.ctx.sc.nbdry, b[2] - b[0] + 1 + 2 * g)
+        return ushape, bshape
+
+    def touches_fault(self, p) -> bool:
+        return self.ctx.sc.scheme.fault_law != A.TMK_FAULT_NONE and self.boxes[p][1] == self.domain[1]
+
+    def set_patch(self, p, U, B=None):
+        """U: (22, ny+8, nx+8) float64 over the patch grown by 4 ghosts; numpy
+        (host) or CUDA tensor (device)."""
+        host = isinstance(U, np.ndarray)
+        if host:
+            U = np.ascontiguousarray(U, dtype=np.float64)
+            Bp = np.ascontiguousarray(B, dtype=np.float64) if B is not None else None
+            A.check(self.lib.tmk_level_set_patch(self.h, p, U.ctypes.data, Bp.ctypes.data if Bp is not None else None,
+                                                 1), "tmk_level_set_patch")
+        else:
+            A.check(self.lib.tmk_level_set_patch(self.h, p, U.data_ptr(), B.data_ptr() if B is not None else None,
+                                                 0), "tmk_level_set_patch")
+
+    def get_patch(self, p, U=None, B=None):
+        """Copy out one patch (into numpy arrays allocated here if not given)."""
+        ushape, bshape = self.patch_shapes(p)
+        if U is None:
+            U = np.empty(ushape)
+        if B is None and self.touches_fault(p):
+            B = np.empty(bshape)
+        host = isinstance(U, np.ndarray)
+        uptr = U.ctypes.data if host else U.data_ptr()
+        bptr = None
+        if B is not None:
+            bptr = B.ctypes.data if isinstance(B, np.ndarray) else B.data_ptr()
+        A.check(self.lib.tmk_level_get_patch(self.h, p, uptr, bptr, 1 if host else 0), "tmk_level_get_patch")
+        return U, B
+
+    def set_level(self, Ug: np.ndarray, Bg: np.ndarray | None):
+        """Scatter a domain-wide state (22, ny+8, nx+8) / fault row (nb, nx+8) into the patches."""
+        g = A.TMK_NGHOST
+        for p, b in enumerate(self.boxes):
+            U = np.ascontiguousarray(Ug[:, b[1] - self.domain[1]:b[3] - self.domain[1] + 1 + 2 * g,
+                                        b[0] - self.domain[0]:b[2] - self.domain[0] + 1 + 2 * g])
+            B = None
+            if self.touches_fault(p):
+                B = np.ascontiguousarray(Bg[:, b[0] - self.domain[0]:b[2] - self.domain[0] + 1 + 2 * g])
+            self.set_patch(p, U, B)
+
+    def get_level(self, Ug: np.ndarray, Bg: np.ndarray | None):
+        """Gather the valid cells of every patch into domain-wide arrays (in place)."""
+        g = A.TMK_NGHOST
+        for p, b in enumerate(self.boxes):
+            U, B = self.get_patch(p)
+            ys = slice(b[1] - self.domain[1] + g, b[3] - self.domain[1] + 1 + g)
+            xs = slice(b[0] - self.domain[0] + g, b[2] - self.domain[0] + 1 + g)
+            Ug[:, ys, xs] = U[:, g:-g, g:-g]
+            if B is not None and Bg is not None:
+                Bg[:, xs] = B[:, g:-g]
+
+    def step(self, time: float, dt: float, stream=None) -> float:
+        dtn = C.c_double(0.0)
+        A.check(self.lib.tmk_level_step(self.h, time, dt, _stream_ptr(stream), C.byref(dtn)), "tmk_level_step")
+        return dtn.value
+
+    def status(self):
+        info = (C.c_longlong * 3)()
+        rc = self.lib.tmk_level_status(self.h, info)
+        return rc, list(info)
+
+    def launches_per_step(self) -> int:
+        return self.lib.tmk_level_launches_per_step(self.h)
+
+    def profile(self, enable: bool, max_steps: int = 0):
+        A.check(self.lib.tmk_level_profile(self.h, int(enable), max_steps), "tmk_level_profile")
+
+    def profile_read(self):
+        """Average ms per step: (exchange, fault kernel, volume kernel, whole step), nsteps."""
+        out = (C.c_double * 4)()
+        n = C.c_int(0)
+        A.check(self.lib.tmk_level_profile_read(self.h, out, C.byref(n)), "tmk_level_profile_read")
+        return list(out), n.value
+
+    def close(self):
+        if self.h:
+            self.lib.tmk_level_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
