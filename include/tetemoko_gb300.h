@@ -50,7 +50,9 @@ typedef enum {
   TMK_ERR_CUDA          = 4,  /* a CUDA runtime call failed */
   TMK_ERR_UNSUPPORTED   = 5,  /* option the reference rejects or this build lacks */
   TMK_ERR_ALLOC         = 6,  /* device allocation failed */
-  TMK_ERR_NO_DEVICE     = 7   /* no CUDA device visible */
+  TMK_ERR_NO_DEVICE     = 7,  /* no CUDA device visible */
+  TMK_ERR_TOO_LARGE     = 8   /* patch needs more than the fixed scratch of
+                                 tmk_patch_update_state_noalloc */
 } tmk_status;
 
 /* boundary types of comp.x_boundary / y_boundary (execLinElast/amrGodunov.cpp:571-590) */
@@ -159,6 +161,29 @@ tmk_status tmk_patch_update_state(tmk_context* ctx,
                                   const tmk_box* valid, const tmk_box* domain,
                                   double dx, double time, double dt,
                                   double* max_wave_speed, void* stream);
+
+/* Same computation and arguments as tmk_patch_update_state, but the call
+ * allocates no device memory at all.  This entry point has no counterpart in
+ * the reference.  It exists for callers that cannot allocate during a step:
+ * a driver that has handed the GPU's memory to its own pool (a Chombo run
+ * sizing its level data to fill HBM, where a cudaMalloc here would fail), or
+ * one that cannot afford the device-wide synchronisation cudaMalloc/cudaFree
+ * may impose in the middle of a time step.  Its temporaries live in a fixed
+ * device array of TMK_NOALLOC_SCRATCH_BYTES that every GPU loading this
+ * library holds until the process exits; a patch that needs more is refused
+ * with TMK_ERR_TOO_LARGE.  The first call on each device looks up that
+ * array's address (make the first call before any stream capture).  All calls
+ * on a device share the one array and it keeps the previous call's contents
+ * (every value is rewritten before it is read): calls that overlap on the GPU
+ * -- on different streams, or from several host threads -- race, so order
+ * them on one stream. */
+#define TMK_NOALLOC_SCRATCH_BYTES (8u << 20)
+tmk_status tmk_patch_update_state_noalloc(tmk_context* ctx,
+                                          const tmk_fab* U, const tmk_fab* B,
+                                          const tmk_fab* Fx, const tmk_fab* Fy,
+                                          const tmk_box* valid, const tmk_box* domain,
+                                          double dx, double time, double dt,
+                                          double* max_wave_speed, void* stream);
 
 /* LinElastPhysics::plasticUpdate -> PLASTICCORRECTION on device FAB U over box
  * (srcLinElast/LinElastPhysics.cpp:544-554, srcLinElast/PlasticPhysicsF.ChF:30-69). */

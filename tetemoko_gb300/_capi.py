@@ -19,7 +19,10 @@ TMK_OK = 0
 STATUS_NAMES = {
     0: "TMK_OK", 1: "TMK_ERR_BAD_DESC", 2: "TMK_ERR_NAN_STATE", 3: "TMK_ERR_TIMEOUT",
     4: "TMK_ERR_CUDA", 5: "TMK_ERR_UNSUPPORTED", 6: "TMK_ERR_ALLOC", 7: "TMK_ERR_NO_DEVICE",
+    8: "TMK_ERR_TOO_LARGE",
 }
+TMK_ERR_TOO_LARGE = 8
+TMK_NOALLOC_SCRATCH_BYTES = 8 << 20
 
 TMK_BC_OUTFLOW, TMK_BC_FREE, TMK_BC_FAULT = 0, 1, 2
 TMK_FAULT_NONE, TMK_FAULT_RS, TMK_FAULT_SW = 0, 1, 2
@@ -107,6 +110,8 @@ def lib() -> C.CDLL:
     L.tmk_patch_update_state.argtypes = [vp, C.POINTER(Fab), C.POINTER(Fab), C.POINTER(Fab), C.POINTER(Fab),
                                          C.POINTER(Box), C.POINTER(Box), C.c_double, C.c_double, C.c_double,
                                          dp, vp]
+    L.tmk_patch_update_state_noalloc.argtypes = L.tmk_patch_update_state.argtypes
+    L.tmk_patch_update_state_noalloc.restype = C.c_int
     L.tmk_plastic_update.argtypes = [vp, C.POINTER(Fab), C.POINTER(Box), C.c_double, vp]
     L.tmk_max_wave_speed.argtypes = [vp, dp]
     L.tmk_level_create.argtypes = [vp, C.POINTER(Box), C.c_double, C.c_int, C.POINTER(Box), C.POINTER(vp)]

@@ -600,3 +600,20 @@ extern "C" tmk_status tmk_level_status(tmk_level* L, long long info[3]) {
   info[0] = h.code; info[1] = h.first_index; info[2] = (long long)h.newton_maxed;
   return h.code == 0 ? TMK_OK : (tmk_status)h.code;
 }
+
+// Read-only view of a context for other translation units of this library.
+namespace tmk {
+struct CtxView {
+  const DevParams* dp;
+  DevStatus* st;
+  int fault_law;
+  int nb;
+  double max_speed;
+};
+CtxView context_view(const tmk_context* c) {
+  CtxView v;
+  v.dp = c->dp; v.st = c->dstatus; v.fault_law = c->scheme.fault_law; v.nb = c->nb;
+  v.max_speed = std::max(c->hp.cs, c->hp.cp);
+  return v;
+}
+}  // namespace tmk
