@@ -55,6 +55,20 @@ def rank_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def replica_rate(cells: int, steps: int, seconds_local: float, world: int, device=None) -> tuple[float, float]:
+    """Whole-job throughput of `world` independent replicas: every rank advanced
+    `cells` cells `steps` times; the job took the slowest rank's time.
+    Returns (cell-updates/s, max seconds)."""
+    t = seconds_local
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        x = torch.tensor([seconds_local], dtype=torch.float64, device=device)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        t = float(x.item())
+    return world * cells * steps / t, t
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -151,15 +165,16 @@ def run_reference(args):
         return 0
     from tetemoko_gb300 import scenarios as S
     nthreads = host_threads()
-    sc = S.rate_state(nx=NX, ny=NY)
+    nx, ny = args.nx, args.ny
+    sc = S.rate_state(nx=nx, ny=ny)
     # size the per-step sample so that warm-up + steps stay within about two minutes
-    probe_rate, _ = cpu_sample(sc, 2.0, nthreads, strip_rows=64)
+    probe_rate, _ = cpu_sample(sc, min(2.0, args.cpu_seconds), nthreads, strip_rows=min(64, ny))
     budget = 120.0
     steps = max(1, args.steps) + max(0, args.warmup)
-    rows = int(probe_rate * budget / steps / NX)
-    rows = max(16, min(NY, (rows // 8) * 8))
+    rows = int(probe_rate * budget / steps / nx)
+    rows = max(min(16, ny), min(ny, (rows // 8) * 8))
     import oracle as O
-    sub = S.rate_state(nx=NX, ny=rows, dx=sc.dx)
+    sub = S.rate_state(nx=nx, ny=rows, dx=sc.dx)
     boxes = O.tile_boxes(sub.nx, sub.ny, 128)
     U, B = sub.initial_U(), sub.initial_B()
     dt, t = sub.dt(), 0.0
@@ -172,13 +187,13 @@ def run_reference(args):
         t += dt
     el = time.perf_counter() - t0
     value = sub.nx * sub.ny * args.steps / el
-    sample = (f"each step: one level step of a {NX}x{rows} strip (fault row included) of the {NX}x{NY} "
+    sample = (f"each step: one level step of a {nx}x{rows} strip (fault row included) of the {nx}x{ny} "
               f"workload, 128x128 patches, OpenMP over patches")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": workload_config(),
+        "data": "synthetic", "config": workload_config(nx, ny),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's Chombo/Fortran build cannot be compiled here (no Fortran compiler, no "
@@ -219,13 +234,6 @@ def main():
     def barrier():
         if world > 1:
             dist.barrier()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     nx, ny = args.nx, args.ny
     cells = nx * ny
@@ -273,9 +281,9 @@ def main():
     sc, ctx, lvl = make_level(A.TMK_PREC_MIXED)
     sampler = ClockSampler() if rank == 0 else None
     ms, prof, clocks, st = timed(lvl, sc, args.steps, args.warmup, profile=True, sampler=sampler)
-    ms = max_over_ranks(ms)
+    value, secs = replica_rate(cells, args.steps, ms * 1e-3, world, device="cuda")
+    ms = secs * 1e3
     launches = lvl.launches_per_step() * args.steps
-    value = world * cells * args.steps / (ms * 1e-3)
     (ex_ms, fault_ms, vol_ms, step_ms), nprof = prof
     peaks = {}
     try:
@@ -319,8 +327,7 @@ def main():
         lvl.get_patch(0, Uh.numpy(), Bh.numpy())
         t += dt
     torch.cuda.synchronize()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e_value = world * cells * args.e2e_steps / e2e_s
+    e2e_value, _ = replica_rate(cells, args.e2e_steps, time.perf_counter() - t0, world, device="cuda")
     h2d = Uh.numel() * 8 + Bh.numel() * 8
     lvl.close()
     ctx.close()
@@ -329,8 +336,8 @@ def main():
     sc64, ctx64, lvl64 = make_level(A.TMK_PREC_FP64)
     n64 = max(1, args.fp64_steps)
     ms64, prof64, _, st64 = timed(lvl64, sc64, n64, 3, profile=True)
-    ms64 = max_over_ranks(ms64)
-    value64 = world * cells * n64 / (ms64 * 1e-3)
+    value64, secs64 = replica_rate(cells, n64, ms64 * 1e-3, world, device="cuda")
+    ms64 = secs64 * 1e3
     vol64 = prof64[0][2]
     lvl64.close()
     ctx64.close()
