@@ -112,7 +112,14 @@ typedef struct {
   int fault_law;                          /* TMK_FAULT_* on the y-lo face when boundary_type[2]==2 */
   int plasticity;                         /* apply PLASTICCORRECTION after the step */
   int precision;                          /* TMK_PREC_* for level objects */
+  int volume_kernel;                      /* TMK_VOLUME_* implementation of the volume update */
 } tmk_scheme;
+
+/* Implementations of the volume update (same results to rounding):
+ * TILE  shared-memory tiles, one side of the fault per CTA (also fuses plasticity);
+ * MARCH column-marching warps with both sides packed per lane (no plasticity);
+ * AUTO  MARCH for the mixed form without plasticity, TILE otherwise. */
+enum { TMK_VOLUME_AUTO = 0, TMK_VOLUME_TILE = 1, TMK_VOLUME_MARCH = 2 };
 
 /* Chombo FArrayBox view: data[((c*(hi1-lo1+1)) + (j-lo1))*(hi0-lo0+1) + (i-lo0)] */
 typedef struct {

@@ -16,6 +16,7 @@
 
 #include "../../include/tetemoko_gb300.h"
 #include "tmk_kernels.cuh"
+#include "tmk_march.cuh"
 #include "tmk_launch.h"
 
 using tmk::DevParams;
@@ -83,6 +84,8 @@ extern "C" tmk_status tmk_context_create(const tmk_elastic_params* e, const tmk_
   if (!(e->cs > 0) || !(e->cp >= e->cs)) return TMK_ERR_BAD_DESC;   // char transforms assume cp >= cs
   if (sw && s->fault_law == TMK_FAULT_SW && (sw->num_patches < 0 || sw->num_patches > TMK_SW_MAX_PATCHES))
     return TMK_ERR_BAD_DESC;
+  if (s->volume_kernel < TMK_VOLUME_AUTO || s->volume_kernel > TMK_VOLUME_MARCH) return TMK_ERR_BAD_DESC;
+  if (s->volume_kernel == TMK_VOLUME_MARCH && s->plasticity) return TMK_ERR_UNSUPPORTED;
   if (!device_ok()) return TMK_ERR_NO_DEVICE;
   tmk_context* c = new (std::nothrow) tmk_context_s();
   if (!c) return TMK_ERR_ALLOC;
@@ -165,6 +168,24 @@ void make_tiles(std::vector<TileDev>& out, int patch, const tmk_box& v, int TX, 
 }
 
 size_t align_up(size_t n) { return (n + 255) & ~(size_t)255; }
+
+// work items of the column-marching kernel: strips of MARCH_COLS columns by
+// runs of up to 64 rows over a valid box
+constexpr int kMarchRows = 64;
+void make_march_items(std::vector<tmk::MarchItem>& out, int patch, const tmk_box& v) {
+  for (int y0 = v.lo[1]; y0 <= v.hi[1]; y0 += kMarchRows)
+    for (int x0 = v.lo[0]; x0 <= v.hi[0]; x0 += tmk::MARCH_COLS) {
+      tmk::MarchItem m;
+      m.patch = patch; m.x0 = x0; m.y0 = y0; m.y1 = std::min(y0 + kMarchRows - 1, v.hi[1]);
+      out.push_back(m);
+    }
+}
+
+bool uses_march(const tmk_scheme& s) {
+  if (s.volume_kernel == TMK_VOLUME_MARCH) return true;
+  if (s.volume_kernel == TMK_VOLUME_TILE) return false;
+  return s.precision == TMK_PREC_MIXED && !s.plasticity;
+}
 
 }  // namespace
 
@@ -285,6 +306,9 @@ struct tmk_level_s {
   std::vector<char> hpatch[2];
   TileDev* dtiles = nullptr;
   int ntiles = 0;
+  int march = 0;                           // column-marching volume kernel
+  tmk::MarchItem* ditems = nullptr;
+  int nitems = 0;
   int* dfault = nullptr;
   int nfault = 0, max_faces = 0;
   CopyDev* dcopies = nullptr;
@@ -439,6 +463,15 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
   }
   if (dalloc(&L->dtiles, tiles.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
   L->allocs.push_back(L->dtiles);
+  L->march = uses_march(c->scheme) ? 1 : 0;
+  if (L->march) {
+    std::vector<tmk::MarchItem> items;
+    for (int p = 0; p < npatch; ++p) make_march_items(items, p, boxes[p]);
+    L->nitems = (int)items.size();
+    if (dalloc(&L->ditems, items.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+    L->allocs.push_back(L->ditems);
+    TMK_CU(cudaMemcpy(L->ditems, items.data(), items.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
+  }
   TMK_CU(cudaMemcpy(L->dtiles, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice));
   if (L->nfault) {
     if (dalloc(&L->dfault, fault_idx.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
@@ -538,7 +571,8 @@ extern "C" tmk_status tmk_level_step(tmk_level* L, double time, double dt, void*
     if (ev) TMK_CU(cudaEventRecord(ev[1], s));
     TMK_CU(tmk::Launch<float>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, s));
     if (ev) TMK_CU(cudaEventRecord(ev[2], s));
-    TMK_CU(tmk::Launch<float>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
+    if (L->march) TMK_CU(tmk::Launch<float>::march(pd, L->ditems, L->nitems, c->dp, s));
+    else TMK_CU(tmk::Launch<float>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
   } else {
     const PatchDev<double>* pd = (const PatchDev<double>*)L->dpatch[par];
     TMK_CU(tmk::Launch<double>::exchange(pd, L->dcopies, L->ncopies, 0, TMK_NCOMP, s));
@@ -546,7 +580,8 @@ extern "C" tmk_status tmk_level_step(tmk_level* L, double time, double dt, void*
     if (ev) TMK_CU(cudaEventRecord(ev[1], s));
     TMK_CU(tmk::Launch<double>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, s));
     if (ev) TMK_CU(cudaEventRecord(ev[2], s));
-    TMK_CU(tmk::Launch<double>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
+    if (L->march) TMK_CU(tmk::Launch<double>::march(pd, L->ditems, L->nitems, c->dp, s));
+    else TMK_CU(tmk::Launch<double>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
   }
   if (ev) TMK_CU(cudaEventRecord(ev[3], s));
   L->parity = 1 - par;
@@ -588,7 +623,8 @@ extern "C" tmk_status tmk_level_profile_read(tmk_level* L, double out[4], int* n
 
 extern "C" int tmk_level_launches_per_step(const tmk_level* L) {
   if (!L) return 0;
-  return (L->ncopies ? 1 : 0) + (L->nbcopies ? 1 : 0) + (L->nfault ? 1 : 0) + (L->ntiles ? 1 : 0);
+  const int vol = L->march ? (L->nitems ? 2 : 0) : (L->ntiles ? 1 : 0);
+  return (L->ncopies ? 1 : 0) + (L->nbcopies ? 1 : 0) + (L->nfault ? 1 : 0) + vol;
 }
 
 extern "C" tmk_status tmk_level_status(tmk_level* L, long long info[3]) {

@@ -10,6 +10,7 @@ namespace tmk {
 template <typename Real> struct PatchDev;
 struct TileDev;
 struct CopyDev;
+struct MarchItem;
 
 template <typename Real>
 struct Launch {
@@ -24,6 +25,9 @@ struct Launch {
   static cudaError_t exchange(const PatchDev<Real>* patches, const CopyDev* copies, int ncopies, int c0,
                               int ncomp, cudaStream_t s);
   static size_t volume_smem();
+  // column-marching volume update: one warp per item, both component groups
+  static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* items, int nitems,
+                           const DevParams* params, cudaStream_t s);
 };
 
 // FP64 <-> Real conversion of a FAB on the device

@@ -2,6 +2,7 @@
 // translation unit per arithmetic type.
 #pragma once
 #include "tmk_kernels.cuh"
+#include "tmk_march.cuh"
 #include "tmk_launch.h"
 
 namespace tmk {
@@ -37,6 +38,16 @@ struct LaunchImpl {
     exchange_kernel<Real><<<ncopies, 256, 0, s>>>(patches, copies, c0, ncomp, 0);
     return cudaGetLastError();
   }
+  static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* items, int nitems,
+                           const DevParams* params, cudaStream_t s) {
+    if (nitems <= 0) return cudaSuccess;
+    const int blocks = (nitems + MARCH_WARPS - 1) / MARCH_WARPS;
+    march_kernel<Real, 0><<<blocks, 32 * MARCH_WARPS, 0, s>>>(patches, items, nitems, params);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    march_kernel<Real, 1><<<blocks, 32 * MARCH_WARPS, 0, s>>>(patches, items, nitems, params);
+    return cudaGetLastError();
+  }
 };
 
 }  // namespace tmk
@@ -58,4 +69,8 @@ struct LaunchImpl {
     return LaunchImpl<REAL, TXV, TYV, NTV>::exchange(p, c, n, c0, nc, s);                                    \
   }                                                                                                          \
   template <> size_t Launch<REAL>::volume_smem() { return LaunchImpl<REAL, TXV, TYV, NTV>::smem(); }         \
+  template <> cudaError_t Launch<REAL>::march(const PatchDev<REAL>* p, const MarchItem* it, int n,           \
+                                              const DevParams* prm, cudaStream_t s) {                       \
+    return LaunchImpl<REAL, TXV, TYV, NTV>::march(p, it, n, prm, s);                                         \
+  }                                                                                                          \
   }

@@ -1,0 +1,509 @@
+// tmk_march.cuh -- column-marching volume kernel.
+//
+// A warp owns 32 adjacent columns of a patch (26 updated columns plus a
+// 3-column halo on each side) and streams up a run of rows.  Per row it
+// computes the x predictor (neighbours by warp shuffles) and the y predictor
+// (a rolling window of rows in registers), the first-pass Riemann states,
+// the transverse corrections, the final Riemann states, the fluxes and the
+// conservative update -- the CTU sequence of LinElastPatchGodunov::computeWHalf
+// and LinElastPhysics::computeUpdate (srcLinElast/LinElastPatchGodunov.cpp:174-469)
+// -- emitting one updated row per step, three rows behind the loads.
+//
+// The state of the two fault sides is packed into one pair per component
+// (.x = side 1, .y = side 2; the y direction of side 2 is mirrored, rv = -1),
+// so the linear algebra runs as packed FP32x2 instructions in the FP32 form.
+// The components split into two groups that never mix inside the volume:
+//   in-plane  (vx vy sxx syy szz sxy): a P-wave pair, an S-wave pair and the
+//             two normal stresses tied to the P-wave stress by lam/(lam+2G);
+//   antiplane (vz sxz syz): an S-wave pair and one stress with zero speed.
+// The characteristic transforms, the PPM tracing (Colella & Woodward 1984
+// eq. 1.12, written as a*w_near + b*w_far with a = (1-s)^2, b = s^2 - s) and
+// the syntheses of srcLinElast/LinElastPhysicsF.ChF:359-555 are applied per
+// wave pair.
+#pragma once
+#include "tmk_device.cuh"
+#include "tmk_kernels.cuh"
+
+namespace tmk {
+
+// ------------------------------------------------------------ pair arithmetic
+template <typename T> struct PairOf;
+template <> struct PairOf<float> { using P = float2; };
+template <> struct PairOf<double> { using P = double2; };
+
+TMK_D float2 mk2(float a, float b) { return make_float2(a, b); }
+TMK_D double2 mk2(double a, double b) { return make_double2(a, b); }
+TMK_D float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+TMK_D float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+TMK_D float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+TMK_D float2 psub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+TMK_D double2 padd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+TMK_D double2 pmul(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
+TMK_D double2 pfma(double2 a, double2 b, double2 c) { return make_double2(a.x * b.x + c.x, a.y * b.y + c.y); }
+TMK_D double2 psub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+template <typename P> TMK_D P pneg(P a) { return pmul(a, mk2(decltype(a.x)(-1), decltype(a.x)(-1))); }
+
+TMK_D float2 shfl_up2(float2 v, int d) {
+  return make_float2(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
+}
+TMK_D float2 shfl_dn2(float2 v, int d) {
+  return make_float2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+TMK_D double2 shfl_up2(double2 v, int d) {
+  return make_double2(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
+}
+TMK_D double2 shfl_dn2(double2 v, int d) {
+  return make_double2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+
+// ------------------------------------------------------------ groups and roles
+template <int G> struct Grp;
+template <> struct Grp<0> {   // in-plane
+  static constexpr int N = 6;
+  TMK_HD static constexpr int glob(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 3 : k == 3 ? 4 : k == 4 ? 5 : 6; }
+};
+template <> struct Grp<1> {   // antiplane
+  static constexpr int N = 3;
+  TMK_HD static constexpr int glob(int k) { return k == 0 ? 2 : k == 1 ? 7 : 8; }
+};
+
+// Wave roles of the group's components in direction D (indices into the group):
+//   P pair (vP, sP), S pair (vS, sS), zero-speed components coupled to sP
+//   (zc0, zc1: normal stresses, z - lam/(lam+2G) sP is invariant), and a
+//   zero-speed component with no coupling (zf).
+template <int G, int D> struct Role;
+template <> struct Role<0, 0> { static constexpr bool hasP = true, hasZc = true, hasZf = false;
+  static constexpr int vP = 0, sP = 2, vS = 1, sS = 5, zc0 = 3, zc1 = 4, zf = 0; };
+template <> struct Role<0, 1> { static constexpr bool hasP = true, hasZc = true, hasZf = false;
+  static constexpr int vP = 1, sP = 3, vS = 0, sS = 5, zc0 = 4, zc1 = 2, zf = 0; };
+template <> struct Role<1, 0> { static constexpr bool hasP = false, hasZc = false, hasZf = true;
+  static constexpr int vP = 0, sP = 0, vS = 0, sS = 1, zc0 = 0, zc1 = 0, zf = 2; };
+template <> struct Role<1, 1> { static constexpr bool hasP = false, hasZc = false, hasZf = true;
+  static constexpr int vP = 0, sP = 0, vS = 0, sS = 2, zc0 = 0, zc1 = 0, zf = 1; };
+
+// Packed constants of one direction.
+template <typename T>
+struct MK {
+  using P = typename PairOf<T>::P;
+  P ZpE, ZsE;          // characteristic w = s +- ZE v (ZE = rv Z)
+  P hZpE, hZsE;        // synthesis v = (w- - w+) * rv/(2Z)
+  P half, r;           // 1/2, lam/(lam+2G)
+  P aP, bP, aS, bS;    // PPM tracing coefficients of the P and S speeds
+  P f_irho, f_l2g, f_lam, f_G;   // GETFLUXF: -rv * {1/rho, lam+2G, lam, G}
+  P a_irho, a_l2g, a_lam, a_G;   // GETADWDXF: -rv*scale * {...}
+  TMK_D void load(const DevParams& p, int D, double dtdx, double scale) {
+    const T s2 = (D == 1) ? T(-1) : T(1);       // rv of side 2
+    ZpE = mk2((T)p.Zp, (T)(s2 * p.Zp)); ZsE = mk2((T)p.Zs, (T)(s2 * p.Zs));
+    hZpE = mk2((T)(0.5 / p.Zp), (T)(s2 * 0.5 / p.Zp)); hZsE = mk2((T)(0.5 / p.Zs), (T)(s2 * 0.5 / p.Zs));
+    half = mk2(T(0.5), T(0.5));
+    const T rr = (T)(p.lam / (p.lam + 2.0 * p.G));
+    r = mk2(rr, rr);
+    const double sp = p.cp * dtdx, ss = p.cs * dtdx;
+    const T ap = (T)((1.0 - sp) * (1.0 - sp)), bp = (T)(sp * sp - sp);
+    const T as = (T)((1.0 - ss) * (1.0 - ss)), bs = (T)(ss * ss - ss);
+    aP = mk2(ap, ap); bP = mk2(bp, bp); aS = mk2(as, as); bS = mk2(bs, bs);
+    const double m1 = -1.0, m2 = -s2;
+    f_irho = mk2((T)(m1 / p.rho), (T)(m2 / p.rho));
+    f_l2g = mk2((T)(m1 * (p.lam + 2.0 * p.G)), (T)(m2 * (p.lam + 2.0 * p.G)));
+    f_lam = mk2((T)(m1 * p.lam), (T)(m2 * p.lam));
+    f_G = mk2((T)(m1 * p.G), (T)(m2 * p.G));
+    a_irho = mk2((T)(m1 * scale / p.rho), (T)(m2 * scale / p.rho));
+    a_l2g = mk2((T)(m1 * scale * (p.lam + 2.0 * p.G)), (T)(m2 * scale * (p.lam + 2.0 * p.G)));
+    a_lam = mk2((T)(m1 * scale * p.lam), (T)(m2 * scale * p.lam));
+    a_G = mk2((T)(m1 * scale * p.G), (T)(m2 * scale * p.G));
+  }
+};
+
+// per-half scalar stages on pairs
+template <typename P> TMK_D P slope2(P wm, P w0, P wp, bool hasL, bool hasR, bool limit) {
+  return mk2(vl_slope(wm.x, w0.x, wp.x, hasL, hasR, limit), vl_slope(wm.y, w0.y, wp.y, hasL, hasR, limit));
+}
+template <typename P> TMK_D void limit2(P& m, P& p) { ppm_limit(m.x, p.x); ppm_limit(m.y, p.y); }
+
+// interior PPM face value between cells a (lower) and b: (a+b)/2 - (sb - sa)/6
+template <typename T, typename P> TMK_D P face2(P a, P b, P sa, P sb) {
+  const P h = mk2(T(0.5), T(0.5)), m6 = mk2(T(-1.0 / 6.0), T(-1.0 / 6.0));
+  return pfma(psub(sb, sa), m6, pmul(h, padd(a, b)));
+}
+
+// PPM normal predictor of a group in direction D from the unlimited face
+// deltas dm (lo face) and dp (hi face) of each component; WM, WP = w + traced.
+template <int G, int D, typename T>
+TMK_D void predict(const MK<T>& k, const typename PairOf<T>::P* w, typename PairOf<T>::P* dm,
+                   typename PairOf<T>::P* dp, bool plim, bool clim, typename PairOf<T>::P* WM,
+                   typename PairOf<T>::P* WP) {
+  using P = typename PairOf<T>::P;
+  using R = Role<G, D>;
+  constexpr int N = Grp<G>::N;
+  if (plim) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) limit2(dm[c], dp[c]);
+  }
+  // S wave pair
+  {
+    P nm = pfma(k.ZsE, dm[R::vS], dm[R::sS]), pm = pfma(pneg(k.ZsE), dm[R::vS], dm[R::sS]);
+    P np = pfma(k.ZsE, dp[R::vS], dp[R::sS]), pp = pfma(pneg(k.ZsE), dp[R::vS], dp[R::sS]);
+    if (clim) { limit2(nm, np); limit2(pm, pp); }
+    P nmt = pfma(k.aS, nm, pmul(k.bS, np));       // w- traced to the lo face
+    P ppt = pfma(k.aS, pp, pmul(k.bS, pm));       // w+ traced to the hi face
+    WM[R::sS] = padd(w[R::sS], pmul(k.half, padd(nmt, pm)));
+    WM[R::vS] = padd(w[R::vS], pmul(k.hZsE, psub(nmt, pm)));
+    WP[R::sS] = padd(w[R::sS], pmul(k.half, padd(np, ppt)));
+    WP[R::vS] = padd(w[R::vS], pmul(k.hZsE, psub(np, ppt)));
+  }
+  if constexpr (R::hasP) {
+    P nm = pfma(k.ZpE, dm[R::vP], dm[R::sP]), pm = pfma(pneg(k.ZpE), dm[R::vP], dm[R::sP]);
+    P np = pfma(k.ZpE, dp[R::vP], dp[R::sP]), pp = pfma(pneg(k.ZpE), dp[R::vP], dp[R::sP]);
+    P z0m = dm[R::zc0], z0p = dp[R::zc0], z1m = dm[R::zc1], z1p = dp[R::zc1];
+    if (clim) {
+      limit2(nm, np); limit2(pm, pp);
+      P sPm = dm[R::sP], sPp = dp[R::sP];
+      z0m = pfma(pneg(k.r), sPm, z0m); z0p = pfma(pneg(k.r), sPp, z0p);
+      z1m = pfma(pneg(k.r), sPm, z1m); z1p = pfma(pneg(k.r), sPp, z1p);
+      limit2(z0m, z0p); limit2(z1m, z1p);
+    } else {
+      z0m = pfma(pneg(k.r), dm[R::sP], z0m); z0p = pfma(pneg(k.r), dp[R::sP], z0p);
+      z1m = pfma(pneg(k.r), dm[R::sP], z1m); z1p = pfma(pneg(k.r), dp[R::sP], z1p);
+    }
+    P nmt = pfma(k.aP, nm, pmul(k.bP, np));
+    P ppt = pfma(k.aP, pp, pmul(k.bP, pm));
+    P sPm = pmul(k.half, padd(nmt, pm)), sPp = pmul(k.half, padd(np, ppt));
+    WM[R::sP] = padd(w[R::sP], sPm);
+    WM[R::vP] = padd(w[R::vP], pmul(k.hZpE, psub(nmt, pm)));
+    WP[R::sP] = padd(w[R::sP], sPp);
+    WP[R::vP] = padd(w[R::vP], pmul(k.hZpE, psub(np, ppt)));
+    WM[R::zc0] = padd(w[R::zc0], pfma(k.r, sPm, z0m));
+    WP[R::zc0] = padd(w[R::zc0], pfma(k.r, sPp, z0p));
+    WM[R::zc1] = padd(w[R::zc1], pfma(k.r, sPm, z1m));
+    WP[R::zc1] = padd(w[R::zc1], pfma(k.r, sPp, z1p));
+  }
+  if constexpr (R::hasZf) {
+    P zm = dm[R::zf], zp = dp[R::zf];
+    if (clim) limit2(zm, zp);
+    WM[R::zf] = padd(w[R::zf], zm);
+    WP[R::zf] = padd(w[R::zf], zp);
+  }
+}
+
+// RIEMANNF for a group: L = state left of the face, Rt = right
+template <int G, int D, typename T>
+TMK_D void riem(const MK<T>& k, const typename PairOf<T>::P* L, const typename PairOf<T>::P* Rt,
+                typename PairOf<T>::P* g) {
+  using P = typename PairOf<T>::P;
+  using R = Role<G, D>;
+  {
+    P wpos = pfma(pneg(k.ZsE), L[R::vS], L[R::sS]);
+    P wneg = pfma(k.ZsE, Rt[R::vS], Rt[R::sS]);
+    g[R::sS] = pmul(k.half, padd(wneg, wpos));
+    g[R::vS] = pmul(k.hZsE, psub(wneg, wpos));
+  }
+  if constexpr (R::hasP) {
+    P wpos = pfma(pneg(k.ZpE), L[R::vP], L[R::sP]);
+    P wneg = pfma(k.ZpE, Rt[R::vP], Rt[R::sP]);
+    P s = pmul(k.half, padd(wneg, wpos));
+    g[R::sP] = s;
+    g[R::vP] = pmul(k.hZpE, psub(wneg, wpos));
+    P zr0 = pfma(pneg(k.r), Rt[R::sP], Rt[R::zc0]), zl0 = pfma(pneg(k.r), L[R::sP], L[R::zc0]);
+    P zr1 = pfma(pneg(k.r), Rt[R::sP], Rt[R::zc1]), zl1 = pfma(pneg(k.r), L[R::sP], L[R::zc1]);
+    g[R::zc0] = pfma(k.r, s, pmul(k.half, padd(zr0, zl0)));
+    g[R::zc1] = pfma(k.r, s, pmul(k.half, padd(zr1, zl1)));
+  }
+  if constexpr (R::hasZf) g[R::zf] = pmul(k.half, padd(Rt[R::zf], L[R::zf]));
+}
+
+// LINELASTOUTBCF / LINELASTFREEBCF for a group.  lo: the inside state is the
+// cell above/right of the face; SHF keeps the reference's velocity-minus-stress form.
+template <int G, int D, typename T>
+TMK_D void edge2(const MK<T>& k, bool lo, bool outflow, const typename PairOf<T>::P* Wi,
+                 const typename PairOf<T>::P* bg, typename PairOf<T>::P* g) {
+  using P = typename PairOf<T>::P;
+  using R = Role<G, D>;
+  {
+    P wneg, wpos;
+    if (lo) {
+      wneg = pfma(k.ZsE, Wi[R::vS], Wi[R::sS]);
+      wpos = outflow ? pfma(pneg(k.ZsE), bg[R::vS], bg[R::sS]) : pneg(wneg);
+    } else {
+      wpos = pfma(pneg(k.ZsE), Wi[R::vS], Wi[R::sS]);
+      wneg = outflow ? pfma(k.ZsE, bg[R::vS], bg[R::sS]) : pneg(wpos);
+    }
+    g[R::sS] = pmul(k.half, padd(wneg, wpos));
+    g[R::vS] = pmul(k.hZsE, psub(wneg, wpos));
+  }
+  if constexpr (R::hasP) {
+    P wneg, wpos;
+    if (lo) {
+      wneg = pfma(k.ZpE, Wi[R::vP], Wi[R::sP]);
+      wpos = outflow ? pfma(pneg(k.ZpE), bg[R::vP], bg[R::sP]) : pneg(wneg);
+    } else {
+      wpos = pfma(pneg(k.ZpE), Wi[R::vP], Wi[R::sP]);
+      wneg = outflow ? pfma(k.ZpE, bg[R::vP], bg[R::sP]) : pneg(wpos);
+    }
+    P s = pmul(k.half, padd(wneg, wpos));
+    g[R::sP] = s;
+    g[R::vP] = pmul(k.hZpE, psub(wneg, wpos));
+    P shf = pmul(pneg(k.r), psub(Wi[R::vP], s));
+    g[R::zc0] = padd(Wi[R::zc0], shf);
+    g[R::zc1] = padd(Wi[R::zc1], shf);
+  }
+  if constexpr (R::hasZf) g[R::zf] = Wi[R::zf];
+}
+
+// GETFLUXF for a group
+template <int G, int D, typename T>
+TMK_D void flux2(const MK<T>& k, const typename PairOf<T>::P* g, typename PairOf<T>::P* F) {
+  using R = Role<G, D>;
+  F[R::vS] = pmul(k.f_irho, g[R::sS]);
+  F[R::sS] = pmul(k.f_G, g[R::vS]);
+  if constexpr (R::hasP) {
+    F[R::vP] = pmul(k.f_irho, g[R::sP]);
+    F[R::sP] = pmul(k.f_l2g, g[R::vP]);
+    F[R::zc0] = pmul(k.f_lam, g[R::vP]);
+    F[R::zc1] = pmul(k.f_lam, g[R::vP]);
+  }
+  if constexpr (R::hasZf) F[R::zf] = mk2(decltype(g[0].x)(0), decltype(g[0].x)(0));
+}
+
+// GETADWDXF increment from the face states at the hi (h) and lo (l) faces, added to q1 and q2
+template <int G, int D, typename T>
+TMK_D void adw2(const MK<T>& k, const typename PairOf<T>::P* h, const typename PairOf<T>::P* l,
+                typename PairOf<T>::P* q1, typename PairOf<T>::P* q2) {
+  using P = typename PairOf<T>::P;
+  using R = Role<G, D>;
+  {
+    P a = pmul(k.a_irho, psub(h[R::sS], l[R::sS]));
+    q1[R::vS] = padd(q1[R::vS], a); q2[R::vS] = padd(q2[R::vS], a);
+    P b = pmul(k.a_G, psub(h[R::vS], l[R::vS]));
+    q1[R::sS] = padd(q1[R::sS], b); q2[R::sS] = padd(q2[R::sS], b);
+  }
+  if constexpr (R::hasP) {
+    P a = pmul(k.a_irho, psub(h[R::sP], l[R::sP]));
+    q1[R::vP] = padd(q1[R::vP], a); q2[R::vP] = padd(q2[R::vP], a);
+    P dv = psub(h[R::vP], l[R::vP]);
+    P b = pmul(k.a_l2g, dv);
+    q1[R::sP] = padd(q1[R::sP], b); q2[R::sP] = padd(q2[R::sP], b);
+    P c = pmul(k.a_lam, dv);
+    q1[R::zc0] = padd(q1[R::zc0], c); q2[R::zc0] = padd(q2[R::zc0], c);
+    q1[R::zc1] = padd(q1[R::zc1], c); q2[R::zc1] = padd(q2[R::zc1], c);
+  }
+}
+
+// ---------------------------------------------------------------- the kernel
+struct MarchItem { int patch, x0, y0, y1; };
+
+constexpr int MARCH_COLS = 26;   // updated columns per warp
+constexpr int MARCH_WARPS = 4;   // warps per CTA
+
+template <typename T, int G>
+__global__ void __launch_bounds__(32 * MARCH_WARPS) march_kernel(const PatchDev<T>* __restrict__ patches,
+                                                                 const MarchItem* __restrict__ items, int nitems,
+                                                                 const DevParams* __restrict__ params) {
+  using P = typename PairOf<T>::P;
+  constexpr int N = Grp<G>::N;
+  const int wid = blockIdx.x * MARCH_WARPS + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (wid >= nitems) return;
+  const MarchItem it = items[wid];
+  const PatchDev<T>& pp = patches[it.patch];
+  const DevParams& Pm = params[pp.scen];
+  const int x = it.x0 - 3 + lane;
+  const int dlo0 = pp.dlo0, dhi0 = pp.dhi0, dlo1 = pp.dlo1, dhi1 = pp.dhi1;
+  const int ahi0 = pp.alo0 + pp.anx - 1;
+  const bool lane_in = x >= dlo0 && x <= dhi0 && x >= pp.alo0 && x <= ahi0;
+  const bool inL = x - 1 >= dlo0, inR = x + 1 <= dhi0;
+  const bool plim = Pm.prim_lim != 0, clim = Pm.char_lim != 0, lim = plim || clim;
+  const bool ppm = Pm.order != 0;
+  const double dtdx = pp.dt / pp.dx;
+  MK<T> kx, ky;
+  kx.load(Pm, 0, dtdx, -(1.0 / 2.0) * pp.dt / pp.dx);
+  ky.load(Pm, 1, dtdx, -(1.0 / 2.0) * pp.dt / pp.dx);
+  const P sc = mk2((T)(-pp.dt / pp.dx), (T)(-pp.dt / pp.dx));
+  P bg[N];
+#pragma unroll
+  for (int c = 0; c < N; ++c) bg[c] = mk2((T)Pm.bg[Grp<G>::glob(c)], (T)Pm.bg[11 + Grp<G>::glob(c)]);
+  const bool xout_lo = Pm.bc[0] == 0, xout_hi = Pm.bc[1] == 0, yout_lo = Pm.bc[2] == 0, yout_hi = Pm.bc[3] == 0;
+  const bool fault = pp.fault != 0;
+  const bool col_valid = x >= it.x0 && x < it.x0 + MARCH_COLS && x >= pp.vlo0 && x <= pp.vhi0;
+  const size_t plane = (size_t)pp.anx * pp.any;
+
+  auto load_row = [&](int y, P* w) {
+    const bool ok = lane_in && y >= dlo1 && y <= dhi1;
+    const size_t o = ok ? fab_idx(pp, 0, x, y) : 0;
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      const int g = Grp<G>::glob(c);
+      w[c] = ok ? mk2(pp.Uin[o + (size_t)g * plane], pp.Uin[o + (size_t)(11 + g) * plane]) : mk2(T(0), T(0));
+    }
+  };
+
+  // x-direction normal predictor of row w and the first-pass x-face state on
+  // the lane's lo face (H1 lo) and hi face (H1 hi)
+  auto xrow = [&](const P* w, P* WM, P* WP, P* H1lo, P* H1hi) {
+    if (ppm) {
+      P dm[N], dp[N];
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        P wl = shfl_up2(w[c], 1), wr = shfl_dn2(w[c], 1);
+        P s = slope2(wl, w[c], wr, inL, inR, lim);
+        P sl = shfl_up2(s, 1);
+        P flo = inL ? face2<T>(wl, w[c], sl, s) : pfma(mk2(T(-0.5), T(-0.5)), s, w[c]);
+        P fhi = shfl_dn2(flo, 1);
+        if (!inR) fhi = pfma(mk2(T(0.5), T(0.5)), s, w[c]);
+        dm[c] = psub(flo, w[c]);
+        dp[c] = psub(fhi, w[c]);
+      }
+      predict<G, 0, T>(kx, w, dm, dp, plim, clim, WM, WP);
+    } else {
+#pragma unroll
+      for (int c = 0; c < N; ++c) { WM[c] = w[c]; WP[c] = w[c]; }
+    }
+    P L[N];
+#pragma unroll
+    for (int c = 0; c < N; ++c) L[c] = shfl_up2(WP[c], 1);
+    if (x == dlo0) edge2<G, 0, T>(kx, true, xout_lo, WM, bg, H1lo);
+    else if (x == dhi0 + 1) edge2<G, 0, T>(kx, false, xout_hi, L, bg, H1lo);
+    else riem<G, 0, T>(kx, L, WM, H1lo);
+#pragma unroll
+    for (int c = 0; c < N; ++c) H1hi[c] = shfl_dn2(H1lo[c], 1);
+  };
+
+  const int q_s = max(it.y0 - 1, dlo1);
+  const int q_e = it.y1 + 1;
+  // rolling window: W0 = W(q), W1 = W(q+1), W2 = W(q+2); sy0 = slope(q); Fy0 = lo-face value of row q
+  P W0[N], W1[N], W2[N], sy0[N], Fy0[N];
+  {
+    P Wa[N], Wb[N];
+    load_row(q_s - 2, Wa);
+    load_row(q_s - 1, Wb);
+    load_row(q_s, W0);
+    load_row(q_s + 1, W1);
+    load_row(q_s + 2, W2);
+    const bool hl = q_s - 1 >= dlo1, hr = q_s + 1 <= dhi1;
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      sy0[c] = slope2(Wb[c], W0[c], W1[c], hl, hr, lim);
+      if (hl) {
+        P sm = slope2(Wa[c], Wb[c], W0[c], q_s - 2 >= dlo1, true, lim);
+        Fy0[c] = face2<T>(Wb[c], W0[c], sm, sy0[c]);
+      } else {
+        Fy0[c] = pfma(mk2(T(-0.5), T(-0.5)), sy0[c], W0[c]);
+      }
+    }
+  }
+  // carried state of row q-1
+  P WPy_p[N], WPcy_p[N], H1y_p[N], WMx_p[N], WPx_p[N], Fy_p[N];
+
+  for (int q = q_s; q <= q_e; ++q) {
+    const bool rowin = q <= dhi1;
+    P WMy[N], WPy[N], WMcy[N], WPcy[N], WMx[N], WPx[N], H1lo[N], H1hi[N];
+    P sy1[N], Fy1[N];
+    if (rowin) {
+      // y predictor of row q
+      if (ppm) {
+        const bool hl = true, hr = q + 2 <= dhi1;
+        P dm[N], dp[N];
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+          sy1[c] = slope2(W0[c], W1[c], W2[c], hl, hr, lim);
+          Fy1[c] = (q + 1 <= dhi1) ? face2<T>(W0[c], W1[c], sy0[c], sy1[c])
+                                   : pfma(mk2(T(0.5), T(0.5)), sy0[c], W0[c]);
+          dm[c] = psub(Fy0[c], W0[c]);
+          dp[c] = psub(Fy1[c], W0[c]);
+        }
+        predict<G, 1, T>(ky, W0, dm, dp, plim, clim, WMy, WPy);
+      } else {
+#pragma unroll
+        for (int c = 0; c < N; ++c) { WMy[c] = W0[c]; WPy[c] = W0[c]; sy1[c] = sy0[c]; Fy1[c] = Fy0[c]; }
+      }
+      // x predictor of row q, first-pass x faces, corrected y states of row q
+      xrow(W0, WMx, WPx, H1lo, H1hi);
+#pragma unroll
+      for (int c = 0; c < N; ++c) { WMcy[c] = WMy[c]; WPcy[c] = WPy[c]; }
+      adw2<G, 0, T>(kx, H1hi, H1lo, WMcy, WPcy);
+    }
+    // first-pass y face q (lo face of row q)
+    P H1y[N];
+    const bool need_h1y = (q > q_s) || (q == dlo1);
+    if (need_h1y) {
+      if (q == dlo1) {
+        if (fault) {
+          const int fi = x - (pp.vlo0 - 1);
+          const bool ok = fi >= 0 && fi < pp.nfirst && x >= dlo0 && x <= dhi0;
+#pragma unroll
+          for (int c = 0; c < N; ++c) {
+            const int g = Grp<G>::glob(c);
+            H1y[c] = ok ? mk2((T)pp.first[(size_t)g * pp.nfirst + fi], (T)pp.first[(size_t)(11 + g) * pp.nfirst + fi])
+                        : mk2(T(0), T(0));
+          }
+        } else {
+          edge2<G, 1, T>(ky, true, yout_lo, WMy, bg, H1y);
+        }
+      } else if (!rowin) {
+        edge2<G, 1, T>(ky, false, yout_hi, WPy_p, bg, H1y);
+      } else {
+        riem<G, 1, T>(ky, WPy_p, WMy, H1y);
+      }
+    }
+    // final y face q
+    P Fy[N];
+    if (q >= it.y0) {
+      if (q == dlo1 && fault) {
+        const int nv = pp.vhi0 - pp.vlo0 + 1;
+        const int fi = x - pp.vlo0;
+        const bool ok = fi >= 0 && fi < nv;
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+          const int g = Grp<G>::glob(c);
+          Fy[c] = ok ? mk2((T)pp.ffault[(size_t)g * nv + fi], (T)pp.ffault[(size_t)(11 + g) * nv + fi])
+                     : mk2(T(0), T(0));
+        }
+      } else {
+        P g[N];
+        if (q == dlo1) edge2<G, 1, T>(ky, true, yout_lo, WMcy, bg, g);
+        else if (!rowin) edge2<G, 1, T>(ky, false, yout_hi, WPcy_p, bg, g);
+        else riem<G, 1, T>(ky, WPcy_p, WMcy, g);
+        flux2<G, 1, T>(ky, g, Fy);
+      }
+    }
+    // row q-1: transverse correction of its x states, final x faces, update
+    if (q - 1 >= it.y0) {
+      P WMcx[N], WPcx[N];
+#pragma unroll
+      for (int c = 0; c < N; ++c) { WMcx[c] = WMx_p[c]; WPcx[c] = WPx_p[c]; }
+      adw2<G, 1, T>(ky, H1y, H1y_p, WMcx, WPcx);
+      P L[N], g[N], Fx[N], Fxh[N];
+#pragma unroll
+      for (int c = 0; c < N; ++c) L[c] = shfl_up2(WPcx[c], 1);
+      if (x == dlo0) edge2<G, 0, T>(kx, true, xout_lo, WMcx, bg, g);
+      else if (x == dhi0 + 1) edge2<G, 0, T>(kx, false, xout_hi, L, bg, g);
+      else riem<G, 0, T>(kx, L, WMcx, g);
+      flux2<G, 0, T>(kx, g, Fx);
+#pragma unroll
+      for (int c = 0; c < N; ++c) Fxh[c] = shfl_dn2(Fx[c], 1);
+      const int yr = q - 1;
+      if (col_valid && yr <= it.y1) {
+        const size_t o = fab_idx(pp, 0, x, yr);
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+          const int gg = Grp<G>::glob(c);
+          P u = mk2(pp.Uin[o + (size_t)gg * plane], pp.Uin[o + (size_t)(11 + gg) * plane]);
+          P du = padd(psub(Fxh[c], Fx[c]), psub(Fy[c], Fy_p[c]));
+          u = pfma(du, sc, u);
+          pp.Uout[o + (size_t)gg * plane] = u.x;
+          pp.Uout[o + (size_t)(11 + gg) * plane] = u.y;
+        }
+      }
+    }
+    // advance the window
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      WPy_p[c] = WPy[c]; WPcy_p[c] = WPcy[c]; H1y_p[c] = H1y[c];
+      WMx_p[c] = WMx[c]; WPx_p[c] = WPx[c]; Fy_p[c] = Fy[c];
+      sy0[c] = sy1[c]; Fy0[c] = Fy1[c];
+      W0[c] = W1[c]; W1[c] = W2[c];
+    }
+    load_row(q + 3, W2);
+  }
+}
+
+}  // namespace tmk
