@@ -277,13 +277,17 @@ def main():
         rc, info = lvl.status()
         return ms, prof, clocks, (rc, info)
 
-    # ---- mixed form (headline)
+    # ---- mixed form (headline): an uninstrumented timed pass for the value, then
+    # a second timed pass with CUDA events around every launch for the roofline
+    # (events between the fault and volume kernels serialise their overlap)
     sc, ctx, lvl = make_level(A.TMK_PREC_MIXED)
     sampler = ClockSampler() if rank == 0 else None
-    ms, prof, clocks, st = timed(lvl, sc, args.steps, args.warmup, profile=True, sampler=sampler)
+    ms, _, clocks, st = timed(lvl, sc, args.steps, args.warmup, profile=False, sampler=sampler)
     value, secs = replica_rate(cells, args.steps, ms * 1e-3, world, device="cuda")
     ms = secs * 1e3
     launches = lvl.launches_per_step() * args.steps
+    nprof_steps = min(args.steps, 200)
+    _, prof, _, _ = timed(lvl, sc, nprof_steps, 1, profile=True)
     (ex_ms, fault_ms, vol_ms, step_ms), nprof = prof
     peaks = {}
     try:
@@ -302,9 +306,12 @@ def main():
         except Exception:
             traffic = None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "volume_kernel<float,32,8>",
+                "frac": achieved / hbm_peak, "traffic": traffic,
+                "kernel": "volume update: march_kernel<float,0> (in-plane) + march_kernel<float,1> (antiplane)",
                 "algorithmic_bytes_per_launch": BYTES_PER_CELL_MIXED * cells, "peak_source": peak_src,
-                "kernel_ms": vol_ms, "fault_kernel_ms": fault_ms, "step_ms_profiled": step_ms}
+                "kernel_ms": vol_ms, "fault_kernel_ms": fault_ms, "step_ms_profiled": step_ms,
+                "timing": f"average over a second timed pass of {nprof} steps with CUDA events on the launch "
+                          "stream around each launch (serialises the fault/volume overlap of the headline pass)"}
 
     # ---- e2e through the C ABI with pinned host buffers
     ushape, bshape = lvl.patch_shapes(0)

@@ -73,17 +73,26 @@ def test_march_fp64_matches_oracle(cuda_lib, name, sc, boxes):
 
 
 @pytest.mark.parametrize("name,sc", CASES[:3], ids=[n for n, _ in CASES[:3]])
-def test_march_fp32_matches_tile_fp32(cuda_lib, name, sc):
+def test_march_fp32_is_as_accurate_as_tile_fp32(cuda_lib, name, sc):
+    """Both FP32 volume kernels round differently; each is measured against the
+    FP64 oracle and the marching kernel must be about as accurate."""
     rng = np.random.default_rng(6)
-    sc.scheme.precision = A.TMK_PREC_MIXED
     U0 = perturbed_state(sc, rng, amp_v=0.05, amp_s=1.0)
     B0 = sc.initial_B()
+    Ur, Br = U0.copy(), B0.copy()
+    t = 0.0
+    for _ in range(6):
+        assert O.level_step(sc, Ur, Br, BOXES, t, sc.dt()) == 0
+        t += sc.dt()
+    sc.scheme.precision = A.TMK_PREC_MIXED
     sc.scheme.volume_kernel = A.TMK_VOLUME_TILE
     Ut, Bt = _run_level(sc, BOXES, U0, B0, 6)
     sc.scheme.volume_kernel = A.TMK_VOLUME_MARCH
     Um, Bm = _run_level(sc, BOXES, U0, B0, 6)
     g = A.TMK_NGHOST
     vs = (slice(None), slice(g, -g), slice(g, -g))
-    # both round in FP32 (state ~1e2 MPa, increments ~1e-1): agreement to FP32 rounding of the state
-    assert rel_err(Um[vs], Ut[vs]) <= 2e-5
-    assert rel_err(Bm[:, g:-g], Bt[:, g:-g]) <= 1e-4
+    et, em = rel_err(Ut[vs], Ur[vs]), rel_err(Um[vs], Ur[vs])
+    print(f"{name}: FP32 tile {et:.2e}, FP32 march {em:.2e} (relative to the FP64 oracle)")
+    assert em <= 1e-4
+    assert em <= max(2.0 * et, 5e-6)      # both at FP32 rounding of a ~1e2 MPa state
+    assert rel_err(Bm[:, g:-g], Br[:, g:-g]) <= 1e-3

@@ -169,16 +169,32 @@ void make_tiles(std::vector<TileDev>& out, int patch, const tmk_box& v, int TX, 
 
 size_t align_up(size_t n) { return (n + 255) & ~(size_t)255; }
 
-// work items of the column-marching kernel: strips of MARCH_COLS columns by
-// runs of up to 64 rows over a valid box
-constexpr int kMarchRows = 64;
-void make_march_items(std::vector<tmk::MarchItem>& out, int patch, const tmk_box& v) {
-  for (int y0 = v.lo[1]; y0 <= v.hi[1]; y0 += kMarchRows)
-    for (int x0 = v.lo[0]; x0 <= v.hi[0]; x0 += tmk::MARCH_COLS) {
-      tmk::MarchItem m;
-      m.patch = patch; m.x0 = x0; m.y0 = y0; m.y1 = std::min(y0 + kMarchRows - 1, v.hi[1]);
-      out.push_back(m);
-    }
+// Work items of the column-marching kernel: strips of MARCH_COLS columns by
+// runs of rows.  Each warp marches one item; the runs are sized so that all
+// items of a level fit in one wave of resident warps (`slots`): a strip of a
+// patch gets max(1, floor(slots * rows / total strip-rows)) runs of equal
+// length (at least kMinRun rows, which bounds the 2-row start-up overhead).
+constexpr int kMinRun = 16;
+void make_march_items(std::vector<tmk::MarchItem>& out, const std::vector<tmk_box>& boxes, int slots) {
+  long long strip_rows = 0;
+  for (const tmk_box& v : boxes) {
+    const int ns = (v.hi[0] - v.lo[0] + tmk::MARCH_COLS) / tmk::MARCH_COLS;
+    strip_rows += (long long)ns * (v.hi[1] - v.lo[1] + 1);
+  }
+  if (slots <= 0) slots = 1;
+  for (size_t p = 0; p < boxes.size(); ++p) {
+    const tmk_box& v = boxes[p];
+    const int rows = v.hi[1] - v.lo[1] + 1;
+    int k = (int)((long long)slots * rows / std::max(1LL, strip_rows));
+    k = std::max(1, std::min(k, (rows + kMinRun - 1) / kMinRun));
+    const int run = (rows + k - 1) / k;
+    for (int y0 = v.lo[1]; y0 <= v.hi[1]; y0 += run)
+      for (int x0 = v.lo[0]; x0 <= v.hi[0]; x0 += tmk::MARCH_COLS) {
+        tmk::MarchItem m;
+        m.patch = (int)p; m.x0 = x0; m.y0 = y0; m.y1 = std::min(y0 + run - 1, v.hi[1]);
+        out.push_back(m);
+      }
+  }
 }
 
 bool uses_march(const tmk_scheme& s) {
@@ -466,7 +482,9 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
   L->march = uses_march(c->scheme) ? 1 : 0;
   if (L->march) {
     std::vector<tmk::MarchItem> items;
-    for (int p = 0; p < npatch; ++p) make_march_items(items, p, boxes[p]);
+    const int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots()
+                                                 : tmk::Launch<double>::march_slots();
+    make_march_items(items, std::vector<tmk_box>(boxes, boxes + npatch), slots);
     L->nitems = (int)items.size();
     if (dalloc(&L->ditems, items.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
     L->allocs.push_back(L->ditems);

@@ -109,90 +109,134 @@ TMK_D void xface_state(const DevParams& P, const Consts<T>& k, int f, int dlo0, 
   else riemann<0, T>(k, T(1), WPl, WMr, g);
 }
 
+// One CTA per segment of FAULT_SEG fault faces of a fault patch.  The
+// predictors of the fault row are computed once per cell and side, in
+// parallel, into shared memory; one thread per face then runs the friction
+// solves, whose Newton iterations are sequential by nature.
+constexpr int FAULT_SEG = 32;
+constexpr int FAULT_THREADS = 128;
+
 template <typename Real>
-__global__ void __launch_bounds__(128) fault_kernel(const PatchDev<Real>* __restrict__ patches,
-                                                    const int* __restrict__ fault_patches,
-                                                    const DevParams* __restrict__ params, double time,
-                                                    DevStatus* st) {
+__global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Real>* __restrict__ patches,
+                                                              const int* __restrict__ fault_patches,
+                                                              const DevParams* __restrict__ params, double time,
+                                                              DevStatus* st) {
   using T = Real;
+  constexpr int NCELL = FAULT_SEG + 2;       // cells / faces [s0-1, s0+FAULT_SEG]
+  __shared__ T xWM[2][NCELL][NSIDE], xWP[2][NCELL][NSIDE];
+  __shared__ T H1x[2][FAULT_SEG + 1][NSIDE];
+  __shared__ double sWi[NCELL][NC];
+  __shared__ double sTmp[NCELL];
+  // the volume update launched after this kernel may start now: its interior
+  // work does not read the fault buffers (it waits before it does)
+  asm volatile("griddepcontrol.launch_dependents;");
   const PatchDev<Real> p = patches[fault_patches[blockIdx.y]];
   const DevParams& P = params[p.scen];
-  const int i = p.vlo0 - 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > p.vhi0 + 1 || i < p.dlo0 || i > p.dhi0) return;
+  const int s0 = p.vlo0 + blockIdx.x * FAULT_SEG;
+  if (s0 > p.vhi0) return;
+  const int s1 = min(s0 + FAULT_SEG - 1, p.vhi0);
+  // faces whose first-pass state this segment produces: its own, plus the
+  // ghost faces lo-1 / hi+1 of the patch for the first / last segment
+  const int fa = (s0 == p.vlo0) ? max(p.vlo0 - 1, p.dlo0) : s0;
+  const int fb = (s1 == p.vhi0) ? min(p.vhi0 + 1, p.dhi0) : s1;
+  const int tid = threadIdx.x;
   Consts<T> k; k.load(P);
   const double dt = p.dt, dx = p.dx;
-  T sigy[9], sigx[9];
-  make_sig(P, dt / dx, sigy);
-  make_sig(P, dt / dx, sigx);
+  T sig[9];
+  make_sig(P, dt / dx, sig);
   const bool lim = P.prim_lim || P.char_lim;
   const int bs = p.bnx;
-  double* Bi = p.B + (i - p.blo0);
 
-  // (1) predicted states entering the fault from both sides
-  double Wi[NC];
-  fault_ypred_side(p, P, k, 0, i, sigy, lim, Wi);
-  fault_ypred_side(p, P, k, 1, i, sigy, lim, Wi + 11);
-
-  // (2) first-pass friction solve with the persistent boundary data
-  const double xc = (i + 0.5) * dx;
-  double Wg[NC];
-  for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
-  int it = 0;
-  if (P.fault_law == 1) it = rs_fault(P, Wi, Bi[10 * bs], xc - P.rs_x0, Wg);
-  else sw_fault(P, Wi, Bi[7 * bs], xc, Wg);
-  if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
-  double* first = p.first + (i - (p.vlo0 - 1));
-  for (int c = 0; c < NC; ++c) first[c * p.nfirst] = Wg[c];
-
-  if (i < p.vlo0 || i > p.vhi0) return;
-
-  // (3) half-step predicted boundary data (RSIBC/SWIBC::updateBoundary, final=false)
-  double tmpv;
-  if (P.fault_law == 1) tmpv = rs_setbnd(P, Wg, Bi, bs, 0.5 * dt, xc - P.rs_x0, 0.0, false);
-  else tmpv = sw_setbnd(P, Wg, Bi, bs, 0.5 * dt, 0.0, false);
-
-  // (4) transverse correction of the predicted fault states by the x fluxes of row j0
-  const double scale = -(1.0 / 2.0) * dt / dx;
-  for (int s = 0; s < 2; ++s) {
-    double bgd[NSIDE]; side_bg(P, s, bgd);
-    T bg[NSIDE];
-    for (int c = 0; c < NSIDE; ++c) bg[c] = (T)bgd[c];
-    T WMl[NSIDE], WPl[NSIDE], WMc[NSIDE], WPc[NSIDE], WMr[NSIDE], WPr[NSIDE];
-    if (i - 1 >= p.dlo0) fault_xpred_side(p, P, k, s, i - 1, sigx, WMl, WPl);
-    fault_xpred_side(p, P, k, s, i, sigx, WMc, WPc);
-    if (i + 1 <= p.dhi0) fault_xpred_side(p, P, k, s, i + 1, sigx, WMr, WPr);
-    T glo[NSIDE], ghi[NSIDE];
-    xface_state<T>(P, k, i, p.dlo0, p.dhi0, WPl, WMc, bg, glo);
-    xface_state<T>(P, k, i + 1, p.dlo0, p.dhi0, WPc, WMr, bg, ghi);
-    T q[NSIDE];
-    for (int c = 0; c < NSIDE; ++c) q[c] = (T)Wi[11 * s + c];
-    adwdx_add<0, T>(k, T(1), (T)scale, ghi, glo, q);
-    for (int c = 0; c < NSIDE; ++c) Wi[11 * s + c] = (double)q[c];
+  // (A) x predictors of the fault-row cells [s0-1, s1+1] and y predictors of the
+  //     states entering the fault faces [fa, fb], both sides
+  for (int t = tid; t < 4 * NCELL; t += FAULT_THREADS) {
+    const int kind = t / (2 * NCELL), s = (t / NCELL) & 1, ci = t % NCELL;
+    const int c = s0 - 1 + ci;
+    if (kind == 0) {
+      if (c >= p.dlo0 && c <= p.dhi0 && c <= s1 + 1) {
+        T WM[NSIDE], WP[NSIDE];
+        fault_xpred_side(p, P, k, s, c, sig, WM, WP);
+        for (int q = 0; q < NSIDE; ++q) { xWM[s][ci][q] = WM[q]; xWP[s][ci][q] = WP[q]; }
+      }
+    } else if (c >= fa && c <= fb) {
+      fault_ypred_side(p, P, k, s, c, sig, lim, &sWi[ci][11 * s]);
+    }
   }
+  __syncthreads();
 
-  // (5) final friction solve with the predicted boundary data
-  for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
-  it = 0;
-  if (P.fault_law == 1) it = rs_fault(P, Wi, tmpv, xc - P.rs_x0, Wg);
-  else sw_fault(P, Wi, tmpv, xc, Wg);
-  if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
-
-  // (6) y fluxes through the fault face (GETFLUXF, FP64)
-  Consts<double> kd; kd.load(P);
-  double F[NSIDE];
-  double* ff = p.ffault + (i - p.vlo0);
-  const int nv = p.vhi0 - p.vlo0 + 1;
-  flux<1, double>(kd, 1.0, Wg, F);
-  for (int c = 0; c < NSIDE; ++c) ff[c * nv] = F[c];
-  flux<1, double>(kd, -1.0, Wg + 11, F);
-  for (int c = 0; c < NSIDE; ++c) ff[(11 + c) * nv] = F[c];
-
-  // (7) boundary-data update with the final fault state (final=true, t+dt)
-  if (P.fault_law == 1) {
-    double np = rs_setbnd(P, Wg, Bi, bs, dt, xc - P.rs_x0, time + dt, true);
-    if (isnan(np)) report(st, ST_NAN, (long long)i);
+  if (tid < NCELL) {
+    // (B) first-pass friction solve with the persistent boundary data, and the
+    //     half-step predicted boundary data (updateBoundary, final=false)
+    const int i = s0 - 1 + tid;
+    if (i >= fa && i <= fb) {
+      double* Bi = p.B + (i - p.blo0);
+      const double xc = (i + 0.5) * dx;
+      double Wg[NC];
+      for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
+      int it = 0;
+      if (P.fault_law == 1) it = rs_fault(P, sWi[tid], Bi[10 * bs], xc - P.rs_x0, Wg);
+      else sw_fault(P, sWi[tid], Bi[7 * bs], xc, Wg);
+      if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
+      double* first = p.first + (i - (p.vlo0 - 1));
+      for (int c = 0; c < NC; ++c) first[c * p.nfirst] = Wg[c];
+      if (i >= s0 && i <= s1) {
+        if (P.fault_law == 1) sTmp[tid] = rs_setbnd(P, Wg, Bi, bs, 0.5 * dt, xc - P.rs_x0, 0.0, false);
+        else sTmp[tid] = sw_setbnd(P, Wg, Bi, bs, 0.5 * dt, 0.0, false);
+      }
+    }
   } else {
-    sw_setbnd(P, Wg, Bi, bs, dt, time + dt, true);
+    // (C) first-pass x faces [s0, s1+1] of the fault row, both sides
+    for (int t = tid - NCELL; t < 2 * (FAULT_SEG + 1); t += FAULT_THREADS - NCELL) {
+      const int s = t / (FAULT_SEG + 1), fi = t % (FAULT_SEG + 1);
+      const int f = s0 + fi;
+      if (f > s1 + 1) continue;
+      double bgd[NSIDE]; side_bg(P, s, bgd);
+      T bg[NSIDE];
+      for (int c = 0; c < NSIDE; ++c) bg[c] = (T)bgd[c];
+      T g[NSIDE];
+      xface_state<T>(P, k, f, p.dlo0, p.dhi0, xWP[s][fi], xWM[s][fi + 1], bg, g);
+      for (int q = 0; q < NSIDE; ++q) H1x[s][fi][q] = g[q];
+    }
+  }
+  __syncthreads();
+
+  if (tid <= s1 - s0) {
+    const int i = s0 + tid, ci = tid + 1;
+    double* Bi = p.B + (i - p.blo0);
+    const double xc = (i + 0.5) * dx;
+    // (D) transverse correction of the fault states by the x fluxes of the row
+    const double scale = -(1.0 / 2.0) * dt / dx;
+    double Wi[NC];
+    for (int c = 0; c < NC; ++c) Wi[c] = sWi[ci][c];
+    for (int s = 0; s < 2; ++s) {
+      T q[NSIDE];
+      for (int c = 0; c < NSIDE; ++c) q[c] = (T)Wi[11 * s + c];
+      adwdx_add<0, T>(k, T(1), (T)scale, H1x[s][tid + 1], H1x[s][tid], q);
+      for (int c = 0; c < NSIDE; ++c) Wi[11 * s + c] = (double)q[c];
+    }
+    // (E) final friction solve with the predicted boundary data
+    double Wg[NC];
+    for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
+    int it = 0;
+    if (P.fault_law == 1) it = rs_fault(P, Wi, sTmp[ci], xc - P.rs_x0, Wg);
+    else sw_fault(P, Wi, sTmp[ci], xc, Wg);
+    if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
+    // (F) y fluxes through the fault face (GETFLUXF, FP64)
+    Consts<double> kd; kd.load(P);
+    double F[NSIDE];
+    double* ff = p.ffault + (i - p.vlo0);
+    const int nv = p.vhi0 - p.vlo0 + 1;
+    flux<1, double>(kd, 1.0, Wg, F);
+    for (int c = 0; c < NSIDE; ++c) ff[c * nv] = F[c];
+    flux<1, double>(kd, -1.0, Wg + 11, F);
+    for (int c = 0; c < NSIDE; ++c) ff[(11 + c) * nv] = F[c];
+    // (G) boundary-data update with the final fault state (final=true, t+dt)
+    if (P.fault_law == 1) {
+      double np = rs_setbnd(P, Wg, Bi, bs, dt, xc - P.rs_x0, time + dt, true);
+      if (isnan(np)) report(st, ST_NAN, (long long)i);
+    } else {
+      sw_setbnd(P, Wg, Bi, bs, dt, time + dt, true);
+    }
   }
 }
 

@@ -28,6 +28,8 @@ struct Launch {
   // column-marching volume update: one warp per item, both component groups
   static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* items, int nitems,
                            const DevParams* params, cudaStream_t s);
+  // warps of the marching kernel that are resident at once on the current device
+  static int march_slots();
 };
 
 // FP64 <-> Real conversion of a FAB on the device

@@ -12,8 +12,8 @@ struct LaunchImpl {
   static cudaError_t fault(const PatchDev<Real>* patches, const int* fp, int nfault, int max_faces,
                            const DevParams* params, double time, DevStatus* st, cudaStream_t s) {
     if (nfault <= 0) return cudaSuccess;
-    dim3 grid((max_faces + 2 + 127) / 128, nfault);
-    fault_kernel<Real><<<grid, 128, 0, s>>>(patches, fp, params, time, st);
+    dim3 grid((max_faces + FAULT_SEG - 1) / FAULT_SEG, nfault);
+    fault_kernel<Real><<<grid, FAULT_THREADS, 0, s>>>(patches, fp, params, time, st);
     return cudaGetLastError();
   }
   static size_t smem() { return sizeof(VolSmem<Real, TX_, TY_>); }
@@ -42,11 +42,48 @@ struct LaunchImpl {
                            const DevParams* params, cudaStream_t s) {
     if (nitems <= 0) return cudaSuccess;
     const int blocks = (nitems + MARCH_WARPS - 1) / MARCH_WARPS;
-    march_kernel<Real, 0><<<blocks, 32 * MARCH_WARPS, 0, s>>>(patches, items, nitems, params);
-    cudaError_t e = cudaGetLastError();
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e0 = cudaFuncSetAttribute(march_kernel<Real, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)march_smem_bytes<Real, 0>());
+      cudaError_t e1 = cudaFuncSetAttribute(march_kernel<Real, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)march_smem_bytes<Real, 1>());
+      if (e0 != cudaSuccess) return e0;
+      if (e1 != cudaSuccess) return e1;
+      configured = true;
+    }
+    // programmatic dependent launch: each group's kernel may start while the
+    // kernel before it in the stream is still running (see march_kernel)
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(32 * MARCH_WARPS);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.dynamicSmemBytes = march_smem_bytes<Real, 0>();
+    cudaError_t e = cudaLaunchKernelEx(&cfg, march_kernel<Real, 0>, patches, items, nitems, params);
     if (e != cudaSuccess) return e;
-    march_kernel<Real, 1><<<blocks, 32 * MARCH_WARPS, 0, s>>>(patches, items, nitems, params);
-    return cudaGetLastError();
+    cfg.dynamicSmemBytes = march_smem_bytes<Real, 1>();
+    return cudaLaunchKernelEx(&cfg, march_kernel<Real, 1>, patches, items, nitems, params);
+  }
+  static int march_slots() {
+    int dev = 0, sms = 0, b0 = 0, b1 = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return 0;
+    cudaFuncSetAttribute(march_kernel<Real, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)march_smem_bytes<Real, 0>());
+    cudaFuncSetAttribute(march_kernel<Real, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)march_smem_bytes<Real, 1>());
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, march_kernel<Real, 0>, 32 * MARCH_WARPS,
+                                                      march_smem_bytes<Real, 0>()) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, march_kernel<Real, 1>, 32 * MARCH_WARPS,
+                                                      march_smem_bytes<Real, 1>()) != cudaSuccess)
+      return 0;
+    return std::min(b0, b1) * sms * MARCH_WARPS;
   }
 };
 
@@ -73,4 +110,5 @@ struct LaunchImpl {
                                               const DevParams* prm, cudaStream_t s) {                       \
     return LaunchImpl<REAL, TXV, TYV, NTV>::march(p, it, n, prm, s);                                         \
   }                                                                                                          \
+  template <> int Launch<REAL>::march_slots() { return LaunchImpl<REAL, TXV, TYV, NTV>::march_slots(); }     \
   }

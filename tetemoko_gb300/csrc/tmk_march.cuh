@@ -86,18 +86,21 @@ template <typename T>
 struct MK {
   using P = typename PairOf<T>::P;
   P ZpE, ZsE;          // characteristic w = s +- ZE v (ZE = rv Z)
+  P nZpE, nZsE;        // -ZE
   P hZpE, hZsE;        // synthesis v = (w- - w+) * rv/(2Z)
-  P half, r;           // 1/2, lam/(lam+2G)
+  P half, r, nr;       // 1/2, lam/(lam+2G), -lam/(lam+2G)
   P aP, bP, aS, bS;    // PPM tracing coefficients of the P and S speeds
   P f_irho, f_l2g, f_lam, f_G;   // GETFLUXF: -rv * {1/rho, lam+2G, lam, G}
   P a_irho, a_l2g, a_lam, a_G;   // GETADWDXF: -rv*scale * {...}
   TMK_D void load(const DevParams& p, int D, double dtdx, double scale) {
     const T s2 = (D == 1) ? T(-1) : T(1);       // rv of side 2
     ZpE = mk2((T)p.Zp, (T)(s2 * p.Zp)); ZsE = mk2((T)p.Zs, (T)(s2 * p.Zs));
+    nZpE = mk2((T)-p.Zp, (T)(-s2 * p.Zp)); nZsE = mk2((T)-p.Zs, (T)(-s2 * p.Zs));
     hZpE = mk2((T)(0.5 / p.Zp), (T)(s2 * 0.5 / p.Zp)); hZsE = mk2((T)(0.5 / p.Zs), (T)(s2 * 0.5 / p.Zs));
     half = mk2(T(0.5), T(0.5));
     const T rr = (T)(p.lam / (p.lam + 2.0 * p.G));
     r = mk2(rr, rr);
+    nr = mk2(-rr, -rr);
     const double sp = p.cp * dtdx, ss = p.cs * dtdx;
     const T ap = (T)((1.0 - sp) * (1.0 - sp)), bp = (T)(sp * sp - sp);
     const T as = (T)((1.0 - ss) * (1.0 - ss)), bs = (T)(ss * ss - ss);
@@ -114,11 +117,43 @@ struct MK {
   }
 };
 
-// per-half scalar stages on pairs
-template <typename P> TMK_D P slope2(P wm, P w0, P wp, bool hasL, bool hasR, bool limit) {
-  return mk2(vl_slope(wm.x, w0.x, wp.x, hasL, hasR, limit), vl_slope(wm.y, w0.y, wp.y, hasL, hasR, limit));
+// ---- limiters on pairs (differences packed, the nonlinear part per half)
+TMK_D float copysg(float a, float b) { return copysignf(a, b); }
+TMK_D double copysg(double a, double b) { return copysign(a, b); }
+
+// van Leer: sign(dc) min(|dc|, 2|dl|, 2|dr|) when dl dr > 0, else 0
+template <typename T> TMK_D T vl1(T dl, T dr, T dc, T prod) {
+  const T t = fmin(fabs(dc), T(2) * fmin(fabs(dl), fabs(dr)));
+  return prod > T(0) ? copysg(t, dc) : T(0);
 }
-template <typename P> TMK_D void limit2(P& m, P& p) { ppm_limit(m.x, p.x); ppm_limit(m.y, p.y); }
+
+// Limited slope of the middle value.  A missing neighbour (outside the
+// domain) is replaced by the reflection 2 w0 - w_other, which turns the
+// centred formula into the one-sided difference the reference uses there.
+template <typename P> TMK_D P slope2(P wm, P w0, P wp, bool hasL, bool hasR, bool limit) {
+  using T = decltype(wm.x);
+  const P two = mk2(T(2), T(2)), half = mk2(T(0.5), T(0.5));
+  if (!hasL) wm = psub(pmul(two, w0), wp);
+  if (!hasR) wp = psub(pmul(two, w0), wm);
+  const P dl = psub(w0, wm), dr = psub(wp, w0);
+  const P dc = pmul(half, padd(dl, dr));
+  if (!limit) return dc;
+  const P prod = pmul(dl, dr);
+  return mk2(vl1(dl.x, dr.x, dc.x, prod.x), vl1(dl.y, dr.y, dc.y, prod.y));
+}
+
+// PPM limiter (Colella & Woodward 1984 eq. 1.10): both deltas zero at an
+// extremum, otherwise each clipped to twice the other's magnitude.
+template <typename T> TMK_D T clampabs(T v, T b) { return fmin(fmax(v, -fabs(b)), fabs(b)); }
+template <typename P> TMK_D void limit2(P& m, P& p) {
+  using T = decltype(m.x);
+  const P two = mk2(T(2), T(2));
+  const P m2 = pmul(two, m), p2 = pmul(two, p), prod = pmul(m, p);
+  const T amx = clampabs(m.x, p2.x), apx = clampabs(p.x, m2.x);
+  const T amy = clampabs(m.y, p2.y), apy = clampabs(p.y, m2.y);
+  m.x = prod.x < T(0) ? amx : T(0); p.x = prod.x < T(0) ? apx : T(0);
+  m.y = prod.y < T(0) ? amy : T(0); p.y = prod.y < T(0) ? apy : T(0);
+}
 
 // interior PPM face value between cells a (lower) and b: (a+b)/2 - (sb - sa)/6
 template <typename T, typename P> TMK_D P face2(P a, P b, P sa, P sb) {
@@ -141,8 +176,8 @@ TMK_D void predict(const MK<T>& k, const typename PairOf<T>::P* w, typename Pair
   }
   // S wave pair
   {
-    P nm = pfma(k.ZsE, dm[R::vS], dm[R::sS]), pm = pfma(pneg(k.ZsE), dm[R::vS], dm[R::sS]);
-    P np = pfma(k.ZsE, dp[R::vS], dp[R::sS]), pp = pfma(pneg(k.ZsE), dp[R::vS], dp[R::sS]);
+    P nm = pfma(k.ZsE, dm[R::vS], dm[R::sS]), pm = pfma(k.nZsE, dm[R::vS], dm[R::sS]);
+    P np = pfma(k.ZsE, dp[R::vS], dp[R::sS]), pp = pfma(k.nZsE, dp[R::vS], dp[R::sS]);
     if (clim) { limit2(nm, np); limit2(pm, pp); }
     P nmt = pfma(k.aS, nm, pmul(k.bS, np));       // w- traced to the lo face
     P ppt = pfma(k.aS, pp, pmul(k.bS, pm));       // w+ traced to the hi face
@@ -152,18 +187,18 @@ TMK_D void predict(const MK<T>& k, const typename PairOf<T>::P* w, typename Pair
     WP[R::vS] = padd(w[R::vS], pmul(k.hZsE, psub(np, ppt)));
   }
   if constexpr (R::hasP) {
-    P nm = pfma(k.ZpE, dm[R::vP], dm[R::sP]), pm = pfma(pneg(k.ZpE), dm[R::vP], dm[R::sP]);
-    P np = pfma(k.ZpE, dp[R::vP], dp[R::sP]), pp = pfma(pneg(k.ZpE), dp[R::vP], dp[R::sP]);
+    P nm = pfma(k.ZpE, dm[R::vP], dm[R::sP]), pm = pfma(k.nZpE, dm[R::vP], dm[R::sP]);
+    P np = pfma(k.ZpE, dp[R::vP], dp[R::sP]), pp = pfma(k.nZpE, dp[R::vP], dp[R::sP]);
     P z0m = dm[R::zc0], z0p = dp[R::zc0], z1m = dm[R::zc1], z1p = dp[R::zc1];
     if (clim) {
       limit2(nm, np); limit2(pm, pp);
       P sPm = dm[R::sP], sPp = dp[R::sP];
-      z0m = pfma(pneg(k.r), sPm, z0m); z0p = pfma(pneg(k.r), sPp, z0p);
-      z1m = pfma(pneg(k.r), sPm, z1m); z1p = pfma(pneg(k.r), sPp, z1p);
+      z0m = pfma(k.nr, sPm, z0m); z0p = pfma(k.nr, sPp, z0p);
+      z1m = pfma(k.nr, sPm, z1m); z1p = pfma(k.nr, sPp, z1p);
       limit2(z0m, z0p); limit2(z1m, z1p);
     } else {
-      z0m = pfma(pneg(k.r), dm[R::sP], z0m); z0p = pfma(pneg(k.r), dp[R::sP], z0p);
-      z1m = pfma(pneg(k.r), dm[R::sP], z1m); z1p = pfma(pneg(k.r), dp[R::sP], z1p);
+      z0m = pfma(k.nr, dm[R::sP], z0m); z0p = pfma(k.nr, dp[R::sP], z0p);
+      z1m = pfma(k.nr, dm[R::sP], z1m); z1p = pfma(k.nr, dp[R::sP], z1p);
     }
     P nmt = pfma(k.aP, nm, pmul(k.bP, np));
     P ppt = pfma(k.aP, pp, pmul(k.bP, pm));
@@ -192,19 +227,19 @@ TMK_D void riem(const MK<T>& k, const typename PairOf<T>::P* L, const typename P
   using P = typename PairOf<T>::P;
   using R = Role<G, D>;
   {
-    P wpos = pfma(pneg(k.ZsE), L[R::vS], L[R::sS]);
+    P wpos = pfma(k.nZsE, L[R::vS], L[R::sS]);
     P wneg = pfma(k.ZsE, Rt[R::vS], Rt[R::sS]);
     g[R::sS] = pmul(k.half, padd(wneg, wpos));
     g[R::vS] = pmul(k.hZsE, psub(wneg, wpos));
   }
   if constexpr (R::hasP) {
-    P wpos = pfma(pneg(k.ZpE), L[R::vP], L[R::sP]);
+    P wpos = pfma(k.nZpE, L[R::vP], L[R::sP]);
     P wneg = pfma(k.ZpE, Rt[R::vP], Rt[R::sP]);
     P s = pmul(k.half, padd(wneg, wpos));
     g[R::sP] = s;
     g[R::vP] = pmul(k.hZpE, psub(wneg, wpos));
-    P zr0 = pfma(pneg(k.r), Rt[R::sP], Rt[R::zc0]), zl0 = pfma(pneg(k.r), L[R::sP], L[R::zc0]);
-    P zr1 = pfma(pneg(k.r), Rt[R::sP], Rt[R::zc1]), zl1 = pfma(pneg(k.r), L[R::sP], L[R::zc1]);
+    P zr0 = pfma(k.nr, Rt[R::sP], Rt[R::zc0]), zl0 = pfma(k.nr, L[R::sP], L[R::zc0]);
+    P zr1 = pfma(k.nr, Rt[R::sP], Rt[R::zc1]), zl1 = pfma(k.nr, L[R::sP], L[R::zc1]);
     g[R::zc0] = pfma(k.r, s, pmul(k.half, padd(zr0, zl0)));
     g[R::zc1] = pfma(k.r, s, pmul(k.half, padd(zr1, zl1)));
   }
@@ -222,9 +257,9 @@ TMK_D void edge2(const MK<T>& k, bool lo, bool outflow, const typename PairOf<T>
     P wneg, wpos;
     if (lo) {
       wneg = pfma(k.ZsE, Wi[R::vS], Wi[R::sS]);
-      wpos = outflow ? pfma(pneg(k.ZsE), bg[R::vS], bg[R::sS]) : pneg(wneg);
+      wpos = outflow ? pfma(k.nZsE, bg[R::vS], bg[R::sS]) : pneg(wneg);
     } else {
-      wpos = pfma(pneg(k.ZsE), Wi[R::vS], Wi[R::sS]);
+      wpos = pfma(k.nZsE, Wi[R::vS], Wi[R::sS]);
       wneg = outflow ? pfma(k.ZsE, bg[R::vS], bg[R::sS]) : pneg(wpos);
     }
     g[R::sS] = pmul(k.half, padd(wneg, wpos));
@@ -234,15 +269,15 @@ TMK_D void edge2(const MK<T>& k, bool lo, bool outflow, const typename PairOf<T>
     P wneg, wpos;
     if (lo) {
       wneg = pfma(k.ZpE, Wi[R::vP], Wi[R::sP]);
-      wpos = outflow ? pfma(pneg(k.ZpE), bg[R::vP], bg[R::sP]) : pneg(wneg);
+      wpos = outflow ? pfma(k.nZpE, bg[R::vP], bg[R::sP]) : pneg(wneg);
     } else {
-      wpos = pfma(pneg(k.ZpE), Wi[R::vP], Wi[R::sP]);
+      wpos = pfma(k.nZpE, Wi[R::vP], Wi[R::sP]);
       wneg = outflow ? pfma(k.ZpE, bg[R::vP], bg[R::sP]) : pneg(wpos);
     }
     P s = pmul(k.half, padd(wneg, wpos));
     g[R::sP] = s;
     g[R::vP] = pmul(k.hZpE, psub(wneg, wpos));
-    P shf = pmul(pneg(k.r), psub(Wi[R::vP], s));
+    P shf = pmul(k.nr, psub(Wi[R::vP], s));
     g[R::zc0] = padd(Wi[R::zc0], shf);
     g[R::zc1] = padd(Wi[R::zc1], shf);
   }
@@ -294,15 +329,33 @@ struct MarchItem { int patch, x0, y0, y1; };
 constexpr int MARCH_COLS = 26;   // updated columns per warp
 constexpr int MARCH_WARPS = 4;   // warps per CTA
 
+// Number of per-row vectors a lane keeps in shared memory instead of registers
+// (the x states of row q-1, the first-pass y face q-1, the final y flux q-1
+// and the old state of row q-1).
+constexpr int MARCH_SMEM_VECS = 5;
 template <typename T, int G>
-__global__ void __launch_bounds__(32 * MARCH_WARPS) march_kernel(const PatchDev<T>* __restrict__ patches,
+constexpr size_t march_smem_bytes() {
+  return (size_t)MARCH_WARPS * MARCH_SMEM_VECS * Grp<G>::N * 32 * sizeof(typename PairOf<T>::P);
+}
+
+template <typename T, int G>
+__global__ void __launch_bounds__(32 * MARCH_WARPS, 2) march_kernel(const PatchDev<T>* __restrict__ patches,
                                                                  const MarchItem* __restrict__ items, int nitems,
                                                                  const DevParams* __restrict__ params) {
   using P = typename PairOf<T>::P;
   constexpr int N = Grp<G>::N;
+  extern __shared__ __align__(16) unsigned char march_smem[];
+  P* const carry = reinterpret_cast<P*>(march_smem) + (size_t)(threadIdx.x >> 5) * MARCH_SMEM_VECS * N * 32;
   const int wid = blockIdx.x * MARCH_WARPS + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (wid >= nitems) return;
+  // a later kernel of the step may be scheduled now; every warp waits for the
+  // kernel before it (the fault kernel or the other component group) before
+  // it reads the fault buffers or exits, so kernels still complete in order
+  asm volatile("griddepcontrol.launch_dependents;");
+  if (wid >= nitems) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    return;
+  }
   const MarchItem it = items[wid];
   const PatchDev<T>& pp = patches[it.patch];
   const DevParams& Pm = params[pp.scen];
@@ -323,6 +376,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS) march_kernel(const PatchDev<
   for (int c = 0; c < N; ++c) bg[c] = mk2((T)Pm.bg[Grp<G>::glob(c)], (T)Pm.bg[11 + Grp<G>::glob(c)]);
   const bool xout_lo = Pm.bc[0] == 0, xout_hi = Pm.bc[1] == 0, yout_lo = Pm.bc[2] == 0, yout_hi = Pm.bc[3] == 0;
   const bool fault = pp.fault != 0;
+  if (fault && it.y0 == dlo1) asm volatile("griddepcontrol.wait;" ::: "memory");
   const bool col_valid = x >= it.x0 && x < it.x0 + MARCH_COLS && x >= pp.vlo0 && x <= pp.vhi0;
   const size_t plane = (size_t)pp.anx * pp.any;
 
@@ -390,11 +444,24 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS) march_kernel(const PatchDev<
       }
     }
   }
-  // carried state of row q-1
-  P WPy_p[N], WPcy_p[N], H1y_p[N], WMx_p[N], WPx_p[N], Fy_p[N];
+  // carried state of row q-1: WPy_p, WPcy_p in registers; the x states of row
+  // q-1 (WMx, WPx), the first-pass face q-1 (H1y) and the final flux q-1 (Fy)
+  // in this lane's own shared-memory slots (vector v, component c)
+  P WPy_p[N], WPcy_p[N];
+  auto cput = [&](int v, const P* a) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) carry[(v * N + c) * 32 + lane] = a[c];
+  };
+  auto cget = [&](int v, P* a) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) a[c] = carry[(v * N + c) * 32 + lane];
+  };
+  enum { kWMx = 0, kWPx = 1, kH1y = 2, kFy = 3, kWold = 4 };
 
   for (int q = q_s; q <= q_e; ++q) {
     const bool rowin = q <= dhi1;
+    P Wn[N];
+    load_row(q + 3, Wn);     // next row in flight while this one is computed
     P WMy[N], WPy[N], WMcy[N], WPcy[N], WMx[N], WPx[N], H1lo[N], H1hi[N];
     P sy1[N], Fy1[N];
     if (rowin) {
@@ -468,9 +535,13 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS) march_kernel(const PatchDev<
     // row q-1: transverse correction of its x states, final x faces, update
     if (q - 1 >= it.y0) {
       P WMcx[N], WPcx[N];
-#pragma unroll
-      for (int c = 0; c < N; ++c) { WMcx[c] = WMx_p[c]; WPcx[c] = WPx_p[c]; }
-      adw2<G, 1, T>(ky, H1y, H1y_p, WMcx, WPcx);
+      {
+        P H1y_p[N];
+        cget(kWMx, WMcx);
+        cget(kWPx, WPcx);
+        cget(kH1y, H1y_p);
+        adw2<G, 1, T>(ky, H1y, H1y_p, WMcx, WPcx);
+      }
       P L[N], g[N], Fx[N], Fxh[N];
 #pragma unroll
       for (int c = 0; c < N; ++c) L[c] = shfl_up2(WPcx[c], 1);
@@ -481,29 +552,35 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS) march_kernel(const PatchDev<
 #pragma unroll
       for (int c = 0; c < N; ++c) Fxh[c] = shfl_dn2(Fx[c], 1);
       const int yr = q - 1;
+      P Fy_p[N], Wold[N];
+      cget(kFy, Fy_p);
+      cget(kWold, Wold);
       if (col_valid && yr <= it.y1) {
         const size_t o = fab_idx(pp, 0, x, yr);
 #pragma unroll
         for (int c = 0; c < N; ++c) {
           const int gg = Grp<G>::glob(c);
-          P u = mk2(pp.Uin[o + (size_t)gg * plane], pp.Uin[o + (size_t)(11 + gg) * plane]);
           P du = padd(psub(Fxh[c], Fx[c]), psub(Fy[c], Fy_p[c]));
-          u = pfma(du, sc, u);
+          P u = pfma(du, sc, Wold[c]);
           pp.Uout[o + (size_t)gg * plane] = u.x;
           pp.Uout[o + (size_t)(11 + gg) * plane] = u.y;
         }
       }
     }
     // advance the window
+    cput(kWMx, WMx);
+    cput(kWPx, WPx);
+    cput(kH1y, H1y);
+    cput(kFy, Fy);
+    cput(kWold, W0);
 #pragma unroll
     for (int c = 0; c < N; ++c) {
-      WPy_p[c] = WPy[c]; WPcy_p[c] = WPcy[c]; H1y_p[c] = H1y[c];
-      WMx_p[c] = WMx[c]; WPx_p[c] = WPx[c]; Fy_p[c] = Fy[c];
+      WPy_p[c] = WPy[c]; WPcy_p[c] = WPcy[c];
       sy0[c] = sy1[c]; Fy0[c] = Fy1[c];
-      W0[c] = W1[c]; W1[c] = W2[c];
+      W0[c] = W1[c]; W1[c] = W2[c]; W2[c] = Wn[c];
     }
-    load_row(q + 3, W2);
   }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 }  // namespace tmk
