@@ -46,8 +46,49 @@ TMK_D int rs_newton(const DevParams& P, double phi, double psi, double sn, doubl
   return it;
 }
 
+// The friction equation of RSNEWTON solved for z = asinh(beta V) instead of V:
+//   f(z) = alpha z + (eta/beta) sinh z - phi = 0,  V = sinh(z)/beta, tau = alpha z.
+// f is smooth and monotone in z on the same bracket (0, asinh(beta phi/Zs)], so
+// Newton converges in a few steps where the iteration in V creeps up through
+// tens of decades.  As in the reference, a root beyond the bracket's upper
+// end V = phi/Zs yields that end.  Used by the mixed form; FP64 arithmetic.
+TMK_D int rs_newton_z(const DevParams& P, double phi, double psi, double sn, double c_rs_a, double& V,
+                      double& tau) {
+  const double atolG = 2.220446049250313e-16 * 1e4;
+  const double alpha = sn * c_rs_a;
+  const double beta = exp(psi / c_rs_a) / (2.0 * P.rs_V0);
+  const double eta = 0.5 * P.Zs;
+  const double Vmax = phi / P.Zs;
+  if (!(alpha > 0.0) || !(beta > 0.0) || !(beta < 1e300) || !(phi > 0.0)) return rs_newton(P, phi, psi, sn, c_rs_a, V, tau);
+  const double zmax = asinh(beta * Vmax);
+  if (alpha * zmax + eta * Vmax - phi <= 0.0) {     // root beyond the reference's bracket
+    V = Vmax;
+    tau = alpha * zmax;
+    return RS_IMAX + 1;
+  }
+  const double c = eta / beta;
+  double z = fmin(phi / alpha, zmax);
+  int it;
+  for (it = 1; it <= RS_IMAX; ++it) {
+    const double e = exp(z), ie = 1.0 / e;
+    const double sh = 0.5 * (e - ie), ch = 0.5 * (e + ie);
+    const double f = alpha * z + c * sh - phi;
+    const double dz = -f / (alpha + c * ch);
+    double zn = z + dz;
+    if (zn < 0.0) zn = 0.5 * z;
+    if (zn > zmax) zn = 0.5 * (z + zmax);
+    z = zn;
+    if (fabs(f) <= atolG || fabs(dz) <= 1e-15 * fmax(1.0, z)) break;
+  }
+  const double e = exp(z);
+  V = 0.5 * (e - 1.0 / e) / beta;
+  tau = alpha * z;
+  return it;
+}
+
 // RSFAULTBCF (ibcLinElast/RSIBCF.ChF:158-323) at one fault face; Wi, Wg: 22 comps.
-TMK_D int rs_fault(const DevParams& P, const double* Wi, double psi, double x, double* Wg) {
+// zsolve selects rs_newton_z (mixed form) instead of the reference's RSNEWTON.
+TMK_D int rs_fault(const DevParams& P, const double* Wi, double psi, double x, double* Wg, bool zsolve = false) {
   const double Zs = P.Zs, Zp = P.Zp, lam = P.lam, G = P.G;
   double vx1 = Wi[0], vy1 = Wi[1], vz1 = Wi[2], sxx1 = Wi[3], syy1 = Wi[4], szz1 = Wi[5];
   double sxy1 = Wi[6], sxz1 = Wi[7], syz1 = Wi[8];
@@ -72,7 +113,7 @@ TMK_D int rs_fault(const DevParams& P, const double* Wi, double psi, double x, d
   double c_ramp = fmin(1.0, fmax(0.0, (x - P.ramp_x) / P.ramp_w));
   double c_rs_a = P.rs_a + P.ramp_a * c_ramp;
   double tau;
-  int it = rs_newton(P, phi, psi, -syy1, c_rs_a, V, tau);
+  int it = zsolve ? rs_newton_z(P, phi, psi, -syy1, c_rs_a, V, tau) : rs_newton(P, phi, psi, -syy1, c_rs_a, V, tau);
   sxy1 = (phi_xy / phi) * tau - tau_xy_0;
   syz1 = (phi_yz / phi) * tau - tau_yz_0;
   double Vx = (phi_xy / phi) * V;

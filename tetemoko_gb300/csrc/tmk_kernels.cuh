@@ -122,6 +122,9 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
                                                               const DevParams* __restrict__ params, double time,
                                                               DevStatus* st) {
   using T = Real;
+  // the mixed form solves the friction equation in z = asinh(beta V); the FP64
+  // form keeps the reference's Newton iteration on V
+  constexpr bool kZSolve = !std::is_same<Real, double>::value;
   constexpr int NCELL = FAULT_SEG + 2;       // cells / faces [s0-1, s0+FAULT_SEG]
   __shared__ T xWM[2][NCELL][NSIDE], xWP[2][NCELL][NSIDE];
   __shared__ T H1x[2][FAULT_SEG + 1][NSIDE];
@@ -174,7 +177,7 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
       double Wg[NC];
       for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
       int it = 0;
-      if (P.fault_law == 1) it = rs_fault(P, sWi[tid], Bi[10 * bs], xc - P.rs_x0, Wg);
+      if (P.fault_law == 1) it = rs_fault(P, sWi[tid], Bi[10 * bs], xc - P.rs_x0, Wg, kZSolve);
       else sw_fault(P, sWi[tid], Bi[7 * bs], xc, Wg);
       if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
       double* first = p.first + (i - (p.vlo0 - 1));
@@ -218,7 +221,7 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
     double Wg[NC];
     for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
     int it = 0;
-    if (P.fault_law == 1) it = rs_fault(P, Wi, sTmp[ci], xc - P.rs_x0, Wg);
+    if (P.fault_law == 1) it = rs_fault(P, Wi, sTmp[ci], xc - P.rs_x0, Wg, kZSolve);
     else sw_fault(P, Wi, sTmp[ci], xc, Wg);
     if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
     // (F) y fluxes through the fault face (GETFLUXF, FP64)
