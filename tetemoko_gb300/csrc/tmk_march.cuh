@@ -333,19 +333,34 @@ constexpr int MARCH_WARPS = 4;   // warps per CTA
 // (the x states of row q-1, the first-pass y face q-1, the final y flux q-1
 // and the old state of row q-1).
 constexpr int MARCH_SMEM_VECS = 5;
+// Rows q..q+2 of the rolling window plus the row in flight live in a per-warp
+// ring of shared memory filled by cp.async; slot = row & 3.
+constexpr int MARCH_RING = 4;
 template <typename T, int G>
 constexpr size_t march_smem_bytes() {
-  return (size_t)MARCH_WARPS * MARCH_SMEM_VECS * Grp<G>::N * 32 * sizeof(typename PairOf<T>::P);
+  return (size_t)MARCH_WARPS * (MARCH_SMEM_VECS + MARCH_RING) * Grp<G>::N * 32 * sizeof(typename PairOf<T>::P);
 }
 
+// resident CTAs per SM the register allocation targets (in-plane 3, antiplane 4)
+template <int G> struct MarchMinBlocks { static constexpr int value = (G == 0) ? 3 : 4; };
+
+// asynchronous copy of one element into shared memory (completion tracked per thread)
+template <typename T> TMK_D void cp_async_elem(T* dst_smem, const T* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(src), "n"(sizeof(T)) : "memory");
+}
+TMK_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+TMK_D void cp_async_wait_all_but_newest() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
 template <typename T, int G>
-__global__ void __launch_bounds__(32 * MARCH_WARPS, 2) march_kernel(const PatchDev<T>* __restrict__ patches,
+__global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) march_kernel(const PatchDev<T>* __restrict__ patches,
                                                                  const MarchItem* __restrict__ items, int nitems,
                                                                  const DevParams* __restrict__ params) {
   using P = typename PairOf<T>::P;
   constexpr int N = Grp<G>::N;
   extern __shared__ __align__(16) unsigned char march_smem[];
-  P* const carry = reinterpret_cast<P*>(march_smem) + (size_t)(threadIdx.x >> 5) * MARCH_SMEM_VECS * N * 32;
+  P* const carry = reinterpret_cast<P*>(march_smem) + (size_t)(threadIdx.x >> 5) * (MARCH_SMEM_VECS + MARCH_RING) * N * 32;
+  P* const ring = carry + MARCH_SMEM_VECS * N * 32;
   const int wid = blockIdx.x * MARCH_WARPS + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   // a later kernel of the step may be scheduled now; every warp waits for the
@@ -389,6 +404,30 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, 2) march_kernel(const PatchD
       w[c] = ok ? mk2(pp.Uin[o + (size_t)g * plane], pp.Uin[o + (size_t)(11 + g) * plane]) : mk2(T(0), T(0));
     }
   };
+  // row y into its ring slot: cp.async for cells in the domain, zeros elsewhere
+  auto ring_row = [&](int y) -> P* { return ring + (size_t)((y & (MARCH_RING - 1)) * N) * 32 + lane; };
+  auto load_row_async = [&](int y) {
+    const bool ok = lane_in && y >= dlo1 && y <= dhi1;
+    const size_t o = ok ? fab_idx(pp, 0, x, y) : 0;
+    P* dst = ring_row(y);
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      const int g = Grp<G>::glob(c);
+      T* d2 = reinterpret_cast<T*>(dst + c * 32);
+      if (ok) {
+        cp_async_elem(d2, pp.Uin + o + (size_t)g * plane);
+        cp_async_elem(d2 + 1, pp.Uin + o + (size_t)(11 + g) * plane);
+      } else {
+        dst[c * 32] = mk2(T(0), T(0));
+      }
+    }
+    cp_async_commit();
+  };
+  auto get_row = [&](int y, P* w) {
+    const P* src = ring_row(y);
+#pragma unroll
+    for (int c = 0; c < N; ++c) w[c] = src[c * 32];
+  };
 
   // x-direction normal predictor of row w and the first-pass x-face state on
   // the lane's lo face (H1 lo) and hi face (H1 hi)
@@ -423,15 +462,20 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, 2) march_kernel(const PatchD
 
   const int q_s = max(it.y0 - 1, dlo1);
   const int q_e = it.y1 + 1;
-  // rolling window: W0 = W(q), W1 = W(q+1), W2 = W(q+2); sy0 = slope(q); Fy0 = lo-face value of row q
-  P W0[N], W1[N], W2[N], sy0[N], Fy0[N];
+  // rolling window of rows q, q+1, q+2 (ring slots); sy0 = slope(q); Fy0 = lo-face value of row q
+  P sy0[N], Fy0[N];
   {
-    P Wa[N], Wb[N];
+    P Wa[N], Wb[N], W0[N], W1[N], W2[N];
     load_row(q_s - 2, Wa);
     load_row(q_s - 1, Wb);
     load_row(q_s, W0);
     load_row(q_s + 1, W1);
     load_row(q_s + 2, W2);
+    {
+      P* r0 = ring_row(q_s); P* r1 = ring_row(q_s + 1); P* r2 = ring_row(q_s + 2);
+#pragma unroll
+      for (int c = 0; c < N; ++c) { r0[c * 32] = W0[c]; r1[c * 32] = W1[c]; r2[c * 32] = W2[c]; }
+    }
     const bool hl = q_s - 1 >= dlo1, hr = q_s + 1 <= dhi1;
 #pragma unroll
     for (int c = 0; c < N; ++c) {
@@ -460,8 +504,12 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, 2) march_kernel(const PatchD
 
   for (int q = q_s; q <= q_e; ++q) {
     const bool rowin = q <= dhi1;
-    P Wn[N];
-    load_row(q + 3, Wn);     // next row in flight while this one is computed
+    load_row_async(q + 3);            // next row in flight while this one is computed
+    cp_async_wait_all_but_newest();   // rows up to q+2 have landed
+    P W0[N], W1[N], W2[N];
+    get_row(q, W0);
+    get_row(q + 1, W1);
+    get_row(q + 2, W2);
     P WMy[N], WPy[N], WMcy[N], WPcy[N], WMx[N], WPx[N], H1lo[N], H1hi[N];
     P sy1[N], Fy1[N];
     if (rowin) {
@@ -577,9 +625,9 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, 2) march_kernel(const PatchD
     for (int c = 0; c < N; ++c) {
       WPy_p[c] = WPy[c]; WPcy_p[c] = WPcy[c];
       sy0[c] = sy1[c]; Fy0[c] = Fy1[c];
-      W0[c] = W1[c]; W1[c] = W2[c]; W2[c] = Wn[c];
     }
   }
+  asm volatile("cp.async.wait_all;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
