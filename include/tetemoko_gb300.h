@@ -132,6 +132,7 @@ typedef struct { int lo[2], hi[2]; } tmk_box;   /* cell-centred, inclusive */
 
 typedef struct tmk_context_s tmk_context;
 typedef struct tmk_level_s   tmk_level;
+typedef struct tmk_amr_s     tmk_amr;
 
 /* ---------------------------------------------------------------------------
  * Parameters (replaces the process-global Fortran COMMON blocks /IBC/, /rs/,
@@ -223,6 +224,16 @@ tmk_status tmk_level_get_patch(tmk_level* lvl, int patch, double* U, double* B,
  * speed (LinElastLevelGodunov.cpp:377-391).  Graph-capturable: no host sync. */
 tmk_status tmk_level_step(tmk_level* lvl, double time, double dt, void* stream,
                           double* dt_new);
+/* The full LinElastLevelGodunov::step signature for a level that has a coarser
+ * level (LinElastLevelGodunov.H:91-105): the coarse level's old and new times
+ * give the time-interpolation coefficient of the coarse-fine ghost fill,
+ * alpha = (time - t_coarse_old) / (t_coarse_new - t_coarse_old), snapped to 0 or
+ * 1 within 0.04 dt / ratio (LinElastLevelGodunov.cpp:225-256); alpha outside
+ * [0, 1] is TMK_ERR_BAD_DESC (the reference's MayDay).  The step also keeps
+ * the flux registers with the coarser and finer levels.  tmk_level_step is
+ * this call for a level without a coarser level. */
+tmk_status tmk_level_step_cf(tmk_level* lvl, double time, double dt, double t_coarse_old,
+                             double t_coarse_new, void* stream, double* dt_new);
 /* Read and clear the device status word: returns the first recorded error and
  * fills info[0]=code, info[1]=flat index of the first bad value,
  * info[2]=Newton iterations that hit the limit (not an error in the reference). */
@@ -236,6 +247,63 @@ tmk_status tmk_level_profile(tmk_level* lvl, int enable, int max_steps);
 /* Average milliseconds per recorded step of: out[0] ghost exchange,
  * out[1] fault kernel, out[2] volume kernel, out[3] whole step. */
 tmk_status tmk_level_profile_read(tmk_level* lvl, double out[4], int* nsteps);
+
+/* ---------------------------------------------------------------------------
+ * Coarse-fine coupling (AMRLevelLinElast::levelSetup,
+ * srcLinElast/AMRLevelLinElast.cpp:1960-2050).  A fine level is attached to the
+ * next coarser level with the refinement ratio between them; the fine domain
+ * must be the refined coarse domain, every fine patch aligned to the ratio, and
+ * the fine level properly nested (each coarse cell an operator reads is a valid
+ * cell of the coarse level), else TMK_ERR_BAD_DESC.  Attaching replaces an
+ * earlier attachment of either level.  Both levels must use the same precision
+ * and fault law.  A level with attachments computes its volume update with the
+ * tile kernel, which also stores the fluxes of the coarse-fine faces.
+ * ------------------------------------------------------------------------- */
+tmk_status tmk_level_attach_coarser(tmk_level* fine, tmk_level* coarse, int ref_ratio);
+tmk_status tmk_level_detach_coarser(tmk_level* fine);
+/* Coarse-fine ghost fill of the fine level's current state from the coarse
+ * level's state before (old) and after (new) its last step, at time
+ * coefficient alpha: PiecewiseLinearFillPatch::fillInterp for U (radius
+ * TMK_NGHOST) and D1PiecewiseLinearFillPatch::fillInterp for the fault rows
+ * (srcLinElast/D1PiecewiseLinearFillPatch.cpp:276-324).  tmk_level_step_cf
+ * performs it; this entry point exposes it alone. */
+tmk_status tmk_level_fill_coarse_fine(tmk_level* fine, double alpha, void* stream);
+/* LevelFluxRegister::reflux(U, -1/dx) of the coarse level with the fluxes its
+ * finer level accumulated since the coarse level's last step
+ * (srcLinElast/AMRLevelLinElast.cpp:505-506). */
+tmk_status tmk_level_reflux(tmk_level* coarse, void* stream);
+/* CoarseAverage (U) and D1CoarseAverage (fault rows) of the finer level onto
+ * the coarse level (srcLinElast/AMRLevelLinElast.cpp:508-515,
+ * srcLinElast/D1CoarseAverage.cpp:62-139). */
+tmk_status tmk_level_average_down(tmk_level* coarse, void* stream);
+/* Regrid prolongation: FineInterp (U) and D1FineInterp (fault rows) of the
+ * coarse level onto every valid cell of the fine level
+ * (srcLinElast/AMRLevelLinElast.cpp:927-931, srcLinElast/D1FineInterp.cpp:61-267). */
+tmk_status tmk_level_interp_from_coarser(tmk_level* fine, void* stream);
+/* Copy the valid cells (U and fault rows) where the patches of two levels of
+ * the same domain overlap: the "copy from old state" of a regrid
+ * (srcLinElast/AMRLevelLinElast.cpp:934-946). */
+tmk_status tmk_level_copy_overlap(tmk_level* dst, const tmk_level* src, void* stream);
+/* Number of coarse-fine faces in the flux register of an attached fine level. */
+tmk_status tmk_level_register_size(const tmk_level* fine, int* entries);
+
+/* ---------------------------------------------------------------------------
+ * Subcycled AMR hierarchy (Chombo AMR::timeStep over AMRLevelLinElast::advance
+ * and postTimeStep, srcLinElast/AMRLevelLinElast.cpp:420-515).  The caller owns
+ * the levels; creating the hierarchy attaches level l+1 to level l with
+ * ratios[l].  One tmk_amr_step advances level 0 by dt0 and level l by
+ * dt0 / (ratios[0] ... ratios[l-1]), each finer level taking ratio substeps per
+ * step of its coarser level, then refluxes and averages down.  No host sync.
+ * ------------------------------------------------------------------------- */
+tmk_status tmk_amr_create(int nlevels, tmk_level* const* levels, const int* ratios, double time,
+                          tmk_amr** out);
+void       tmk_amr_destroy(tmk_amr* amr);
+tmk_status tmk_amr_step(tmk_amr* amr, double dt0, void* stream);
+tmk_status tmk_amr_time(const tmk_amr* amr, int level, double* time);
+/* Cell-updates of one tmk_amr_step: sum over levels of valid cells x substeps. */
+long long  tmk_amr_cell_updates(const tmk_amr* amr);
+/* Kernel launches of one tmk_amr_step. */
+int        tmk_amr_launches_per_step(const tmk_amr* amr);
 
 #ifdef __cplusplus
 }

@@ -61,8 +61,19 @@ def lib() -> C.CDLL:
         L.tmko_plastic_correction.argtypes = [E, PL, dp, ip, ip, ip, ip, C.c_double]
         L.tmko_level_step.argtypes = [E, S, R, W, PL, ip, ip, C.c_int, ip, dp, dp, C.c_double,
                                       C.c_double, C.c_double, C.c_int]
+        LV = P(_Level)
+        L.tmko_cf_fill.argtypes = [C.c_int, C.c_int, LV, LV, C.c_double, LV]
+        L.tmko_average_down.argtypes = [C.c_int, C.c_int, LV, LV]
+        L.tmko_fine_interp.argtypes = [C.c_int, C.c_int, LV, LV]
+        L.tmko_register_entries.argtypes = [C.c_int, LV, LV, ip]
+        L.tmko_amr_run.argtypes = [E, S, R, W, PL, C.c_int, LV, ip, C.c_double, C.c_double, C.c_int, C.c_int]
         _lib = L
     return _lib
+
+
+class _Level(C.Structure):
+    _fields_ = [("dom", C.c_int * 4), ("dx", C.c_double), ("npatch", C.c_int),
+                ("boxes", C.POINTER(C.c_int)), ("U", C.POINTER(C.c_double)), ("B", C.POINTER(C.c_double))]
 
 
 def _dp(a: np.ndarray | None):
@@ -180,6 +191,111 @@ def level_step(sc, Ug: np.ndarray, Bg: np.ndarray | None, boxes, time: float, dt
         C.byref(sc.elastic), C.byref(sc.scheme), _ref(sc.rs), _ref(sc.sw), _ref(sc.plastic),
         _iv(0, 0), _iv(sc.nx - 1, sc.ny - 1), len(boxes), flat.ctypes.data_as(C.POINTER(C.c_int)),
         _dp(Ug), _dp(Bg), sc.dx, time, dt, nthreads)
+
+
+# ------------------------------------------------------------------ AMR --
+class LevelData:
+    """A level as per-patch host arrays: U[p] (22, ny+8, nx+8) over the valid
+    box grown by 4 ghosts, B[p] (nb, nx+8) for patches on the fault row, else
+    None -- the layout of tetemoko_gb300.level.LinElastLevelGodunov's
+    get_patch / set_patch."""
+
+    def __init__(self, domain, dx: float, boxes, nb: int, U=None, B=None):
+        self.domain = tuple(domain)
+        self.dx = dx
+        self.boxes = [tuple(b) for b in boxes]
+        self.nb = nb
+        g = A.TMK_NGHOST
+        if U is None:
+            U = [np.zeros((22, b[3] - b[1] + 1 + 2 * g, b[2] - b[0] + 1 + 2 * g)) for b in self.boxes]
+        if B is None:
+            B = [np.zeros((nb, b[2] - b[0] + 1 + 2 * g)) if self.fault(p) else None
+                 for p, b in enumerate(self.boxes)]
+        self.U = [np.ascontiguousarray(u, dtype=np.float64) for u in U]
+        self.B = [None if b is None else np.ascontiguousarray(b, dtype=np.float64) for b in B]
+
+    def fault(self, p) -> bool:
+        return self.nb > 0 and self.boxes[p][1] == self.domain[1]
+
+    def copy(self) -> "LevelData":
+        return LevelData(self.domain, self.dx, self.boxes, self.nb, [u.copy() for u in self.U],
+                         [None if b is None else b.copy() for b in self.B])
+
+    def _pack(self):
+        boxes = np.ascontiguousarray(np.array(self.boxes, dtype=np.int32).reshape(-1))
+        U = np.concatenate([u.reshape(-1) for u in self.U])
+        bl = [b.reshape(-1) for b in self.B if b is not None]
+        B = np.concatenate(bl) if bl else None
+        lv = _Level()
+        for k in range(4):
+            lv.dom[k] = self.domain[k]
+        lv.dx = self.dx
+        lv.npatch = len(self.boxes)
+        lv.boxes = boxes.ctypes.data_as(C.POINTER(C.c_int))
+        lv.U = _dp(U)
+        lv.B = _dp(B)
+        return lv, (boxes, U, B)
+
+    def _unpack(self, keep):
+        _, U, B = keep
+        o = 0
+        for u in self.U:
+            u.reshape(-1)[:] = U[o:o + u.size]
+            o += u.size
+        o = 0
+        for b in self.B:
+            if b is not None:
+                b.reshape(-1)[:] = B[o:o + b.size]
+                o += b.size
+
+
+def cf_fill(r: int, coarse_old: LevelData, coarse_new: LevelData, alpha: float, fine: LevelData) -> int:
+    """Coarse-fine ghost fill of `fine` (in place)."""
+    co, ko = coarse_old._pack()
+    cn, kn = coarse_new._pack()
+    f, kf = fine._pack()
+    rc = lib().tmko_cf_fill(r, fine.nb, C.byref(co), C.byref(cn), alpha, C.byref(f))
+    if rc == 0:
+        fine._unpack(kf)
+    return rc
+
+
+def average_down(r: int, coarse: LevelData, fine: LevelData) -> int:
+    c, kc = coarse._pack()
+    f, kf = fine._pack()
+    rc = lib().tmko_average_down(r, fine.nb, C.byref(c), C.byref(f))
+    if rc == 0:
+        coarse._unpack(kc)
+    return rc
+
+
+def fine_interp(r: int, coarse: LevelData, fine: LevelData) -> int:
+    c, kc = coarse._pack()
+    f, kf = fine._pack()
+    rc = lib().tmko_fine_interp(r, fine.nb, C.byref(c), C.byref(f))
+    if rc == 0:
+        fine._unpack(kf)
+    return rc
+
+
+def register_entries(r: int, coarse: LevelData, fine: LevelData) -> int:
+    c, kc = coarse._pack()
+    f, kf = fine._pack()
+    n = C.c_int(0)
+    assert lib().tmko_register_entries(r, C.byref(c), C.byref(f), C.byref(n)) == 0
+    return n.value
+
+
+def amr_run(sc, levels: list[LevelData], ratios, time: float, dt0: float, ncoarse: int, nthreads: int = 1) -> int:
+    """`ncoarse` subcycled hierarchy steps (all levels updated in place)."""
+    packed = [lv._pack() for lv in levels]
+    arr = (_Level * len(levels))(*[p[0] for p in packed])
+    rat = (C.c_int * max(1, len(ratios)))(*(list(ratios) or [1]))
+    rc = lib().tmko_amr_run(C.byref(sc.elastic), C.byref(sc.scheme), _ref(sc.rs), _ref(sc.sw), _ref(sc.plastic),
+                            len(levels), arr, rat, time, dt0, ncoarse, nthreads)
+    for lv, (_, keep) in zip(levels, packed):
+        lv._unpack(keep)
+    return rc
 
 
 def tile_boxes(nx: int, ny: int, max_grid: int):

@@ -1007,6 +1007,527 @@ FAB wrap(const double* p, const int lo[2], const int hi[2], int nc) {
 }
 void unwrap(const FAB& f, double* p) { std::memcpy(p, f.v.data(), f.v.size()*sizeof(double)); }
 
+// ============================================================ AMR coupling ==
+// The coarse-fine operators of the reference's AMR path, on levels stored as
+// one ghosted FAB per patch (the LevelData layout):
+//   coarse-fine ghost fill of U   Chombo PiecewiseLinearFillPatch, called at
+//                                 srcLinElast/LinElastLevelGodunov.cpp:260-264
+//   coarse-fine ghost fill of B   srcLinElast/D1PiecewiseLinearFillPatch.cpp:85-324
+//   flux registers + reflux       Chombo LevelFluxRegister, called at
+//                                 srcLinElast/LinElastLevelGodunov.cpp:334-355,
+//                                 srcLinElast/AMRLevelLinElast.cpp:505-506
+//   average-down of U and B       Chombo CoarseAverage; srcLinElast/D1CoarseAverage.cpp:62-139
+//                                 with d1average (tetemoko_chombo_patchfile:141-188)
+//   regrid prolongation of U, B   Chombo FineInterp; srcLinElast/D1FineInterp.cpp:61-267
+//   subcycled hierarchy step      Chombo AMR::timeStep driving
+//                                 srcLinElast/AMRLevelLinElast.cpp:420-512
+// The Chombo pieces are restated from their published descriptions (Chombo
+// design document: piecewise-linear coarse-fine interpolation with centred or
+// one-sided slopes and a limiter that keeps the linear profile within the
+// range of the neighbouring coarse values; flux-register refluxing; arithmetic
+// averaging over the r^D children).  Choices where the reference would read
+// memory it never wrote are fixed here and hold on the device as well:
+//   * a slope whose two neighbours are both unavailable is 0;
+//   * the limiter takes its min/max over neighbours the coarse level covers;
+//   * every coarse cell an operator needs must be covered by the coarse level
+//     (proper nesting), else the call fails.
+// Fine patches must be aligned to the refinement ratio.
+
+int cdiv(int i, int r) { return i >= 0 ? i / r : -((-i + r - 1) / r); }
+Box coarsenBox(const Box& b, int r) {
+  return mk(cdiv(b.lo[0], r), cdiv(b.lo[1], r), cdiv(b.hi[0], r), cdiv(b.hi[1], r));
+}
+bool boxIn(const Box& inner, const Box& outer) {
+  return inner.lo[0] >= outer.lo[0] && inner.lo[1] >= outer.lo[1] &&
+         inner.hi[0] <= outer.hi[0] && inner.hi[1] <= outer.hi[1];
+}
+
+// time interpolation of D1PiecewiseLinearFillPatch::timeInterp (:328-393) and
+// of PiecewiseLinearFillPatch: new*a + old*(1-a), exact copies at a = 0 or 1
+double tinterp(double o, double n, double a) {
+  if (a == 1.0) return n;
+  if (a == 0.0) return o;
+  double v = n * a;
+  double t = o * (1.0 - a);
+  return v + t;
+}
+
+// fine offset -> linear coefficient (incrementLinearInterp, D1PiecewiseLinearFillPatch.cpp:567-600)
+double interpCoef(int f, int c, int r) { return -0.5 + ((double)(f - r * c) + 0.5) / (double)r; }
+
+// the multidimensional limiter: scale the slopes so that the linear profile
+// stays inside [min, max] of the coarse neighbourhood
+void interpLimit(double& sx, double& sy, double u, double mn, double mx) {
+  double dmax = 0.5 * (std::fabs(sx) + std::fabs(sy));
+  double theta = 1.0;
+  if (dmax > 0.0) {
+    theta = std::min(theta, (mx - u) / dmax);
+    theta = std::min(theta, (u - mn) / dmax);
+  }
+  sx = sx * theta;
+  sy = sy * theta;
+}
+
+struct OLevel {
+  Box dom; double dx = 0; int nb = 0;
+  std::vector<Box> boxes;
+  std::vector<FAB> U, B;              // B[p].nc == 0: patch p has no fault row
+  std::vector<FAB> Uold, Bold;        // AMRLevelLinElast m_UOld / m_BOld
+  double time = 0, dtlast = 0;
+  bool fault(int p) const { return B[p].nc > 0; }
+  int patchAt(int i, int j) const {
+    for (size_t p = 0; p < boxes.size(); ++p) if (boxes[p].contains(i, j)) return (int)p;
+    return -1;
+  }
+  int faultPatchAt(int i) const {
+    for (size_t p = 0; p < boxes.size(); ++p)
+      if (fault((int)p) && i >= boxes[p].lo[0] && i <= boxes[p].hi[0]) return (int)p;
+    return -1;
+  }
+};
+
+// LevelData::exchange of U and B (LinElastLevelGodunov.cpp:220-221)
+void exchangeLevel(OLevel& L) {
+  const int np = (int)L.boxes.size();
+  for (int p = 0; p < np; ++p) {
+    Box g = isect(grow(L.boxes[p], TMK_NGHOST), L.dom);
+    for (int q = 0; q < np; ++q) {
+      if (q == p) continue;
+      Box x = isect(g, L.boxes[q]);
+      if (x.empty()) continue;
+      for (int c = 0; c < 22; ++c)
+        for (int j = x.lo[1]; j <= x.hi[1]; ++j)
+          for (int i = x.lo[0]; i <= x.hi[0]; ++i) L.U[p](i, j, c) = L.U[q](i, j, c);
+    }
+    if (!L.fault(p)) continue;
+    for (int q = 0; q < np; ++q) {
+      if (q == p || !L.fault(q)) continue;
+      int lo = std::max(L.B[p].b.lo[0], L.boxes[q].lo[0]), hi = std::min(L.B[p].b.hi[0], L.boxes[q].hi[0]);
+      for (int c = 0; c < L.nb; ++c)
+        for (int i = lo; i <= hi; ++i) L.B[p](i, L.dom.lo[1], c) = L.B[q](i, L.dom.lo[1], c);
+    }
+  }
+}
+
+// Coarse-fine ghost fill of U: PiecewiseLinearFillPatch::fillInterp with
+// interpolation radius TMK_NGHOST (LinElastLevelGodunov.cpp:154-160, 260-264).
+bool cfFillU(OLevel& F, const OLevel& C, const std::vector<FAB>& Co, const std::vector<FAB>& Cn,
+             double a, int r) {
+  std::vector<Box> cfb;
+  for (const Box& b : F.boxes) cfb.push_back(coarsenBox(b, r));
+  auto coveredByFine = [&](int ci, int cj) {
+    for (const Box& b : cfb) if (b.contains(ci, cj)) return true;
+    return false;
+  };
+  for (size_t p = 0; p < F.boxes.size(); ++p) {
+    const Box& V = F.boxes[p];
+    Box g = isect(grow(V, TMK_NGHOST), F.dom);
+    for (int j = g.lo[1]; j <= g.hi[1]; ++j)
+      for (int i = g.lo[0]; i <= g.hi[0]; ++i) {
+        if (V.contains(i, j)) continue;
+        const int ci = cdiv(i, r), cj = cdiv(j, r);
+        if (coveredByFine(ci, cj)) continue;
+        if (C.patchAt(ci, cj) < 0) return false;
+        const double cx = interpCoef(i, ci, r), cy = interpCoef(j, cj, r);
+        const bool lim = boxIn(grow(mk(ci, cj, ci, cj), 1), C.dom);
+        for (int c = 0; c < 22; ++c) {
+          auto val = [&](int x, int y) {
+            int q = C.patchAt(x, y);
+            return tinterp(Co[q](x, y, c), Cn[q](x, y, c), a);
+          };
+          const double u0 = val(ci, cj);
+          double s[2];
+          for (int d = 0; d < 2; ++d) {
+            int e0 = d == 0, e1 = d == 1;
+            bool hp = C.patchAt(ci + e0, cj + e1) >= 0, hm = C.patchAt(ci - e0, cj - e1) >= 0;
+            if (hp && hm) s[d] = 0.5 * (val(ci + e0, cj + e1) - val(ci - e0, cj - e1));
+            else if (hm) s[d] = u0 - val(ci - e0, cj - e1);
+            else if (hp) s[d] = val(ci + e0, cj + e1) - u0;
+            else s[d] = 0.0;
+          }
+          if (lim) {
+            double mn = u0, mx = u0;
+            for (int dj = -1; dj <= 1; ++dj)
+              for (int di = -1; di <= 1; ++di) {
+                if (C.patchAt(ci + di, cj + dj) < 0) continue;
+                double v = val(ci + di, cj + dj);
+                mn = std::min(mn, v); mx = std::max(mx, v);
+              }
+            interpLimit(s[0], s[1], u0, mn, mx);
+          }
+          double v = u0;
+          v = v + cx * s[0];
+          v = v + cy * s[1];
+          F.U[p](i, j, c) = v;
+        }
+      }
+  }
+  return true;
+}
+
+// Coarse-fine ghost fill of the fault rows: D1PiecewiseLinearFillPatch (the
+// limiter's box is empty for a one-row layout, :510-520, so slopes stay
+// unlimited; slopes are centred, or one-sided where the coarse fault rows end).
+bool cfFillB(OLevel& F, const OLevel& C, const std::vector<FAB>& Bo, const std::vector<FAB>& Bn,
+             double a, int r) {
+  if (F.nb == 0) return true;
+  const int jf = F.dom.lo[1], jc = C.dom.lo[1];
+  auto coveredByFine = [&](int ci) {
+    for (size_t q = 0; q < F.boxes.size(); ++q)
+      if (F.fault((int)q) && ci >= cdiv(F.boxes[q].lo[0], r) && ci <= cdiv(F.boxes[q].hi[0], r)) return true;
+    return false;
+  };
+  for (size_t p = 0; p < F.boxes.size(); ++p) {
+    if (!F.fault((int)p)) continue;
+    const Box& V = F.boxes[p];
+    const int lo = std::max(V.lo[0] - TMK_NGHOST, F.dom.lo[0]), hi = std::min(V.hi[0] + TMK_NGHOST, F.dom.hi[0]);
+    for (int i = lo; i <= hi; ++i) {
+      if (i >= V.lo[0] && i <= V.hi[0]) continue;
+      const int ci = cdiv(i, r);
+      if (coveredByFine(ci)) continue;
+      if (C.faultPatchAt(ci) < 0) return false;
+      const double cx = interpCoef(i, ci, r);
+      const bool hp = C.faultPatchAt(ci + 1) >= 0, hm = C.faultPatchAt(ci - 1) >= 0;
+      for (int c = 0; c < F.nb; ++c) {
+        auto val = [&](int x) {
+          int q = C.faultPatchAt(x);
+          return tinterp(Bo[q](x, jc, c), Bn[q](x, jc, c), a);
+        };
+        const double u0 = val(ci);
+        double s;
+        if (hp && hm) s = 0.5 * (val(ci + 1) - val(ci - 1));
+        else if (hm) s = u0 - val(ci - 1);
+        else if (hp) s = val(ci + 1) - u0;
+        else s = 0.0;
+        double v = u0;
+        v = v + cx * s;
+        F.B[p](i, jf, c) = v;
+      }
+    }
+  }
+  return true;
+}
+
+// Average-down (AMRLevelLinElast::postTimeStep, :511-515): arithmetic mean of
+// the r^2 children (U) and of the r fault-face children (d1average).
+bool averageDown(OLevel& C, const OLevel& F, int r) {
+  const double sU = 1.0 / (double)(r * r), sB = 1.0 / (double)r;
+  for (size_t p = 0; p < F.boxes.size(); ++p) {
+    Box vc = coarsenBox(F.boxes[p], r);
+    for (int cj = vc.lo[1]; cj <= vc.hi[1]; ++cj)
+      for (int ci = vc.lo[0]; ci <= vc.hi[0]; ++ci) {
+        int q = C.patchAt(ci, cj);
+        if (q < 0) return false;
+        for (int c = 0; c < 22; ++c) {
+          double sum = 0.0;
+          for (int jj = 0; jj < r; ++jj)
+            for (int ii = 0; ii < r; ++ii) sum = sum + F.U[p](r * ci + ii, r * cj + jj, c);
+          C.U[q](ci, cj, c) = sum * sU;
+        }
+      }
+    if (!F.fault((int)p) || C.nb == 0) continue;
+    for (int ci = vc.lo[0]; ci <= vc.hi[0]; ++ci) {
+      int q = C.faultPatchAt(ci);
+      if (q < 0) return false;
+      for (int c = 0; c < C.nb; ++c) {
+        double sum = 0.0;
+        for (int ii = 0; ii < r; ++ii) sum = sum + F.B[p](r * ci + ii, F.dom.lo[1], c);
+        C.B[q](ci, C.dom.lo[1], c) = sum * sB;
+      }
+    }
+  }
+  return true;
+}
+
+// Regrid prolongation of the valid cells (FineInterp::interpToFine for U,
+// D1FineInterp::interpToFine for B): centred slopes, one-sided at the coarse
+// domain boundary, limited away from it.
+bool fineInterp(OLevel& F, const OLevel& C, int r) {
+  for (size_t p = 0; p < F.boxes.size(); ++p) {
+    const Box& V = F.boxes[p];
+    Box vc = coarsenBox(V, r);
+    for (int cj = vc.lo[1]; cj <= vc.hi[1]; ++cj)
+      for (int ci = vc.lo[0]; ci <= vc.hi[0]; ++ci) {
+        if (C.patchAt(ci, cj) < 0) return false;
+        const bool lim = boxIn(grow(mk(ci, cj, ci, cj), 1), C.dom);
+        int kind[2];
+        for (int d = 0; d < 2; ++d) {
+          int cd = d == 0 ? ci : cj;
+          bool atlo = cd == C.dom.lo[d], athi = cd == C.dom.hi[d];
+          kind[d] = (!atlo && !athi) ? 0 : (atlo && !athi) ? 2 : (athi && !atlo) ? 1 : 3;
+          int e0 = d == 0, e1 = d == 1;
+          if ((kind[d] == 0 || kind[d] == 2) && C.patchAt(ci + e0, cj + e1) < 0) return false;
+          if ((kind[d] == 0 || kind[d] == 1) && C.patchAt(ci - e0, cj - e1) < 0) return false;
+        }
+        for (int c = 0; c < 22; ++c) {
+          auto val = [&](int x, int y) { return C.U[C.patchAt(x, y)](x, y, c); };
+          const double u0 = val(ci, cj);
+          double s[2];
+          for (int d = 0; d < 2; ++d) {
+            int e0 = d == 0, e1 = d == 1;
+            if (kind[d] == 0) s[d] = 0.5 * (val(ci + e0, cj + e1) - val(ci - e0, cj - e1));
+            else if (kind[d] == 2) s[d] = val(ci + e0, cj + e1) - u0;
+            else if (kind[d] == 1) s[d] = u0 - val(ci - e0, cj - e1);
+            else s[d] = 0.0;
+          }
+          if (lim) {
+            double mn = u0, mx = u0;
+            for (int dj = -1; dj <= 1; ++dj)
+              for (int di = -1; di <= 1; ++di) {
+                if (C.patchAt(ci + di, cj + dj) < 0) continue;
+                double v = val(ci + di, cj + dj);
+                mn = std::min(mn, v); mx = std::max(mx, v);
+              }
+            interpLimit(s[0], s[1], u0, mn, mx);
+          }
+          for (int jj = 0; jj < r; ++jj)
+            for (int ii = 0; ii < r; ++ii) {
+              int i = r * ci + ii, j = r * cj + jj;
+              double v = u0;
+              v = v + interpCoef(i, ci, r) * s[0];
+              v = v + interpCoef(j, cj, r) * s[1];
+              F.U[p](i, j, c) = v;
+            }
+        }
+      }
+    if (!F.fault((int)p) || F.nb == 0) continue;
+    const int jc = C.dom.lo[1], jf = F.dom.lo[1];
+    for (int ci = vc.lo[0]; ci <= vc.hi[0]; ++ci) {
+      if (C.faultPatchAt(ci) < 0) return false;
+      bool atlo = ci == C.dom.lo[0], athi = ci == C.dom.hi[0];
+      int kind = (!atlo && !athi) ? 0 : (atlo && !athi) ? 2 : (athi && !atlo) ? 1 : 3;
+      if ((kind == 0 || kind == 2) && C.faultPatchAt(ci + 1) < 0) return false;
+      if ((kind == 0 || kind == 1) && C.faultPatchAt(ci - 1) < 0) return false;
+      const bool lim = ci - 1 >= C.dom.lo[0] && ci + 1 <= C.dom.hi[0];
+      for (int c = 0; c < F.nb; ++c) {
+        auto val = [&](int x) { return C.B[C.faultPatchAt(x)](x, jc, c); };
+        const double u0 = val(ci);
+        double s = kind == 0 ? 0.5 * (val(ci + 1) - val(ci - 1)) : kind == 2 ? val(ci + 1) - u0
+                 : kind == 1 ? u0 - val(ci - 1) : 0.0;
+        if (lim) {
+          double mn = u0, mx = u0;
+          for (int di = -1; di <= 1; ++di) {
+            double v = val(ci + di);
+            mn = std::min(mn, v); mx = std::max(mx, v);
+          }
+          double s1 = 0.0;
+          interpLimit(s, s1, u0, mn, mx);
+        }
+        for (int ii = 0; ii < r; ++ii) {
+          int i = r * ci + ii;
+          double v = u0;
+          v = v + interpCoef(i, ci, r) * s;
+          F.B[p](i, jf, c) = v;
+        }
+      }
+    }
+  }
+  return true;
+}
+
+// One flux-register entry: a coarse cell k outside the fine region whose face
+// in direction d on the fine side is a coarse-fine face.  side = -1 when the
+// fine region lies above k (the face is k's hi face), +1 when below.
+struct RegEntry { int ci, cj, d, side, fp, kt; };
+
+// LevelFluxRegister::define: the entries, in the order d, side (lo, hi), fine
+// patch, tangential index.
+std::vector<RegEntry> registerEntries(const OLevel& F, const OLevel& C, int r) {
+  std::vector<Box> cfb;
+  for (const Box& b : F.boxes) cfb.push_back(coarsenBox(b, r));
+  auto coveredByFine = [&](int ci, int cj) {
+    for (const Box& b : cfb) if (b.contains(ci, cj)) return true;
+    return false;
+  };
+  std::vector<RegEntry> out;
+  for (int d = 0; d < 2; ++d)
+    for (int side = -1; side <= 1; side += 2)
+      for (size_t p = 0; p < F.boxes.size(); ++p) {
+        const Box& vc = cfb[p];
+        const int t = 1 - d;
+        const int kd = side < 0 ? vc.lo[d] - 1 : vc.hi[d] + 1;
+        for (int kt = vc.lo[t]; kt <= vc.hi[t]; ++kt) {
+          int ci = d == 0 ? kd : kt, cj = d == 0 ? kt : kd;
+          if (!C.dom.contains(ci, cj) || coveredByFine(ci, cj)) continue;
+          RegEntry e; e.ci = ci; e.cj = cj; e.d = d; e.side = side; e.fp = (int)p; e.kt = kt;
+          out.push_back(e);
+        }
+      }
+  return out;
+}
+
+// coarse face of an entry (in face indices of direction d) and its fine faces
+int coarseFace(const RegEntry& e) { return (e.d == 0 ? e.ci : e.cj) + (e.side < 0 ? 1 : 0); }
+
+// LevelFluxRegister::incrementCoarse: R = -dt * F_coarse
+void regIncrementCoarse(std::vector<double>& R, const std::vector<RegEntry>& E, const OLevel& C,
+                        const std::vector<std::vector<FAB>>& Fc, double dt) {
+  R.assign(E.size() * 22, 0.0);
+  for (size_t k = 0; k < E.size(); ++k) {
+    const RegEntry& e = E[k];
+    int q = C.patchAt(e.ci, e.cj);
+    int f = coarseFace(e);
+    int i = e.d == 0 ? f : e.ci, j = e.d == 0 ? e.cj : f;
+    for (int c = 0; c < 22; ++c) R[k * 22 + c] = -(dt * Fc[q][e.d](i, j, c));
+  }
+}
+
+// LevelFluxRegister::incrementFine: R += (dt / r) * F_fine over the r fine faces
+void regIncrementFine(std::vector<double>& R, const std::vector<RegEntry>& E, const OLevel& F,
+                      const std::vector<std::vector<FAB>>& Ff, double dt, int r) {
+  const double s = dt / (double)r;
+  for (size_t k = 0; k < E.size(); ++k) {
+    const RegEntry& e = E[k];
+    const Box& V = F.boxes[e.fp];
+    int f = e.side < 0 ? V.lo[e.d] : V.hi[e.d] + 1;
+    for (int m = 0; m < r; ++m) {
+      int t = r * e.kt + m;
+      int i = e.d == 0 ? f : t, j = e.d == 0 ? t : f;
+      for (int c = 0; c < 22; ++c) R[k * 22 + c] = R[k * 22 + c] + s * Ff[e.fp][e.d](i, j, c);
+    }
+  }
+}
+
+// LevelFluxRegister::reflux(U, -1/dx) (AMRLevelLinElast.cpp:505-506)
+void reflux(OLevel& C, const std::vector<double>& R, const std::vector<RegEntry>& E) {
+  const double scale = -1.0 / C.dx;
+  for (size_t k = 0; k < E.size(); ++k) {
+    const RegEntry& e = E[k];
+    int q = C.patchAt(e.ci, e.cj);
+    const double sc = e.side < 0 ? scale : -scale;
+    for (int c = 0; c < 22; ++c) C.U[q](e.ci, e.cj, c) = C.U[q](e.ci, e.cj, c) + R[k * 22 + c] * sc;
+  }
+}
+
+struct Hierarchy {
+  const Phys& P;
+  std::vector<OLevel> L;
+  std::vector<int> ratio;                          // ratio[l]: level l -> l+1
+  std::vector<std::vector<RegEntry>> E;            // E[l]: register between l and l+1
+  std::vector<std::vector<double>> R;
+  int nthreads = 1;
+  int err = 0;                                     // 2 NaN state, 3 not nested, 1 bad time
+  Hierarchy(const Phys& p) : P(p) {}
+
+  // LinElastLevelGodunov::step (+ plasticUpdate) on level l with its
+  // coarse-fine ghost fill and flux-register increments
+  void levelStep(int l, double dt) {
+    OLevel& Lv = L[l];
+    Lv.Uold = Lv.U; Lv.Bold = Lv.B;
+    exchangeLevel(Lv);
+    if (l > 0) {
+      const OLevel& C = L[l - 1];
+      const double tco = C.time - C.dtlast, tcn = C.time;
+      double alpha = (Lv.time - tco) / (tcn - tco);
+      const double eps = 0.04 * dt / ratio[l - 1];
+      if (std::fabs(alpha) < eps) alpha = 0.0;
+      if (std::fabs(1.0 - alpha) < eps) alpha = 1.0;
+      if (alpha < 0.0 || alpha > 1.0) { err = 1; return; }
+      if (!cfFillU(Lv, C, C.Uold, C.U, alpha, ratio[l - 1])) { err = 3; return; }
+      if (!cfFillB(Lv, C, C.Bold, C.B, alpha, ratio[l - 1])) { err = 3; return; }
+    }
+    const int np = (int)Lv.boxes.size();
+    std::vector<std::vector<FAB>> Fl(np, std::vector<FAB>(2));
+    int bad = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads) reduction(|:bad)
+#endif
+    for (int p = 0; p < np; ++p) {
+      FaultData fd;
+      if (Lv.fault(p)) fd.B = &Lv.B[p];
+      Patch pt(P);
+      pt.dom = Lv.dom; pt.cur = Lv.boxes[p]; pt.dx = Lv.dx; pt.time = Lv.time;
+      pt.fd = Lv.fault(p) ? &fd : nullptr;
+      if (!pt.updateState(Lv.U[p], Fl[p].data(), dt)) bad |= 1;
+    }
+    if (bad) err = 2;
+    if (l + 1 < (int)L.size()) regIncrementCoarse(R[l], E[l], Lv, Fl, dt);
+    if (l > 0) regIncrementFine(R[l - 1], E[l - 1], Lv, Fl, dt, ratio[l - 1]);
+    if (P.sch.plasticity)
+      for (int p = 0; p < np; ++p) plasticcorrection(P, Lv.U[p], dt, Lv.boxes[p]);
+    Lv.time += dt;
+    Lv.dtlast = dt;
+  }
+
+  // AMR::timeStep recursion: advance l, then r substeps of l+1, then
+  // AMRLevelLinElast::postTimeStep (reflux, average-down)
+  void advance(int l, double dt) {
+    levelStep(l, dt);
+    if (err) return;
+    if (l + 1 < (int)L.size()) {
+      const int r = ratio[l];
+      for (int k = 0; k < r && !err; ++k) advance(l + 1, dt / r);
+      if (err) return;
+      reflux(L[l], R[l], E[l]);
+      if (!averageDown(L[l], L[l + 1], r)) err = 3;
+    }
+  }
+};
+
+}  // namespace
+
+// ------------------------------------------------ level descriptors (C API) --
+// A level as the C API passes it: patches' valid boxes (lo0 lo1 hi0 hi1 each),
+// U = the patches' FABs over the valid box grown by TMK_NGHOST, 22 comps each,
+// concatenated in patch order; B = the fault rows (x over the valid range grown
+// by TMK_NGHOST, nb comps) of the patches whose box starts on the domain's
+// y-lo row, concatenated in patch order (NULL when nb == 0).
+extern "C" {
+typedef struct {
+  int dom[4];
+  double dx;
+  int npatch;
+  const int* boxes;
+  double* U;
+  double* B;
+} tmko_level;
+}
+
+namespace {
+
+bool loadLevel(OLevel& L, const tmko_level& d, int nb) {
+  L.dom = mk(d.dom[0], d.dom[1], d.dom[2], d.dom[3]);
+  L.dx = d.dx; L.nb = nb;
+  L.boxes.clear(); L.U.clear(); L.B.clear();
+  size_t ou = 0, ob = 0;
+  for (int p = 0; p < d.npatch; ++p) {
+    Box b = mk(d.boxes[4*p], d.boxes[4*p+1], d.boxes[4*p+2], d.boxes[4*p+3]);
+    L.boxes.push_back(b);
+    FAB u(grow(b, TMK_NGHOST), 22);
+    if (d.U) std::memcpy(u.v.data(), d.U + ou, u.v.size() * sizeof(double));
+    ou += u.v.size();
+    L.U.push_back(std::move(u));
+    FAB bf;
+    if (nb > 0 && b.lo[1] == L.dom.lo[1]) {
+      bf.define(mk(b.lo[0] - TMK_NGHOST, L.dom.lo[1], b.hi[0] + TMK_NGHOST, L.dom.lo[1]), nb);
+      if (!d.B) return false;
+      std::memcpy(bf.v.data(), d.B + ob, bf.v.size() * sizeof(double));
+      ob += bf.v.size();
+    }
+    L.B.push_back(std::move(bf));
+  }
+  return true;
+}
+
+void storeLevel(const OLevel& L, const tmko_level& d) {
+  size_t ou = 0, ob = 0;
+  for (size_t p = 0; p < L.boxes.size(); ++p) {
+    if (d.U) std::memcpy(d.U + ou, L.U[p].v.data(), L.U[p].v.size() * sizeof(double));
+    ou += L.U[p].v.size();
+    if (L.B[p].nc > 0 && d.B) {
+      std::memcpy(d.B + ob, L.B[p].v.data(), L.B[p].v.size() * sizeof(double));
+      ob += L.B[p].v.size();
+    }
+  }
+}
+
+bool alignedTo(const OLevel& F, int r) {
+  for (const Box& b : F.boxes)
+    for (int d = 0; d < 2; ++d)
+      if (b.lo[d] % r != 0 || (b.hi[d] + 1) % r != 0) return false;
+  return true;
+}
+
 }  // namespace
 
 // ================================================================= C API ===
@@ -1174,6 +1695,84 @@ int tmko_level_step(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_
   unwrap(Unew, Ug);
   if (fault) unwrap(Bnew, Bg);
   return bad ? 2 : 0;
+}
+
+// ---------------------------------------------------------- AMR operators --
+// Return codes: 0 ok, 1 bad arguments, 3 a needed coarse cell is not covered
+// by the coarse level (fine level not properly nested), 2 NaN state.
+
+// Coarse-fine ghost fill of a fine level from coarse states old/new at time
+// coefficient alpha (LinElastLevelGodunov::step, :225-270): U ghosts and, with
+// nb > 0, the fault-row ghosts.  Only the fill: no same-level exchange.
+int tmko_cf_fill(int r, int nb, const tmko_level* c_old, const tmko_level* c_new, double alpha,
+                 tmko_level* fine) {
+  if (!c_old || !c_new || !fine || r < 1 || alpha < 0.0 || alpha > 1.0) return 1;
+  OLevel Co, Cn, F;
+  if (!loadLevel(Co, *c_old, nb) || !loadLevel(Cn, *c_new, nb) || !loadLevel(F, *fine, nb)) return 1;
+  if (!alignedTo(F, r)) return 1;
+  if (!cfFillU(F, Cn, Co.U, Cn.U, alpha, r)) return 3;
+  if (!cfFillB(F, Cn, Co.B, Cn.B, alpha, r)) return 3;
+  storeLevel(F, *fine);
+  return 0;
+}
+
+// Average-down of U and B from fine to coarse (AMRLevelLinElast::postTimeStep).
+int tmko_average_down(int r, int nb, tmko_level* coarse, const tmko_level* fine) {
+  if (!coarse || !fine || r < 1) return 1;
+  OLevel C, F;
+  if (!loadLevel(C, *coarse, nb) || !loadLevel(F, *fine, nb)) return 1;
+  if (!alignedTo(F, r)) return 1;
+  if (!averageDown(C, F, r)) return 3;
+  storeLevel(C, *coarse);
+  return 0;
+}
+
+// Regrid prolongation of the fine valid cells from the coarse level.
+int tmko_fine_interp(int r, int nb, const tmko_level* coarse, tmko_level* fine) {
+  if (!coarse || !fine || r < 1) return 1;
+  OLevel C, F;
+  if (!loadLevel(C, *coarse, nb) || !loadLevel(F, *fine, nb)) return 1;
+  if (!alignedTo(F, r)) return 1;
+  if (!fineInterp(F, C, r)) return 3;
+  storeLevel(F, *fine);
+  return 0;
+}
+
+// Number of flux-register entries between a fine level and its coarse level.
+int tmko_register_entries(int r, const tmko_level* coarse, const tmko_level* fine, int* out) {
+  if (!coarse || !fine || r < 1 || !out) return 1;
+  OLevel C, F;
+  if (!loadLevel(C, *coarse, 0) || !loadLevel(F, *fine, 0)) return 1;
+  *out = (int)registerEntries(F, C, r).size();
+  return 0;
+}
+
+// `ncoarse` subcycled hierarchy steps of levels[0..nlev-1] (level 0 by dt0,
+// level l by dt0 / prod ratios): AMR::timeStep with AMRLevelLinElast::advance
+// and postTimeStep.  All levels start at `time`.
+int tmko_amr_run(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_rs_params* rs,
+                 const tmk_sw_params* sw, const tmk_plastic_params* pl,
+                 int nlev, tmko_level* levels, const int* ratios, double time, double dt0,
+                 int ncoarse, int nthreads) {
+  Phys P;
+  if (!setup(P, e, s, rs, sw, pl) || nlev < 1 || !levels || (nlev > 1 && !ratios)) return 1;
+  const int nb = s->fault_law == TMK_FAULT_RS ? TMK_RS_NBDRY : s->fault_law == TMK_FAULT_SW ? TMK_SW_NBDRY : 0;
+  Hierarchy H(P);
+  H.nthreads = nthreads > 0 ? nthreads : 1;
+  H.L.resize(nlev);
+  for (int l = 0; l < nlev; ++l) {
+    if (!loadLevel(H.L[l], levels[l], nb)) return 1;
+    H.L[l].time = time;
+  }
+  for (int l = 0; l + 1 < nlev; ++l) {
+    if (ratios[l] < 1 || !alignedTo(H.L[l + 1], ratios[l])) return 1;
+    H.ratio.push_back(ratios[l]);
+    H.E.push_back(registerEntries(H.L[l + 1], H.L[l], ratios[l]));
+  }
+  H.R.resize(H.E.size());
+  for (int k = 0; k < ncoarse && !H.err; ++k) H.advance(0, dt0);
+  for (int l = 0; l < nlev; ++l) storeLevel(H.L[l], levels[l]);
+  return H.err;
 }
 
 }  // extern "C"

@@ -129,10 +129,31 @@ def lib() -> C.CDLL:
     L.tmk_level_launches_per_step.restype = C.c_int
     L.tmk_level_profile.argtypes = [vp, C.c_int, C.c_int]
     L.tmk_level_profile_read.argtypes = [vp, dp, ip]
+    L.tmk_level_step_cf.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, vp, dp]
+    L.tmk_level_attach_coarser.argtypes = [vp, vp, C.c_int]
+    L.tmk_level_detach_coarser.argtypes = [vp]
+    L.tmk_level_fill_coarse_fine.argtypes = [vp, C.c_double, vp]
+    L.tmk_level_reflux.argtypes = [vp, vp]
+    L.tmk_level_average_down.argtypes = [vp, vp]
+    L.tmk_level_interp_from_coarser.argtypes = [vp, vp]
+    L.tmk_level_copy_overlap.argtypes = [vp, vp, vp]
+    L.tmk_level_register_size.argtypes = [vp, ip]
+    L.tmk_amr_create.argtypes = [C.c_int, C.POINTER(vp), ip, C.c_double, C.POINTER(vp)]
+    L.tmk_amr_destroy.argtypes = [vp]
+    L.tmk_amr_destroy.restype = None
+    L.tmk_amr_step.argtypes = [vp, C.c_double, vp]
+    L.tmk_amr_time.argtypes = [vp, C.c_int, dp]
+    L.tmk_amr_cell_updates.argtypes = [vp]
+    L.tmk_amr_cell_updates.restype = C.c_longlong
+    L.tmk_amr_launches_per_step.argtypes = [vp]
+    L.tmk_amr_launches_per_step.restype = C.c_int
     for name in ("tmk_context_create", "tmk_context_constants", "tmk_patch_update_state",
                  "tmk_plastic_update", "tmk_max_wave_speed", "tmk_level_create", "tmk_level_set_patch",
                  "tmk_level_get_patch", "tmk_level_step", "tmk_level_status", "tmk_level_profile",
-                 "tmk_level_profile_read"):
+                 "tmk_level_profile_read", "tmk_level_step_cf", "tmk_level_attach_coarser",
+                 "tmk_level_detach_coarser", "tmk_level_fill_coarse_fine", "tmk_level_reflux",
+                 "tmk_level_average_down", "tmk_level_interp_from_coarser", "tmk_level_copy_overlap",
+                 "tmk_level_register_size", "tmk_amr_create", "tmk_amr_step", "tmk_amr_time"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

@@ -1,0 +1,1028 @@
+// tmk_amr.cu -- coarse-fine coupling of device levels and the subcycled AMR
+// hierarchy (compiled without FMA contraction: the FP64 form matches the CPU
+// oracle's operation order exactly).
+//
+// A CFLink couples a level (fine side) with the next coarser level.  Built once
+// on the host from the two box layouts, it holds device work lists for:
+//   * the coarse-fine ghost fill of U (Chombo PiecewiseLinearFillPatch with
+//     interpolation radius 4, srcLinElast/LinElastLevelGodunov.cpp:154-160,
+//     260-264) and of the fault rows (srcLinElast/D1PiecewiseLinearFillPatch.cpp),
+//     as "sites" (coarse cells: time-interpolated value + limited slopes) and
+//     "fine entries" (ghost cells: site value + linear terms);
+//   * the flux register (Chombo LevelFluxRegister, LinElastLevelGodunov.cpp:
+//     334-355): the coarse and fine faces of every coarse-fine face, captured
+//     by the volume kernel of each level into its `cap` buffer, and the reflux
+//     of AMRLevelLinElast::postTimeStep (:505-506);
+//   * average-down (Chombo CoarseAverage; srcLinElast/D1CoarseAverage.cpp with
+//     d1average, tetemoko_chombo_patchfile:141-188);
+//   * regrid prolongation (Chombo FineInterp; srcLinElast/D1FineInterp.cpp).
+// Every list is laid out so that one thread owns one (item, component) and
+// writes distinct addresses: no atomics, results independent of scheduling.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <new>
+#include <tuple>
+#include <vector>
+
+#include "tmk_internal.h"
+
+using tmk::PatchDev;
+using tmk::TileDev;
+using tmk::CopyDev;
+using tmk::fab_idx;
+using namespace tmk_host;
+
+namespace {
+
+constexpr int NC = TMK_NCOMP;
+constexpr int NG = TMK_NGHOST;
+
+// slope kinds: centred, one-sided towards lo (u0 - u[-1]), towards hi (u[+1] - u0), none
+enum { SL_CENTRED = 0, SL_LO = 1, SL_HI = 2, SL_NONE = 3 };
+
+struct SiteU { int ci, cj; int nb[9]; int kx, ky, lim; };   // nb[(dj+1)*3+(di+1)]: coarse patch or -1
+struct FineU { int fpatch, i, j, site; double cx, cy; };
+struct SiteB { int ci; int nb[3]; int kind; };
+struct FineB { int fpatch, i, site; double cx; };
+struct AvgU { int cpatch, ci, cj, fpatch; };
+struct AvgB { int cpatch, ci, fpatch; };
+struct InterpU { int fpatch, ci, cj; int nb[9]; int kx, ky, lim; };
+struct InterpB { int fpatch, ci; int nb[3]; int kind, lim; };
+struct RefluxCell { int cpatch, ci, cj, e0, e1; };
+
+int cdiv(int i, int r) { return i >= 0 ? i / r : -((-i + r - 1) / r); }
+tmk_box coarsen(const tmk_box& b, int r) {
+  tmk_box c;
+  c.lo[0] = cdiv(b.lo[0], r); c.lo[1] = cdiv(b.lo[1], r);
+  c.hi[0] = cdiv(b.hi[0], r); c.hi[1] = cdiv(b.hi[1], r);
+  return c;
+}
+
+// ------------------------------------------------------------- device code
+__device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
+
+// new*a + old*(1-a); exact copies at a = 1 and a = 0
+__device__ __forceinline__ double tinterp(double o, double n, double a) {
+  if (a == 1.0) return n;
+  if (a == 0.0) return o;
+  double v = n * a;
+  double t = o * (1.0 - a);
+  return v + t;
+}
+
+__device__ __forceinline__ double slope(int kind, double um, double u0, double up) {
+  return kind == SL_CENTRED ? 0.5 * (up - um) : kind == SL_LO ? u0 - um : kind == SL_HI ? up - u0 : 0.0;
+}
+
+__device__ __forceinline__ void limit2(double& sx, double& sy, double u, double mn, double mx) {
+  double dm = 0.5 * (fabs(sx) + fabs(sy));
+  double th = 1.0;
+  if (dm > 0.0) {
+    th = dmin(th, (mx - u) / dm);
+    th = dmin(th, (u - mn) / dm);
+  }
+  sx = sx * th;
+  sy = sy * th;
+}
+
+__device__ __forceinline__ double icoef(int f, int c, int r) { return -0.5 + ((double)(f - r * c) + 0.5) / (double)r; }
+
+template <typename Real>
+__device__ __forceinline__ double uval(const PatchDev<Real>& P, int c, int i, int j, double a, bool interp) {
+  const size_t o = fab_idx(P, c, i, j);
+  const double n = (double)P.Uin[o];
+  if (!interp || a == 1.0) return n;
+  return tinterp((double)P.Uout[o], n, a);
+}
+
+__device__ __forceinline__ double bval(const double* B, int blo, int bnx, int c, int i) {
+  return B[(size_t)c * bnx + (i - blo)];
+}
+
+// coarse sites: time-interpolated value and limited slopes, 3 doubles per (site, comp)
+template <typename Real>
+__global__ void cf_sites_kernel(const PatchDev<Real>* __restrict__ cp, const SiteU* __restrict__ su, int nsu,
+                                const SiteB* __restrict__ sb, int nsb, int nb, double a,
+                                double* __restrict__ svu, double* __restrict__ svb) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nsu * NC) {
+    const SiteU s = su[t / NC];
+    const int c = t % NC;
+    double v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      v[k] = s.nb[k] >= 0 ? uval(cp[s.nb[k]], c, s.ci + k % 3 - 1, s.cj + k / 3 - 1, a, true) : 0.0;
+    const double u0 = v[4];
+    double sx = slope(s.kx, v[3], u0, v[5]);
+    double sy = slope(s.ky, v[1], u0, v[7]);
+    if (s.lim) {
+      double mn = u0, mx = u0;
+#pragma unroll
+      for (int k = 0; k < 9; ++k)
+        if (s.nb[k] >= 0) { mn = dmin(mn, v[k]); mx = dmax(mx, v[k]); }
+      limit2(sx, sy, u0, mn, mx);
+    }
+    double* o = svu + (size_t)t * 3;
+    o[0] = u0; o[1] = sx; o[2] = sy;
+    return;
+  }
+  t -= nsu * NC;
+  if (t < nsb * nb) {
+    const SiteB s = sb[t / nb];
+    const int c = t % nb;
+    double v[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      v[k] = 0.0;
+      if (s.nb[k] < 0) continue;
+      const PatchDev<Real>& P = cp[s.nb[k]];
+      const int i = s.ci + k - 1;
+      const double n = bval(P.B, P.blo0, P.bnx, c, i);
+      v[k] = a == 1.0 ? n : tinterp(bval(P.Bold, P.blo0, P.bnx, c, i), n, a);
+    }
+    double* o = svb + (size_t)t * 2;
+    o[0] = v[1];
+    o[1] = slope(s.kind, v[0], v[1], v[2]);
+  }
+}
+
+// fine ghost cells: site value + linear terms (x first, then y)
+template <typename Real>
+__global__ void cf_apply_kernel(const PatchDev<Real>* __restrict__ fp, const FineU* __restrict__ fu, int nfu,
+                                const FineB* __restrict__ fb, int nfb, int nb,
+                                const double* __restrict__ svu, const double* __restrict__ svb) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nfu * NC) {
+    const FineU e = fu[t / NC];
+    const int c = t % NC;
+    const double* s = svu + ((size_t)e.site * NC + c) * 3;
+    double v = s[0];
+    v = v + e.cx * s[1];
+    v = v + e.cy * s[2];
+    const PatchDev<Real>& P = fp[e.fpatch];
+    ((Real*)P.Uin)[fab_idx(P, c, e.i, e.j)] = (Real)v;
+    return;
+  }
+  t -= nfu * NC;
+  if (t < nfb * nb) {
+    const FineB e = fb[t / nb];
+    const int c = t % nb;
+    const double* s = svb + ((size_t)e.site * nb + c) * 2;
+    double v = s[0];
+    v = v + e.cx * s[1];
+    const PatchDev<Real>& P = fp[e.fpatch];
+    P.B[(size_t)c * P.bnx + (e.i - P.blo0)] = v;
+  }
+}
+
+// fault data at the start of a step (AMRLevelLinElast::advance m_BOld.copy)
+template <typename Real>
+__global__ void bsnap_kernel(const PatchDev<Real>* __restrict__ pd, const int* __restrict__ fpatches, int nb) {
+  const PatchDev<Real>& P = pd[fpatches[blockIdx.x]];
+  const int n = nb * P.bnx;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) P.Bold[k] = P.B[k];
+}
+
+// LevelFluxRegister::incrementCoarse: R = -dt * F_coarse
+__global__ void reg_coarse_kernel(const double* __restrict__ cap, const int* __restrict__ cslot, int nent, double dt,
+                                  double* __restrict__ R) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nent * NC) return;
+  const int e = t / NC, c = t % NC;
+  R[t] = -(dt * cap[(size_t)cslot[e] * NC + c]);
+}
+
+// LevelFluxRegister::incrementFine: R += (dt / r) * F_fine over the r fine faces
+__global__ void reg_fine_kernel(const double* __restrict__ cap, const int* __restrict__ fslot, int nent, int r,
+                                double s, double* __restrict__ R) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nent * NC) return;
+  const int e = t / NC, c = t % NC;
+  double v = R[t];
+  for (int m = 0; m < r; ++m) v = v + s * cap[(size_t)fslot[e * r + m] * NC + c];
+  R[t] = v;
+}
+
+// LevelFluxRegister::reflux: each coarse cell applies its entries in order
+template <typename Real>
+__global__ void reflux_kernel(const PatchDev<Real>* __restrict__ cp, const RefluxCell* __restrict__ cells, int ncells,
+                              const int* __restrict__ list, const double* __restrict__ sc,
+                              const double* __restrict__ R) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncells * NC) return;
+  const RefluxCell cl = cells[t / NC];
+  const int c = t % NC;
+  const PatchDev<Real>& P = cp[cl.cpatch];
+  Real* U = (Real*)P.Uin;
+  const size_t o = fab_idx(P, c, cl.ci, cl.cj);
+  double v = (double)U[o];
+  for (int k = cl.e0; k < cl.e1; ++k) {
+    const int e = list[k];
+    v = v + R[(size_t)e * NC + c] * sc[e];
+  }
+  U[o] = (Real)v;
+}
+
+// average-down of U (r x r children, x fastest) and of the fault rows (r children)
+template <typename Real>
+__global__ void avgdown_kernel(const PatchDev<Real>* __restrict__ cp, const PatchDev<Real>* __restrict__ fp,
+                               const AvgU* __restrict__ au, int nau, const AvgB* __restrict__ ab, int nab, int nb,
+                               int r, double sU, double sB, int both) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nau * NC) {
+    const AvgU e = au[t / NC];
+    const int c = t % NC;
+    const PatchDev<Real>& F = fp[e.fpatch];
+    double sum = 0.0;
+    for (int jj = 0; jj < r; ++jj)
+      for (int ii = 0; ii < r; ++ii) sum = sum + (double)F.Uin[fab_idx(F, c, r * e.ci + ii, r * e.cj + jj)];
+    const PatchDev<Real>& C = cp[e.cpatch];
+    const size_t o = fab_idx(C, c, e.ci, e.cj);
+    const Real v = (Real)(sum * sU);
+    ((Real*)C.Uin)[o] = v;
+    // lambda, gamma: a step without plasticity never rewrites them, keep both buffers equal
+    if (both && (c == 9 || c == 10 || c == 20 || c == 21)) C.Uout[o] = v;
+    return;
+  }
+  t -= nau * NC;
+  if (t < nab * nb) {
+    const AvgB e = ab[t / nb];
+    const int c = t % nb;
+    const PatchDev<Real>& F = fp[e.fpatch];
+    double sum = 0.0;
+    for (int ii = 0; ii < r; ++ii) sum = sum + bval(F.B, F.blo0, F.bnx, c, r * e.ci + ii);
+    const PatchDev<Real>& C = cp[e.cpatch];
+    C.B[(size_t)c * C.bnx + (e.ci - C.blo0)] = sum * sB;
+  }
+}
+
+// regrid prolongation of valid cells: constant + limited linear, into both buffers
+template <typename Real>
+__global__ void finterp_kernel(const PatchDev<Real>* __restrict__ cp, const PatchDev<Real>* __restrict__ fp,
+                               const InterpU* __restrict__ iu, int niu, const InterpB* __restrict__ ib, int nib,
+                               int nb, int r) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < niu * NC) {
+    const InterpU e = iu[t / NC];
+    const int c = t % NC;
+    double v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      v[k] = e.nb[k] >= 0 ? (double)cp[e.nb[k]].Uin[fab_idx(cp[e.nb[k]], c, e.ci + k % 3 - 1, e.cj + k / 3 - 1)]
+                          : 0.0;
+    const double u0 = v[4];
+    double sx = slope(e.kx, v[3], u0, v[5]);
+    double sy = slope(e.ky, v[1], u0, v[7]);
+    if (e.lim) {
+      double mn = u0, mx = u0;
+#pragma unroll
+      for (int k = 0; k < 9; ++k)
+        if (e.nb[k] >= 0) { mn = dmin(mn, v[k]); mx = dmax(mx, v[k]); }
+      limit2(sx, sy, u0, mn, mx);
+    }
+    const PatchDev<Real>& F = fp[e.fpatch];
+    for (int jj = 0; jj < r; ++jj)
+      for (int ii = 0; ii < r; ++ii) {
+        const int i = r * e.ci + ii, j = r * e.cj + jj;
+        double w = u0;
+        w = w + icoef(i, e.ci, r) * sx;
+        w = w + icoef(j, e.cj, r) * sy;
+        const size_t o = fab_idx(F, c, i, j);
+        ((Real*)F.Uin)[o] = (Real)w;
+        F.Uout[o] = (Real)w;
+      }
+    return;
+  }
+  t -= niu * NC;
+  if (t < nib * nb) {
+    const InterpB e = ib[t / nb];
+    const int c = t % nb;
+    double v[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      v[k] = 0.0;
+      if (e.nb[k] >= 0) { const PatchDev<Real>& P = cp[e.nb[k]]; v[k] = bval(P.B, P.blo0, P.bnx, c, e.ci + k - 1); }
+    }
+    const double u0 = v[1];
+    double s = slope(e.kind, v[0], u0, v[2]);
+    if (e.lim) {
+      double mn = u0, mx = u0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { mn = dmin(mn, v[k]); mx = dmax(mx, v[k]); }
+      double s1 = 0.0;
+      limit2(s, s1, u0, mn, mx);
+    }
+    const PatchDev<Real>& F = fp[e.fpatch];
+    for (int ii = 0; ii < r; ++ii) {
+      const int i = r * e.ci + ii;
+      double w = u0;
+      w = w + icoef(i, e.ci, r) * s;
+      F.B[(size_t)c * F.bnx + (i - F.blo0)] = w;
+    }
+  }
+}
+
+// copy of overlapping valid regions between two levels (regrid), both buffers
+template <typename Real>
+__global__ void xcopy_kernel(const PatchDev<Real>* __restrict__ dst, const PatchDev<Real>* __restrict__ src,
+                             const CopyDev* __restrict__ copies, int nu, int nb) {
+  const CopyDev cp = copies[blockIdx.x];
+  const PatchDev<Real>& S = src[cp.src];
+  const PatchDev<Real>& D = dst[cp.dst];
+  const int nx = cp.hi0 - cp.lo0 + 1, ny = cp.hi1 - cp.lo1 + 1;
+  if ((int)blockIdx.x < nu) {
+    for (int idx = threadIdx.x; idx < NC * nx * ny; idx += blockDim.x) {
+      const int c = idx / (nx * ny), j = cp.lo1 + (idx / nx) % ny, i = cp.lo0 + idx % nx;
+      const Real v = S.Uin[fab_idx(S, c, i, j)];
+      const size_t o = fab_idx(D, c, i, j);
+      ((Real*)D.Uin)[o] = v;
+      D.Uout[o] = v;
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < nb * nx; idx += blockDim.x) {
+      const int c = idx / nx, i = cp.lo0 + idx % nx;
+      D.B[(size_t)c * D.bnx + (i - D.blo0)] = bval(S.B, S.blo0, S.bnx, c, i);
+    }
+  }
+}
+
+unsigned blocks_for(long long n, int nt) { return (unsigned)std::max(1LL, (n + nt - 1) / nt); }
+
+template <typename T>
+tmk_status upload(std::vector<void*>& allocs, T** dptr, const std::vector<T>& v) {
+  *dptr = nullptr;
+  if (v.empty()) return TMK_OK;
+  if (dalloc(dptr, v.size()) != cudaSuccess) return TMK_ERR_ALLOC;
+  allocs.push_back(*dptr);
+  TMK_CU(cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return TMK_OK;
+}
+
+int patch_at(const tmk_level_s* L, int i, int j) {
+  for (size_t p = 0; p < L->patches.size(); ++p)
+    if (box_has(L->patches[p].valid, i, j)) return (int)p;
+  return -1;
+}
+int fault_patch_at(const tmk_level_s* L, int i) {
+  for (size_t p = 0; p < L->patches.size(); ++p)
+    if (L->patches[p].fault && i >= L->patches[p].valid.lo[0] && i <= L->patches[p].valid.hi[0]) return (int)p;
+  return -1;
+}
+
+}  // namespace
+
+namespace tmk_host {
+
+// a captured face: the patch that computes it, the direction and face index
+using FaceKey = std::tuple<int, int, int, int>;   // (patch, dir, i, j)
+
+struct CFLink {
+  tmk_level_s* F = nullptr;
+  tmk_level_s* C = nullptr;
+  int r = 1;
+  std::vector<void*> allocs;
+  // coarse-fine ghost fill
+  SiteU* dsu = nullptr; int nsu = 0;
+  FineU* dfu = nullptr; int nfu = 0;
+  SiteB* dsb = nullptr; int nsb = 0;
+  FineB* dfb = nullptr; int nfb = 0;
+  double* dsvu = nullptr;
+  double* dsvb = nullptr;
+  // flux register
+  int nent = 0;
+  std::vector<FaceKey> cface;        // per entry, captured by C
+  std::vector<FaceKey> fface;        // r per entry, captured by F
+  int* dcslot = nullptr;
+  int* dfslot = nullptr;
+  double* dR = nullptr;
+  RefluxCell* dcells = nullptr; int ncells = 0;
+  int* dlist = nullptr;
+  double* dsc = nullptr;
+  // average-down and prolongation
+  AvgU* dau = nullptr; int nau = 0;
+  AvgB* dab = nullptr; int nab = 0;
+  InterpU* diu = nullptr; int niu = 0;
+  InterpB* dib = nullptr; int nib = 0;
+  ~CFLink() { for (void* p : allocs) cudaFree(p); }
+};
+
+}  // namespace tmk_host
+
+namespace {
+
+// Assign capture slots to the faces that the level's links need, group them
+// by the tile that computes them, and refresh the links' slot tables.
+tmk_status rebuild_captures(tmk_level_s* L) {
+  std::map<FaceKey, int> slot;
+  if (L->coarser) for (const FaceKey& k : L->coarser->fface) slot.emplace(k, 0);
+  if (L->finer) for (const FaceKey& k : L->finer->cface) slot.emplace(k, 0);
+  int n = 0;
+  for (auto& kv : slot) kv.second = n++;
+  // owning tile of each face: x face i belongs to the tile holding cell i (the
+  // patch's last hi face to its last tile), likewise for y faces
+  std::vector<std::vector<int4>> per_tile(L->htiles.size());
+  for (const auto& kv : slot) {
+    const int p = std::get<0>(kv.first), d = std::get<1>(kv.first);
+    const int i = std::get<2>(kv.first), j = std::get<3>(kv.first);
+    const tmk_box& v = L->patches[p].valid;
+    const int ci = d == 0 ? std::min(i, v.hi[0]) : i, cj = d == 1 ? std::min(j, v.hi[1]) : j;
+    int owner = -1;
+    for (size_t t = 0; t < L->htiles.size(); ++t) {
+      const TileDev& tl = L->htiles[t];
+      if (tl.patch == p && ci >= tl.x0 && ci < tl.x0 + tl.nx && cj >= tl.y0 && cj < tl.y0 + tl.ny) { owner = (int)t; break; }
+    }
+    if (owner < 0) return TMK_ERR_BAD_DESC;
+    per_tile[owner].push_back(make_int4(d, i, j, kv.second));
+  }
+  std::vector<int4> list;
+  for (size_t t = 0; t < L->htiles.size(); ++t) {
+    L->htiles[t].cap0 = (int)list.size();
+    L->htiles[t].ncap = (int)per_tile[t].size();
+    list.insert(list.end(), per_tile[t].begin(), per_tile[t].end());
+  }
+  TMK_CU(cudaDeviceSynchronize());
+  for (void* p : L->cap_allocs) cudaFree(p);
+  L->cap_allocs.clear();
+  L->cap = nullptr; L->dcaplist = nullptr; L->ncap = n;
+  if (n) {
+    if (dalloc(&L->cap, (size_t)n * NC) != cudaSuccess) return TMK_ERR_ALLOC;
+    L->cap_allocs.push_back(L->cap);
+    TMK_CU(cudaMemset(L->cap, 0, (size_t)n * NC * sizeof(double)));
+    if (dalloc(&L->dcaplist, list.size()) != cudaSuccess) return TMK_ERR_ALLOC;
+    L->cap_allocs.push_back(L->dcaplist);
+    TMK_CU(cudaMemcpy(L->dcaplist, list.data(), list.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  }
+  TMK_CU(cudaMemcpy(L->dtiles, L->htiles.data(), L->htiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice));
+  L->march = (L->march_allowed && n == 0) ? 1 : 0;    // the tile kernel captures faces
+  if (upload_patchdev(L, 0) != TMK_OK) return TMK_ERR_CUDA;
+  // slot tables of the links that use this level's captures
+  if (L->coarser && L->coarser->nent) {
+    std::vector<int> fs;
+    for (const FaceKey& k : L->coarser->fface) fs.push_back(slot[k]);
+    TMK_CU(cudaMemcpy(L->coarser->dfslot, fs.data(), fs.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  if (L->finer && L->finer->nent) {
+    std::vector<int> cs;
+    for (const FaceKey& k : L->finer->cface) cs.push_back(slot[k]);
+    TMK_CU(cudaMemcpy(L->finer->dcslot, cs.data(), cs.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  TMK_CU(cudaDeviceSynchronize());
+  return TMK_OK;
+}
+
+void free_link(CFLink* k) {
+  if (!k) return;
+  cudaDeviceSynchronize();
+  delete k;
+}
+
+// Unlink level F from its coarser level (both sides' captures are rebuilt).
+void detach(tmk_level_s* F) {
+  CFLink* k = F->coarser;
+  if (!k) return;
+  tmk_level_s* C = k->C;
+  F->coarser = nullptr;
+  if (C && C->finer == k) C->finer = nullptr;
+  free_link(k);
+  rebuild_captures(F);
+  if (C) rebuild_captures(C);
+}
+
+tmk_status build_link(CFLink* k) {
+  tmk_level_s* F = k->F;
+  tmk_level_s* C = k->C;
+  const int r = k->r;
+  const int nb = F->ctx->nb;
+  const tmk_box& fdom = F->domain;
+  const tmk_box& cdom = C->domain;
+  std::vector<tmk_box> cfb;
+  for (const LevelPatch& lp : F->patches) cfb.push_back(coarsen(lp.valid, r));
+  auto covered_by_fine = [&](int ci, int cj) {
+    for (const tmk_box& b : cfb) if (box_has(b, ci, cj)) return true;
+    return false;
+  };
+  auto covered_by_fine_row = [&](int ci) {
+    for (size_t q = 0; q < F->patches.size(); ++q)
+      if (F->patches[q].fault && ci >= cfb[q].lo[0] && ci <= cfb[q].hi[0]) return true;
+    return false;
+  };
+  // ---- coarse-fine ghost fill of U
+  std::vector<SiteU> su;
+  std::vector<FineU> fu;
+  std::map<std::pair<int, int>, int> site_of;
+  for (size_t p = 0; p < F->patches.size(); ++p) {
+    const tmk_box& V = F->patches[p].valid;
+    const tmk_box g = box_isect(box_grow(V, NG), fdom);
+    for (int j = g.lo[1]; j <= g.hi[1]; ++j)
+      for (int i = g.lo[0]; i <= g.hi[0]; ++i) {
+        if (box_has(V, i, j)) continue;
+        const int ci = cdiv(i, r), cj = cdiv(j, r);
+        if (covered_by_fine(ci, cj)) continue;
+        if (patch_at(C, ci, cj) < 0) return TMK_ERR_BAD_DESC;   // not properly nested
+        auto it = site_of.find({ci, cj});
+        int sidx;
+        if (it == site_of.end()) {
+          SiteU s;
+          s.ci = ci; s.cj = cj;
+          for (int k9 = 0; k9 < 9; ++k9) s.nb[k9] = patch_at(C, ci + k9 % 3 - 1, cj + k9 / 3 - 1);
+          const bool xm = s.nb[3] >= 0, xp = s.nb[5] >= 0, ym = s.nb[1] >= 0, yp = s.nb[7] >= 0;
+          s.kx = (xm && xp) ? SL_CENTRED : xm ? SL_LO : xp ? SL_HI : SL_NONE;
+          s.ky = (ym && yp) ? SL_CENTRED : ym ? SL_LO : yp ? SL_HI : SL_NONE;
+          tmk_box one; one.lo[0] = ci - 1; one.lo[1] = cj - 1; one.hi[0] = ci + 1; one.hi[1] = cj + 1;
+          s.lim = box_contains(cdom, one) ? 1 : 0;
+          sidx = (int)su.size();
+          su.push_back(s);
+          site_of[{ci, cj}] = sidx;
+        } else {
+          sidx = it->second;
+        }
+        FineU e;
+        e.fpatch = (int)p; e.i = i; e.j = j; e.site = sidx;
+        e.cx = -0.5 + ((double)(i - r * ci) + 0.5) / (double)r;
+        e.cy = -0.5 + ((double)(j - r * cj) + 0.5) / (double)r;
+        fu.push_back(e);
+      }
+  }
+  // ---- coarse-fine ghost fill of the fault rows
+  std::vector<SiteB> sb;
+  std::vector<FineB> fb;
+  std::map<int, int> bsite_of;
+  if (nb > 0)
+    for (size_t p = 0; p < F->patches.size(); ++p) {
+      if (!F->patches[p].fault) continue;
+      const tmk_box& V = F->patches[p].valid;
+      const int lo = std::max(V.lo[0] - NG, fdom.lo[0]), hi = std::min(V.hi[0] + NG, fdom.hi[0]);
+      for (int i = lo; i <= hi; ++i) {
+        if (i >= V.lo[0] && i <= V.hi[0]) continue;
+        const int ci = cdiv(i, r);
+        if (covered_by_fine_row(ci)) continue;
+        if (fault_patch_at(C, ci) < 0) return TMK_ERR_BAD_DESC;
+        auto it = bsite_of.find(ci);
+        int sidx;
+        if (it == bsite_of.end()) {
+          SiteB s;
+          s.ci = ci;
+          for (int k3 = 0; k3 < 3; ++k3) s.nb[k3] = fault_patch_at(C, ci + k3 - 1);
+          const bool hm = s.nb[0] >= 0, hp = s.nb[2] >= 0;
+          s.kind = (hm && hp) ? SL_CENTRED : hm ? SL_LO : hp ? SL_HI : SL_NONE;
+          sidx = (int)sb.size();
+          sb.push_back(s);
+          bsite_of[ci] = sidx;
+        } else {
+          sidx = it->second;
+        }
+        FineB e;
+        e.fpatch = (int)p; e.i = i; e.site = sidx;
+        e.cx = -0.5 + ((double)(i - r * ci) + 0.5) / (double)r;
+        fb.push_back(e);
+      }
+    }
+  // ---- flux register: entries in the order d, side (lo, hi), fine patch, tangential
+  struct Ent { int q, ci, cj, side; };
+  std::vector<Ent> ents;
+  for (int d = 0; d < 2; ++d)
+    for (int side = -1; side <= 1; side += 2)
+      for (size_t p = 0; p < F->patches.size(); ++p) {
+        const tmk_box& vc = cfb[p];
+        const tmk_box& V = F->patches[p].valid;
+        const int t = 1 - d;
+        const int kd = side < 0 ? vc.lo[d] - 1 : vc.hi[d] + 1;
+        for (int kt = vc.lo[t]; kt <= vc.hi[t]; ++kt) {
+          const int ci = d == 0 ? kd : kt, cj = d == 0 ? kt : kd;
+          if (!box_has(cdom, ci, cj) || covered_by_fine(ci, cj)) continue;
+          const int q = patch_at(C, ci, cj);
+          if (q < 0) return TMK_ERR_BAD_DESC;
+          const int cf = kd + (side < 0 ? 1 : 0);
+          k->cface.emplace_back(q, d, d == 0 ? cf : ci, d == 0 ? cj : cf);
+          const int ff = side < 0 ? V.lo[d] : V.hi[d] + 1;
+          for (int m = 0; m < r; ++m) {
+            const int tt = r * kt + m;
+            k->fface.emplace_back((int)p, d, d == 0 ? ff : tt, d == 0 ? tt : ff);
+          }
+          ents.push_back({q, ci, cj, side});
+        }
+      }
+  k->nent = (int)ents.size();
+  // reflux: entries grouped by coarse cell, each cell's entries in register order
+  std::map<std::tuple<int, int, int>, std::vector<int>> by_cell;
+  for (int e = 0; e < k->nent; ++e) by_cell[std::make_tuple(ents[e].q, ents[e].ci, ents[e].cj)].push_back(e);
+  std::vector<RefluxCell> cells;
+  std::vector<int> list;
+  for (const auto& kv : by_cell) {
+    RefluxCell rc;
+    rc.cpatch = std::get<0>(kv.first); rc.ci = std::get<1>(kv.first); rc.cj = std::get<2>(kv.first);
+    rc.e0 = (int)list.size();
+    list.insert(list.end(), kv.second.begin(), kv.second.end());
+    rc.e1 = (int)list.size();
+    cells.push_back(rc);
+  }
+  const double scale = -1.0 / C->dx;
+  std::vector<double> sc;
+  for (const Ent& e : ents) sc.push_back(e.side < 0 ? scale : -scale);
+  // ---- average-down and prolongation lists
+  std::vector<AvgU> au;
+  std::vector<AvgB> ab;
+  std::vector<InterpU> iu;
+  std::vector<InterpB> ib;
+  for (size_t p = 0; p < F->patches.size(); ++p) {
+    const tmk_box& vc = cfb[p];
+    for (int cj = vc.lo[1]; cj <= vc.hi[1]; ++cj)
+      for (int ci = vc.lo[0]; ci <= vc.hi[0]; ++ci) {
+        const int q = patch_at(C, ci, cj);
+        if (q < 0) return TMK_ERR_BAD_DESC;
+        au.push_back({q, ci, cj, (int)p});
+        InterpU e;
+        e.fpatch = (int)p; e.ci = ci; e.cj = cj;
+        for (int k9 = 0; k9 < 9; ++k9) e.nb[k9] = patch_at(C, ci + k9 % 3 - 1, cj + k9 / 3 - 1);
+        int kind[2];
+        for (int d = 0; d < 2; ++d) {
+          const int cd = d == 0 ? ci : cj;
+          const bool atlo = cd == cdom.lo[d], athi = cd == cdom.hi[d];
+          kind[d] = (!atlo && !athi) ? SL_CENTRED : (atlo && !athi) ? SL_HI : (athi && !atlo) ? SL_LO : SL_NONE;
+          const int kp = d == 0 ? 5 : 7, km = d == 0 ? 3 : 1;
+          if ((kind[d] == SL_CENTRED || kind[d] == SL_HI) && e.nb[kp] < 0) return TMK_ERR_BAD_DESC;
+          if ((kind[d] == SL_CENTRED || kind[d] == SL_LO) && e.nb[km] < 0) return TMK_ERR_BAD_DESC;
+        }
+        e.kx = kind[0]; e.ky = kind[1];
+        tmk_box one; one.lo[0] = ci - 1; one.lo[1] = cj - 1; one.hi[0] = ci + 1; one.hi[1] = cj + 1;
+        e.lim = box_contains(cdom, one) ? 1 : 0;
+        iu.push_back(e);
+      }
+    if (nb == 0 || !F->patches[p].fault) continue;
+    for (int ci = vc.lo[0]; ci <= vc.hi[0]; ++ci) {
+      const int q = fault_patch_at(C, ci);
+      if (q < 0) return TMK_ERR_BAD_DESC;
+      ab.push_back({q, ci, (int)p});
+      InterpB e;
+      e.fpatch = (int)p; e.ci = ci;
+      for (int k3 = 0; k3 < 3; ++k3) e.nb[k3] = fault_patch_at(C, ci + k3 - 1);
+      const bool atlo = ci == cdom.lo[0], athi = ci == cdom.hi[0];
+      e.kind = (!atlo && !athi) ? SL_CENTRED : (atlo && !athi) ? SL_HI : (athi && !atlo) ? SL_LO : SL_NONE;
+      if ((e.kind == SL_CENTRED || e.kind == SL_HI) && e.nb[2] < 0) return TMK_ERR_BAD_DESC;
+      if ((e.kind == SL_CENTRED || e.kind == SL_LO) && e.nb[0] < 0) return TMK_ERR_BAD_DESC;
+      e.lim = (ci - 1 >= cdom.lo[0] && ci + 1 <= cdom.hi[0]) ? 1 : 0;
+      ib.push_back(e);
+    }
+  }
+  // ---- upload
+  tmk_status st;
+  if ((st = upload(k->allocs, &k->dsu, su)) != TMK_OK) return st;
+  if ((st = upload(k->allocs, &k->dfu, fu)) != TMK_OK) return st;
+  if ((st = upload(k->allocs, &k->dsb, sb)) != TMK_OK) return st;
+  if ((st = upload(k->allocs, &k->dfb, fb)) != TMK_OK) return st;
+  k->nsu = (int)su.size(); k->nfu = (int)fu.size(); k->nsb = (int)sb.size(); k->nfb = (int)fb.size();
+  if (k->nsu) {
+    if (dalloc(&k->dsvu, (size_t)k->nsu * NC * 3) != cudaSuccess) return TMK_ERR_ALLOC;
+    k->allocs.push_back(k->dsvu);
+  }
+  if (k->nsb) {
+    if (dalloc(&k->dsvb, (size_t)k->nsb * nb * 2) != cudaSuccess) return TMK_ERR_ALLOC;
+    k->allocs.push_back(k->dsvb);
+  }
+  if (k->nent) {
+    if (dalloc(&k->dcslot, (size_t)k->nent) != cudaSuccess || dalloc(&k->dfslot, (size_t)k->nent * r) != cudaSuccess ||
+        dalloc(&k->dR, (size_t)k->nent * NC) != cudaSuccess)
+      return TMK_ERR_ALLOC;
+    k->allocs.push_back(k->dcslot); k->allocs.push_back(k->dfslot); k->allocs.push_back(k->dR);
+    TMK_CU(cudaMemset(k->dR, 0, (size_t)k->nent * NC * sizeof(double)));
+  }
+  if ((st = upload(k->allocs, &k->dcells, cells)) != TMK_OK) return st;
+  if ((st = upload(k->allocs, &k->dlist, list)) != TMK_OK) return st;
+  if ((st = upload(k->allocs, &k->dsc, sc)) != TMK_OK) return st;
+  k->ncells = (int)cells.size();
+  if ((st = upload(k->allocs, &k->dau, au)) != TMK_OK) return st;
+  if ((st = upload(k->allocs, &k->dab, ab)) != TMK_OK) return st;
+  if ((st = upload(k->allocs, &k->diu, iu)) != TMK_OK) return st;
+  if ((st = upload(k->allocs, &k->dib, ib)) != TMK_OK) return st;
+  k->nau = (int)au.size(); k->nab = (int)ab.size(); k->niu = (int)iu.size(); k->nib = (int)ib.size();
+  return TMK_OK;
+}
+
+// fault data snapshots for the levels that have a finer level
+tmk_status ensure_bold(tmk_level_s* L) {
+  for (LevelPatch& lp : L->patches) {
+    if (!lp.fault || lp.Bold) continue;
+    if (dalloc(&lp.Bold, (size_t)L->ctx->nb * lp.bnx) != cudaSuccess) return TMK_ERR_ALLOC;
+    L->allocs.push_back(lp.Bold);
+    TMK_CU(cudaMemcpy(lp.Bold, lp.B, (size_t)L->ctx->nb * lp.bnx * sizeof(double), cudaMemcpyDeviceToDevice));
+  }
+  return TMK_OK;
+}
+
+template <typename Real>
+tmk_status launch_fill(CFLink* k, double alpha, cudaStream_t s) {
+  const int nb = k->F->ctx->nb;
+  const long long ns = (long long)k->nsu * NC + (long long)k->nsb * nb;
+  const long long nf = (long long)k->nfu * NC + (long long)k->nfb * nb;
+  if (ns == 0) return TMK_OK;
+  const PatchDev<Real>* cp = (const PatchDev<Real>*)k->C->dpatch[k->C->parity];
+  const PatchDev<Real>* fp = (const PatchDev<Real>*)k->F->dpatch[k->F->parity];
+  cf_sites_kernel<Real><<<blocks_for(ns, 128), 128, 0, s>>>(cp, k->dsu, k->nsu, k->dsb, k->nsb, nb, alpha,
+                                                             k->dsvu, k->dsvb);
+  TMK_CU(cudaGetLastError());
+  cf_apply_kernel<Real><<<blocks_for(nf, 128), 128, 0, s>>>(fp, k->dfu, k->nfu, k->dfb, k->nfb, nb, k->dsvu,
+                                                             k->dsvb);
+  TMK_CU(cudaGetLastError());
+  return TMK_OK;
+}
+
+tmk_status fill(CFLink* k, double alpha, cudaStream_t s) {
+  return k->F->prec == TMK_PREC_MIXED ? launch_fill<float>(k, alpha, s) : launch_fill<double>(k, alpha, s);
+}
+
+template <typename Real>
+tmk_status launch_reflux(CFLink* k, cudaStream_t s) {
+  if (!k->ncells) return TMK_OK;
+  const PatchDev<Real>* cp = (const PatchDev<Real>*)k->C->dpatch[k->C->parity];
+  reflux_kernel<Real><<<blocks_for((long long)k->ncells * NC, 128), 128, 0, s>>>(cp, k->dcells, k->ncells,
+                                                                                   k->dlist, k->dsc, k->dR);
+  TMK_CU(cudaGetLastError());
+  return TMK_OK;
+}
+
+template <typename Real>
+tmk_status launch_avgdown(CFLink* k, cudaStream_t s) {
+  const int nb = k->F->ctx->nb;
+  const long long n = (long long)k->nau * NC + (long long)k->nab * nb;
+  if (!n) return TMK_OK;
+  const PatchDev<Real>* cp = (const PatchDev<Real>*)k->C->dpatch[k->C->parity];
+  const PatchDev<Real>* fp = (const PatchDev<Real>*)k->F->dpatch[k->F->parity];
+  const int r = k->r;
+  const int both = k->C->ctx->scheme.plasticity ? 0 : 1;
+  avgdown_kernel<Real><<<blocks_for(n, 128), 128, 0, s>>>(cp, fp, k->dau, k->nau, k->dab, k->nab, nb, r,
+                                                          1.0 / (double)(r * r), 1.0 / (double)r, both);
+  TMK_CU(cudaGetLastError());
+  return TMK_OK;
+}
+
+template <typename Real>
+tmk_status launch_interp(CFLink* k, cudaStream_t s) {
+  const int nb = k->F->ctx->nb;
+  const long long n = (long long)k->niu * NC + (long long)k->nib * nb;
+  if (!n) return TMK_OK;
+  const PatchDev<Real>* cp = (const PatchDev<Real>*)k->C->dpatch[k->C->parity];
+  const PatchDev<Real>* fp = (const PatchDev<Real>*)k->F->dpatch[k->F->parity];
+  finterp_kernel<Real><<<blocks_for(n, 128), 128, 0, s>>>(cp, fp, k->diu, k->niu, k->dib, k->nib, nb, k->r);
+  TMK_CU(cudaGetLastError());
+  return TMK_OK;
+}
+
+double snap_alpha(double time, double dt, double tco, double tcn, int r) {
+  double alpha = (time - tco) / (tcn - tco);
+  const double eps = 0.04 * dt / r;
+  if (std::fabs(alpha) < eps) alpha = 0.0;
+  if (std::fabs(1.0 - alpha) < eps) alpha = 1.0;
+  return alpha;
+}
+
+}  // namespace
+
+// ------------------------------------------------------- level-step hooks
+namespace tmk_host {
+
+tmk_status amr_pre_step(tmk_level_s* L, double time, double dt, double tco, double tcn, cudaStream_t s) {
+  if (L->finer && L->nfault && L->ctx->nb > 0) {
+    if (L->prec == TMK_PREC_MIXED)
+      bsnap_kernel<float><<<L->nfault, 256, 0, s>>>((const PatchDev<float>*)L->dpatch[L->parity], L->dfault,
+                                                     L->ctx->nb);
+    else
+      bsnap_kernel<double><<<L->nfault, 256, 0, s>>>((const PatchDev<double>*)L->dpatch[L->parity], L->dfault,
+                                                      L->ctx->nb);
+    TMK_CU(cudaGetLastError());
+  }
+  if (L->coarser) {
+    const double alpha = snap_alpha(time, dt, tco, tcn, L->coarser->r);
+    if (!(alpha >= 0.0 && alpha <= 1.0)) return TMK_ERR_BAD_DESC;   // LinElastLevelGodunov.cpp:246-256
+    return fill(L->coarser, alpha, s);
+  }
+  return TMK_OK;
+}
+
+tmk_status amr_post_step(tmk_level_s* L, double dt, cudaStream_t s) {
+  if (L->finer && L->finer->nent) {
+    CFLink* k = L->finer;
+    reg_coarse_kernel<<<blocks_for((long long)k->nent * NC, 128), 128, 0, s>>>(L->cap, k->dcslot, k->nent, dt, k->dR);
+    TMK_CU(cudaGetLastError());
+  }
+  if (L->coarser && L->coarser->nent) {
+    CFLink* k = L->coarser;
+    reg_fine_kernel<<<blocks_for((long long)k->nent * NC, 128), 128, 0, s>>>(L->cap, k->dfslot, k->nent, k->r,
+                                                                             dt / (double)k->r, k->dR);
+    TMK_CU(cudaGetLastError());
+  }
+  return TMK_OK;
+}
+
+int amr_launches(const tmk_level_s* L) {
+  int n = 0;
+  if (L->finer && L->nfault && L->ctx->nb > 0) ++n;
+  if (L->coarser && (L->coarser->nsu || L->coarser->nsb)) n += 2;
+  if (L->finer && L->finer->nent) ++n;
+  if (L->coarser && L->coarser->nent) ++n;
+  return n;
+}
+
+void amr_release(tmk_level_s* L) {
+  if (L->finer) detach(L->finer->F);
+  if (L->coarser) detach(L);
+}
+
+}  // namespace tmk_host
+
+// ================================================================= C ABI ===
+extern "C" tmk_status tmk_level_attach_coarser(tmk_level* fine, tmk_level* coarse, int ref_ratio) {
+  if (!fine || !coarse || fine == coarse || ref_ratio < 2) return TMK_ERR_BAD_DESC;
+  if (fine->ctx->nb != coarse->ctx->nb || fine->prec != coarse->prec) return TMK_ERR_BAD_DESC;
+  const int r = ref_ratio;
+  for (int d = 0; d < 2; ++d)
+    if (fine->domain.lo[d] != coarse->domain.lo[d] * r || fine->domain.hi[d] != (coarse->domain.hi[d] + 1) * r - 1)
+      return TMK_ERR_BAD_DESC;
+  if (std::fabs(fine->dx * r - coarse->dx) > 1e-9 * coarse->dx) return TMK_ERR_BAD_DESC;
+  for (const LevelPatch& lp : fine->patches)
+    for (int d = 0; d < 2; ++d)
+      if (lp.valid.lo[d] % r != 0 || (lp.valid.hi[d] + 1) % r != 0) return TMK_ERR_BAD_DESC;
+  detach(fine);
+  if (coarse->finer) detach(coarse->finer->F);
+  CFLink* k = new (std::nothrow) CFLink();
+  if (!k) return TMK_ERR_ALLOC;
+  k->F = fine; k->C = coarse; k->r = r;
+  tmk_status st = build_link(k);
+  if (st != TMK_OK) { free_link(k); return st; }
+  if ((st = ensure_bold(coarse)) != TMK_OK) { free_link(k); return st; }
+  fine->coarser = k;
+  coarse->finer = k;
+  if ((st = rebuild_captures(fine)) != TMK_OK || (st = rebuild_captures(coarse)) != TMK_OK) {
+    detach(fine);
+    return st;
+  }
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_detach_coarser(tmk_level* fine) {
+  if (!fine) return TMK_ERR_BAD_DESC;
+  detach(fine);
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_fill_coarse_fine(tmk_level* fine, double alpha, void* stream) {
+  if (!fine || !fine->coarser || !(alpha >= 0.0 && alpha <= 1.0)) return TMK_ERR_BAD_DESC;
+  return fill(fine->coarser, alpha, (cudaStream_t)stream);
+}
+
+extern "C" tmk_status tmk_level_reflux(tmk_level* coarse, void* stream) {
+  if (!coarse || !coarse->finer) return TMK_ERR_BAD_DESC;
+  CFLink* k = coarse->finer;
+  cudaStream_t s = (cudaStream_t)stream;
+  return coarse->prec == TMK_PREC_MIXED ? launch_reflux<float>(k, s) : launch_reflux<double>(k, s);
+}
+
+extern "C" tmk_status tmk_level_average_down(tmk_level* coarse, void* stream) {
+  if (!coarse || !coarse->finer) return TMK_ERR_BAD_DESC;
+  CFLink* k = coarse->finer;
+  cudaStream_t s = (cudaStream_t)stream;
+  return coarse->prec == TMK_PREC_MIXED ? launch_avgdown<float>(k, s) : launch_avgdown<double>(k, s);
+}
+
+extern "C" tmk_status tmk_level_interp_from_coarser(tmk_level* fine, void* stream) {
+  if (!fine || !fine->coarser) return TMK_ERR_BAD_DESC;
+  CFLink* k = fine->coarser;
+  cudaStream_t s = (cudaStream_t)stream;
+  return fine->prec == TMK_PREC_MIXED ? launch_interp<float>(k, s) : launch_interp<double>(k, s);
+}
+
+extern "C" tmk_status tmk_level_copy_overlap(tmk_level* dst, const tmk_level* src, void* stream) {
+  if (!dst || !src || dst == src || dst->prec != src->prec || dst->ctx->nb != src->ctx->nb) return TMK_ERR_BAD_DESC;
+  for (int d = 0; d < 2; ++d)
+    if (dst->domain.lo[d] != src->domain.lo[d] || dst->domain.hi[d] != src->domain.hi[d]) return TMK_ERR_BAD_DESC;
+  std::vector<CopyDev> cu, cb;
+  for (size_t p = 0; p < dst->patches.size(); ++p)
+    for (size_t q = 0; q < src->patches.size(); ++q) {
+      const tmk_box x = box_isect(dst->patches[p].valid, src->patches[q].valid);
+      if (!box_ok(x)) continue;
+      CopyDev c; c.src = (int)q; c.dst = (int)p; c.lo0 = x.lo[0]; c.lo1 = x.lo[1]; c.hi0 = x.hi[0]; c.hi1 = x.hi[1];
+      cu.push_back(c);
+      if (dst->patches[p].fault && src->patches[q].fault && dst->ctx->nb > 0) { c.lo1 = c.hi1 = dst->domain.lo[1]; cb.push_back(c); }
+    }
+  if (cu.empty()) return TMK_OK;
+  std::vector<CopyDev> all(cu);
+  all.insert(all.end(), cb.begin(), cb.end());
+  CopyDev* d = nullptr;
+  if (dalloc(&d, all.size()) != cudaSuccess) return TMK_ERR_ALLOC;
+  cudaStream_t s = (cudaStream_t)stream;
+  tmk_status st = TMK_OK;
+  if (cudaMemcpy(d, all.data(), all.size() * sizeof(CopyDev), cudaMemcpyHostToDevice) != cudaSuccess) st = TMK_ERR_CUDA;
+  if (st == TMK_OK) {
+    if (dst->prec == TMK_PREC_MIXED)
+      xcopy_kernel<float><<<(unsigned)all.size(), 256, 0, s>>>((const PatchDev<float>*)dst->dpatch[dst->parity],
+                                                               (const PatchDev<float>*)src->dpatch[src->parity], d,
+                                                               (int)cu.size(), dst->ctx->nb);
+    else
+      xcopy_kernel<double><<<(unsigned)all.size(), 256, 0, s>>>((const PatchDev<double>*)dst->dpatch[dst->parity],
+                                                                (const PatchDev<double>*)src->dpatch[src->parity], d,
+                                                                (int)cu.size(), dst->ctx->nb);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) st = TMK_ERR_CUDA;
+  }
+  cudaFree(d);
+  return st;
+}
+
+extern "C" tmk_status tmk_level_register_size(const tmk_level* fine, int* entries) {
+  if (!fine || !entries || !fine->coarser) return TMK_ERR_BAD_DESC;
+  *entries = fine->coarser->nent;
+  return TMK_OK;
+}
+
+// --------------------------------------------------------------- hierarchy
+struct tmk_amr_s {
+  std::vector<tmk_level*> L;
+  std::vector<int> ratio;
+  std::vector<double> time, dtlast;
+};
+
+extern "C" tmk_status tmk_amr_create(int nlevels, tmk_level* const* levels, const int* ratios, double time,
+                                     tmk_amr** out) {
+  if (!out) return TMK_ERR_BAD_DESC;
+  *out = nullptr;
+  if (nlevels < 1 || !levels || (nlevels > 1 && !ratios)) return TMK_ERR_BAD_DESC;
+  for (int l = 0; l < nlevels; ++l) if (!levels[l]) return TMK_ERR_BAD_DESC;
+  if (levels[0]->coarser) detach(levels[0]);
+  for (int l = 0; l + 1 < nlevels; ++l) {
+    tmk_status st = tmk_level_attach_coarser(levels[l + 1], levels[l], ratios[l]);
+    if (st != TMK_OK) return st;
+  }
+  if (levels[nlevels - 1]->finer) detach(levels[nlevels - 1]->finer->F);
+  tmk_amr* h = new (std::nothrow) tmk_amr_s();
+  if (!h) return TMK_ERR_ALLOC;
+  h->L.assign(levels, levels + nlevels);
+  if (nlevels > 1) h->ratio.assign(ratios, ratios + nlevels - 1);
+  h->time.assign(nlevels, time);
+  h->dtlast.assign(nlevels, 0.0);
+  *out = h;
+  return TMK_OK;
+}
+
+extern "C" void tmk_amr_destroy(tmk_amr* h) { delete h; }
+
+namespace {
+// AMR::timeStep: advance level l, then ratio[l] substeps of level l+1, then
+// AMRLevelLinElast::postTimeStep (reflux, average-down of U and B)
+tmk_status amr_advance(tmk_amr* h, int l, double dt, cudaStream_t s) {
+  double tco = 0.0, tcn = 0.0;
+  if (l > 0) { tcn = h->time[l - 1]; tco = tcn - h->dtlast[l - 1]; }
+  tmk_status st = tmk_level_step_cf(h->L[l], h->time[l], dt, tco, tcn, s, nullptr);
+  if (st != TMK_OK) return st;
+  h->time[l] += dt;
+  h->dtlast[l] = dt;
+  if (l + 1 < (int)h->L.size()) {
+    const int r = h->ratio[l];
+    for (int k = 0; k < r; ++k)
+      if ((st = amr_advance(h, l + 1, dt / r, s)) != TMK_OK) return st;
+    if ((st = tmk_level_reflux(h->L[l], s)) != TMK_OK) return st;
+    if ((st = tmk_level_average_down(h->L[l], s)) != TMK_OK) return st;
+  }
+  return TMK_OK;
+}
+}  // namespace
+
+extern "C" tmk_status tmk_amr_step(tmk_amr* h, double dt0, void* stream) {
+  if (!h || !(dt0 > 0)) return TMK_ERR_BAD_DESC;
+  return amr_advance(h, 0, dt0, (cudaStream_t)stream);
+}
+
+extern "C" tmk_status tmk_amr_time(const tmk_amr* h, int level, double* t) {
+  if (!h || !t || level < 0 || level >= (int)h->L.size()) return TMK_ERR_BAD_DESC;
+  *t = h->time[level];
+  return TMK_OK;
+}
+
+extern "C" long long tmk_amr_cell_updates(const tmk_amr* h) {
+  if (!h) return 0;
+  long long total = 0, sub = 1;
+  for (size_t l = 0; l < h->L.size(); ++l) {
+    long long cells = 0;
+    for (const LevelPatch& lp : h->L[l]->patches)
+      cells += (long long)(lp.valid.hi[0] - lp.valid.lo[0] + 1) * (lp.valid.hi[1] - lp.valid.lo[1] + 1);
+    total += cells * sub;
+    if (l < h->ratio.size()) sub *= h->ratio[l];
+  }
+  return total;
+}
+
+extern "C" int tmk_amr_launches_per_step(const tmk_amr* h) {
+  if (!h) return 0;
+  int total = 0, sub = 1;
+  for (size_t l = 0; l < h->L.size(); ++l) {
+    int n = tmk_level_launches_per_step(h->L[l]);
+    if (l + 1 < h->L.size()) {
+      const CFLink* k = h->L[l]->finer;
+      if (k && k->ncells) ++n;
+      if (k && (k->nau || k->nab)) ++n;
+    }
+    total += n * sub;
+    if (l < h->ratio.size()) sub *= h->ratio[l];
+  }
+  return total;
+}

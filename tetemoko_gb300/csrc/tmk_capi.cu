@@ -14,34 +14,16 @@
 #include <new>
 #include <vector>
 
-#include "../../include/tetemoko_gb300.h"
-#include "tmk_kernels.cuh"
-#include "tmk_march.cuh"
-#include "tmk_launch.h"
+#include "tmk_internal.h"
 
 using tmk::DevParams;
 using tmk::DevStatus;
 using tmk::PatchDev;
 using tmk::TileDev;
 using tmk::CopyDev;
-
-#define TMK_CU(call)                                   \
-  do {                                                 \
-    cudaError_t e_ = (call);                           \
-    if (e_ != cudaSuccess) return TMK_ERR_CUDA;        \
-  } while (0)
+using namespace tmk_host;
 
 namespace {
-
-bool box_ok(const tmk_box& b) { return b.lo[0] <= b.hi[0] && b.lo[1] <= b.hi[1]; }
-bool box_contains(const tmk_box& a, const tmk_box& b) {
-  return a.lo[0] <= b.lo[0] && a.lo[1] <= b.lo[1] && a.hi[0] >= b.hi[0] && a.hi[1] >= b.hi[1];
-}
-tmk_box box_grow(tmk_box b, int n) { b.lo[0] -= n; b.lo[1] -= n; b.hi[0] += n; b.hi[1] += n; return b; }
-tmk_box box_isect(tmk_box a, const tmk_box& b) {
-  for (int d = 0; d < 2; ++d) { a.lo[d] = std::max(a.lo[d], b.lo[d]); a.hi[d] = std::min(a.hi[d], b.hi[d]); }
-  return a;
-}
 
 int device_ok() {
   int n = 0;
@@ -49,21 +31,7 @@ int device_ok() {
   return 1;
 }
 
-template <typename T>
-cudaError_t dalloc(T** p, size_t n) { return cudaMalloc((void**)p, n * sizeof(T) + 16); }
-
 }  // namespace
-
-struct tmk_context_s {
-  DevParams hp;
-  DevParams* dp = nullptr;
-  tmk_scheme scheme;
-  int nb = 0;
-  // patch-level scratch (grown on demand)
-  void* scratch = nullptr;
-  size_t scratch_bytes = 0;
-  DevStatus* dstatus = nullptr;
-};
 
 extern "C" int tmk_abi_version(void) { return TMK_ABI_VERSION; }
 
@@ -300,52 +268,6 @@ extern "C" tmk_status tmk_plastic_update(tmk_context* c, const tmk_fab* U, const
 // ---------------------------------------------------------------- level API
 namespace {
 
-struct LevelPatch {
-  tmk_box valid, alloc;
-  int fault = 0;
-  void* U[2] = {nullptr, nullptr};
-  double* B = nullptr;
-  int blo = 0, bnx = 0;
-  double* first = nullptr;
-  double* ffault = nullptr;
-};
-
-}  // namespace
-
-struct tmk_level_s {
-  tmk_context* ctx = nullptr;
-  tmk_box domain;
-  double dx = 0;
-  int prec = TMK_PREC_FP64;
-  std::vector<LevelPatch> patches;
-  void* dpatch[2] = {nullptr, nullptr};   // PatchDev arrays, parity 0 (U0->U1) and 1 (U1->U0)
-  std::vector<char> hpatch[2];
-  TileDev* dtiles = nullptr;
-  int ntiles = 0;
-  int march = 0;                           // column-marching volume kernel
-  tmk::MarchItem* ditems = nullptr;
-  int nitems = 0;
-  int* dfault = nullptr;
-  int nfault = 0, max_faces = 0;
-  CopyDev* dcopies = nullptr;
-  int ncopies = 0;
-  CopyDev* dbcopies = nullptr;
-  int nbcopies = 0;
-  double** dbptr = nullptr;
-  int* dblo = nullptr;
-  int* dbnx = nullptr;
-  double* stage = nullptr;                 // FP64 staging for set/get of the mixed form
-  size_t stage_count = 0;
-  int parity = 0;
-  double cur_dt = -1.0;
-  std::vector<void*> allocs;
-  // per-launch timing (tmk_level_profile)
-  std::vector<cudaEvent_t> ev;            // 4 events per recorded step
-  int prof_on = 0, prof_max = 0, prof_n = 0;
-};
-
-namespace {
-
 template <typename Real>
 void fill_patchdev(tmk_level_s* L, int parity) {
   L->hpatch[parity].assign(L->patches.size() * sizeof(PatchDev<Real>), 0);
@@ -366,25 +288,29 @@ void fill_patchdev(tmk_level_s* L, int parity) {
     d.first = lp.first; d.ffault = lp.ffault;
     d.nfirst = lp.valid.hi[0] - lp.valid.lo[0] + 3;
     d.Fx = nullptr; d.Fy = nullptr;
+    d.Bold = lp.Bold;
+    d.cap = L->cap;
+    d.caplist = L->dcaplist;
   }
 }
 
-size_t real_size(int prec) { return prec == TMK_PREC_MIXED ? sizeof(float) : sizeof(double); }
+}  // namespace
 
-tmk_status upload_patchdev(tmk_level_s* L, cudaStream_t s) {
+tmk_status tmk_host::upload_patchdev(tmk_level_s* L, cudaStream_t s) {
   for (int par = 0; par < 2; ++par) {
     if (L->prec == TMK_PREC_MIXED) fill_patchdev<float>(L, par); else fill_patchdev<double>(L, par);
+    // a copy from pageable memory returns once the source has been staged
     TMK_CU(cudaMemcpyAsync(L->dpatch[par], L->hpatch[par].data(), L->hpatch[par].size(), cudaMemcpyHostToDevice, s));
   }
   return TMK_OK;
 }
 
-}  // namespace
-
 extern "C" void tmk_level_destroy(tmk_level* L) {
   if (!L) return;
   cudaDeviceSynchronize();
+  amr_release(L);
   for (void* p : L->allocs) cudaFree(p);
+  for (void* p : L->cap_allocs) cudaFree(p);
   for (cudaEvent_t e : L->ev) cudaEventDestroy(e);
   delete L;
 }
@@ -479,7 +405,9 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
   }
   if (dalloc(&L->dtiles, tiles.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
   L->allocs.push_back(L->dtiles);
-  L->march = uses_march(c->scheme) ? 1 : 0;
+  L->htiles = tiles;
+  L->march_allowed = uses_march(c->scheme) ? 1 : 0;
+  L->march = L->march_allowed;
   if (L->march) {
     std::vector<tmk::MarchItem> items;
     const int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots()
@@ -571,6 +499,13 @@ extern "C" tmk_status tmk_level_get_patch(tmk_level* L, int p, double* U, double
 }
 
 extern "C" tmk_status tmk_level_step(tmk_level* L, double time, double dt, void* stream, double* dt_new) {
+  if (!L) return TMK_ERR_BAD_DESC;
+  if (L->coarser) return TMK_ERR_BAD_DESC;   // a level with a coarser level needs the coarse times
+  return tmk_level_step_cf(L, time, dt, 0.0, 0.0, stream, dt_new);
+}
+
+extern "C" tmk_status tmk_level_step_cf(tmk_level* L, double time, double dt, double t_coarse_old,
+                                        double t_coarse_new, void* stream, double* dt_new) {
   if (!L || !(dt > 0)) return TMK_ERR_BAD_DESC;
   cudaStream_t s = (cudaStream_t)stream;
   tmk_context* c = L->ctx;
@@ -582,6 +517,11 @@ extern "C" tmk_status tmk_level_step(tmk_level* L, double time, double dt, void*
   cudaEvent_t* ev = nullptr;
   if (L->prof_on && L->prof_n < L->prof_max) ev = &L->ev[4 * (size_t)L->prof_n++];
   if (ev) TMK_CU(cudaEventRecord(ev[0], s));
+  // fault data at the start of the step (for a finer level's time interpolation)
+  // and the coarse-fine ghost fill; the fill writes only ghosts that no patch
+  // of this level covers, so it is independent of the same-level exchange
+  tmk_status st = amr_pre_step(L, time, dt, t_coarse_old, t_coarse_new, s);
+  if (st != TMK_OK) return st;
   if (L->prec == TMK_PREC_MIXED) {
     const PatchDev<float>* pd = (const PatchDev<float>*)L->dpatch[par];
     TMK_CU(tmk::Launch<float>::exchange(pd, L->dcopies, L->ncopies, 0, TMK_NCOMP, s));
@@ -601,6 +541,9 @@ extern "C" tmk_status tmk_level_step(tmk_level* L, double time, double dt, void*
     if (L->march) TMK_CU(tmk::Launch<double>::march(pd, L->ditems, L->nitems, c->dp, s));
     else TMK_CU(tmk::Launch<double>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
   }
+  // flux-register increments from the captured faces
+  st = amr_post_step(L, dt, s);
+  if (st != TMK_OK) return st;
   if (ev) TMK_CU(cudaEventRecord(ev[3], s));
   L->parity = 1 - par;
   if (dt_new) *dt_new = L->dx / std::max(c->hp.cs, c->hp.cp);
@@ -642,7 +585,7 @@ extern "C" tmk_status tmk_level_profile_read(tmk_level* L, double out[4], int* n
 extern "C" int tmk_level_launches_per_step(const tmk_level* L) {
   if (!L) return 0;
   const int vol = L->march ? (L->nitems ? 2 : 0) : (L->ntiles ? 1 : 0);
-  return (L->ncopies ? 1 : 0) + (L->nbcopies ? 1 : 0) + (L->nfault ? 1 : 0) + vol;
+  return (L->ncopies ? 1 : 0) + (L->nbcopies ? 1 : 0) + (L->nfault ? 1 : 0) + vol + amr_launches(L);
 }
 
 extern "C" tmk_status tmk_level_status(tmk_level* L, long long info[3]) {

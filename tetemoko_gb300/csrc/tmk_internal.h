@@ -1,0 +1,115 @@
+// tmk_internal.h -- host-side objects shared by the translation units that
+// implement the C ABI (tmk_capi.cu: contexts, patches, levels; tmk_amr.cu:
+// coarse-fine coupling and the AMR hierarchy).
+#pragma once
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <vector>
+
+#include "../../include/tetemoko_gb300.h"
+#include "tmk_kernels.cuh"
+#include "tmk_march.cuh"
+#include "tmk_launch.h"
+
+#define TMK_CU(call)                                   \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return TMK_ERR_CUDA;        \
+  } while (0)
+
+namespace tmk_host {
+
+inline bool box_ok(const tmk_box& b) { return b.lo[0] <= b.hi[0] && b.lo[1] <= b.hi[1]; }
+inline bool box_contains(const tmk_box& a, const tmk_box& b) {
+  return a.lo[0] <= b.lo[0] && a.lo[1] <= b.lo[1] && a.hi[0] >= b.hi[0] && a.hi[1] >= b.hi[1];
+}
+inline bool box_has(const tmk_box& a, int i, int j) {
+  return i >= a.lo[0] && i <= a.hi[0] && j >= a.lo[1] && j <= a.hi[1];
+}
+inline tmk_box box_grow(tmk_box b, int n) { b.lo[0] -= n; b.lo[1] -= n; b.hi[0] += n; b.hi[1] += n; return b; }
+inline tmk_box box_isect(tmk_box a, const tmk_box& b) {
+  for (int d = 0; d < 2; ++d) { a.lo[d] = std::max(a.lo[d], b.lo[d]); a.hi[d] = std::min(a.hi[d], b.hi[d]); }
+  return a;
+}
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) { return cudaMalloc((void**)p, n * sizeof(T) + 16); }
+
+inline size_t real_size(int prec) { return prec == TMK_PREC_MIXED ? sizeof(float) : sizeof(double); }
+
+struct LevelPatch {
+  tmk_box valid, alloc;
+  int fault = 0;
+  void* U[2] = {nullptr, nullptr};
+  double* B = nullptr;
+  double* Bold = nullptr;   // fault data at the start of the step (levels with a finer level)
+  int blo = 0, bnx = 0;
+  double* first = nullptr;
+  double* ffault = nullptr;
+};
+
+struct CFLink;   // coarse-fine coupling of a level with its coarser level (tmk_amr.cu)
+
+}  // namespace tmk_host
+
+struct tmk_context_s {
+  tmk::DevParams hp;
+  tmk::DevParams* dp = nullptr;
+  tmk_scheme scheme;
+  int nb = 0;
+  // patch-level scratch (grown on demand)
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  tmk::DevStatus* dstatus = nullptr;
+};
+
+struct tmk_level_s {
+  tmk_context* ctx = nullptr;
+  tmk_box domain;
+  double dx = 0;
+  int prec = TMK_PREC_FP64;
+  std::vector<tmk_host::LevelPatch> patches;
+  void* dpatch[2] = {nullptr, nullptr};   // PatchDev arrays, parity 0 (U0->U1) and 1 (U1->U0)
+  std::vector<char> hpatch[2];
+  std::vector<tmk::TileDev> htiles;        // tile list (host copy; capture ranges rewritten by the AMR links)
+  tmk::TileDev* dtiles = nullptr;
+  int ntiles = 0;
+  int march = 0;                           // column-marching volume kernel
+  int march_allowed = 0;                   // the scheme selects it (captures force the tile kernel)
+  tmk::MarchItem* ditems = nullptr;
+  int nitems = 0;
+  int* dfault = nullptr;
+  int nfault = 0, max_faces = 0;
+  tmk::CopyDev* dcopies = nullptr;
+  int ncopies = 0;
+  tmk::CopyDev* dbcopies = nullptr;
+  int nbcopies = 0;
+  double** dbptr = nullptr;
+  int* dblo = nullptr;
+  int* dbnx = nullptr;
+  double* stage = nullptr;                 // FP64 staging for set/get of the mixed form
+  size_t stage_count = 0;
+  int parity = 0;
+  double cur_dt = -1.0;
+  std::vector<void*> allocs;
+  // per-launch timing (tmk_level_profile)
+  std::vector<cudaEvent_t> ev;            // 4 events per recorded step
+  int prof_on = 0, prof_max = 0, prof_n = 0;
+  // coarse-fine coupling
+  tmk_host::CFLink* coarser = nullptr;    // owned: coupling with the next coarser level
+  tmk_host::CFLink* finer = nullptr;      // the next finer level's coupling (owned by that level)
+  double* cap = nullptr;                  // captured face fluxes, 22 doubles per slot
+  int ncap = 0;
+  int4* dcaplist = nullptr;               // (dir, i, j, slot) per captured face, grouped by tile
+  std::vector<void*> cap_allocs;
+};
+
+namespace tmk_host {
+// tmk_capi.cu
+tmk_status upload_patchdev(tmk_level_s* L, cudaStream_t s);
+// tmk_amr.cu: the coarse-fine parts of a level step
+tmk_status amr_pre_step(tmk_level_s* L, double time, double dt, double tco, double tcn, cudaStream_t s);
+tmk_status amr_post_step(tmk_level_s* L, double dt, cudaStream_t s);
+int amr_launches(const tmk_level_s* L);
+void amr_release(tmk_level_s* L);
+}  // namespace tmk_host

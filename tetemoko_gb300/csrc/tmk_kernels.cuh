@@ -39,9 +39,13 @@ struct PatchDev {
   int nfirst;
   Real* Fx;                 // optional reflux fluxes (22 comps over x faces of valid)
   Real* Fy;
+  double* Bold;             // fault data at the start of the step (coarse-fine time interpolation)
+  double* cap;              // captured face fluxes of the level (flux registers), 22 per slot
+  const int4* caplist;      // (dir, i, j, slot) of the captured faces, grouped by tile
 };
 
-struct TileDev { int patch, x0, y0, nx, ny; };
+// A tile of the volume kernel; [cap0, cap0+ncap) are the captured faces it owns.
+struct TileDev { int patch, x0, y0, nx, ny, cap0 = 0, ncap = 0; };
 
 template <typename Real>
 TMK_D size_t fab_idx(const PatchDev<Real>& p, int c, int i, int j) {
@@ -457,6 +461,13 @@ __global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __rest
       size_t o = ((size_t)(11 * s + c) * nvy + (y0 + gi - p.vlo1)) * nvx + (x0 + cx - p.vlo0);
       p.Fy[o] = sm.Fy[c][gi][cx];
     }
+  }
+  // flux-register faces owned by this tile (LevelFluxRegister increments)
+  for (int q = threadIdx.x; q < tl.ncap * NSIDE; q += NT) {
+    const int4 cr = p.caplist[tl.cap0 + q / NSIDE];
+    const int c = q % NSIDE;
+    const T v = cr.x == 0 ? sm.Fx[c][cr.z - y0][cr.y - x0] : sm.Fy[c][cr.z - y0][cr.y - x0];
+    p.cap[(size_t)cr.w * 22 + 11 * s + c] = (double)v;
   }
 }
 

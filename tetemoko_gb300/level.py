@@ -204,10 +204,62 @@ class LinElastLevelGodunov:
             if B is not None and Bg is not None:
                 Bg[:, xs] = B[:, g:-g]
 
-    def step(self, time: float, dt: float, stream=None) -> float:
+    def step(self, time: float, dt: float, stream=None, t_coarse_old: float | None = None,
+             t_coarse_new: float | None = None) -> float:
+        """LinElastLevelGodunov::step; a level with a coarser level also needs the
+        coarse level's old and new times (the coarse-fine time interpolation)."""
         dtn = C.c_double(0.0)
-        A.check(self.lib.tmk_level_step(self.h, time, dt, _stream_ptr(stream), C.byref(dtn)), "tmk_level_step")
+        if t_coarse_old is None:
+            A.check(self.lib.tmk_level_step(self.h, time, dt, _stream_ptr(stream), C.byref(dtn)), "tmk_level_step")
+        else:
+            A.check(self.lib.tmk_level_step_cf(self.h, time, dt, t_coarse_old, t_coarse_new, _stream_ptr(stream),
+                                               C.byref(dtn)), "tmk_level_step_cf")
         return dtn.value
+
+    # -------------------------------------------------- coarse-fine coupling
+    def attach_coarser(self, coarse: "LinElastLevelGodunov", ref_ratio: int):
+        A.check(self.lib.tmk_level_attach_coarser(self.h, coarse.h, ref_ratio), "tmk_level_attach_coarser")
+
+    def detach_coarser(self):
+        A.check(self.lib.tmk_level_detach_coarser(self.h), "tmk_level_detach_coarser")
+
+    def fill_coarse_fine(self, alpha: float, stream=None):
+        """PiecewiseLinearFillPatch / D1PiecewiseLinearFillPatch::fillInterp."""
+        A.check(self.lib.tmk_level_fill_coarse_fine(self.h, alpha, _stream_ptr(stream)), "tmk_level_fill_coarse_fine")
+
+    def reflux(self, stream=None):
+        """LevelFluxRegister::reflux with the finer level's fluxes."""
+        A.check(self.lib.tmk_level_reflux(self.h, _stream_ptr(stream)), "tmk_level_reflux")
+
+    def average_down(self, stream=None):
+        """CoarseAverage / D1CoarseAverage::averageToCoarse from the finer level."""
+        A.check(self.lib.tmk_level_average_down(self.h, _stream_ptr(stream)), "tmk_level_average_down")
+
+    def interp_from_coarser(self, stream=None):
+        """FineInterp / D1FineInterp::interpToFine (regrid initialisation)."""
+        A.check(self.lib.tmk_level_interp_from_coarser(self.h, _stream_ptr(stream)), "tmk_level_interp_from_coarser")
+
+    def copy_overlap(self, src: "LinElastLevelGodunov", stream=None):
+        """Copy the valid cells that this level's patches share with `src`'s."""
+        A.check(self.lib.tmk_level_copy_overlap(self.h, src.h, _stream_ptr(stream)), "tmk_level_copy_overlap")
+
+    def register_size(self) -> int:
+        n = C.c_int(0)
+        A.check(self.lib.tmk_level_register_size(self.h, C.byref(n)), "tmk_level_register_size")
+        return n.value
+
+    def set_patches(self, Us, Bs):
+        """Per-patch state: Us[p] (22, ny+8, nx+8), Bs[p] fault row or None."""
+        for p, U in enumerate(Us):
+            self.set_patch(p, U, Bs[p])
+
+    def get_patches(self):
+        Us, Bs = [], []
+        for p in range(len(self.boxes)):
+            U, B = self.get_patch(p)
+            Us.append(U)
+            Bs.append(B)
+        return Us, Bs
 
     def status(self):
         info = (C.c_longlong * 3)()
