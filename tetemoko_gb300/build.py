@@ -20,6 +20,7 @@ OUT = os.path.join(HERE, "libtetemoko_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+          "-Xcompiler", "-ffp-contract=off",   # host-computed launch constants: no FMA contraction
           "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
 UNITS = {
     "tmk_fp64.cu": ["--fmad=false"],

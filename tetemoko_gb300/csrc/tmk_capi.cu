@@ -529,7 +529,7 @@ extern "C" tmk_status tmk_level_step_cf(tmk_level* L, double time, double dt, do
     if (ev) TMK_CU(cudaEventRecord(ev[1], s));
     TMK_CU(tmk::Launch<float>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, s));
     if (ev) TMK_CU(cudaEventRecord(ev[2], s));
-    if (L->march) TMK_CU(tmk::Launch<float>::march(pd, L->ditems, L->nitems, c->dp, s));
+    if (L->march) TMK_CU(tmk::Launch<float>::march(pd, L->ditems, L->nitems, c->hp, dt, L->dx, s));
     else TMK_CU(tmk::Launch<float>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
   } else {
     const PatchDev<double>* pd = (const PatchDev<double>*)L->dpatch[par];
@@ -538,7 +538,7 @@ extern "C" tmk_status tmk_level_step_cf(tmk_level* L, double time, double dt, do
     if (ev) TMK_CU(cudaEventRecord(ev[1], s));
     TMK_CU(tmk::Launch<double>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, s));
     if (ev) TMK_CU(cudaEventRecord(ev[2], s));
-    if (L->march) TMK_CU(tmk::Launch<double>::march(pd, L->ditems, L->nitems, c->dp, s));
+    if (L->march) TMK_CU(tmk::Launch<double>::march(pd, L->ditems, L->nitems, c->hp, dt, L->dx, s));
     else TMK_CU(tmk::Launch<double>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
   }
   // flux-register increments from the captured faces

@@ -25,9 +25,10 @@ struct Launch {
   static cudaError_t exchange(const PatchDev<Real>* patches, const CopyDev* copies, int ncopies, int c0,
                               int ncomp, cudaStream_t s);
   static size_t volume_smem();
-  // column-marching volume update: one warp per item, both component groups
+  // column-marching volume update: one warp per item, both component groups;
+  // hp is the host copy of the scenario, dt/dx those of every patch
   static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* items, int nitems,
-                           const DevParams* params, cudaStream_t s);
+                           const DevParams& hp, double dt, double dx, cudaStream_t s);
   // warps of the marching kernel that are resident at once on the current device
   static int march_slots();
 };

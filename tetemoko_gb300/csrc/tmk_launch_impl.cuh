@@ -39,8 +39,10 @@ struct LaunchImpl {
     return cudaGetLastError();
   }
   static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* items, int nitems,
-                           const DevParams* params, cudaStream_t s) {
+                           const DevParams& hp, double dt, double dx, cudaStream_t s) {
     if (nitems <= 0) return cudaSuccess;
+    MarchConst<Real> mc;
+    mc.load(hp, dt, dx);
     const int blocks = (nitems + MARCH_WARPS - 1) / MARCH_WARPS;
     static bool configured = false;
     if (!configured) {
@@ -64,10 +66,10 @@ struct LaunchImpl {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cfg.dynamicSmemBytes = march_smem_bytes<Real, 0>();
-    cudaError_t e = cudaLaunchKernelEx(&cfg, march_kernel<Real, 0>, patches, items, nitems, params);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, march_kernel<Real, 0>, patches, items, nitems, mc);
     if (e != cudaSuccess) return e;
     cfg.dynamicSmemBytes = march_smem_bytes<Real, 1>();
-    return cudaLaunchKernelEx(&cfg, march_kernel<Real, 1>, patches, items, nitems, params);
+    return cudaLaunchKernelEx(&cfg, march_kernel<Real, 1>, patches, items, nitems, mc);
   }
   static int march_slots() {
     int dev = 0, sms = 0, b0 = 0, b1 = 0;
@@ -107,8 +109,8 @@ struct LaunchImpl {
   }                                                                                                          \
   template <> size_t Launch<REAL>::volume_smem() { return LaunchImpl<REAL, TXV, TYV, NTV>::smem(); }         \
   template <> cudaError_t Launch<REAL>::march(const PatchDev<REAL>* p, const MarchItem* it, int n,           \
-                                              const DevParams* prm, cudaStream_t s) {                       \
-    return LaunchImpl<REAL, TXV, TYV, NTV>::march(p, it, n, prm, s);                                         \
+                                              const DevParams& hp, double dt, double dx, cudaStream_t s) {  \
+    return LaunchImpl<REAL, TXV, TYV, NTV>::march(p, it, n, hp, dt, dx, s);                                  \
   }                                                                                                          \
   template <> int Launch<REAL>::march_slots() { return LaunchImpl<REAL, TXV, TYV, NTV>::march_slots(); }     \
   }

@@ -31,8 +31,8 @@ template <typename T> struct PairOf;
 template <> struct PairOf<float> { using P = float2; };
 template <> struct PairOf<double> { using P = double2; };
 
-TMK_D float2 mk2(float a, float b) { return make_float2(a, b); }
-TMK_D double2 mk2(double a, double b) { return make_double2(a, b); }
+TMK_HD float2 mk2(float a, float b) { return make_float2(a, b); }
+TMK_HD double2 mk2(double a, double b) { return make_double2(a, b); }
 TMK_D float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 TMK_D float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
 TMK_D float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
@@ -92,7 +92,7 @@ struct MK {
   P aP, bP, aS, bS;    // PPM tracing coefficients of the P and S speeds
   P f_irho, f_l2g, f_lam, f_G;   // GETFLUXF: -rv * {1/rho, lam+2G, lam, G}
   P a_irho, a_l2g, a_lam, a_G;   // GETADWDXF: -rv*scale * {...}
-  TMK_D void load(const DevParams& p, int D, double dtdx, double scale) {
+  TMK_HD void load(const DevParams& p, int D, double dtdx, double scale) {
     const T s2 = (D == 1) ? T(-1) : T(1);       // rv of side 2
     ZpE = mk2((T)p.Zp, (T)(s2 * p.Zp)); ZsE = mk2((T)p.Zs, (T)(s2 * p.Zs));
     nZpE = mk2((T)-p.Zp, (T)(-s2 * p.Zp)); nZsE = mk2((T)-p.Zs, (T)(-s2 * p.Zs));
@@ -114,6 +114,30 @@ struct MK {
     a_l2g = mk2((T)(m1 * scale * (p.lam + 2.0 * p.G)), (T)(m2 * scale * (p.lam + 2.0 * p.G)));
     a_lam = mk2((T)(m1 * scale * p.lam), (T)(m2 * scale * p.lam));
     a_G = mk2((T)(m1 * scale * p.G), (T)(m2 * scale * p.G));
+  }
+};
+
+// Everything the marching kernel needs that is uniform over a launch (all
+// patches of a level share the scenario, dt and dx).  Built on the host and
+// passed by value as a __grid_constant__ parameter, so the kernel reads the
+// constants from the parameter bank instead of holding ~90 of them in
+// registers through the row loop.
+template <typename T>
+struct MarchConst {
+  using P = typename PairOf<T>::P;
+  MK<T> kx, ky;
+  P bg[9];           // background of the evolving components (.x side 1, .y side 2)
+  P sc;              // -dt/dx
+  int plim, clim, lim, ppm;
+  int xout_lo, xout_hi, yout_lo, yout_hi;
+  TMK_HD void load(const DevParams& p, double dt, double dx) {
+    const double dtdx = dt / dx;
+    kx.load(p, 0, dtdx, -(1.0 / 2.0) * dt / dx);
+    ky.load(p, 1, dtdx, -(1.0 / 2.0) * dt / dx);
+    for (int c = 0; c < 9; ++c) bg[c] = mk2((T)p.bg[c], (T)p.bg[11 + c]);
+    sc = mk2((T)(-dt / dx), (T)(-dt / dx));
+    plim = p.prim_lim != 0; clim = p.char_lim != 0; lim = plim || clim; ppm = p.order != 0;
+    xout_lo = p.bc[0] == 0; xout_hi = p.bc[1] == 0; yout_lo = p.bc[2] == 0; yout_hi = p.bc[3] == 0;
   }
 };
 
@@ -246,11 +270,18 @@ TMK_D void riem(const MK<T>& k, const typename PairOf<T>::P* L, const typename P
   if constexpr (R::hasZf) g[R::zf] = pmul(k.half, padd(Rt[R::zf], L[R::zf]));
 }
 
+// Background state of a group, read from the launch constants by group index.
+template <int G, typename P>
+struct BgView {
+  const P* all;   // the 9 evolving components
+  TMK_D P operator[](int c) const { return all[Grp<G>::glob(c)]; }
+};
+
 // LINELASTOUTBCF / LINELASTFREEBCF for a group.  lo: the inside state is the
 // cell above/right of the face; SHF keeps the reference's velocity-minus-stress form.
 template <int G, int D, typename T>
 TMK_D void edge2(const MK<T>& k, bool lo, bool outflow, const typename PairOf<T>::P* Wi,
-                 const typename PairOf<T>::P* bg, typename PairOf<T>::P* g) {
+                 const BgView<G, typename PairOf<T>::P>& bg, typename PairOf<T>::P* g) {
   using P = typename PairOf<T>::P;
   using R = Role<G, D>;
   {
@@ -355,7 +386,7 @@ TMK_D void cp_async_wait_all_but_newest() { asm volatile("cp.async.wait_group 1;
 template <typename T, int G>
 __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) march_kernel(const PatchDev<T>* __restrict__ patches,
                                                                  const MarchItem* __restrict__ items, int nitems,
-                                                                 const DevParams* __restrict__ params) {
+                                                                 const __grid_constant__ MarchConst<T> mc) {
   using P = typename PairOf<T>::P;
   constexpr int N = Grp<G>::N;
   extern __shared__ __align__(16) unsigned char march_smem[];
@@ -373,23 +404,19 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
   }
   const MarchItem it = items[wid];
   const PatchDev<T>& pp = patches[it.patch];
-  const DevParams& Pm = params[pp.scen];
   const int x = it.x0 - 3 + lane;
   const int dlo0 = pp.dlo0, dhi0 = pp.dhi0, dlo1 = pp.dlo1, dhi1 = pp.dhi1;
   const int ahi0 = pp.alo0 + pp.anx - 1;
   const bool lane_in = x >= dlo0 && x <= dhi0 && x >= pp.alo0 && x <= ahi0;
   const bool inL = x - 1 >= dlo0, inR = x + 1 <= dhi0;
-  const bool plim = Pm.prim_lim != 0, clim = Pm.char_lim != 0, lim = plim || clim;
-  const bool ppm = Pm.order != 0;
-  const double dtdx = pp.dt / pp.dx;
-  MK<T> kx, ky;
-  kx.load(Pm, 0, dtdx, -(1.0 / 2.0) * pp.dt / pp.dx);
-  ky.load(Pm, 1, dtdx, -(1.0 / 2.0) * pp.dt / pp.dx);
-  const P sc = mk2((T)(-pp.dt / pp.dx), (T)(-pp.dt / pp.dx));
-  P bg[N];
-#pragma unroll
-  for (int c = 0; c < N; ++c) bg[c] = mk2((T)Pm.bg[Grp<G>::glob(c)], (T)Pm.bg[11 + Grp<G>::glob(c)]);
-  const bool xout_lo = Pm.bc[0] == 0, xout_hi = Pm.bc[1] == 0, yout_lo = Pm.bc[2] == 0, yout_hi = Pm.bc[3] == 0;
+  const bool plim = mc.plim != 0, clim = mc.clim != 0, lim = mc.lim != 0;
+  const bool ppm = mc.ppm != 0;
+  const MK<T>& kx = mc.kx;
+  const MK<T>& ky = mc.ky;
+  const P sc = mc.sc;
+  const BgView<G, P> bg{mc.bg};
+  const bool xout_lo = mc.xout_lo != 0, xout_hi = mc.xout_hi != 0, yout_lo = mc.yout_lo != 0,
+             yout_hi = mc.yout_hi != 0;
   const bool fault = pp.fault != 0;
   if (fault && it.y0 == dlo1) asm volatile("griddepcontrol.wait;" ::: "memory");
   const bool col_valid = x >= it.x0 && x < it.x0 + MARCH_COLS && x >= pp.vlo0 && x <= pp.vhi0;
