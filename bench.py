@@ -277,6 +277,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--fp64-kernel", default="march", choices=["march", "tile"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--nx", type=int, default=NX)
@@ -306,8 +307,9 @@ def main():
     cells = nx * ny
     stream = torch.cuda.current_stream()
 
-    def make_level(prec):
+    def make_level(prec, volume_kernel=A.TMK_VOLUME_AUTO):
         sc = S.rate_state(nx=nx, ny=ny, precision=prec)
+        sc.scheme.volume_kernel = volume_kernel
         ctx = Context(sc)
         lvl = LinElastLevelGodunov(ctx, [(0, 0, nx - 1, ny - 1)])
         lvl.set_patch(0, sc.initial_U(), sc.initial_B())
@@ -408,7 +410,8 @@ def main():
     ctx.close()
 
     # ---- plain FP64 form on the same workload
-    sc64, ctx64, lvl64 = make_level(A.TMK_PREC_FP64)
+    fp64_kernel = {"march": A.TMK_VOLUME_MARCH, "tile": A.TMK_VOLUME_TILE}[args.fp64_kernel]
+    sc64, ctx64, lvl64 = make_level(A.TMK_PREC_FP64, fp64_kernel)
     n64 = max(1, args.fp64_steps)
     ms64, prof64, _, st64 = timed(lvl64, sc64, n64, 3, profile=True)
     value64, secs64 = replica_rate(cells, n64, ms64 * 1e-3, world, device="cuda")
@@ -437,7 +440,7 @@ def main():
             "gpu_launches": launches,
             "clocks": clocks,
             "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_step": ms64 / n64, "steps": n64,
-                           "volume_kernel_ms": vol64,
+                           "volume_kernel": args.fp64_kernel, "volume_kernel_ms": vol64,
                            "volume_hbm_gbs": BYTES_PER_CELL_FP64 * cells / (vol64 * 1e-3) / 1e9},
             "mixed_over_fp64": value / value64,
             "device_status": {"mixed": st[1], "fp64": st64[1]},

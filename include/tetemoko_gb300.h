@@ -118,7 +118,9 @@ typedef struct {
 /* Implementations of the volume update (same results to rounding):
  * TILE  shared-memory tiles, one side of the fault per CTA (also fuses plasticity);
  * MARCH column-marching warps with both sides packed per lane (no plasticity);
- * AUTO  MARCH for the mixed form without plasticity, TILE otherwise. */
+ * AUTO  MARCH without plasticity, TILE with plasticity and on levels coupled
+ *       to a coarser or finer level (the tile kernel stores the coarse-fine
+ *       face fluxes). */
 enum { TMK_VOLUME_AUTO = 0, TMK_VOLUME_TILE = 1, TMK_VOLUME_MARCH = 2 };
 
 /* Chombo FArrayBox view: data[((c*(hi1-lo1+1)) + (j-lo1))*(hi0-lo0+1) + (i-lo0)] */

@@ -168,7 +168,7 @@ void make_march_items(std::vector<tmk::MarchItem>& out, const std::vector<tmk_bo
 bool uses_march(const tmk_scheme& s) {
   if (s.volume_kernel == TMK_VOLUME_MARCH) return true;
   if (s.volume_kernel == TMK_VOLUME_TILE) return false;
-  return s.precision == TMK_PREC_MIXED && !s.plasticity;
+  return !s.plasticity;
 }
 
 }  // namespace
