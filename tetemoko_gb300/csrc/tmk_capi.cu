@@ -137,33 +137,47 @@ void make_tiles(std::vector<TileDev>& out, int patch, const tmk_box& v, int TX, 
 
 size_t align_up(size_t n) { return (n + 255) & ~(size_t)255; }
 
-// Work items of the column-marching kernel: strips of MARCH_COLS columns by
-// runs of rows.  Each warp marches one item; the runs are sized so that all
-// items of a level fit in one wave of resident warps (`slots`): a strip of a
-// patch gets max(1, floor(slots * rows / total strip-rows)) runs of equal
-// length (at least kMinRun rows, which bounds the 2-row start-up overhead).
+// Work items of one component group's marching kernel: strips of MARCH_COLS
+// columns by runs of rows.  Each warp marches one item; the runs are sized so
+// that all items fit in one wave of resident warps (`slots`): a strip gets
+// max(1, floor(slots * rows / total strip-rows)) runs (at least kMinRun rows
+// each, which bounds the 2-row start-up overhead).  The first run of a strip
+// on the fault row waits for the fault kernel before it starts; it counts
+// `wait_rows` extra rows and is shortened by as many.
 constexpr int kMinRun = 16;
-void make_march_items(std::vector<tmk::MarchItem>& out, const std::vector<tmk_box>& boxes, int slots) {
+void make_march_items(std::vector<tmk::MarchItem>& out, const std::vector<tmk_box>& boxes,
+                      const std::vector<int>& fault, int slots, int wait_rows) {
   long long strip_rows = 0;
-  for (const tmk_box& v : boxes) {
+  for (size_t p = 0; p < boxes.size(); ++p) {
+    const tmk_box& v = boxes[p];
     const int ns = (v.hi[0] - v.lo[0] + tmk::MARCH_COLS) / tmk::MARCH_COLS;
-    strip_rows += (long long)ns * (v.hi[1] - v.lo[1] + 1);
+    strip_rows += (long long)ns * (v.hi[1] - v.lo[1] + 1 + (fault[p] ? wait_rows : 0));
   }
   if (slots <= 0) slots = 1;
   for (size_t p = 0; p < boxes.size(); ++p) {
     const tmk_box& v = boxes[p];
     const int rows = v.hi[1] - v.lo[1] + 1;
-    int k = (int)((long long)slots * rows / std::max(1LL, strip_rows));
-    k = std::max(1, std::min(k, (rows + kMinRun - 1) / kMinRun));
-    const int run = (rows + k - 1) / k;
-    for (int y0 = v.lo[1]; y0 <= v.hi[1]; y0 += run)
-      for (int x0 = v.lo[0]; x0 <= v.hi[0]; x0 += tmk::MARCH_COLS) {
+    const int w = fault[p] ? wait_rows : 0;
+    int k = (int)((long long)slots * (rows + w) / std::max(1LL, strip_rows));
+    k = std::max(1, std::min(k, (rows + w + kMinRun - 1) / kMinRun));
+    const int run = (rows + w + k - 1) / k;
+    const int first = std::min(rows, std::max(4, run - w));
+    for (int x0 = v.lo[0]; x0 <= v.hi[0]; x0 += tmk::MARCH_COLS)
+      for (int y0 = v.lo[1]; y0 <= v.hi[1];) {
+        const int len = (y0 == v.lo[1]) ? first : run;
         tmk::MarchItem m;
-        m.patch = (int)p; m.x0 = x0; m.y0 = y0; m.y1 = std::min(y0 + run - 1, v.hi[1]);
+        m.patch = (int)p; m.x0 = x0; m.y0 = y0; m.y1 = std::min(y0 + len - 1, v.hi[1]);
         out.push_back(m);
+        y0 = m.y1 + 1;
       }
   }
 }
+
+// Row-equivalents a fault-row item waits for the fault kernel, and the CTAs
+// of the marching kernel each fault-kernel CTA keeps from being resident (both
+// measured best at 0 for the in-plane kernel launched after the fault kernel).
+constexpr int kFaultWaitRows = 0;
+constexpr int kFaultDisplace = 0;
 
 bool uses_march(const tmk_scheme& s) {
   if (s.volume_kernel == TMK_VOLUME_MARCH) return true;
@@ -409,14 +423,29 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
   L->march_allowed = uses_march(c->scheme) ? 1 : 0;
   L->march = L->march_allowed;
   if (L->march) {
-    std::vector<tmk::MarchItem> items;
-    const int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots()
-                                                 : tmk::Launch<double>::march_slots();
-    make_march_items(items, std::vector<tmk_box>(boxes, boxes + npatch), slots);
-    L->nitems = (int)items.size();
-    if (dalloc(&L->ditems, items.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
-    L->allocs.push_back(L->ditems);
-    TMK_CU(cudaMemcpy(L->ditems, items.data(), items.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
+    // one work list per component group, each one wave of that kernel's
+    // resident warps; the in-plane kernel shares the SMs with the fault kernel
+    std::vector<int> fault_flags(npatch, 0);
+    int fault_ctas = 0;
+    for (int p = 0; p < npatch; ++p)
+      if (L->patches[p].fault) {
+        fault_flags[p] = 1;
+        fault_ctas += (boxes[p].hi[0] - boxes[p].lo[0] + tmk::FAULT_SEG) / tmk::FAULT_SEG;
+      }
+    const int warps = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_warps()
+                                                 : tmk::Launch<double>::march_warps();
+    for (int g = 0; g < 2; ++g) {
+      int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots(g)
+                                            : tmk::Launch<double>::march_slots(g);
+      if (g == 0) slots = std::max(warps, slots - kFaultDisplace * warps * fault_ctas);
+      std::vector<tmk::MarchItem> items;
+      make_march_items(items, std::vector<tmk_box>(boxes, boxes + npatch), fault_flags, slots,
+                       g == 0 && fault_ctas ? kFaultWaitRows : 0);
+      L->nitems[g] = (int)items.size();
+      if (dalloc(&L->ditems[g], items.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+      L->allocs.push_back(L->ditems[g]);
+      TMK_CU(cudaMemcpy(L->ditems[g], items.data(), items.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
+    }
   }
   TMK_CU(cudaMemcpy(L->dtiles, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice));
   if (L->nfault) {
@@ -584,7 +613,7 @@ extern "C" tmk_status tmk_level_profile_read(tmk_level* L, double out[4], int* n
 
 extern "C" int tmk_level_launches_per_step(const tmk_level* L) {
   if (!L) return 0;
-  const int vol = L->march ? (L->nitems ? 2 : 0) : (L->ntiles ? 1 : 0);
+  const int vol = L->march ? (L->nitems[0] ? 1 : 0) + (L->nitems[1] ? 1 : 0) : (L->ntiles ? 1 : 0);
   return (L->ncopies ? 1 : 0) + (L->nbcopies ? 1 : 0) + (L->nfault ? 1 : 0) + vol + amr_launches(L);
 }
 

@@ -76,8 +76,8 @@ struct tmk_level_s {
   int ntiles = 0;
   int march = 0;                           // column-marching volume kernel
   int march_allowed = 0;                   // the scheme selects it (captures force the tile kernel)
-  tmk::MarchItem* ditems = nullptr;
-  int nitems = 0;
+  tmk::MarchItem* ditems[2] = {nullptr, nullptr};   // work lists of the in-plane / antiplane kernels
+  int nitems[2] = {0, 0};
   int* dfault = nullptr;
   int nfault = 0, max_faces = 0;
   tmk::CopyDev* dcopies = nullptr;

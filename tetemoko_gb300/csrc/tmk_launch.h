@@ -25,12 +25,15 @@ struct Launch {
   static cudaError_t exchange(const PatchDev<Real>* patches, const CopyDev* copies, int ncopies, int c0,
                               int ncomp, cudaStream_t s);
   static size_t volume_smem();
-  // column-marching volume update: one warp per item, both component groups;
-  // hp is the host copy of the scenario, dt/dx those of every patch
-  static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* items, int nitems,
+  // column-marching volume update: one warp per item of each component group's
+  // list (items[0]: in-plane, items[1]: antiplane); hp is the host copy of the
+  // scenario, dt/dx those of every patch
+  static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* const items[2], const int nitems[2],
                            const DevParams& hp, double dt, double dx, cudaStream_t s);
-  // warps of the marching kernel that are resident at once on the current device
-  static int march_slots();
+  // warps of group g's marching kernel resident at once on the current device
+  static int march_slots(int g);
+  // warps per CTA of the marching kernels
+  static int march_warps();
 };
 
 // FP64 <-> Real conversion of a FAB on the device

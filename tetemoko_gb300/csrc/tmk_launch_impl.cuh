@@ -38,12 +38,11 @@ struct LaunchImpl {
     exchange_kernel<Real><<<ncopies, 256, 0, s>>>(patches, copies, c0, ncomp, 0);
     return cudaGetLastError();
   }
-  static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* items, int nitems,
+  static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* const items[2], const int nitems[2],
                            const DevParams& hp, double dt, double dx, cudaStream_t s) {
-    if (nitems <= 0) return cudaSuccess;
+    if (nitems[0] <= 0 && nitems[1] <= 0) return cudaSuccess;
     MarchConst<Real> mc;
     mc.load(hp, dt, dx);
-    const int blocks = (nitems + MARCH_WARPS - 1) / MARCH_WARPS;
     static bool configured = false;
     if (!configured) {
       cudaError_t e0 = cudaFuncSetAttribute(march_kernel<Real, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -60,32 +59,42 @@ struct LaunchImpl {
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(blocks);
     cfg.blockDim = dim3(32 * MARCH_WARPS);
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cfg.dynamicSmemBytes = march_smem_bytes<Real, 0>();
-    cudaError_t e = cudaLaunchKernelEx(&cfg, march_kernel<Real, 0>, patches, items, nitems, mc);
-    if (e != cudaSuccess) return e;
-    cfg.dynamicSmemBytes = march_smem_bytes<Real, 1>();
-    return cudaLaunchKernelEx(&cfg, march_kernel<Real, 1>, patches, items, nitems, mc);
+    if (nitems[0] > 0) {
+      cfg.gridDim = dim3((nitems[0] + MARCH_WARPS - 1) / MARCH_WARPS);
+      cfg.dynamicSmemBytes = march_smem_bytes<Real, 0>();
+      cudaError_t e = cudaLaunchKernelEx(&cfg, march_kernel<Real, 0>, patches, items[0], nitems[0], mc);
+      if (e != cudaSuccess) return e;
+    }
+    if (nitems[1] > 0) {
+      cfg.gridDim = dim3((nitems[1] + MARCH_WARPS - 1) / MARCH_WARPS);
+      cfg.dynamicSmemBytes = march_smem_bytes<Real, 1>();
+      return cudaLaunchKernelEx(&cfg, march_kernel<Real, 1>, patches, items[1], nitems[1], mc);
+    }
+    return cudaSuccess;
   }
-  static int march_slots() {
-    int dev = 0, sms = 0, b0 = 0, b1 = 0;
+  static int march_slots(int g) {
+    int dev = 0, sms = 0, b = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       return 0;
-    cudaFuncSetAttribute(march_kernel<Real, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)march_smem_bytes<Real, 0>());
-    cudaFuncSetAttribute(march_kernel<Real, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)march_smem_bytes<Real, 1>());
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, march_kernel<Real, 0>, 32 * MARCH_WARPS,
-                                                      march_smem_bytes<Real, 0>()) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, march_kernel<Real, 1>, 32 * MARCH_WARPS,
-                                                      march_smem_bytes<Real, 1>()) != cudaSuccess)
-      return 0;
-    return std::min(b0, b1) * sms * MARCH_WARPS;
+    cudaError_t e;
+    if (g == 0) {
+      cudaFuncSetAttribute(march_kernel<Real, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)march_smem_bytes<Real, 0>());
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, march_kernel<Real, 0>, 32 * MARCH_WARPS,
+                                                        march_smem_bytes<Real, 0>());
+    } else {
+      cudaFuncSetAttribute(march_kernel<Real, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)march_smem_bytes<Real, 1>());
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, march_kernel<Real, 1>, 32 * MARCH_WARPS,
+                                                        march_smem_bytes<Real, 1>());
+    }
+    if (e != cudaSuccess) return 0;
+    return b * sms * MARCH_WARPS;
   }
 };
 
@@ -108,9 +117,11 @@ struct LaunchImpl {
     return LaunchImpl<REAL, TXV, TYV, NTV>::exchange(p, c, n, c0, nc, s);                                    \
   }                                                                                                          \
   template <> size_t Launch<REAL>::volume_smem() { return LaunchImpl<REAL, TXV, TYV, NTV>::smem(); }         \
-  template <> cudaError_t Launch<REAL>::march(const PatchDev<REAL>* p, const MarchItem* it, int n,           \
-                                              const DevParams& hp, double dt, double dx, cudaStream_t s) {  \
+  template <> cudaError_t Launch<REAL>::march(const PatchDev<REAL>* p, const MarchItem* const it[2],        \
+                                              const int n[2], const DevParams& hp, double dt, double dx,   \
+                                              cudaStream_t s) {                                              \
     return LaunchImpl<REAL, TXV, TYV, NTV>::march(p, it, n, hp, dt, dx, s);                                  \
   }                                                                                                          \
-  template <> int Launch<REAL>::march_slots() { return LaunchImpl<REAL, TXV, TYV, NTV>::march_slots(); }     \
+  template <> int Launch<REAL>::march_slots(int g) { return LaunchImpl<REAL, TXV, TYV, NTV>::march_slots(g); } \
+  template <> int Launch<REAL>::march_warps() { return MARCH_WARPS; }                                        \
   }
