@@ -145,8 +145,8 @@ size_t align_up(size_t n) { return (n + 255) & ~(size_t)255; }
 // on the fault row waits for the fault kernel before it starts; it counts
 // `wait_rows` extra rows and is shortened by as many.
 constexpr int kMinRun = 16;
-void make_march_items(std::vector<tmk::MarchItem>& out, const std::vector<tmk_box>& boxes,
-                      const std::vector<int>& fault, int slots, int wait_rows) {
+void make_march_items(std::vector<tmk::MarchItem>& out, std::vector<tmk::MarchItem>& fault_rows,
+                      const std::vector<tmk_box>& boxes, const std::vector<int>& fault, int slots, int wait_rows) {
   long long strip_rows = 0;
   for (size_t p = 0; p < boxes.size(); ++p) {
     const tmk_box& v = boxes[p];
@@ -167,17 +167,23 @@ void make_march_items(std::vector<tmk::MarchItem>& out, const std::vector<tmk_bo
         const int len = (y0 == v.lo[1]) ? first : run;
         tmk::MarchItem m;
         m.patch = (int)p; m.x0 = x0; m.y0 = y0; m.y1 = std::min(y0 + len - 1, v.hi[1]);
+        m.fslot = -1;
+        if (fault[p] && y0 == v.lo[1]) {       // row 0 waits for the fault kernel: finished later
+          m.fslot = (int)fault_rows.size();
+          fault_rows.push_back(m);
+        }
         out.push_back(m);
         y0 = m.y1 + 1;
       }
   }
 }
 
-// Row-equivalents a fault-row item waits for the fault kernel, and the CTAs
-// of the marching kernel each fault-kernel CTA keeps from being resident (both
-// measured best at 0 for the in-plane kernel launched after the fault kernel).
+// Row-equivalents a fault-row item waits for the fault kernel (0: no marching
+// item waits, row 0 of the fault patches is finished after the fault kernel),
+// and the antiplane CTAs each fault-kernel CTA keeps from being resident (the
+// fault kernel runs beside the antiplane kernel; measured best at 1).
 constexpr int kFaultWaitRows = 0;
-constexpr int kFaultDisplace = 0;
+constexpr int kFaultDisplace = 1;
 
 bool uses_march(const tmk_scheme& s) {
   if (s.volume_kernel == TMK_VOLUME_MARCH) return true;
@@ -257,7 +263,7 @@ extern "C" tmk_status tmk_patch_update_state(tmk_context* c, const tmk_fab* U, c
   if (Fy) TMK_CU(cudaMemsetAsync(Fy->data, 0, (size_t)TMK_NCOMP * nvx * (nvy + 1) * sizeof(double), s));
   const PatchDev<double>* dpd = (const PatchDev<double>*)(base + off_pd);
   if (fault)
-    TMK_CU(tmk::Launch<double>::fault(dpd, (const int*)(base + off_fp), 1, nvx, c->dp, time, c->dstatus, s));
+    TMK_CU(tmk::Launch<double>::fault(dpd, (const int*)(base + off_fp), 1, nvx, c->dp, time, c->dstatus, false, s));
   TMK_CU(tmk::Launch<double>::volume(dpd, (const TileDev*)(base + off_tl), (int)tiles.size(), c->dp, s));
   // the volume kernel writes the nine evolving components of each side;
   // lambda and gamma are left untouched, as updateState leaves them
@@ -424,7 +430,7 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
   L->march = L->march_allowed;
   if (L->march) {
     // one work list per component group, each one wave of that kernel's
-    // resident warps; the in-plane kernel shares the SMs with the fault kernel
+    // resident warps; the antiplane kernel shares the SMs with the fault kernel
     std::vector<int> fault_flags(npatch, 0);
     int fault_ctas = 0;
     for (int p = 0; p < npatch; ++p)
@@ -437,14 +443,23 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
     for (int g = 0; g < 2; ++g) {
       int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots(g)
                                             : tmk::Launch<double>::march_slots(g);
-      if (g == 0) slots = std::max(warps, slots - kFaultDisplace * warps * fault_ctas);
-      std::vector<tmk::MarchItem> items;
-      make_march_items(items, std::vector<tmk_box>(boxes, boxes + npatch), fault_flags, slots,
+      if (g == 1) slots = std::max(warps, slots - kFaultDisplace * warps * fault_ctas);
+      std::vector<tmk::MarchItem> items, frows;
+      make_march_items(items, frows, std::vector<tmk_box>(boxes, boxes + npatch), fault_flags, slots,
                        g == 0 && fault_ctas ? kFaultWaitRows : 0);
       L->nitems[g] = (int)items.size();
       if (dalloc(&L->ditems[g], items.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
       L->allocs.push_back(L->ditems[g]);
       TMK_CU(cudaMemcpy(L->ditems[g], items.data(), items.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
+      L->nfrows[g] = (int)frows.size();
+      if (!frows.empty()) {
+        if (dalloc(&L->dfrows[g], frows.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+        L->allocs.push_back(L->dfrows[g]);
+        TMK_CU(cudaMemcpy(L->dfrows[g], frows.data(), frows.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
+        const size_t bytes = frows.size() * tmk::MARCH_STASH_VECS * (g == 0 ? 6 : 3) * 32 * 2 * rs;
+        if (cudaMalloc(&L->stash[g], bytes) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+        L->allocs.push_back(L->stash[g]);
+      }
     }
   }
   TMK_CU(cudaMemcpy(L->dtiles, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice));
@@ -527,6 +542,46 @@ extern "C" tmk_status tmk_level_get_patch(tmk_level* L, int p, double* U, double
   return TMK_OK;
 }
 
+namespace {
+
+// The kernels of one level step after the coarse-fine fill.  Marching form:
+// the in-plane kernel, then the fault kernel (scheduled as in-plane CTAs
+// retire, reading only the step's input state), then the antiplane kernel
+// beside it, then row 0 of the fault patches, which alone needs the fault
+// results.  With per-launch timing the fault kernel runs first and alone.
+template <typename Real>
+tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEvent_t* ev, cudaStream_t s) {
+  tmk_context* c = L->ctx;
+  const PatchDev<Real>* pd = (const PatchDev<Real>*)L->dpatch[par];
+  TMK_CU(tmk::Launch<Real>::exchange(pd, L->dcopies, L->ncopies, 0, TMK_NCOMP, s));
+  TMK_CU(tmk::bexchange(L->dbptr, L->dblo, L->dbnx, L->dbcopies, L->nbcopies, c->nb, s));
+  if (ev) TMK_CU(cudaEventRecord(ev[1], s));
+  if (!L->march) {
+    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, false, s));
+    if (ev) TMK_CU(cudaEventRecord(ev[2], s));
+    TMK_CU(tmk::Launch<Real>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
+    return TMK_OK;
+  }
+  tmk::MarchConst<Real> mc;
+  mc.load(c->hp, dt, L->dx);
+  mc.stash[0] = L->stash[0];
+  mc.stash[1] = L->stash[1];
+  if (ev) {
+    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, false, s));
+    TMK_CU(cudaEventRecord(ev[2], s));
+    TMK_CU(tmk::Launch<Real>::march(0, pd, L->ditems[0], L->nitems[0], mc, false, s));
+    TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, true, s));
+  } else {
+    TMK_CU(tmk::Launch<Real>::march(0, pd, L->ditems[0], L->nitems[0], mc, false, s));
+    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, true, s));
+    TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, true, s));
+  }
+  TMK_CU(tmk::Launch<Real>::march_fault_rows(pd, L->dfrows[0], L->nfrows[0], L->dfrows[1], L->nfrows[1], mc, s));
+  return TMK_OK;
+}
+
+}  // namespace
+
 extern "C" tmk_status tmk_level_step(tmk_level* L, double time, double dt, void* stream, double* dt_new) {
   if (!L) return TMK_ERR_BAD_DESC;
   if (L->coarser) return TMK_ERR_BAD_DESC;   // a level with a coarser level needs the coarse times
@@ -551,25 +606,9 @@ extern "C" tmk_status tmk_level_step_cf(tmk_level* L, double time, double dt, do
   // of this level covers, so it is independent of the same-level exchange
   tmk_status st = amr_pre_step(L, time, dt, t_coarse_old, t_coarse_new, s);
   if (st != TMK_OK) return st;
-  if (L->prec == TMK_PREC_MIXED) {
-    const PatchDev<float>* pd = (const PatchDev<float>*)L->dpatch[par];
-    TMK_CU(tmk::Launch<float>::exchange(pd, L->dcopies, L->ncopies, 0, TMK_NCOMP, s));
-    TMK_CU(tmk::bexchange(L->dbptr, L->dblo, L->dbnx, L->dbcopies, L->nbcopies, c->nb, s));
-    if (ev) TMK_CU(cudaEventRecord(ev[1], s));
-    TMK_CU(tmk::Launch<float>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, s));
-    if (ev) TMK_CU(cudaEventRecord(ev[2], s));
-    if (L->march) TMK_CU(tmk::Launch<float>::march(pd, L->ditems, L->nitems, c->hp, dt, L->dx, s));
-    else TMK_CU(tmk::Launch<float>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
-  } else {
-    const PatchDev<double>* pd = (const PatchDev<double>*)L->dpatch[par];
-    TMK_CU(tmk::Launch<double>::exchange(pd, L->dcopies, L->ncopies, 0, TMK_NCOMP, s));
-    TMK_CU(tmk::bexchange(L->dbptr, L->dblo, L->dbnx, L->dbcopies, L->nbcopies, c->nb, s));
-    if (ev) TMK_CU(cudaEventRecord(ev[1], s));
-    TMK_CU(tmk::Launch<double>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, s));
-    if (ev) TMK_CU(cudaEventRecord(ev[2], s));
-    if (L->march) TMK_CU(tmk::Launch<double>::march(pd, L->ditems, L->nitems, c->hp, dt, L->dx, s));
-    else TMK_CU(tmk::Launch<double>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
-  }
+  st = L->prec == TMK_PREC_MIXED ? step_kernels<float>(L, par, time, dt, ev, s)
+                                 : step_kernels<double>(L, par, time, dt, ev, s);
+  if (st != TMK_OK) return st;
   // flux-register increments from the captured faces
   st = amr_post_step(L, dt, s);
   if (st != TMK_OK) return st;
@@ -613,7 +652,8 @@ extern "C" tmk_status tmk_level_profile_read(tmk_level* L, double out[4], int* n
 
 extern "C" int tmk_level_launches_per_step(const tmk_level* L) {
   if (!L) return 0;
-  const int vol = L->march ? (L->nitems[0] ? 1 : 0) + (L->nitems[1] ? 1 : 0) : (L->ntiles ? 1 : 0);
+  const int vol = L->march ? (L->nitems[0] ? 1 : 0) + (L->nitems[1] ? 1 : 0) + (L->nfrows[0] + L->nfrows[1] ? 1 : 0)
+                           : (L->ntiles ? 1 : 0);
   return (L->ncopies ? 1 : 0) + (L->nbcopies ? 1 : 0) + (L->nfault ? 1 : 0) + vol + amr_launches(L);
 }
 

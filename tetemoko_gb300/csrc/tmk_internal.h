@@ -78,6 +78,9 @@ struct tmk_level_s {
   int march_allowed = 0;                   // the scheme selects it (captures force the tile kernel)
   tmk::MarchItem* ditems[2] = {nullptr, nullptr};   // work lists of the in-plane / antiplane kernels
   int nitems[2] = {0, 0};
+  tmk::MarchItem* dfrows[2] = {nullptr, nullptr};   // their fault-row items (row 0 finished after the fault kernel)
+  int nfrows[2] = {0, 0};
+  void* stash[2] = {nullptr, nullptr};              // row-0 intermediates of those items
   int* dfault = nullptr;
   int nfault = 0, max_faces = 0;
   tmk::CopyDev* dcopies = nullptr;

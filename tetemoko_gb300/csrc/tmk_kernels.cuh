@@ -134,13 +134,19 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
   __shared__ T H1x[2][FAULT_SEG + 1][NSIDE];
   __shared__ double sWi[NCELL][NC];
   __shared__ double sTmp[NCELL];
-  // the volume update launched after this kernel may start now: its interior
-  // work does not read the fault buffers (it waits before it does)
+  // the kernel launched after this one may be scheduled now (it reads none of
+  // this kernel's outputs before it waits for it).  When this kernel itself is
+  // a programmatic dependent of the in-plane marching kernel, it reads nothing
+  // that kernel writes (the state it reads is the step's input buffer) and it
+  // waits for it before exiting, so that the step's kernels complete in order.
   asm volatile("griddepcontrol.launch_dependents;");
   const PatchDev<Real> p = patches[fault_patches[blockIdx.y]];
   const DevParams& P = params[p.scen];
   const int s0 = p.vlo0 + blockIdx.x * FAULT_SEG;
-  if (s0 > p.vhi0) return;
+  if (s0 > p.vhi0) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    return;
+  }
   const int s1 = min(s0 + FAULT_SEG - 1, p.vhi0);
   // faces whose first-pass state this segment produces: its own, plus the
   // ghost faces lo-1 / hi+1 of the patch for the first / last segment
@@ -245,6 +251,7 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
       sw_setbnd(P, Wg, Bi, bs, dt, time + dt, true);
     }
   }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 // ============================================================== volume kernel

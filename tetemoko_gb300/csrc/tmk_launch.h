@@ -8,6 +8,7 @@
 namespace tmk {
 
 template <typename Real> struct PatchDev;
+template <typename Real> struct MarchConst;
 struct TileDev;
 struct CopyDev;
 struct MarchItem;
@@ -15,9 +16,9 @@ struct MarchItem;
 template <typename Real>
 struct Launch {
   static const int TX, TY;
-  // one thread per fault face of every fault patch
+  // one thread per fault face of every fault patch; pdl as for march
   static cudaError_t fault(const PatchDev<Real>* patches, const int* fault_patches, int nfault, int max_faces,
-                           const DevParams* params, double time, DevStatus* st, cudaStream_t s);
+                           const DevParams* params, double time, DevStatus* st, bool pdl, cudaStream_t s);
   // one CTA per (tile, side)
   static cudaError_t volume(const PatchDev<Real>* patches, const TileDev* tiles, int ntiles,
                             const DevParams* params, cudaStream_t s);
@@ -25,11 +26,16 @@ struct Launch {
   static cudaError_t exchange(const PatchDev<Real>* patches, const CopyDev* copies, int ncopies, int c0,
                               int ncomp, cudaStream_t s);
   static size_t volume_smem();
-  // column-marching volume update: one warp per item of each component group's
-  // list (items[0]: in-plane, items[1]: antiplane); hp is the host copy of the
-  // scenario, dt/dx those of every patch
-  static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* const items[2], const int nitems[2],
-                           const DevParams& hp, double dt, double dx, cudaStream_t s);
+  // column-marching volume update of component group g (0 in-plane, 1
+  // antiplane): one warp per item.  pdl: the kernel may be scheduled while
+  // the kernel before it in the stream still runs (programmatic dependent
+  // launch; it waits for that kernel before it exits)
+  static cudaError_t march(int g, const PatchDev<Real>* patches, const MarchItem* items, int nitems,
+                           const MarchConst<Real>& mc, bool pdl, cudaStream_t s);
+  // row 0 of the fault-row strips of both groups, after the fault kernel
+  static cudaError_t march_fault_rows(const PatchDev<Real>* patches, const MarchItem* rows0, int n0,
+                                      const MarchItem* rows1, int n1, const MarchConst<Real>& mc,
+                                      cudaStream_t s);
   // warps of group g's marching kernel resident at once on the current device
   static int march_slots(int g);
   // warps per CTA of the marching kernels

@@ -10,11 +10,18 @@ namespace tmk {
 template <typename Real, int TX_, int TY_, int NT_>
 struct LaunchImpl {
   static cudaError_t fault(const PatchDev<Real>* patches, const int* fp, int nfault, int max_faces,
-                           const DevParams* params, double time, DevStatus* st, cudaStream_t s) {
+                           const DevParams* params, double time, DevStatus* st, bool pdl, cudaStream_t s) {
     if (nfault <= 0) return cudaSuccess;
-    dim3 grid((max_faces + FAULT_SEG - 1) / FAULT_SEG, nfault);
-    fault_kernel<Real><<<grid, FAULT_THREADS, 0, s>>>(patches, fp, params, time, st);
-    return cudaGetLastError();
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((max_faces + FAULT_SEG - 1) / FAULT_SEG, nfault);
+    cfg.blockDim = dim3(FAULT_THREADS);
+    cfg.stream = s;
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, fault_kernel<Real>, patches, fp, params, time, st);
   }
   static size_t smem() { return sizeof(VolSmem<Real, TX_, TY_>); }
   static cudaError_t volume(const PatchDev<Real>* patches, const TileDev* tiles, int ntiles,
@@ -38,11 +45,9 @@ struct LaunchImpl {
     exchange_kernel<Real><<<ncopies, 256, 0, s>>>(patches, copies, c0, ncomp, 0);
     return cudaGetLastError();
   }
-  static cudaError_t march(const PatchDev<Real>* patches, const MarchItem* const items[2], const int nitems[2],
-                           const DevParams& hp, double dt, double dx, cudaStream_t s) {
-    if (nitems[0] <= 0 && nitems[1] <= 0) return cudaSuccess;
-    MarchConst<Real> mc;
-    mc.load(hp, dt, dx);
+  static cudaError_t march(int g, const PatchDev<Real>* patches, const MarchItem* items, int nitems,
+                           const MarchConst<Real>& mc, bool pdl, cudaStream_t s) {
+    if (nitems <= 0) return cudaSuccess;
     static bool configured = false;
     if (!configured) {
       cudaError_t e0 = cudaFuncSetAttribute(march_kernel<Real, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -53,28 +58,28 @@ struct LaunchImpl {
       if (e1 != cudaSuccess) return e1;
       configured = true;
     }
-    // programmatic dependent launch: each group's kernel may start while the
-    // kernel before it in the stream is still running (see march_kernel)
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cudaLaunchConfig_t cfg = {};
     cfg.blockDim = dim3(32 * MARCH_WARPS);
+    cfg.gridDim = dim3((nitems + MARCH_WARPS - 1) / MARCH_WARPS);
     cfg.stream = s;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    if (nitems[0] > 0) {
-      cfg.gridDim = dim3((nitems[0] + MARCH_WARPS - 1) / MARCH_WARPS);
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    if (g == 0) {
       cfg.dynamicSmemBytes = march_smem_bytes<Real, 0>();
-      cudaError_t e = cudaLaunchKernelEx(&cfg, march_kernel<Real, 0>, patches, items[0], nitems[0], mc);
-      if (e != cudaSuccess) return e;
+      return cudaLaunchKernelEx(&cfg, march_kernel<Real, 0>, patches, items, nitems, mc);
     }
-    if (nitems[1] > 0) {
-      cfg.gridDim = dim3((nitems[1] + MARCH_WARPS - 1) / MARCH_WARPS);
-      cfg.dynamicSmemBytes = march_smem_bytes<Real, 1>();
-      return cudaLaunchKernelEx(&cfg, march_kernel<Real, 1>, patches, items[1], nitems[1], mc);
-    }
-    return cudaSuccess;
+    cfg.dynamicSmemBytes = march_smem_bytes<Real, 1>();
+    return cudaLaunchKernelEx(&cfg, march_kernel<Real, 1>, patches, items, nitems, mc);
+  }
+  static cudaError_t march_fault_rows(const PatchDev<Real>* patches, const MarchItem* rows0, int n0,
+                                      const MarchItem* rows1, int n1, const MarchConst<Real>& mc, cudaStream_t s) {
+    if (n0 + n1 <= 0) return cudaSuccess;
+    const int blocks = (n0 + n1 + MARCH_WARPS - 1) / MARCH_WARPS;
+    march_fault_row_kernel<Real><<<blocks, 32 * MARCH_WARPS, 0, s>>>(patches, rows0, n0, rows1, n1, mc);
+    return cudaGetLastError();
   }
   static int march_slots(int g) {
     int dev = 0, sms = 0, b = 0;
@@ -105,8 +110,9 @@ struct LaunchImpl {
   template <> const int Launch<REAL>::TX = TXV;                                                             \
   template <> const int Launch<REAL>::TY = TYV;                                                             \
   template <> cudaError_t Launch<REAL>::fault(const PatchDev<REAL>* p, const int* fp, int nf, int mf,        \
-                                              const DevParams* prm, double t, DevStatus* st, cudaStream_t s) { \
-    return LaunchImpl<REAL, TXV, TYV, NTV>::fault(p, fp, nf, mf, prm, t, st, s);                             \
+                                              const DevParams* prm, double t, DevStatus* st, bool pdl,       \
+                                              cudaStream_t s) {                                              \
+    return LaunchImpl<REAL, TXV, TYV, NTV>::fault(p, fp, nf, mf, prm, t, st, pdl, s);                        \
   }                                                                                                          \
   template <> cudaError_t Launch<REAL>::volume(const PatchDev<REAL>* p, const TileDev* tl, int nt,          \
                                                const DevParams* prm, cudaStream_t s) {                      \
@@ -117,10 +123,14 @@ struct LaunchImpl {
     return LaunchImpl<REAL, TXV, TYV, NTV>::exchange(p, c, n, c0, nc, s);                                    \
   }                                                                                                          \
   template <> size_t Launch<REAL>::volume_smem() { return LaunchImpl<REAL, TXV, TYV, NTV>::smem(); }         \
-  template <> cudaError_t Launch<REAL>::march(const PatchDev<REAL>* p, const MarchItem* const it[2],        \
-                                              const int n[2], const DevParams& hp, double dt, double dx,   \
-                                              cudaStream_t s) {                                              \
-    return LaunchImpl<REAL, TXV, TYV, NTV>::march(p, it, n, hp, dt, dx, s);                                  \
+  template <> cudaError_t Launch<REAL>::march(int g, const PatchDev<REAL>* p, const MarchItem* it, int n,    \
+                                              const MarchConst<REAL>& mc, bool pdl, cudaStream_t s) {      \
+    return LaunchImpl<REAL, TXV, TYV, NTV>::march(g, p, it, n, mc, pdl, s);                                  \
+  }                                                                                                          \
+  template <> cudaError_t Launch<REAL>::march_fault_rows(const PatchDev<REAL>* p, const MarchItem* r0,      \
+                                                         int n0, const MarchItem* r1, int n1,              \
+                                                         const MarchConst<REAL>& mc, cudaStream_t s) {     \
+    return LaunchImpl<REAL, TXV, TYV, NTV>::march_fault_rows(p, r0, n0, r1, n1, mc, s);                      \
   }                                                                                                          \
   template <> int Launch<REAL>::march_slots(int g) { return LaunchImpl<REAL, TXV, TYV, NTV>::march_slots(g); } \
   template <> int Launch<REAL>::march_warps() { return MARCH_WARPS; }                                        \

@@ -130,6 +130,7 @@ struct MarchConst {
   P sc;              // -dt/dx
   int plim, clim, lim, ppm;
   int xout_lo, xout_hi, yout_lo, yout_hi;
+  void* stash[2];    // row-0 intermediates of the fault-row items, per component group
   TMK_HD void load(const DevParams& p, double dt, double dx) {
     const double dtdx = dt / dx;
     kx.load(p, 0, dtdx, -(1.0 / 2.0) * dt / dx);
@@ -355,7 +356,14 @@ TMK_D void adw2(const MK<T>& k, const typename PairOf<T>::P* h, const typename P
 }
 
 // ---------------------------------------------------------------- the kernel
-struct MarchItem { int patch, x0, y0, y1; };
+// A strip of MARCH_COLS columns of a patch by the rows [y0, y1].  fslot >= 0
+// marks the first item of a strip on the fault row: its row 0 needs the fault
+// kernel's results, so the kernel leaves that row to march_fault_row_kernel
+// and keeps what it needs in stash slot fslot.
+struct MarchItem { int patch, x0, y0, y1, fslot; };
+// vectors a fault-row item keeps for its row 0 (x states, first-pass y face 1,
+// final y flux 1, old state)
+constexpr int MARCH_STASH_VECS = 5;
 
 constexpr int MARCH_COLS = 26;   // updated columns per warp
 constexpr int MARCH_WARPS = 4;   // warps per CTA
@@ -418,7 +426,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
   const bool xout_lo = mc.xout_lo != 0, xout_hi = mc.xout_hi != 0, yout_lo = mc.yout_lo != 0,
              yout_hi = mc.yout_hi != 0;
   const bool fault = pp.fault != 0;
-  if (fault && it.y0 == dlo1) asm volatile("griddepcontrol.wait;" ::: "memory");
+  const bool defer0 = it.fslot >= 0;      // row 0 is finished by march_fault_row_kernel
   const bool col_valid = x >= it.x0 && x < it.x0 + MARCH_COLS && x >= pp.vlo0 && x <= pp.vhi0;
   const size_t plane = (size_t)pp.anx * pp.any;
 
@@ -569,14 +577,10 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
     if (need_h1y) {
       if (q == dlo1) {
         if (fault) {
-          const int fi = x - (pp.vlo0 - 1);
-          const bool ok = fi >= 0 && fi < pp.nfirst && x >= dlo0 && x <= dhi0;
+          // the fault kernel's first-pass face state: only row 0's transverse
+          // correction reads it, and row 0 of a fault patch is finished later
 #pragma unroll
-          for (int c = 0; c < N; ++c) {
-            const int g = Grp<G>::glob(c);
-            H1y[c] = ok ? mk2((T)pp.first[(size_t)g * pp.nfirst + fi], (T)pp.first[(size_t)(11 + g) * pp.nfirst + fi])
-                        : mk2(T(0), T(0));
-          }
+          for (int c = 0; c < N; ++c) H1y[c] = mk2(T(0), T(0));
         } else {
           edge2<G, 1, T>(ky, true, yout_lo, WMy, bg, H1y);
         }
@@ -590,15 +594,8 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
     P Fy[N];
     if (q >= it.y0) {
       if (q == dlo1 && fault) {
-        const int nv = pp.vhi0 - pp.vlo0 + 1;
-        const int fi = x - pp.vlo0;
-        const bool ok = fi >= 0 && fi < nv;
 #pragma unroll
-        for (int c = 0; c < N; ++c) {
-          const int g = Grp<G>::glob(c);
-          Fy[c] = ok ? mk2((T)pp.ffault[(size_t)g * nv + fi], (T)pp.ffault[(size_t)(11 + g) * nv + fi])
-                     : mk2(T(0), T(0));
-        }
+        for (int c = 0; c < N; ++c) Fy[c] = mk2(T(0), T(0));   // the fault flux: row 0 is finished later
       } else {
         P g[N];
         if (q == dlo1) edge2<G, 1, T>(ky, true, yout_lo, WMcy, bg, g);
@@ -607,8 +604,23 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
         flux2<G, 1, T>(ky, g, Fy);
       }
     }
-    // row q-1: transverse correction of its x states, final x faces, update
-    if (q - 1 >= it.y0) {
+    // row q-1: transverse correction of its x states, final x faces, update;
+    // row 0 of a fault patch: keep what march_fault_row_kernel needs
+    if (defer0 && q - 1 == dlo1) {
+      P* st = reinterpret_cast<P*>(mc.stash[G]) + (size_t)it.fslot * MARCH_STASH_VECS * N * 32 + lane;
+      P a[N];
+      cget(kWMx, a);
+#pragma unroll
+      for (int c = 0; c < N; ++c) st[(0 * N + c) * 32] = a[c];
+      cget(kWPx, a);
+#pragma unroll
+      for (int c = 0; c < N; ++c) st[(1 * N + c) * 32] = a[c];
+#pragma unroll
+      for (int c = 0; c < N; ++c) { st[(2 * N + c) * 32] = H1y[c]; st[(3 * N + c) * 32] = Fy[c]; }
+      cget(kWold, a);
+#pragma unroll
+      for (int c = 0; c < N; ++c) st[(4 * N + c) * 32] = a[c];
+    } else if (q - 1 >= it.y0) {
       P WMcx[N], WPcx[N];
       {
         P H1y_p[N];
@@ -656,6 +668,78 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// Row 0 of a fault-row strip of group G once the fault kernel has produced the
+// first-pass fault states and the fault-face fluxes: the transverse correction
+// of the row's x states, its final x faces and its update (the same steps as
+// the marching loop, with the stashed row-0 intermediates).
+template <typename T, int G>
+TMK_D void fault_row_finish(const PatchDev<T>& pp, const MarchItem& it, const MarchConst<T>& mc, int lane) {
+  using P = typename PairOf<T>::P;
+  constexpr int N = Grp<G>::N;
+  const int x = it.x0 - 3 + lane;
+  const int dlo0 = pp.dlo0, dhi0 = pp.dhi0, dlo1 = pp.dlo1;
+  const P* st = reinterpret_cast<const P*>(mc.stash[G]) + (size_t)it.fslot * MARCH_STASH_VECS * N * 32 + lane;
+  P WMcx[N], WPcx[N], H1y1[N], Fy1[N], Wold[N], H1y0[N], Fy0[N];
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    WMcx[c] = st[(0 * N + c) * 32]; WPcx[c] = st[(1 * N + c) * 32];
+    H1y1[c] = st[(2 * N + c) * 32]; Fy1[c] = st[(3 * N + c) * 32]; Wold[c] = st[(4 * N + c) * 32];
+  }
+  const int fi1 = x - (pp.vlo0 - 1);
+  const bool ok1 = fi1 >= 0 && fi1 < pp.nfirst && x >= dlo0 && x <= dhi0;
+  const int nv = pp.vhi0 - pp.vlo0 + 1, fi2 = x - pp.vlo0;
+  const bool ok2 = fi2 >= 0 && fi2 < nv;
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const int g = Grp<G>::glob(c);
+    H1y0[c] = ok1 ? mk2((T)pp.first[(size_t)g * pp.nfirst + fi1], (T)pp.first[(size_t)(11 + g) * pp.nfirst + fi1])
+                  : mk2(T(0), T(0));
+    Fy0[c] = ok2 ? mk2((T)pp.ffault[(size_t)g * nv + fi2], (T)pp.ffault[(size_t)(11 + g) * nv + fi2])
+                 : mk2(T(0), T(0));
+  }
+  adw2<G, 1, T>(mc.ky, H1y1, H1y0, WMcx, WPcx);
+  const BgView<G, P> bg{mc.bg};
+  P L[N], g[N], Fx[N], Fxh[N];
+#pragma unroll
+  for (int c = 0; c < N; ++c) L[c] = shfl_up2(WPcx[c], 1);
+  if (x == dlo0) edge2<G, 0, T>(mc.kx, true, mc.xout_lo != 0, WMcx, bg, g);
+  else if (x == dhi0 + 1) edge2<G, 0, T>(mc.kx, false, mc.xout_hi != 0, L, bg, g);
+  else riem<G, 0, T>(mc.kx, L, WMcx, g);
+  flux2<G, 0, T>(mc.kx, g, Fx);
+#pragma unroll
+  for (int c = 0; c < N; ++c) Fxh[c] = shfl_dn2(Fx[c], 1);
+  const bool col_valid = x >= it.x0 && x < it.x0 + MARCH_COLS && x >= pp.vlo0 && x <= pp.vhi0;
+  if (col_valid) {
+    const size_t plane = (size_t)pp.anx * pp.any;
+    const size_t o = fab_idx(pp, 0, x, dlo1);
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      const int gg = Grp<G>::glob(c);
+      P du = padd(psub(Fxh[c], Fx[c]), psub(Fy1[c], Fy0[c]));
+      P u = pfma(du, mc.sc, Wold[c]);
+      pp.Uout[o + (size_t)gg * plane] = u.x;
+      pp.Uout[o + (size_t)(11 + gg) * plane] = u.y;
+    }
+  }
+}
+
+// One warp per fault-row strip: rows0 (in-plane) then rows1 (antiplane).
+template <typename T>
+__global__ void __launch_bounds__(32 * MARCH_WARPS) march_fault_row_kernel(const PatchDev<T>* __restrict__ patches,
+                                                                           const MarchItem* __restrict__ rows0, int n0,
+                                                                           const MarchItem* __restrict__ rows1, int n1,
+                                                                           const __grid_constant__ MarchConst<T> mc) {
+  const int wid = blockIdx.x * MARCH_WARPS + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (wid < n0) {
+    const MarchItem it = rows0[wid];
+    fault_row_finish<T, 0>(patches[it.patch], it, mc, lane);
+  } else if (wid < n0 + n1) {
+    const MarchItem it = rows1[wid - n0];
+    fault_row_finish<T, 1>(patches[it.patch], it, mc, lane);
+  }
 }
 
 }  // namespace tmk
