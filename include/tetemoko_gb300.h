@@ -5,7 +5,7 @@
  * Every entry point is plain C: pointers, sizes and POD structs only.  A Chombo
  * build calls these from thin shims that keep the reference's class names
  * (LinElastLevelGodunov, LinElastPatchGodunov, LEPhysIBC/RSIBC/SWIBC,
- * LinElastPhysics::plasticUpdate); the shims are shown in INTEGRATION.md.
+ * LinElastPhysics::plasticUpdate).
  *
  * Data layout.  State arrays use Chombo's FArrayBox layout: structure of arrays,
  * i fastest, then j, then component, over the allocated box (valid box grown by
@@ -135,6 +135,7 @@ typedef struct { int lo[2], hi[2]; } tmk_box;   /* cell-centred, inclusive */
 typedef struct tmk_context_s tmk_context;
 typedef struct tmk_level_s   tmk_level;
 typedef struct tmk_amr_s     tmk_amr;
+typedef struct tmk_graph_s   tmk_graph;
 
 /* ---------------------------------------------------------------------------
  * Parameters (replaces the process-global Fortran COMMON blocks /IBC/, /rs/,
@@ -306,6 +307,21 @@ tmk_status tmk_amr_time(const tmk_amr* amr, int level, double* time);
 long long  tmk_amr_cell_updates(const tmk_amr* amr);
 /* Kernel launches of one tmk_amr_step. */
 int        tmk_amr_launches_per_step(const tmk_amr* amr);
+
+/* ---------------------------------------------------------------------------
+ * CUDA graphs of whole steps.  tmk_level_graph_create records `nsteps` (even)
+ * steps of a level without a coarser level, starting at `time` by `dt`;
+ * tmk_amr_graph_create records `ncoarse` (even) subcycled coarse steps of a
+ * hierarchy by `dt0` from its current time.  Recording runs nothing.
+ * tmk_graph_launch replays the steps on `stream` starting at `time` (the start
+ * times of the recorded fault solves are shifted accordingly) and, for a
+ * hierarchy, advances its clock.  The recorded steps keep the level layout,
+ * attachments and dt of the recording: rebuild the graph after a regrid.
+ * ------------------------------------------------------------------------- */
+tmk_status tmk_level_graph_create(tmk_level* lvl, int nsteps, double time, double dt, tmk_graph** out);
+tmk_status tmk_amr_graph_create(tmk_amr* amr, int ncoarse, double dt0, tmk_graph** out);
+tmk_status tmk_graph_launch(tmk_graph* graph, double time, void* stream);
+void       tmk_graph_destroy(tmk_graph* graph);
 
 #ifdef __cplusplus
 }

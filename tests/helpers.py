@@ -5,7 +5,7 @@ import numpy as np
 
 from tetemoko_gb300 import _capi as A
 
-# FP64 parity tolerance against the oracle (spec: 1e-12 relative)
+# FP64 parity tolerance against the oracle: 1e-12 relative
 RTOL_FP64 = 1e-12
 
 

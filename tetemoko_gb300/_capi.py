@@ -147,13 +147,19 @@ def lib() -> C.CDLL:
     L.tmk_amr_cell_updates.restype = C.c_longlong
     L.tmk_amr_launches_per_step.argtypes = [vp]
     L.tmk_amr_launches_per_step.restype = C.c_int
+    L.tmk_level_graph_create.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.POINTER(vp)]
+    L.tmk_amr_graph_create.argtypes = [vp, C.c_int, C.c_double, C.POINTER(vp)]
+    L.tmk_graph_launch.argtypes = [vp, C.c_double, vp]
+    L.tmk_graph_destroy.argtypes = [vp]
+    L.tmk_graph_destroy.restype = None
     for name in ("tmk_context_create", "tmk_context_constants", "tmk_patch_update_state",
                  "tmk_plastic_update", "tmk_max_wave_speed", "tmk_level_create", "tmk_level_set_patch",
                  "tmk_level_get_patch", "tmk_level_step", "tmk_level_status", "tmk_level_profile",
                  "tmk_level_profile_read", "tmk_level_step_cf", "tmk_level_attach_coarser",
                  "tmk_level_detach_coarser", "tmk_level_fill_coarse_fine", "tmk_level_reflux",
                  "tmk_level_average_down", "tmk_level_interp_from_coarser", "tmk_level_copy_overlap",
-                 "tmk_level_register_size", "tmk_amr_create", "tmk_amr_step", "tmk_amr_time"):
+                 "tmk_level_register_size", "tmk_amr_create", "tmk_amr_step", "tmk_amr_time",
+                 "tmk_level_graph_create", "tmk_amr_graph_create", "tmk_graph_launch"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

@@ -14,7 +14,7 @@ from __future__ import annotations
 import ctypes as C
 
 from . import _capi as A
-from .level import LinElastLevelGodunov, _stream_ptr
+from .level import LinElastLevelGodunov, StepGraph, _stream_ptr
 
 
 def refine_domain(domain, r: int):
@@ -52,6 +52,13 @@ class AMRHierarchy:
 
     def launches_per_step(self) -> int:
         return int(self.lib.tmk_amr_launches_per_step(self.h))
+
+    def graph(self, ncoarse: int, dt0: float) -> StepGraph:
+        """Record `ncoarse` (even) subcycled coarse steps as one CUDA graph from
+        the current time; StepGraph.launch(t) replays them from time t."""
+        h = C.c_void_p()
+        A.check(self.lib.tmk_amr_graph_create(self.h, ncoarse, dt0, C.byref(h)), "tmk_amr_graph_create")
+        return StepGraph(self.lib, h)
 
     def close(self):
         if self.h:

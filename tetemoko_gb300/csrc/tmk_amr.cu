@@ -1026,3 +1026,145 @@ extern "C" int tmk_amr_launches_per_step(const tmk_amr* h) {
   }
   return total;
 }
+
+// ------------------------------------------------------------ CUDA graphs
+// A captured sequence of level steps or AMR coarse steps.  Every step's
+// launches are recorded once; a replay shifts the start-time argument of the
+// captured fault-kernel nodes (the only launch argument that changes from one
+// replay to the next) and launches the executable graph.
+struct tmk_graph_s {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<cudaGraphNode_t> tnodes;   // fault-kernel nodes
+  std::vector<double> tbase;             // their time argument at capture
+  double t0 = 0.0;                       // start time at capture
+  double span = 0.0;                     // time advanced by one replay
+  double dt0 = 0.0;                      // coarse step of an AMR graph
+  tmk_amr* amr = nullptr;                // hierarchy whose host clock a replay advances
+};
+
+namespace {
+
+tmk_status graph_finish(tmk_graph_s* g) {
+  if (cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess) return TMK_ERR_CUDA;
+  size_t n = 0;
+  if (cudaGraphGetNodes(g->graph, nullptr, &n) != cudaSuccess) return TMK_ERR_CUDA;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (n && cudaGraphGetNodes(g->graph, nodes.data(), &n) != cudaSuccess) return TMK_ERR_CUDA;
+  const void* f32 = tmk::Launch<float>::fault_entry();
+  const void* f64 = tmk::Launch<double>::fault_entry();
+  for (cudaGraphNode_t nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) != cudaSuccess) return TMK_ERR_CUDA;
+    if (t != cudaGraphNodeTypeKernel) continue;
+    cudaKernelNodeParams p;
+    if (cudaGraphKernelNodeGetParams(nd, &p) != cudaSuccess) return TMK_ERR_CUDA;
+    if (p.func != f32 && p.func != f64) continue;
+    g->tnodes.push_back(nd);
+    g->tbase.push_back(*(const double*)p.kernelParams[3]);
+  }
+  return TMK_OK;
+}
+
+void graph_free(tmk_graph_s* g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+}
+
+// descriptors of every level for its step size, before a capture (no host
+// copies may happen while capturing)
+tmk_status prepare_dt(tmk_level_s* L, double dt, cudaStream_t s) {
+  if (dt == L->cur_dt) return TMK_OK;
+  L->cur_dt = dt;
+  if (upload_patchdev(L, s) != TMK_OK) return TMK_ERR_CUDA;
+  TMK_CU(cudaStreamSynchronize(s));
+  return TMK_OK;
+}
+
+}  // namespace
+
+extern "C" tmk_status tmk_level_graph_create(tmk_level* L, int nsteps, double time, double dt, tmk_graph** out) {
+  if (!out) return TMK_ERR_BAD_DESC;
+  *out = nullptr;
+  if (!L || nsteps <= 0 || (nsteps & 1) || !(dt > 0) || L->coarser || L->prof_on) return TMK_ERR_BAD_DESC;
+  cudaStream_t cs;
+  TMK_CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  tmk_status st = prepare_dt(L, dt, cs);
+  tmk_graph_s* g = st == TMK_OK ? new (std::nothrow) tmk_graph_s() : nullptr;
+  if (st == TMK_OK && !g) st = TMK_ERR_ALLOC;
+  if (st == TMK_OK && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) st = TMK_ERR_CUDA;
+  if (st == TMK_OK) {
+    for (int k = 0; k < nsteps && st == TMK_OK; ++k) st = tmk_level_step(L, time + k * dt, dt, cs, nullptr);
+    if (cudaStreamEndCapture(cs, &g->graph) != cudaSuccess && st == TMK_OK) st = TMK_ERR_CUDA;
+  }
+  if (st == TMK_OK) st = graph_finish(g);
+  cudaStreamDestroy(cs);
+  if (st != TMK_OK) { graph_free(g); return st; }
+  g->t0 = time;
+  g->span = nsteps * dt;
+  *out = g;
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_amr_graph_create(tmk_amr* h, int ncoarse, double dt0, tmk_graph** out) {
+  if (!out) return TMK_ERR_BAD_DESC;
+  *out = nullptr;
+  if (!h || ncoarse <= 0 || (ncoarse & 1) || !(dt0 > 0)) return TMK_ERR_BAD_DESC;
+  for (tmk_level* L : h->L) if (L->prof_on) return TMK_ERR_BAD_DESC;
+  cudaStream_t cs;
+  TMK_CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  tmk_status st = TMK_OK;
+  double dtl = dt0;
+  for (size_t l = 0; l < h->L.size() && st == TMK_OK; ++l) {
+    st = prepare_dt(h->L[l], dtl, cs);
+    if (l < h->ratio.size()) dtl /= h->ratio[l];
+  }
+  const std::vector<double> time0 = h->time, dtlast0 = h->dtlast;
+  tmk_graph_s* g = st == TMK_OK ? new (std::nothrow) tmk_graph_s() : nullptr;
+  if (st == TMK_OK && !g) st = TMK_ERR_ALLOC;
+  if (st == TMK_OK && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) st = TMK_ERR_CUDA;
+  if (st == TMK_OK) {
+    for (int k = 0; k < ncoarse && st == TMK_OK; ++k) st = amr_advance(h, 0, dt0, cs);
+    if (cudaStreamEndCapture(cs, &g->graph) != cudaSuccess && st == TMK_OK) st = TMK_ERR_CUDA;
+  }
+  // nothing ran: the hierarchy's clock stays where it was
+  h->time = time0;
+  h->dtlast = dtlast0;
+  if (st == TMK_OK) st = graph_finish(g);
+  cudaStreamDestroy(cs);
+  if (st != TMK_OK) { graph_free(g); return st; }
+  g->t0 = time0[0];
+  g->span = ncoarse * dt0;
+  g->dt0 = dt0;
+  g->amr = h;
+  *out = g;
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_graph_launch(tmk_graph* g, double time, void* stream) {
+  if (!g || !g->exec) return TMK_ERR_BAD_DESC;
+  const double shift = time - g->t0;
+  for (size_t k = 0; k < g->tnodes.size(); ++k) {
+    cudaKernelNodeParams p;
+    TMK_CU(cudaGraphKernelNodeGetParams(g->tnodes[k], &p));
+    double t = g->tbase[k] + shift;
+    void* args[5] = {p.kernelParams[0], p.kernelParams[1], p.kernelParams[2], &t, p.kernelParams[4]};
+    p.kernelParams = args;
+    TMK_CU(cudaGraphExecKernelNodeSetParams(g->exec, g->tnodes[k], &p));
+  }
+  TMK_CU(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+  if (g->amr) {   // the hierarchy's clock after the replayed coarse steps
+    tmk_amr* h = g->amr;
+    double dtl = g->dt0;
+    for (size_t l = 0; l < h->L.size(); ++l) {
+      h->time[l] = time + g->span;
+      h->dtlast[l] = dtl;
+      if (l < h->ratio.size()) dtl /= h->ratio[l];
+    }
+  }
+  return TMK_OK;
+}
+
+extern "C" void tmk_graph_destroy(tmk_graph* g) { graph_free(g); }

@@ -40,6 +40,9 @@ struct Launch {
   static int march_slots(int g);
   // warps per CTA of the marching kernels
   static int march_warps();
+  // the fault kernel's entry (to find its nodes in a captured graph); its
+  // fourth parameter is the step's start time
+  static const void* fault_entry();
 };
 
 // FP64 <-> Real conversion of a FAB on the device

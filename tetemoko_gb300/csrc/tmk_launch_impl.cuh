@@ -134,4 +134,5 @@ struct LaunchImpl {
   }                                                                                                          \
   template <> int Launch<REAL>::march_slots(int g) { return LaunchImpl<REAL, TXV, TYV, NTV>::march_slots(g); } \
   template <> int Launch<REAL>::march_warps() { return MARCH_WARPS; }                                        \
+  template <> const void* Launch<REAL>::fault_entry() { return (const void*)fault_kernel<REAL>; }           \
   }

@@ -269,6 +269,12 @@ class LinElastLevelGodunov:
     def launches_per_step(self) -> int:
         return self.lib.tmk_level_launches_per_step(self.h)
 
+    def graph(self, nsteps: int, time: float, dt: float) -> "StepGraph":
+        """Record `nsteps` (even) steps as one CUDA graph (nothing runs yet)."""
+        h = C.c_void_p()
+        A.check(self.lib.tmk_level_graph_create(self.h, nsteps, time, dt, C.byref(h)), "tmk_level_graph_create")
+        return StepGraph(self.lib, h)
+
     def profile(self, enable: bool, max_steps: int = 0):
         A.check(self.lib.tmk_level_profile(self.h, int(enable), max_steps), "tmk_level_profile")
 
@@ -282,6 +288,29 @@ class LinElastLevelGodunov:
     def close(self):
         if self.h:
             self.lib.tmk_level_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class StepGraph:
+    """Recorded steps of a level or an AMR hierarchy (tmk_graph)."""
+
+    def __init__(self, lib, h):
+        self.lib = lib
+        self.h = h
+
+    def launch(self, time: float, stream=None):
+        """Replay the recorded steps starting at `time`."""
+        A.check(self.lib.tmk_graph_launch(self.h, time, _stream_ptr(stream)), "tmk_graph_launch")
+
+    def close(self):
+        if self.h:
+            self.lib.tmk_graph_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -117,7 +117,7 @@ def psi_steady(tau: float, sn: float, V: float, a: float, V0: float, Zs: float) 
 def slip_weakening(nx=512, ny=256, dx=0.1, precision=A.TMK_PREC_FP64,
                    layout=A.TMK_SW_LAYOUT_OFFSET11, cfl=0.9, plasticity=False,
                    nuc_tau=11.6, nuc_half_width=1.5) -> Scenario:
-    """Slip-weakening planar fault at y=0 (BASELINE configuration 1 at 512x256, dx=0.1 km):
+    """Slip-weakening planar fault at y=0 (the 512x256, dx=0.1 km CPU-runnable workload):
     mu_s=0.677, mu_d=0.525, Dc=0.4 m, sn=120 MPa, tau=70 MPa, a 3 km nucleation
     window at 81.6 MPa (11.6 MPa excess), friction box covering the whole fault."""
     sw = A.SWParams()
@@ -138,7 +138,7 @@ def slip_weakening(nx=512, ny=256, dx=0.1, precision=A.TMK_PREC_FP64,
 
 def rate_state(nx=2048, ny=1024, dx=0.1, precision=A.TMK_PREC_FP64,
                state_law=A.TMK_RS_AGING_LAW, cfl=0.9, plasticity=False, V_init=1e-12) -> Scenario:
-    """Rate-and-state planar fault at y=0 (BASELINE configuration 2 at 2048x1024, dx=0.1 km):
+    """Rate-and-state planar fault at y=0 (the 2048x1024, dx=0.1 km benchmark workload):
     a=0.008, b=0.012, L=0.02 m, f0=0.6, V0=1e-6 m/s, initial V=1e-12 m/s, Gaussian
     shear nucleation of 25 MPa amplitude and 3 km width at the fault centre."""
     e = _elastic()
