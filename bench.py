@@ -219,6 +219,101 @@ def cpu_sample(sc, max_seconds, nthreads, strip_rows=None):
     return rate, desc
 
 
+def tile_boxes(lo0, lo1, hi0, hi1, max_grid):
+    """Cover [lo0, hi0] x [lo1, hi1] with boxes of at most max_grid cells per side."""
+    out = []
+    for j0 in range(lo1, hi1 + 1, max_grid):
+        for i0 in range(lo0, hi0 + 1, max_grid):
+            out.append((i0, j0, min(i0 + max_grid - 1, hi0), min(j0 + max_grid - 1, hi1)))
+    return out
+
+
+# 4-level hierarchy, ratio 2, base 1024 x 512 (dx 0.1 km, effective 8192 x 4096 at
+# 12.5 m): nested bands along the fault around the nucleation (cell boxes per level)
+AMR_BASE = (1024, 512)
+AMR_REGIONS = [(512, 0, 1535, 255), (1280, 0, 2815, 383), (3072, 0, 5119, 511)]
+
+
+def amr_measurement(steps, warmup, stream):
+    """Subcycled 4-level rate-and-state hierarchy with plasticity, a normal
+    stress rising along strike from 20 to 120 MPa and the shear prestress in
+    proportion; steps replayed from a CUDA graph of 2 coarse steps.  Returns
+    the JSON object of the measurement."""
+    import numpy as np
+    import torch
+    from tetemoko_gb300 import _capi as A, scenarios as S
+    from tetemoko_gb300.amr import AMRHierarchy, refine_domain
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    nx, ny = AMR_BASE
+    sc = S.rate_state(nx=nx, ny=ny, precision=A.TMK_PREC_MIXED, plasticity=True)
+    ctx = Context(sc)
+    g = A.TMK_NGHOST
+    levels, boxes_all = [], []
+    dom = (0, 0, nx - 1, ny - 1)
+    dx = sc.dx
+    boxes = tile_boxes(0, 0, nx - 1, ny - 1, 128)
+    for l in range(4):
+        if l > 0:
+            dom = refine_domain(dom, 2)
+            dx = dx / 2
+            boxes = tile_boxes(*AMR_REGIONS[l - 1], 128)
+        levels.append(LinElastLevelGodunov(ctx, boxes, domain=dom, dx=dx))
+        boxes_all.append(boxes)
+    # level 0: background with syy(x) from -20 to -120 MPa along strike
+    x = (np.arange(-g, nx + g) + 0.5) / nx
+    for p, b in enumerate(boxes_all[0]):
+        U = sc.initial_U(lo=b[:2], hi=b[2:])
+        xs = np.clip(x[b[0]:b[2] + 2 * g + 1], 0.0, 1.0)
+        for side in (0, 11):          # shear keeps the 70/120 ratio of the uniform workload
+            U[side + 4] = -(20.0 + 100.0 * xs)[None, :]
+            U[side + 6] = (70.0 / 120.0) * (20.0 + 100.0 * xs)[None, :]
+        B = sc.initial_B(xlo=b[0], xhi=b[2]) if b[1] == 0 else None
+        levels[0].set_patch(p, U, B)
+    for l in range(1, 4):        # finer levels from the coarser ones (regrid prolongation)
+        levels[l].attach_coarser(levels[l - 1], 2)
+        levels[l].interp_from_coarser(stream)
+    torch.cuda.synchronize()
+    h = AMRHierarchy(levels, [2, 2, 2])
+    dt0 = sc.dt()
+    for _ in range(warmup):
+        h.step(dt0, stream)
+    graph = h.graph(2, dt0)
+    t = h.time(0)
+    graph.launch(t, stream)
+    t += 2 * dt0
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    nrep = max(1, steps // 2)
+    e0.record(stream)
+    for _ in range(nrep):
+        graph.launch(t, stream)
+        t += 2 * dt0
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    per_step = h.cell_updates()
+    status = [lv.status()[1] for lv in levels]
+    cells = [sum((b[2] - b[0] + 1) * (b[3] - b[1] + 1) for b in bx) for bx in boxes_all]
+    out = {"value": per_step * 2 * nrep / (ms * 1e-3), "unit": "cell-updates/s",
+           "ms_per_coarse_step": ms / (2 * nrep), "coarse_steps": 2 * nrep,
+           "cell_updates_per_coarse_step": per_step, "cells_per_level": cells,
+           "patches_per_level": [len(b) for b in boxes_all],
+           "launches_per_coarse_step": h.launches_per_step(),
+           "config": "4 levels, ratio 2, base 1024x512 at dx=0.1 km (finest 12.5 m, effective 8192x4096), "
+                     "rate-and-state aging law, Drucker-Prager plasticity, normal stress 20-120 MPa along "
+                     "strike, FP32 volume / FP64 fault, patches of at most 128x128, static nested bands "
+                     "around the nucleation (no tagging)",
+           "execution": "CUDA graph of 2 subcycled coarse steps (tmk_amr_graph_create), replayed",
+           "device_status": status}
+    graph.close()
+    h.close()
+    for lv in levels:
+        lv.close()
+    ctx.close()
+    return out
+
+
 def host_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -280,6 +375,7 @@ def main():
     ap.add_argument("--fp64-kernel", default="march", choices=["march", "tile"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--amr-steps", type=int, default=16)   # timed coarse steps of the AMR measurement
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     args = ap.parse_args()
@@ -315,12 +411,19 @@ def main():
         lvl.set_patch(0, sc.initial_U(), sc.initial_B())
         return sc, ctx, lvl
 
-    def timed(lvl, sc, steps, warmup, profile=False, sampler=None):
+    def timed(lvl, sc, steps, warmup, profile=False, sampler=None, graph_steps=0):
         dt = sc.dt()
         t = 0.0
         for _ in range(warmup):
             lvl.step(t, dt, stream)
             t += dt
+        graph = None
+        if graph_steps:
+            # record graph_steps steps once; the timed loop replays them
+            graph = lvl.graph(graph_steps, t, dt)
+            for _ in range(2):
+                graph.launch(t, stream)
+                t += graph_steps * dt
         if profile:
             lvl.profile(True, steps)
         torch.cuda.synchronize()
@@ -333,9 +436,14 @@ def main():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(steps):
-            lvl.step(t, dt, stream)
-            t += dt
+        if graph is not None:
+            for _ in range(steps // graph_steps):
+                graph.launch(t, stream)
+                t += graph_steps * dt
+        else:
+            for _ in range(steps):
+                lvl.step(t, dt, stream)
+                t += dt
         e1.record(stream)
         torch.cuda.synchronize()
         clocks = sampler.stop() if sampler else None
@@ -345,14 +453,25 @@ def main():
         if profile:
             lvl.profile(False)
         rc, info = lvl.status()
+        if graph is not None:
+            graph.close()
         return ms, prof, clocks, (rc, info)
 
     # ---- mixed form (headline): an uninstrumented timed pass for the value, then
     # a second timed pass with CUDA events around every launch for the roofline
     # (events between the fault and volume kernels serialise their overlap)
     sc, ctx, lvl = make_level(A.TMK_PREC_MIXED)
+    # steps replayed from a CUDA graph of graph_steps recorded steps (the
+    # largest even divisor of --steps up to 100); also timed call by call
+    graph_steps = next((g for g in range(min(100, args.steps), 1, -1) if args.steps % g == 0 and g % 2 == 0), 0)
+    _, ctx_c, lvl_c = make_level(A.TMK_PREC_MIXED)       # same workload from its initial state
+    ms_call, _, _, _ = timed(lvl_c, sc, args.steps, args.warmup, profile=False)
+    value_call, _ = replica_rate(cells, args.steps, ms_call * 1e-3, world, device="cuda")
+    lvl_c.close()
+    ctx_c.close()
     sampler = make_clock_sampler() if rank == 0 else None
-    ms, _, clocks, st = timed(lvl, sc, args.steps, args.warmup, profile=False, sampler=sampler)
+    ms, _, clocks, st = timed(lvl, sc, args.steps, args.warmup, profile=False, sampler=sampler,
+                              graph_steps=graph_steps)
     value, secs = replica_rate(cells, args.steps, ms * 1e-3, world, device="cuda")
     ms = secs * 1e3
     launches = lvl.launches_per_step() * args.steps
@@ -420,6 +539,9 @@ def main():
     lvl64.close()
     ctx64.close()
 
+    # ---- subcycled 4-level AMR hierarchy (rank 0 reports its own)
+    amr = amr_measurement(args.amr_steps, 2, stream) if args.amr_steps > 0 else None
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and args.cpu_seconds > 0:
@@ -438,11 +560,16 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "note": "per step: FP64 state copied host->device (pinned), level step, state copied back"},
             "gpu_launches": launches,
+            "execution": (f"steps replayed from a CUDA graph of {graph_steps} recorded level steps "
+                          "(tmk_level_graph_create / tmk_graph_launch)") if graph_steps else "one call per step",
+            "per_call": {"value": value_call, "unit": UNIT, "ms_per_step": ms_call / args.steps,
+                         "note": "the same steps, one tmk_level_step call each"},
             "clocks": clocks,
             "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_step": ms64 / n64, "steps": n64,
                            "volume_kernel": args.fp64_kernel, "volume_kernel_ms": vol64,
                            "volume_hbm_gbs": BYTES_PER_CELL_FP64 * cells / (vol64 * 1e-3) / 1e9},
             "mixed_over_fp64": value / value64,
+            "amr": amr,
             "device_status": {"mixed": st[1], "fp64": st64[1]},
         }
         print(json.dumps(line), flush=True)

@@ -116,11 +116,10 @@ typedef struct {
 } tmk_scheme;
 
 /* Implementations of the volume update (same results to rounding):
- * TILE  shared-memory tiles, one side of the fault per CTA (also fuses plasticity);
- * MARCH column-marching warps with both sides packed per lane (no plasticity);
- * AUTO  MARCH without plasticity, TILE with plasticity and on levels coupled
- *       to a coarser or finer level (the tile kernel stores the coarse-fine
- *       face fluxes). */
+ * TILE  shared-memory tiles, one side of the fault per CTA (fuses plasticity);
+ * MARCH column-marching warps with both sides packed per lane, plasticity as a
+ *       pointwise pass after the update;
+ * AUTO  MARCH.  Both store the coarse-fine face fluxes of coupled levels. */
 enum { TMK_VOLUME_AUTO = 0, TMK_VOLUME_TILE = 1, TMK_VOLUME_MARCH = 2 };
 
 /* Chombo FArrayBox view: data[((c*(hi1-lo1+1)) + (j-lo1))*(hi0-lo0+1) + (i-lo0)] */
@@ -259,8 +258,8 @@ tmk_status tmk_level_profile_read(tmk_level* lvl, double out[4], int* nsteps);
  * the fine level properly nested (each coarse cell an operator reads is a valid
  * cell of the coarse level), else TMK_ERR_BAD_DESC.  Attaching replaces an
  * earlier attachment of either level.  Both levels must use the same precision
- * and fault law.  A level with attachments computes its volume update with the
- * tile kernel, which also stores the fluxes of the coarse-fine faces.
+ * and fault law.  The volume update of an attached level also stores the
+ * fluxes of its coarse-fine faces for the flux registers.
  * ------------------------------------------------------------------------- */
 tmk_status tmk_level_attach_coarser(tmk_level* fine, tmk_level* coarse, int ref_ratio);
 tmk_status tmk_level_detach_coarser(tmk_level* fine);

@@ -447,6 +447,7 @@ tmk_status rebuild_captures(tmk_level_s* L) {
   for (void* p : L->cap_allocs) cudaFree(p);
   L->cap_allocs.clear();
   L->cap = nullptr; L->dcaplist = nullptr; L->ncap = n;
+  L->dmcap[0] = L->dmcap[1] = nullptr;
   if (n) {
     if (dalloc(&L->cap, (size_t)n * NC) != cudaSuccess) return TMK_ERR_ALLOC;
     L->cap_allocs.push_back(L->cap);
@@ -456,7 +457,48 @@ tmk_status rebuild_captures(tmk_level_s* L) {
     TMK_CU(cudaMemcpy(L->dcaplist, list.data(), list.size() * sizeof(int4), cudaMemcpyHostToDevice));
   }
   TMK_CU(cudaMemcpy(L->dtiles, L->htiles.data(), L->htiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice));
-  L->march = (L->march_allowed && n == 0) ? 1 : 0;    // the tile kernel captures faces
+  // the same faces for the marching items of each component group: the item
+  // holding the cell on the face's side inside the patch, sorted by row
+  for (int g = 0; g < 2 && L->march_allowed; ++g) {
+    std::vector<tmk::MarchItem>& items = L->hitems[g];
+    std::vector<std::vector<int4>> per(items.size());
+    for (const auto& kv : slot) {
+      const int p = std::get<0>(kv.first), d = std::get<1>(kv.first);
+      const int i = std::get<2>(kv.first), j = std::get<3>(kv.first);
+      const tmk_box& v = L->patches[p].valid;
+      int ci = i, cj = j, kind;
+      if (d == 0) { kind = i <= v.hi[0] ? 0 : 1; if (kind == 1) ci = i - 1; }
+      else { kind = j <= v.hi[1] ? 2 : 3; if (kind == 3) cj = j - 1; }
+      int owner = -1;
+      for (size_t k = 0; k < items.size(); ++k) {
+        const tmk::MarchItem& m = items[k];
+        if (m.patch == p && ci >= m.x0 && ci < m.x0 + tmk::MARCH_COLS && cj >= m.y0 && cj <= m.y1) { owner = (int)k; break; }
+      }
+      if (owner < 0) return TMK_ERR_BAD_DESC;
+      per[owner].push_back(make_int4(cj, kind, ci - items[owner].x0 + 3, kv.second));
+    }
+    std::vector<int4> caps;
+    for (size_t k = 0; k < items.size(); ++k) {
+      std::stable_sort(per[k].begin(), per[k].end(), [](const int4& a, const int4& b) { return a.x < b.x; });
+      items[k].cap0 = (int)caps.size();
+      items[k].ncap = (int)per[k].size();
+      caps.insert(caps.end(), per[k].begin(), per[k].end());
+    }
+    for (tmk::MarchItem& f : L->hfrows[g])
+      for (const tmk::MarchItem& m : items)
+        if (m.patch == f.patch && m.x0 == f.x0 && m.y0 == f.y0) { f.cap0 = m.cap0; f.ncap = m.ncap; break; }
+    L->dmcap[g] = nullptr;
+    if (!caps.empty()) {
+      if (dalloc(&L->dmcap[g], caps.size()) != cudaSuccess) return TMK_ERR_ALLOC;
+      L->cap_allocs.push_back(L->dmcap[g]);
+      TMK_CU(cudaMemcpy(L->dmcap[g], caps.data(), caps.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    }
+    TMK_CU(cudaMemcpy(L->ditems[g], items.data(), items.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
+    if (!L->hfrows[g].empty())
+      TMK_CU(cudaMemcpy(L->dfrows[g], L->hfrows[g].data(), L->hfrows[g].size() * sizeof(tmk::MarchItem),
+                        cudaMemcpyHostToDevice));
+  }
+  L->march = L->march_allowed;
   if (upload_patchdev(L, 0) != TMK_OK) return TMK_ERR_CUDA;
   // slot tables of the links that use this level's captures
   if (L->coarser && L->coarser->nent) {

@@ -53,7 +53,6 @@ extern "C" tmk_status tmk_context_create(const tmk_elastic_params* e, const tmk_
   if (sw && s->fault_law == TMK_FAULT_SW && (sw->num_patches < 0 || sw->num_patches > TMK_SW_MAX_PATCHES))
     return TMK_ERR_BAD_DESC;
   if (s->volume_kernel < TMK_VOLUME_AUTO || s->volume_kernel > TMK_VOLUME_MARCH) return TMK_ERR_BAD_DESC;
-  if (s->volume_kernel == TMK_VOLUME_MARCH && s->plasticity) return TMK_ERR_UNSUPPORTED;
   if (!device_ok()) return TMK_ERR_NO_DEVICE;
   tmk_context* c = new (std::nothrow) tmk_context_s();
   if (!c) return TMK_ERR_ALLOC;
@@ -168,6 +167,8 @@ void make_march_items(std::vector<tmk::MarchItem>& out, std::vector<tmk::MarchIt
         tmk::MarchItem m;
         m.patch = (int)p; m.x0 = x0; m.y0 = y0; m.y1 = std::min(y0 + len - 1, v.hi[1]);
         m.fslot = -1;
+        m.cap0 = 0;
+        m.ncap = 0;
         if (fault[p] && y0 == v.lo[1]) {       // row 0 waits for the fault kernel: finished later
           m.fslot = (int)fault_rows.size();
           fault_rows.push_back(m);
@@ -185,11 +186,7 @@ void make_march_items(std::vector<tmk::MarchItem>& out, std::vector<tmk::MarchIt
 constexpr int kFaultWaitRows = 0;
 constexpr int kFaultDisplace = 1;
 
-bool uses_march(const tmk_scheme& s) {
-  if (s.volume_kernel == TMK_VOLUME_MARCH) return true;
-  if (s.volume_kernel == TMK_VOLUME_TILE) return false;
-  return !s.plasticity;
-}
+bool uses_march(const tmk_scheme& s) { return s.volume_kernel != TMK_VOLUME_TILE; }
 
 }  // namespace
 
@@ -448,6 +445,8 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
       make_march_items(items, frows, std::vector<tmk_box>(boxes, boxes + npatch), fault_flags, slots,
                        g == 0 && fault_ctas ? kFaultWaitRows : 0);
       L->nitems[g] = (int)items.size();
+      L->hitems[g] = items;
+      L->hfrows[g] = frows;
       if (dalloc(&L->ditems[g], items.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
       L->allocs.push_back(L->ditems[g]);
       TMK_CU(cudaMemcpy(L->ditems[g], items.data(), items.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
@@ -566,6 +565,8 @@ tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEve
   mc.load(c->hp, dt, L->dx);
   mc.stash[0] = L->stash[0];
   mc.stash[1] = L->stash[1];
+  mc.caps[0] = L->dmcap[0];
+  mc.caps[1] = L->dmcap[1];
   if (ev) {
     TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, false, s));
     TMK_CU(cudaEventRecord(ev[2], s));
@@ -577,6 +578,7 @@ tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEve
     TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, true, s));
   }
   TMK_CU(tmk::Launch<Real>::march_fault_rows(pd, L->dfrows[0], L->nfrows[0], L->dfrows[1], L->nfrows[1], mc, s));
+  if (c->scheme.plasticity) TMK_CU(tmk::Launch<Real>::plastic(pd, L->dtiles, L->ntiles, c->dp, s));
   return TMK_OK;
 }
 
@@ -652,7 +654,8 @@ extern "C" tmk_status tmk_level_profile_read(tmk_level* L, double out[4], int* n
 
 extern "C" int tmk_level_launches_per_step(const tmk_level* L) {
   if (!L) return 0;
-  const int vol = L->march ? (L->nitems[0] ? 1 : 0) + (L->nitems[1] ? 1 : 0) + (L->nfrows[0] + L->nfrows[1] ? 1 : 0)
+  const int vol = L->march ? (L->nitems[0] ? 1 : 0) + (L->nitems[1] ? 1 : 0) + (L->nfrows[0] + L->nfrows[1] ? 1 : 0) +
+                               (L->ctx->scheme.plasticity && L->ntiles ? 1 : 0)
                            : (L->ntiles ? 1 : 0);
   return (L->ncopies ? 1 : 0) + (L->nbcopies ? 1 : 0) + (L->nfault ? 1 : 0) + vol + amr_launches(L);
 }

@@ -80,6 +80,8 @@ struct tmk_level_s {
   int nitems[2] = {0, 0};
   tmk::MarchItem* dfrows[2] = {nullptr, nullptr};   // their fault-row items (row 0 finished after the fault kernel)
   int nfrows[2] = {0, 0};
+  std::vector<tmk::MarchItem> hitems[2], hfrows[2];  // host copies (capture ranges rewritten by the AMR links)
+  int4* dmcap[2] = {nullptr, nullptr};              // coarse-fine faces the marching items store
   void* stash[2] = {nullptr, nullptr};              // row-0 intermediates of those items
   int* dfault = nullptr;
   int nfault = 0, max_faces = 0;

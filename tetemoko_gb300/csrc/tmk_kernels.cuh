@@ -478,6 +478,40 @@ __global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __rest
   }
 }
 
+// =============================================================== plasticity
+// PLASTICCORRECTION (srcLinElast/PlasticPhysicsF.ChF:30-69) over the valid
+// cells of a level after the marching kernels wrote the updated stresses:
+// one thread per cell of a tile, both sides.  lambda and gamma are read from
+// the step's input buffer (the volume update leaves them unchanged) and both
+// are written to the output buffer.
+template <typename Real>
+__global__ void __launch_bounds__(256) plastic_tiles_kernel(const PatchDev<Real>* __restrict__ patches,
+                                                            const TileDev* __restrict__ tiles,
+                                                            const DevParams* __restrict__ params) {
+  using T = Real;
+  const TileDev tl = tiles[blockIdx.x];
+  const PatchDev<Real>& p = patches[tl.patch];
+  const DevParams& P = params[p.scen];
+  const T dt = (T)p.dt;
+  for (int idx = threadIdx.x; idx < tl.nx * tl.ny; idx += blockDim.x) {
+    const int x = tl.x0 + idx % tl.nx, y = tl.y0 + idx / tl.nx;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int O = 11 * s;
+      T u[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) u[c] = p.Uout[fab_idx(p, O + 3 + c, x, y)];
+      T lam = p.Uin[fab_idx(p, O + 9, x, y)];
+      T gam = p.Uin[fab_idx(p, O + 10, x, y)];
+      plastic_flow<T>(P, u[0], u[1], u[2], u[3], u[4], u[5], lam, gam, dt);
+#pragma unroll
+      for (int c = 0; c < 6; ++c) p.Uout[fab_idx(p, O + 3 + c, x, y)] = u[c];
+      p.Uout[fab_idx(p, O + 9, x, y)] = lam;
+      p.Uout[fab_idx(p, O + 10, x, y)] = gam;
+    }
+  }
+}
+
 // =============================================================== exchange
 // Copy `ncomp` planes (first component c0) of box [lo, hi] from src to dst.
 struct CopyDev { int src, dst; int lo0, lo1, hi0, hi1; };

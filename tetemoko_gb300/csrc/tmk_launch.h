@@ -22,6 +22,9 @@ struct Launch {
   // one CTA per (tile, side)
   static cudaError_t volume(const PatchDev<Real>* patches, const TileDev* tiles, int ntiles,
                             const DevParams* params, cudaStream_t s);
+  // plastic correction of every tile's cells after the marching kernels
+  static cudaError_t plastic(const PatchDev<Real>* patches, const TileDev* tiles, int ntiles,
+                             const DevParams* params, cudaStream_t s);
   // same-level ghost exchange of components [c0, c0+ncomp) into the input buffers
   static cudaError_t exchange(const PatchDev<Real>* patches, const CopyDev* copies, int ncopies, int c0,
                               int ncomp, cudaStream_t s);

@@ -39,6 +39,12 @@ struct LaunchImpl {
     volume_kernel<Real, TX_, TY_, NT_><<<grid, NT_, sm, s>>>(patches, tiles, params);
     return cudaGetLastError();
   }
+  static cudaError_t plastic(const PatchDev<Real>* patches, const TileDev* tiles, int ntiles,
+                             const DevParams* params, cudaStream_t s) {
+    if (ntiles <= 0) return cudaSuccess;
+    plastic_tiles_kernel<Real><<<ntiles, 256, 0, s>>>(patches, tiles, params);
+    return cudaGetLastError();
+  }
   static cudaError_t exchange(const PatchDev<Real>* patches, const CopyDev* copies, int ncopies, int c0,
                               int ncomp, cudaStream_t s) {
     if (ncopies <= 0) return cudaSuccess;
@@ -123,6 +129,10 @@ struct LaunchImpl {
     return LaunchImpl<REAL, TXV, TYV, NTV>::exchange(p, c, n, c0, nc, s);                                    \
   }                                                                                                          \
   template <> size_t Launch<REAL>::volume_smem() { return LaunchImpl<REAL, TXV, TYV, NTV>::smem(); }         \
+  template <> cudaError_t Launch<REAL>::plastic(const PatchDev<REAL>* p, const TileDev* tl, int nt,         \
+                                                const DevParams* prm, cudaStream_t s) {                     \
+    return LaunchImpl<REAL, TXV, TYV, NTV>::plastic(p, tl, nt, prm, s);                                      \
+  }                                                                                                          \
   template <> cudaError_t Launch<REAL>::march(int g, const PatchDev<REAL>* p, const MarchItem* it, int n,    \
                                               const MarchConst<REAL>& mc, bool pdl, cudaStream_t s) {      \
     return LaunchImpl<REAL, TXV, TYV, NTV>::march(g, p, it, n, mc, pdl, s);                                  \

@@ -131,6 +131,7 @@ struct MarchConst {
   int plim, clim, lim, ppm;
   int xout_lo, xout_hi, yout_lo, yout_hi;
   void* stash[2];    // row-0 intermediates of the fault-row items, per component group
+  const int4* caps[2];   // coarse-fine faces each group's items store (row, kind, lane, slot)
   TMK_HD void load(const DevParams& p, double dt, double dx) {
     const double dtdx = dt / dx;
     kx.load(p, 0, dtdx, -(1.0 / 2.0) * dt / dx);
@@ -360,7 +361,8 @@ TMK_D void adw2(const MK<T>& k, const typename PairOf<T>::P* h, const typename P
 // marks the first item of a strip on the fault row: its row 0 needs the fault
 // kernel's results, so the kernel leaves that row to march_fault_row_kernel
 // and keeps what it needs in stash slot fslot.
-struct MarchItem { int patch, x0, y0, y1, fslot; };
+// [cap0, cap0+ncap) are the item's entries in its group's capture list.
+struct MarchItem { int patch, x0, y0, y1, fslot, cap0, ncap; };
 // vectors a fault-row item keeps for its row 0 (x states, first-pass y face 1,
 // final y flux 1, old state)
 constexpr int MARCH_STASH_VECS = 5;
@@ -390,6 +392,34 @@ template <typename T> TMK_D void cp_async_elem(T* dst_smem, const T* src) {
 }
 TMK_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 TMK_D void cp_async_wait_all_but_newest() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Fluxes of the coarse-fine faces of row `row` that this item owns, into the
+// level's flux-register capture buffer (flux registers of the AMR coupling).
+// Entry kinds: 0 the x face below the lane's column, 1 the one above, 2 the
+// y face below the row, 3 the one above; entries are sorted by row and the
+// loop is uniform over the warp.
+template <typename T, int G>
+TMK_D void march_capture(const PatchDev<T>& pp, const MarchItem& it, const MarchConst<T>& mc, int row, int lane,
+                         const typename PairOf<T>::P* Fx, const typename PairOf<T>::P* Fxh,
+                         const typename PairOf<T>::P* Fylo, const typename PairOf<T>::P* Fyhi, int& cpos) {
+  using P = typename PairOf<T>::P;
+  constexpr int N = Grp<G>::N;
+  const int4* caps = mc.caps[G];
+  const int cend = it.cap0 + it.ncap;
+  while (cpos < cend) {
+    const int4 e = caps[cpos];
+    if (e.x > row) break;
+    ++cpos;
+    if (e.x < row || e.z != lane) continue;   // rows left to the fault-row kernel, other lanes
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      const P v = e.y == 0 ? Fx[c] : e.y == 1 ? Fxh[c] : e.y == 2 ? Fylo[c] : Fyhi[c];
+      const int g = Grp<G>::glob(c);
+      pp.cap[(size_t)e.w * 22 + g] = (double)v.x;
+      pp.cap[(size_t)e.w * 22 + 11 + g] = (double)v.y;
+    }
+  }
+}
 
 template <typename T, int G>
 __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) march_kernel(const PatchDev<T>* __restrict__ patches,
@@ -497,6 +527,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
 
   const int q_s = max(it.y0 - 1, dlo1);
   const int q_e = it.y1 + 1;
+  int cpos = it.cap0;                     // next coarse-fine face to store
   // rolling window of rows q, q+1, q+2 (ring slots); sy0 = slope(q); Fy0 = lo-face value of row q
   P sy0[N], Fy0[N];
   {
@@ -653,6 +684,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
           pp.Uout[o + (size_t)(11 + gg) * plane] = u.y;
         }
       }
+      if (it.ncap && yr <= it.y1) march_capture<T, G>(pp, it, mc, yr, lane, Fx, Fxh, Fy_p, Fy, cpos);
     }
     // advance the window
     cput(kWMx, WMx);
@@ -710,6 +742,10 @@ TMK_D void fault_row_finish(const PatchDev<T>& pp, const MarchItem& it, const Ma
   flux2<G, 0, T>(mc.kx, g, Fx);
 #pragma unroll
   for (int c = 0; c < N; ++c) Fxh[c] = shfl_dn2(Fx[c], 1);
+  if (it.ncap) {
+    int cpos = it.cap0;
+    march_capture<T, G>(pp, it, mc, dlo1, lane, Fx, Fxh, Fy0, Fy1, cpos);
+  }
   const bool col_valid = x >= it.x0 && x < it.x0 + MARCH_COLS && x >= pp.vlo0 && x <= pp.vhi0;
   if (col_valid) {
     const size_t plane = (size_t)pp.anx * pp.any;
