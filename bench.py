@@ -376,6 +376,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--amr-steps", type=int, default=16)   # timed coarse steps of the AMR measurement
+    ap.add_argument("--amr-only", action="store_true")      # only the AMR measurement (profiling runs)
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     args = ap.parse_args()
@@ -460,6 +461,11 @@ def main():
     # ---- mixed form (headline): an uninstrumented timed pass for the value, then
     # a second timed pass with CUDA events around every launch for the roofline
     # (events between the fault and volume kernels serialise their overlap)
+    if args.amr_only:
+        amr = amr_measurement(args.amr_steps, args.warmup, stream)
+        if rank == 0:
+            print(json.dumps({"amr": amr}), flush=True)
+        return 0
     sc, ctx, lvl = make_level(A.TMK_PREC_MIXED)
     # steps replayed from a CUDA graph of graph_steps recorded steps (the
     # largest even divisor of --steps up to 100); also timed call by call

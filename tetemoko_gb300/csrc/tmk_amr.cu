@@ -18,6 +18,8 @@
 //   * regrid prolongation (Chombo FineInterp; srcLinElast/D1FineInterp.cpp).
 // Every list is laid out so that one thread owns one (item, component) and
 // writes distinct addresses: no atomics, results independent of scheduling.
+// Threads run component-major (neighbouring threads take neighbouring items
+// of one component plane), so their state accesses coalesce along x.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
@@ -61,26 +63,32 @@ tmk_box coarsen(const tmk_box& b, int r) {
 }
 
 // ------------------------------------------------------------- device code
-__device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
+// The state transfers compute in the state's own type R (FP32 in the mixed
+// form: GB300's FP64 rate would dominate these bulk passes; FP64 in the plain
+// form, where they match the oracle to rounding).  Fault rows stay FP64.
+template <typename R> __device__ __forceinline__ R dmin(R a, R b) { return (b < a) ? b : a; }
+template <typename R> __device__ __forceinline__ R dmax(R a, R b) { return (a < b) ? b : a; }
 
 // new*a + old*(1-a); exact copies at a = 1 and a = 0
-__device__ __forceinline__ double tinterp(double o, double n, double a) {
-  if (a == 1.0) return n;
-  if (a == 0.0) return o;
-  double v = n * a;
-  double t = o * (1.0 - a);
+template <typename R>
+__device__ __forceinline__ R tinterp(R o, R n, R a) {
+  if (a == R(1)) return n;
+  if (a == R(0)) return o;
+  R v = n * a;
+  R t = o * (R(1) - a);
   return v + t;
 }
 
-__device__ __forceinline__ double slope(int kind, double um, double u0, double up) {
-  return kind == SL_CENTRED ? 0.5 * (up - um) : kind == SL_LO ? u0 - um : kind == SL_HI ? up - u0 : 0.0;
+template <typename R>
+__device__ __forceinline__ R slope(int kind, R um, R u0, R up) {
+  return kind == SL_CENTRED ? R(0.5) * (up - um) : kind == SL_LO ? u0 - um : kind == SL_HI ? up - u0 : R(0);
 }
 
-__device__ __forceinline__ void limit2(double& sx, double& sy, double u, double mn, double mx) {
-  double dm = 0.5 * (fabs(sx) + fabs(sy));
-  double th = 1.0;
-  if (dm > 0.0) {
+template <typename R>
+__device__ __forceinline__ void limit2(R& sx, R& sy, R u, R mn, R mx) {
+  R dm = R(0.5) * (fabs(sx) + fabs(sy));
+  R th = R(1);
+  if (dm > R(0)) {
     th = dmin(th, (mx - u) / dm);
     th = dmin(th, (u - mn) / dm);
   }
@@ -91,48 +99,50 @@ __device__ __forceinline__ void limit2(double& sx, double& sy, double u, double 
 __device__ __forceinline__ double icoef(int f, int c, int r) { return -0.5 + ((double)(f - r * c) + 0.5) / (double)r; }
 
 template <typename Real>
-__device__ __forceinline__ double uval(const PatchDev<Real>& P, int c, int i, int j, double a, bool interp) {
+__device__ __forceinline__ Real uval(const PatchDev<Real>& P, int c, int i, int j, Real a) {
   const size_t o = fab_idx(P, c, i, j);
-  const double n = (double)P.Uin[o];
-  if (!interp || a == 1.0) return n;
-  return tinterp((double)P.Uout[o], n, a);
+  const Real n = P.Uin[o];
+  if (a == Real(1)) return n;
+  return tinterp(P.Uout[o], n, a);
 }
 
 __device__ __forceinline__ double bval(const double* B, int blo, int bnx, int c, int i) {
   return B[(size_t)c * bnx + (i - blo)];
 }
 
-// coarse sites: time-interpolated value and limited slopes, 3 doubles per (site, comp)
+// coarse sites: time-interpolated value and limited slopes, 3 values per
+// (site, comp) in the state's type, 2 doubles per (fault site, comp)
 template <typename Real>
 __global__ void cf_sites_kernel(const PatchDev<Real>* __restrict__ cp, const SiteU* __restrict__ su, int nsu,
                                 const SiteB* __restrict__ sb, int nsb, int nb, double a,
-                                double* __restrict__ svu, double* __restrict__ svb) {
+                                Real* __restrict__ svu, double* __restrict__ svb) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < nsu * NC) {
-    const SiteU s = su[t / NC];
-    const int c = t % NC;
-    double v[9];
+  if (t < nsu * NC) {                      // component-major: neighbouring threads, neighbouring sites
+    const SiteU s = su[t % nsu];
+    const int c = t / nsu;
+    const Real ar = (Real)a;
+    Real v[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k)
-      v[k] = s.nb[k] >= 0 ? uval(cp[s.nb[k]], c, s.ci + k % 3 - 1, s.cj + k / 3 - 1, a, true) : 0.0;
-    const double u0 = v[4];
-    double sx = slope(s.kx, v[3], u0, v[5]);
-    double sy = slope(s.ky, v[1], u0, v[7]);
+      v[k] = s.nb[k] >= 0 ? uval(cp[s.nb[k]], c, s.ci + k % 3 - 1, s.cj + k / 3 - 1, ar) : Real(0);
+    const Real u0 = v[4];
+    Real sx = slope(s.kx, v[3], u0, v[5]);
+    Real sy = slope(s.ky, v[1], u0, v[7]);
     if (s.lim) {
-      double mn = u0, mx = u0;
+      Real mn = u0, mx = u0;
 #pragma unroll
       for (int k = 0; k < 9; ++k)
         if (s.nb[k] >= 0) { mn = dmin(mn, v[k]); mx = dmax(mx, v[k]); }
       limit2(sx, sy, u0, mn, mx);
     }
-    double* o = svu + (size_t)t * 3;
+    Real* o = svu + ((size_t)(t % nsu) * NC + c) * 3;
     o[0] = u0; o[1] = sx; o[2] = sy;
     return;
   }
   t -= nsu * NC;
   if (t < nsb * nb) {
-    const SiteB s = sb[t / nb];
-    const int c = t % nb;
+    const SiteB s = sb[t % nsb];
+    const int c = t / nsb;
     double v[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -141,11 +151,11 @@ __global__ void cf_sites_kernel(const PatchDev<Real>* __restrict__ cp, const Sit
       const PatchDev<Real>& P = cp[s.nb[k]];
       const int i = s.ci + k - 1;
       const double n = bval(P.B, P.blo0, P.bnx, c, i);
-      v[k] = a == 1.0 ? n : tinterp(bval(P.Bold, P.blo0, P.bnx, c, i), n, a);
+      v[k] = a == 1.0 ? n : tinterp<double>(bval(P.Bold, P.blo0, P.bnx, c, i), n, a);
     }
-    double* o = svb + (size_t)t * 2;
+    double* o = svb + ((size_t)(t % nsb) * nb + c) * 2;
     o[0] = v[1];
-    o[1] = slope(s.kind, v[0], v[1], v[2]);
+    o[1] = slope<double>(s.kind, v[0], v[1], v[2]);
   }
 }
 
@@ -153,23 +163,23 @@ __global__ void cf_sites_kernel(const PatchDev<Real>* __restrict__ cp, const Sit
 template <typename Real>
 __global__ void cf_apply_kernel(const PatchDev<Real>* __restrict__ fp, const FineU* __restrict__ fu, int nfu,
                                 const FineB* __restrict__ fb, int nfb, int nb,
-                                const double* __restrict__ svu, const double* __restrict__ svb) {
+                                const Real* __restrict__ svu, const double* __restrict__ svb) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < nfu * NC) {
-    const FineU e = fu[t / NC];
-    const int c = t % NC;
-    const double* s = svu + ((size_t)e.site * NC + c) * 3;
-    double v = s[0];
-    v = v + e.cx * s[1];
-    v = v + e.cy * s[2];
+    const FineU e = fu[t % nfu];
+    const int c = t / nfu;
+    const Real* s = svu + ((size_t)e.site * NC + c) * 3;
+    Real v = s[0];
+    v = v + (Real)e.cx * s[1];
+    v = v + (Real)e.cy * s[2];
     const PatchDev<Real>& P = fp[e.fpatch];
-    ((Real*)P.Uin)[fab_idx(P, c, e.i, e.j)] = (Real)v;
+    ((Real*)P.Uin)[fab_idx(P, c, e.i, e.j)] = v;
     return;
   }
   t -= nfu * NC;
   if (t < nfb * nb) {
-    const FineB e = fb[t / nb];
-    const int c = t % nb;
+    const FineB e = fb[t % nfb];
+    const int c = t / nfb;
     const double* s = svb + ((size_t)e.site * nb + c) * 2;
     double v = s[0];
     v = v + e.cx * s[1];
@@ -213,8 +223,8 @@ __global__ void reflux_kernel(const PatchDev<Real>* __restrict__ cp, const Reflu
                               const double* __restrict__ R) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ncells * NC) return;
-  const RefluxCell cl = cells[t / NC];
-  const int c = t % NC;
+  const RefluxCell cl = cells[t % ncells];
+  const int c = t / ncells;
   const PatchDev<Real>& P = cp[cl.cpatch];
   Real* U = (Real*)P.Uin;
   const size_t o = fab_idx(P, c, cl.ci, cl.cj);
@@ -232,16 +242,16 @@ __global__ void avgdown_kernel(const PatchDev<Real>* __restrict__ cp, const Patc
                                const AvgU* __restrict__ au, int nau, const AvgB* __restrict__ ab, int nab, int nb,
                                int r, double sU, double sB, int both) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < nau * NC) {
-    const AvgU e = au[t / NC];
-    const int c = t % NC;
+  if (t < nau * NC) {                      // component-major: neighbouring threads, neighbouring cells
+    const AvgU e = au[t % nau];
+    const int c = t / nau;
     const PatchDev<Real>& F = fp[e.fpatch];
-    double sum = 0.0;
+    Real sum = Real(0);
     for (int jj = 0; jj < r; ++jj)
-      for (int ii = 0; ii < r; ++ii) sum = sum + (double)F.Uin[fab_idx(F, c, r * e.ci + ii, r * e.cj + jj)];
+      for (int ii = 0; ii < r; ++ii) sum = sum + F.Uin[fab_idx(F, c, r * e.ci + ii, r * e.cj + jj)];
     const PatchDev<Real>& C = cp[e.cpatch];
     const size_t o = fab_idx(C, c, e.ci, e.cj);
-    const Real v = (Real)(sum * sU);
+    const Real v = sum * (Real)sU;
     ((Real*)C.Uin)[o] = v;
     // lambda, gamma: a step without plasticity never rewrites them, keep both buffers equal
     if (both && (c == 9 || c == 10 || c == 20 || c == 21)) C.Uout[o] = v;
@@ -249,8 +259,8 @@ __global__ void avgdown_kernel(const PatchDev<Real>* __restrict__ cp, const Patc
   }
   t -= nau * NC;
   if (t < nab * nb) {
-    const AvgB e = ab[t / nb];
-    const int c = t % nb;
+    const AvgB e = ab[t % nab];
+    const int c = t / nab;
     const PatchDev<Real>& F = fp[e.fpatch];
     double sum = 0.0;
     for (int ii = 0; ii < r; ++ii) sum = sum + bval(F.B, F.blo0, F.bnx, c, r * e.ci + ii);
@@ -266,8 +276,8 @@ __global__ void finterp_kernel(const PatchDev<Real>* __restrict__ cp, const Patc
                                int nb, int r) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < niu * NC) {
-    const InterpU e = iu[t / NC];
-    const int c = t % NC;
+    const InterpU e = iu[t % niu];
+    const int c = t / niu;
     double v[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k)
@@ -298,8 +308,8 @@ __global__ void finterp_kernel(const PatchDev<Real>* __restrict__ cp, const Patc
   }
   t -= niu * NC;
   if (t < nib * nb) {
-    const InterpB e = ib[t / nb];
-    const int c = t % nb;
+    const InterpB e = ib[t % nib];
+    const int c = t / nib;
     double v[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -763,10 +773,10 @@ tmk_status launch_fill(CFLink* k, double alpha, cudaStream_t s) {
   const PatchDev<Real>* cp = (const PatchDev<Real>*)k->C->dpatch[k->C->parity];
   const PatchDev<Real>* fp = (const PatchDev<Real>*)k->F->dpatch[k->F->parity];
   cf_sites_kernel<Real><<<blocks_for(ns, 128), 128, 0, s>>>(cp, k->dsu, k->nsu, k->dsb, k->nsb, nb, alpha,
-                                                             k->dsvu, k->dsvb);
+                                                             (Real*)k->dsvu, k->dsvb);
   TMK_CU(cudaGetLastError());
-  cf_apply_kernel<Real><<<blocks_for(nf, 128), 128, 0, s>>>(fp, k->dfu, k->nfu, k->dfb, k->nfb, nb, k->dsvu,
-                                                             k->dsvb);
+  cf_apply_kernel<Real><<<blocks_for(nf, 128), 128, 0, s>>>(fp, k->dfu, k->nfu, k->dfb, k->nfb, nb,
+                                                             (const Real*)k->dsvu, k->dsvb);
   TMK_CU(cudaGetLastError());
   return TMK_OK;
 }

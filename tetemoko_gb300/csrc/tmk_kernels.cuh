@@ -525,7 +525,8 @@ __global__ void exchange_kernel(const PatchDev<Real>* __restrict__ patches, cons
   const int nx = cp.hi0 - cp.lo0 + 1, ny = cp.hi1 - cp.lo1 + 1;
   const Real* src = to_in ? ps.Uout : ps.Uin;
   Real* dst = to_in ? (Real*)pd.Uout : (Real*)pd.Uin;
-  for (int idx = threadIdx.x; idx < ncomp * nx * ny; idx += blockDim.x) {
+  // a copy box is spread over gridDim.y CTAs (more loads in flight)
+  for (int idx = threadIdx.x + blockIdx.y * blockDim.x; idx < ncomp * nx * ny; idx += blockDim.x * gridDim.y) {
     int c = c0 + idx / (nx * ny), j = cp.lo1 + (idx / nx) % ny, i = cp.lo0 + idx % nx;
     dst[fab_idx(pd, c, i, j)] = src[fab_idx(ps, c, i, j)];
   }

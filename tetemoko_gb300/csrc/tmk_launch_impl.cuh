@@ -48,7 +48,7 @@ struct LaunchImpl {
   static cudaError_t exchange(const PatchDev<Real>* patches, const CopyDev* copies, int ncopies, int c0,
                               int ncomp, cudaStream_t s) {
     if (ncopies <= 0) return cudaSuccess;
-    exchange_kernel<Real><<<ncopies, 256, 0, s>>>(patches, copies, c0, ncomp, 0);
+    exchange_kernel<Real><<<dim3(ncopies, 8), 256, 0, s>>>(patches, copies, c0, ncomp, 0);
     return cudaGetLastError();
   }
   static cudaError_t march(int g, const PatchDev<Real>* patches, const MarchItem* items, int nitems,
