@@ -314,6 +314,66 @@ def amr_measurement(steps, warmup, stream):
     return out
 
 
+ENSEMBLE_SIZE = 64
+
+
+def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE):
+    """64 independent rate-and-state scenarios (seeded friction, lognormal shear
+    prestress, grids drawn from 256x128 / 512x256 / 1024x512) stepped as one
+    level in the mixed form; steps replayed from a CUDA graph.  Returns the JSON
+    object of the measurement."""
+    import torch
+    from tetemoko_gb300 import _capi as A, scenarios as S
+    from tetemoko_gb300.level import Context, LinElastEnsemble
+    members = [S.ensemble_member(k, precision=A.TMK_PREC_MIXED) for k in range(nscen)]
+    ctxs = [Context(sc) for sc, _ in members]
+    doms = [(0, 0, sc.nx - 1, sc.ny - 1) for sc, _ in members]
+    ens = LinElastEnsemble(ctxs, doms, [tile_boxes(0, 0, sc.nx - 1, sc.ny - 1, 128) for sc, _ in members])
+    for k, (sc, tau0) in enumerate(members):
+        U, B = S.prestressed_state(sc, tau0)
+        ens.set_scenario(k, U, B)
+    dt = members[0][0].dt()
+    t = 0.0
+    for _ in range(warmup):
+        ens.step(t, dt, stream)
+        t += dt
+    gsteps = 20
+    graph = ens.graph(gsteps, t, dt)
+    graph.launch(t, stream)
+    t += gsteps * dt
+    torch.cuda.synchronize()
+    nrep = max(1, steps // gsteps)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(nrep):
+        graph.launch(t, stream)
+        t += gsteps * dt
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    cells = ens.cells()
+    grids = {}
+    for sc, _ in members:
+        grids[f"{sc.nx}x{sc.ny}"] = grids.get(f"{sc.nx}x{sc.ny}", 0) + 1
+    out = {"value": cells * gsteps * nrep / (ms * 1e-3), "unit": "cell-updates/s",
+           "ms_per_step": ms / (gsteps * nrep), "steps": gsteps * nrep, "scenarios": nscen,
+           "cells": cells, "patches": len(ens.boxes), "grids": grids,
+           "launches_per_step": ens.launches_per_step(),
+           "config": "rate-and-state aging law, a ~ U[0.006,0.012], b-a ~ U[0.002,0.006], L ~ U[0.01,0.05] m "
+                     "(seed 5000+k), shear prestress 70 exp(g - s^2/2) MPa with g Gaussian, exponential "
+                     "covariance, 1 km correlation, s = 0.1 (seed 6000+k), dx = 0.1 km, FP32 volume / FP64 "
+                     "fault, patches of at most 128x128, one level of all scenarios",
+           "execution": f"CUDA graph of {gsteps} ensemble steps (tmk_ensemble_create + tmk_level_graph_create), "
+                        "replayed",
+           "device_status": ens.status()[1]}
+    graph.close()
+    ens.close()
+    for c in ctxs:
+        c.close()
+    return out
+
+
 def host_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -377,6 +437,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--amr-steps", type=int, default=16)   # timed coarse steps of the AMR measurement
     ap.add_argument("--amr-only", action="store_true")      # only the AMR measurement (profiling runs)
+    ap.add_argument("--ensemble-steps", type=int, default=200)   # timed steps of the ensemble measurement
+    ap.add_argument("--ensemble-only", action="store_true")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     args = ap.parse_args()
@@ -466,6 +528,11 @@ def main():
         if rank == 0:
             print(json.dumps({"amr": amr}), flush=True)
         return 0
+    if args.ensemble_only:
+        ens = ensemble_measurement(args.ensemble_steps, args.warmup, stream)
+        if rank == 0:
+            print(json.dumps({"ensemble": ens}), flush=True)
+        return 0
     sc, ctx, lvl = make_level(A.TMK_PREC_MIXED)
     # steps replayed from a CUDA graph of graph_steps recorded steps (the
     # largest even divisor of --steps up to 100); also timed call by call
@@ -547,6 +614,8 @@ def main():
 
     # ---- subcycled 4-level AMR hierarchy (rank 0 reports its own)
     amr = amr_measurement(args.amr_steps, 2, stream) if args.amr_steps > 0 else None
+    # ---- ensemble of 64 independent scenarios in one level
+    ens = ensemble_measurement(args.ensemble_steps, 3, stream) if args.ensemble_steps > 0 else None
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
@@ -576,6 +645,7 @@ def main():
                            "volume_hbm_gbs": BYTES_PER_CELL_FP64 * cells / (vol64 * 1e-3) / 1e9},
             "mixed_over_fp64": value / value64,
             "amr": amr,
+            "ensemble": ens,
             "device_status": {"mixed": st[1], "fp64": st64[1]},
         }
         print(json.dumps(line), flush=True)

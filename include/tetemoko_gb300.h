@@ -213,6 +213,19 @@ tmk_status tmk_max_wave_speed(const tmk_context* ctx, double* speed);
 tmk_status tmk_level_create(tmk_context* ctx, const tmk_box* domain, double dx,
                             int npatch, const tmk_box* patches, tmk_level** out);
 void       tmk_level_destroy(tmk_level* lvl);
+/* Ensemble of independent scenarios stepped as one level (an extension: the
+ * reference runs one scenario per process with its parameters in COMMON
+ * blocks, srcLinElast/LinElastPhysicsF.ChF:1149-1210, ibcLinElast/RSIBCF.ChF:8-55).
+ * Scenario k has context ctxs[k] and problem domain domains[k]; patch p covers
+ * boxes[p] of scenario patch_scen[p].  All scenarios share dx and every
+ * parameter but friction (material, background stress, scheme, boundary types,
+ * plasticity): TMK_ERR_UNSUPPORTED otherwise.  Ghost exchange stays within a
+ * scenario; each kernel of a step covers every patch of every scenario.  The
+ * result handle takes every tmk_level_* call except the coarse-fine ones
+ * (TMK_ERR_UNSUPPORTED); the fault status is ctxs[0]'s. */
+tmk_status tmk_ensemble_create(int nscen, tmk_context* const* ctxs, const tmk_box* domains,
+                               double dx, int npatch, const tmk_box* boxes,
+                               const int* patch_scen, tmk_level** out);
 /* Copy one patch's state in / out.  `host` selects host (1) or device (0)
  * pointers.  U covers the valid box grown by TMK_NGHOST, 22 components (FP64);
  * B covers the patch's fault row grown by TMK_NGHOST in x (NULL if none). */

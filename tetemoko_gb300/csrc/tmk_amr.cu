@@ -887,6 +887,7 @@ void amr_release(tmk_level_s* L) {
 // ================================================================= C ABI ===
 extern "C" tmk_status tmk_level_attach_coarser(tmk_level* fine, tmk_level* coarse, int ref_ratio) {
   if (!fine || !coarse || fine == coarse || ref_ratio < 2) return TMK_ERR_BAD_DESC;
+  if (fine->nscen != 1 || coarse->nscen != 1) return TMK_ERR_UNSUPPORTED;   // ensembles step single levels
   if (fine->ctx->nb != coarse->ctx->nb || fine->prec != coarse->prec) return TMK_ERR_BAD_DESC;
   const int r = ref_ratio;
   for (int d = 0; d < 2; ++d)
@@ -947,6 +948,7 @@ extern "C" tmk_status tmk_level_interp_from_coarser(tmk_level* fine, void* strea
 
 extern "C" tmk_status tmk_level_copy_overlap(tmk_level* dst, const tmk_level* src, void* stream) {
   if (!dst || !src || dst == src || dst->prec != src->prec || dst->ctx->nb != src->ctx->nb) return TMK_ERR_BAD_DESC;
+  if (dst->nscen != 1 || src->nscen != 1) return TMK_ERR_UNSUPPORTED;
   for (int d = 0; d < 2; ++d)
     if (dst->domain.lo[d] != src->domain.lo[d] || dst->domain.hi[d] != src->domain.hi[d]) return TMK_ERR_BAD_DESC;
   std::vector<CopyDev> cu, cb;

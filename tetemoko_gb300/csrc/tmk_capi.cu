@@ -297,8 +297,8 @@ void fill_patchdev(tmk_level_s* L, int parity) {
     d.alo0 = lp.alloc.lo[0]; d.alo1 = lp.alloc.lo[1];
     d.anx = lp.alloc.hi[0] - lp.alloc.lo[0] + 1; d.any = lp.alloc.hi[1] - lp.alloc.lo[1] + 1;
     d.vlo0 = lp.valid.lo[0]; d.vlo1 = lp.valid.lo[1]; d.vhi0 = lp.valid.hi[0]; d.vhi1 = lp.valid.hi[1];
-    d.dlo0 = L->domain.lo[0]; d.dlo1 = L->domain.lo[1]; d.dhi0 = L->domain.hi[0]; d.dhi1 = L->domain.hi[1];
-    d.dx = L->dx; d.dt = L->cur_dt; d.scen = 0;
+    d.dlo0 = lp.domain.lo[0]; d.dlo1 = lp.domain.lo[1]; d.dhi0 = lp.domain.hi[0]; d.dhi1 = lp.domain.hi[1];
+    d.dx = L->dx; d.dt = L->cur_dt; d.scen = lp.scen;
     d.plastic = L->ctx->scheme.plasticity ? 1 : 0;
     d.fault = lp.fault;
     d.B = lp.B; d.blo0 = lp.blo; d.bnx = lp.bnx;
@@ -332,23 +332,29 @@ extern "C" void tmk_level_destroy(tmk_level* L) {
   delete L;
 }
 
-extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, double dx, int npatch,
-                                       const tmk_box* boxes, tmk_level** out) {
-  if (!out) return TMK_ERR_BAD_DESC;
-  *out = nullptr;
-  if (!c || !domain || !boxes || npatch <= 0 || !(dx > 0) || !box_ok(*domain)) return TMK_ERR_BAD_DESC;
-  if (domain->hi[1] - domain->lo[1] < 2) return TMK_ERR_BAD_DESC;   // the fault stencil needs 3 rows
-  // patches must be valid, inside the domain and disjoint
+namespace {
+
+// A level whose patch p covers boxes[p] of domain pdom[p] and belongs to
+// scenario pscen[p] (context ctxs[pscen[p]]): one scenario for a level of the
+// reference, several for an ensemble.
+tmk_status level_create_impl(tmk_context* const* ctxs, int nscen, const tmk_box* pdom, const int* pscen,
+                             double dx, int npatch, const tmk_box* boxes, tmk_level** out) {
+  tmk_context* c = ctxs[0];
+  // patches must be valid, inside their domain and disjoint within a scenario
   for (int p = 0; p < npatch; ++p) {
-    if (!box_ok(boxes[p]) || !box_contains(*domain, boxes[p])) return TMK_ERR_BAD_DESC;
+    if (pscen[p] < 0 || pscen[p] >= nscen) return TMK_ERR_BAD_DESC;
+    if (!box_ok(pdom[p]) || pdom[p].hi[1] - pdom[p].lo[1] < 2) return TMK_ERR_BAD_DESC;  // fault stencil: 3 rows
+    if (!box_ok(boxes[p]) || !box_contains(pdom[p], boxes[p])) return TMK_ERR_BAD_DESC;
     for (int q = 0; q < p; ++q) {
       tmk_box x = box_isect(boxes[p], boxes[q]);
-      if (box_ok(x)) return TMK_ERR_BAD_DESC;
+      if (pscen[q] == pscen[p] && box_ok(x)) return TMK_ERR_BAD_DESC;
     }
   }
   tmk_level_s* L = new (std::nothrow) tmk_level_s();
   if (!L) return TMK_ERR_ALLOC;
-  L->ctx = c; L->domain = *domain; L->dx = dx; L->prec = c->scheme.precision;
+  L->ctx = c; L->domain = pdom[0]; L->dx = dx; L->prec = c->scheme.precision;
+  L->nscen = nscen;
+  L->dparams = c->dp;
   L->patches.resize(npatch);
   const size_t rs = real_size(L->prec);
   const int nb = c->nb;
@@ -358,9 +364,17 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
   const int TY = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::TY : tmk::Launch<double>::TY;
   auto fail = [&](tmk_status st) { tmk_level_destroy(L); return st; };
   size_t max_count = 0;
+  if (nscen > 1) {
+    if (dalloc(&L->dparams, (size_t)nscen) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+    L->allocs.push_back(L->dparams);
+    for (int k = 0; k < nscen; ++k)
+      TMK_CU(cudaMemcpy(L->dparams + k, &ctxs[k]->hp, sizeof(DevParams), cudaMemcpyHostToDevice));
+  }
   for (int p = 0; p < npatch; ++p) {
     LevelPatch& lp = L->patches[p];
     lp.valid = boxes[p];
+    lp.domain = pdom[p];
+    lp.scen = pscen[p];
     lp.alloc = box_grow(boxes[p], TMK_NGHOST);
     const int anx = lp.alloc.hi[0] - lp.alloc.lo[0] + 1, any = lp.alloc.hi[1] - lp.alloc.lo[1] + 1;
     const size_t count = (size_t)TMK_NCOMP * anx * any;
@@ -370,7 +384,7 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
       L->allocs.push_back(lp.U[k]);
       if (cudaMemset(lp.U[k], 0, count * rs) != cudaSuccess) return fail(TMK_ERR_CUDA);
     }
-    lp.fault = (c->scheme.fault_law != TMK_FAULT_NONE && boxes[p].lo[1] == domain->lo[1]) ? 1 : 0;
+    lp.fault = (c->scheme.fault_law != TMK_FAULT_NONE && boxes[p].lo[1] == pdom[p].lo[1]) ? 1 : 0;
     if (lp.fault) {
       lp.blo = boxes[p].lo[0] - TMK_NGHOST;
       lp.bnx = boxes[p].hi[0] - boxes[p].lo[0] + 1 + 2 * TMK_NGHOST;
@@ -390,14 +404,14 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
   }
   // fault-row tiles first so that their CTAs start early
   std::stable_sort(tiles.begin(), tiles.end(), [&](const TileDev& a, const TileDev& b) {
-    return (a.y0 == domain->lo[1]) > (b.y0 == domain->lo[1]);
+    return (a.y0 == pdom[a.patch].lo[1]) > (b.y0 == pdom[b.patch].lo[1]);
   });
   // same-level exchange lists: ghost cells of p covered by valid cells of q
   std::vector<CopyDev> copies, bcopies;
   for (int p = 0; p < npatch; ++p)
     for (int q = 0; q < npatch; ++q) {
-      if (p == q) continue;
-      tmk_box g = box_isect(box_isect(L->patches[p].alloc, boxes[q]), *domain);
+      if (p == q || pscen[p] != pscen[q]) continue;
+      tmk_box g = box_isect(box_isect(L->patches[p].alloc, boxes[q]), pdom[p]);
       if (box_ok(g)) {
         CopyDev cd; cd.src = q; cd.dst = p; cd.lo0 = g.lo[0]; cd.lo1 = g.lo[1]; cd.hi0 = g.hi[0]; cd.hi1 = g.hi[1];
         copies.push_back(cd);
@@ -406,7 +420,7 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
         int lo = std::max(L->patches[p].blo, boxes[q].lo[0]);
         int hi = std::min(L->patches[p].blo + L->patches[p].bnx - 1, boxes[q].hi[0]);
         if (lo <= hi) {
-          CopyDev cd; cd.src = q; cd.dst = p; cd.lo0 = lo; cd.hi0 = hi; cd.lo1 = cd.hi1 = domain->lo[1];
+          CopyDev cd; cd.src = q; cd.dst = p; cd.lo0 = lo; cd.hi0 = hi; cd.lo1 = cd.hi1 = pdom[p].lo[1];
           bcopies.push_back(cd);
         }
       }
@@ -497,6 +511,53 @@ extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, do
   return TMK_OK;
 }
 
+// the parameters an ensemble's scenarios must share: everything but friction
+bool same_bulk(const tmk_context* a, const tmk_context* b) {
+  const DevParams &p = a->hp, &q = b->hp;
+  if (p.cs != q.cs || p.cp != q.cp || p.G != q.G || p.rho != q.rho) return false;
+  for (int k = 0; k < 22; ++k) if (p.bg[k] != q.bg[k]) return false;
+  const tmk_scheme &s = a->scheme, &t = b->scheme;
+  if (s.normal_pred_order != t.normal_pred_order || s.use_prim_limiting != t.use_prim_limiting ||
+      s.use_char_limiting != t.use_char_limiting || s.fault_law != t.fault_law || s.plasticity != t.plasticity ||
+      s.precision != t.precision || s.volume_kernel != t.volume_kernel)
+    return false;
+  for (int k = 0; k < 6; ++k) if (s.boundary_type[k] != t.boundary_type[k]) return false;
+  if (s.plasticity && (p.p_mu != q.p_mu || p.p_beta != q.p_beta || p.p_eta != q.p_eta || p.p_b != q.p_b ||
+                       p.p_h != q.p_h))
+    return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" tmk_status tmk_level_create(tmk_context* c, const tmk_box* domain, double dx, int npatch,
+                                       const tmk_box* boxes, tmk_level** out) {
+  if (!out) return TMK_ERR_BAD_DESC;
+  *out = nullptr;
+  if (!c || !domain || !boxes || npatch <= 0 || !(dx > 0) || !box_ok(*domain)) return TMK_ERR_BAD_DESC;
+  std::vector<tmk_box> pdom(npatch, *domain);
+  std::vector<int> pscen(npatch, 0);
+  return level_create_impl(&c, 1, pdom.data(), pscen.data(), dx, npatch, boxes, out);
+}
+
+extern "C" tmk_status tmk_ensemble_create(int nscen, tmk_context* const* ctxs, const tmk_box* domains, double dx,
+                                          int npatch, const tmk_box* boxes, const int* patch_scen,
+                                          tmk_level** out) {
+  if (!out) return TMK_ERR_BAD_DESC;
+  *out = nullptr;
+  if (nscen < 1 || !ctxs || !domains || !boxes || !patch_scen || npatch <= 0 || !(dx > 0)) return TMK_ERR_BAD_DESC;
+  for (int k = 0; k < nscen; ++k) {
+    if (!ctxs[k] || !box_ok(domains[k])) return TMK_ERR_BAD_DESC;
+    if (!same_bulk(ctxs[0], ctxs[k])) return TMK_ERR_UNSUPPORTED;
+  }
+  std::vector<tmk_box> pdom(npatch);
+  for (int p = 0; p < npatch; ++p) {
+    if (patch_scen[p] < 0 || patch_scen[p] >= nscen) return TMK_ERR_BAD_DESC;
+    pdom[p] = domains[patch_scen[p]];
+  }
+  return level_create_impl(ctxs, nscen, pdom.data(), patch_scen, dx, npatch, boxes, out);
+}
+
 extern "C" tmk_status tmk_level_set_patch(tmk_level* L, int p, const double* U, const double* B, int host) {
   if (!L || p < 0 || p >= (int)L->patches.size() || !U) return TMK_ERR_BAD_DESC;
   LevelPatch& lp = L->patches[p];
@@ -556,9 +617,9 @@ tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEve
   TMK_CU(tmk::bexchange(L->dbptr, L->dblo, L->dbnx, L->dbcopies, L->nbcopies, c->nb, s));
   if (ev) TMK_CU(cudaEventRecord(ev[1], s));
   if (!L->march) {
-    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, false, s));
+    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false, s));
     if (ev) TMK_CU(cudaEventRecord(ev[2], s));
-    TMK_CU(tmk::Launch<Real>::volume(pd, L->dtiles, L->ntiles, c->dp, s));
+    TMK_CU(tmk::Launch<Real>::volume(pd, L->dtiles, L->ntiles, L->dparams, s));
     return TMK_OK;
   }
   tmk::MarchConst<Real> mc;
@@ -568,17 +629,17 @@ tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEve
   mc.caps[0] = L->dmcap[0];
   mc.caps[1] = L->dmcap[1];
   if (ev) {
-    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, false, s));
+    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false, s));
     TMK_CU(cudaEventRecord(ev[2], s));
     TMK_CU(tmk::Launch<Real>::march(0, pd, L->ditems[0], L->nitems[0], mc, false, s));
     TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, true, s));
   } else {
     TMK_CU(tmk::Launch<Real>::march(0, pd, L->ditems[0], L->nitems[0], mc, false, s));
-    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, c->dp, time, c->dstatus, true, s));
+    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, true, s));
     TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, true, s));
   }
   TMK_CU(tmk::Launch<Real>::march_fault_rows(pd, L->dfrows[0], L->nfrows[0], L->dfrows[1], L->nfrows[1], mc, s));
-  if (c->scheme.plasticity) TMK_CU(tmk::Launch<Real>::plastic(pd, L->dtiles, L->ntiles, c->dp, s));
+  if (c->scheme.plasticity) TMK_CU(tmk::Launch<Real>::plastic(pd, L->dtiles, L->ntiles, L->dparams, s));
   return TMK_OK;
 }
 

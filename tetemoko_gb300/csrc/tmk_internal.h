@@ -39,6 +39,8 @@ inline size_t real_size(int prec) { return prec == TMK_PREC_MIXED ? sizeof(float
 
 struct LevelPatch {
   tmk_box valid, alloc;
+  tmk_box domain;           // the patch's problem domain (ensembles: its scenario's)
+  int scen = 0;             // scenario of the patch (index into the level's parameters)
   int fault = 0;
   void* U[2] = {nullptr, nullptr};
   double* B = nullptr;
@@ -64,7 +66,9 @@ struct tmk_context_s {
 };
 
 struct tmk_level_s {
-  tmk_context* ctx = nullptr;
+  tmk_context* ctx = nullptr;              // the (first) scenario's context
+  int nscen = 1;                           // scenarios of an ensemble level
+  tmk::DevParams* dparams = nullptr;       // device parameters per scenario (ctx->dp for one)
   tmk_box domain;
   double dx = 0;
   int prec = TMK_PREC_FP64;

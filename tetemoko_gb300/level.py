@@ -143,6 +143,7 @@ class LinElastLevelGodunov:
         A.check(self.lib.tmk_level_create(ctx.h, C.byref(A.box(*self.domain)), self.dx, len(self.boxes), arr,
                                           C.byref(h)), "tmk_level_create")
         self.h = h
+        self.pdomains = [self.domain] * len(self.boxes)
 
     def patch_shapes(self, p):
         b = self.boxes[p]
@@ -152,7 +153,7 @@ class LinElastLevelGodunov:
         return ushape, bshape
 
     def touches_fault(self, p) -> bool:
-        return self.ctx.sc.scheme.fault_law != A.TMK_FAULT_NONE and self.boxes[p][1] == self.domain[1]
+        return self.ctx.sc.scheme.fault_law != A.TMK_FAULT_NONE and self.boxes[p][1] == self.pdomains[p][1]
 
     def set_patch(self, p, U, B=None):
         """U: (22, ny+8, nx+8) float64 over the patch grown by 4 ghosts; numpy
@@ -182,27 +183,35 @@ class LinElastLevelGodunov:
         A.check(self.lib.tmk_level_get_patch(self.h, p, uptr, bptr, 1 if host else 0), "tmk_level_get_patch")
         return U, B
 
-    def set_level(self, Ug: np.ndarray, Bg: np.ndarray | None):
-        """Scatter a domain-wide state (22, ny+8, nx+8) / fault row (nb, nx+8) into the patches."""
+    def _scatter(self, patches, dom, Ug, Bg):
         g = A.TMK_NGHOST
-        for p, b in enumerate(self.boxes):
-            U = np.ascontiguousarray(Ug[:, b[1] - self.domain[1]:b[3] - self.domain[1] + 1 + 2 * g,
-                                        b[0] - self.domain[0]:b[2] - self.domain[0] + 1 + 2 * g])
+        for p in patches:
+            b = self.boxes[p]
+            U = np.ascontiguousarray(Ug[:, b[1] - dom[1]:b[3] - dom[1] + 1 + 2 * g,
+                                        b[0] - dom[0]:b[2] - dom[0] + 1 + 2 * g])
             B = None
             if self.touches_fault(p):
-                B = np.ascontiguousarray(Bg[:, b[0] - self.domain[0]:b[2] - self.domain[0] + 1 + 2 * g])
+                B = np.ascontiguousarray(Bg[:, b[0] - dom[0]:b[2] - dom[0] + 1 + 2 * g])
             self.set_patch(p, U, B)
 
-    def get_level(self, Ug: np.ndarray, Bg: np.ndarray | None):
-        """Gather the valid cells of every patch into domain-wide arrays (in place)."""
+    def _gather(self, patches, dom, Ug, Bg):
         g = A.TMK_NGHOST
-        for p, b in enumerate(self.boxes):
+        for p in patches:
+            b = self.boxes[p]
             U, B = self.get_patch(p)
-            ys = slice(b[1] - self.domain[1] + g, b[3] - self.domain[1] + 1 + g)
-            xs = slice(b[0] - self.domain[0] + g, b[2] - self.domain[0] + 1 + g)
+            ys = slice(b[1] - dom[1] + g, b[3] - dom[1] + 1 + g)
+            xs = slice(b[0] - dom[0] + g, b[2] - dom[0] + 1 + g)
             Ug[:, ys, xs] = U[:, g:-g, g:-g]
             if B is not None and Bg is not None:
                 Bg[:, xs] = B[:, g:-g]
+
+    def set_level(self, Ug: np.ndarray, Bg: np.ndarray | None):
+        """Scatter a domain-wide state (22, ny+8, nx+8) / fault row (nb, nx+8) into the patches."""
+        self._scatter(range(len(self.boxes)), self.domain, Ug, Bg)
+
+    def get_level(self, Ug: np.ndarray, Bg: np.ndarray | None):
+        """Gather the valid cells of every patch into domain-wide arrays (in place)."""
+        self._gather(range(len(self.boxes)), self.domain, Ug, Bg)
 
     def step(self, time: float, dt: float, stream=None, t_coarse_old: float | None = None,
              t_coarse_new: float | None = None) -> float:
@@ -295,6 +304,53 @@ class LinElastLevelGodunov:
             self.close()
         except Exception:
             pass
+
+
+class LinElastEnsemble(LinElastLevelGodunov):
+    """Independent scenarios stepped together as one level (tmk_ensemble_create):
+    scenario k has its own context (friction parameters), problem domain and
+    patches; every kernel of a step covers all of them.  The reference runs one
+    scenario per process; this is an extension."""
+
+    def __init__(self, ctxs, domains, boxes, dx: float | None = None):
+        """ctxs[k], domains[k] = (xlo, ylo, xhi, yhi) and boxes[k] (a list of
+        patch boxes) per scenario k."""
+        self.ctxs = list(ctxs)
+        self.ctx = self.ctxs[0]
+        self.lib = self.ctx.lib
+        self.dx = self.ctx.sc.dx if dx is None else dx
+        self.domains = [tuple(d) for d in domains]
+        self.domain = self.domains[0]
+        self.boxes, self.scen = [], []
+        for k, bk in enumerate(boxes):
+            for b in bk:
+                self.boxes.append(tuple(b))
+                self.scen.append(k)
+        self.pdomains = [self.domains[k] for k in self.scen]
+        n = len(self.boxes)
+        harr = (C.c_void_p * len(self.ctxs))(*[c.h for c in self.ctxs])
+        darr = (A.Box * len(self.domains))(*[A.box(*d) for d in self.domains])
+        barr = (A.Box * n)(*[A.box(*b) for b in self.boxes])
+        sarr = (C.c_int * n)(*self.scen)
+        h = C.c_void_p()
+        self.h = None
+        A.check(self.lib.tmk_ensemble_create(len(self.ctxs), harr, darr, self.dx, n, barr, sarr, C.byref(h)),
+                "tmk_ensemble_create")
+        self.h = h
+
+    def patches_of(self, k):
+        return [p for p, s in enumerate(self.scen) if s == k]
+
+    def set_scenario(self, k, Ug: np.ndarray, Bg: np.ndarray | None):
+        """Scatter scenario k's domain-wide state into its patches."""
+        self._scatter(self.patches_of(k), self.domains[k], Ug, Bg)
+
+    def get_scenario(self, k, Ug: np.ndarray, Bg: np.ndarray | None):
+        """Gather scenario k's valid cells into domain-wide arrays (in place)."""
+        self._gather(self.patches_of(k), self.domains[k], Ug, Bg)
+
+    def cells(self) -> int:
+        return sum((b[2] - b[0] + 1) * (b[3] - b[1] + 1) for b in self.boxes)
 
 
 class StepGraph:

@@ -166,3 +166,58 @@ def plastic_params(mu=math.sin(0.75), eta_time=0.03, G=None) -> A.PlasticParams:
     p = A.PlasticParams()
     p.mu, p.beta, p.eta, p.b, p.h = mu, mu / 2.0, eta_time * G, 0.0, 0.0
     return p
+
+
+# ------------------------------------------------------------------ ensembles
+ENSEMBLE_GRIDS = ((256, 128), (512, 256), (1024, 512))
+
+
+def lognormal_field(n: int, dx: float, corr_len: float, mean: float, s: float, seed: int) -> np.ndarray:
+    """mean * exp(g - s^2/2) on n cells of width dx, with g a stationary Gaussian
+    field of variance s^2 and exponential covariance s^2 exp(-|r|/corr_len).
+    Spectral synthesis by circulant embedding (Dietrich & Newsam 1997) on a
+    periodic grid of 2n cells, whose eigenvalues are non-negative for this
+    covariance in one dimension."""
+    m = 2 * n
+    j = np.arange(m)
+    r = np.minimum(j, m - j) * dx
+    lam = np.fft.fft(s * s * np.exp(-r / corr_len)).real
+    lam = np.maximum(lam, 0.0)
+    rng = np.random.default_rng(seed)
+    z = rng.standard_normal(m) + 1j * rng.standard_normal(m)
+    g = np.fft.fft(np.sqrt(lam / m) * z).real[:n]
+    return mean * np.exp(g - 0.5 * s * s)
+
+
+def ensemble_member(k: int, precision=A.TMK_PREC_MIXED, dx=0.1, grids=ENSEMBLE_GRIDS, V_init=1e-12):
+    """Scenario k of the seeded rate-and-state ensemble: grid drawn from `grids`,
+    a ~ U[0.006, 0.012], b - a ~ U[0.002, 0.006], L ~ U[0.01, 0.05] m (seed
+    5000 + k), and a shear prestress tau0(x) = 70 exp(g(x) - s^2/2) MPa along
+    strike, g Gaussian with exponential covariance, correlation length 1 km and
+    s = 0.1 (seed 6000 + k).  Returns (scenario, tau0 per fault face)."""
+    rng = np.random.default_rng(5000 + k)
+    nx, ny = grids[int(rng.integers(len(grids)))]
+    a = float(rng.uniform(0.006, 0.012))
+    ba = float(rng.uniform(0.002, 0.006))
+    L = float(rng.uniform(0.01, 0.05))
+    sc = rate_state(nx=nx, ny=ny, dx=dx, precision=precision, V_init=V_init)
+    sc.rs.a, sc.rs.b, sc.rs.L = a, a + ba, L
+    sc.rs.psi_init = psi_steady(sc.elastic.sxy0, -sc.elastic.syy0, V_init, a, sc.rs.V0, sc.constants()["Zs"])
+    tau0 = lognormal_field(nx, dx, 1.0, 70.0, 0.1, 6000 + k)
+    return sc, tau0
+
+
+def prestressed_state(sc: Scenario, tau0: np.ndarray, V_init=1e-12):
+    """Domain-wide U and B of a rate-and-state scenario whose shear stress is
+    tau0(x) in every row (both sides) and whose state psi is steady at V_init
+    under it, face by face."""
+    g = A.TMK_NGHOST
+    U = sc.initial_U()
+    B = sc.initial_B()
+    t = np.pad(np.asarray(tau0, dtype=np.float64), g, mode="edge")
+    for side in (0, 11):
+        U[side + 6] = t[None, :]
+    sn = -sc.elastic.syy0
+    Zs = sc.constants()["Zs"]
+    B[10] = [psi_steady(float(ti), sn, V_init, sc.rs.a, sc.rs.V0, Zs) for ti in t]
+    return U, B
