@@ -235,10 +235,11 @@ AMR_REGIONS = [(512, 0, 1535, 255), (1280, 0, 2815, 383), (3072, 0, 5119, 511)]
 
 
 def amr_measurement(steps, warmup, stream):
-    """Subcycled 4-level rate-and-state hierarchy with plasticity, a normal
-    stress rising along strike from 20 to 120 MPa and the shear prestress in
-    proportion; steps replayed from a CUDA graph of 2 coarse steps.  Returns
-    the JSON object of the measurement."""
+    """Subcycled 4-level rate-and-state hierarchy with plasticity, per-face
+    friction (a, b, L within 10 % of nominal), a normal stress rising along
+    strike from 20 to 120 MPa and the shear prestress in proportion; steps
+    replayed from a CUDA graph of 2 coarse steps.  Returns the JSON object of
+    the measurement."""
     import numpy as np
     import torch
     from tetemoko_gb300 import _capi as A, scenarios as S
@@ -272,6 +273,10 @@ def amr_measurement(steps, warmup, stream):
     for l in range(1, 4):        # finer levels from the coarser ones (regrid prolongation)
         levels[l].attach_coarser(levels[l - 1], 2)
         levels[l].interp_from_coarser(stream)
+    # a, b, L per fault face: nominal x (1 + U(-0.1, 0.1)), seed 4001, drawn on the
+    # base level's faces; finer faces take their coarse face's values
+    for l in range(4):
+        levels[l].set_level_friction(S.friction_field(sc, seed=4001, amp=0.1, refine=2 ** l))
     torch.cuda.synchronize()
     h = AMRHierarchy(levels, [2, 2, 2])
     dt0 = sc.dt()
@@ -301,9 +306,10 @@ def amr_measurement(steps, warmup, stream):
            "patches_per_level": [len(b) for b in boxes_all],
            "launches_per_coarse_step": h.launches_per_step(),
            "config": "4 levels, ratio 2, base 1024x512 at dx=0.1 km (finest 12.5 m, effective 8192x4096), "
-                     "rate-and-state aging law, Drucker-Prager plasticity, normal stress 20-120 MPa along "
-                     "strike, FP32 volume / FP64 fault, patches of at most 128x128, static nested bands "
-                     "around the nucleation (no tagging)",
+                     "rate-and-state aging law with a, b, L per fault face = nominal x (1 + U(-0.1, 0.1)) "
+                     "(seed 4001, base-level faces, refined piecewise constant), Drucker-Prager plasticity, "
+                     "normal stress 20-120 MPa along strike, FP32 volume / FP64 fault, patches of at most "
+                     "128x128, static nested bands around the nucleation (no tagging)",
            "execution": "CUDA graph of 2 subcycled coarse steps (tmk_amr_graph_create), replayed",
            "device_status": status}
     graph.close()
@@ -352,6 +358,16 @@ def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
+    # per-kernel times: a few steps call by call with events around each launch
+    # (the fault kernel then runs before the marching kernels, not beside them)
+    nprof = 10
+    ens.profile(True, nprof)
+    for _ in range(nprof):
+        ens.step(t, dt, stream)
+        t += dt
+    torch.cuda.synchronize()
+    prof, _ = ens.profile_read()
+    ens.profile(False)
     cells = ens.cells()
     grids = {}
     for sc, _ in members:
@@ -360,6 +376,8 @@ def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE):
            "ms_per_step": ms / (gsteps * nrep), "steps": gsteps * nrep, "scenarios": nscen,
            "cells": cells, "patches": len(ens.boxes), "grids": grids,
            "launches_per_step": ens.launches_per_step(),
+           "kernel_ms": {"exchange": prof[0], "fault": prof[1], "volume": prof[2], "step_serialised": prof[3]},
+           "volume_hbm_gbs": BYTES_PER_CELL_MIXED * cells / (prof[2] * 1e-3) / 1e9,
            "config": "rate-and-state aging law, a ~ U[0.006,0.012], b-a ~ U[0.002,0.006], L ~ U[0.01,0.05] m "
                      "(seed 5000+k), shear prestress 70 exp(g - s^2/2) MPa with g Gaussian, exponential "
                      "covariance, 1 km correlation, s = 0.1 (seed 6000+k), dx = 0.1 km, FP32 volume / FP64 "

@@ -213,6 +213,14 @@ tmk_status tmk_max_wave_speed(const tmk_context* ctx, double* speed);
 tmk_status tmk_level_create(tmk_context* ctx, const tmk_box* domain, double dx,
                             int npatch, const tmk_box* patches, tmk_level** out);
 void       tmk_level_destroy(tmk_level* lvl);
+/* Per-face rate-and-state friction of one fault patch (an extension: the
+ * reference varies only a and Vw along strike, by the linear ramp of RSSETF,
+ * ibcLinElast/RSIBCF.ChF:8-55).  abL holds 3 planes (a, b, L) over the patch's
+ * fault row grown by TMK_NGHOST in x, laid out like B; `host` as for
+ * tmk_level_set_patch.  The face's a replaces the scenario's a (the ramp is still
+ * added), b and L replace the scenario's.  Every value must be positive.  Levels
+ * of an AMR hierarchy each take their own faces' values. */
+tmk_status tmk_level_set_fault_friction(tmk_level* lvl, int patch, const double* abL, int host);
 /* Ensemble of independent scenarios stepped as one level (an extension: the
  * reference runs one scenario per process with its parameters in COMMON
  * blocks, srcLinElast/LinElastPhysicsF.ChF:1149-1210, ibcLinElast/RSIBCF.ChF:8-55).

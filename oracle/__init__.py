@@ -61,6 +61,8 @@ def lib() -> C.CDLL:
         L.tmko_plastic_correction.argtypes = [E, PL, dp, ip, ip, ip, ip, C.c_double]
         L.tmko_level_step.argtypes = [E, S, R, W, PL, ip, ip, C.c_int, ip, dp, dp, C.c_double,
                                       C.c_double, C.c_double, C.c_int]
+        L.tmko_level_step_fric.argtypes = [E, S, R, W, PL, ip, ip, C.c_int, ip, dp, dp, dp, C.c_double,
+                                           C.c_double, C.c_double, C.c_int]
         LV = P(_Level)
         L.tmko_cf_fill.argtypes = [C.c_int, C.c_int, LV, LV, C.c_double, LV]
         L.tmko_average_down.argtypes = [C.c_int, C.c_int, LV, LV]
@@ -182,15 +184,17 @@ def plastic_correction(sc, U: np.ndarray, ulo, blo, bhi, dt: float) -> None:
 
 
 def level_step(sc, Ug: np.ndarray, Bg: np.ndarray | None, boxes, time: float, dt: float,
-               nthreads: int = 1) -> int:
+               nthreads: int = 1, fric: np.ndarray | None = None) -> int:
     """LinElastLevelGodunov::step (+ plasticUpdate) for a single level whose
     patches `boxes` [(lo0, lo1, hi0, hi1), ...] tile the domain.  Ug is
-    (22, ny+8, nx+8), Bg (nbdry, nx+8); both updated in place."""
+    (22, ny+8, nx+8), Bg (nbdry, nx+8); both updated in place.  `fric` (3, nx+8):
+    optional per-face rate-and-state a, b, L (an extension)."""
     flat = np.ascontiguousarray(np.array(boxes, dtype=np.int32).reshape(-1))
-    return lib().tmko_level_step(
+    F = None if fric is None else np.ascontiguousarray(fric, dtype=np.float64)
+    return lib().tmko_level_step_fric(
         C.byref(sc.elastic), C.byref(sc.scheme), _ref(sc.rs), _ref(sc.sw), _ref(sc.plastic),
         _iv(0, 0), _iv(sc.nx - 1, sc.ny - 1), len(boxes), flat.ctypes.data_as(C.POINTER(C.c_int)),
-        _dp(Ug), _dp(Bg), sc.dx, time, dt, nthreads)
+        _dp(Ug), _dp(Bg), None if F is None else _dp(F), sc.dx, time, dt, nthreads)
 
 
 # ------------------------------------------------------------------ AMR --

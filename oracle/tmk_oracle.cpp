@@ -751,6 +751,7 @@ void ppmNormalPred(FAB& dWm, FAB& dWp, const double* lambda, double dtbydx, int 
 // ---------------------------------------------------------- the patch ----
 struct FaultData {
   FAB* B = nullptr;       // persistent boundary data (m_bdryData)
+  const FAB* fric = nullptr;   // optional per-face rate-and-state a, b, L (extension), B's box
   FAB tmp;                // m_tmpBdryData
   bool tmpSet = false;    // m_tmpBdryDataSet
 };
@@ -761,6 +762,14 @@ struct Patch {
   double dx, time;
   FaultData* fd;
   Patch(const Phys& p) : P(p) {}
+
+  // the parameters of fault face (i, j): the scenario's, with a, b, L replaced
+  // by the face's own when the patch carries per-face friction
+  Phys faceParams(int i, int j) const {
+    Phys Q = P;
+    if (fd && fd->fric) { Q.rs.a = (*fd->fric)(i, j, 0); Q.rs.b = (*fd->fric)(i, j, 1); Q.rs.L = (*fd->fric)(i, j, 2); }
+    return Q;
+  }
 
   // LinElastPatchGodunov::PPMNormalPred (srcLinElast/LinElastPatchGodunov.cpp:603-702)
   void PPMNormalPred(FAB& WM, FAB& WP, double dt, const FAB& W, int d, const Box& box) {
@@ -825,7 +834,7 @@ struct Patch {
         FAB& src = fd->tmpSet ? fd->tmp : *fd->B;
         double xc = (i + 0.5) * dx;
         if (P.sch.fault_law == TMK_FAULT_RS) {
-          rsfaultpt(P, wg, wi, src(i, j, 10), xc - P.rs.x0);
+          rsfaultpt(faceParams(i, j), wg, wi, src(i, j, 10), xc - P.rs.x0);
         } else {
           double b[TMK_SW_NBDRY];
           for (int c = 0; c < TMK_SW_NBDRY; ++c) b[c] = src(i, j, c);
@@ -887,7 +896,7 @@ struct Patch {
       for (int c = 0; c < nb; ++c) { bin[c] = Bin(i,j,c); bout[c] = Bout(i,j,c); }
       for (int c = 0; c < 22; ++c) u[c] = WH(i,j,c);
       if (P.sch.fault_law == TMK_FAULT_RS)
-        ok = rssetbndpt(P, bout, bin, u, dt, (i + 0.5)*dx - P.rs.x0, t) && ok;
+        ok = rssetbndpt(faceParams(i, j), bout, bin, u, dt, (i + 0.5)*dx - P.rs.x0, t) && ok;
       else
         swsetbndpt(P, bout, bin, u, dt, t, final_);
       for (int c = 0; c < nb; ++c) Bout(i,j,c) = bout[c];
@@ -1633,10 +1642,14 @@ int tmko_plastic_correction(const tmk_elastic_params* e, const tmk_plastic_param
 // comps); Bg the fault row over x in [dom.lo-4, dom.hi+4] (or NULL).  The
 // same-level exchange is the copy of neighbour values into each patch's ghosts.
 // `nthreads` > 0 runs the patch loop with that many OpenMP threads.
-int tmko_level_step(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_rs_params* rs,
-                    const tmk_sw_params* sw, const tmk_plastic_params* pl,
-                    const int dlo[2], const int dhi[2], int npatch, const int* boxes /*npatch*4: lo0 lo1 hi0 hi1*/,
-                    double* Ug, double* Bg, double dx, double time, double dt, int nthreads) {
+// As tmko_level_step, with optional per-face rate-and-state a, b, L (Fg: 3
+// planes over the domain's fault row grown by TMK_NGHOST, B's layout; NULL for
+// the scenario's constants).
+int tmko_level_step_fric(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_rs_params* rs,
+                         const tmk_sw_params* sw, const tmk_plastic_params* pl,
+                         const int dlo[2], const int dhi[2], int npatch, const int* boxes,
+                         double* Ug, double* Bg, const double* Fg, double dx, double time, double dt,
+                         int nthreads) {
   Phys P;
   if (!setup(P, e, s, rs, sw, pl)) return 1;
   Box dom = mk(dlo[0], dlo[1], dhi[0], dhi[1]);
@@ -1647,8 +1660,9 @@ int tmko_level_step(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_
   FAB Uold = wrap(Ug, gbox.lo, gbox.hi, 22);
   FAB Unew = Uold;
   Box bbox = mk(dom.lo[0]-TMK_NGHOST, dom.lo[1], dom.hi[0]+TMK_NGHOST, dom.lo[1]);
-  FAB Bold, Bnew;
+  FAB Bold, Bnew, Fric;
   if (fault) { Bold = wrap(Bg, bbox.lo, bbox.hi, nb); Bnew = Bold; }
+  if (fault && Fg && s->fault_law == TMK_FAULT_RS) Fric = wrap(Fg, bbox.lo, bbox.hi, 3);
   int bad = 0;
 #ifdef _OPENMP
   int nt = nthreads > 0 ? nthreads : 1;
@@ -1672,6 +1686,7 @@ int tmko_level_step(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_
         for (int i = std::max(bb.lo[0], bbox.lo[0]); i <= std::min(bb.hi[0], bbox.hi[0]); ++i)
           B(i, dom.lo[1], c) = Bold(i, dom.lo[1], c);
       fdt.B = &B;
+      if (Fric.nc == 3) fdt.fric = &Fric;
     }
     Patch pt(P);
     pt.dom = dom; pt.cur = cur; pt.dx = dx; pt.time = time; pt.fd = touches ? &fdt : nullptr;
@@ -1695,6 +1710,13 @@ int tmko_level_step(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_
   unwrap(Unew, Ug);
   if (fault) unwrap(Bnew, Bg);
   return bad ? 2 : 0;
+}
+
+int tmko_level_step(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_rs_params* rs,
+                    const tmk_sw_params* sw, const tmk_plastic_params* pl,
+                    const int dlo[2], const int dhi[2], int npatch, const int* boxes /*npatch*4: lo0 lo1 hi0 hi1*/,
+                    double* Ug, double* Bg, double dx, double time, double dt, int nthreads) {
+  return tmko_level_step_fric(e, s, rs, sw, pl, dlo, dhi, npatch, boxes, Ug, Bg, nullptr, dx, time, dt, nthreads);
 }
 
 // ---------------------------------------------------------- AMR operators --

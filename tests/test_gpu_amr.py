@@ -227,3 +227,43 @@ def test_attach_rejects_bad_layouts(cuda_lib):
     with pytest.raises(A.TmkError):          # a level with a coarser level needs the coarse times
         F2.step(0.0, sc.dt() / 2)
     F2.close(); F.close(); C.close(); ctx.close()
+
+
+def test_amr_per_face_friction(cuda_lib):
+    """Per-face friction on every level of a subcycled hierarchy (mixed form):
+    values equal to the scenario's constants give the constant run bit for bit;
+    a +-10% field, refined piecewise constant onto the finer level, changes it."""
+    from tetemoko_gb300.amr import AMRHierarchy
+    from tetemoko_gb300.level import Context
+    sc = _scenario("rs", A.TMK_PREC_MIXED)
+    datas = H.hierarchy(sc, np.random.default_rng(26), nlev=2)
+    ctx = Context(sc)
+    out = []
+    for mode in ("none", "const", "field"):
+        lvs = _levels_on_gpu(ctx, datas)
+        for l, lv in enumerate(lvs):
+            if mode == "none":
+                continue
+            F = S.friction_field(sc, refine=2 ** l)
+            if mode == "const":
+                F = np.tile(np.array([sc.rs.a, sc.rs.b, sc.rs.L])[:, None], (1, F.shape[1]))
+            lv.set_level_friction(F)
+        h = AMRHierarchy(lvs, [2])
+        for _ in range(3):
+            h.step(sc.dt())
+        out.append([_read(lv, d) for lv, d in zip(lvs, datas)])
+        for lv in lvs:
+            assert lv.status()[0] == 0
+        h.close()
+        for lv in lvs:
+            lv.close()
+    for a, b, c in zip(*out):
+        for p in range(len(a.boxes)):
+            np.testing.assert_array_equal(a.U[p], b.U[p])
+            if a.B[p] is not None:
+                np.testing.assert_array_equal(a.B[p], b.B[p])
+    fine_a, fine_c = out[0][1], out[2][1]
+    diffs = [rel_err(fine_c.B[p][10:11, G:-G], fine_a.B[p][10:11, G:-G])
+             for p in range(len(fine_a.boxes)) if fine_a.B[p] is not None]
+    assert diffs and max(diffs) > 1e-9
+    ctx.close()

@@ -145,3 +145,65 @@ def test_plastic_update_matches_oracle(cuda_lib):
     assert (Ur[9] > 0).any(), "the test state must yield somewhere"
     assert rel_err(Ug, Ur) <= RTOL_FP64
     ctx.close()
+
+
+@pytest.mark.parametrize("name", ["rs_slip", "rs_aging"])
+def test_level_steps_with_per_face_friction_match_oracle(cuda_lib, name):
+    """Per-face a, b, L (+-10% about the scenario's, seed 4001) on a level of
+    uneven patches: ten steps against the oracle given the same field."""
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    sc = dict(SCEN)[name]
+    rng = np.random.default_rng(98)
+    boxes = [(0, 0, 20, 9), (21, 0, 63, 9), (0, 10, 31, 31), (32, 10, 63, 31)]
+    Ug = perturbed_state(sc, rng, amp_v=0.05, amp_s=1.0)
+    Bg = sc.initial_B()
+    F = S.friction_field(sc, seed=4001)
+    Ur, Br = Ug.copy(), Bg.copy()
+    ctx = Context(sc)
+    lvl = LinElastLevelGodunov(ctx, boxes)
+    lvl.set_level(Ug, Bg)
+    lvl.set_level_friction(F)
+    dt = sc.dt()
+    t = 0.0
+    for n in range(10):
+        assert O.level_step(sc, Ur, Br, boxes, t, dt, fric=F) == 0
+        lvl.step(t, dt)
+        t += dt
+    Uo, Bo = Ug.copy(), Bg.copy()
+    lvl.get_level(Uo, Bo)
+    g = A.TMK_NGHOST
+    assert rel_err(Uo[:, g:-g, g:-g], Ur[:, g:-g, g:-g]) <= 1e-11
+    assert rel_err(Bo[:, g:-g], Br[:, g:-g]) <= 1e-11
+    # the field mattered: the constant-friction oracle run differs
+    Uc, Bc = Ug.copy(), Bg.copy()
+    t = 0.0
+    for n in range(10):
+        assert O.level_step(sc, Uc, Bc, boxes, t, dt) == 0
+        t += dt
+    assert rel_err(Bc[10:11, g:-g], Br[10:11, g:-g]) > 1e-9
+    rc, info = lvl.status()
+    assert rc == 0 and info[0] == 0
+    lvl.close()
+    ctx.close()
+
+
+def test_fault_friction_descriptor_checks(cuda_lib):
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    sc = S.rate_state(nx=64, ny=32, dx=0.1)
+    ctx = Context(sc)
+    lvl = LinElastLevelGodunov(ctx, [(0, 0, 63, 15), (0, 16, 63, 31)])
+    F = S.friction_field(sc)
+    with pytest.raises(A.TmkError):
+        lvl.set_fault_friction(1, F)             # patch 1 is not on the fault
+    F[1, 7] = 0.0
+    with pytest.raises(A.TmkError):
+        lvl.set_fault_friction(0, F)             # b must be positive
+    lvl.close()
+    ctx.close()
+    sw = S.slip_weakening(nx=64, ny=32, dx=0.1)
+    ctx = Context(sw)
+    lvl = LinElastLevelGodunov(ctx, [(0, 0, 63, 31)])
+    with pytest.raises(A.TmkError):
+        lvl.set_fault_friction(0, S.friction_field(sc))   # slip weakening has no a, b, L
+    lvl.close()
+    ctx.close()

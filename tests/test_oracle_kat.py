@@ -196,3 +196,26 @@ def test_rupture_propagates_in_the_oracle():
     rt = B[8, 4:-4]
     assert (rt < 1e9).sum() > 30
     assert np.isfinite(U).all()
+
+
+def test_per_face_friction_in_the_oracle():
+    """Per-face a, b, L equal to the scenario's constants reproduce the constant
+    run bit for bit; a +-10% field changes the fault's evolution."""
+    sc = S.rate_state(nx=48, ny=24, dx=0.1)
+    sc.rs.L = 0.002
+    rng = np.random.default_rng(12)
+    U = sc.initial_U()
+    U[:, 4:-4, 4:-4] += rng.normal(0, 0.05, U[:, 4:-4, 4:-4].shape)
+    B = sc.initial_B()
+    const = np.tile(np.array([sc.rs.a, sc.rs.b, sc.rs.L])[:, None], (1, B.shape[1]))
+    hetero = S.friction_field(sc, seed=4001)
+    runs = []
+    for F in (None, const, hetero):
+        Ur, Br = U.copy(), B.copy()
+        t = 0.0
+        for _ in range(4):
+            assert O.level_step(sc, Ur, Br, [(0, 0, 23, 23), (24, 0, 47, 23)], t, sc.dt(), fric=F) == 0
+            t += sc.dt()
+        runs.append((Ur, Br))
+    assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
+    assert not np.array_equal(runs[0][1][10], runs[2][1][10])

@@ -120,6 +120,7 @@ def lib() -> C.CDLL:
     L.tmk_max_wave_speed.argtypes = [vp, dp]
     L.tmk_level_create.argtypes = [vp, C.POINTER(Box), C.c_double, C.c_int, C.POINTER(Box), C.POINTER(vp)]
     L.tmk_level_destroy.argtypes = [vp]
+    L.tmk_level_set_fault_friction.argtypes = [vp, C.c_int, vp, C.c_int]
     L.tmk_ensemble_create.argtypes = [C.c_int, C.POINTER(vp), C.POINTER(Box), C.c_double, C.c_int,
                                       C.POINTER(Box), ip, C.POINTER(vp)]
     L.tmk_level_destroy.restype = None

@@ -308,6 +308,7 @@ void fill_patchdev(tmk_level_s* L, int parity) {
     d.Bold = lp.Bold;
     d.cap = L->cap;
     d.caplist = L->dcaplist;
+    d.fric = lp.fric;
   }
 }
 
@@ -319,6 +320,26 @@ tmk_status tmk_host::upload_patchdev(tmk_level_s* L, cudaStream_t s) {
     // a copy from pageable memory returns once the source has been staged
     TMK_CU(cudaMemcpyAsync(L->dpatch[par], L->hpatch[par].data(), L->hpatch[par].size(), cudaMemcpyHostToDevice, s));
   }
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_set_fault_friction(tmk_level* L, int patch, const double* abL, int host) {
+  if (!L || !abL || patch < 0 || patch >= (int)L->patches.size()) return TMK_ERR_BAD_DESC;
+  LevelPatch& lp = L->patches[patch];
+  if (!lp.fault || L->ctx->scheme.fault_law != TMK_FAULT_RS) return TMK_ERR_BAD_DESC;
+  const size_t n = 3 * (size_t)lp.bnx;
+  std::vector<double> h(n);   // staged on the host: every face's a, b, L must be positive
+  TMK_CU(cudaMemcpy(h.data(), abL, n * sizeof(double), host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost));
+  for (int i = 0; i < lp.bnx; ++i)
+    if (!(h[i] > 0) || !(h[lp.bnx + i] > 0) || !(h[2 * lp.bnx + i] > 0)) return TMK_ERR_BAD_DESC;
+  const bool fresh = lp.fric == nullptr;
+  if (fresh) {
+    if (dalloc(&lp.fric, n) != cudaSuccess) return TMK_ERR_ALLOC;
+    L->allocs.push_back(lp.fric);
+  }
+  TMK_CU(cudaMemcpy(lp.fric, h.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  if (fresh && upload_patchdev(L, 0) != TMK_OK) return TMK_ERR_CUDA;
+  TMK_CU(cudaDeviceSynchronize());
   return TMK_OK;
 }
 

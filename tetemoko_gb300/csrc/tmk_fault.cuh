@@ -19,6 +19,16 @@ TMK_D double boxcar(double w, double r) { return (r >= w) ? 0.0 : 1.0; }
 
 constexpr int RS_IMAX = 100;
 
+// Rate-and-state parameters of one fault face: the scenario's a, b, L, or the
+// face's own when the level carries per-face friction (an extension: the
+// reference varies only a and Vw along x, by the linear ramp that RSSETF sets,
+// ibcLinElast/RSIBCF.ChF:8-55).
+struct RSFace { double a, b, L; };
+TMK_D RSFace rs_face(const DevParams& P, const double* fric, int off, int stride) {
+  if (!fric) return RSFace{P.rs_a, P.rs_b, P.rs_L};
+  return RSFace{fric[off], fric[off + stride], fric[off + 2 * stride]};
+}
+
 // RSNEWTON (ibcLinElast/RSIBCF.ChF:336-401): bracketed Newton on the slip rate
 // for  sn a asinh(V exp(psi/a)/(2V0)) + Zs/2 V = phi  on (0, phi/Zs).  The loop
 // is bounded by IMAX; returns the iterations used.
@@ -88,7 +98,8 @@ TMK_D int rs_newton_z(const DevParams& P, double phi, double psi, double sn, dou
 
 // RSFAULTBCF (ibcLinElast/RSIBCF.ChF:158-323) at one fault face; Wi, Wg: 22 comps.
 // zsolve selects rs_newton_z (mixed form) instead of the reference's RSNEWTON.
-TMK_D int rs_fault(const DevParams& P, const double* Wi, double psi, double x, double* Wg, bool zsolve = false) {
+TMK_D int rs_fault(const DevParams& P, const RSFace& fr, const double* Wi, double psi, double x, double* Wg,
+                   bool zsolve = false) {
   const double Zs = P.Zs, Zp = P.Zp, lam = P.lam, G = P.G;
   double vx1 = Wi[0], vy1 = Wi[1], vz1 = Wi[2], sxx1 = Wi[3], syy1 = Wi[4], szz1 = Wi[5];
   double sxy1 = Wi[6], sxz1 = Wi[7], syz1 = Wi[8];
@@ -111,7 +122,7 @@ TMK_D int rs_fault(const DevParams& P, const double* Wi, double psi, double x, d
   vy2 = -(wpyy1 + wpyy2) / 2.0 / Zp;
   double V = sqrt((vx1 - vx2) * (vx1 - vx2) + (vz1 - vz2) * (vz1 - vz2));
   double c_ramp = fmin(1.0, fmax(0.0, (x - P.ramp_x) / P.ramp_w));
-  double c_rs_a = P.rs_a + P.ramp_a * c_ramp;
+  double c_rs_a = fr.a + P.ramp_a * c_ramp;
   double tau;
   int it = zsolve ? rs_newton_z(P, phi, psi, -syy1, c_rs_a, V, tau) : rs_newton(P, phi, psi, -syy1, c_rs_a, V, tau);
   sxy1 = (phi_xy / phi) * tau - tau_xy_0;
@@ -141,11 +152,11 @@ TMK_D int rs_fault(const DevParams& P, const double* Wi, double psi, double x, d
 // strided).  When `final_` is false only psi is produced (the predictor's
 // tmp data, of which the fault solve reads nothing else).  Returns the new
 // psi (NaN is reported by the caller; the reference stops there).
-TMK_D double rs_setbnd(const DevParams& P, const double* U, double* B, int bstride, double dt, double x,
-                       double time, bool final_) {
+TMK_D double rs_setbnd(const DevParams& P, const RSFace& fr, const double* U, double* B, int bstride, double dt,
+                       double x, double time, bool final_) {
   double tau_xy_0 = P.rs_nsig * gaussian(P.rs_r0, x);
   double c_ramp = fmin(1.0, fmax(0.0, (x - P.ramp_x) / P.ramp_w));
-  double c_rs_a = P.rs_a + P.ramp_a * c_ramp;
+  double c_rs_a = fr.a + P.ramp_a * c_ramp;
   double c_rs_Vw = P.rs_Vw + P.ramp_Vw * c_ramp;
   double Vx = U[0] - U[11];
   double Vz = U[2] - U[13];
@@ -155,18 +166,18 @@ TMK_D double rs_setbnd(const DevParams& P, const double* U, double* B, int bstri
   if (P.state_law == 1) {
     // aging law (extension), exact at constant V over dt:
     // theta' = theta exp(-x) + dt (1-exp(-x))/x, x = V dt / L
-    double xx = V * dt / P.rs_L;
+    double xx = V * dt / fr.L;
     double phi1 = (xx > 1e-12) ? -expm1(-xx) / xx : 1.0 - 0.5 * xx;
-    double q = (psi - P.rs_f0) / P.rs_b - xx;
-    dPsi = P.rs_f0 + P.rs_b * log(exp(q) + (P.rs_V0 * dt / P.rs_L) * phi1);
+    double q = (psi - P.rs_f0) / fr.b - xx;
+    dPsi = P.rs_f0 + fr.b * log(exp(q) + (P.rs_V0 * dt / fr.L) * phi1);
   } else {
     double f = c_rs_a * asinh(V * exp(psi / c_rs_a) / (2.0 * P.rs_V0));
-    double fss = P.rs_f0 - (P.rs_b - c_rs_a) * log(V / P.rs_V0);
+    double fss = P.rs_f0 - (fr.b - c_rs_a) * log(V / P.rs_V0);
     if (P.rs_fexp > 0.0) {
       double q = V / c_rs_Vw, q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
       fss = P.rs_fw + (fss - P.rs_fw) / pow(1.0 + q8, 0.125);
     }
-    dPsi = psi - dt * (V / P.rs_L) * (f - fss);
+    dPsi = psi - dt * (V / fr.L) * (f - fss);
   }
   if (final_) {
     double rt = B[9 * bstride];

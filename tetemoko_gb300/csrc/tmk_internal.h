@@ -48,6 +48,7 @@ struct LevelPatch {
   int blo = 0, bnx = 0;
   double* first = nullptr;
   double* ffault = nullptr;
+  double* fric = nullptr;   // per-face rate-and-state a, b, L (3 planes of bnx), if set
 };
 
 struct CFLink;   // coarse-fine coupling of a level with its coarser level (tmk_amr.cu)

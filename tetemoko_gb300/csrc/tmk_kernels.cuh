@@ -42,6 +42,7 @@ struct PatchDev {
   double* Bold;             // fault data at the start of the step (coarse-fine time interpolation)
   double* cap;              // captured face fluxes of the level (flux registers), 22 per slot
   const int4* caplist;      // (dir, i, j, slot) of the captured faces, grouped by tile
+  const double* fric;       // optional per-face rate-and-state a, b, L: 3 planes like B (stride bnx)
 };
 
 // A tile of the volume kernel; [cap0, cap0+ncap) are the captured faces it owns.
@@ -187,13 +188,14 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
       double Wg[NC];
       for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
       int it = 0;
-      if (P.fault_law == 1) it = rs_fault(P, sWi[tid], Bi[10 * bs], xc - P.rs_x0, Wg, kZSolve);
+      const RSFace fr = rs_face(P, p.fric, i - p.blo0, bs);
+      if (P.fault_law == 1) it = rs_fault(P, fr, sWi[tid], Bi[10 * bs], xc - P.rs_x0, Wg, kZSolve);
       else sw_fault(P, sWi[tid], Bi[7 * bs], xc, Wg);
       if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
       double* first = p.first + (i - (p.vlo0 - 1));
       for (int c = 0; c < NC; ++c) first[c * p.nfirst] = Wg[c];
       if (i >= s0 && i <= s1) {
-        if (P.fault_law == 1) sTmp[tid] = rs_setbnd(P, Wg, Bi, bs, 0.5 * dt, xc - P.rs_x0, 0.0, false);
+        if (P.fault_law == 1) sTmp[tid] = rs_setbnd(P, fr, Wg, Bi, bs, 0.5 * dt, xc - P.rs_x0, 0.0, false);
         else sTmp[tid] = sw_setbnd(P, Wg, Bi, bs, 0.5 * dt, 0.0, false);
       }
     }
@@ -231,7 +233,8 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
     double Wg[NC];
     for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
     int it = 0;
-    if (P.fault_law == 1) it = rs_fault(P, Wi, sTmp[ci], xc - P.rs_x0, Wg, kZSolve);
+    const RSFace fr = rs_face(P, p.fric, i - p.blo0, bs);
+    if (P.fault_law == 1) it = rs_fault(P, fr, Wi, sTmp[ci], xc - P.rs_x0, Wg, kZSolve);
     else sw_fault(P, Wi, sTmp[ci], xc, Wg);
     if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
     // (F) y fluxes through the fault face (GETFLUXF, FP64)
@@ -245,7 +248,7 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
     for (int c = 0; c < NSIDE; ++c) ff[(11 + c) * nv] = F[c];
     // (G) boundary-data update with the final fault state (final=true, t+dt)
     if (P.fault_law == 1) {
-      double np = rs_setbnd(P, Wg, Bi, bs, dt, xc - P.rs_x0, time + dt, true);
+      double np = rs_setbnd(P, fr, Wg, Bi, bs, dt, xc - P.rs_x0, time + dt, true);
       if (isnan(np)) report(st, ST_NAN, (long long)i);
     } else {
       sw_setbnd(P, Wg, Bi, bs, dt, time + dt, true);
@@ -523,12 +526,41 @@ __global__ void exchange_kernel(const PatchDev<Real>* __restrict__ patches, cons
   const PatchDev<Real>& ps = patches[cp.src];
   const PatchDev<Real>& pd = patches[cp.dst];
   const int nx = cp.hi0 - cp.lo0 + 1, ny = cp.hi1 - cp.lo1 + 1;
-  const Real* src = to_in ? ps.Uout : ps.Uin;
-  Real* dst = to_in ? (Real*)pd.Uout : (Real*)pd.Uin;
+  const Real* src = (to_in ? ps.Uout : ps.Uin) + fab_idx(ps, c0, cp.lo0, cp.lo1);
+  Real* dst = (to_in ? (Real*)pd.Uout : (Real*)pd.Uin) + fab_idx(pd, c0, cp.lo0, cp.lo1);
+  const size_t splane = (size_t)ps.any * ps.anx, dplane = (size_t)pd.any * pd.anx;
+  const int nrow = ncomp * ny;
+  const int step = blockDim.x * gridDim.y, t0 = threadIdx.x + blockIdx.y * blockDim.x;
+  // rows of 16-byte vectors when every row of both boxes starts on a 16-byte boundary
+  constexpr int W = 16 / sizeof(Real);
+  const bool vec = nx % W == 0 && ps.anx % W == 0 && pd.anx % W == 0 && splane % W == 0 && dplane % W == 0 &&
+                   ((uintptr_t)src & 15) == 0 && ((uintptr_t)dst & 15) == 0;
+  if (vec) {
+    // four vectors per thread in flight: all loads, then all stores
+    constexpr int U = 4;
+    const int nv = nx / W, n = nrow * nv;
+    for (int base = t0; base < n; base += U * step) {
+      float4 v[U];
+      size_t o[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int idx = base + u * step;
+        if (idx < n) {
+          const int row = idx / nv, k = idx - row * nv, c = row / ny, j = row - c * ny;
+          v[u] = __ldg((const float4*)(src + c * splane + (size_t)j * ps.anx + k * W));
+          o[u] = c * dplane + (size_t)j * pd.anx + k * W;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (base + u * step < n) *(float4*)(dst + o[u]) = v[u];
+    }
+    return;
+  }
   // a copy box is spread over gridDim.y CTAs (more loads in flight)
-  for (int idx = threadIdx.x + blockIdx.y * blockDim.x; idx < ncomp * nx * ny; idx += blockDim.x * gridDim.y) {
-    int c = c0 + idx / (nx * ny), j = cp.lo1 + (idx / nx) % ny, i = cp.lo0 + idx % nx;
-    dst[fab_idx(pd, c, i, j)] = src[fab_idx(ps, c, i, j)];
+  for (int idx = t0; idx < nrow * nx; idx += step) {
+    const int row = idx / nx, i = idx - row * nx, c = row / ny, j = row - c * ny;
+    dst[c * dplane + (size_t)j * pd.anx + i] = src[c * splane + (size_t)j * ps.anx + i];
   }
 }
 

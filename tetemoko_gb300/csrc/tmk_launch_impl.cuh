@@ -48,7 +48,9 @@ struct LaunchImpl {
   static cudaError_t exchange(const PatchDev<Real>* patches, const CopyDev* copies, int ncopies, int c0,
                               int ncomp, cudaStream_t s) {
     if (ncopies <= 0) return cudaSuccess;
-    exchange_kernel<Real><<<dim3(ncopies, 8), 256, 0, s>>>(patches, copies, c0, ncomp, 0);
+    // about two waves of 256-thread CTAs: each copy box spread over up to 8 CTAs
+    const int chunks = std::max(1, std::min(8, (2 * 8 * 152 + ncopies - 1) / ncopies));
+    exchange_kernel<Real><<<dim3(ncopies, chunks), 256, 0, s>>>(patches, copies, c0, ncomp, 0);
     return cudaGetLastError();
   }
   static cudaError_t march(int g, const PatchDev<Real>* patches, const MarchItem* items, int nitems,

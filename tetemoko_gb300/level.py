@@ -183,6 +183,23 @@ class LinElastLevelGodunov:
         A.check(self.lib.tmk_level_get_patch(self.h, p, uptr, bptr, 1 if host else 0), "tmk_level_get_patch")
         return U, B
 
+    def set_fault_friction(self, p, F):
+        """Per-face rate-and-state a, b, L of fault patch p: F (3, nx+8) over the
+        patch's fault row grown by 4 ghosts (numpy or CUDA tensor)."""
+        if isinstance(F, np.ndarray):
+            F = np.ascontiguousarray(F, dtype=np.float64)
+            A.check(self.lib.tmk_level_set_fault_friction(self.h, p, F.ctypes.data, 1), "tmk_level_set_fault_friction")
+        else:
+            A.check(self.lib.tmk_level_set_fault_friction(self.h, p, F.data_ptr(), 0), "tmk_level_set_fault_friction")
+
+    def set_level_friction(self, Fg: np.ndarray):
+        """Scatter a domain-wide per-face friction row (3, nx+8) into the fault patches."""
+        g = A.TMK_NGHOST
+        for p, b in enumerate(self.boxes):
+            if self.touches_fault(p):
+                dom = self.pdomains[p]
+                self.set_fault_friction(p, Fg[:, b[0] - dom[0]:b[2] - dom[0] + 1 + 2 * g])
+
     def _scatter(self, patches, dom, Ug, Bg):
         g = A.TMK_NGHOST
         for p in patches:

@@ -221,3 +221,18 @@ def prestressed_state(sc: Scenario, tau0: np.ndarray, V_init=1e-12):
     Zs = sc.constants()["Zs"]
     B[10] = [psi_steady(float(ti), sn, V_init, sc.rs.a, sc.rs.V0, Zs) for ti in t]
     return U, B
+
+
+def friction_field(sc: Scenario, seed: int = 4001, amp: float = 0.1, refine: int = 1) -> np.ndarray:
+    """Per-face rate-and-state (a, b, L) = nominal x (1 + U(-amp, amp)), drawn on
+    the scenario's nx faces (seed `seed`), each face's three values independent.
+    `refine` > 1 gives the same field on a level refined by that ratio (every
+    fine face takes its coarse face's values).  Returned over the faces grown
+    by TMK_NGHOST (edge values repeated), shape (3, nx*refine + 8): the layout
+    of LinElastLevelGodunov.set_level_friction."""
+    rng = np.random.default_rng(seed)
+    nom = np.array([sc.rs.a, sc.rs.b, sc.rs.L])[:, None]
+    F = nom * (1.0 + rng.uniform(-amp, amp, size=(3, sc.nx)))
+    if refine > 1:
+        F = np.repeat(F, refine, axis=1)
+    return np.pad(F, ((0, 0), (A.TMK_NGHOST, A.TMK_NGHOST)), mode="edge")
