@@ -234,7 +234,7 @@ AMR_BASE = (1024, 512)
 AMR_REGIONS = [(512, 0, 1535, 255), (1280, 0, 2815, 383), (3072, 0, 5119, 511)]
 
 
-def amr_measurement(steps, warmup, stream):
+def amr_measurement(steps, warmup, stream, autotune=True):
     """Subcycled 4-level rate-and-state hierarchy with plasticity, per-face
     friction (a, b, L within 10 % of nominal), a normal stress rising along
     strike from 20 to 120 MPa and the shear prestress in proportion; steps
@@ -277,6 +277,19 @@ def amr_measurement(steps, warmup, stream):
     # base level's faces; finer faces take their coarse face's values
     for l in range(4):
         levels[l].set_level_friction(S.friction_field(sc, seed=4001, amp=0.1, refine=2 ** l))
+    # each level's tuning from the autotuner, run on a standalone copy of the
+    # level (an attached level steps only inside its hierarchy)
+    tunings = []
+    if autotune:
+        for l in range(4):
+            probe = LinElastLevelGodunov(ctx, boxes_all[l], domain=levels[l].domain, dx=levels[l].dx)
+            Us, Bs = levels[l].get_patches()
+            probe.set_patches(Us, Bs)
+            probe.set_level_friction(S.friction_field(sc, seed=4001, amp=0.1, refine=2 ** l))
+            t, _ = probe.autotune(0.0, sc.dt() / 2 ** l, steps=4, stream=stream)
+            probe.close()
+            levels[l].set_tuning(t)
+            tunings.append(t.as_dict())
     torch.cuda.synchronize()
     h = AMRHierarchy(levels, [2, 2, 2])
     dt0 = sc.dt()
@@ -311,6 +324,7 @@ def amr_measurement(steps, warmup, stream):
                      "normal stress 20-120 MPa along strike, FP32 volume / FP64 fault, patches of at most "
                      "128x128, static nested bands around the nucleation (no tagging)",
            "execution": "CUDA graph of 2 subcycled coarse steps (tmk_amr_graph_create), replayed",
+           "tuning": {"autotuned": bool(autotune), "per_level": tunings},
            "device_status": status}
     graph.close()
     h.close()
@@ -323,7 +337,7 @@ def amr_measurement(steps, warmup, stream):
 ENSEMBLE_SIZE = 64
 
 
-def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE):
+def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE, autotune=True):
     """64 independent rate-and-state scenarios (seeded friction, lognormal shear
     prestress, grids drawn from 256x128 / 512x256 / 1024x512) stepped as one
     level in the mixed form; steps replayed from a CUDA graph.  Returns the JSON
@@ -339,6 +353,7 @@ def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE):
         U, B = S.prestressed_state(sc, tau0)
         ens.set_scenario(k, U, B)
     dt = members[0][0].dt()
+    tuning = ens.autotune(0.0, dt, steps=4, stream=stream)[0].as_dict() if autotune else None
     t = 0.0
     for _ in range(warmup):
         ens.step(t, dt, stream)
@@ -384,6 +399,7 @@ def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE):
                      "fault, patches of at most 128x128, one level of all scenarios",
            "execution": f"CUDA graph of {gsteps} ensemble steps (tmk_ensemble_create + tmk_level_graph_create), "
                         "replayed",
+           "tuning": {"autotuned": bool(autotune), "choice": tuning},
            "device_status": ens.status()[1]}
     graph.close()
     ens.close()
@@ -457,6 +473,7 @@ def main():
     ap.add_argument("--amr-only", action="store_true")      # only the AMR measurement (profiling runs)
     ap.add_argument("--ensemble-steps", type=int, default=200)   # timed steps of the ensemble measurement
     ap.add_argument("--ensemble-only", action="store_true")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false")   # keep the default tuning
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     args = ap.parse_args()
@@ -542,20 +559,28 @@ def main():
     # a second timed pass with CUDA events around every launch for the roofline
     # (events between the fault and volume kernels serialise their overlap)
     if args.amr_only:
-        amr = amr_measurement(args.amr_steps, args.warmup, stream)
+        amr = amr_measurement(args.amr_steps, args.warmup, stream, args.autotune)
         if rank == 0:
             print(json.dumps({"amr": amr}), flush=True)
         return 0
     if args.ensemble_only:
-        ens = ensemble_measurement(args.ensemble_steps, args.warmup, stream)
+        ens = ensemble_measurement(args.ensemble_steps, args.warmup, stream, autotune=args.autotune)
         if rank == 0:
             print(json.dumps({"ensemble": ens}), flush=True)
         return 0
     sc, ctx, lvl = make_level(A.TMK_PREC_MIXED)
+    # work-list shape and fault-kernel variant picked by the autotuner (trial
+    # steps from the initial state, which it puts back)
+    tuning, tune_ms = None, None
+    if args.autotune:
+        t, tune_ms = lvl.autotune(0.0, sc.dt(), steps=10, stream=stream)
+        tuning = t.as_dict()
     # steps replayed from a CUDA graph of graph_steps recorded steps (the
     # largest even divisor of --steps up to 100); also timed call by call
     graph_steps = next((g for g in range(min(100, args.steps), 1, -1) if args.steps % g == 0 and g % 2 == 0), 0)
     _, ctx_c, lvl_c = make_level(A.TMK_PREC_MIXED)       # same workload from its initial state
+    if args.autotune:
+        lvl_c.set_tuning(lvl.tuning())
     ms_call, _, _, _ = timed(lvl_c, sc, args.steps, args.warmup, profile=False)
     value_call, _ = replica_rate(cells, args.steps, ms_call * 1e-3, world, device="cuda")
     lvl_c.close()
@@ -631,9 +656,10 @@ def main():
     ctx64.close()
 
     # ---- subcycled 4-level AMR hierarchy (rank 0 reports its own)
-    amr = amr_measurement(args.amr_steps, 2, stream) if args.amr_steps > 0 else None
+    amr = amr_measurement(args.amr_steps, 2, stream, args.autotune) if args.amr_steps > 0 else None
     # ---- ensemble of 64 independent scenarios in one level
-    ens = ensemble_measurement(args.ensemble_steps, 3, stream) if args.ensemble_steps > 0 else None
+    ens = ensemble_measurement(args.ensemble_steps, 3, stream, autotune=args.autotune) \
+        if args.ensemble_steps > 0 else None
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
@@ -655,6 +681,7 @@ def main():
             "gpu_launches": launches,
             "execution": (f"steps replayed from a CUDA graph of {graph_steps} recorded level steps "
                           "(tmk_level_graph_create / tmk_graph_launch)") if graph_steps else "one call per step",
+            "tuning": {"autotuned": bool(args.autotune), "choice": tuning, "trial_ms_per_step": tune_ms},
             "per_call": {"value": value_call, "unit": UNIT, "ms_per_step": ms_call / args.steps,
                          "note": "the same steps, one tmk_level_step call each"},
             "clocks": clocks,

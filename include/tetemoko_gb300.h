@@ -131,6 +131,18 @@ typedef struct {
 
 typedef struct { int lo[2], hi[2]; } tmk_box;   /* cell-centred, inclusive */
 
+/* How a level's step is cut into work (an extension: the reference's patch
+ * loop has no such choices).  Defaults: the scheme's volume kernel, one wave
+ * per marching group, runs of at least 16 rows, one antiplane slot per
+ * fault-kernel CTA, 32 fault faces per fault-kernel CTA. */
+typedef struct {
+  int volume_kernel;    /* TMK_VOLUME_MARCH or TMK_VOLUME_TILE (march only if the scheme allows it) */
+  int march_waves[2];   /* marching items of the in-plane / antiplane group, in waves of resident CTAs: 1..8 */
+  int min_run;          /* fewest rows of a marching item: 4..4096 */
+  int fault_displace;   /* antiplane CTA slots left free per fault-kernel CTA: 0..4 */
+  int fault_seg;        /* fault faces per fault-kernel CTA: 32 (4 warps) or 16 (2 warps) */
+} tmk_tuning;
+
 typedef struct tmk_context_s tmk_context;
 typedef struct tmk_level_s   tmk_level;
 typedef struct tmk_amr_s     tmk_amr;
@@ -270,6 +282,20 @@ tmk_status tmk_level_profile(tmk_level* lvl, int enable, int max_steps);
 /* Average milliseconds per recorded step of: out[0] ghost exchange,
  * out[1] fault kernel, out[2] volume kernel, out[3] whole step. */
 tmk_status tmk_level_profile_read(tmk_level* lvl, double out[4], int* nsteps);
+/* The level's tuning; setting it rebuilds the work lists (and the coarse-fine
+ * capture lists of an attached level).  TMK_ERR_BAD_DESC for values out of
+ * range or while a recorded graph launches the level's kernels. */
+tmk_status tmk_level_get_tuning(const tmk_level* lvl, tmk_tuning* out);
+tmk_status tmk_level_set_tuning(tmk_level* lvl, const tmk_tuning* t);
+/* Autotuner: times `steps` level steps (after 2 untimed ones) from the level's
+ * present state for each candidate tuning -- volume kernel, marching waves per
+ * group, shortest run, fault displacement and fault segment -- keeps the
+ * fastest, and puts the state back as it was.  *best (optional) receives the
+ * choice and *ms_per_step (optional) its time.  Synchronous on `stream`.  Not
+ * for a level attached to another level (TMK_ERR_BAD_DESC): tune the levels
+ * of a hierarchy before attaching them. */
+tmk_status tmk_level_autotune(tmk_level* lvl, double time, double dt, int steps, void* stream,
+                              tmk_tuning* best, double* ms_per_step);
 
 /* ---------------------------------------------------------------------------
  * Coarse-fine coupling (AMRLevelLinElast::levelSetup,

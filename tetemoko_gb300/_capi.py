@@ -71,6 +71,16 @@ class Scheme(C.Structure):
 TMK_VOLUME_AUTO, TMK_VOLUME_TILE, TMK_VOLUME_MARCH = 0, 1, 2
 
 
+class Tuning(C.Structure):
+    _fields_ = [("volume_kernel", C.c_int), ("march_waves", C.c_int * 2), ("min_run", C.c_int),
+                ("fault_displace", C.c_int), ("fault_seg", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {"volume_kernel": {TMK_VOLUME_MARCH: "march", TMK_VOLUME_TILE: "tile"}.get(self.volume_kernel),
+                "march_waves": list(self.march_waves), "min_run": self.min_run,
+                "fault_displace": self.fault_displace, "fault_seg": self.fault_seg}
+
+
 class Fab(C.Structure):
     _fields_ = [("data", C.c_void_p), ("lo", C.c_int * 2), ("hi", C.c_int * 2), ("ncomp", C.c_int)]
 
@@ -120,6 +130,9 @@ def lib() -> C.CDLL:
     L.tmk_max_wave_speed.argtypes = [vp, dp]
     L.tmk_level_create.argtypes = [vp, C.POINTER(Box), C.c_double, C.c_int, C.POINTER(Box), C.POINTER(vp)]
     L.tmk_level_destroy.argtypes = [vp]
+    L.tmk_level_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.tmk_level_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.tmk_level_autotune.argtypes = [vp, C.c_double, C.c_double, C.c_int, vp, C.POINTER(Tuning), dp]
     L.tmk_level_set_fault_friction.argtypes = [vp, C.c_int, vp, C.c_int]
     L.tmk_ensemble_create.argtypes = [C.c_int, C.POINTER(vp), C.POINTER(Box), C.c_double, C.c_int,
                                       C.POINTER(Box), ip, C.POINTER(vp)]

@@ -425,7 +425,7 @@ namespace {
 
 // Assign capture slots to the faces that the level's links need, group them
 // by the tile that computes them, and refresh the links' slot tables.
-tmk_status rebuild_captures(tmk_level_s* L) {
+tmk_status rebuild_captures_impl(tmk_level_s* L) {
   std::map<FaceKey, int> slot;
   if (L->coarser) for (const FaceKey& k : L->coarser->fface) slot.emplace(k, 0);
   if (L->finer) for (const FaceKey& k : L->finer->cface) slot.emplace(k, 0);
@@ -508,7 +508,7 @@ tmk_status rebuild_captures(tmk_level_s* L) {
       TMK_CU(cudaMemcpy(L->dfrows[g], L->hfrows[g].data(), L->hfrows[g].size() * sizeof(tmk::MarchItem),
                         cudaMemcpyHostToDevice));
   }
-  L->march = L->march_allowed;
+  L->march = L->march_allowed && L->tune.volume_kernel == TMK_VOLUME_MARCH;
   if (upload_patchdev(L, 0) != TMK_OK) return TMK_ERR_CUDA;
   // slot tables of the links that use this level's captures
   if (L->coarser && L->coarser->nent) {
@@ -539,8 +539,8 @@ void detach(tmk_level_s* F) {
   F->coarser = nullptr;
   if (C && C->finer == k) C->finer = nullptr;
   free_link(k);
-  rebuild_captures(F);
-  if (C) rebuild_captures(C);
+  rebuild_captures_impl(F);
+  if (C) rebuild_captures_impl(C);
 }
 
 tmk_status build_link(CFLink* k) {
@@ -835,6 +835,8 @@ double snap_alpha(double time, double dt, double tco, double tcn, int r) {
 // ------------------------------------------------------- level-step hooks
 namespace tmk_host {
 
+tmk_status rebuild_captures(tmk_level_s* L) { return rebuild_captures_impl(L); }
+
 tmk_status amr_pre_step(tmk_level_s* L, double time, double dt, double tco, double tcn, cudaStream_t s) {
   if (L->finer && L->nfault && L->ctx->nb > 0) {
     if (L->prec == TMK_PREC_MIXED)
@@ -888,6 +890,7 @@ void amr_release(tmk_level_s* L) {
 extern "C" tmk_status tmk_level_attach_coarser(tmk_level* fine, tmk_level* coarse, int ref_ratio) {
   if (!fine || !coarse || fine == coarse || ref_ratio < 2) return TMK_ERR_BAD_DESC;
   if (fine->nscen != 1 || coarse->nscen != 1) return TMK_ERR_UNSUPPORTED;   // ensembles step single levels
+  if (fine->graphs || coarse->graphs) return TMK_ERR_BAD_DESC;   // a recorded graph uses their lists
   if (fine->ctx->nb != coarse->ctx->nb || fine->prec != coarse->prec) return TMK_ERR_BAD_DESC;
   const int r = ref_ratio;
   for (int d = 0; d < 2; ++d)
@@ -907,7 +910,7 @@ extern "C" tmk_status tmk_level_attach_coarser(tmk_level* fine, tmk_level* coars
   if ((st = ensure_bold(coarse)) != TMK_OK) { free_link(k); return st; }
   fine->coarser = k;
   coarse->finer = k;
-  if ((st = rebuild_captures(fine)) != TMK_OK || (st = rebuild_captures(coarse)) != TMK_OK) {
+  if ((st = rebuild_captures_impl(fine)) != TMK_OK || (st = rebuild_captures_impl(coarse)) != TMK_OK) {
     detach(fine);
     return st;
   }
@@ -916,6 +919,7 @@ extern "C" tmk_status tmk_level_attach_coarser(tmk_level* fine, tmk_level* coars
 
 extern "C" tmk_status tmk_level_detach_coarser(tmk_level* fine) {
   if (!fine) return TMK_ERR_BAD_DESC;
+  if (fine->graphs || (fine->coarser && fine->coarser->C->graphs)) return TMK_ERR_BAD_DESC;
   detach(fine);
   return TMK_OK;
 }
@@ -1095,6 +1099,8 @@ struct tmk_graph_s {
   double span = 0.0;                     // time advanced by one replay
   double dt0 = 0.0;                      // coarse step of an AMR graph
   tmk_amr* amr = nullptr;                // hierarchy whose host clock a replay advances
+  std::vector<tmk_level_s*> levels;      // levels whose kernels the graph launches (their work
+                                         // lists stay fixed while it exists)
 };
 
 namespace {
@@ -1105,15 +1111,17 @@ tmk_status graph_finish(tmk_graph_s* g) {
   if (cudaGraphGetNodes(g->graph, nullptr, &n) != cudaSuccess) return TMK_ERR_CUDA;
   std::vector<cudaGraphNode_t> nodes(n);
   if (n && cudaGraphGetNodes(g->graph, nodes.data(), &n) != cudaSuccess) return TMK_ERR_CUDA;
-  const void* f32 = tmk::Launch<float>::fault_entry();
-  const void* f64 = tmk::Launch<double>::fault_entry();
+  const void* fe[4] = {tmk::Launch<float>::fault_entry(tmk::FAULT_SEG),
+                       tmk::Launch<float>::fault_entry(tmk::FAULT_SEG_SMALL),
+                       tmk::Launch<double>::fault_entry(tmk::FAULT_SEG),
+                       tmk::Launch<double>::fault_entry(tmk::FAULT_SEG_SMALL)};
   for (cudaGraphNode_t nd : nodes) {
     cudaGraphNodeType t;
     if (cudaGraphNodeGetType(nd, &t) != cudaSuccess) return TMK_ERR_CUDA;
     if (t != cudaGraphNodeTypeKernel) continue;
     cudaKernelNodeParams p;
     if (cudaGraphKernelNodeGetParams(nd, &p) != cudaSuccess) return TMK_ERR_CUDA;
-    if (p.func != f32 && p.func != f64) continue;
+    if (p.func != fe[0] && p.func != fe[1] && p.func != fe[2] && p.func != fe[3]) continue;
     g->tnodes.push_back(nd);
     g->tbase.push_back(*(const double*)p.kernelParams[3]);
   }
@@ -1122,6 +1130,7 @@ tmk_status graph_finish(tmk_graph_s* g) {
 
 void graph_free(tmk_graph_s* g) {
   if (!g) return;
+  for (tmk_level_s* L : g->levels) --L->graphs;
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   delete g;
@@ -1158,6 +1167,8 @@ extern "C" tmk_status tmk_level_graph_create(tmk_level* L, int nsteps, double ti
   if (st != TMK_OK) { graph_free(g); return st; }
   g->t0 = time;
   g->span = nsteps * dt;
+  g->levels.push_back(L);
+  ++L->graphs;
   *out = g;
   return TMK_OK;
 }
@@ -1193,6 +1204,7 @@ extern "C" tmk_status tmk_amr_graph_create(tmk_amr* h, int ncoarse, double dt0, 
   g->span = ncoarse * dt0;
   g->dt0 = dt0;
   g->amr = h;
+  for (tmk_level* L : h->L) { g->levels.push_back(L); ++L->graphs; }
   *out = g;
   return TMK_OK;
 }

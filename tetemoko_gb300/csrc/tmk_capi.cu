@@ -145,7 +145,8 @@ size_t align_up(size_t n) { return (n + 255) & ~(size_t)255; }
 // `wait_rows` extra rows and is shortened by as many.
 constexpr int kMinRun = 16;
 void make_march_items(std::vector<tmk::MarchItem>& out, std::vector<tmk::MarchItem>& fault_rows,
-                      const std::vector<tmk_box>& boxes, const std::vector<int>& fault, int slots, int wait_rows) {
+                      const std::vector<tmk_box>& boxes, const std::vector<int>& fault, int slots, int wait_rows,
+                      int min_run) {
   long long strip_rows = 0;
   for (size_t p = 0; p < boxes.size(); ++p) {
     const tmk_box& v = boxes[p];
@@ -158,7 +159,7 @@ void make_march_items(std::vector<tmk::MarchItem>& out, std::vector<tmk::MarchIt
     const int rows = v.hi[1] - v.lo[1] + 1;
     const int w = fault[p] ? wait_rows : 0;
     int k = (int)((long long)slots * (rows + w) / std::max(1LL, strip_rows));
-    k = std::max(1, std::min(k, (rows + w + kMinRun - 1) / kMinRun));
+    k = std::max(1, std::min(k, (rows + w + min_run - 1) / min_run));
     const int run = (rows + w + k - 1) / k;
     const int first = std::min(rows, std::max(4, run - w));
     for (int x0 = v.lo[0]; x0 <= v.hi[0]; x0 += tmk::MARCH_COLS)
@@ -187,6 +188,86 @@ constexpr int kFaultWaitRows = 0;
 constexpr int kFaultDisplace = 1;
 
 bool uses_march(const tmk_scheme& s) { return s.volume_kernel != TMK_VOLUME_TILE; }
+
+tmk_tuning default_tuning(int march_allowed) {
+  tmk_tuning t;
+  t.volume_kernel = march_allowed ? TMK_VOLUME_MARCH : TMK_VOLUME_TILE;
+  t.march_waves[0] = t.march_waves[1] = 1;
+  t.min_run = kMinRun;
+  t.fault_displace = kFaultDisplace;
+  t.fault_seg = tmk::FAULT_SEG;
+  return t;
+}
+
+bool tuning_ok(const tmk_level_s* L, const tmk_tuning& t) {
+  if (t.volume_kernel != TMK_VOLUME_MARCH && t.volume_kernel != TMK_VOLUME_TILE) return false;
+  if (t.volume_kernel == TMK_VOLUME_MARCH && !L->march_allowed) return false;
+  for (int g = 0; g < 2; ++g)
+    if (t.march_waves[g] < 1 || t.march_waves[g] > 8) return false;
+  if (t.min_run < 4 || t.min_run > 4096 || t.fault_displace < 0 || t.fault_displace > 4) return false;
+  return t.fault_seg == tmk::FAULT_SEG || t.fault_seg == tmk::FAULT_SEG_SMALL;
+}
+
+// Free a device allocation the level owns.
+template <typename T>
+void level_free(tmk_level_s* L, T*& p) {
+  if (!p) return;
+  void* v = (void*)p;
+  cudaFree(v);
+  L->allocs.erase(std::remove(L->allocs.begin(), L->allocs.end(), v), L->allocs.end());
+  p = nullptr;
+}
+
+// The marching work lists of both component groups under the level's tuning:
+// group g's list holds about march_waves[g] waves of its kernel's resident
+// warps; the antiplane kernel shares the SMs with the fault kernel, leaving
+// fault_displace CTA slots per fault-kernel CTA.
+tmk_status build_march_lists(tmk_level_s* L) {
+  const int npatch = (int)L->patches.size();
+  const tmk_tuning& tu = L->tune;
+  const int seg = tu.fault_seg;
+  std::vector<int> fault_flags(npatch, 0);
+  std::vector<tmk_box> boxes(npatch);
+  int fault_ctas = 0;
+  for (int p = 0; p < npatch; ++p) {
+    boxes[p] = L->patches[p].valid;
+    if (L->patches[p].fault) {
+      fault_flags[p] = 1;
+      fault_ctas += (boxes[p].hi[0] - boxes[p].lo[0] + seg) / seg;
+    }
+  }
+  const size_t rs = real_size(L->prec);
+  const int warps = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_warps()
+                                               : tmk::Launch<double>::march_warps();
+  for (int g = 0; g < 2; ++g) {
+    level_free(L, L->ditems[g]);
+    level_free(L, L->dfrows[g]);
+    level_free(L, L->stash[g]);
+    int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots(g)
+                                          : tmk::Launch<double>::march_slots(g);
+    slots *= tu.march_waves[g];
+    if (g == 1) slots = std::max(warps, slots - tu.fault_displace * warps * fault_ctas);
+    std::vector<tmk::MarchItem> items, frows;
+    make_march_items(items, frows, boxes, fault_flags, slots, g == 0 && fault_ctas ? kFaultWaitRows : 0,
+                     tu.min_run);
+    L->nitems[g] = (int)items.size();
+    L->hitems[g] = items;
+    L->hfrows[g] = frows;
+    if (dalloc(&L->ditems[g], items.size()) != cudaSuccess) return TMK_ERR_ALLOC;
+    L->allocs.push_back(L->ditems[g]);
+    TMK_CU(cudaMemcpy(L->ditems[g], items.data(), items.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
+    L->nfrows[g] = (int)frows.size();
+    if (!frows.empty()) {
+      if (dalloc(&L->dfrows[g], frows.size()) != cudaSuccess) return TMK_ERR_ALLOC;
+      L->allocs.push_back(L->dfrows[g]);
+      TMK_CU(cudaMemcpy(L->dfrows[g], frows.data(), frows.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
+      const size_t bytes = frows.size() * tmk::MARCH_STASH_VECS * (g == 0 ? 6 : 3) * 32 * 2 * rs;
+      if (cudaMalloc(&L->stash[g], bytes) != cudaSuccess) return TMK_ERR_ALLOC;
+      L->allocs.push_back(L->stash[g]);
+    }
+  }
+  return TMK_OK;
+}
 
 }  // namespace
 
@@ -260,7 +341,7 @@ extern "C" tmk_status tmk_patch_update_state(tmk_context* c, const tmk_fab* U, c
   if (Fy) TMK_CU(cudaMemsetAsync(Fy->data, 0, (size_t)TMK_NCOMP * nvx * (nvy + 1) * sizeof(double), s));
   const PatchDev<double>* dpd = (const PatchDev<double>*)(base + off_pd);
   if (fault)
-    TMK_CU(tmk::Launch<double>::fault(dpd, (const int*)(base + off_fp), 1, nvx, c->dp, time, c->dstatus, false, s));
+    TMK_CU(tmk::Launch<double>::fault(dpd, (const int*)(base + off_fp), 1, nvx, c->dp, time, c->dstatus, false, tmk::FAULT_SEG, s));
   TMK_CU(tmk::Launch<double>::volume(dpd, (const TileDev*)(base + off_tl), (int)tiles.size(), c->dp, s));
   // the volume kernel writes the nine evolving components of each side;
   // lambda and gamma are left untouched, as updateState leaves them
@@ -460,41 +541,10 @@ tmk_status level_create_impl(tmk_context* const* ctxs, int nscen, const tmk_box*
   L->htiles = tiles;
   L->march_allowed = uses_march(c->scheme) ? 1 : 0;
   L->march = L->march_allowed;
-  if (L->march) {
-    // one work list per component group, each one wave of that kernel's
-    // resident warps; the antiplane kernel shares the SMs with the fault kernel
-    std::vector<int> fault_flags(npatch, 0);
-    int fault_ctas = 0;
-    for (int p = 0; p < npatch; ++p)
-      if (L->patches[p].fault) {
-        fault_flags[p] = 1;
-        fault_ctas += (boxes[p].hi[0] - boxes[p].lo[0] + tmk::FAULT_SEG) / tmk::FAULT_SEG;
-      }
-    const int warps = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_warps()
-                                                 : tmk::Launch<double>::march_warps();
-    for (int g = 0; g < 2; ++g) {
-      int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots(g)
-                                            : tmk::Launch<double>::march_slots(g);
-      if (g == 1) slots = std::max(warps, slots - kFaultDisplace * warps * fault_ctas);
-      std::vector<tmk::MarchItem> items, frows;
-      make_march_items(items, frows, std::vector<tmk_box>(boxes, boxes + npatch), fault_flags, slots,
-                       g == 0 && fault_ctas ? kFaultWaitRows : 0);
-      L->nitems[g] = (int)items.size();
-      L->hitems[g] = items;
-      L->hfrows[g] = frows;
-      if (dalloc(&L->ditems[g], items.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
-      L->allocs.push_back(L->ditems[g]);
-      TMK_CU(cudaMemcpy(L->ditems[g], items.data(), items.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
-      L->nfrows[g] = (int)frows.size();
-      if (!frows.empty()) {
-        if (dalloc(&L->dfrows[g], frows.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
-        L->allocs.push_back(L->dfrows[g]);
-        TMK_CU(cudaMemcpy(L->dfrows[g], frows.data(), frows.size() * sizeof(tmk::MarchItem), cudaMemcpyHostToDevice));
-        const size_t bytes = frows.size() * tmk::MARCH_STASH_VECS * (g == 0 ? 6 : 3) * 32 * 2 * rs;
-        if (cudaMalloc(&L->stash[g], bytes) != cudaSuccess) return fail(TMK_ERR_ALLOC);
-        L->allocs.push_back(L->stash[g]);
-      }
-    }
+  L->tune = default_tuning(L->march_allowed);
+  if (L->march_allowed) {
+    tmk_status st = build_march_lists(L);
+    if (st != TMK_OK) return fail(st);
   }
   TMK_CU(cudaMemcpy(L->dtiles, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice));
   if (L->nfault) {
@@ -638,7 +688,7 @@ tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEve
   TMK_CU(tmk::bexchange(L->dbptr, L->dblo, L->dbnx, L->dbcopies, L->nbcopies, c->nb, s));
   if (ev) TMK_CU(cudaEventRecord(ev[1], s));
   if (!L->march) {
-    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false, s));
+    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false, L->tune.fault_seg, s));
     if (ev) TMK_CU(cudaEventRecord(ev[2], s));
     TMK_CU(tmk::Launch<Real>::volume(pd, L->dtiles, L->ntiles, L->dparams, s));
     return TMK_OK;
@@ -650,13 +700,13 @@ tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEve
   mc.caps[0] = L->dmcap[0];
   mc.caps[1] = L->dmcap[1];
   if (ev) {
-    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false, s));
+    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false, L->tune.fault_seg, s));
     TMK_CU(cudaEventRecord(ev[2], s));
     TMK_CU(tmk::Launch<Real>::march(0, pd, L->ditems[0], L->nitems[0], mc, false, s));
     TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, true, s));
   } else {
     TMK_CU(tmk::Launch<Real>::march(0, pd, L->ditems[0], L->nitems[0], mc, false, s));
-    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, true, s));
+    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, true, L->tune.fault_seg, s));
     TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, true, s));
   }
   TMK_CU(tmk::Launch<Real>::march_fault_rows(pd, L->dfrows[0], L->nfrows[0], L->dfrows[1], L->nfrows[1], mc, s));
@@ -732,6 +782,173 @@ extern "C" tmk_status tmk_level_profile_read(tmk_level* L, double out[4], int* n
   for (int k = 0; k < 4; ++k) out[k] = L->prof_n ? acc[k] / L->prof_n : 0.0;
   if (nsteps) *nsteps = L->prof_n;
   return TMK_OK;
+}
+
+// ------------------------------------------------------------------ tuning
+extern "C" tmk_status tmk_level_get_tuning(const tmk_level* L, tmk_tuning* out) {
+  if (!L || !out) return TMK_ERR_BAD_DESC;
+  *out = L->tune;
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_set_tuning(tmk_level* L, const tmk_tuning* t) {
+  if (!L || !t || !tuning_ok(L, *t) || L->graphs) return TMK_ERR_BAD_DESC;
+  TMK_CU(cudaDeviceSynchronize());
+  L->tune = *t;
+  if (L->march_allowed) {
+    tmk_status st = build_march_lists(L);
+    if (st != TMK_OK) return st;
+  }
+  L->march = L->march_allowed && t->volume_kernel == TMK_VOLUME_MARCH;
+  if (L->coarser || L->finer) return tmk_host::rebuild_captures(L);
+  TMK_CU(cudaDeviceSynchronize());
+  return TMK_OK;
+}
+
+namespace {
+
+// The level's state (each patch's input buffer and fault data) and its
+// context's status word, saved on the device for the autotuner's trials.
+struct LevelSnapshot {
+  void* buf = nullptr;
+  std::vector<size_t> uoff, ubytes, boff, bbytes;
+  size_t soff = 0;
+  int parity = 0;
+  tmk_status save(tmk_level_s* L) {
+    size_t n = 0;
+    const size_t rs = real_size(L->prec);
+    for (const LevelPatch& lp : L->patches) {
+      const size_t ub = (size_t)TMK_NCOMP * (lp.alloc.hi[0] - lp.alloc.lo[0] + 1) * (lp.alloc.hi[1] - lp.alloc.lo[1] + 1) * rs;
+      const size_t bb = lp.B ? (size_t)L->ctx->nb * lp.bnx * sizeof(double) : 0;
+      uoff.push_back(n); ubytes.push_back(ub); n += (ub + 255) / 256 * 256;
+      boff.push_back(n); bbytes.push_back(bb); n += (bb + 255) / 256 * 256;
+    }
+    soff = n;
+    n += sizeof(DevStatus);
+    TMK_CU(cudaMalloc(&buf, n));
+    parity = L->parity;
+    char* b = (char*)buf;
+    for (size_t p = 0; p < L->patches.size(); ++p) {
+      const LevelPatch& lp = L->patches[p];
+      TMK_CU(cudaMemcpy(b + uoff[p], lp.U[parity], ubytes[p], cudaMemcpyDeviceToDevice));
+      if (bbytes[p]) TMK_CU(cudaMemcpy(b + boff[p], lp.B, bbytes[p], cudaMemcpyDeviceToDevice));
+    }
+    TMK_CU(cudaMemcpy(b + soff, L->ctx->dstatus, sizeof(DevStatus), cudaMemcpyDeviceToDevice));
+    TMK_CU(cudaDeviceSynchronize());
+    return TMK_OK;
+  }
+  tmk_status restore(tmk_level_s* L) {
+    TMK_CU(cudaDeviceSynchronize());
+    L->parity = parity;
+    char* b = (char*)buf;
+    for (size_t p = 0; p < L->patches.size(); ++p) {
+      const LevelPatch& lp = L->patches[p];
+      TMK_CU(cudaMemcpy(lp.U[parity], b + uoff[p], ubytes[p], cudaMemcpyDeviceToDevice));
+      if (bbytes[p]) TMK_CU(cudaMemcpy(lp.B, b + boff[p], bbytes[p], cudaMemcpyDeviceToDevice));
+    }
+    TMK_CU(cudaMemcpy(L->ctx->dstatus, b + soff, sizeof(DevStatus), cudaMemcpyDeviceToDevice));
+    TMK_CU(cudaDeviceSynchronize());
+    return TMK_OK;
+  }
+  ~LevelSnapshot() { if (buf) cudaFree(buf); }
+};
+
+// milliseconds per step of `steps` level steps after 2 untimed ones
+tmk_status time_steps(tmk_level_s* L, double time, double dt, int steps, cudaStream_t s, cudaEvent_t e0,
+                      cudaEvent_t e1, double* ms) {
+  for (int k = 0; k < 2; ++k) {
+    tmk_status st = tmk_level_step(L, time + k * dt, dt, s, nullptr);
+    if (st != TMK_OK) return st;
+  }
+  TMK_CU(cudaEventRecord(e0, s));
+  for (int k = 0; k < steps; ++k) {
+    tmk_status st = tmk_level_step(L, time + (k + 2) * dt, dt, s, nullptr);
+    if (st != TMK_OK) return st;
+  }
+  TMK_CU(cudaEventRecord(e1, s));
+  TMK_CU(cudaEventSynchronize(e1));
+  float f = 0.f;
+  TMK_CU(cudaEventElapsedTime(&f, e0, e1));
+  *ms = f / steps;
+  return TMK_OK;
+}
+
+std::vector<tmk_tuning> tuning_candidates(const tmk_level_s* L) {
+  std::vector<tmk_tuning> out;
+  tmk_tuning t = default_tuning(L->march_allowed);
+  for (int seg : {tmk::FAULT_SEG, tmk::FAULT_SEG_SMALL}) {
+    t.fault_seg = seg;
+    if (L->march_allowed) {
+      t.volume_kernel = TMK_VOLUME_MARCH;
+      for (int w0 : {1, 2})
+        for (int w1 : {1, 2})
+          for (int run : {8, 16, 32})
+            for (int disp : {0, 1, 2}) {
+              t.march_waves[0] = w0; t.march_waves[1] = w1; t.min_run = run; t.fault_displace = disp;
+              out.push_back(t);
+            }
+    }
+    tmk_tuning tt = default_tuning(L->march_allowed);
+    tt.volume_kernel = TMK_VOLUME_TILE;
+    tt.fault_seg = seg;
+    out.push_back(tt);
+  }
+  return out;
+}
+
+}  // namespace
+
+extern "C" tmk_status tmk_level_autotune(tmk_level* L, double time, double dt, int steps, void* stream,
+                                         tmk_tuning* best, double* ms_per_step) {
+  if (!L || !(dt > 0) || steps < 1) return TMK_ERR_BAD_DESC;
+  if (L->coarser || L->finer || L->graphs || L->prof_on) return TMK_ERR_BAD_DESC;
+  cudaStream_t s = (cudaStream_t)stream;
+  TMK_CU(cudaDeviceSynchronize());
+  LevelSnapshot snap;
+  tmk_status st = snap.save(L);
+  if (st != TMK_OK) return st;
+  const tmk_tuning t0 = L->tune;
+  cudaEvent_t e0, e1;
+  TMK_CU(cudaEventCreate(&e0));
+  TMK_CU(cudaEventCreate(&e1));
+  // every candidate once, then the four fastest twice more (mean of three)
+  std::vector<tmk_tuning> cand = tuning_candidates(L);
+  std::vector<std::pair<double, int>> timed;
+  for (size_t k = 0; k < cand.size() && st == TMK_OK; ++k) {
+    double ms = 0;
+    if ((st = tmk_level_set_tuning(L, &cand[k])) != TMK_OK) break;
+    if ((st = snap.restore(L)) != TMK_OK) break;
+    if ((st = time_steps(L, time, dt, steps, s, e0, e1, &ms)) != TMK_OK) break;
+    timed.push_back({ms, (int)k});
+  }
+  std::sort(timed.begin(), timed.end());
+  const size_t top = std::min<size_t>(4, timed.size());
+  for (size_t r = 0; r < 2 && st == TMK_OK; ++r)
+    for (size_t q = 0; q < top && st == TMK_OK; ++q) {
+      double ms = 0;
+      if ((st = tmk_level_set_tuning(L, &cand[timed[q].second])) != TMK_OK) break;
+      if ((st = snap.restore(L)) != TMK_OK) break;
+      if ((st = time_steps(L, time, dt, steps, s, e0, e1, &ms)) != TMK_OK) break;
+      timed[q].first += ms;
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  tmk_tuning pick = t0;
+  double pick_ms = 0.0;
+  if (st == TMK_OK && top) {
+    size_t b = 0;
+    for (size_t q = 1; q < top; ++q) if (timed[q].first < timed[b].first) b = q;
+    pick = cand[timed[b].second];
+    pick_ms = timed[b].first / 3.0;
+  }
+  tmk_status st2 = tmk_level_set_tuning(L, &pick);
+  tmk_status st3 = snap.restore(L);
+  if (st == TMK_OK) st = st2 != TMK_OK ? st2 : st3;
+  if (st == TMK_OK) {
+    if (best) *best = pick;
+    if (ms_per_step) *ms_per_step = pick_ms;
+  }
+  return st;
 }
 
 extern "C" int tmk_level_launches_per_step(const tmk_level* L) {

@@ -69,6 +69,8 @@ struct tmk_context_s {
 struct tmk_level_s {
   tmk_context* ctx = nullptr;              // the (first) scenario's context
   int nscen = 1;                           // scenarios of an ensemble level
+  tmk_tuning tune;                         // work-list shapes and kernel variants
+  int graphs = 0;                          // recorded graphs that launch this level's kernels
   tmk::DevParams* dparams = nullptr;       // device parameters per scenario (ctx->dp for one)
   tmk_box domain;
   double dx = 0;
@@ -117,6 +119,8 @@ struct tmk_level_s {
 namespace tmk_host {
 // tmk_capi.cu
 tmk_status upload_patchdev(tmk_level_s* L, cudaStream_t s);
+// tmk_amr.cu: the capture lists of a level's coarse-fine faces (after its work lists change)
+tmk_status rebuild_captures(tmk_level_s* L);
 // tmk_amr.cu: the coarse-fine parts of a level step
 tmk_status amr_pre_step(tmk_level_s* L, double time, double dt, double tco, double tcn, cudaStream_t s);
 tmk_status amr_post_step(tmk_level_s* L, double dt, cudaStream_t s);

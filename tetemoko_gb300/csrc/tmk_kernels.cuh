@@ -114,25 +114,30 @@ TMK_D void xface_state(const DevParams& P, const Consts<T>& k, int f, int dlo0, 
   else riemann<0, T>(k, T(1), WPl, WMr, g);
 }
 
-// One CTA per segment of FAULT_SEG fault faces of a fault patch.  The
+// One CTA of NT threads per segment of SEG fault faces of a fault patch.  The
 // predictors of the fault row are computed once per cell and side, in
 // parallel, into shared memory; one thread per face then runs the friction
-// solves, whose Newton iterations are sequential by nature.
+// solves, whose Newton iterations are sequential by nature.  Two variants:
+// 32 faces on 4 warps (the default) and 16 faces on 2 warps (twice the CTAs
+// for short fault rows); the level's tuning picks one.
 constexpr int FAULT_SEG = 32;
 constexpr int FAULT_THREADS = 128;
+constexpr int FAULT_SEG_SMALL = 16;
+constexpr int FAULT_THREADS_SMALL = 64;
 
-template <typename Real>
-__global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Real>* __restrict__ patches,
-                                                              const int* __restrict__ fault_patches,
-                                                              const DevParams* __restrict__ params, double time,
-                                                              DevStatus* st) {
+template <typename Real, int SEG, int NT>
+__global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restrict__ patches,
+                                                   const int* __restrict__ fault_patches,
+                                                   const DevParams* __restrict__ params, double time,
+                                                   DevStatus* st) {
+  static_assert(NT > SEG + 2, "the x-face threads need the threads beyond the face threads");
   using T = Real;
   // the mixed form solves the friction equation in z = asinh(beta V); the FP64
   // form keeps the reference's Newton iteration on V
   constexpr bool kZSolve = !std::is_same<Real, double>::value;
-  constexpr int NCELL = FAULT_SEG + 2;       // cells / faces [s0-1, s0+FAULT_SEG]
+  constexpr int NCELL = SEG + 2;             // cells / faces [s0-1, s0+SEG]
   __shared__ T xWM[2][NCELL][NSIDE], xWP[2][NCELL][NSIDE];
-  __shared__ T H1x[2][FAULT_SEG + 1][NSIDE];
+  __shared__ T H1x[2][SEG + 1][NSIDE];
   __shared__ double sWi[NCELL][NC];
   __shared__ double sTmp[NCELL];
   // the kernel launched after this one may be scheduled now (it reads none of
@@ -143,12 +148,12 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
   asm volatile("griddepcontrol.launch_dependents;");
   const PatchDev<Real> p = patches[fault_patches[blockIdx.y]];
   const DevParams& P = params[p.scen];
-  const int s0 = p.vlo0 + blockIdx.x * FAULT_SEG;
+  const int s0 = p.vlo0 + blockIdx.x * SEG;
   if (s0 > p.vhi0) {
     asm volatile("griddepcontrol.wait;" ::: "memory");
     return;
   }
-  const int s1 = min(s0 + FAULT_SEG - 1, p.vhi0);
+  const int s1 = min(s0 + SEG - 1, p.vhi0);
   // faces whose first-pass state this segment produces: its own, plus the
   // ghost faces lo-1 / hi+1 of the patch for the first / last segment
   const int fa = (s0 == p.vlo0) ? max(p.vlo0 - 1, p.dlo0) : s0;
@@ -163,7 +168,7 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
 
   // (A) x predictors of the fault-row cells [s0-1, s1+1] and y predictors of the
   //     states entering the fault faces [fa, fb], both sides
-  for (int t = tid; t < 4 * NCELL; t += FAULT_THREADS) {
+  for (int t = tid; t < 4 * NCELL; t += NT) {
     const int kind = t / (2 * NCELL), s = (t / NCELL) & 1, ci = t % NCELL;
     const int c = s0 - 1 + ci;
     if (kind == 0) {
@@ -201,8 +206,8 @@ __global__ void __launch_bounds__(FAULT_THREADS) fault_kernel(const PatchDev<Rea
     }
   } else {
     // (C) first-pass x faces [s0, s1+1] of the fault row, both sides
-    for (int t = tid - NCELL; t < 2 * (FAULT_SEG + 1); t += FAULT_THREADS - NCELL) {
-      const int s = t / (FAULT_SEG + 1), fi = t % (FAULT_SEG + 1);
+    for (int t = tid - NCELL; t < 2 * (SEG + 1); t += NT - NCELL) {
+      const int s = t / (SEG + 1), fi = t % (SEG + 1);
       const int f = s0 + fi;
       if (f > s1 + 1) continue;
       double bgd[NSIDE]; side_bg(P, s, bgd);

@@ -16,9 +16,11 @@ struct MarchItem;
 template <typename Real>
 struct Launch {
   static const int TX, TY;
-  // one thread per fault face of every fault patch; pdl as for march
+  // one thread per fault face of every fault patch, seg faces per CTA (32 or
+  // 16); pdl as for march
   static cudaError_t fault(const PatchDev<Real>* patches, const int* fault_patches, int nfault, int max_faces,
-                           const DevParams* params, double time, DevStatus* st, bool pdl, cudaStream_t s);
+                           const DevParams* params, double time, DevStatus* st, bool pdl, int seg,
+                           cudaStream_t s);
   // one CTA per (tile, side)
   static cudaError_t volume(const PatchDev<Real>* patches, const TileDev* tiles, int ntiles,
                             const DevParams* params, cudaStream_t s);
@@ -43,9 +45,9 @@ struct Launch {
   static int march_slots(int g);
   // warps per CTA of the marching kernels
   static int march_warps();
-  // the fault kernel's entry (to find its nodes in a captured graph); its
-  // fourth parameter is the step's start time
-  static const void* fault_entry();
+  // the entry of the fault kernel variant with seg faces per CTA (to find its
+  // nodes in a captured graph); its fourth parameter is the step's start time
+  static const void* fault_entry(int seg);
 };
 
 // FP64 <-> Real conversion of a FAB on the device

@@ -10,18 +10,24 @@ namespace tmk {
 template <typename Real, int TX_, int TY_, int NT_>
 struct LaunchImpl {
   static cudaError_t fault(const PatchDev<Real>* patches, const int* fp, int nfault, int max_faces,
-                           const DevParams* params, double time, DevStatus* st, bool pdl, cudaStream_t s) {
+                           const DevParams* params, double time, DevStatus* st, bool pdl, int seg,
+                           cudaStream_t s) {
     if (nfault <= 0) return cudaSuccess;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((max_faces + FAULT_SEG - 1) / FAULT_SEG, nfault);
-    cfg.blockDim = dim3(FAULT_THREADS);
+    const bool small = seg == FAULT_SEG_SMALL;
+    const int sg = small ? FAULT_SEG_SMALL : FAULT_SEG;
+    cfg.gridDim = dim3((max_faces + sg - 1) / sg, nfault);
+    cfg.blockDim = dim3(small ? FAULT_THREADS_SMALL : FAULT_THREADS);
     cfg.stream = s;
     cfg.attrs = pdl ? attr : nullptr;
     cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, fault_kernel<Real>, patches, fp, params, time, st);
+    if (small)
+      return cudaLaunchKernelEx(&cfg, fault_kernel<Real, FAULT_SEG_SMALL, FAULT_THREADS_SMALL>, patches, fp,
+                                params, time, st);
+    return cudaLaunchKernelEx(&cfg, fault_kernel<Real, FAULT_SEG, FAULT_THREADS>, patches, fp, params, time, st);
   }
   static size_t smem() { return sizeof(VolSmem<Real, TX_, TY_>); }
   static cudaError_t volume(const PatchDev<Real>* patches, const TileDev* tiles, int ntiles,
@@ -119,8 +125,8 @@ struct LaunchImpl {
   template <> const int Launch<REAL>::TY = TYV;                                                             \
   template <> cudaError_t Launch<REAL>::fault(const PatchDev<REAL>* p, const int* fp, int nf, int mf,        \
                                               const DevParams* prm, double t, DevStatus* st, bool pdl,       \
-                                              cudaStream_t s) {                                              \
-    return LaunchImpl<REAL, TXV, TYV, NTV>::fault(p, fp, nf, mf, prm, t, st, pdl, s);                        \
+                                              int seg, cudaStream_t s) {                                     \
+    return LaunchImpl<REAL, TXV, TYV, NTV>::fault(p, fp, nf, mf, prm, t, st, pdl, seg, s);                   \
   }                                                                                                          \
   template <> cudaError_t Launch<REAL>::volume(const PatchDev<REAL>* p, const TileDev* tl, int nt,          \
                                                const DevParams* prm, cudaStream_t s) {                      \
@@ -146,5 +152,8 @@ struct LaunchImpl {
   }                                                                                                          \
   template <> int Launch<REAL>::march_slots(int g) { return LaunchImpl<REAL, TXV, TYV, NTV>::march_slots(g); } \
   template <> int Launch<REAL>::march_warps() { return MARCH_WARPS; }                                        \
-  template <> const void* Launch<REAL>::fault_entry() { return (const void*)fault_kernel<REAL>; }           \
+  template <> const void* Launch<REAL>::fault_entry(int seg) {                                               \
+    return seg == FAULT_SEG_SMALL ? (const void*)fault_kernel<REAL, FAULT_SEG_SMALL, FAULT_THREADS_SMALL>     \
+                                  : (const void*)fault_kernel<REAL, FAULT_SEG, FAULT_THREADS>;               \
+  }                                                                                                          \
   }

@@ -150,7 +150,7 @@ extern "C" tmk_status tmk_patch_update_state_noalloc(tmk_context* c, const tmk_f
   TMK_CU(cudaGetLastError());
   if (Fx) TMK_CU(cudaMemsetAsync(Fx->data, 0, (size_t)TMK_NCOMP * (nvx + 1) * nvy * sizeof(double), s));
   if (Fy) TMK_CU(cudaMemsetAsync(Fy->data, 0, (size_t)TMK_NCOMP * nvx * (nvy + 1) * sizeof(double), s));
-  if (fault) TMK_CU(tmk::Launch<double>::fault(dpd, dfi, 1, nvx, cv.dp, time, cv.st, false, s));
+  if (fault) TMK_CU(tmk::Launch<double>::fault(dpd, dfi, 1, nvx, cv.dp, time, cv.st, false, tmk::FAULT_SEG, s));
   TMK_CU(tmk::Launch<double>::volume(dpd, dtl, ntiles, cv.dp, s));
   for (int sd = 0; sd < 2; ++sd)
     TMK_CU(tmk::copy_valid(pd.Uout, U->data, pd.alo0, pd.alo1, anx, any, pd.vlo0, pd.vlo1, pd.vhi0, pd.vhi1,

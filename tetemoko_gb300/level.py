@@ -301,6 +301,24 @@ class LinElastLevelGodunov:
         A.check(self.lib.tmk_level_graph_create(self.h, nsteps, time, dt, C.byref(h)), "tmk_level_graph_create")
         return StepGraph(self.lib, h)
 
+    def tuning(self) -> A.Tuning:
+        t = A.Tuning()
+        A.check(self.lib.tmk_level_get_tuning(self.h, C.byref(t)), "tmk_level_get_tuning")
+        return t
+
+    def set_tuning(self, t: A.Tuning):
+        """Work-list shape and kernel variants (rebuilds the work lists)."""
+        A.check(self.lib.tmk_level_set_tuning(self.h, C.byref(t)), "tmk_level_set_tuning")
+
+    def autotune(self, time: float, dt: float, steps: int = 8, stream=None):
+        """Time the candidate tunings on the level's present state, keep the
+        fastest and put the state back.  Returns (tuning, ms per step)."""
+        t = A.Tuning()
+        ms = C.c_double(0.0)
+        A.check(self.lib.tmk_level_autotune(self.h, time, dt, steps, _stream_ptr(stream), C.byref(t), C.byref(ms)),
+                "tmk_level_autotune")
+        return t, ms.value
+
     def profile(self, enable: bool, max_steps: int = 0):
         A.check(self.lib.tmk_level_profile(self.h, int(enable), max_steps), "tmk_level_profile")
 
