@@ -277,22 +277,15 @@ def amr_measurement(steps, warmup, stream, autotune=True):
     # base level's faces; finer faces take their coarse face's values
     for l in range(4):
         levels[l].set_level_friction(S.friction_field(sc, seed=4001, amp=0.1, refine=2 ** l))
-    # each level's tuning from the autotuner, run on a standalone copy of the
-    # level (an attached level steps only inside its hierarchy)
-    tunings = []
-    if autotune:
-        for l in range(4):
-            probe = LinElastLevelGodunov(ctx, boxes_all[l], domain=levels[l].domain, dx=levels[l].dx)
-            Us, Bs = levels[l].get_patches()
-            probe.set_patches(Us, Bs)
-            probe.set_level_friction(S.friction_field(sc, seed=4001, amp=0.1, refine=2 ** l))
-            t, _ = probe.autotune(0.0, sc.dt() / 2 ** l, steps=4, stream=stream)
-            probe.close()
-            levels[l].set_tuning(t)
-            tunings.append(t.as_dict())
     torch.cuda.synchronize()
     h = AMRHierarchy(levels, [2, 2, 2])
     dt0 = sc.dt()
+    # every level's tuning from the hierarchy autotuner (whole coarse steps
+    # timed from the initial state, which it puts back)
+    tunings = []
+    if autotune:
+        ts, _ = h.autotune(dt0, ncoarse=2, stream=stream)
+        tunings = [t.as_dict() for t in ts]
     for _ in range(warmup):
         h.step(dt0, stream)
     graph = h.graph(2, dt0)

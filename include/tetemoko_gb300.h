@@ -348,6 +348,15 @@ tmk_status tmk_amr_create(int nlevels, tmk_level* const* levels, const int* rati
                           tmk_amr** out);
 void       tmk_amr_destroy(tmk_amr* amr);
 tmk_status tmk_amr_step(tmk_amr* amr, double dt0, void* stream);
+/* Hierarchy autotuner: for each level, finest first, times every candidate
+ * tuning (as tmk_level_autotune, runs of 16 or 32 rows) over `ncoarse` whole
+ * subcycled coarse steps after one untimed one, keeps the fastest, and puts
+ * the hierarchy's state and clock back as they were.  per_level (optional,
+ * one entry per level) receives the choices, *ms_per_coarse_step (optional)
+ * the final time.  Synchronous on `stream`; TMK_ERR_BAD_DESC while a recorded
+ * graph launches the hierarchy's kernels. */
+tmk_status tmk_amr_autotune(tmk_amr* amr, double dt0, int ncoarse, void* stream, tmk_tuning* per_level,
+                            double* ms_per_coarse_step);
 tmk_status tmk_amr_time(const tmk_amr* amr, int level, double* time);
 /* Cell-updates of one tmk_amr_step: sum over levels of valid cells x substeps. */
 long long  tmk_amr_cell_updates(const tmk_amr* amr);

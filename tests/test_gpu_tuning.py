@@ -158,3 +158,39 @@ def test_tuning_an_attached_level_keeps_the_hierarchy_step(cuda_lib):
         for p in range(len(a.boxes)):
             np.testing.assert_array_equal(a.U[p][:, G:-G, G:-G], b.U[p][:, G:-G, G:-G])
     ctx.close()
+
+
+def test_hierarchy_autotune_keeps_the_state_and_the_steps(cuda_lib):
+    """The hierarchy autotuner puts the levels' state and the clock back, and
+    the tuned hierarchy steps as the untuned one (bit for bit unless it picked
+    the tile kernel for a level)."""
+    from tetemoko_gb300.amr import AMRHierarchy
+    from tetemoko_gb300.level import Context
+    from tests.test_gpu_amr import _levels_on_gpu, _read
+    sc = S.rate_state(nx=64, ny=32, dx=0.1)
+    datas = H.hierarchy(sc, np.random.default_rng(44), nlev=3)
+    ctx = Context(sc)
+    la, lb = _levels_on_gpu(ctx, datas), _levels_on_gpu(ctx, datas)
+    ha, hb = AMRHierarchy(la, [2, 2]), AMRHierarchy(lb, [2, 2])
+    ts, ms = hb.autotune(sc.dt(), ncoarse=1)
+    assert ms > 0 and len(ts) == 3
+    assert hb.time(0) == 0.0 and hb.time(2) == 0.0
+    for lv, d in zip(lb, datas):
+        r = _read(lv, d)
+        for p in range(len(d.boxes)):
+            np.testing.assert_array_equal(r.U[p][:, G:-G, G:-G], d.U[p][:, G:-G, G:-G])
+    for _ in range(2):
+        ha.step(sc.dt())
+        hb.step(sc.dt())
+    tile = any(t.volume_kernel == A.TMK_VOLUME_TILE for t in ts)
+    for a, b, d in zip(la, lb, datas):
+        ra, rb = _read(a, d), _read(b, d)
+        for p in range(len(d.boxes)):
+            if tile:
+                assert rel_err(rb.U[p][:, G:-G, G:-G], ra.U[p][:, G:-G, G:-G]) <= 1e-12
+            else:
+                np.testing.assert_array_equal(rb.U[p][:, G:-G, G:-G], ra.U[p][:, G:-G, G:-G])
+    ha.close(); hb.close()
+    for lv in la + lb:
+        lv.close()
+    ctx.close()

@@ -132,6 +132,7 @@ def lib() -> C.CDLL:
     L.tmk_level_destroy.argtypes = [vp]
     L.tmk_level_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.tmk_level_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.tmk_amr_autotune.argtypes = [vp, C.c_double, C.c_int, vp, C.POINTER(Tuning), dp]
     L.tmk_level_autotune.argtypes = [vp, C.c_double, C.c_double, C.c_int, vp, C.POINTER(Tuning), dp]
     L.tmk_level_set_fault_friction.argtypes = [vp, C.c_int, vp, C.c_int]
     L.tmk_ensemble_create.argtypes = [C.c_int, C.POINTER(vp), C.POINTER(Box), C.c_double, C.c_int,

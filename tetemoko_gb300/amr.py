@@ -41,6 +41,17 @@ class AMRHierarchy:
     def step(self, dt0: float, stream=None):
         A.check(self.lib.tmk_amr_step(self.h, dt0, _stream_ptr(stream)), "tmk_amr_step")
 
+    def autotune(self, dt0: float, ncoarse: int = 2, stream=None):
+        """Pick every level's tuning by timing whole subcycled coarse steps
+        (levels one at a time, finest first); the hierarchy's state and clock
+        are put back.  Returns (tunings per level, ms per coarse step)."""
+        n = len(self.levels)
+        out = (A.Tuning * n)()
+        ms = C.c_double(0.0)
+        A.check(self.lib.tmk_amr_autotune(self.h, dt0, ncoarse, _stream_ptr(stream), out, C.byref(ms)),
+                "tmk_amr_autotune")
+        return [out[k] for k in range(n)], ms.value
+
     def time(self, level: int = 0) -> float:
         t = C.c_double(0.0)
         A.check(self.lib.tmk_amr_time(self.h, level, C.byref(t)), "tmk_amr_time")

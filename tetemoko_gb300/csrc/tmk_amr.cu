@@ -1045,6 +1045,89 @@ tmk_status amr_advance(tmk_amr* h, int l, double dt, cudaStream_t s) {
 }
 }  // namespace
 
+// Hierarchy autotuner: coordinate descent over the levels, finest first; each
+// candidate tuning of a level is timed over whole subcycled coarse steps from
+// the hierarchy's present state (put back before every trial and at the end).
+extern "C" tmk_status tmk_amr_autotune(tmk_amr* h, double dt0, int ncoarse, void* stream, tmk_tuning* per_level,
+                                       double* ms_per_coarse_step) {
+  if (!h || !(dt0 > 0) || ncoarse < 1) return TMK_ERR_BAD_DESC;
+  for (tmk_level* L : h->L) if (L->graphs || L->prof_on) return TMK_ERR_BAD_DESC;
+  cudaStream_t s = (cudaStream_t)stream;
+  TMK_CU(cudaDeviceSynchronize());
+  const size_t nl = h->L.size();
+  std::vector<LevelSnapshot> snaps(nl);
+  for (size_t l = 0; l < nl; ++l) {
+    tmk_status st = snaps[l].save(h->L[l]);
+    if (st != TMK_OK) return st;
+  }
+  const std::vector<double> time0 = h->time, dtlast0 = h->dtlast;
+  auto restore_all = [&]() -> tmk_status {
+    for (size_t l = 0; l < nl; ++l) {
+      tmk_status st = snaps[l].restore(h->L[l]);
+      if (st != TMK_OK) return st;
+    }
+    h->time = time0;
+    h->dtlast = dtlast0;
+    return TMK_OK;
+  };
+  cudaEvent_t e0, e1;
+  TMK_CU(cudaEventCreate(&e0));
+  TMK_CU(cudaEventCreate(&e1));
+  auto trial = [&](double* ms) -> tmk_status {
+    tmk_status st = restore_all();
+    if (st == TMK_OK) st = amr_advance(h, 0, dt0, s);
+    if (st != TMK_OK) return st;
+    TMK_CU(cudaEventRecord(e0, s));
+    for (int k = 0; k < ncoarse; ++k)
+      if ((st = amr_advance(h, 0, dt0, s)) != TMK_OK) return st;
+    TMK_CU(cudaEventRecord(e1, s));
+    TMK_CU(cudaEventSynchronize(e1));
+    float f = 0.f;
+    TMK_CU(cudaEventElapsedTime(&f, e0, e1));
+    *ms = f / ncoarse;
+    return TMK_OK;
+  };
+  tmk_status st = TMK_OK;
+  double best_ms = 0.0;
+  for (int l = (int)nl - 1; l >= 0 && st == TMK_OK; --l) {
+    tmk_level_s* L = h->L[l];
+    const tmk_tuning keep = L->tune;
+    std::vector<tmk_tuning> cand = tuning_candidates(L, true);
+    std::vector<std::pair<double, int>> timed;
+    for (size_t k = 0; k < cand.size() && st == TMK_OK; ++k) {
+      double ms = 0.0;
+      if ((st = tmk_level_set_tuning(L, &cand[k])) != TMK_OK) break;
+      if ((st = trial(&ms)) != TMK_OK) break;
+      timed.push_back({ms, (int)k});
+    }
+    if (st != TMK_OK) { tmk_level_set_tuning(L, &keep); break; }
+    std::sort(timed.begin(), timed.end());
+    const size_t top = std::min<size_t>(3, timed.size());
+    for (size_t r = 0; r < 2 && st == TMK_OK; ++r)
+      for (size_t q = 0; q < top && st == TMK_OK; ++q) {
+        double ms = 0.0;
+        if ((st = tmk_level_set_tuning(L, &cand[timed[q].second])) != TMK_OK) break;
+        if ((st = trial(&ms)) != TMK_OK) break;
+        timed[q].first += ms;
+      }
+    size_t b = 0;
+    for (size_t q = 1; q < top; ++q) if (timed[q].first < timed[b].first) b = q;
+    const tmk_tuning pick = st == TMK_OK ? cand[timed[b].second] : keep;
+    best_ms = timed[b].first / 3.0;
+    tmk_status st2 = tmk_level_set_tuning(L, &pick);
+    if (st == TMK_OK) st = st2;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  tmk_status st3 = restore_all();
+  if (st == TMK_OK) st = st3;
+  if (st == TMK_OK) {
+    if (per_level) for (size_t l = 0; l < nl; ++l) per_level[l] = h->L[l]->tune;
+    if (ms_per_coarse_step) *ms_per_coarse_step = best_ms;
+  }
+  return st;
+}
+
 extern "C" tmk_status tmk_amr_step(tmk_amr* h, double dt0, void* stream) {
   if (!h || !(dt0 > 0)) return TMK_ERR_BAD_DESC;
   return amr_advance(h, 0, dt0, (cudaStream_t)stream);

@@ -807,52 +807,6 @@ extern "C" tmk_status tmk_level_set_tuning(tmk_level* L, const tmk_tuning* t) {
 
 namespace {
 
-// The level's state (each patch's input buffer and fault data) and its
-// context's status word, saved on the device for the autotuner's trials.
-struct LevelSnapshot {
-  void* buf = nullptr;
-  std::vector<size_t> uoff, ubytes, boff, bbytes;
-  size_t soff = 0;
-  int parity = 0;
-  tmk_status save(tmk_level_s* L) {
-    size_t n = 0;
-    const size_t rs = real_size(L->prec);
-    for (const LevelPatch& lp : L->patches) {
-      const size_t ub = (size_t)TMK_NCOMP * (lp.alloc.hi[0] - lp.alloc.lo[0] + 1) * (lp.alloc.hi[1] - lp.alloc.lo[1] + 1) * rs;
-      const size_t bb = lp.B ? (size_t)L->ctx->nb * lp.bnx * sizeof(double) : 0;
-      uoff.push_back(n); ubytes.push_back(ub); n += (ub + 255) / 256 * 256;
-      boff.push_back(n); bbytes.push_back(bb); n += (bb + 255) / 256 * 256;
-    }
-    soff = n;
-    n += sizeof(DevStatus);
-    TMK_CU(cudaMalloc(&buf, n));
-    parity = L->parity;
-    char* b = (char*)buf;
-    for (size_t p = 0; p < L->patches.size(); ++p) {
-      const LevelPatch& lp = L->patches[p];
-      TMK_CU(cudaMemcpy(b + uoff[p], lp.U[parity], ubytes[p], cudaMemcpyDeviceToDevice));
-      if (bbytes[p]) TMK_CU(cudaMemcpy(b + boff[p], lp.B, bbytes[p], cudaMemcpyDeviceToDevice));
-    }
-    TMK_CU(cudaMemcpy(b + soff, L->ctx->dstatus, sizeof(DevStatus), cudaMemcpyDeviceToDevice));
-    TMK_CU(cudaDeviceSynchronize());
-    return TMK_OK;
-  }
-  tmk_status restore(tmk_level_s* L) {
-    TMK_CU(cudaDeviceSynchronize());
-    L->parity = parity;
-    char* b = (char*)buf;
-    for (size_t p = 0; p < L->patches.size(); ++p) {
-      const LevelPatch& lp = L->patches[p];
-      TMK_CU(cudaMemcpy(lp.U[parity], b + uoff[p], ubytes[p], cudaMemcpyDeviceToDevice));
-      if (bbytes[p]) TMK_CU(cudaMemcpy(lp.B, b + boff[p], bbytes[p], cudaMemcpyDeviceToDevice));
-    }
-    TMK_CU(cudaMemcpy(L->ctx->dstatus, b + soff, sizeof(DevStatus), cudaMemcpyDeviceToDevice));
-    TMK_CU(cudaDeviceSynchronize());
-    return TMK_OK;
-  }
-  ~LevelSnapshot() { if (buf) cudaFree(buf); }
-};
-
 // milliseconds per step of `steps` level steps after 2 untimed ones
 tmk_status time_steps(tmk_level_s* L, double time, double dt, int steps, cudaStream_t s, cudaEvent_t e0,
                       cudaEvent_t e1, double* ms) {
@@ -873,7 +827,13 @@ tmk_status time_steps(tmk_level_s* L, double time, double dt, int steps, cudaStr
   return TMK_OK;
 }
 
-std::vector<tmk_tuning> tuning_candidates(const tmk_level_s* L) {
+}  // namespace
+
+// Candidate tunings of a level for the autotuners: every combination of the
+// marching choices (waves per group, shortest run, fault displacement) and
+// both fault-kernel variants, plus the tile kernel; `reduced` leaves out the
+// shortest runs of 8 rows (the hierarchy autotuner times whole coarse steps).
+std::vector<tmk_tuning> tmk_host::tuning_candidates(const tmk_level_s* L, bool reduced) {
   std::vector<tmk_tuning> out;
   tmk_tuning t = default_tuning(L->march_allowed);
   for (int seg : {tmk::FAULT_SEG, tmk::FAULT_SEG_SMALL}) {
@@ -882,11 +842,13 @@ std::vector<tmk_tuning> tuning_candidates(const tmk_level_s* L) {
       t.volume_kernel = TMK_VOLUME_MARCH;
       for (int w0 : {1, 2})
         for (int w1 : {1, 2})
-          for (int run : {8, 16, 32})
+          for (int run : {8, 16, 32}) {
+            if (reduced && run == 8) continue;
             for (int disp : {0, 1, 2}) {
               t.march_waves[0] = w0; t.march_waves[1] = w1; t.min_run = run; t.fault_displace = disp;
               out.push_back(t);
             }
+          }
     }
     tmk_tuning tt = default_tuning(L->march_allowed);
     tt.volume_kernel = TMK_VOLUME_TILE;
@@ -896,6 +858,7 @@ std::vector<tmk_tuning> tuning_candidates(const tmk_level_s* L) {
   return out;
 }
 
+namespace {
 }  // namespace
 
 extern "C" tmk_status tmk_level_autotune(tmk_level* L, double time, double dt, int steps, void* stream,
@@ -912,7 +875,7 @@ extern "C" tmk_status tmk_level_autotune(tmk_level* L, double time, double dt, i
   TMK_CU(cudaEventCreate(&e0));
   TMK_CU(cudaEventCreate(&e1));
   // every candidate once, then the four fastest twice more (mean of three)
-  std::vector<tmk_tuning> cand = tuning_candidates(L);
+  std::vector<tmk_tuning> cand = tuning_candidates(L, false);
   std::vector<std::pair<double, int>> timed;
   for (size_t k = 0; k < cand.size() && st == TMK_OK; ++k) {
     double ms = 0;

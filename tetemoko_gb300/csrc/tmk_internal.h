@@ -117,6 +117,57 @@ struct tmk_level_s {
 };
 
 namespace tmk_host {
+// The level's state (each patch's input buffer and fault data) and its
+// context's status word, saved on the device for the autotuner's trials.
+struct LevelSnapshot {
+  LevelSnapshot() = default;
+  LevelSnapshot(const LevelSnapshot&) = delete;
+  LevelSnapshot& operator=(const LevelSnapshot&) = delete;
+  void* buf = nullptr;
+  std::vector<size_t> uoff, ubytes, boff, bbytes;
+  size_t soff = 0;
+  int parity = 0;
+  tmk_status save(tmk_level_s* L) {
+    size_t n = 0;
+    const size_t rs = real_size(L->prec);
+    for (const LevelPatch& lp : L->patches) {
+      const size_t ub = (size_t)TMK_NCOMP * (lp.alloc.hi[0] - lp.alloc.lo[0] + 1) * (lp.alloc.hi[1] - lp.alloc.lo[1] + 1) * rs;
+      const size_t bb = lp.B ? (size_t)L->ctx->nb * lp.bnx * sizeof(double) : 0;
+      uoff.push_back(n); ubytes.push_back(ub); n += (ub + 255) / 256 * 256;
+      boff.push_back(n); bbytes.push_back(bb); n += (bb + 255) / 256 * 256;
+    }
+    soff = n;
+    n += sizeof(tmk::DevStatus);
+    TMK_CU(cudaMalloc(&buf, n));
+    parity = L->parity;
+    char* b = (char*)buf;
+    for (size_t p = 0; p < L->patches.size(); ++p) {
+      const LevelPatch& lp = L->patches[p];
+      TMK_CU(cudaMemcpy(b + uoff[p], lp.U[parity], ubytes[p], cudaMemcpyDeviceToDevice));
+      if (bbytes[p]) TMK_CU(cudaMemcpy(b + boff[p], lp.B, bbytes[p], cudaMemcpyDeviceToDevice));
+    }
+    TMK_CU(cudaMemcpy(b + soff, L->ctx->dstatus, sizeof(tmk::DevStatus), cudaMemcpyDeviceToDevice));
+    TMK_CU(cudaDeviceSynchronize());
+    return TMK_OK;
+  }
+  tmk_status restore(tmk_level_s* L) {
+    TMK_CU(cudaDeviceSynchronize());
+    L->parity = parity;
+    char* b = (char*)buf;
+    for (size_t p = 0; p < L->patches.size(); ++p) {
+      const LevelPatch& lp = L->patches[p];
+      TMK_CU(cudaMemcpy(lp.U[parity], b + uoff[p], ubytes[p], cudaMemcpyDeviceToDevice));
+      if (bbytes[p]) TMK_CU(cudaMemcpy(lp.B, b + boff[p], bbytes[p], cudaMemcpyDeviceToDevice));
+    }
+    TMK_CU(cudaMemcpy(L->ctx->dstatus, b + soff, sizeof(tmk::DevStatus), cudaMemcpyDeviceToDevice));
+    TMK_CU(cudaDeviceSynchronize());
+    return TMK_OK;
+  }
+  ~LevelSnapshot() { if (buf) cudaFree(buf); }
+};
+
+// tmk_capi.cu: candidate tunings of a level for the autotuners
+std::vector<tmk_tuning> tuning_candidates(const tmk_level_s* L, bool reduced);
 // tmk_capi.cu
 tmk_status upload_patchdev(tmk_level_s* L, cudaStream_t s);
 // tmk_amr.cu: the capture lists of a level's coarse-fine faces (after its work lists change)
