@@ -143,6 +143,21 @@ typedef struct {
   int fault_seg;        /* fault faces per fault-kernel CTA: 32 (4 warps) or 16 (2 warps) */
 } tmk_tuning;
 
+/* Refinement tagging parameters (the comp.* keys of the input deck,
+ * execLinElast/amrGodunov.cpp:274-283, 400-440; defaults there in brackets). */
+typedef struct {
+  int    level;                /* index of the level tagged (AMRLevel::m_level) */
+  int    initial;              /* 1: tagCellsInit (fault-law marks only), 0: tagCells */
+  double refine_thresh;        /* comp.refine_thresh */
+  double plastic_thresh;       /* comp.plastic_thresh [1e-5] */
+  int    tag_buffer;           /* comp.tag_buffer_size */
+  double x_coarsen[2], y_coarsen[2];    /* comp.x_coarsen, y_coarsen [-1e40 1e40] */
+  double slope_coarsen;        /* comp.slope_coarsen [0] */
+  double width_coarsen;        /* comp.width_coarsen [1e40] */
+  double x_coarsen2[2], y_coarsen2[2];  /* comp.x_coarsen2, y_coarsen2 [-1e40 1e40] */
+  int    coarsen2_max_level;   /* comp.coarsen2_max_level [max_level] */
+} tmk_tag_params;
+
 typedef struct tmk_context_s tmk_context;
 typedef struct tmk_level_s   tmk_level;
 typedef struct tmk_amr_s     tmk_amr;
@@ -296,6 +311,24 @@ tmk_status tmk_level_set_tuning(tmk_level* lvl, const tmk_tuning* t);
  * of a hierarchy before attaching them. */
 tmk_status tmk_level_autotune(tmk_level* lvl, double time, double dt, int steps, void* stream,
                               tmk_tuning* best, double* ms_per_step);
+
+/* Refinement tags of a level (AMRLevelLinElast::tagCells / tagCellsInit,
+ * srcLinElast/AMRLevelLinElast.cpp:577-717, 721-771).  tagCells first fills
+ * the level's ghost cells from its coarser level's new state (if attached)
+ * and by exchange, then per valid cell takes the largest undivided difference
+ * of side 1's velocities in x and y (GETFULLGRADF and MAXF,
+ * srcLinElast/LinElastPhysicsF.ChF:59-82, 199-259; one-sided on the domain's
+ * edges), sets it to 1 on the fault law's nucleation cells (RSIBC/SWIBC::
+ * tagCellsInit, ibcLinElast/RSIBC.cpp:341-377, ibcLinElast/SWIBC.cpp:336-394),
+ * and tags it where it reaches the coarsening-scaled threshold or either
+ * side's plastic strain reaches plastic_thresh, within the coarsen2 window
+ * from level coarsen2_max_level on.  tagCellsInit tags the nucleation cells
+ * only.  The tags are grown by tag_buffer cells (IntVectSet::grow) and clipped
+ * to the domain.  mask: one byte per cell of the level's domain, x fastest,
+ * 1 tagged; `host` selects a host (1) or device (0) pointer.  Synchronous.
+ * TMK_ERR_UNSUPPORTED for an ensemble level. */
+tmk_status tmk_level_tag_cells(tmk_level* lvl, const tmk_tag_params* p, unsigned char* mask, int host,
+                               void* stream);
 
 /* ---------------------------------------------------------------------------
  * Coarse-fine coupling (AMRLevelLinElast::levelSetup,

@@ -68,6 +68,7 @@ def lib() -> C.CDLL:
         L.tmko_average_down.argtypes = [C.c_int, C.c_int, LV, LV]
         L.tmko_fine_interp.argtypes = [C.c_int, C.c_int, LV, LV]
         L.tmko_register_entries.argtypes = [C.c_int, LV, LV, ip]
+        L.tmko_tag_cells.argtypes = [E, S, R, W, P(A.TagParams), C.c_int, LV, LV, C.c_void_p]
         L.tmko_amr_run.argtypes = [E, S, R, W, PL, C.c_int, LV, ip, C.c_double, C.c_double, C.c_int, C.c_int]
         _lib = L
     return _lib
@@ -280,6 +281,20 @@ def fine_interp(r: int, coarse: LevelData, fine: LevelData) -> int:
     if rc == 0:
         fine._unpack(kf)
     return rc
+
+
+def tag_cells(sc, tp, fine: LevelData, coarse: LevelData | None = None, r: int = 2) -> np.ndarray:
+    """AMRLevelLinElast::tagCells / tagCellsInit of `fine` (ghost cells filled
+    in place): the tag mask over its domain, shape (ny, nx), uint8."""
+    d = fine.domain
+    mask = np.zeros((d[3] - d[1] + 1, d[2] - d[0] + 1), dtype=np.uint8)
+    f, kf = fine._pack()
+    c, kc = coarse._pack() if coarse is not None else (None, None)
+    rc = lib().tmko_tag_cells(C.byref(sc.elastic), C.byref(sc.scheme), _ref(sc.rs), _ref(sc.sw), C.byref(tp), r,
+                              C.byref(c) if c is not None else None, C.byref(f), mask.ctypes.data)
+    assert rc == 0, rc
+    fine._unpack(kf)
+    return mask
 
 
 def register_entries(r: int, coarse: LevelData, fine: LevelData) -> int:

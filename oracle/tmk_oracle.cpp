@@ -1749,6 +1749,116 @@ int tmko_average_down(int r, int nb, tmko_level* coarse, const tmko_level* fine)
   return 0;
 }
 
+// ------------------------------------------------------------- tagging --
+}  // extern "C"
+namespace {
+
+// Cells the fault law marks for refinement on row j = 0, as x ranges
+// (RSIBC::tagCellsInit, ibcLinElast/RSIBC.cpp:341-377: [floor(x0/dx), ceil(x0/dx)];
+// SWIBC::tagCellsInit, ibcLinElast/SWIBC.cpp:336-368: one range per nucleation
+// patch, [floor((c+xc-xw)/dx), ceil((c+xc+xw)/dx)], c the friction box centre).
+std::vector<std::pair<int, int>> nucleationRanges(const Phys& P, double dx) {
+  std::vector<std::pair<int, int>> out;
+  if (P.sch.fault_law == TMK_FAULT_RS) {
+    out.push_back({(int)std::floor(P.rs.x0 / dx), (int)std::ceil(P.rs.x0 / dx)});
+  } else if (P.sch.fault_law == TMK_FAULT_SW) {
+    for (int k = 0; k < P.sw.num_patches; ++k)
+      out.push_back({(int)std::floor((P.sw.fric_box_center[0] + P.sw.xc[k] - P.sw.xw[k]) / dx),
+                     (int)std::ceil((P.sw.fric_box_center[0] + P.sw.xc[k] + P.sw.xw[k]) / dx)});
+  }
+  return out;
+}
+
+// AMRLevelLinElast::tagCells / tagCellsInit (srcLinElast/AMRLevelLinElast.cpp:
+// 577-717, 721-771) on a level whose ghost cells are filled; mask over the
+// domain (x fastest), before and after IntVectSet::grow(tag_buffer) & domain.
+void tagLevel(const Phys& P, const OLevel& L, const tmk_tag_params& tp, std::vector<unsigned char>& mask) {
+  const Box& D = L.dom;
+  const int nx = D.hi[0] - D.lo[0] + 1, ny = D.hi[1] - D.lo[1] + 1;
+  std::vector<unsigned char> raw((size_t)nx * ny, 0);
+  const auto nuc = nucleationRanges(P, L.dx);
+  const bool marks = !nuc.empty();
+  for (size_t p = 0; p < L.boxes.size(); ++p) {
+    const Box& b = L.boxes[p];
+    const FAB& U = L.U[p];
+    for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+      for (int i = b.lo[0]; i <= b.hi[0]; ++i) {
+        bool nucleation = false;
+        if (j == 0) for (const auto& r : nuc) if (i >= r.first && i <= r.second) nucleation = true;
+        bool tag;
+        if (tp.initial) {
+          tag = marks && nucleation;        // markFAB > 0
+        } else {
+          // GETFULLGRADF per direction (srcLinElast/LinElastPhysicsF.ChF:199-259), side 1's velocities
+          double grad[2];
+          for (int d = 0; d < 2; ++d) {
+            const int e0 = d == 0, e1 = d == 1, k = d == 0 ? i : j;
+            double diff = 0.0;
+            if (k > D.lo[d] && k < D.hi[d]) {
+              for (int iv = 0; iv <= 2; ++iv)
+                diff = std::max(diff, 0.5 * std::fabs(U(i + e0, j + e1, iv) - U(i - e0, j - e1, iv)));
+            } else if (k == D.lo[d]) {
+              for (int iv = 0; iv <= 2; ++iv) diff = std::max(diff, std::fabs(U(i + e0, j + e1, iv) - U(i, j, iv)));
+            } else {
+              for (int iv = 0; iv <= 2; ++iv) diff = std::max(diff, std::fabs(U(i, j, iv) - U(i - e0, j - e1, iv)));
+            }
+            grad[d] = diff;
+          }
+          // MAXF (srcLinElast/LinElastPhysicsF.ChF:59-82)
+          double gm = 0.0;
+          for (int d = 0; d < 2; ++d) gm = std::max(gm, std::fabs(grad[d]));
+          if (nucleation) gm = 1.0;          // LEPhysIBC::tagCells -> tagCellsInit marks
+          const double x = i * L.dx, y = j * L.dx;
+          double r = 0;
+          r = std::max(r, std::max(tp.x_coarsen[0] - x, x - tp.x_coarsen[1]));
+          r = std::max(r, std::max(tp.y_coarsen[0] - y, y - tp.y_coarsen[1]));
+          const double thr = tp.refine_thresh * (1 + r * tp.slope_coarsen / tp.width_coarsen);
+          const bool window = tp.level < tp.coarsen2_max_level ||
+                              (x >= tp.x_coarsen2[0] && x <= tp.x_coarsen2[1] && y >= tp.y_coarsen2[0] &&
+                               y <= tp.y_coarsen2[1]);
+          tag = window && (gm >= thr || U(i, j, 10) >= tp.plastic_thresh || U(i, j, 21) >= tp.plastic_thresh);
+        }
+        if (tag) raw[(size_t)(j - D.lo[1]) * nx + (i - D.lo[0])] = 1;
+      }
+  }
+  // IntVectSet::grow(tag_buffer), then & minBox & domain
+  const int n = std::max(0, tp.tag_buffer);
+  mask.assign((size_t)nx * ny, 0);
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) {
+      if (!raw[(size_t)j * nx + i]) continue;
+      for (int jj = std::max(0, j - n); jj <= std::min(ny - 1, j + n); ++jj)
+        for (int ii = std::max(0, i - n); ii <= std::min(nx - 1, i + n); ++ii) mask[(size_t)jj * nx + ii] = 1;
+    }
+}
+
+}  // namespace
+extern "C" {
+
+// Tags of `fine` (its ghost cells first filled from `coarse`'s state at
+// alpha = 1 when given, then by exchange).  Returns 0, 1 bad arguments,
+// 3 a coarse cell the fill needs is not covered.
+int tmko_tag_cells(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_rs_params* rs,
+                   const tmk_sw_params* sw, const tmk_tag_params* tp, int r, const tmko_level* coarse,
+                   tmko_level* fine, unsigned char* mask) {
+  Phys P;
+  if (!tp || !fine || !mask || !setup(P, e, s, rs, sw, nullptr)) return 1;
+  const int nb = s->fault_law == TMK_FAULT_RS ? TMK_RS_NBDRY : (s->fault_law == TMK_FAULT_SW ? TMK_SW_NBDRY : 0);
+  OLevel F;
+  if (!loadLevel(F, *fine, nb)) return 1;
+  if (coarse && !tp->initial) {
+    OLevel C;
+    if (!loadLevel(C, *coarse, nb) || r < 1 || !alignedTo(F, r)) return 1;
+    if (!cfFillU(F, C, C.U, C.U, 1.0, r)) return 3;
+  }
+  if (!tp->initial) exchangeLevel(F);
+  std::vector<unsigned char> m;
+  tagLevel(P, F, *tp, m);
+  std::memcpy(mask, m.data(), m.size());
+  storeLevel(F, *fine);
+  return 0;
+}
+
 // Regrid prolongation of the fine valid cells from the coarse level.
 int tmko_fine_interp(int r, int nb, const tmko_level* coarse, tmko_level* fine) {
   if (!coarse || !fine || r < 1) return 1;

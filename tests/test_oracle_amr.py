@@ -188,3 +188,60 @@ def test_amr_three_levels_runs_and_stays_finite():
     for lv in levels:
         for u in lv.U:
             assert np.isfinite(u[:, G:-G, G:-G]).all()
+
+
+# ------------------------------------------------------------------ tagging
+def _level_of(sc, boxes, U_fn=None):
+    d = O.LevelData((0, 0, sc.nx - 1, sc.ny - 1), sc.dx, boxes, sc.nbdry)
+    for p, b in enumerate(d.boxes):
+        d.U[p][:] = sc.initial_U(lo=b[:2], hi=b[2:])
+        if d.B[p] is not None:
+            d.B[p][:] = sc.initial_B(xlo=b[0], xhi=b[2])
+    return d
+
+
+def test_initial_tags_are_the_nucleation_cells_grown():
+    """tagCellsInit: RS marks [floor(x0/dx), ceil(x0/dx)] on row 0; SW marks each
+    nucleation patch's range; both grown by the tag buffer and clipped to the domain."""
+    sc = S.rate_state(nx=64, ny=32, dx=0.1)
+    sc.rs.x0 = 3.25                          # between cells 32 and 33
+    m = O.tag_cells(sc, A.tag_params(initial=True, tag_buffer=1), _level_of(sc, [(0, 0, 63, 31)]))
+    want = np.zeros_like(m)
+    want[0:2, 31:35] = 1                     # cells 32..33 on row 0, grown by 1 (row -1 clipped)
+    assert np.array_equal(m, want)
+    sw = S.slip_weakening(nx=64, ny=32, dx=0.1)
+    m = O.tag_cells(sw, A.tag_params(initial=True, tag_buffer=0), _level_of(sw, [(0, 0, 31, 31), (32, 0, 63, 31)]))
+    c, xc, xw = sw.sw.fric_box_center[0], sw.sw.xc[0], sw.sw.xw[0]
+    lo, hi = int(np.floor((c + xc - xw) / sw.dx)), int(np.ceil((c + xc + xw) / sw.dx))
+    assert set(np.nonzero(m[0])[0]) == set(range(lo, hi + 1)) and m[1:].sum() == 0
+
+
+def test_gradient_tags_follow_getfullgradf():
+    """A velocity ramp of slope s cells^-1 gives undivided differences of s in
+    the interior (central) and on the domain edges (one-sided): every cell
+    tags when s >= thresh, none when s < thresh; the plastic strain and the
+    coarsening window tag as their tests say."""
+    sc = S.rate_state(nx=48, ny=24, dx=0.1)
+    sc.rs.x0 = -100.0                        # no nucleation marks inside the domain
+    boxes = [(0, 0, 23, 23), (24, 0, 47, 23)]
+    for s, expect in ((0.02, 1), (0.005, 0)):
+        d = _level_of(sc, boxes)
+        for p, b in enumerate(d.boxes):
+            i = np.arange(b[0] - 4, b[2] + 5)
+            d.U[p][1] = s * i[None, :]           # vy ramp along x
+        m = O.tag_cells(sc, A.tag_params(refine_thresh=0.01, tag_buffer=0), d)
+        assert (m == expect).all()
+    d = _level_of(sc, boxes)
+    d.U[1][21, 4 + 5, 4 + 6] = 2e-5              # side-2 plastic strain at cell (30, 5)
+    m = O.tag_cells(sc, A.tag_params(refine_thresh=0.01, tag_buffer=0), d)
+    assert m.sum() == 1 and m[5, 30] == 1
+    # coarsening: the threshold grows by slope*r/width outside [x0, x1]
+    d = _level_of(sc, boxes)
+    for p, b in enumerate(d.boxes):
+        i = np.arange(b[0] - 4, b[2] + 5)
+        d.U[p][0] = 0.02 * i[None, :]
+    tp = A.tag_params(refine_thresh=0.01, tag_buffer=0, x_coarsen=(0.0, 2.0), slope_coarsen=1.0, width_coarsen=0.1)
+    m = O.tag_cells(sc, tp, d)
+    x = np.arange(48) * sc.dx
+    thr = 0.01 * (1 + np.maximum(0.0, x - 2.0) * 1.0 / 0.1)
+    assert np.array_equal(m[0], (0.02 >= thr).astype(np.uint8))

@@ -81,6 +81,28 @@ class Tuning(C.Structure):
                 "fault_displace": self.fault_displace, "fault_seg": self.fault_seg}
 
 
+class TagParams(C.Structure):
+    _fields_ = [("level", C.c_int), ("initial", C.c_int), ("refine_thresh", C.c_double),
+                ("plastic_thresh", C.c_double), ("tag_buffer", C.c_int), ("x_coarsen", C.c_double * 2),
+                ("y_coarsen", C.c_double * 2), ("slope_coarsen", C.c_double), ("width_coarsen", C.c_double),
+                ("x_coarsen2", C.c_double * 2), ("y_coarsen2", C.c_double * 2), ("coarsen2_max_level", C.c_int)]
+
+
+def tag_params(level=0, initial=False, refine_thresh=0.01, plastic_thresh=1e-5, tag_buffer=2,
+               x_coarsen=(-1e40, 1e40), y_coarsen=(-1e40, 1e40), slope_coarsen=0.0, width_coarsen=1e40,
+               x_coarsen2=(-1e40, 1e40), y_coarsen2=(-1e40, 1e40), coarsen2_max_level=100) -> TagParams:
+    """Tagging parameters with the input deck's defaults (execLinElast/amrGodunov.cpp:274-283, 400-440)."""
+    t = TagParams()
+    t.level, t.initial, t.refine_thresh, t.plastic_thresh = level, int(initial), refine_thresh, plastic_thresh
+    t.tag_buffer, t.slope_coarsen, t.width_coarsen = tag_buffer, slope_coarsen, width_coarsen
+    t.x_coarsen[:] = list(x_coarsen)
+    t.y_coarsen[:] = list(y_coarsen)
+    t.x_coarsen2[:] = list(x_coarsen2)
+    t.y_coarsen2[:] = list(y_coarsen2)
+    t.coarsen2_max_level = coarsen2_max_level
+    return t
+
+
 class Fab(C.Structure):
     _fields_ = [("data", C.c_void_p), ("lo", C.c_int * 2), ("hi", C.c_int * 2), ("ncomp", C.c_int)]
 
@@ -134,6 +156,7 @@ def lib() -> C.CDLL:
     L.tmk_level_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.tmk_amr_autotune.argtypes = [vp, C.c_double, C.c_int, vp, C.POINTER(Tuning), dp]
     L.tmk_level_autotune.argtypes = [vp, C.c_double, C.c_double, C.c_int, vp, C.POINTER(Tuning), dp]
+    L.tmk_level_tag_cells.argtypes = [vp, C.POINTER(TagParams), vp, C.c_int, vp]
     L.tmk_level_set_fault_friction.argtypes = [vp, C.c_int, vp, C.c_int]
     L.tmk_ensemble_create.argtypes = [C.c_int, C.POINTER(vp), C.POINTER(Box), C.c_double, C.c_int,
                                       C.POINTER(Box), ip, C.POINTER(vp)]

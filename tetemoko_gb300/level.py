@@ -269,6 +269,19 @@ class LinElastLevelGodunov:
         """Copy the valid cells that this level's patches share with `src`'s."""
         A.check(self.lib.tmk_level_copy_overlap(self.h, src.h, _stream_ptr(stream)), "tmk_level_copy_overlap")
 
+    def tag_cells(self, tp, mask=None, stream=None):
+        """AMRLevelLinElast::tagCells / tagCellsInit on the device: the tag mask
+        over the level's domain, (ny, nx) uint8 (numpy, or a CUDA uint8 tensor
+        given as `mask`)."""
+        d = self.domain
+        if mask is None:
+            mask = np.zeros((d[3] - d[1] + 1, d[2] - d[0] + 1), dtype=np.uint8)
+        host = isinstance(mask, np.ndarray)
+        ptr = mask.ctypes.data if host else mask.data_ptr()
+        A.check(self.lib.tmk_level_tag_cells(self.h, C.byref(tp), ptr, 1 if host else 0, _stream_ptr(stream)),
+                "tmk_level_tag_cells")
+        return mask
+
     def register_size(self) -> int:
         n = C.c_int(0)
         A.check(self.lib.tmk_level_register_size(self.h, C.byref(n)), "tmk_level_register_size")
