@@ -161,6 +161,7 @@ typedef struct {
 typedef struct tmk_context_s tmk_context;
 typedef struct tmk_level_s   tmk_level;
 typedef struct tmk_amr_s     tmk_amr;
+typedef struct tmk_stations_s tmk_stations;
 typedef struct tmk_graph_s   tmk_graph;
 
 /* ---------------------------------------------------------------------------
@@ -329,6 +330,35 @@ tmk_status tmk_level_autotune(tmk_level* lvl, double time, double dt, int steps,
  * TMK_ERR_UNSUPPORTED for an ensemble level. */
 tmk_status tmk_level_tag_cells(tmk_level* lvl, const tmk_tag_params* p, unsigned char* mask, int host,
                                void* stream);
+
+/* Fault and body stations of a level (AMRLevelLinElast::writeStationLevel,
+ * srcLinElast/AMRLevelLinElast.cpp:1758-1869, with the cells and weights of
+ * :257-335): a fault station at x reads the fault data of faces i and i+1,
+ * i = floor((x + center[0])/dx - 0.5), as B(i)(1-w) + B(i+1)w with the
+ * reference's w = x + center[0] - (i + 0.5)dx (a distance, not divided by dx);
+ * a body station at (x, y) reads the state of the four cells from (i, j) the
+ * same way in both directions.  Each of those cells is read from the patch
+ * that holds it (the reference reads the station patch's ghost cells).  A
+ * record is the time, then nb values per fault station, then 22 per body
+ * station, NaN for a station no patch of the level holds; `capacity` records
+ * are kept on the device until read.  Destroy the stations before their level. */
+tmk_status tmk_stations_create(tmk_level* lvl, int nfault, const double* x_fault, int nbody,
+                               const double* x_body, const double* y_body, const double center[2],
+                               int capacity, tmk_stations** out);
+void       tmk_stations_destroy(tmk_stations* st);
+/* One record at `time` (asynchronous on `stream`, graph-capturable). */
+tmk_status tmk_stations_record(tmk_stations* st, double time, void* stream);
+/* Values per record (1 + values of every station) and, per station, whether a
+ * patch of the level holds it. */
+tmk_status tmk_stations_layout(const tmk_stations* st, int* values_per_record, int* present);
+/* Copy out (at most max_records) records made since the last read and start
+ * over; *dropped = records lost to a full buffer or to max_records. */
+tmk_status tmk_stations_read(tmk_stations* st, double* out, int max_records, int* nrec,
+                             long long* dropped);
+/* Record `st` at the end of every step of its level, at the level's new time,
+ * after the finer levels' substeps, reflux and average-down when the level is
+ * in a hierarchy (postTimeStep's order); st = NULL stops. */
+tmk_status tmk_level_attach_stations(tmk_level* lvl, tmk_stations* st);
 
 /* ---------------------------------------------------------------------------
  * Coarse-fine coupling (AMRLevelLinElast::levelSetup,

@@ -324,3 +324,37 @@ def tile_boxes(nx: int, ny: int, max_grid: int):
         for i0 in range(0, nx, max_grid):
             out.append((i0, j0, min(i0 + max_grid, nx) - 1, min(j0 + max_grid, ny) - 1))
     return out
+
+
+# ---------------------------------------------------------------- stations --
+def station_cell(x: float, center: float, dx: float):
+    """AMRLevelLinElast::define (srcLinElast/AMRLevelLinElast.cpp:260-335): the
+    cell below a station and the distance from its centre (the reference's
+    interpolation weight, not divided by dx)."""
+    i = int(np.floor((x + center) / dx - 0.5))
+    return i, -(i + 0.5) * dx + (x + center)
+
+
+def station_values(domain, dx, Ug, Bg, fault_x, body_xy, center=(0.0, 0.0)):
+    """AMRLevelLinElast::writeStationLevel (srcLinElast/AMRLevelLinElast.cpp:
+    1758-1869) on domain-wide arrays (Ug (22, ny+8, nx+8), Bg (nb, nx+8)): one
+    row of nb values per fault station, 22 per body station, in the
+    reference's operation order."""
+    g = A.TMK_NGHOST
+    fault, body = [], []
+    for x in fault_x:
+        i, w = station_cell(x, center[0], dx)
+        ci = i - domain[0] + g
+        fault.append([Bg[c, ci] * (1 - w) + Bg[c, ci + 1] * w for c in range(Bg.shape[0])])
+    for x, y in body_xy:
+        i, wx = station_cell(x, center[0], dx)
+        j, wy = station_cell(y, center[1], dx)
+        ci, cj = i - domain[0] + g, j - domain[1] + g
+        row = []
+        for c in range(22):
+            u = Ug[c]
+            row.append(u[cj, ci] * (1 - wx) * (1 - wy) + u[cj, ci + 1] * wx * (1 - wy)
+                       + u[cj + 1, ci] * (1 - wx) * wy + u[cj + 1, ci + 1] * wx * wy)
+        body.append(row)
+    return np.array(fault, dtype=np.float64).reshape(len(fault_x), -1), np.array(body, dtype=np.float64).reshape(
+        len(body_xy), 22)

@@ -156,6 +156,13 @@ def lib() -> C.CDLL:
     L.tmk_level_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.tmk_amr_autotune.argtypes = [vp, C.c_double, C.c_int, vp, C.POINTER(Tuning), dp]
     L.tmk_level_autotune.argtypes = [vp, C.c_double, C.c_double, C.c_int, vp, C.POINTER(Tuning), dp]
+    L.tmk_stations_create.argtypes = [vp, C.c_int, dp, C.c_int, dp, dp, dp, C.c_int, C.POINTER(vp)]
+    L.tmk_stations_destroy.argtypes = [vp]
+    L.tmk_stations_destroy.restype = None
+    L.tmk_stations_record.argtypes = [vp, C.c_double, vp]
+    L.tmk_stations_layout.argtypes = [vp, ip, ip]
+    L.tmk_stations_read.argtypes = [vp, dp, C.c_int, ip, C.POINTER(C.c_longlong)]
+    L.tmk_level_attach_stations.argtypes = [vp, vp]
     L.tmk_level_tag_cells.argtypes = [vp, C.POINTER(TagParams), vp, C.c_int, vp]
     L.tmk_level_set_fault_friction.argtypes = [vp, C.c_int, vp, C.c_int]
     L.tmk_ensemble_create.argtypes = [C.c_int, C.POINTER(vp), C.POINTER(Box), C.c_double, C.c_int,

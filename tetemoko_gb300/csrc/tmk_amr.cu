@@ -1040,6 +1040,7 @@ tmk_status amr_advance(tmk_amr* h, int l, double dt, cudaStream_t s) {
       if ((st = amr_advance(h, l + 1, dt / r, s)) != TMK_OK) return st;
     if ((st = tmk_level_reflux(h->L[l], s)) != TMK_OK) return st;
     if ((st = tmk_level_average_down(h->L[l], s)) != TMK_OK) return st;
+    if (h->L[l]->stations && (st = tmk_stations_record(h->L[l]->stations, h->time[l], s)) != TMK_OK) return st;
   }
   return TMK_OK;
 }
@@ -1176,8 +1177,9 @@ extern "C" int tmk_amr_launches_per_step(const tmk_amr* h) {
 struct tmk_graph_s {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  std::vector<cudaGraphNode_t> tnodes;   // fault-kernel nodes
+  std::vector<cudaGraphNode_t> tnodes;   // fault-kernel and station-kernel nodes
   std::vector<double> tbase;             // their time argument at capture
+  std::vector<int> nparams;              // their parameter count
   double t0 = 0.0;                       // start time at capture
   double span = 0.0;                     // time advanced by one replay
   double dt0 = 0.0;                      // coarse step of an AMR graph
@@ -1188,25 +1190,34 @@ struct tmk_graph_s {
 
 namespace {
 
+// parameter counts of fault_kernel and station_kernel
+constexpr int kFaultParams = 5;
+constexpr int kStationParams = 10;
+
 tmk_status graph_finish(tmk_graph_s* g) {
   if (cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess) return TMK_ERR_CUDA;
   size_t n = 0;
   if (cudaGraphGetNodes(g->graph, nullptr, &n) != cudaSuccess) return TMK_ERR_CUDA;
   std::vector<cudaGraphNode_t> nodes(n);
   if (n && cudaGraphGetNodes(g->graph, nodes.data(), &n) != cudaSuccess) return TMK_ERR_CUDA;
-  const void* fe[4] = {tmk::Launch<float>::fault_entry(tmk::FAULT_SEG),
+  // kernels whose fourth parameter is a time: the fault kernels (the step's
+  // start) and the station kernels (the record's time)
+  const void* fe[6] = {tmk::Launch<float>::fault_entry(tmk::FAULT_SEG),
                        tmk::Launch<float>::fault_entry(tmk::FAULT_SEG_SMALL),
                        tmk::Launch<double>::fault_entry(tmk::FAULT_SEG),
-                       tmk::Launch<double>::fault_entry(tmk::FAULT_SEG_SMALL)};
+                       tmk::Launch<double>::fault_entry(tmk::FAULT_SEG_SMALL),
+                       station_entry(TMK_PREC_MIXED), station_entry(TMK_PREC_FP64)};
   for (cudaGraphNode_t nd : nodes) {
     cudaGraphNodeType t;
     if (cudaGraphNodeGetType(nd, &t) != cudaSuccess) return TMK_ERR_CUDA;
     if (t != cudaGraphNodeTypeKernel) continue;
     cudaKernelNodeParams p;
     if (cudaGraphKernelNodeGetParams(nd, &p) != cudaSuccess) return TMK_ERR_CUDA;
-    if (p.func != fe[0] && p.func != fe[1] && p.func != fe[2] && p.func != fe[3]) continue;
+    const int which = (int)(std::find(fe, fe + 6, p.func) - fe);
+    if (which == 6) continue;
     g->tnodes.push_back(nd);
     g->tbase.push_back(*(const double*)p.kernelParams[3]);
+    g->nparams.push_back(which < 4 ? kFaultParams : kStationParams);
   }
   return TMK_OK;
 }
@@ -1299,7 +1310,9 @@ extern "C" tmk_status tmk_graph_launch(tmk_graph* g, double time, void* stream) 
     cudaKernelNodeParams p;
     TMK_CU(cudaGraphKernelNodeGetParams(g->tnodes[k], &p));
     double t = g->tbase[k] + shift;
-    void* args[5] = {p.kernelParams[0], p.kernelParams[1], p.kernelParams[2], &t, p.kernelParams[4]};
+    void* args[kStationParams];
+    for (int q = 0; q < g->nparams[k]; ++q) args[q] = p.kernelParams[q];
+    args[3] = &t;
     p.kernelParams = args;
     TMK_CU(cudaGraphExecKernelNodeSetParams(g->exec, g->tnodes[k], &p));
   }

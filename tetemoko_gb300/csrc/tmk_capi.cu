@@ -748,6 +748,12 @@ extern "C" tmk_status tmk_level_step_cf(tmk_level* L, double time, double dt, do
   if (st != TMK_OK) return st;
   if (ev) TMK_CU(cudaEventRecord(ev[3], s));
   L->parity = 1 - par;
+  // postTimeStep's station records; a level with a finer level records after
+  // the finer substeps, reflux and average-down (the hierarchy step does it)
+  if (L->stations && !L->finer) {
+    st = tmk_stations_record(L->stations, time + dt, s);
+    if (st != TMK_OK) return st;
+  }
   if (dt_new) *dt_new = L->dx / std::max(c->hp.cs, c->hp.cp);
   return TMK_OK;
 }

@@ -71,6 +71,7 @@ struct tmk_level_s {
   int nscen = 1;                           // scenarios of an ensemble level
   tmk_tuning tune;                         // work-list shapes and kernel variants
   int graphs = 0;                          // recorded graphs that launch this level's kernels
+  tmk_stations* stations = nullptr;        // recorded after each step (postTimeStep's writeStationLevel)
   tmk::DevParams* dparams = nullptr;       // device parameters per scenario (ctx->dp for one)
   tmk_box domain;
   double dx = 0;
@@ -166,6 +167,8 @@ struct LevelSnapshot {
   ~LevelSnapshot() { if (buf) cudaFree(buf); }
 };
 
+// tmk_regrid.cu: the station kernel of a precision (its fourth parameter is the record's time)
+const void* station_entry(int prec);
 // tmk_capi.cu: candidate tunings of a level for the autotuners
 std::vector<tmk_tuning> tuning_candidates(const tmk_level_s* L, bool reduced);
 // tmk_capi.cu

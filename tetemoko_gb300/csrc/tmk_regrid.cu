@@ -163,3 +163,227 @@ extern "C" tmk_status tmk_level_tag_cells(tmk_level* L, const tmk_tag_params* tp
   cudaFree(buf);
   return st;
 }
+
+// ================================================================ stations
+// AMRLevelLinElast::writeStationLevel (srcLinElast/AMRLevelLinElast.cpp:1758-1869)
+// with the station cells and weights of AMRLevelLinElast::define (:257-335).
+// Each record is one launch of one CTA: the record slot is taken from a
+// device counter, so recording is asynchronous and can sit in a CUDA graph.
+namespace {
+
+struct StationDev {
+  int kind;            // 0 fault (B, nb values), 1 body (U, 22 values)
+  int off;             // first value of the station in a record (after the time)
+  int present;         // a patch of the level holds the station's cell
+  int p[4], i[4], j[4];  // the interpolation's cells: owning patch (or the station patch's ghost) and index
+  double wx, wy;       // the reference's weights (distances from the cell centre, not divided by dx)
+};
+
+template <typename Real>
+__global__ void station_kernel(const StationDev* __restrict__ st, int n, const PatchDev<Real>* __restrict__ patches,
+                               double time, double* __restrict__ rec, int* __restrict__ count,
+                               unsigned long long* __restrict__ dropped, int capacity, int stride, int nb) {
+  __shared__ int slot;
+  if (threadIdx.x == 0) {
+    const int k = *count;
+    slot = k;
+    if (k < capacity) *count = k + 1;
+    else *dropped += 1ull;
+  }
+  __syncthreads();
+  if (slot >= capacity) return;
+  double* r = rec + (size_t)slot * stride;
+  if (threadIdx.x == 0) r[0] = time;
+  for (int s = 0; s < n; ++s) {
+    const StationDev& d = st[s];
+    const int nv = d.kind == 0 ? nb : NC;
+    for (int c = threadIdx.x; c < nv; c += blockDim.x) {
+      double v;
+      if (!d.present) {
+        v = __longlong_as_double(0x7ff8000000000000ll);   // NaN: no patch of this level holds it
+      } else if (d.kind == 0) {
+        const PatchDev<Real>& p0 = patches[d.p[0]];
+        const PatchDev<Real>& p1 = patches[d.p[1]];
+        const double b0 = p0.B[(size_t)c * p0.bnx + (d.i[0] - p0.blo0)];
+        const double b1 = p1.B[(size_t)c * p1.bnx + (d.i[1] - p1.blo0)];
+        v = b0 * (1 - d.wx) + b1 * d.wx;
+      } else {
+        double u[4];
+        for (int k = 0; k < 4; ++k) {
+          const PatchDev<Real>& pk = patches[d.p[k]];
+          u[k] = (double)pk.Uin[fab_idx(pk, c, d.i[k], d.j[k])];
+        }
+        v = u[0] * (1 - d.wx) * (1 - d.wy) + u[1] * d.wx * (1 - d.wy) + u[2] * (1 - d.wx) * d.wy +
+            u[3] * d.wx * d.wy;
+      }
+      r[1 + d.off + c] = v;
+    }
+  }
+}
+
+}  // namespace
+
+struct tmk_stations_s {
+  tmk_level_s* L = nullptr;
+  std::vector<StationDev> h;
+  StationDev* d = nullptr;
+  double* rec = nullptr;
+  int* count = nullptr;
+  unsigned long long* dropped = nullptr;
+  int capacity = 0, stride = 1;
+};
+
+const void* tmk_host::station_entry(int prec) {
+  return prec == TMK_PREC_MIXED ? (const void*)station_kernel<float> : (const void*)station_kernel<double>;
+}
+
+namespace {
+
+// patch whose valid box holds cell (i, j), else -1
+int owner(const tmk_level_s* L, int i, int j) {
+  for (size_t p = 0; p < L->patches.size(); ++p) {
+    const tmk_box& v = L->patches[p].valid;
+    if (i >= v.lo[0] && i <= v.hi[0] && j >= v.lo[1] && j <= v.hi[1]) return (int)p;
+  }
+  return -1;
+}
+
+}  // namespace
+
+extern "C" tmk_status tmk_stations_create(tmk_level* L, int nfault, const double* x_fault, int nbody,
+                                          const double* x_body, const double* y_body, const double* center,
+                                          int capacity, tmk_stations** out) {
+  if (!out) return TMK_ERR_BAD_DESC;
+  *out = nullptr;
+  if (!L || nfault < 0 || nbody < 0 || nfault + nbody == 0 || capacity < 1 || !center) return TMK_ERR_BAD_DESC;
+  if ((nfault && !x_fault) || (nbody && (!x_body || !y_body))) return TMK_ERR_BAD_DESC;
+  if (L->nscen != 1) return TMK_ERR_UNSUPPORTED;
+  if (nfault && L->ctx->nb == 0) return TMK_ERR_BAD_DESC;
+  const double dx = L->dx;
+  const int nb = L->ctx->nb;
+  const int jf = L->domain.lo[1];
+  tmk_stations_s* S = new (std::nothrow) tmk_stations_s();
+  if (!S) return TMK_ERR_ALLOC;
+  S->L = L;
+  int off = 0;
+  for (int k = 0; k < nfault + nbody; ++k) {
+    StationDev s;
+    std::memset(&s, 0, sizeof(s));
+    const bool fault = k < nfault;
+    s.kind = fault ? 0 : 1;
+    s.off = off;
+    off += fault ? nb : TMK_NCOMP;
+    // AMRLevelLinElast::define (:260-335): the cell below the station and the
+    // distances to its centre (in 2-D the z terms vanish)
+    const double x = fault ? x_fault[k] : x_body[k - nfault];
+    const int i0 = (int)std::floor((x + center[0]) / dx - 0.5);
+    s.wx = -(i0 + 0.5) * dx + (x + center[0]);
+    int j0 = jf;
+    if (!fault) {
+      const double y = y_body[k - nfault];
+      j0 = (int)std::floor((y + center[1]) / dx - 0.5);
+      s.wy = -(j0 + 0.5) * dx + (y + center[1]);
+    }
+    if (fault) {
+      // the fault row of a patch holding face i0 (the reference's m_bdryGrids)
+      int p0 = -1;
+      for (size_t p = 0; p < L->patches.size(); ++p) {
+        const LevelPatch& lp = L->patches[p];
+        if (lp.fault && i0 >= lp.valid.lo[0] && i0 <= lp.valid.hi[0]) p0 = (int)p;
+      }
+      s.present = p0 >= 0;
+      if (s.present) {
+        int p1 = -1;
+        for (size_t p = 0; p < L->patches.size(); ++p) {
+          const LevelPatch& lp = L->patches[p];
+          if (lp.fault && i0 + 1 >= lp.valid.lo[0] && i0 + 1 <= lp.valid.hi[0]) p1 = (int)p;
+        }
+        s.p[0] = p0; s.i[0] = i0;
+        s.p[1] = p1 >= 0 ? p1 : p0; s.i[1] = i0 + 1;   // else the station patch's ghost face
+      }
+    } else {
+      const int p0 = owner(L, i0, j0);
+      s.present = p0 >= 0;
+      if (s.present)
+        for (int q = 0; q < 4; ++q) {
+          const int ii = i0 + (q & 1), jj = j0 + (q >> 1);
+          const int pq = owner(L, ii, jj);
+          s.p[q] = pq >= 0 ? pq : p0;                  // else the station patch's ghost cell
+          s.i[q] = ii; s.j[q] = jj;
+        }
+    }
+    S->h.push_back(s);
+  }
+  S->stride = 1 + off;
+  S->capacity = capacity;
+  const size_t recb = (size_t)capacity * S->stride * sizeof(double);
+  if (dalloc(&S->d, S->h.size()) != cudaSuccess || cudaMalloc(&S->rec, recb) != cudaSuccess ||
+      dalloc(&S->count, 1) != cudaSuccess || dalloc(&S->dropped, 1) != cudaSuccess) {
+    tmk_stations_destroy(S);
+    return TMK_ERR_ALLOC;
+  }
+  if (cudaMemcpy(S->d, S->h.data(), S->h.size() * sizeof(StationDev), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(S->count, 0, sizeof(int)) != cudaSuccess ||
+      cudaMemset(S->dropped, 0, sizeof(unsigned long long)) != cudaSuccess) {
+    tmk_stations_destroy(S);
+    return TMK_ERR_CUDA;
+  }
+  *out = S;
+  return TMK_OK;
+}
+
+extern "C" void tmk_stations_destroy(tmk_stations* S) {
+  if (!S) return;
+  cudaDeviceSynchronize();
+  if (S->L && S->L->stations == S) S->L->stations = nullptr;
+  cudaFree(S->d); cudaFree(S->rec); cudaFree(S->count); cudaFree(S->dropped);
+  delete S;
+}
+
+extern "C" tmk_status tmk_stations_record(tmk_stations* S, double time, void* stream) {
+  if (!S || !S->L) return TMK_ERR_BAD_DESC;
+  tmk_level_s* L = S->L;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = (int)S->h.size(), nb = L->ctx->nb;
+  if (L->prec == TMK_PREC_MIXED)
+    station_kernel<float><<<1, 64, 0, s>>>(S->d, n, (const PatchDev<float>*)L->dpatch[L->parity], time, S->rec,
+                                           S->count, S->dropped, S->capacity, S->stride, nb);
+  else
+    station_kernel<double><<<1, 64, 0, s>>>(S->d, n, (const PatchDev<double>*)L->dpatch[L->parity], time, S->rec,
+                                            S->count, S->dropped, S->capacity, S->stride, nb);
+  TMK_CU(cudaGetLastError());
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_stations_layout(const tmk_stations* S, int* values_per_record, int* present) {
+  if (!S) return TMK_ERR_BAD_DESC;
+  if (values_per_record) *values_per_record = S->stride;
+  if (present)
+    for (size_t k = 0; k < S->h.size(); ++k) present[k] = S->h[k].present;
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_stations_read(tmk_stations* S, double* out, int max_records, int* nrec,
+                                        long long* dropped) {
+  if (!S || !nrec || (max_records > 0 && !out)) return TMK_ERR_BAD_DESC;
+  TMK_CU(cudaDeviceSynchronize());
+  int n = 0;
+  unsigned long long dr = 0;
+  TMK_CU(cudaMemcpy(&n, S->count, sizeof(int), cudaMemcpyDeviceToHost));
+  TMK_CU(cudaMemcpy(&dr, S->dropped, sizeof(dr), cudaMemcpyDeviceToHost));
+  const int take = std::min(n, std::max(0, max_records));
+  if (take) TMK_CU(cudaMemcpy(out, S->rec, (size_t)take * S->stride * sizeof(double), cudaMemcpyDeviceToHost));
+  // records beyond max_records are dropped with the rest at the reset
+  dr += (unsigned long long)(n - take);
+  TMK_CU(cudaMemset(S->count, 0, sizeof(int)));
+  TMK_CU(cudaMemset(S->dropped, 0, sizeof(unsigned long long)));
+  *nrec = take;
+  if (dropped) *dropped = (long long)dr;
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_attach_stations(tmk_level* L, tmk_stations* S) {
+  if (!L || (S && S->L != L) || L->graphs) return TMK_ERR_BAD_DESC;
+  L->stations = S;
+  return TMK_OK;
+}
