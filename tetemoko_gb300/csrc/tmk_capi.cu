@@ -629,15 +629,34 @@ extern "C" tmk_status tmk_ensemble_create(int nscen, tmk_context* const* ctxs, c
   return level_create_impl(ctxs, nscen, pdom.data(), patch_scen, dx, npatch, boxes, out);
 }
 
+namespace {
+
+// The device address of host memory the device can read and write directly
+// (pinned memory), else null: pageable memory goes through a staging copy.
+void* mapped_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+}  // namespace
+
 extern "C" tmk_status tmk_level_set_patch(tmk_level* L, int p, const double* U, const double* B, int host) {
   if (!L || p < 0 || p >= (int)L->patches.size() || !U) return TMK_ERR_BAD_DESC;
   LevelPatch& lp = L->patches[p];
   const size_t count = (size_t)TMK_NCOMP * (lp.alloc.hi[0] - lp.alloc.lo[0] + 1) * (lp.alloc.hi[1] - lp.alloc.lo[1] + 1);
   const cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   const int k = L->parity;   // the buffer the next step reads
+  // a device pointer or pinned host memory is read in place by the kernel
+  const double* src = host ? (const double*)mapped_host(U) : U;
   if (L->prec == TMK_PREC_MIXED) {
-    TMK_CU(cudaMemcpy(L->stage, U, count * sizeof(double), kind));
-    TMK_CU(tmk::convert_d2f(L->stage, (float*)lp.U[k], count, 0));
+    if (!src) {
+      TMK_CU(cudaMemcpy(L->stage, U, count * sizeof(double), kind));
+      src = L->stage;
+    }
+    TMK_CU(tmk::convert_d2f(src, (float*)lp.U[k], count, 0));
+  } else if (src) {
+    TMK_CU(tmk::copy_fab(src, (double*)lp.U[k], count, 0));
   } else {
     TMK_CU(cudaMemcpy(lp.U[k], U, count * sizeof(double), kind));
   }
@@ -661,9 +680,12 @@ extern "C" tmk_status tmk_level_get_patch(tmk_level* L, int p, double* U, double
   const cudaMemcpyKind kind = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   TMK_CU(cudaDeviceSynchronize());
   if (U) {
+    double* dst = host ? (double*)mapped_host(U) : U;   // written in place when the device can reach it
     if (L->prec == TMK_PREC_MIXED) {
-      TMK_CU(tmk::convert_f2d((const float*)lp.U[L->parity], L->stage, count, 0));
-      TMK_CU(cudaMemcpy(U, L->stage, count * sizeof(double), kind));
+      TMK_CU(tmk::convert_f2d((const float*)lp.U[L->parity], dst ? dst : L->stage, count, 0));
+      if (!dst) TMK_CU(cudaMemcpy(U, L->stage, count * sizeof(double), kind));
+    } else if (dst) {
+      TMK_CU(tmk::copy_fab((const double*)lp.U[L->parity], dst, count, 0));
     } else {
       TMK_CU(cudaMemcpy(U, lp.U[L->parity], count * sizeof(double), kind));
     }

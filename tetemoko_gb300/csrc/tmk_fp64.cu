@@ -54,24 +54,38 @@ cudaError_t copy_valid(const double* src, double* dst, int alo0, int alo1, int a
   return cudaGetLastError();
 }
 
-__global__ void d2f_kernel(const double* a, float* b, size_t n) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
+// Whole-FAB conversion or copy, four elements per thread in flight (all loads,
+// then all stores).  Either side may be pinned host memory seen through its
+// device address, so a set or get of a level's state crosses the host link
+// once, inside this kernel, with no staging copy.
+template <typename S, typename D>
+__global__ void convert_kernel(const S* __restrict__ a, D* __restrict__ b, size_t n) {
+  constexpr int U = 4;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + (U - 1) * stride < n; i += U * stride) {
+    S v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) v[u] = a[i + u * stride];
+#pragma unroll
+    for (int u = 0; u < U; ++u) b[i + u * stride] = (D)v[u];
+  }
+  for (; i < n; i += stride) b[i] = (D)a[i];
 }
-__global__ void f2d_kernel(const float* a, double* b, size_t n) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    b[i] = (double)a[i];
-}
-cudaError_t convert_d2f(const double* src, float* dst, size_t n, cudaStream_t s) {
+template <typename S, typename D>
+cudaError_t convert_launch(const S* src, D* dst, size_t n, cudaStream_t s) {
   if (!n) return cudaSuccess;
-  d2f_kernel<<<(unsigned)((n + 255) / 256 > 8192 ? 8192 : (n + 255) / 256), 256, 0, s>>>(src, dst, n);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return cudaErrorUnknown;
+  const size_t want = (n + 4 * 256 - 1) / (4 * 256);
+  const unsigned blocks = (unsigned)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * 8));
+  convert_kernel<S, D><<<blocks, 256, 0, s>>>(src, dst, n);
   return cudaGetLastError();
 }
-cudaError_t convert_f2d(const float* src, double* dst, size_t n, cudaStream_t s) {
-  if (!n) return cudaSuccess;
-  f2d_kernel<<<(unsigned)((n + 255) / 256 > 8192 ? 8192 : (n + 255) / 256), 256, 0, s>>>(src, dst, n);
-  return cudaGetLastError();
-}
+cudaError_t convert_d2f(const double* src, float* dst, size_t n, cudaStream_t s) { return convert_launch(src, dst, n, s); }
+cudaError_t convert_f2d(const float* src, double* dst, size_t n, cudaStream_t s) { return convert_launch(src, dst, n, s); }
+cudaError_t copy_fab(const double* src, double* dst, size_t n, cudaStream_t s) { return convert_launch(src, dst, n, s); }
 
 // Fault-row exchange: copy boundary data faces [lo0, hi0] from src to dst patch.
 __global__ void bexchange_kernel(double* const* __restrict__ bptr, const int* __restrict__ blo,

@@ -53,6 +53,8 @@ struct Launch {
 // FP64 <-> Real conversion of a FAB on the device
 cudaError_t convert_d2f(const double* src, float* dst, size_t n, cudaStream_t s);
 cudaError_t convert_f2d(const float* src, double* dst, size_t n, cudaStream_t s);
+// copy of n doubles (either side may be mapped pinned host memory)
+cudaError_t copy_fab(const double* src, double* dst, size_t n, cudaStream_t s);
 // copy components [c0, c0+ncomp) of the valid box of a FAB into another FAB of the same shape
 cudaError_t copy_valid(const double* src, double* dst, int alo0, int alo1, int anx, int any, int vlo0, int vlo1,
                        int vhi0, int vhi1, int c0, int ncomp, cudaStream_t s);
