@@ -49,6 +49,9 @@ struct DevParams {
   int sw_off;               // side-2 component offset, 9 (reference) or 11
   // plasticity (PLASTICSETF)
   double p_mu, p_beta, p_eta, p_b, p_h;
+  // reciprocals the mixed form's friction solve multiplies by (its chain of
+  // FP64 operations is the fault kernel's latency; a division costs several)
+  double inv_Zs, inv_Zp, lam_r, two_V0, inv_2V0;   // lam_r = lam/(lam+2G)
 };
 
 // Constants of one arithmetic type.

@@ -56,50 +56,8 @@ TMK_D int rs_newton(const DevParams& P, double phi, double psi, double sn, doubl
   return it;
 }
 
-// The friction equation of RSNEWTON solved for z = asinh(beta V) instead of V:
-//   f(z) = alpha z + (eta/beta) sinh z - phi = 0,  V = sinh(z)/beta, tau = alpha z.
-// f is smooth and monotone in z on the same bracket (0, asinh(beta phi/Zs)], so
-// Newton converges in a few steps where the iteration in V creeps up through
-// tens of decades.  As in the reference, a root beyond the bracket's upper
-// end V = phi/Zs yields that end.  Used by the mixed form; FP64 arithmetic.
-TMK_D int rs_newton_z(const DevParams& P, double phi, double psi, double sn, double c_rs_a, double& V,
-                      double& tau) {
-  const double atolG = 2.220446049250313e-16 * 1e4;
-  const double alpha = sn * c_rs_a;
-  const double beta = exp(psi / c_rs_a) / (2.0 * P.rs_V0);
-  const double eta = 0.5 * P.Zs;
-  const double Vmax = phi / P.Zs;
-  if (!(alpha > 0.0) || !(beta > 0.0) || !(beta < 1e300) || !(phi > 0.0)) return rs_newton(P, phi, psi, sn, c_rs_a, V, tau);
-  const double zmax = asinh(beta * Vmax);
-  if (alpha * zmax + eta * Vmax - phi <= 0.0) {     // root beyond the reference's bracket
-    V = Vmax;
-    tau = alpha * zmax;
-    return RS_IMAX + 1;
-  }
-  const double c = eta / beta;
-  double z = fmin(phi / alpha, zmax);
-  int it;
-  for (it = 1; it <= RS_IMAX; ++it) {
-    const double e = exp(z), ie = 1.0 / e;
-    const double sh = 0.5 * (e - ie), ch = 0.5 * (e + ie);
-    const double f = alpha * z + c * sh - phi;
-    const double dz = -f / (alpha + c * ch);
-    double zn = z + dz;
-    if (zn < 0.0) zn = 0.5 * z;
-    if (zn > zmax) zn = 0.5 * (z + zmax);
-    z = zn;
-    if (fabs(f) <= atolG || fabs(dz) <= 1e-15 * fmax(1.0, z)) break;
-  }
-  const double e = exp(z);
-  V = 0.5 * (e - 1.0 / e) / beta;
-  tau = alpha * z;
-  return it;
-}
-
 // RSFAULTBCF (ibcLinElast/RSIBCF.ChF:158-323) at one fault face; Wi, Wg: 22 comps.
-// zsolve selects rs_newton_z (mixed form) instead of the reference's RSNEWTON.
-TMK_D int rs_fault(const DevParams& P, const RSFace& fr, const double* Wi, double psi, double x, double* Wg,
-                   bool zsolve = false) {
+TMK_D int rs_fault(const DevParams& P, const RSFace& fr, const double* Wi, double psi, double x, double* Wg) {
   const double Zs = P.Zs, Zp = P.Zp, lam = P.lam, G = P.G;
   double vx1 = Wi[0], vy1 = Wi[1], vz1 = Wi[2], sxx1 = Wi[3], syy1 = Wi[4], szz1 = Wi[5];
   double sxy1 = Wi[6], sxz1 = Wi[7], syz1 = Wi[8];
@@ -124,7 +82,7 @@ TMK_D int rs_fault(const DevParams& P, const RSFace& fr, const double* Wi, doubl
   double c_ramp = fmin(1.0, fmax(0.0, (x - P.ramp_x) / P.ramp_w));
   double c_rs_a = fr.a + P.ramp_a * c_ramp;
   double tau;
-  int it = zsolve ? rs_newton_z(P, phi, psi, -syy1, c_rs_a, V, tau) : rs_newton(P, phi, psi, -syy1, c_rs_a, V, tau);
+  int it = rs_newton(P, phi, psi, -syy1, c_rs_a, V, tau);
   sxy1 = (phi_xy / phi) * tau - tau_xy_0;
   syz1 = (phi_yz / phi) * tau - tau_yz_0;
   double Vx = (phi_xy / phi) * V;
@@ -185,6 +143,176 @@ TMK_D double rs_setbnd(const DevParams& P, const RSFace& fr, const double* U, do
     B[1 * bstride] = Vz;
     B[2 * bstride] = V;
     B[3 * bstride] = U[6] + tau_xy_0;
+    B[4 * bstride] = U[8] + 0.0;
+    B[6 * bstride] = B[6 * bstride] + dt * Vx;
+    B[7 * bstride] = B[7 * bstride] + dt * Vz;
+    B[8 * bstride] = B[8 * bstride] + dt * V;
+    if (rt > time && V > P.rs_thr) B[9 * bstride] = time;
+    else if (rt > time) B[9 * bstride] = 1e10;
+    B[5 * bstride] = U[4];
+    B[10 * bstride] = dPsi;
+  }
+  return dPsi;
+}
+
+// ------------------------------------------------ mixed-form rate-and-state
+// The same friction law for the mixed form, arranged for latency: on GB300 a
+// dependent FP64 operation takes ~70 cycles and an FP64 division or
+// transcendental several hundred, so the per-face chain of the two friction
+// solves and boundary updates is the fault kernel's run time.  Here the
+// quantities that depend only on the face (nucleation shear, ramped a, the
+// reciprocals of a, b, L) are computed once per step beside the predictors,
+// divisions by constants become products with reciprocals, reciprocals inside
+// the Newton loop are Newton-Raphson refinements of an FP32 seed, the Newton
+// step uses an FP32 reciprocal of the derivative (the iteration's fixed point
+// is unchanged), and the solve starts from the slip rate of the states it is
+// given.  Everything stays FP64; the results agree with the reference
+// ordering to rounding and are checked by the rupture metrics.
+
+// Reciprocal by two Newton-Raphson refinements r <- r + r (1 - x r) of an FP32
+// seed (x within FP32 range and nonzero).
+TMK_D double recip_nr(double x) {
+  const double r0 = (double)__frcp_rn((float)x);
+  const double r1 = fma(r0, fma(-x, r0, 1.0), r0);
+  return fma(r1, fma(-x, r1, 1.0), r1);
+}
+
+struct RSFaceK {
+  double tau0;    // nucleation shear at the face
+  double a, inv_a, b, inv_b, inv_L;
+  double c_Vw;    // ramped weakening velocity (slip law with fexp > 0)
+};
+
+TMK_D RSFaceK rs_face_k(const DevParams& P, const RSFace& fr, double x) {
+  RSFaceK k;
+  k.tau0 = P.rs_nsig * gaussian(P.rs_r0, x);
+  const double c_ramp = fmin(1.0, fmax(0.0, (x - P.ramp_x) / P.ramp_w));
+  k.a = fr.a + P.ramp_a * c_ramp;
+  k.inv_a = 1.0 / k.a;
+  k.b = fr.b;
+  k.inv_b = 1.0 / fr.b;
+  k.inv_L = 1.0 / fr.L;
+  k.c_Vw = P.rs_Vw + P.ramp_Vw * c_ramp;
+  return k;
+}
+
+// The friction equation of RSNEWTON solved for z = asinh(beta V) instead of V:
+//   f(z) = alpha z + (eta/beta) sinh z - phi = 0,  V = sinh(z)/beta, tau = alpha z.
+// f is smooth and monotone in z on the same bracket (0, asinh(beta phi/Zs)], so
+// Newton converges in a few steps where the iteration in V creeps up through
+// tens of decades; it starts from the guess V0 when that lies inside the
+// bracket.  As in the reference, a root beyond the bracket's upper end
+// V = phi/Zs yields that end.
+TMK_D int rs_newton_zk(const DevParams& P, const RSFaceK& fk, double phi, double psi, double sn, double V0,
+                       double& V, double& tau) {
+  const double atolG = 2.220446049250313e-16 * 1e4;
+  const double alpha = sn * fk.a;
+  const double ep = exp(psi * fk.inv_a), em = exp(-psi * fk.inv_a);   // independent: issued together
+  const double beta = ep * P.inv_2V0, inv_beta = em * P.two_V0;
+  const double eta = 0.5 * P.Zs;
+  const double Vmax = phi * P.inv_Zs;
+  if (!(alpha > 0.0) || !(beta > 0.0) || !(beta < 1e300) || !(inv_beta > 0.0) || !(phi > 0.0))
+    return rs_newton(P, phi, psi, sn, fk.a, V, tau);
+  const double zmax = asinh(beta * Vmax);
+  const bool guess = V0 > 0.0 && V0 < Vmax;
+  const double zg = guess ? asinh(beta * V0) : 0.0;                      // independent of zmax
+  if (alpha * zmax + eta * Vmax - phi <= 0.0) {     // root beyond the reference's bracket
+    V = Vmax;
+    tau = alpha * zmax;
+    return RS_IMAX + 1;
+  }
+  const double c = eta * inv_beta;
+  double z = guess ? fmin(zg, zmax) : fmin(phi / alpha, zmax);
+  int it;
+  for (it = 1; it <= RS_IMAX; ++it) {
+    const double e = exp(z), ie = z > 20.0 ? 0.0 : recip_nr(e);   // e^-2z below FP64 resolution past 20
+    const double sh = 0.5 * (e - ie), ch = 0.5 * (e + ie);
+    const double f = alpha * z + c * sh - phi;
+    const double dz = -f * (double)__frcp_rn((float)(alpha + c * ch));
+    double zn = z + dz;
+    if (zn < 0.0) zn = 0.5 * z;
+    if (zn > zmax) zn = 0.5 * (z + zmax);
+    z = zn;
+    if (fabs(f) <= atolG || fabs(dz) <= 1e-15 * fmax(1.0, z)) break;
+  }
+  const double e = exp(z);
+  V = 0.5 * (e - (z > 20.0 ? 0.0 : recip_nr(e))) * inv_beta;
+  tau = alpha * z;
+  return it;
+}
+
+// RSFAULTBCF for the mixed form (same states in, same face states out).
+TMK_D int rs_fault_k(const DevParams& P, const RSFaceK& fk, const double* Wi, double psi, double* Wg) {
+  const double Zs = P.Zs, Zp = P.Zp;
+  double vx1 = Wi[0], vy1 = Wi[1], vz1 = Wi[2], sxx1 = Wi[3], syy1 = Wi[4], szz1 = Wi[5];
+  double sxy1 = Wi[6], sxz1 = Wi[7], syz1 = Wi[8];
+  double vx2 = Wi[11], vy2 = Wi[12], vz2 = Wi[13], sxx2 = Wi[14], syy2 = Wi[15], szz2 = Wi[16];
+  double sxy2 = Wi[17], sxz2 = Wi[18], syz2 = Wi[19];
+  const double wpxy1 = -sxy1 - Zs * vx1, wpyy1 = -syy1 - Zp * vy1;
+  const double wpxy2 = sxy2 - Zs * vx2, wpyy2 = syy2 - Zp * vy2;
+  const double phi_xy = 0.5 * (wpxy2 - wpxy1) + fk.tau0;
+  const double phi = fabs(phi_xy);      // the antiplane traction term is zero in 2-D
+  syy1 = -0.5 * (wpyy1 - wpyy2);
+  syy2 = syy1;
+  vy1 = -0.5 * (wpyy1 + wpyy2) * P.inv_Zp;
+  vy2 = vy1;
+  const double dvx = vx1 - vx2, dvz = vz1 - vz2;
+  double V = sqrt(dvx * dvx + dvz * dvz), tau;
+  const int it = rs_newton_zk(P, fk, phi, psi, -syy1, V, V, tau);
+  // phi_xy / phi: +-1, NaN when phi is zero or NaN (as the reference's quotient)
+  const double sgn = phi > 0.0 ? copysign(1.0, phi_xy) : __longlong_as_double(0x7ff8000000000000ll);
+  sxy1 = sgn * tau - fk.tau0;
+  syz1 = 0.0 * tau;                     // (phi_yz / phi) tau - tau_yz_0 with phi_yz = tau_yz_0 = 0
+  const double Vx = sgn * V, Vz = 0.0 * V;
+  vx1 = -(sxy1 + wpxy1) * P.inv_Zs;
+  vz1 = -(syz1 + 0.0) * P.inv_Zs;
+  double SHF = -(vy1 - syy1) * P.lam_r;
+  Wg[0] = vx1; Wg[1] = vy1; Wg[2] = vz1;
+  Wg[3] = sxx1 + SHF; Wg[4] = syy1; Wg[5] = szz1 + SHF;
+  Wg[6] = sxy1; Wg[7] = sxz1; Wg[8] = syz1;
+  Wg[9] = 0.0; Wg[10] = 0.0;
+  sxy2 = sxy1;
+  syz2 = syz1;
+  vx2 = vx1 - Vx;
+  vz2 = vz1 - Vz;
+  SHF = -(vy2 - syy2) * P.lam_r;
+  Wg[11] = vx2; Wg[12] = vy2; Wg[13] = vz2;
+  Wg[14] = sxx2 + SHF; Wg[15] = syy2; Wg[16] = szz2 + SHF;
+  Wg[17] = sxy2; Wg[18] = sxz2; Wg[19] = syz2;
+  Wg[20] = 0.0; Wg[21] = 0.0;
+  (void)syz2;
+  return it;
+}
+
+// RSSETBND for the mixed form (see rs_setbnd).
+TMK_D double rs_setbnd_k(const DevParams& P, const RSFaceK& fk, const double* U, double* B, int bstride, double dt,
+                         double time, bool final_) {
+  const double Vx = U[0] - U[11];
+  const double Vz = U[2] - U[13];
+  const double V = sqrt(Vx * Vx + Vz * Vz);
+  const double psi = B[10 * bstride];
+  double dPsi;
+  if (P.state_law == 1) {
+    const double xx = V * dt * fk.inv_L;
+    const double q = (psi - P.rs_f0) * fk.inv_b - xx;
+    const double eq = exp(q), em1 = expm1(-xx);          // independent: issued together
+    const double phi1 = (xx > 1e-12) ? -em1 / xx : 1.0 - 0.5 * xx;
+    dPsi = P.rs_f0 + fk.b * log(eq + (P.rs_V0 * dt * fk.inv_L) * phi1);
+  } else {
+    const double f = fk.a * asinh(V * exp(psi * fk.inv_a) * P.inv_2V0);
+    double fss = P.rs_f0 - (fk.b - fk.a) * log(V / P.rs_V0);
+    if (P.rs_fexp > 0.0) {
+      const double q = V / fk.c_Vw, q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
+      fss = P.rs_fw + (fss - P.rs_fw) / pow(1.0 + q8, 0.125);
+    }
+    dPsi = psi - dt * (V * fk.inv_L) * (f - fss);
+  }
+  if (final_) {
+    const double rt = B[9 * bstride];
+    B[0] = Vx;
+    B[1 * bstride] = Vz;
+    B[2 * bstride] = V;
+    B[3 * bstride] = U[6] + fk.tau0;
     B[4 * bstride] = U[8] + 0.0;
     B[6 * bstride] = B[6 * bstride] + dt * Vx;
     B[7 * bstride] = B[7 * bstride] + dt * Vz;

@@ -132,14 +132,16 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
                                                    DevStatus* st) {
   static_assert(NT > SEG + 2, "the x-face threads need the threads beyond the face threads");
   using T = Real;
-  // the mixed form solves the friction equation in z = asinh(beta V); the FP64
-  // form keeps the reference's Newton iteration on V
+  // the mixed form runs the latency-arranged rate-and-state path (per-face
+  // constants, z = asinh(beta V) Newton solve); the FP64 form keeps the
+  // reference's operation order and Newton iteration on V
   constexpr bool kZSolve = !std::is_same<Real, double>::value;
   constexpr int NCELL = SEG + 2;             // cells / faces [s0-1, s0+SEG]
   __shared__ T xWM[2][NCELL][NSIDE], xWP[2][NCELL][NSIDE];
   __shared__ T H1x[2][SEG + 1][NSIDE];
   __shared__ double sWi[NCELL][NC];
   __shared__ double sTmp[NCELL];
+  __shared__ RSFaceK sFk[kZSolve ? NCELL : 1];   // mixed form: per-face rate-and-state constants
   // the kernel launched after this one may be scheduled now (it reads none of
   // this kernel's outputs before it waits for it).  When this kernel itself is
   // a programmatic dependent of the in-plane marching kernel, it reads nothing
@@ -167,7 +169,14 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
   const int bs = p.bnx;
 
   // (A) x predictors of the fault-row cells [s0-1, s1+1] and y predictors of the
-  //     states entering the fault faces [fa, fb], both sides
+  //     states entering the fault faces [fa, fb], both sides; in the mixed form
+  //     also the constants of each face
+  if constexpr (kZSolve) {
+    if (P.fault_law == 1 && tid >= NT - NCELL) {
+      const int ci = tid - (NT - NCELL), i = s0 - 1 + ci;
+      if (i >= fa && i <= fb) sFk[ci] = rs_face_k(P, rs_face(P, p.fric, i - p.blo0, bs), (i + 0.5) * dx - P.rs_x0);
+    }
+  }
   for (int t = tid; t < 4 * NCELL; t += NT) {
     const int kind = t / (2 * NCELL), s = (t / NCELL) & 1, ci = t % NCELL;
     const int c = s0 - 1 + ci;
@@ -194,14 +203,22 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
       for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
       int it = 0;
       const RSFace fr = rs_face(P, p.fric, i - p.blo0, bs);
-      if (P.fault_law == 1) it = rs_fault(P, fr, sWi[tid], Bi[10 * bs], xc - P.rs_x0, Wg, kZSolve);
-      else sw_fault(P, sWi[tid], Bi[7 * bs], xc, Wg);
+      if (P.fault_law == 1) {
+        if constexpr (kZSolve) it = rs_fault_k(P, sFk[tid], sWi[tid], Bi[10 * bs], Wg);
+        else it = rs_fault(P, fr, sWi[tid], Bi[10 * bs], xc - P.rs_x0, Wg);
+      } else {
+        sw_fault(P, sWi[tid], Bi[7 * bs], xc, Wg);
+      }
       if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
       double* first = p.first + (i - (p.vlo0 - 1));
       for (int c = 0; c < NC; ++c) first[c * p.nfirst] = Wg[c];
       if (i >= s0 && i <= s1) {
-        if (P.fault_law == 1) sTmp[tid] = rs_setbnd(P, fr, Wg, Bi, bs, 0.5 * dt, xc - P.rs_x0, 0.0, false);
-        else sTmp[tid] = sw_setbnd(P, Wg, Bi, bs, 0.5 * dt, 0.0, false);
+        if (P.fault_law == 1) {
+          if constexpr (kZSolve) sTmp[tid] = rs_setbnd_k(P, sFk[tid], Wg, Bi, bs, 0.5 * dt, 0.0, false);
+          else sTmp[tid] = rs_setbnd(P, fr, Wg, Bi, bs, 0.5 * dt, xc - P.rs_x0, 0.0, false);
+        } else {
+          sTmp[tid] = sw_setbnd(P, Wg, Bi, bs, 0.5 * dt, 0.0, false);
+        }
       }
     }
   } else {
@@ -239,8 +256,12 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
     for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
     int it = 0;
     const RSFace fr = rs_face(P, p.fric, i - p.blo0, bs);
-    if (P.fault_law == 1) it = rs_fault(P, fr, Wi, sTmp[ci], xc - P.rs_x0, Wg, kZSolve);
-    else sw_fault(P, Wi, sTmp[ci], xc, Wg);
+    if (P.fault_law == 1) {
+      if constexpr (kZSolve) it = rs_fault_k(P, sFk[ci], Wi, sTmp[ci], Wg);
+      else it = rs_fault(P, fr, Wi, sTmp[ci], xc - P.rs_x0, Wg);
+    } else {
+      sw_fault(P, Wi, sTmp[ci], xc, Wg);
+    }
     if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
     // (F) y fluxes through the fault face (GETFLUXF, FP64)
     Consts<double> kd; kd.load(P);
@@ -253,7 +274,9 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
     for (int c = 0; c < NSIDE; ++c) ff[(11 + c) * nv] = F[c];
     // (G) boundary-data update with the final fault state (final=true, t+dt)
     if (P.fault_law == 1) {
-      double np = rs_setbnd(P, fr, Wg, Bi, bs, dt, xc - P.rs_x0, time + dt, true);
+      double np;
+      if constexpr (kZSolve) np = rs_setbnd_k(P, sFk[ci], Wg, Bi, bs, dt, time + dt, true);
+      else np = rs_setbnd(P, fr, Wg, Bi, bs, dt, xc - P.rs_x0, time + dt, true);
       if (isnan(np)) report(st, ST_NAN, (long long)i);
     } else {
       sw_setbnd(P, Wg, Bi, bs, dt, time + dt, true);
