@@ -120,3 +120,43 @@ def test_fp64_level_equals_oracle_over_a_rupture(cuda_lib):
     print(f"FP64 GPU vs oracle after {NSTEPS} steps: U {rel:.2e}, B {relb.max():.2e}")
     assert rel < 1e-10
     assert relb.max() < 1e-10
+
+
+@pytest.mark.parametrize("variant", ["slip_law", "slip_law_weakening", "per_face_aging"])
+def test_mixed_fault_path_tracks_the_fp64_oracle(cuda_lib, variant):
+    """The mixed form's latency-arranged rate-and-state path (per-face constants,
+    reciprocal products, z-space Newton) on the laws and options the rupture run
+    does not use: the slip law, its flash-weakening steady state, and per-face
+    a, b, L.  Ten steps of a perturbed level against the FP64 oracle: the state
+    to FP32 rounding of the volume (1e-4) and the fault data to 1e-3."""
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    from tests.helpers import perturbed_state, rel_err
+    law = A.TMK_RS_AGING_LAW if variant == "per_face_aging" else A.TMK_RS_SLIP_LAW
+    sc64 = S.rate_state(nx=64, ny=32, dx=0.1, state_law=law)
+    scm = S.rate_state(nx=64, ny=32, dx=0.1, state_law=law, precision=A.TMK_PREC_MIXED)
+    for sc in (sc64, scm):
+        sc.rs.L = 0.5
+        if variant == "slip_law_weakening":
+            sc.rs.fexp, sc.rs.fw, sc.rs.Vw = 1.0, 0.2, 0.01
+    F = S.friction_field(sc64, seed=4001) if variant == "per_face_aging" else None
+    boxes = [(0, 0, 31, 15), (32, 0, 63, 15), (0, 16, 63, 31)]
+    Ug = perturbed_state(sc64, np.random.default_rng(81), amp_v=0.05, amp_s=1.0)
+    Bg = sc64.initial_B()
+    Ur, Br = Ug.copy(), Bg.copy()
+    ctx = Context(scm)
+    lv = LinElastLevelGodunov(ctx, boxes)
+    lv.set_level(Ug, Bg)
+    if F is not None:
+        lv.set_level_friction(F)
+    dt = sc64.dt()
+    for k in range(10):
+        assert O.level_step(sc64, Ur, Br, boxes, k * dt, dt, fric=F) == 0
+        lv.step(k * dt, dt)
+    Um, Bm = Ug.copy(), Bg.copy()
+    lv.get_level(Um, Bm)
+    g = A.TMK_NGHOST
+    assert lv.status()[0] == 0
+    assert rel_err(Um[:, g:-g, g:-g], Ur[:, g:-g, g:-g]) <= 1e-4
+    assert rel_err(Bm[:, g:-g], Br[:, g:-g]) <= 1e-3
+    lv.close()
+    ctx.close()
