@@ -249,6 +249,10 @@ void       tmk_level_destroy(tmk_level* lvl);
  * added), b and L replace the scenario's.  Every value must be positive.  Levels
  * of an AMR hierarchy each take their own faces' values. */
 tmk_status tmk_level_set_fault_friction(tmk_level* lvl, int patch, const double* abL, int host);
+/* The per-face friction of a fault patch, if set (*present = 1; else 0 and
+ * abL untouched), in the layout tmk_level_set_fault_friction takes. */
+tmk_status tmk_level_get_fault_friction(const tmk_level* lvl, int patch, double* abL, int host,
+                                        int* present);
 /* Ensemble of independent scenarios stepped as one level (an extension: the
  * reference runs one scenario per process with its parameters in COMMON
  * blocks, srcLinElast/LinElastPhysicsF.ChF:1149-1210, ibcLinElast/RSIBCF.ChF:8-55).

@@ -165,6 +165,7 @@ def lib() -> C.CDLL:
     L.tmk_level_attach_stations.argtypes = [vp, vp]
     L.tmk_level_tag_cells.argtypes = [vp, C.POINTER(TagParams), vp, C.c_int, vp]
     L.tmk_level_set_fault_friction.argtypes = [vp, C.c_int, vp, C.c_int]
+    L.tmk_level_get_fault_friction.argtypes = [vp, C.c_int, vp, C.c_int, ip]
     L.tmk_ensemble_create.argtypes = [C.c_int, C.POINTER(vp), C.POINTER(Box), C.c_double, C.c_int,
                                       C.POINTER(Box), ip, C.POINTER(vp)]
     L.tmk_level_destroy.restype = None

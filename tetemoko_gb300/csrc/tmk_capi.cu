@@ -426,6 +426,17 @@ extern "C" tmk_status tmk_level_set_fault_friction(tmk_level* L, int patch, cons
   return TMK_OK;
 }
 
+extern "C" tmk_status tmk_level_get_fault_friction(const tmk_level* L, int patch, double* abL, int host,
+                                                   int* present) {
+  if (!L || !abL || !present || patch < 0 || patch >= (int)L->patches.size()) return TMK_ERR_BAD_DESC;
+  const LevelPatch& lp = L->patches[patch];
+  *present = lp.fric ? 1 : 0;
+  if (!lp.fric) return TMK_OK;
+  TMK_CU(cudaMemcpy(abL, lp.fric, 3 * (size_t)lp.bnx * sizeof(double),
+                    host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice));
+  return TMK_OK;
+}
+
 extern "C" void tmk_level_destroy(tmk_level* L) {
   if (!L) return;
   cudaDeviceSynchronize();

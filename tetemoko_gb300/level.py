@@ -192,6 +192,17 @@ class LinElastLevelGodunov:
         else:
             A.check(self.lib.tmk_level_set_fault_friction(self.h, p, F.data_ptr(), 0), "tmk_level_set_fault_friction")
 
+    def get_fault_friction(self, p):
+        """Per-face a, b, L of fault patch p (3, nx+8), or None if not set."""
+        if not self.touches_fault(p):
+            return None
+        _, bshape = self.patch_shapes(p)
+        F = np.empty((3, bshape[1]))
+        present = C.c_int(0)
+        A.check(self.lib.tmk_level_get_fault_friction(self.h, p, F.ctypes.data, 1, C.byref(present)),
+                "tmk_level_get_fault_friction")
+        return F if present.value else None
+
     def set_level_friction(self, Fg: np.ndarray):
         """Scatter a domain-wide per-face friction row (3, nx+8) into the fault patches."""
         g = A.TMK_NGHOST
