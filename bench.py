@@ -330,7 +330,7 @@ def amr_measurement(steps, warmup, stream, autotune=True):
 ENSEMBLE_SIZE = 64
 
 
-def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE, autotune=True):
+def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE, autotune=True, max_grid=1024):
     """64 independent rate-and-state scenarios (seeded friction, lognormal shear
     prestress, grids drawn from 256x128 / 512x256 / 1024x512) stepped as one
     level in the mixed form; steps replayed from a CUDA graph.  Returns the JSON
@@ -341,7 +341,7 @@ def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE, autotune=Tr
     members = [S.ensemble_member(k, precision=A.TMK_PREC_MIXED) for k in range(nscen)]
     ctxs = [Context(sc) for sc, _ in members]
     doms = [(0, 0, sc.nx - 1, sc.ny - 1) for sc, _ in members]
-    ens = LinElastEnsemble(ctxs, doms, [tile_boxes(0, 0, sc.nx - 1, sc.ny - 1, 128) for sc, _ in members])
+    ens = LinElastEnsemble(ctxs, doms, [tile_boxes(0, 0, sc.nx - 1, sc.ny - 1, max_grid) for sc, _ in members])
     for k, (sc, tau0) in enumerate(members):
         U, B = S.prestressed_state(sc, tau0)
         ens.set_scenario(k, U, B)
@@ -389,7 +389,7 @@ def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE, autotune=Tr
            "config": "rate-and-state aging law, a ~ U[0.006,0.012], b-a ~ U[0.002,0.006], L ~ U[0.01,0.05] m "
                      "(seed 5000+k), shear prestress 70 exp(g - s^2/2) MPa with g Gaussian, exponential "
                      "covariance, 1 km correlation, s = 0.1 (seed 6000+k), dx = 0.1 km, FP32 volume / FP64 "
-                     "fault, patches of at most 128x128, one level of all scenarios",
+                     f"fault, patches of at most {max_grid}x{max_grid}, one level of all scenarios",
            "execution": f"CUDA graph of {gsteps} ensemble steps (tmk_ensemble_create + tmk_level_graph_create), "
                         "replayed",
            "tuning": {"autotuned": bool(autotune), "choice": tuning},
@@ -466,6 +466,7 @@ def main():
     ap.add_argument("--amr-only", action="store_true")      # only the AMR measurement (profiling runs)
     ap.add_argument("--ensemble-steps", type=int, default=200)   # timed steps of the ensemble measurement
     ap.add_argument("--ensemble-only", action="store_true")
+    ap.add_argument("--ensemble-max-grid", type=int, default=1024)  # largest patch side (1024: one patch per scenario)
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")   # keep the default tuning
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
@@ -557,7 +558,8 @@ def main():
             print(json.dumps({"amr": amr}), flush=True)
         return 0
     if args.ensemble_only:
-        ens = ensemble_measurement(args.ensemble_steps, args.warmup, stream, autotune=args.autotune)
+        ens = ensemble_measurement(args.ensemble_steps, args.warmup, stream, autotune=args.autotune,
+                                   max_grid=args.ensemble_max_grid)
         if rank == 0:
             print(json.dumps({"ensemble": ens}), flush=True)
         return 0
@@ -651,7 +653,7 @@ def main():
     # ---- subcycled 4-level AMR hierarchy (rank 0 reports its own)
     amr = amr_measurement(args.amr_steps, 2, stream, args.autotune) if args.amr_steps > 0 else None
     # ---- ensemble of 64 independent scenarios in one level
-    ens = ensemble_measurement(args.ensemble_steps, 3, stream, autotune=args.autotune) \
+    ens = ensemble_measurement(args.ensemble_steps, 3, stream, autotune=args.autotune, max_grid=args.ensemble_max_grid) \
         if args.ensemble_steps > 0 else None
 
     # ---- CPU baseline (rank 0, N = 1 only)
