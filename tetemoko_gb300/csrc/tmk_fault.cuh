@@ -403,9 +403,10 @@ TMK_D double sw_setbnd(const DevParams& P, const double* U, double* B, int bstri
   return st;
 }
 
-// PLASTICFLOW (srcLinElast/PlasticPhysicsF.ChF:74-181) on one side's stresses
+// PLASTICFLOW (srcLinElast/PlasticPhysicsF.ChF:74-181) on one side's stresses;
+// returns whether the point yielded (else only p_lam, set to 0, changed)
 template <typename T>
-TMK_D void plastic_flow(const DevParams& P, T& sxx, T& syy, T& szz, T& sxy, T& sxz, T& syz, T& p_lam,
+TMK_D bool plastic_flow(const DevParams& P, T& sxx, T& syy, T& szz, T& sxy, T& sxz, T& syz, T& p_lam,
                         T& p_gam, T dt) {
   const T mu = (T)P.p_mu, beta = (T)P.p_beta, eta = (T)P.p_eta, pb = (T)P.p_b, ph = (T)P.p_h;
   const T G = (T)P.G, K = (T)P.K;
@@ -415,7 +416,7 @@ TMK_D void plastic_flow(const DevParams& P, T& sxx, T& syy, T& szz, T& sxy, T& s
   T tau = sqrt(J2);
   T b = pb + p_gam * ph;
   T Y = tau - fmax(-mu * sigma + b, T(0));
-  if (Y <= T(0)) { p_lam = T(0); return; }
+  if (Y <= T(0)) { p_lam = T(0); return false; }
   p_lam = Y / (dt * (ph + G + mu * beta * K) + eta);
   p_gam = p_gam + dt * p_lam;
   T sig_e = sigma;
@@ -428,6 +429,7 @@ TMK_D void plastic_flow(const DevParams& P, T& sxx, T& syy, T& szz, T& sxy, T& s
   sxy = factor * sxy;
   sxz = factor * sxz;
   syz = factor * syz;
+  return true;
 }
 
 }  // namespace tmk

@@ -532,11 +532,13 @@ __global__ void __launch_bounds__(256) plastic_tiles_kernel(const PatchDev<Real>
       T u[6];
 #pragma unroll
       for (int c = 0; c < 6; ++c) u[c] = p.Uout[fab_idx(p, O + 3 + c, x, y)];
-      T lam = p.Uin[fab_idx(p, O + 9, x, y)];
+      T lam;                                   // the plastic rate is only written
       T gam = p.Uin[fab_idx(p, O + 10, x, y)];
-      plastic_flow<T>(P, u[0], u[1], u[2], u[3], u[4], u[5], lam, gam, dt);
+      // the stresses are stored back only where the point yielded (else unchanged)
+      if (plastic_flow<T>(P, u[0], u[1], u[2], u[3], u[4], u[5], lam, gam, dt)) {
 #pragma unroll
-      for (int c = 0; c < 6; ++c) p.Uout[fab_idx(p, O + 3 + c, x, y)] = u[c];
+        for (int c = 0; c < 6; ++c) p.Uout[fab_idx(p, O + 3 + c, x, y)] = u[c];
+      }
       p.Uout[fab_idx(p, O + 9, x, y)] = lam;
       p.Uout[fab_idx(p, O + 10, x, y)] = gam;
     }
