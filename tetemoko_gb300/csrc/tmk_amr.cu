@@ -242,22 +242,32 @@ __global__ void avgdown_kernel(const PatchDev<Real>* __restrict__ cp, const Patc
                                const AvgU* __restrict__ au, int nau, const AvgB* __restrict__ ab, int nab, int nb,
                                int r, double sU, double sB, int both) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < nau * NC) {                      // component-major: neighbouring threads, neighbouring cells
-    const AvgU e = au[t % nau];
-    const int c = t / nau;
+  if (t < nau) {                           // one coarse cell, all components: neighbouring threads, neighbouring cells
+    const AvgU e = au[t];
     const PatchDev<Real>& F = fp[e.fpatch];
-    Real sum = Real(0);
-    for (int jj = 0; jj < r; ++jj)
-      for (int ii = 0; ii < r; ++ii) sum = sum + F.Uin[fab_idx(F, c, r * e.ci + ii, r * e.cj + jj)];
     const PatchDev<Real>& C = cp[e.cpatch];
-    const size_t o = fab_idx(C, c, e.ci, e.cj);
-    const Real v = sum * (Real)sU;
-    ((Real*)C.Uin)[o] = v;
-    // lambda, gamma: a step without plasticity never rewrites them, keep both buffers equal
-    if (both && (c == 9 || c == 10 || c == 20 || c == 21)) C.Uout[o] = v;
+    const Real* src = F.Uin + fab_idx(F, 0, r * e.ci, r * e.cj);
+    const size_t fplane = (size_t)F.anx * F.any, frow = F.anx;
+    const size_t o = fab_idx(C, 0, e.ci, e.cj), cplane = (size_t)C.anx * C.any;
+    const Real s = (Real)sU;
+#pragma unroll 2
+    for (int c = 0; c < NC; ++c) {
+      Real sum = Real(0);
+      if (r == 2) {                        // the common ratio: four independent loads
+        const Real* q = src + c * fplane;
+        sum = sum + q[0]; sum = sum + q[1]; sum = sum + q[frow]; sum = sum + q[frow + 1];
+      } else {
+        for (int jj = 0; jj < r; ++jj)
+          for (int ii = 0; ii < r; ++ii) sum = sum + src[c * fplane + jj * frow + ii];
+      }
+      const Real v = sum * s;
+      ((Real*)C.Uin)[o + c * cplane] = v;
+      // lambda, gamma: a step without plasticity never rewrites them, keep both buffers equal
+      if (both && (c == 9 || c == 10 || c == 20 || c == 21)) C.Uout[o + c * cplane] = v;
+    }
     return;
   }
-  t -= nau * NC;
+  t -= nau;
   if (t < nab * nb) {
     const AvgB e = ab[t % nab];
     const int c = t / nab;
@@ -798,7 +808,7 @@ tmk_status launch_reflux(CFLink* k, cudaStream_t s) {
 template <typename Real>
 tmk_status launch_avgdown(CFLink* k, cudaStream_t s) {
   const int nb = k->F->ctx->nb;
-  const long long n = (long long)k->nau * NC + (long long)k->nab * nb;
+  const long long n = (long long)k->nau + (long long)k->nab * nb;
   if (!n) return TMK_OK;
   const PatchDev<Real>* cp = (const PatchDev<Real>*)k->C->dpatch[k->C->parity];
   const PatchDev<Real>* fp = (const PatchDev<Real>*)k->F->dpatch[k->F->parity];
