@@ -105,7 +105,7 @@ typedef struct { double mu, beta, eta, b, h; } tmk_plastic_params;
 
 /* AMRLevelLinElastFactory / LinElastPatchGodunov::define options */
 typedef struct {
-  int normal_pred_order;                  /* 0 CTU, 2 PPM (srcLinElast/LinElastPatchGodunov.cpp:272-287) */
+  int normal_pred_order;                  /* 0 CTU, 1 PLM, 2 PPM (srcLinElast/LinElastPatchGodunov.cpp:272-314) */
   int use_prim_limiting;
   int use_char_limiting;
   int boundary_type[6];                   /* x lo, x hi, y lo, y hi, z lo, z hi */
@@ -113,13 +113,15 @@ typedef struct {
   int plasticity;                         /* apply PLASTICCORRECTION after the step */
   int precision;                          /* TMK_PREC_* for level objects */
   int volume_kernel;                      /* TMK_VOLUME_* implementation of the volume update */
+  int use_fourth_order_slopes;            /* comp.use_fourth_order_slopes: PLM slopes of fourth order */
 } tmk_scheme;
 
 /* Implementations of the volume update (same results to rounding):
  * TILE  shared-memory tiles, one side of the fault per CTA (fuses plasticity);
  * MARCH column-marching warps with both sides packed per lane, plasticity as a
  *       pointwise pass after the update;
- * AUTO  MARCH.  Both store the coarse-fine face fluxes of coupled levels. */
+ * AUTO  MARCH (TILE with the PLM predictor, which the marching kernels do not
+ *       implement).  Both store the coarse-fine face fluxes of coupled levels. */
 enum { TMK_VOLUME_AUTO = 0, TMK_VOLUME_TILE = 1, TMK_VOLUME_MARCH = 2 };
 
 /* Chombo FArrayBox view: data[((c*(hi1-lo1+1)) + (j-lo1))*(hi0-lo0+1) + (i-lo0)] */

@@ -728,6 +728,69 @@ void ppmLimiter(FAB& dWm, FAB& dWp, int nc, const Box& box) {
       }
 }
 
+// Fourth-order slopes (Chombo fourthOrderSlopes; the limited fourth-order
+// slopes of Colella & Glaz 1985): dW4 = (4/3) dWc - (1/6)(dWvL_{i+1} + dWvL_{i-1})
+// with dWc the centred difference, where both neighbours lie in the domain;
+// the van Leer slope elsewhere.  Limiting is left to slopeLimiter.
+void fourthOrderSlopes(FAB& dW4, const FAB& W, const FAB& dWvL, int nc, int d, const Box& box, const Box& dom) {
+  int e0 = (d == 0), e1 = (d == 1);
+  for (int c = 0; c < nc; ++c)
+    for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+      for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+        int ii = d == 0 ? i : j;
+        if (ii - 1 >= dom.lo[d] && ii + 1 <= dom.hi[d]) {
+          double dwc = 0.5*(W(i+e0,j+e1,c) - W(i-e0,j-e1,c));
+          dW4(i,j,c) = (4.0/3.0)*dwc - (1.0/6.0)*(dWvL(i+e0,j+e1,c) + dWvL(i-e0,j-e1,c));
+        } else {
+          dW4(i,j,c) = dWvL(i,j,c);
+        }
+      }
+}
+
+// One-sided differences (Chombo oneSidedDifferences): dWm = W_i - W_{i-1},
+// dWp = W_{i+1} - W_i; next to a domain edge the missing one takes the other's value.
+void oneSidedDifferences(FAB& dWm, FAB& dWp, const FAB& W, int nc, int d, const Box& box, const Box& dom) {
+  int e0 = (d == 0), e1 = (d == 1);
+  for (int c = 0; c < nc; ++c)
+    for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+      for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+        int ii = d == 0 ? i : j;
+        bool hasL = ii - 1 >= dom.lo[d], hasR = ii + 1 <= dom.hi[d];
+        double m = hasL ? W(i,j,c) - W(i-e0,j-e1,c) : 0.0;
+        double p = hasR ? W(i+e0,j+e1,c) - W(i,j,c) : 0.0;
+        if (!hasL) m = p;
+        if (!hasR) p = m;
+        dWm(i,j,c) = m; dWp(i,j,c) = p;
+      }
+}
+
+// Slope limiter (Chombo slopeLimiter, the van Leer limiter): sign(dW) min(|dW|,
+// 2|dWm|, 2|dWp|) where dWm dWp > 0, else 0.
+void slopeLimiter(FAB& dW, const FAB& dWm, const FAB& dWp, int nc, const Box& box) {
+  for (int c = 0; c < nc; ++c)
+    for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+      for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+        double l = dWm(i,j,c), r = dWp(i,j,c), s = dW(i,j,c);
+        if (l*r > 0.0) {
+          double m = std::min(std::fabs(s), std::min(2.0*std::fabs(l), 2.0*std::fabs(r)));
+          dW(i,j,c) = (s >= 0.0) ? m : -m;
+        } else dW(i,j,c) = 0.0;
+      }
+}
+
+// PLM characteristic tracing (Chombo PLMNormalPred, Colella 1990):
+//   dWm = -1/2 (1 + min(lambda dt/dx, 0)) dW,  dWp = 1/2 (1 - max(lambda dt/dx, 0)) dW
+void plmNormalPred(FAB& dWm, FAB& dWp, const FAB& dW, const double* lambda, double dtbydx, int nc, const Box& box) {
+  for (int c = 0; c < nc; ++c) {
+    double sig = lambda[c] * dtbydx;
+    for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+      for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+        dWm(i,j,c) = -0.5 * (1.0 + std::min(sig, 0.0)) * dW(i,j,c);
+        dWp(i,j,c) = 0.5 * (1.0 - std::max(sig, 0.0)) * dW(i,j,c);
+      }
+  }
+}
+
 // PPM characteristic tracing (Colella & Woodward 1984 eq. 1.12): average of
 // the parabola over the domain of dependence |lambda| dt of the face the
 // characteristic moves towards; the other face keeps its limited value.
@@ -769,6 +832,42 @@ struct Patch {
     Phys Q = P;
     if (fd && fd->fric) { Q.rs.a = (*fd->fric)(i, j, 0); Q.rs.b = (*fd->fric)(i, j, 1); Q.rs.L = (*fd->fric)(i, j, 2); }
     return Q;
+  }
+
+  // LinElastPatchGodunov::PLMNormalPred (srcLinElast/LinElastPatchGodunov.cpp:486-601)
+  void PLMNormalPred(FAB& WM, FAB& WP, double dt, const FAB& W, int d, const Box& box) {
+    const int nc = 22;
+    const bool charL = P.sch.use_char_limiting, primL = P.sch.use_prim_limiting;
+    const bool fourth = P.sch.use_fourth_order_slopes != 0;
+    FAB dW(box, nc);
+    if (fourth) {
+      Box boxVL = isect(growd(box, d, 1), dom);
+      FAB dWvL(boxVL, nc);
+      vanLeerSlopes(dWvL, W, nc, charL || primL, d, boxVL, dom);
+      fourthOrderSlopes(dW, W, dWvL, nc, d, box, dom);
+    } else {
+      vanLeerSlopes(dW, W, nc, charL || primL, d, box, dom);
+    }
+    WM.define(box, nc); WP.define(box, nc);
+    if (charL || fourth) oneSidedDifferences(WM, WP, W, nc, d, box, dom);
+    double lambda[22]; charvalues(P, lambda);
+    std::vector<double> tmp(22);
+    auto apply = [&](FAB& F, bool analyse) {
+      for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+        for (int i = box.lo[0]; i <= box.hi[0]; ++i) {
+          for (int c = 0; c < nc; ++c) tmp[c] = F(i,j,c);
+          if (analyse) charanalysis(P, tmp.data(), d); else charsynthesis(P, tmp.data(), d);
+          for (int c = 0; c < nc; ++c) F(i,j,c) = tmp[c];
+        }
+    };
+    if (charL) { apply(WM, true); apply(WP, true); apply(dW, true); }
+    if ((charL || primL) && (charL || fourth)) slopeLimiter(dW, WM, WP, nc, box);
+    if (!charL) apply(dW, true);
+    plmNormalPred(WM, WP, dW, lambda, dt / dx, nc, box);
+    apply(WM, false); apply(WP, false);
+    for (int c = 0; c < nc; ++c)
+      for (int j = box.lo[1]; j <= box.hi[1]; ++j)
+        for (int i = box.lo[0]; i <= box.hi[0]; ++i) { WM(i,j,c) += W(i,j,c); WP(i,j,c) += W(i,j,c); }
   }
 
   // LinElastPatchGodunov::PPMNormalPred (srcLinElast/LinElastPatchGodunov.cpp:603-702)
@@ -930,6 +1029,8 @@ struct Patch {
     for (int d = 0; d < 2; ++d) {
       if (P.sch.normal_pred_order == 2) {
         PPMNormalPred(WM[d], WP[d], dt, W, d, slopeBox);
+      } else if (P.sch.normal_pred_order == 1) {
+        PLMNormalPred(WM[d], WP[d], dt, W, d, slopeBox);
       } else {   // CTUNormalPred: straight copy
         WM[d].define(slopeBox, 22); WP[d].define(slopeBox, 22);
         for (int c = 0; c < 22; ++c)
@@ -1004,7 +1105,7 @@ bool setup(Phys& P, const tmk_elastic_params* e, const tmk_scheme* s, const tmk_
   if (rs) P.rs = *rs;
   if (sw) P.sw = *sw;
   if (pl) { P.p_mu = pl->mu; P.p_beta = pl->beta; P.p_eta = pl->eta; P.p_b = pl->b; P.p_h = pl->h; }
-  if (s->normal_pred_order != 0 && s->normal_pred_order != 2) return false;
+  if (s->normal_pred_order < 0 || s->normal_pred_order > 2) return false;
   if (s->use_char_limiting && s->use_prim_limiting) return false;
   return true;
 }

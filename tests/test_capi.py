@@ -57,9 +57,9 @@ def test_context_argument_errors(cuda_lib):
     sc2 = S.rate_state(nx=32, ny=16)
     sc2.scheme.use_char_limiting = 1
     assert _create(lib, sc2)[0] == 5
-    # PLM normal predictor is not built
+    # a normal predictor order other than CTU (0), PLM (1), PPM (2)
     sc3 = S.rate_state(nx=32, ny=16)
-    sc3.scheme.normal_pred_order = 1
+    sc3.scheme.normal_pred_order = 3
     assert _create(lib, sc3)[0] == 5
     # invalid boundary type ("Invalid Boundary Type")
     sc4 = S.rate_state(nx=32, ny=16)

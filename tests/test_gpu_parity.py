@@ -36,6 +36,15 @@ def _scenarios():
     sc = S.slip_weakening(nx=64, ny=32, dx=0.1)
     sc.scheme.use_prim_limiting = 0
     out.append(("sw_unlimited", sc))
+    # PLM normal predictor: fourth-order slopes with primitive limiting (the decks'
+    # slope setting), second-order slopes, characteristic limiting, no limiting
+    for name, prim, char, fourth in (("rs_plm4", 1, 0, 1), ("sw_plm2", 1, 0, 0), ("sw_plm4_char", 0, 1, 1),
+                                     ("rs_plm4_unlimited", 0, 0, 1)):
+        sc = S.rate_state(nx=64, ny=32, dx=0.1) if name.startswith("rs") else S.slip_weakening(nx=64, ny=32, dx=0.1)
+        sc.scheme.normal_pred_order = 1
+        sc.scheme.use_prim_limiting, sc.scheme.use_char_limiting = prim, char
+        sc.scheme.use_fourth_order_slopes = fourth
+        out.append((name, sc))
     return out
 
 
@@ -205,5 +214,33 @@ def test_fault_friction_descriptor_checks(cuda_lib):
     lvl = LinElastLevelGodunov(ctx, [(0, 0, 63, 31)])
     with pytest.raises(A.TmkError):
         lvl.set_fault_friction(0, S.friction_field(sc))   # slip weakening has no a, b, L
+    lvl.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("name", ["rs_plm4", "sw_plm4_char"])
+def test_plm_level_steps_match_oracle(cuda_lib, name):
+    """Ten steps of a level of uneven patches with the PLM predictor (the tile
+    volume kernel, the fault kernel's PLM predictors) against the oracle."""
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    sc = dict(SCEN)[name]
+    rng = np.random.default_rng(97)
+    boxes = [(0, 0, 20, 9), (21, 0, 63, 9), (0, 10, 31, 31), (32, 10, 63, 31)]
+    Ug = perturbed_state(sc, rng, amp_v=0.05, amp_s=1.0)
+    Bg = sc.initial_B()
+    Ur, Br = Ug.copy(), Bg.copy()
+    ctx = Context(sc)
+    lvl = LinElastLevelGodunov(ctx, boxes)
+    lvl.set_level(Ug, Bg)
+    dt = sc.dt()
+    for n in range(10):
+        assert O.level_step(sc, Ur, Br, boxes, n * dt, dt) == 0
+        lvl.step(n * dt, dt)
+    Uo, Bo = Ug.copy(), Bg.copy()
+    lvl.get_level(Uo, Bo)
+    g = A.TMK_NGHOST
+    assert rel_err(Uo[:, g:-g, g:-g], Ur[:, g:-g, g:-g]) <= 1e-11
+    assert rel_err(Bo[:, g:-g], Br[:, g:-g]) <= 1e-11
+    assert lvl.status()[0] == 0
     lvl.close()
     ctx.close()

@@ -219,3 +219,30 @@ def test_per_face_friction_in_the_oracle():
         runs.append((Ur, Br))
     assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
     assert not np.array_equal(runs[0][1][10], runs[2][1][10])
+
+
+def test_plm_predictor_in_the_oracle():
+    """The PLM normal predictor keeps a uniform state uniform and, on a smooth
+    perturbation, stays within the second-order agreement of the PPM step;
+    fourth-order and second-order slopes differ only slightly."""
+    res = {}
+    for order, fourth in ((2, 1), (1, 1), (1, 0)):
+        sc = S.rate_state(nx=48, ny=24, dx=0.1)
+        sc.scheme.normal_pred_order, sc.scheme.use_fourth_order_slopes = order, fourth
+        U, B = sc.initial_U(), sc.initial_B()
+        U0 = U.copy()
+        assert O.level_step(sc, U, B, [(0, 0, 47, 23)], 0.0, sc.dt()) == 0
+        far = (slice(None), slice(12, 20), slice(30, 40))      # away from the fault and the nucleation
+        assert np.array_equal(U[far], U0[far])
+        x = (np.arange(48 + 8) + 0.5) / 48.0
+        U = sc.initial_U()
+        U[1] += 0.05 * np.sin(2 * np.pi * x)[None, :]
+        B = sc.initial_B()
+        for k in range(3):
+            assert O.level_step(sc, U, B, [(0, 0, 47, 23)], k * sc.dt(), sc.dt()) == 0
+        assert np.isfinite(U).all()
+        res[(order, fourth)] = U[:, 4:-4, 4:-4]
+    ref = np.abs(res[(2, 1)][1]).max()
+    assert np.abs(res[(1, 1)][1] - res[(2, 1)][1]).max() < 0.05 * ref
+    assert np.abs(res[(1, 1)][1] - res[(1, 0)][1]).max() < 0.05 * ref
+    assert not np.array_equal(res[(1, 1)], res[(1, 0)])

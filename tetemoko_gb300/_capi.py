@@ -65,7 +65,7 @@ class Scheme(C.Structure):
     _fields_ = [("normal_pred_order", C.c_int), ("use_prim_limiting", C.c_int),
                 ("use_char_limiting", C.c_int), ("boundary_type", C.c_int * 6),
                 ("fault_law", C.c_int), ("plasticity", C.c_int), ("precision", C.c_int),
-                ("volume_kernel", C.c_int)]
+                ("volume_kernel", C.c_int), ("use_fourth_order_slopes", C.c_int)]
 
 
 TMK_VOLUME_AUTO, TMK_VOLUME_TILE, TMK_VOLUME_MARCH = 0, 1, 2

@@ -41,7 +41,7 @@ extern "C" tmk_status tmk_context_create(const tmk_elastic_params* e, const tmk_
   if (!out) return TMK_ERR_BAD_DESC;
   *out = nullptr;
   if (!e || !s) return TMK_ERR_BAD_DESC;
-  if (s->normal_pred_order != 0 && s->normal_pred_order != 2) return TMK_ERR_UNSUPPORTED;
+  if (s->normal_pred_order < 0 || s->normal_pred_order > 2) return TMK_ERR_UNSUPPORTED;
   if (s->use_char_limiting && s->use_prim_limiting) return TMK_ERR_UNSUPPORTED;  // PPMNormalPred MayDay
   for (int k = 0; k < 4; ++k)
     if (s->boundary_type[k] < 0 || s->boundary_type[k] > 2) return TMK_ERR_BAD_DESC;  // "Invalid Boundary Type"
@@ -70,6 +70,7 @@ extern "C" tmk_status tmk_context_create(const tmk_elastic_params* e, const tmk_
   for (int sd = 0; sd < 2; ++sd)
     for (int k = 0; k < 11; ++k) P.bg[11 * sd + k] = bg[k];
   P.order = s->normal_pred_order; P.prim_lim = s->use_prim_limiting; P.char_lim = s->use_char_limiting;
+  P.fourth = s->use_fourth_order_slopes ? 1 : 0;
   for (int k = 0; k < 6; ++k) P.bc[k] = s->boundary_type[k];
   P.fault_law = s->fault_law;
   P.plasticity = s->plasticity;
@@ -189,7 +190,8 @@ void make_march_items(std::vector<tmk::MarchItem>& out, std::vector<tmk::MarchIt
 constexpr int kFaultWaitRows = 0;
 constexpr int kFaultDisplace = 1;
 
-bool uses_march(const tmk_scheme& s) { return s.volume_kernel != TMK_VOLUME_TILE; }
+// the marching kernels implement the PPM and CTU predictors; PLM runs the tile kernel
+bool uses_march(const tmk_scheme& s) { return s.volume_kernel != TMK_VOLUME_TILE && s.normal_pred_order != 1; }
 
 tmk_tuning default_tuning(int march_allowed) {
   tmk_tuning t;
@@ -602,6 +604,7 @@ bool same_bulk(const tmk_context* a, const tmk_context* b) {
   for (int k = 0; k < 22; ++k) if (p.bg[k] != q.bg[k]) return false;
   const tmk_scheme &s = a->scheme, &t = b->scheme;
   if (s.normal_pred_order != t.normal_pred_order || s.use_prim_limiting != t.use_prim_limiting ||
+      s.use_fourth_order_slopes != t.use_fourth_order_slopes ||
       s.use_char_limiting != t.use_char_limiting || s.fault_law != t.fault_law || s.plasticity != t.plasticity ||
       s.precision != t.precision || s.volume_kernel != t.volume_kernel)
     return false;

@@ -34,6 +34,7 @@ struct DevParams {
   double bg[22];
   // scheme
   int order, prim_lim, char_lim;
+  int fourth;               // fourth-order slopes (PLM)
   int bc[6];
   int fault_law;            // 0 none, 1 RS, 2 SW
   int plasticity;
@@ -350,18 +351,94 @@ TMK_D void ppm_trace(T sig, T& m, T& p) {
   }
 }
 
+// PLM stages (LinElastPatchGodunov::PLMNormalPred, srcLinElast/
+// LinElastPatchGodunov.cpp:486-601, with Chombo's slope utilities restated):
+// the slope of the middle cell of w[0..4] -- van Leer, or where both
+// neighbours lie in the domain and `fourth` is set the fourth-order slope
+// (4/3) dWc - (1/6)(dWvL_{+1} + dWvL_{-1}) (Colella & Glaz 1985) --, its
+// one-sided differences (the missing one next to a domain edge takes the
+// other's value) and the van Leer limiter of a slope by them.
+template <typename T>
+TMK_D T plm_slope(const T* w, const bool* in, bool limit, bool fourth) {
+  const T s0 = vl_slope(w[1], w[2], w[3], in[1], in[3], limit);
+  if (!fourth || !in[1] || !in[3]) return s0;
+  const T sm = vl_slope(w[0], w[1], w[2], in[0], true, limit);
+  const T sp = vl_slope(w[2], w[3], w[4], true, in[4], limit);
+  const T dwc = T(0.5) * (w[3] - w[1]);
+  return (T(4) / T(3)) * dwc - (T(1) / T(6)) * (sp + sm);
+}
+template <typename T>
+TMK_D void plm_onesided(const T* w, const bool* in, T& m, T& p) {
+  m = in[1] ? w[2] - w[1] : T(0);
+  p = in[3] ? w[3] - w[2] : T(0);
+  if (!in[1]) m = p;
+  if (!in[3]) p = m;
+}
+template <typename T>
+TMK_D T plm_limit(T s, T l, T r) {
+  if (l * r > T(0)) {
+    const T m = fmin(fabs(s), fmin(T(2) * fabs(l), T(2) * fabs(r)));
+    return s >= T(0) ? m : -m;
+  }
+  return T(0);
+}
+
+// PLM normal predictor of one side of one cell (characteristic tracing
+// dWm = -1/2 (1 + min(sig, 0)) dW, dWp = 1/2 (1 - max(sig, 0)) dW, Colella 1990)
+template <int D, typename T>
+TMK_D void plm_predict(const Consts<T>& k, T rv, const T (*w5)[5], const bool* in, bool prim_lim, bool char_lim,
+                       bool fourth, const T* sig, T* WM, T* WP) {
+  const bool limit = prim_lim || char_lim;
+  T dW[NSIDE], dm[NSIDE], dp[NSIDE];
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) {
+    dW[c] = plm_slope(w5[c], in, limit, fourth);
+    dm[c] = T(0); dp[c] = T(0);
+    if (char_lim || fourth) plm_onesided(w5[c], in, dm[c], dp[c]);
+  }
+  T cW[NSIDE];
+  if (char_lim) {
+    T cm[NSIDE], cp[NSIDE];
+    char_analysis<D>(k, rv, dm, cm);
+    char_analysis<D>(k, rv, dp, cp);
+    char_analysis<D>(k, rv, dW, cW);
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) cW[c] = plm_limit(cW[c], cm[c], cp[c]);
+  } else {
+    if (prim_lim && fourth) {
+#pragma unroll
+      for (int c = 0; c < NSIDE; ++c) dW[c] = plm_limit(dW[c], dm[c], dp[c]);
+    }
+    char_analysis<D>(k, rv, dW, cW);
+  }
+  T cmo[NSIDE], cpo[NSIDE];
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) {
+    cmo[c] = -T(0.5) * (T(1) + fmin(sig[c], T(0))) * cW[c];
+    cpo[c] = T(0.5) * (T(1) - fmax(sig[c], T(0))) * cW[c];
+  }
+  char_synthesis<D>(k, rv, cmo, WM);
+  char_synthesis<D>(k, rv, cpo, WP);
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) { WM[c] += w5[c][2]; WP[c] += w5[c][2]; }
+}
+
 // Normal predictor of one side of one cell in direction D (order 2: PPM;
-// order 0: CTUNormalPred, a straight copy of the cell state to both faces,
-// srcLinElast/LinElastPatchGodunov.cpp:471-483).
+// order 1: PLM; order 0: CTUNormalPred, a straight copy of the cell state to
+// both faces, srcLinElast/LinElastPatchGodunov.cpp:471-483).
 // Full PPM normal predictor of one side of one cell in direction D:
 // w5[c][k] holds component c at cells -2..+2.  Produces WM (lo face) and WP.
 // sig[9] are the characteristic Courant numbers (-cp,-cs,-cs,0,0,0,cs,cs,cp)*dt/dx.
 template <int D, typename T>
 TMK_D void ppm_predict(const Consts<T>& k, T rv, const T (*w5)[5], const bool* in, bool prim_lim,
-                       bool char_lim, const T* sig, T* WM, T* WP, int order = 2) {
+                       bool char_lim, const T* sig, T* WM, T* WP, int order = 2, bool fourth = false) {
   if (order == 0) {
 #pragma unroll
     for (int c = 0; c < NSIDE; ++c) { WM[c] = w5[c][2]; WP[c] = w5[c][2]; }
+    return;
+  }
+  if (order == 1) {
+    plm_predict<D, T>(k, rv, w5, in, prim_lim, char_lim, fourth, sig, WM, WP);
     return;
   }
   T dm[NSIDE], dp[NSIDE];

@@ -78,12 +78,22 @@ TMK_D void fault_ypred_side(const PatchDev<Real>& p, const DevParams& P, const C
     for (int m = 0; m < 5; ++m) w5[c][m] = in[m] ? (T)p.Uin[fab_idx(p, 11 * s + c, i, j0 - 2 + m)] : T(0);
   T WM[NSIDE], WP[NSIDE];
   T rv = (s == 1) ? T(-1) : T(1);
-  ppm_predict<1, T>(k, rv, w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM, WP, P.order);
+  ppm_predict<1, T>(k, rv, w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM, WP, P.order, P.fourth != 0);
   for (int c = 0; c < NSIDE; ++c) out11[c] = (double)WM[c];
   for (int c = 9; c < 11; ++c) {
     T w[5];
     for (int m = 0; m < 5; ++m) w[m] = in[m] ? (T)p.Uin[fab_idx(p, 11 * s + c, i, j0 - 2 + m)] : T(0);
     if (P.order == 0) { out11[c] = (double)w[2]; continue; }
+    if (P.order == 1) {          // PLM: lo-face value of a zero-speed component
+      T sl = plm_slope(w, in, lim, P.fourth != 0);
+      if (lim && (P.char_lim || P.fourth)) {
+        T m, p1;
+        plm_onesided(w, in, m, p1);
+        sl = plm_limit(sl, m, p1);
+      }
+      out11[c] = (double)(-T(0.5) * sl + w[2]);
+      continue;
+    }
     T dm, dp;
     ppm_deltas(w, in, lim, dm, dp);
     if (lim) ppm_limit(dm, dp);
@@ -101,7 +111,7 @@ TMK_D void fault_xpred_side(const PatchDev<Real>& p, const DevParams& P, const C
   T w5[NSIDE][5];
   for (int c = 0; c < NSIDE; ++c)
     for (int m = 0; m < 5; ++m) w5[c][m] = in[m] ? (T)p.Uin[fab_idx(p, 11 * s + c, i - 2 + m, j0)] : T(0);
-  ppm_predict<0, T>(k, T(1), w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM, WP, P.order);
+  ppm_predict<0, T>(k, T(1), w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM, WP, P.order, P.fourth != 0);
 }
 
 // x face state (first pass) of one side at face f of row j0 from the cells
@@ -349,7 +359,7 @@ __global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __rest
     for (int c = 0; c < NSIDE; ++c)
 #pragma unroll
       for (int m = 0; m < 5; ++m) w5[c][m] = sm.W[c][py + 2][px + m];
-    ppm_predict<0, T>(k, T(1), w5, in, plim, clim, sig, WM, WP, P.order);
+    ppm_predict<0, T>(k, T(1), w5, in, plim, clim, sig, WM, WP, P.order, P.fourth != 0);
 #pragma unroll
     for (int c = 0; c < NSIDE; ++c) { sm.WMx[c][py][px] = WM[c]; sm.WPx[c][py][px] = WP[c]; }
 #pragma unroll
@@ -358,7 +368,7 @@ __global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __rest
     for (int c = 0; c < NSIDE; ++c)
 #pragma unroll
       for (int m = 0; m < 5; ++m) w5[c][m] = sm.W[c][py + m][px + 2];
-    ppm_predict<1, T>(k, rvy, w5, in, plim, clim, sig, WM, WP, P.order);
+    ppm_predict<1, T>(k, rvy, w5, in, plim, clim, sig, WM, WP, P.order, P.fourth != 0);
 #pragma unroll
     for (int c = 0; c < NSIDE; ++c) { sm.WMy[c][py][px] = WM[c]; sm.WPy[c][py][px] = WP[c]; }
   }

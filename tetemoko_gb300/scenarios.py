@@ -97,6 +97,7 @@ def _scheme(fault_law: int, precision: int = A.TMK_PREC_FP64, plasticity: int = 
     s.fault_law = fault_law
     s.plasticity = plasticity
     s.precision = precision
+    s.use_fourth_order_slopes = 1     # the decks' setting (used by the PLM predictor only)
     return s
 
 
