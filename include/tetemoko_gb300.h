@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TMK_ABI_VERSION 1
+#define TMK_ABI_VERSION 2   /* 2: tmk_scheme gained use_fourth_order_slopes */
 
 #define TMK_NCOMP      22   /* state components, srcLinElast/LEINDEX.H:12-47 */
 #define TMK_NSIDE_COMP 11   /* IX_OFFSET, srcLinElast/LEINDEX.H:23 */
