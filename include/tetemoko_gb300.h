@@ -234,6 +234,39 @@ tmk_status tmk_plastic_update(tmk_context* ctx, const tmk_fab* U,
 tmk_status tmk_max_wave_speed(const tmk_context* ctx, double* speed);
 
 /* ---------------------------------------------------------------------------
+ * 3-D (a CH_SPACEDIM == 3 build of the reference).  The fault is the domain's
+ * y-lo plane, spanning x and z.
+ * Chombo FArrayBox view: data[((c*nz + (k-lo2))*ny + (j-lo1))*nx + (i-lo0)] */
+typedef struct {
+  double* data;
+  int lo[3], hi[3];
+  int ncomp;
+} tmk_fab3;
+
+typedef struct { int lo[3], hi[3]; } tmk_box3;   /* cell-centred, inclusive */
+
+/* LinElastPatchGodunov::updateState with CH_SPACEDIM == 3
+ * (srcLinElast/LinElastPatchGodunov.cpp:101-129, 174-469: the 3-D corner
+ * transport upwind corrections of :329-381 and :422-440) on one patch, FP64,
+ * with the fault laws' 3-D forms (ibcLinElast/RSIBCF.ChF, SWIBCF.ChF z terms).
+ * U: device FAB of 22 comps containing grow(valid, 3) & domain, updated in
+ * place over valid (lambda, gamma and ghosts untouched).  B: when the scheme
+ * has a fault law and valid starts on the domain's y-lo plane, the fault's
+ * boundary data, a device FAB3 with lo[1] = hi[1] = domain lo[1] covering
+ * grow(valid, 1) & domain in x and z (nbdry comps); else ignored.  F0, F1, F2:
+ * optional device FAB3s over the faces of valid in x, y, z (22 comps) that
+ * receive the fluxes (for the flux registers). */
+tmk_status tmk_patch_update_state_3d(tmk_context* ctx, const tmk_fab3* U, const tmk_fab3* B,
+                                     const tmk_fab3* F0, const tmk_fab3* F1, const tmk_fab3* F2,
+                                     const tmk_box3* valid, const tmk_box3* domain,
+                                     double dx, double time, double dt,
+                                     double* max_wave_speed, void* stream);
+
+/* LinElastPhysics::plasticUpdate -> PLASTICCORRECTION on a 3-D device FAB over box. */
+tmk_status tmk_plastic_update_3d(tmk_context* ctx, const tmk_fab3* U, const tmk_box3* box,
+                                 double dt, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Device-resident level (LinElastLevelGodunov::define/step/plasticUpdate,
  * srcLinElast/LinElastLevelGodunov.cpp:45-398, 643-667).  The level owns the
  * device mirrors of every patch's U (two buffers, swapped each step) and B.

@@ -59,6 +59,9 @@ def lib() -> C.CDLL:
         L.tmko_patch_update_state.argtypes = [E, S, R, W, dp, ip, ip, dp, C.c_int, C.c_int, dp, dp,
                                               ip, ip, ip, ip, C.c_double, C.c_double, C.c_double]
         L.tmko_plastic_correction.argtypes = [E, PL, dp, ip, ip, ip, ip, C.c_double]
+        L.tmko_patch_update_state_3d.argtypes = [E, S, R, W, dp, ip, ip, dp, ip, ip, dp, dp, dp,
+                                                 ip, ip, ip, ip, C.c_double, C.c_double, C.c_double]
+        L.tmko_plastic_correction_3d.argtypes = [E, PL, dp, ip, ip, ip, ip, C.c_double]
         L.tmko_level_step.argtypes = [E, S, R, W, PL, ip, ip, C.c_int, ip, dp, dp, C.c_double,
                                       C.c_double, C.c_double, C.c_int]
         L.tmko_level_step_fric.argtypes = [E, S, R, W, PL, ip, ip, C.c_int, ip, dp, dp, dp, C.c_double,
@@ -182,6 +185,39 @@ def plastic_correction(sc, U: np.ndarray, ulo, blo, bhi, dt: float) -> None:
     uhi = (ulo[0] + U.shape[2] - 1, ulo[1] + U.shape[1] - 1)
     lib().tmko_plastic_correction(C.byref(sc.elastic), C.byref(sc.plastic), _dp(U), _iv(*ulo),
                                   _iv(*uhi), _iv(*blo), _iv(*bhi), dt)
+
+
+def patch_update_state_3d(sc, U: np.ndarray, ulo, valid_lo, valid_hi, domain_lo, domain_hi,
+                          B: np.ndarray | None, blo, dx: float, time: float, dt: float,
+                          with_flux: bool = False):
+    """LinElastPatchGodunov::updateState in 3-D on a host FAB U (22, nz, ny, nx)
+    starting at cell ulo = (i, j, k); B (nb, nz_b, nx_b) the fault data on the
+    domain's y-lo plane starting at blo = (i, k).  U, B are updated in place.
+    Returns (rc, [F0, F1, F2]) with the face fluxes of the valid box."""
+    assert U.shape[0] == 22 and U.ndim == 4
+    uhi = (ulo[0] + U.shape[3] - 1, ulo[1] + U.shape[2] - 1, ulo[2] + U.shape[1] - 1)
+    F = [None, None, None]
+    if with_flux:
+        n = [valid_hi[d] - valid_lo[d] + 1 for d in range(3)]
+        for d in range(3):
+            m = list(n)
+            m[d] += 1
+            F[d] = np.zeros((22, m[2], m[1], m[0]))
+    if B is not None:
+        bhi = (blo[0] + B.shape[2] - 1, blo[1] + B.shape[1] - 1)
+    else:
+        blo, bhi = (0, 0), (0, 0)
+    rc = lib().tmko_patch_update_state_3d(
+        C.byref(sc.elastic), C.byref(sc.scheme), _ref(sc.rs), _ref(sc.sw), _dp(U), _iv(*ulo), _iv(*uhi),
+        _dp(B), _iv(*blo), _iv(*bhi), _dp(F[0]), _dp(F[1]), _dp(F[2]), _iv(*valid_lo), _iv(*valid_hi),
+        _iv(*domain_lo), _iv(*domain_hi), dx, time, dt)
+    return rc, F
+
+
+def plastic_correction_3d(sc, U: np.ndarray, ulo, blo, bhi, dt: float) -> None:
+    uhi = (ulo[0] + U.shape[3] - 1, ulo[1] + U.shape[2] - 1, ulo[2] + U.shape[1] - 1)
+    lib().tmko_plastic_correction_3d(C.byref(sc.elastic), C.byref(sc.plastic), _dp(U), _iv(*ulo),
+                                     _iv(*uhi), _iv(*blo), _iv(*bhi), dt)
 
 
 def level_step(sc, Ug: np.ndarray, Bg: np.ndarray | None, boxes, time: float, dt: float,

@@ -549,11 +549,16 @@ bool rssetbndpt(const Phys& P, double* Bout, const double* Bin, const double* U,
 
 // SWFAULTBCF (ibcLinElast/SWIBCF.ChF:79-267) at one fault face.  `off` is the
 // side-2 component offset (9 in the reference source, 11 when corrected).
-void swfaultpt(const Phys& P, double* Wg, const double* Wi, const double* B, double xcell) {
+// With `zcell` (the 3-D path) the nucleation patches and the friction box are
+// products of x and z profiles: tau_0 += (tau valx) valz and the box value is
+// valx valz (:118-126,175-180, CHF_DTERM over x and z).
+void swfaultpt(const Phys& P, double* Wg, const double* Wi, const double* B, double xcell,
+               const double* zcell = nullptr) {
   const tmk_sw_params& w = P.sw;
   const int off = (w.layout == TMK_SW_LAYOUT_OFFSET11) ? 11 : 9;
   const double Zs = P.Zs, Zp = P.Zp, lam = P.lam, G = P.G;
   double x = xcell - w.fric_box_center[0];
+  double z = zcell ? *zcell - w.fric_box_center[1] : 0.0;
   double vx1 = Wi[0], vy1 = Wi[1], vz1 = Wi[2], sxx1 = Wi[3], syy1 = Wi[4], szz1 = Wi[5];
   double sxy1 = Wi[6], sxz1 = Wi[7], syz1 = Wi[8];
   double vx2 = Wi[off+0], vy2 = Wi[off+1], vz2 = Wi[off+2], sxx2 = Wi[off+3], syy2 = Wi[off+4];
@@ -567,7 +572,12 @@ void swfaultpt(const Phys& P, double* Wg, const double* Wi, const double* B, dou
   double tau_0 = 0;
   for (int ip = 0; ip < w.num_patches; ++ip) {
     double valx = smoothfunc(w.smooth, std::fabs(x - w.xc[ip]) - w.xw[ip]);
-    tau_0 = tau_0 + w.tau[ip] * valx;
+    if (zcell) {
+      double valz = smoothfunc(w.smooth, std::fabs(z - w.zc[ip]) - w.zw[ip]);
+      tau_0 = tau_0 + w.tau[ip] * valx * valz;
+    } else {
+      tau_0 = tau_0 + w.tau[ip] * valx;
+    }
   }
   double a1 = 0.5*(wpxy2-wpxy1)+tau_0, a2 = 0.5*(wpyz2-wpyz1);
   double tau_lock = std::sqrt(a1*a1 + a2*a2);
@@ -576,7 +586,13 @@ void swfaultpt(const Phys& P, double* Wg, const double* Wi, const double* B, dou
   vy1 = -(wpyy1+wpyy2)/2.0/Zp;
   vy2 = -(wpyy1+wpyy2)/2.0/Zp;
   double valx = boxcarfunc(w.fric_box_width[0], std::fabs(x));
-  double fric = w.fs*valx + (1-valx)*w.outside_friction;
+  double fric;
+  if (zcell) {
+    double valz = boxcarfunc(w.fric_box_width[1], std::fabs(z));
+    fric = w.fs*valx*valz + (1-valx*valz)*w.outside_friction;
+  } else {
+    fric = w.fs*valx + (1-valx)*w.outside_friction;
+  }
   fric = fric-(fric-w.fd)*std::min(1.0, B[7]/w.dw);
   double tau = std::min(tau_lock, -syy1*fric)-tau_0;
   double phi_xy = 0.5*(wpxy2-wpxy1);
@@ -1116,6 +1132,410 @@ FAB wrap(const double* p, const int lo[2], const int hi[2], int nc) {
   return f;
 }
 void unwrap(const FAB& f, double* p) { std::memcpy(p, f.v.data(), f.v.size()*sizeof(double)); }
+
+// ================================================================ 3-D path ==
+// LinElastPatchGodunov::updateState with CH_SPACEDIM == 3
+// (srcLinElast/LinElastPatchGodunov.cpp:174-454): the same normal predictors
+// and Riemann solves in three directions, then the 3-D corner transport
+// upwind corrections -- WHalf2[d1][d2], the d1 face states after the normal
+// states were moved by -(1/3) dt/dx A dW/dx of the first-pass d2 face states
+// (:329-381), and the final d1 states corrected by both WHalf2[d2][d3] with
+// -(1/2) dt/dx (:422-440) -- with the fault's boundary data predicted at
+// (1/3) dt and (1/2) dt in the reference's call order.  The fault is the y-lo
+// face of the domain, a plane over x and z; the rate-and-state law has no z
+// dependence (ibcLinElast/RSIBCF.ChF zeroes the antiplane characteristic and
+// its nucleation is a function of x), the slip-weakening law has z profiles.
+// Cells outside ccBox[d2] of a quasilinear update keep their value (the
+// reference adds an AdWdx FAB it never wrote there; no face that the returned
+// state, fluxes or boundary data depend on reads those cells).
+struct Box3 {
+  int lo[3], hi[3];
+  bool empty() const { return lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]; }
+  bool contains(int i, int j, int k) const {
+    return i >= lo[0] && i <= hi[0] && j >= lo[1] && j <= hi[1] && k >= lo[2] && k <= hi[2];
+  }
+};
+Box3 mk3(const int lo[3], const int hi[3]) { Box3 b; for (int d = 0; d < 3; ++d) { b.lo[d] = lo[d]; b.hi[d] = hi[d]; } return b; }
+Box3 grow3(Box3 b, int n) { for (int d = 0; d < 3; ++d) { b.lo[d] -= n; b.hi[d] += n; } return b; }
+Box3 growd3(Box3 b, int d, int n) { b.lo[d] -= n; b.hi[d] += n; return b; }
+Box3 isect3(Box3 a, const Box3& b) {
+  for (int d = 0; d < 3; ++d) { a.lo[d] = std::max(a.lo[d], b.lo[d]); a.hi[d] = std::min(a.hi[d], b.hi[d]); }
+  return a;
+}
+Box3 nodes3(Box3 b, int d) { b.hi[d] += 1; return b; }
+
+struct FAB3 {
+  Box3 b; int nc = 0; std::vector<double> v;
+  FAB3() {}
+  FAB3(Box3 bx, int n) { define(bx, n); }
+  void define(Box3 bx, int n) {
+    b = bx; nc = n;
+    size_t sz = (size_t)n;
+    for (int d = 0; d < 3; ++d) sz *= (size_t)(b.hi[d] - b.lo[d] + 1);
+    v.assign(sz, 0.0);
+  }
+  size_t idx(int i, int j, int k, int c) const {
+    size_t nx = b.hi[0]-b.lo[0]+1, ny = b.hi[1]-b.lo[1]+1, nz = b.hi[2]-b.lo[2]+1;
+    return (((size_t)c * nz + (size_t)(k-b.lo[2])) * ny + (size_t)(j-b.lo[1])) * nx + (size_t)(i-b.lo[0]);
+  }
+  double& operator()(int i, int j, int k, int c) { return v[idx(i,j,k,c)]; }
+  double operator()(int i, int j, int k, int c) const { return v[idx(i,j,k,c)]; }
+  double& at(const int* q, int c) { return v[idx(q[0],q[1],q[2],c)]; }
+  double at(const int* q, int c) const { return v[idx(q[0],q[1],q[2],c)]; }
+};
+
+template <class F> void forBox3(const Box3& b, F f) {
+  for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+    for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+      for (int i = b.lo[0]; i <= b.hi[0]; ++i) { int q[3] = {i, j, k}; f(q); }
+}
+// q shifted by s along d
+struct Sh { int q[3]; Sh(const int* p, int d, int s) { q[0] = p[0]; q[1] = p[1]; q[2] = p[2]; q[d] += s; } };
+
+// vanLeerSlopes in direction d (as the 2-D restatement)
+void vanLeerSlopes3(FAB3& dW, const FAB3& W, int nc, bool limit, int d, const Box3& box, const Box3& dom) {
+  forBox3(box, [&](const int* q) {
+    Sh m(q, d, -1), p(q, d, +1);
+    bool hasL = q[d]-1 >= dom.lo[d], hasR = q[d]+1 <= dom.hi[d];
+    for (int c = 0; c < nc; ++c) {
+      double dwc, dwl, dwr;
+      if (hasL && hasR) {
+        dwl = W.at(q,c) - W.at(m.q,c);
+        dwr = W.at(p.q,c) - W.at(q,c);
+        dwc = 0.5*(W.at(p.q,c) - W.at(m.q,c));
+      } else if (hasR) {
+        dwr = W.at(p.q,c) - W.at(q,c); dwl = dwr; dwc = dwr;
+      } else if (hasL) {
+        dwl = W.at(q,c) - W.at(m.q,c); dwr = dwl; dwc = dwl;
+      } else { dwl = dwr = dwc = 0.0; }
+      double s = dwc;
+      if (limit) {
+        if (dwl*dwr > 0.0) {
+          double mm = std::min(std::fabs(dwc), std::min(2.0*std::fabs(dwl), 2.0*std::fabs(dwr)));
+          s = (dwc >= 0.0) ? mm : -mm;
+        } else s = 0.0;
+      }
+      dW.at(q,c) = s;
+    }
+  });
+}
+
+struct Patch3 {
+  const Phys& P;
+  Box3 dom, cur;
+  double dx, time;
+  FAB3* B = nullptr;      // m_bdryData over (x, dom.lo[1], z)
+  FAB3 tmp;               // m_tmpBdryData
+  bool tmpSet = false;
+  Patch3(const Phys& p) : P(p) {}
+
+  // PPMNormalPred in direction d (the 2-D restatement's stages, cell by cell)
+  void PPMNormalPred(FAB3& WM, FAB3& WP, double dt, const FAB3& W, int d, const Box3& box) {
+    const int nc = 22;
+    const bool charL = P.sch.use_char_limiting, primL = P.sch.use_prim_limiting;
+    const bool limit = charL || primL;
+    Box3 faceBox = nodes3(box, d);
+    Box3 cells = faceBox; cells.hi[d] -= 1;
+    cells = isect3(growd3(cells, d, 1), dom);
+    FAB3 dW(cells, nc);
+    vanLeerSlopes3(dW, W, nc, limit, d, cells, dom);
+    FAB3 WFace(faceBox, nc);
+    forBox3(faceBox, [&](const int* q) {
+      Sh m(q, d, -1);
+      bool lowIn = q[d]-1 >= dom.lo[d], highIn = q[d] <= dom.hi[d];
+      for (int c = 0; c < nc; ++c) {
+        double v;
+        if (lowIn && highIn) v = 0.5*(W.at(m.q,c) + W.at(q,c)) - (dW.at(q,c) - dW.at(m.q,c))/6.0;
+        else if (highIn) v = W.at(q,c) - 0.5*dW.at(q,c);
+        else v = W.at(m.q,c) + 0.5*dW.at(m.q,c);
+        WFace.at(q,c) = v;
+      }
+    });
+    WM.define(box, nc); WP.define(box, nc);
+    double lambda[22]; charvalues(P, lambda);
+    const double dtbydx = dt / dx;
+    forBox3(box, [&](const int* q) {
+      Sh p(q, d, +1);
+      double m[22], pp[22];
+      for (int c = 0; c < nc; ++c) {
+        m[c] = (0.0 - W.at(q,c)) + WFace.at(q,c);
+        pp[c] = (0.0 - W.at(q,c)) + WFace.at(p.q,c);
+      }
+      if (charL) { charanalysis(P, m, d); charanalysis(P, pp, d); }
+      if (limit)
+        for (int c = 0; c < nc; ++c) {
+          double a = m[c], b = pp[c];
+          if (a*b < 0.0) {
+            double am = std::min(std::fabs(a), 2.0*std::fabs(b));
+            double ap = std::min(std::fabs(b), 2.0*std::fabs(a));
+            m[c] = (a >= 0.0) ? am : -am;
+            pp[c] = (b >= 0.0) ? ap : -ap;
+          } else { m[c] = 0.0; pp[c] = 0.0; }
+        }
+      if (!charL) { charanalysis(P, m, d); charanalysis(P, pp, d); }
+      for (int c = 0; c < nc; ++c) {
+        double sig = lambda[c] * dtbydx;
+        double a = m[c], b = pp[c];
+        if (sig > 0.0) {
+          double s = sig;
+          pp[c] = b - 0.5*s*((b - a) + 3.0*(1.0 - (2.0/3.0)*s)*(a + b));
+        } else if (sig < 0.0) {
+          double s = -sig;
+          m[c] = a + 0.5*s*(b - a) - 3.0*(a + b)*(0.5*s - s*s/3.0);
+        }
+      }
+      charsynthesis(P, m, d); charsynthesis(P, pp, d);
+      for (int c = 0; c < nc; ++c) { WM.at(q,c) = m[c] + W.at(q,c); WP.at(q,c) = pp[c] + W.at(q,c); }
+    });
+  }
+
+  // PLMNormalPred in direction d (the 2-D restatement's stages, cell by cell)
+  void PLMNormalPred(FAB3& WM, FAB3& WP, double dt, const FAB3& W, int d, const Box3& box) {
+    const int nc = 22;
+    const bool charL = P.sch.use_char_limiting, primL = P.sch.use_prim_limiting;
+    const bool fourth = P.sch.use_fourth_order_slopes != 0;
+    FAB3 dW(box, nc);
+    if (fourth) {
+      Box3 boxVL = isect3(growd3(box, d, 1), dom);
+      FAB3 dWvL(boxVL, nc);
+      vanLeerSlopes3(dWvL, W, nc, charL || primL, d, boxVL, dom);
+      forBox3(box, [&](const int* q) {
+        Sh m(q, d, -1), p(q, d, +1);
+        bool inner = q[d]-1 >= dom.lo[d] && q[d]+1 <= dom.hi[d];
+        for (int c = 0; c < nc; ++c) {
+          if (inner) {
+            double dwc = 0.5*(W.at(p.q,c) - W.at(m.q,c));
+            dW.at(q,c) = (4.0/3.0)*dwc - (1.0/6.0)*(dWvL.at(p.q,c) + dWvL.at(m.q,c));
+          } else {
+            dW.at(q,c) = dWvL.at(q,c);
+          }
+        }
+      });
+    } else {
+      vanLeerSlopes3(dW, W, nc, charL || primL, d, box, dom);
+    }
+    WM.define(box, nc); WP.define(box, nc);
+    double lambda[22]; charvalues(P, lambda);
+    const double dtbydx = dt / dx;
+    forBox3(box, [&](const int* q) {
+      Sh mq(q, d, -1), pq(q, d, +1);
+      double s[22], l[22], r[22];
+      for (int c = 0; c < nc; ++c) { s[c] = dW.at(q,c); l[c] = 0.0; r[c] = 0.0; }
+      if (charL || fourth) {
+        bool hasL = q[d]-1 >= dom.lo[d], hasR = q[d]+1 <= dom.hi[d];
+        for (int c = 0; c < nc; ++c) {
+          double m = hasL ? W.at(q,c) - W.at(mq.q,c) : 0.0;
+          double p = hasR ? W.at(pq.q,c) - W.at(q,c) : 0.0;
+          if (!hasL) m = p;
+          if (!hasR) p = m;
+          l[c] = m; r[c] = p;
+        }
+      }
+      if (charL) { charanalysis(P, l, d); charanalysis(P, r, d); charanalysis(P, s, d); }
+      if ((charL || primL) && (charL || fourth))
+        for (int c = 0; c < nc; ++c) {
+          if (l[c]*r[c] > 0.0) {
+            double m = std::min(std::fabs(s[c]), std::min(2.0*std::fabs(l[c]), 2.0*std::fabs(r[c])));
+            s[c] = (s[c] >= 0.0) ? m : -m;
+          } else s[c] = 0.0;
+        }
+      if (!charL) charanalysis(P, s, d);
+      double m[22], p[22];
+      for (int c = 0; c < nc; ++c) {
+        double sig = lambda[c] * dtbydx;
+        m[c] = -0.5 * (1.0 + std::min(sig, 0.0)) * s[c];
+        p[c] = 0.5 * (1.0 - std::max(sig, 0.0)) * s[c];
+      }
+      charsynthesis(P, m, d); charsynthesis(P, p, d);
+      for (int c = 0; c < nc; ++c) { WM.at(q,c) = m[c] + W.at(q,c); WP.at(q,c) = p[c] + W.at(q,c); }
+    });
+  }
+
+  // LEPhysIBC::primBC on the faces of WgBox on `side` that lie on the domain boundary
+  void primBC(FAB3& Wg, const FAB3& Wshift, const Box3& WgBox, int d, int side) {
+    int f = (side < 0) ? WgBox.lo[d] : WgBox.hi[d];
+    int domFace = (side < 0) ? dom.lo[d] : dom.hi[d] + 1;
+    if (f != domFace) return;
+    Box3 fb = isect3(WgBox, dom);
+    fb.lo[d] = fb.hi[d] = f;
+    double wg[22], wi[22];
+    forBox3(fb, [&](const int* q) {
+      for (int c = 0; c < 22; ++c) { wi[c] = Wshift.at(q,c); wg[c] = Wg.at(q,c); }
+      if (side == -1 && d == 1 && P.sch.fault_law != TMK_FAULT_NONE) {
+        const FAB3& src = tmpSet ? tmp : *B;
+        const int bq[3] = {q[0], dom.lo[1], q[2]};
+        double xc = (q[0] + 0.5) * dx;
+        if (P.sch.fault_law == TMK_FAULT_RS) {
+          rsfaultpt(P, wg, wi, src.at(bq, 10), xc - P.rs.x0);
+        } else {
+          double b[TMK_SW_NBDRY];
+          for (int c = 0; c < TMK_SW_NBDRY; ++c) b[c] = src.at(bq, c);
+          double zc = (q[2] + 0.5) * dx;
+          swfaultpt(P, wg, wi, b, xc, &zc);
+        }
+      } else {
+        int bt = P.sch.boundary_type[d*2 + (side+1)/2];
+        edgebcpt(P, wg, wi, side, d, bt == TMK_BC_OUTFLOW);
+      }
+      for (int c = 0; c < 22; ++c) Wg.at(q,c) = wg[c];
+    });
+  }
+
+  // LinElastPhysics::riemann: interior faces of faceBox, then primBC at the domain faces
+  void riemann(FAB3& Wg, const FAB3& WLeftCells, const FAB3& WRightCells, int d, const Box3& faceBox) {
+    double wl[22], wr[22], wg[22];
+    forBox3(faceBox, [&](const int* q) {
+      Sh m(q, d, -1);
+      for (int c = 0; c < 22; ++c) { wl[c] = WLeftCells.at(m.q,c); wr[c] = WRightCells.at(q,c); }
+      riemannpt(P, wg, wl, wr, d);
+      for (int c = 0; c < 22; ++c) Wg.at(q,c) = wg[c];
+    });
+    const Box3& gb = Wg.b;
+    FAB3 shiftL(gb, 22), shiftR(gb, 22);
+    if (gb.hi[d] == dom.hi[d]+1) {
+      Box3 fb = gb; fb.lo[d] = gb.hi[d];
+      forBox3(fb, [&](const int* q) {
+        Sh m(q, d, -1);
+        if (WLeftCells.b.contains(m.q[0], m.q[1], m.q[2]))
+          for (int c = 0; c < 22; ++c) shiftL.at(q,c) = WLeftCells.at(m.q,c);
+      });
+    }
+    if (gb.lo[d] == dom.lo[d]) {
+      Box3 fb = gb; fb.hi[d] = gb.lo[d];
+      forBox3(fb, [&](const int* q) {
+        if (WRightCells.b.contains(q[0], q[1], q[2]))
+          for (int c = 0; c < 22; ++c) shiftR.at(q,c) = WRightCells.at(q,c);
+      });
+    }
+    primBC(Wg, shiftL, gb, d, +1);
+    primBC(Wg, shiftR, gb, d, -1);
+  }
+
+  // LEPhysIBC::updateBoundary: the y faces of WH on the domain's y-lo plane
+  bool updateBoundary(const FAB3& WH, int d, double dt, double t, bool final_) {
+    if (d != 1 || P.sch.fault_law == TMK_FAULT_NONE) return true;
+    if (WH.b.lo[1] != dom.lo[1]) return true;
+    for (int e = 0; e < 3; e += 2)
+      if (WH.b.lo[e] < dom.lo[e] || WH.b.hi[e] > dom.hi[e]) return true;
+    FAB3& Bin = *B;
+    FAB3& Bout = final_ ? *B : tmp;
+    const int nb = Bin.nc;
+    bool ok = true;
+    double bin[TMK_RS_NBDRY], bout[TMK_RS_NBDRY], u[22];
+    Box3 fb = WH.b; fb.hi[1] = fb.lo[1];
+    forBox3(fb, [&](const int* q) {
+      for (int c = 0; c < nb; ++c) { bin[c] = Bin.at(q,c); bout[c] = Bout.at(q,c); }
+      for (int c = 0; c < 22; ++c) u[c] = WH.at(q,c);
+      if (P.sch.fault_law == TMK_FAULT_RS)
+        ok = rssetbndpt(P, bout, bin, u, dt, (q[0] + 0.5)*dx - P.rs.x0, t) && ok;
+      else
+        swsetbndpt(P, bout, bin, u, dt, t, final_);
+      for (int c = 0; c < nb; ++c) Bout.at(q,c) = bout[c];
+    });
+    if (!final_) tmpSet = true;
+    return ok;
+  }
+
+  // T += quasilinearUpdate(WH, scale, d) on the cells of cc
+  void qlupdate(FAB3& T, const FAB3& WH, double scale, int d, const Box3& cc) {
+    double a[22], hi[22], lo[22];
+    forBox3(cc, [&](const int* q) {
+      Sh p(q, d, +1);
+      for (int c = 0; c < 22; ++c) { hi[c] = WH.at(p.q,c); lo[c] = WH.at(q,c); }
+      getadwdxpt(P, a, hi, lo, scale, d);
+      for (int c = 0; c < 22; ++c) T.at(q,c) += a[c];
+    });
+  }
+
+  bool updateState(FAB3& U, FAB3* Fout, double dt) {
+    bool ok = true;
+    if (B) { tmp.define(B->b, B->nc); tmpSet = false; }
+    Box3 faceBox[3], ccBox[3], fluxBox[3];
+    for (int d = 0; d < 3; ++d) {
+      Box3 fb = isect3(grow3(cur, 1), dom);
+      fb = growd3(fb, d, -1);
+      faceBox[d] = nodes3(fb, d);
+      ccBox[d] = isect3(growd3(grow3(cur, 1), d, -1), dom);
+      fluxBox[d] = nodes3(ccBox[d], d);
+    }
+    Box3 WBox = isect3(U.b, dom);
+    FAB3 W(WBox, 22);
+    forBox3(WBox, [&](const int* q) { for (int c = 0; c < 22; ++c) W.at(q,c) = U.at(q,c); });
+    Box3 slopeBox = isect3(grow3(cur, 1), dom);
+    FAB3 WM[3], WP[3], WH1[3];
+    for (int d = 0; d < 3; ++d) {
+      if (P.sch.normal_pred_order == 2) {
+        PPMNormalPred(WM[d], WP[d], dt, W, d, slopeBox);
+      } else if (P.sch.normal_pred_order == 1) {
+        PLMNormalPred(WM[d], WP[d], dt, W, d, slopeBox);
+      } else {
+        WM[d].define(slopeBox, 22); WP[d].define(slopeBox, 22);
+        forBox3(slopeBox, [&](const int* q) {
+          for (int c = 0; c < 22; ++c) WM[d].at(q,c) = WP[d].at(q,c) = W.at(q,c);
+        });
+      }
+      WH1[d].define(fluxBox[d], 22);
+      riemann(WH1[d], WP[d], WM[d], d, faceBox[d]);
+    }
+    // WHalf2[d1][d2] (the diagonal is unused)
+    FAB3 WH2[3][3];
+    for (int d1 = 0; d1 < 3; ++d1)
+      for (int d2 = 0; d2 < 3; ++d2) {
+        if (d2 == d1) continue;
+        FAB3 TM = WM[d1], TP = WP[d1];
+        qlupdate(TM, WH1[d2], -(1.0/3.0) * dt / dx, d2, ccBox[d2]);
+        qlupdate(TP, WH1[d2], -(1.0/3.0) * dt / dx, d2, ccBox[d2]);
+        ok = updateBoundary(WH1[d2], d2, (1.0/3.0)*dt, 0.0, false) && ok;
+        WH2[d1][d2].define(fluxBox[d1], 22);
+        riemann(WH2[d1][d2], TP, TM, d1, faceBox[d1]);
+      }
+    for (int d = 0; d < 3; ++d) {
+      Box3 fb = isect3(growd3(cur, d, 1), dom);
+      fb = growd3(fb, d, -1);
+      faceBox[d] = nodes3(fb, d);
+      fluxBox[d] = nodes3(cur, d);
+    }
+    FAB3 WHalf[3];
+    for (int d1 = 0; d1 < 3; ++d1) {
+      for (int d2 = 0; d2 < 3; ++d2) {
+        if (d2 == d1) continue;
+        int d3 = 3 - d1 - d2;
+        qlupdate(WM[d1], WH2[d2][d3], -(1.0/2.0) * dt / dx, d2, ccBox[d2]);
+        qlupdate(WP[d1], WH2[d2][d3], -(1.0/2.0) * dt / dx, d2, ccBox[d2]);
+        ok = updateBoundary(WH2[d2][d3], d2, (1.0/2.0)*dt, 0.0, false) && ok;
+      }
+      WHalf[d1].define(fluxBox[d1], 22);
+      riemann(WHalf[d1], WP[d1], WM[d1], d1, faceBox[d1]);
+    }
+    // computeUpdate
+    FAB3 dU(U.b, 22);
+    double f[22], a[22];
+    for (int d = 0; d < 3; ++d) {
+      FAB3 F(fluxBox[d], 22);
+      forBox3(fluxBox[d], [&](const int* q) {
+        for (int c = 0; c < 22; ++c) a[c] = WHalf[d].at(q,c);
+        getfluxpt(P, f, a, d);
+        for (int c = 0; c < 22; ++c) F.at(q,c) = f[c];
+      });
+      forBox3(cur, [&](const int* q) {
+        Sh p(q, d, +1);
+        for (int c = 0; c < 22; ++c) dU.at(q,c) += F.at(p.q,c) - F.at(q,c);
+      });
+      if (Fout) Fout[d] = F;
+      ok = updateBoundary(WHalf[d], d, dt, time + dt, true) && ok;
+    }
+    double sc = -dt / dx;
+    forBox3(cur, [&](const int* q) { for (int c = 0; c < 22; ++c) U.at(q,c) += dU.at(q,c) * sc; });
+    return ok;
+  }
+};
+
+FAB3 wrap3(const double* p, const int lo[3], const int hi[3], int nc) {
+  FAB3 f(mk3(lo, hi), nc);
+  std::memcpy(f.v.data(), p, f.v.size()*sizeof(double));
+  return f;
+}
+void unwrap3(const FAB3& f, double* p) { std::memcpy(p, f.v.data(), f.v.size()*sizeof(double)); }
 
 // ============================================================ AMR coupling ==
 // The coarse-fine operators of the reference's AMR path, on levels stored as
@@ -1723,6 +2143,62 @@ int tmko_patch_update_state(const tmk_elastic_params* e, const tmk_scheme* s, co
   if (Fx) unwrap(F[0], Fx);
   if (Fy) unwrap(F[1], Fy);
   return ok ? 0 : 2;
+}
+
+// LinElastPatchGodunov::updateState in 3-D on host FABs: U over ulo..uhi (22
+// comps), B the fault data over (x, z) in blo..bhi (nb comps, x fastest) when
+// the valid box starts on the domain's y-lo plane, F0/F1/F2 the face fluxes
+// over the faces of the valid box (or NULL).
+int tmko_patch_update_state_3d(const tmk_elastic_params* e, const tmk_scheme* s, const tmk_rs_params* rs,
+                               const tmk_sw_params* sw, double* U, const int ulo[3], const int uhi[3],
+                               double* B, const int blo[2], const int bhi[2],
+                               double* F0, double* F1, double* F2,
+                               const int vlo[3], const int vhi[3], const int dlo[3], const int dhi[3],
+                               double dx, double time, double dt) {
+  Phys P;
+  if (!setup(P, e, s, rs, sw, nullptr)) return 1;
+  FAB3 Uf = wrap3(U, ulo, uhi, 22);
+  const int nb = s->fault_law == TMK_FAULT_RS ? TMK_RS_NBDRY : TMK_SW_NBDRY;
+  const bool fault = s->fault_law != TMK_FAULT_NONE && vlo[1] == dlo[1];
+  if (fault && !B) return 1;
+  Patch3 pt(P);
+  pt.dom = mk3(dlo, dhi);
+  pt.cur = mk3(vlo, vhi);
+  pt.dx = dx; pt.time = time;
+  FAB3 Bf;
+  if (fault) {
+    int bl[3] = {blo[0], dlo[1], blo[1]}, bh[3] = {bhi[0], dlo[1], bhi[1]};
+    Bf = wrap3(B, bl, bh, nb);
+    Box3 need = isect3(grow3(pt.cur, 1), pt.dom);
+    if (Bf.b.lo[0] > need.lo[0] || Bf.b.hi[0] < need.hi[0] || Bf.b.lo[2] > need.lo[2] || Bf.b.hi[2] < need.hi[2])
+      return 1;
+    pt.B = &Bf;
+  }
+  FAB3 F[3];
+  bool ok = pt.updateState(Uf, (F0 || F1 || F2) ? F : nullptr, dt);
+  unwrap3(Uf, U);
+  if (fault) unwrap3(Bf, B);
+  double* Fo[3] = {F0, F1, F2};
+  for (int d = 0; d < 3; ++d) if (Fo[d]) unwrap3(F[d], Fo[d]);
+  return ok ? 0 : 2;
+}
+
+// PLASTICCORRECTION over the 3-D box blo..bhi of host FAB U
+int tmko_plastic_correction_3d(const tmk_elastic_params* e, const tmk_plastic_params* pl, double* U,
+                               const int ulo[3], const int uhi[3], const int blo[3], const int bhi[3],
+                               double dt) {
+  Phys P; tmk_scheme s; std::memset(&s, 0, sizeof(s)); s.normal_pred_order = 2;
+  setup(P, e, &s, nullptr, nullptr, pl);
+  FAB3 Uf = wrap3(U, ulo, uhi, 22);
+  forBox3(mk3(blo, bhi), [&](const int* q) {
+    for (int sd = 0; sd < 2; ++sd) {
+      const int O = 11*sd;
+      plasticflow(P, Uf.at(q,O+3), Uf.at(q,O+4), Uf.at(q,O+5), Uf.at(q,O+6), Uf.at(q,O+7),
+                  Uf.at(q,O+8), Uf.at(q,O+9), Uf.at(q,O+10), dt);
+    }
+  });
+  unwrap3(Uf, U);
+  return 0;
 }
 
 // PLASTICCORRECTION over box on host FAB U

@@ -1,0 +1,180 @@
+"""3-D patch step (CH_SPACEDIM == 3) on the GPU == the oracle's 3-D
+restatement, through the C ABI (tmk_patch_update_state_3d,
+tmk_plastic_update_3d).  FP64 on both sides: 1e-12 relative per component
+(RTOL_FP64), for the state over the valid box, the face fluxes and the fault's
+boundary data, on patches that touch the fault plane and the domain's edges in
+every direction and on interior patches."""
+import numpy as np
+import pytest
+
+import oracle as O
+from tetemoko_gb300 import _capi as A, scenarios as S
+from tests.helpers import RTOL_FP64, perturbed_state_3d, random_B_3d, rel_err
+
+pytestmark = pytest.mark.gpu
+
+G = A.TMK_NGHOST
+NX, NY, NZ, DX = 12, 10, 8, 0.1
+DOM = ((0, 0, 0), (NX - 1, NY - 1, NZ - 1))
+
+
+def _sw(layout=A.TMK_SW_LAYOUT_OFFSET11):
+    """Slip weakening with z profiles that vary over the test domain: a smooth
+    nucleation patch centred at z = 0.4 and a friction box |z| < 0.5."""
+    sc = S.slip_weakening(nx=NX, ny=NY, dx=DX, layout=layout)
+    w = sc.sw
+    w.smooth = 0.3
+    w.xc[0], w.xw[0], w.zc[0], w.zw[0] = 0.1, 0.2, 0.4, 0.15
+    w.num_patches = 2
+    w.xc[1], w.xw[1], w.zc[1], w.zw[1], w.tau[1] = -0.3, 0.1, 0.1, 0.05, 4.0
+    w.fric_box_width[0], w.fric_box_width[1] = 0.45, 0.5
+    w.outside_friction = 2.0
+    return sc
+
+
+def _scenarios():
+    out = []
+    sc = S.rate_state(nx=NX, ny=NY, dx=DX, state_law=A.TMK_RS_SLIP_LAW)
+    sc.rs.L = 0.5
+    out.append(("rs_slip", sc))
+    out.append(("rs_aging", S.rate_state(nx=NX, ny=NY, dx=DX)))
+    out.append(("sw_ref9", _sw(A.TMK_SW_LAYOUT_REFERENCE9)))
+    out.append(("sw_off11", _sw()))
+    sc = _sw()
+    sc.scheme.use_prim_limiting, sc.scheme.use_char_limiting = 0, 1
+    out.append(("sw_charlim", sc))
+    sc = S.rate_state(nx=NX, ny=NY, dx=DX)
+    for k, v in enumerate((1, 0, 2, 1, 1, 0)):
+        sc.scheme.boundary_type[k] = v
+    out.append(("rs_free_edges", sc))
+    sc = S.rate_state(nx=NX, ny=NY, dx=DX)
+    sc.scheme.normal_pred_order = 0
+    out.append(("rs_ctu", sc))
+    sc = _sw()
+    sc.scheme.normal_pred_order = 1
+    out.append(("sw_plm4", sc))
+    sc = S.rate_state(nx=NX, ny=NY, dx=DX)
+    sc.scheme.normal_pred_order = 1
+    sc.scheme.use_fourth_order_slopes = 0
+    out.append(("rs_plm2", sc))
+    sc = S.rate_state(nx=NX, ny=NY, dx=DX)
+    sc.scheme.fault_law = A.TMK_FAULT_NONE
+    for k, v in enumerate((0, 1, 0, 1, 1, 0)):
+        sc.scheme.boundary_type[k] = v
+    out.append(("no_fault", sc))
+    return out
+
+
+SCEN = _scenarios()
+VALID = [((0, 0, 0), (11, 9, 7)), ((2, 0, 1), (9, 5, 6)), ((5, 4, 3), (11, 9, 7)), ((0, 3, 0), (7, 9, 4)),
+         ((3, 2, 2), (8, 7, 5))]
+VALID_IDS = ["whole", "fault_inner", "corner_hi", "edge_lo", "interior"]
+
+
+@pytest.mark.parametrize("name,sc", SCEN, ids=[n for n, _ in SCEN])
+@pytest.mark.parametrize("valid", VALID, ids=VALID_IDS)
+def test_patch_update_state_3d_matches_oracle(cuda_lib, name, sc, valid):
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    lo, hi = valid
+    rng = np.random.default_rng(4321)
+    U0 = perturbed_state_3d(sc, rng, lo, hi)
+    ulo = tuple(l - G for l in lo)
+    fault = sc.scheme.fault_law != A.TMK_FAULT_NONE and lo[1] == 0
+    # fault data over the valid x, z grown by the ghost width
+    blo = (lo[0] - G, lo[2] - G)
+    B0 = random_B_3d(sc, rng, hi[0] - lo[0] + 1 + 2 * G, hi[2] - lo[2] + 1 + 2 * G) if fault else None
+    dt, time = sc.dt(), 0.75
+    Ur, Br = U0.copy(), (B0.copy() if fault else None)
+    rc, Fr = O.patch_update_state_3d(sc, Ur, ulo, lo, hi, DOM[0], DOM[1], Br, blo, DX, time, dt, with_flux=True)
+    assert rc == 0
+    ctx = Context(sc)
+    pg = LinElastPatchGodunov3D(ctx, DOM)
+    pg.set_current_box(valid)
+    pg.set_current_time(time)
+    Ud = torch.from_numpy(U0.copy()).cuda()
+    Bd = torch.from_numpy(B0.copy()).cuda() if fault else None
+    mws, F = pg.update_state(Ud, ulo, dt, B=Bd, blo=blo, with_flux=True)
+    torch.cuda.synchronize()
+    assert mws == max(sc.elastic.cs, sc.elastic.cp)
+    Ug = Ud.cpu().numpy()
+    v = (slice(None), slice(G, -G), slice(G, -G), slice(G, -G))
+    assert rel_err(Ug[v], Ur[v]) <= RTOL_FP64
+    assert np.array_equal(Ug[[9, 10, 20, 21]], U0[[9, 10, 20, 21]])
+    assert np.array_equal(Ug[:, :G], U0[:, :G])
+    assert np.array_equal(Ug[:, :, :G], U0[:, :, :G])
+    ev = [c for c in range(22) if c % 11 < 9]
+    for d in range(3):
+        assert rel_err(F[d].cpu().numpy()[ev], Fr[d][ev]) <= RTOL_FP64, d
+    if fault:
+        Bg = Bd.cpu().numpy()
+        bv = (slice(None), slice(G, -G), slice(G, -G))
+        assert rel_err(Bg[bv], Br[bv]) <= RTOL_FP64
+        assert not np.array_equal(Br[bv], B0[bv])
+    ctx.close()
+
+
+def test_z_uniform_gpu_step_reduces_to_2d_gpu_step(cuda_lib):
+    """A state without z variation on a patch away from the z edges: the 3-D
+    kernels reproduce the 2-D patch kernels exactly off the fault row."""
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov, LinElastPatchGodunov3D
+    from tests.helpers import perturbed_state
+    sc = S.rate_state(nx=NX, ny=NY, dx=DX)
+    rng = np.random.default_rng(5)
+    U2 = perturbed_state(sc, rng)
+    B2 = sc.initial_B()
+    ctx = Context(sc)
+    p2 = LinElastPatchGodunov(ctx)
+    p2.set_current_box((0, 0, NX - 1, NY - 1))
+    U2d = torch.from_numpy(U2.copy()).cuda()
+    p2.update_state(U2d, (-G, -G), sc.dt(), B=torch.from_numpy(B2.copy()).cuda(), bxlo=-G)
+    p3 = LinElastPatchGodunov3D(ctx, ((0, 0, 0), (NX - 1, NY - 1, 9)))
+    p3.set_current_box(((0, 0, 3), (NX - 1, NY - 1, 5)))
+    U3 = torch.from_numpy(np.repeat(U2[:, None], 3 + 2 * G, axis=1).copy()).cuda()
+    B3 = torch.from_numpy(np.repeat(B2[:, None], 3 + 2 * G, axis=1).copy()).cuda()
+    p3.update_state(U3, (-G, -G, 3 - G), sc.dt(), B=B3, blo=(-G, 3 - G))
+    torch.cuda.synchronize()
+    a = U3.cpu().numpy()
+    b = U2d.cpu().numpy()
+    for k in range(G, G + 3):
+        assert np.array_equal(a[:, k, G + 1:], b[:, G + 1:])
+    ctx.close()
+
+
+def test_plastic_update_3d_matches_oracle(cuda_lib):
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    sc = S.slip_weakening(nx=NX, ny=NY, dx=DX, plasticity=True)
+    rng = np.random.default_rng(8)
+    lo, hi = (0, 0, 0), (NX - 1, NY - 1, NZ - 1)
+    U0 = perturbed_state_3d(sc, rng, lo, hi, amp_s=60.0)
+    U0[[10, 21]] = np.abs(rng.standard_normal((2,) + U0.shape[1:]))
+    Ur = U0.copy()
+    box = ((1, 0, 2), (10, 8, 7))
+    O.plastic_correction_3d(sc, Ur, (-G, -G, -G), box[0], box[1], sc.dt())
+    ctx = Context(sc)
+    pg = LinElastPatchGodunov3D(ctx, DOM)
+    Ud = torch.from_numpy(U0.copy()).cuda()
+    pg.plastic_update(Ud, (-G, -G, -G), sc.dt(), box=box)
+    Ug = Ud.cpu().numpy()
+    assert (Ur[9] > 0).any(), "the test state must yield somewhere"
+    assert rel_err(Ug, Ur) <= RTOL_FP64
+    ctx.close()
+
+
+def test_bad_descriptors_are_refused(cuda_lib):
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    sc = S.rate_state(nx=NX, ny=NY, dx=DX)
+    ctx = Context(sc)
+    pg = LinElastPatchGodunov3D(ctx, DOM)
+    pg.set_current_box(((0, 1, 0), (5, 5, 5)))
+    U = torch.zeros((22, 6 + 2, 5 + 2, 6 + 2), dtype=torch.float64, device="cuda")   # too few ghosts
+    with pytest.raises(A.TmkError):
+        pg.update_state(U, (-1, 0, -1), sc.dt())
+    pg.set_current_box(((0, 0, 0), (5, 5, 5)))
+    U = torch.zeros((22, 6 + 2 * G, 6 + 2 * G, 6 + 2 * G), dtype=torch.float64, device="cuda")
+    with pytest.raises(A.TmkError):      # a fault patch without fault data
+        pg.update_state(U, (-G, -G, -G), sc.dt())
+    ctx.close()

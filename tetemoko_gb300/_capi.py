@@ -117,6 +117,21 @@ def box(lo0, lo1, hi0, hi1) -> Box:
     return b
 
 
+class Fab3(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("lo", C.c_int * 3), ("hi", C.c_int * 3), ("ncomp", C.c_int)]
+
+
+class Box3(C.Structure):
+    _fields_ = [("lo", C.c_int * 3), ("hi", C.c_int * 3)]
+
+
+def box3(lo, hi) -> Box3:
+    b = Box3()
+    for d in range(3):
+        b.lo[d], b.hi[d] = lo[d], hi[d]
+    return b
+
+
 LIBNAME = "libtetemoko_gb300.so"
 _lib = None
 
@@ -150,6 +165,10 @@ def lib() -> C.CDLL:
     L.tmk_patch_update_state_noalloc.restype = C.c_int
     L.tmk_plastic_update.argtypes = [vp, C.POINTER(Fab), C.POINTER(Box), C.c_double, vp]
     L.tmk_max_wave_speed.argtypes = [vp, dp]
+    F3 = C.POINTER(Fab3)
+    L.tmk_patch_update_state_3d.argtypes = [vp, F3, F3, F3, F3, F3, C.POINTER(Box3), C.POINTER(Box3), C.c_double,
+                                            C.c_double, C.c_double, dp, vp]
+    L.tmk_plastic_update_3d.argtypes = [vp, F3, C.POINTER(Box3), C.c_double, vp]
     L.tmk_level_create.argtypes = [vp, C.POINTER(Box), C.c_double, C.c_int, C.POINTER(Box), C.POINTER(vp)]
     L.tmk_level_destroy.argtypes = [vp]
     L.tmk_level_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
@@ -207,7 +226,8 @@ def lib() -> C.CDLL:
                  "tmk_level_detach_coarser", "tmk_level_fill_coarse_fine", "tmk_level_reflux",
                  "tmk_level_average_down", "tmk_level_interp_from_coarser", "tmk_level_copy_overlap",
                  "tmk_level_register_size", "tmk_amr_create", "tmk_amr_step", "tmk_amr_time",
-                 "tmk_level_graph_create", "tmk_amr_graph_create", "tmk_graph_launch"):
+                 "tmk_level_graph_create", "tmk_amr_graph_create", "tmk_graph_launch",
+                 "tmk_patch_update_state_3d", "tmk_plastic_update_3d"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

@@ -1,12 +1,13 @@
 """In-tree build of libtetemoko_gb300.so for sm_103a with nvcc.
 
-Six translation units, compiled in parallel:
+Seven translation units, compiled in parallel:
   tmk_fp64.cu  plain FP64 kernels, --fmad=false (parity with the CPU oracle)
   tmk_fp32.cu  mixed-form kernels (FP32 volume, FP64 friction)
   tmk_capi.cu  the C ABI (host code)
   tmk_noalloc.cu  the allocation-free patch step (fixed device scratch array)
   tmk_amr.cu   coarse-fine coupling and the AMR hierarchy, --fmad=false
   tmk_regrid.cu  refinement tagging, --fmad=false
+  tmk_3d.cu    the 3-D patch step (CH_SPACEDIM == 3), --fmad=false
 """
 from __future__ import annotations
 
@@ -30,6 +31,7 @@ UNITS = {
     "tmk_noalloc.cu": [],
     "tmk_amr.cu": ["--fmad=false"],
     "tmk_regrid.cu": ["--fmad=false"],
+    "tmk_3d.cu": ["--fmad=false"],
 }
 
 

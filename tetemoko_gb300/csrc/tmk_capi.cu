@@ -84,6 +84,8 @@ extern "C" tmk_status tmk_context_create(const tmk_elastic_params* e, const tmk_
     P.sw_fs = sw->fs; P.sw_fd = sw->fd; P.sw_dw = sw->dw; P.sw_smooth = sw->smooth; P.sw_np = sw->num_patches;
     for (int k = 0; k < TMK_SW_MAX_PATCHES; ++k) { P.sw_xc[k] = sw->xc[k]; P.sw_xw[k] = sw->xw[k]; P.sw_tau[k] = sw->tau[k]; }
     P.sw_fbc0 = sw->fric_box_center[0]; P.sw_fbw0 = sw->fric_box_width[0];
+    for (int k = 0; k < TMK_SW_MAX_PATCHES; ++k) { P.sw_zc[k] = sw->zc[k]; P.sw_zw[k] = sw->zw[k]; }
+    P.sw_fbc1 = sw->fric_box_center[1]; P.sw_fbw1 = sw->fric_box_width[1];
     P.sw_outside = sw->outside_friction; P.sw_thr = sw->rupture_threshold;
     P.sw_off = sw->layout == TMK_SW_LAYOUT_OFFSET11 ? 11 : 9;
   }

@@ -48,6 +48,7 @@ struct DevParams {
   double sw_xc[SW_MAXP], sw_xw[SW_MAXP], sw_tau[SW_MAXP];
   double sw_fbc0, sw_fbw0, sw_outside, sw_thr;
   int sw_off;               // side-2 component offset, 9 (reference) or 11
+  double sw_zc[SW_MAXP], sw_zw[SW_MAXP], sw_fbc1, sw_fbw1;   // z profiles (3-D)
   // plasticity (PLASTICSETF)
   double p_mu, p_beta, p_eta, p_b, p_h;
   // reciprocals the mixed form's friction solve multiplies by (its chain of
@@ -79,6 +80,7 @@ template <typename T> constexpr bool kExact = std::is_same<T, double>::value;
 template <int D> struct Rot;
 template <> struct Rot<0> { static constexpr int cx = 0, cy = 1, cz = 2, cxy = 6, cxz = 7, cyz = 8; };
 template <> struct Rot<1> { static constexpr int cx = 1, cy = 2, cz = 0, cxy = 8, cxz = 6, cyz = 7; };
+template <> struct Rot<2> { static constexpr int cx = 2, cy = 0, cz = 1, cxy = 7, cxz = 8, cyz = 6; };
 
 // lambda-ratio product  s*lam/(2G+lam)
 template <typename T> TMK_D T lratio(const Consts<T>& k, T s) {

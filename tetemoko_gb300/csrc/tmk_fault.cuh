@@ -327,11 +327,17 @@ TMK_D double rs_setbnd_k(const DevParams& P, const RSFaceK& fk, const double* U,
 
 // SWFAULTBCF (ibcLinElast/SWIBCF.ChF:79-267) at one fault face.  Side 2 is read
 // and written at component offset P.sw_off (9 as in the reference source).
-// Components the law does not write keep the values already in Wg.
-TMK_D void sw_fault(const DevParams& P, const double* Wi, double slip_total, double xcell, double* Wg) {
+// Components the law does not write keep the values already in Wg.  Z3 (the
+// 3-D fault plane): the nucleation patches and the friction box are products
+// of x and z profiles, tau_0 += (tau valx) valz and box value valx valz
+// (:118-126,175-180).
+template <bool Z3 = false>
+TMK_D void sw_fault(const DevParams& P, const double* Wi, double slip_total, double xcell, double* Wg,
+                    double zcell = 0.0) {
   const int off = P.sw_off;
   const double Zs = P.Zs, Zp = P.Zp, lam = P.lam, G = P.G;
   double x = xcell - P.sw_fbc0;
+  const double z = zcell - P.sw_fbc1;
   double vx1 = Wi[0], vy1 = Wi[1], vz1 = Wi[2], sxx1 = Wi[3], syy1 = Wi[4], szz1 = Wi[5];
   double sxy1 = Wi[6], sxz1 = Wi[7], syz1 = Wi[8];
   double vx2 = Wi[off + 0], vy2 = Wi[off + 1], vz2 = Wi[off + 2], sxx2 = Wi[off + 3], syy2 = Wi[off + 4];
@@ -345,7 +351,12 @@ TMK_D void sw_fault(const DevParams& P, const double* Wi, double slip_total, dou
   double tau_0 = 0;
   for (int ip = 0; ip < P.sw_np; ++ip) {
     double valx = smoothfn(P.sw_smooth, fabs(x - P.sw_xc[ip]) - P.sw_xw[ip]);
-    tau_0 = tau_0 + P.sw_tau[ip] * valx;
+    if constexpr (Z3) {
+      double valz = smoothfn(P.sw_smooth, fabs(z - P.sw_zc[ip]) - P.sw_zw[ip]);
+      tau_0 = tau_0 + P.sw_tau[ip] * valx * valz;
+    } else {
+      tau_0 = tau_0 + P.sw_tau[ip] * valx;
+    }
   }
   double a1 = 0.5 * (wpxy2 - wpxy1) + tau_0, a2 = 0.5 * (wpyz2 - wpyz1);
   double tau_lock = sqrt(a1 * a1 + a2 * a2);
@@ -354,7 +365,13 @@ TMK_D void sw_fault(const DevParams& P, const double* Wi, double slip_total, dou
   vy1 = -(wpyy1 + wpyy2) / 2.0 / Zp;
   vy2 = -(wpyy1 + wpyy2) / 2.0 / Zp;
   double valx = boxcar(P.sw_fbw0, fabs(x));
-  double fric = P.sw_fs * valx + (1 - valx) * P.sw_outside;
+  double fric;
+  if constexpr (Z3) {
+    double valz = boxcar(P.sw_fbw1, fabs(z));
+    fric = P.sw_fs * valx * valz + (1 - valx * valz) * P.sw_outside;
+  } else {
+    fric = P.sw_fs * valx + (1 - valx) * P.sw_outside;
+  }
   fric = fric - (fric - P.sw_fd) * fmin(1.0, slip_total / P.sw_dw);
   double tau = fmin(tau_lock, -syy1 * fric) - tau_0;
   double phi_xy = 0.5 * (wpxy2 - wpxy1);

@@ -128,6 +128,75 @@ class LinElastPatchGodunov:
                                                 _stream_ptr(stream)), "tmk_plastic_update")
 
 
+def _fab3(t, lo) -> A.Fab3:
+    """tmk_fab3 over a (ncomp, nz, ny, nx) float64 CUDA tensor whose first cell is lo = (i, j, k)."""
+    assert t.dtype == _torch().float64 and t.is_cuda and t.is_contiguous() and t.dim() == 4
+    f = A.Fab3()
+    f.data = t.data_ptr()
+    for d in range(3):
+        f.lo[d] = lo[d]
+        f.hi[d] = lo[d] + t.shape[3 - d] - 1
+    f.ncomp = t.shape[0]
+    return f
+
+
+class LinElastPatchGodunov3D:
+    """Patch integrator of a CH_SPACEDIM == 3 build (LinElastPatchGodunov with
+    the 3-D corner transport upwind corrections) on caller-owned device FABs
+    (FP64).  Boxes are ((lo0, lo1, lo2), (hi0, hi1, hi2)); the fault is the
+    domain's y-lo plane."""
+
+    def __init__(self, ctx: Context, domain, dx: float | None = None):
+        self.ctx = ctx
+        self.domain = (tuple(domain[0]), tuple(domain[1]))
+        self.dx = ctx.sc.dx if dx is None else dx
+        self.time = 0.0
+        self.box = None
+
+    def set_current_time(self, t: float):
+        self.time = t
+
+    def set_current_box(self, box):
+        self.box = (tuple(box[0]), tuple(box[1]))
+
+    def update_state(self, U, ulo, dt: float, B=None, blo=(0, 0), with_flux: bool = False, stream=None):
+        """Advance the valid box of U ((22, nz, ny, nx) FP64 CUDA tensor whose
+        first cell is ulo = (i, j, k)) by dt; B ((nb, nz_b, nx_b), first face
+        blo = (i, k) on the fault plane) updated in place.  Returns
+        (max_wave_speed, [F0, F1, F2])."""
+        torch = _torch()
+        v = A.box3(*self.box)
+        d = A.box3(*self.domain)
+        Uf = _fab3(U, ulo)
+        Bf = None
+        if B is not None:
+            Bf = A.Fab3()
+            Bf.data = B.data_ptr()
+            Bf.lo[0], Bf.lo[1], Bf.lo[2] = blo[0], self.domain[0][1], blo[1]
+            Bf.hi[0], Bf.hi[1], Bf.hi[2] = blo[0] + B.shape[2] - 1, self.domain[0][1], blo[1] + B.shape[1] - 1
+            Bf.ncomp = B.shape[0]
+        F = [None, None, None]
+        Ff = [None, None, None]
+        if with_flux:
+            n = [self.box[1][e] - self.box[0][e] + 1 for e in range(3)]
+            for e in range(3):
+                m = list(n)
+                m[e] += 1
+                F[e] = torch.empty((22, m[2], m[1], m[0]), dtype=torch.float64, device=U.device)
+                Ff[e] = _fab3(F[e], self.box[0])
+        mws = C.c_double(0.0)
+        ref = lambda x: C.byref(x) if x is not None else None
+        A.check(self.ctx.lib.tmk_patch_update_state_3d(
+            self.ctx.h, C.byref(Uf), ref(Bf), ref(Ff[0]), ref(Ff[1]), ref(Ff[2]), C.byref(v), C.byref(d),
+            self.dx, self.time, dt, C.byref(mws), _stream_ptr(stream)), "tmk_patch_update_state_3d")
+        return mws.value, F
+
+    def plastic_update(self, U, ulo, dt: float, box=None, stream=None):
+        b = A.box3(*(box or self.box))
+        A.check(self.ctx.lib.tmk_plastic_update_3d(self.ctx.h, C.byref(_fab3(U, ulo)), C.byref(b), dt,
+                                                   _stream_ptr(stream)), "tmk_plastic_update_3d")
+
+
 class LinElastLevelGodunov:
     """Device-resident single level (all patches of the level in one launch)."""
 
