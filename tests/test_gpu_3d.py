@@ -178,3 +178,89 @@ def test_bad_descriptors_are_refused(cuda_lib):
     with pytest.raises(A.TmkError):      # a fault patch without fault data
         pg.update_state(U, (-G, -G, -G), sc.dt())
     ctx.close()
+
+
+MIXED = [n for n in ("rs_slip", "rs_aging", "sw_ref9", "sw_off11", "rs_plm2", "no_fault")]
+
+
+@pytest.mark.parametrize("name", MIXED)
+def test_mixed_patch_step_3d_close_to_oracle(cuda_lib, name):
+    """The mixed form (FP32 volume arithmetic and intermediates; FP64 state,
+    friction and boundary data) against the FP64 oracle: one step, FP32
+    rounding of the increments (2e-5 of each component's scale for the state
+    and the fluxes, 1e-3 for the fault's boundary data, whose slip rates
+    amplify the rounding of the shear through the friction law)."""
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    sc = dict(SCEN)[name]
+    lo, hi = (0, 0, 0), (NX - 1, NY - 1, NZ - 1)
+    rng = np.random.default_rng(77)
+    U0 = perturbed_state_3d(sc, rng, lo, hi)
+    fault = sc.scheme.fault_law != A.TMK_FAULT_NONE
+    blo = (-G, -G)
+    B0 = random_B_3d(sc, rng, NX + 2 * G, NZ + 2 * G) if fault else None
+    dt, time = sc.dt(), 0.5
+    Ur, Br = U0.copy(), (B0.copy() if fault else None)
+    rc, Fr = O.patch_update_state_3d(sc, Ur, (-G, -G, -G), lo, hi, DOM[0], DOM[1], Br, blo, DX, time, dt,
+                                     with_flux=True)
+    assert rc == 0
+    old = sc.scheme.precision
+    sc.scheme.precision = A.TMK_PREC_MIXED
+    try:
+        ctx = Context(sc)
+    finally:
+        sc.scheme.precision = old
+    pg = LinElastPatchGodunov3D(ctx, DOM)
+    pg.set_current_box((lo, hi))
+    pg.set_current_time(time)
+    Ud = torch.from_numpy(U0.copy()).cuda()
+    Bd = torch.from_numpy(B0.copy()).cuda() if fault else None
+    _, F = pg.update_state(Ud, (-G, -G, -G), dt, B=Bd, blo=blo, with_flux=True)
+    torch.cuda.synchronize()
+    Ug = Ud.cpu().numpy()
+    v = (slice(None), slice(G, -G), slice(G, -G), slice(G, -G))
+    eu = rel_err(Ug[v], Ur[v])
+    ev = [c for c in range(22) if c % 11 < 9]
+    ef = max(rel_err(F[d].cpu().numpy()[ev], Fr[d][ev]) for d in range(3))
+    print(name, "state", eu, "flux", ef)
+    assert eu < 2e-5 and ef < 2e-5
+    assert eu > 0.0, "the mixed form must not be the FP64 path"
+    if fault:
+        bv = (slice(None), slice(G, -G), slice(G, -G))
+        eb = rel_err(Bd.cpu().numpy()[bv], Br[bv])
+        print(name, "bdry", eb)
+        assert eb < 1e-3
+    ctx.close()
+
+
+def test_mixed_3d_tracks_fp64_over_steps(cuda_lib):
+    """Twenty steps of a smooth rate-and-state state in both forms on the GPU:
+    the mixed form stays within 1e-4 of the FP64 form."""
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    sc = S.rate_state(nx=NX, ny=NY, dx=DX)
+    lo, hi = (0, 0, 0), (NX - 1, NY - 1, NZ - 1)
+    rng = np.random.default_rng(12)
+    U0 = perturbed_state_3d(sc, rng, lo, hi, amp_v=0.01, amp_s=0.5)
+    B0 = random_B_3d(sc, rng, NX + 2 * G, NZ + 2 * G)
+    out = {}
+    for prec in (A.TMK_PREC_FP64, A.TMK_PREC_MIXED):
+        sc.scheme.precision = prec
+        ctx = Context(sc)
+        pg = LinElastPatchGodunov3D(ctx, DOM)
+        pg.set_current_box((lo, hi))
+        Ud = torch.from_numpy(U0.copy()).cuda()
+        Bd = torch.from_numpy(B0.copy()).cuda()
+        for n in range(20):
+            pg.set_current_time(n * sc.dt())
+            pg.update_state(Ud, (-G, -G, -G), sc.dt(), B=Bd, blo=(-G, -G))
+        torch.cuda.synchronize()
+        out[prec] = (Ud.cpu().numpy(), Bd.cpu().numpy())
+        ctx.close()
+    sc.scheme.precision = A.TMK_PREC_FP64
+    v = (slice(None), slice(G, -G), slice(G, -G), slice(G, -G))
+    a, b = out[A.TMK_PREC_MIXED][0][v], out[A.TMK_PREC_FP64][0][v]
+    assert np.isfinite(a).all()
+    e = rel_err(a, b)
+    print("20 steps", e)
+    assert 0.0 < e < 1e-4

@@ -1,13 +1,14 @@
 """In-tree build of libtetemoko_gb300.so for sm_103a with nvcc.
 
-Seven translation units, compiled in parallel:
+Eight translation units, compiled in parallel:
   tmk_fp64.cu  plain FP64 kernels, --fmad=false (parity with the CPU oracle)
   tmk_fp32.cu  mixed-form kernels (FP32 volume, FP64 friction)
   tmk_capi.cu  the C ABI (host code)
   tmk_noalloc.cu  the allocation-free patch step (fixed device scratch array)
   tmk_amr.cu   coarse-fine coupling and the AMR hierarchy, --fmad=false
   tmk_regrid.cu  refinement tagging, --fmad=false
-  tmk_3d.cu    the 3-D patch step (CH_SPACEDIM == 3), --fmad=false
+  tmk_3d.cu    the 3-D patch step (CH_SPACEDIM == 3), FP64 form, --fmad=false
+  tmk_3d_f32.cu  its mixed form (FP32 volume arithmetic)
 """
 from __future__ import annotations
 
@@ -32,6 +33,7 @@ UNITS = {
     "tmk_amr.cu": ["--fmad=false"],
     "tmk_regrid.cu": ["--fmad=false"],
     "tmk_3d.cu": ["--fmad=false"],
+    "tmk_3d_f32.cu": [],
 }
 
 

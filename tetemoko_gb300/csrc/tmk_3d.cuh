@@ -1,0 +1,500 @@
+// The 3-D patch step (CH_SPACEDIM == 3): kernels, templated on the arithmetic
+// of the volume stencil T.
+//
+// LinElastPatchGodunov::updateState in 3-D (srcLinElast/LinElastPatchGodunov.cpp:
+// 101-129, 174-469) as five kinds of passes over one patch, each a grid of one
+// thread per cell or face, with the intermediates in device scratch:
+//   pred<D>      normal predictor in direction D on the slope box (both sides
+//                of the fault packed as 18 components: the nine evolving
+//                components of each side; lambda and gamma carry no flux)
+//   riem1<D>     first-pass face states WHalf1[D] (Riemann solve, or the
+//                domain-edge / fault condition)
+//   riem2<D1,D2> WHalf2[D1][D2]: the D1 face states after the normal states
+//                were moved by -(1/3) dt/dx A dW/dx of WHalf1[D2] (:329-381)
+//   final<D1>    the time-centred WHalf[D1], normal states moved by both
+//                WHalf2[D2][D3] with -(1/2) dt/dx (:422-440)
+//   update       fluxes, their divergence and U += -dt/dx dU in place; then
+//                the fault's boundary data (RSSETBND / SWSETBND, final)
+// The fault is the y-lo plane of the domain.  Its boundary data predicted at
+// (1/3) dt from WHalf1[1] and at (1/2) dt from WHalf2[1][2] (the reference's
+// call order leaves those in m_tmpBdryData when WHalf2[1][*] and WHalf[1] are
+// solved) are formed at the face that reads them.  Fault faces keep all 22
+// components of their states (FP64) beside the 18-component arrays, because
+// the reference-layout slip-weakening law reads and writes side 2 from
+// component 9.
+//
+// T = double: the plain FP64 form (built without FMA contraction; equal to the
+// CPU oracle to rounding).  T = float: the mixed form -- predictors, Riemann
+// solves, transverse corrections and fluxes in FP32 with FP32 intermediates;
+// the state U, its update, the friction solves and the boundary data in FP64.
+#pragma once
+
+#include "tmk_kernels.cuh"
+
+namespace tmk {
+namespace d3 {
+
+constexpr int NS = 2 * NSIDE;     // 18 stored components
+
+struct Bx {
+  int lo[3], n[3];
+  TMK_HD long long cells() const { return (long long)n[0] * n[1] * n[2]; }
+  TMK_HD bool has(int i, int j, int k) const {
+    return i >= lo[0] && i < lo[0] + n[0] && j >= lo[1] && j < lo[1] + n[1] && k >= lo[2] && k < lo[2] + n[2];
+  }
+  TMK_HD long long at(int i, int j, int k) const {
+    return ((long long)(k - lo[2]) * n[1] + (j - lo[1])) * n[0] + (i - lo[0]);
+  }
+  TMK_HD void cell(long long t, int& i, int& j, int& k) const {
+    i = lo[0] + (int)(t % n[0]);
+    long long r = t / n[0];
+    j = lo[1] + (int)(r % n[1]);
+    k = lo[2] + (int)(r / n[1]);
+  }
+};
+
+template <typename T>
+struct Step3 {
+  Bx A;                 // U's box
+  Bx S;                 // slope box: grow(valid, 1) & domain
+  Bx fl1[3];            // first-pass faces: nodes(ccBox[d], d)
+  Bx cc[3];             // ccBox[d]: grow(valid, 1) shrunk by 1 in d, & domain
+  Bx flF[3];            // final faces: nodes(valid, d)
+  Bx cur;
+  int dlo[3], dhi[3];
+  Bx fplane;            // fault faces of the first pass (x, z of fl1[1]; j = domain lo)
+  Bx bb;                // B's box (j = domain lo)
+  double* U;
+  T* WM[3];
+  T* WP[3];
+  T* WH1[3];
+  T* WH2[3][3];         // WHalf2[d1][d2], d1 != d2
+  T* WH[3];
+  double* LG;           // lambda, gamma of side 1 predicted at the fault's lo faces (fplane)
+  double* FF[3];        // 22-comp fault-face states of WHalf1[1], WHalf2[1][2], WHalf[1] (fplane)
+  double* B;
+  double* F[3];         // optional face fluxes (22 comps over flF[d])
+  double dx, dt, time;
+  int fault;
+};
+
+template <int D> TMK_HD double rvs(int s) { return (D == 1 && s == 1) ? -1.0 : 1.0; }
+
+template <typename T>
+TMK_D void load18(const T* a, const Bx& b, int i, int j, int k, T* q) {
+  const long long cs = b.cells(), o = b.at(i, j, k);
+#pragma unroll
+  for (int c = 0; c < NS; ++c) q[c] = a[c * cs + o];
+}
+template <typename T>
+TMK_D void store18(T* a, const Bx& b, int i, int j, int k, const T* q) {
+  const long long cs = b.cells(), o = b.at(i, j, k);
+#pragma unroll
+  for (int c = 0; c < NS; ++c) a[c * cs + o] = q[c];
+}
+template <int D> TMK_D void step(int& i, int& j, int& k, int s) {
+  if (D == 0) i += s; else if (D == 1) j += s; else k += s;
+}
+template <int D> TMK_D int coord(int i, int j, int k) { return D == 0 ? i : (D == 1 ? j : k); }
+
+// Predicted lo-face value of a zero-speed component (lambda or gamma) in the
+// arithmetic of ppm_predict / plm_predict: PPM limited delta, PLM traced slope,
+// or the cell value (CTU).
+TMK_D double zero_speed_lo(const DevParams& P, const double* w, const bool* in) {
+  const bool lim = P.prim_lim || P.char_lim;
+  if (P.order == 0) return w[2];
+  if (P.order == 1) {
+    double sl = plm_slope(w, in, lim, P.fourth != 0);
+    if (lim && (P.char_lim || P.fourth)) {
+      double m, p1;
+      plm_onesided(w, in, m, p1);
+      sl = plm_limit(sl, m, p1);
+    }
+    return -0.5 * sl + w[2];
+  }
+  double dm, dp;
+  ppm_deltas(w, in, lim, dm, dp);
+  if (lim) ppm_limit(dm, dp);
+  return dm + w[2];
+}
+
+// ------------------------------------------------------------- predictors
+template <int D, typename T>
+__global__ void __launch_bounds__(128) pred_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp) {
+  const DevParams& P = *Pp;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= g.S.cells()) return;
+  int i, j, k;
+  g.S.cell(t, i, j, k);
+  Consts<T> kc;
+  kc.load(P);
+  T sig[NSIDE];
+  make_sig(P, g.dt / g.dx, sig);
+  const int q0 = coord<D>(i, j, k);
+  bool in[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) in[m] = q0 - 2 + m >= g.dlo[D] && q0 - 2 + m <= g.dhi[D];
+  const long long acs = g.A.cells();
+  T WM[NS], WP[NS];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    T w5[NSIDE][5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      int ii = i, jj = j, kk = k;
+      step<D>(ii, jj, kk, m - 2);
+      const long long o = in[m] ? g.A.at(ii, jj, kk) : 0;
+#pragma unroll
+      for (int c = 0; c < NSIDE; ++c) w5[c][m] = in[m] ? (T)g.U[(11 * s + c) * acs + o] : T(0);
+    }
+    ppm_predict<D, T>(kc, (T)rvs<D>(s), w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM + NSIDE * s,
+                      WP + NSIDE * s, P.order, P.fourth != 0);
+  }
+  store18(g.WM[D], g.S, i, j, k, WM);
+  store18(g.WP[D], g.S, i, j, k, WP);
+  if (D == 1 && g.fault && j == g.dlo[1]) {
+    // lambda and gamma of side 1 at the fault's lo faces (read by the
+    // reference-layout slip-weakening law as side-2 velocities)
+#pragma unroll
+    for (int c = 9; c < 11; ++c) {
+      double w[5];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        int ii = i, jj = j, kk = k;
+        step<D>(ii, jj, kk, m - 2);
+        w[m] = in[m] ? g.U[c * acs + g.A.at(ii, jj, kk)] : 0.0;
+      }
+      g.LG[(c - 9) * g.fplane.cells() + g.fplane.at(i, j, k)] = zero_speed_lo(P, w, in);
+    }
+  }
+}
+
+// -------------------------------------------------------- face conditions
+// Boundary data value the fault law reads at face (i, k): psi (rate and
+// state) or slip (slip weakening), from B, or from B moved by the 22-comp face
+// state U22 over `dtp` (the predictor's m_tmpBdryData, updateBoundary final=false).
+template <typename T>
+TMK_D double bdry_value(const DevParams& P, const Step3<T>& g, int i, int k, const double* U22, double dtp) {
+  double* Bi = g.B + g.bb.at(i, g.dlo[1], k);
+  const long long bs = g.bb.cells();
+  if (!U22) return P.fault_law == 1 ? Bi[10 * bs] : Bi[7 * bs];
+  if (P.fault_law == 1) {
+    const RSFace fr = rs_face(P, nullptr, 0, 0);
+    return rs_setbnd(P, fr, U22, Bi, (int)bs, dtp, (i + 0.5) * g.dx - P.rs_x0, 0.0, false);
+  }
+  return sw_setbnd(P, U22, Bi, (int)bs, dtp, 0.0, false);
+}
+
+// fault face (i, dom lo, k): 22-comp state Wg from the interior state Wi22
+TMK_D void fault_face(const DevParams& P, double dx, int i, int k, const double* Wi, double bval, double* Wg,
+                      DevStatus* st) {
+#pragma unroll
+  for (int c = 0; c < NC; ++c) Wg[c] = 0.0;
+  const double xc = (i + 0.5) * dx;
+  if (P.fault_law == 1) {
+    const RSFace fr = rs_face(P, nullptr, 0, 0);
+    const int it = rs_fault(P, fr, Wi, bval, xc - P.rs_x0, Wg);
+    if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
+  } else {
+    sw_fault<true>(P, Wi, bval, xc, Wg, (k + 0.5) * dx);
+  }
+}
+
+// Face f of direction D with left cell state L18 and right cell state R18:
+// Riemann solve, or the domain-edge condition.  Returns false for the fault
+// faces (y lo with a fault law), which the caller solves.
+template <int D, typename T>
+TMK_D bool face_state(const DevParams& P, const Consts<T>& kc, const Step3<T>& g, int f, const T* L18,
+                      const T* R18, T* G18) {
+  if (f == g.dlo[D] || f == g.dhi[D] + 1) {
+    const bool lo = f == g.dlo[D];
+    if (lo && D == 1 && g.fault) return false;
+    const bool outflow = P.bc[2 * D + (lo ? 0 : 1)] == 0;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      T bg[NSIDE];
+#pragma unroll
+      for (int c = 0; c < NSIDE; ++c) bg[c] = (T)P.bg[11 * s + c];
+      edge_bc<D, T>(kc, (T)rvs<D>(s), lo ? -1 : +1, outflow, bg, (lo ? R18 : L18) + NSIDE * s, G18 + NSIDE * s);
+    }
+  } else {
+#pragma unroll
+    for (int s = 0; s < 2; ++s) riemann<D, T>(kc, (T)rvs<D>(s), L18 + NSIDE * s, R18 + NSIDE * s, G18 + NSIDE * s);
+  }
+  return true;
+}
+
+// fault face: gather the 22-comp interior state, solve in FP64, keep 22 comps in FFk
+template <typename T>
+TMK_D void fault_solve(const DevParams& P, const Step3<T>& g, int i, int k, const T* R18, double bval,
+                       double* FFk, T* G18, DevStatus* st) {
+  double Wi[NC], Wg[NC];
+  const long long fo = g.fplane.at(i, g.dlo[1], k), fcs = g.fplane.cells();
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) { Wi[c] = (double)R18[c]; Wi[11 + c] = (double)R18[NSIDE + c]; }
+  Wi[9] = g.LG[fo]; Wi[10] = g.LG[fcs + fo];
+  Wi[20] = 0.0; Wi[21] = 0.0;
+  fault_face(P, g.dx, i, k, Wi, bval, Wg, st);
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) { G18[c] = (T)Wg[c]; G18[NSIDE + c] = (T)Wg[11 + c]; }
+  if (FFk) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) FFk[c * fcs + fo] = Wg[c];
+  }
+}
+
+template <typename T>
+TMK_D void load_ff(const Step3<T>& g, const double* FFk, int i, int k, double* U22) {
+  const long long fo = g.fplane.at(i, g.dlo[1], k), fcs = g.fplane.cells();
+#pragma unroll
+  for (int c = 0; c < NC; ++c) U22[c] = FFk[c * fcs + fo];
+}
+
+// ------------------------------------------------------------ first pass
+template <int D, typename T>
+__global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
+                                                    DevStatus* st) {
+  const DevParams& P = *Pp;
+  const Bx& fb = g.fl1[D];
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= fb.cells()) return;
+  int i, j, k;
+  fb.cell(t, i, j, k);
+  Consts<T> kc;
+  kc.load(P);
+  const int f = coord<D>(i, j, k);
+  T L[NS], R[NS], G[NS];
+  int li = i, lj = j, lk = k;
+  step<D>(li, lj, lk, -1);
+  if (f > g.dlo[D]) load18(g.WP[D], g.S, li, lj, lk, L);
+  if (f <= g.dhi[D]) load18(g.WM[D], g.S, i, j, k, R);
+  if (!face_state<D, T>(P, kc, g, f, L, R, G))
+    fault_solve(P, g, i, k, R, bdry_value(P, g, i, k, nullptr, 0.0), g.FF[0], G, st);
+  store18(g.WH1[D], fb, i, j, k, G);
+}
+
+// cell state T18 of array A (direction-D1 normal states) at (i, j, k), moved by
+// -(scale) A dW/dx of the face states H in direction D2 where the cell lies in ccBox[D2]
+template <int D2, typename T>
+TMK_D void corrected(const Step3<T>& g, const Consts<T>& kc, const T* A, const T* H, const Bx& hb, T scale, int i,
+                     int j, int k, T* T18) {
+  load18(A, g.S, i, j, k, T18);
+  if (!g.cc[D2].has(i, j, k)) return;
+  T h[NS], l[NS];
+  int hi = i, hj = j, hk = k;
+  step<D2>(hi, hj, hk, 1);
+  load18(H, hb, hi, hj, hk, h);
+  load18(H, hb, i, j, k, l);
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+    adwdx_add<D2, T>(kc, (T)rvs<D2>(s), scale, h + NSIDE * s, l + NSIDE * s, T18 + NSIDE * s);
+}
+
+// ----------------------------------------------------------- second pass
+template <int D1, int D2, typename T>
+__global__ void __launch_bounds__(128) riem2_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
+                                                    DevStatus* st) {
+  const DevParams& P = *Pp;
+  const Bx& fb = g.fl1[D1];
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= fb.cells()) return;
+  int i, j, k;
+  fb.cell(t, i, j, k);
+  Consts<T> kc;
+  kc.load(P);
+  const T scale = (T)(-(1.0 / 3.0) * g.dt / g.dx);
+  const int f = coord<D1>(i, j, k);
+  T L[NS], R[NS], G[NS];
+  int li = i, lj = j, lk = k;
+  step<D1>(li, lj, lk, -1);
+  if (f > g.dlo[D1]) corrected<D2, T>(g, kc, g.WP[D1], g.WH1[D2], g.fl1[D2], scale, li, lj, lk, L);
+  if (f <= g.dhi[D1]) corrected<D2, T>(g, kc, g.WM[D1], g.WH1[D2], g.fl1[D2], scale, i, j, k, R);
+  if (!face_state<D1, T>(P, kc, g, f, L, R, G)) {
+    double U22[NC];
+    load_ff(g, g.FF[0], i, k, U22);
+    const double bval = bdry_value(P, g, i, k, U22, (1.0 / 3.0) * g.dt);
+    fault_solve(P, g, i, k, R, bval, (D2 == 2) ? g.FF[1] : nullptr, G, st);
+  }
+  store18(g.WH2[D1][D2], fb, i, j, k, G);
+}
+
+// ------------------------------------------------------------ final pass
+template <int D1, int Dc, typename T>
+TMK_D void add_final(const Step3<T>& g, const Consts<T>& kc, T scale, int i, int j, int k, T* T18) {
+  if (!g.cc[Dc].has(i, j, k)) return;
+  constexpr int D3 = 3 - D1 - Dc;
+  T h[NS], l[NS];
+  int hi = i, hj = j, hk = k;
+  step<Dc>(hi, hj, hk, 1);
+  load18(g.WH2[Dc][D3], g.fl1[Dc], hi, hj, hk, h);
+  load18(g.WH2[Dc][D3], g.fl1[Dc], i, j, k, l);
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+    adwdx_add<Dc, T>(kc, (T)rvs<Dc>(s), scale, h + NSIDE * s, l + NSIDE * s, T18 + NSIDE * s);
+}
+
+template <int D1, typename T>
+TMK_D void final_state(const Step3<T>& g, const Consts<T>& kc, const T* A, T scale, int i, int j, int k, T* T18) {
+  constexpr int Da = (D1 == 0) ? 1 : 0;      // the two other directions, ascending
+  constexpr int Db = (D1 == 2) ? 1 : 2;
+  load18(A, g.S, i, j, k, T18);
+  add_final<D1, Da, T>(g, kc, scale, i, j, k, T18);
+  add_final<D1, Db, T>(g, kc, scale, i, j, k, T18);
+}
+
+template <int D1, typename T>
+__global__ void __launch_bounds__(128) final_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
+                                                    DevStatus* st) {
+  const DevParams& P = *Pp;
+  const Bx& fb = g.flF[D1];
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= fb.cells()) return;
+  int i, j, k;
+  fb.cell(t, i, j, k);
+  Consts<T> kc;
+  kc.load(P);
+  const T scale = (T)(-(1.0 / 2.0) * g.dt / g.dx);
+  const int f = coord<D1>(i, j, k);
+  T L[NS], R[NS], G[NS];
+  int li = i, lj = j, lk = k;
+  step<D1>(li, lj, lk, -1);
+  if (f > g.dlo[D1]) final_state<D1, T>(g, kc, g.WP[D1], scale, li, lj, lk, L);
+  if (f <= g.dhi[D1]) final_state<D1, T>(g, kc, g.WM[D1], scale, i, j, k, R);
+  if (!face_state<D1, T>(P, kc, g, f, L, R, G)) {
+    double U22[NC];
+    load_ff(g, g.FF[1], i, k, U22);
+    const double bval = bdry_value(P, g, i, k, U22, (1.0 / 2.0) * g.dt);
+    fault_solve(P, g, i, k, R, bval, g.FF[2], G, st);
+  }
+  store18(g.WH[D1], fb, i, j, k, G);
+}
+
+// ---------------------------------------------------------------- update
+template <int D, typename T>
+TMK_D void flux_diff(const Step3<T>& g, const Consts<T>& kc, int i, int j, int k, T* dU) {
+  T h[NS], l[NS], Fh[NS], Fl[NS];
+  int hi = i, hj = j, hk = k;
+  step<D>(hi, hj, hk, 1);
+  load18(g.WH[D], g.flF[D], hi, hj, hk, h);
+  load18(g.WH[D], g.flF[D], i, j, k, l);
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    flux<D, T>(kc, (T)rvs<D>(s), h + NSIDE * s, Fh + NSIDE * s);
+    flux<D, T>(kc, (T)rvs<D>(s), l + NSIDE * s, Fl + NSIDE * s);
+  }
+#pragma unroll
+  for (int c = 0; c < NS; ++c) dU[c] += Fh[c] - Fl[c];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) update_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp) {
+  const DevParams& P = *Pp;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= g.cur.cells()) return;
+  int i, j, k;
+  g.cur.cell(t, i, j, k);
+  Consts<T> kc;
+  kc.load(P);
+  T dU[NS];
+#pragma unroll
+  for (int c = 0; c < NS; ++c) dU[c] = T(0);
+  flux_diff<0, T>(g, kc, i, j, k, dU);
+  flux_diff<1, T>(g, kc, i, j, k, dU);
+  flux_diff<2, T>(g, kc, i, j, k, dU);
+  const double sc = -g.dt / g.dx;
+  const long long acs = g.A.cells(), o = g.A.at(i, j, k);
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) {
+      double* u = g.U + (11 * s + c) * acs + o;
+      *u = *u + (double)dU[NSIDE * s + c] * sc;
+    }
+}
+
+// the face fluxes of direction D (22 comps; lambda, gamma and the antiplane
+// stress of the face normal carry none)
+template <int D, typename T>
+__global__ void __launch_bounds__(128) flux_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp) {
+  const DevParams& P = *Pp;
+  const Bx& fb = g.flF[D];
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= fb.cells()) return;
+  int i, j, k;
+  fb.cell(t, i, j, k);
+  Consts<T> kc;
+  kc.load(P);
+  T w[NS], F[NS];
+  load18(g.WH[D], fb, i, j, k, w);
+#pragma unroll
+  for (int s = 0; s < 2; ++s) flux<D, T>(kc, (T)rvs<D>(s), w + NSIDE * s, F + NSIDE * s);
+  const long long cs = fb.cells();
+  double* out = g.F[D] + t;
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) out[(11 * s + c) * cs] = (double)F[NSIDE * s + c];
+    out[(11 * s + 9) * cs] = 0.0;
+    out[(11 * s + 10) * cs] = 0.0;
+  }
+}
+
+// the fault's boundary data, final (RSSETBND / SWSETBND over the valid x, z)
+template <typename T>
+__global__ void __launch_bounds__(128) bdry_final_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
+                                                         DevStatus* st) {
+  const DevParams& P = *Pp;
+  const int nx = g.cur.n[0], nz = g.cur.n[2];
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)nx * nz) return;
+  const int i = g.cur.lo[0] + (int)(t % nx), k = g.cur.lo[2] + (int)(t / nx);
+  double U22[NC];
+  load_ff(g, g.FF[2], i, k, U22);
+  const long long bo = g.bb.at(i, g.dlo[1], k);
+  double* Bi = g.B + bo;
+  const int bs = (int)g.bb.cells();
+  if (P.fault_law == 1) {
+    const RSFace fr = rs_face(P, nullptr, 0, 0);
+    const double psi = rs_setbnd(P, fr, U22, Bi, bs, g.dt, (i + 0.5) * g.dx - P.rs_x0, g.time + g.dt, true);
+    if (isnan(psi)) report(st, ST_NAN, bo);
+  } else {
+    sw_setbnd(P, U22, Bi, bs, g.dt, g.time + g.dt, true);
+  }
+}
+
+inline unsigned blocks(long long n) { return (unsigned)((n + 127) / 128); }
+
+// the whole step on stream s, in the reference's order
+template <typename T>
+cudaError_t launch_step(const Step3<T>& g, const DevParams* P, DevStatus* st, cudaStream_t s) {
+  const unsigned bS = blocks(g.S.cells());
+  pred_kernel<0, T><<<bS, 128, 0, s>>>(g, P);
+  pred_kernel<1, T><<<bS, 128, 0, s>>>(g, P);
+  pred_kernel<2, T><<<bS, 128, 0, s>>>(g, P);
+  riem1_kernel<0, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st);
+  riem1_kernel<1, T><<<blocks(g.fl1[1].cells()), 128, 0, s>>>(g, P, st);
+  riem1_kernel<2, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st);
+  riem2_kernel<0, 1, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st);
+  riem2_kernel<0, 2, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st);
+  riem2_kernel<1, 0, T><<<blocks(g.fl1[1].cells()), 128, 0, s>>>(g, P, st);
+  riem2_kernel<1, 2, T><<<blocks(g.fl1[1].cells()), 128, 0, s>>>(g, P, st);
+  riem2_kernel<2, 0, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st);
+  riem2_kernel<2, 1, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st);
+  final_kernel<0, T><<<blocks(g.flF[0].cells()), 128, 0, s>>>(g, P, st);
+  final_kernel<1, T><<<blocks(g.flF[1].cells()), 128, 0, s>>>(g, P, st);
+  final_kernel<2, T><<<blocks(g.flF[2].cells()), 128, 0, s>>>(g, P, st);
+  if (g.F[0]) flux_kernel<0, T><<<blocks(g.flF[0].cells()), 128, 0, s>>>(g, P);
+  if (g.F[1]) flux_kernel<1, T><<<blocks(g.flF[1].cells()), 128, 0, s>>>(g, P);
+  if (g.F[2]) flux_kernel<2, T><<<blocks(g.flF[2].cells()), 128, 0, s>>>(g, P);
+  update_kernel<T><<<blocks(g.cur.cells()), 128, 0, s>>>(g, P);
+  if (g.fault) bdry_final_kernel<T><<<blocks((long long)g.cur.n[0] * g.cur.n[2]), 128, 0, s>>>(g, P, st);
+  return cudaGetLastError();
+}
+
+// FP64 instantiation (tmk_3d.cu, built without FMA contraction) and the mixed
+// form (tmk_3d_f32.cu)
+cudaError_t launch_step_f64(const Step3<double>& g, const DevParams* P, DevStatus* st, cudaStream_t s);
+cudaError_t launch_step_f32(const Step3<float>& g, const DevParams* P, DevStatus* st, cudaStream_t s);
+
+}  // namespace d3
+}  // namespace tmk
