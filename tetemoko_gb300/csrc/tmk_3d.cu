@@ -65,6 +65,13 @@ Bx bx_nodes(Bx b, int d) { b.n[d] += 1; return b; }
 
 size_t align_up3(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// make_sig on the host (the same FP64 products, rounded to T)
+template <typename T>
+void make_sig_host(const tmk::DevParams& P, double dtbydx, T* sig) {
+  const double l[9] = {-P.cp, -P.cs, -P.cs, 0.0, 0.0, 0.0, P.cs, P.cs, P.cp};
+  for (int c = 0; c < 9; ++c) sig[c] = (T)(l[c] * dtbydx);
+}
+
 }  // namespace
 
 namespace {
@@ -73,8 +80,9 @@ namespace {
 template <typename T>
 tmk_status step3(tmk_context* c, tmk::d3::Step3<T>& g, cudaStream_t s) {
   using namespace tmk::d3;
-  // scratch: WM, WP (3 each) | WH1 (3) | WH2 (6) | WH (3) | LG | FF (3)
+  // scratch: WM, WP (3 each) | WH1 (3) | WH2 (6) | WH (3) | LG | FF (3) | FP32 copy of U
   const size_t s18 = (size_t)NS * g.S.cells() * sizeof(T);
+  constexpr bool copy = !std::is_same<T, double>::value;
   std::vector<size_t> sizes;
   for (int d = 0; d < 6; ++d) sizes.push_back(s18);
   for (int d = 0; d < 3; ++d) sizes.push_back((size_t)NS * g.fl1[d].cells() * sizeof(T));
@@ -84,6 +92,7 @@ tmk_status step3(tmk_context* c, tmk::d3::Step3<T>& g, cudaStream_t s) {
   for (int d = 0; d < 3; ++d) sizes.push_back((size_t)NS * g.flF[d].cells() * sizeof(T));
   sizes.push_back(2 * (size_t)g.fplane.cells() * sizeof(double));
   for (int k = 0; k < 3; ++k) sizes.push_back((size_t)TMK_NCOMP * g.fplane.cells() * sizeof(double));
+  sizes.push_back(copy ? (size_t)NS * g.Ap.cells() * sizeof(T) : 0);
   size_t total = 0;
   for (size_t z : sizes) total += align_up3(z);
   if (total > c->scratch_bytes) {
@@ -105,6 +114,14 @@ tmk_status step3(tmk_context* c, tmk::d3::Step3<T>& g, cudaStream_t s) {
   for (int d = 0; d < 3; ++d) g.WH[d] = (T*)take();
   g.LG = (double*)take();
   for (int k = 0; k < 3; ++k) g.FF[k] = (double*)take();
+  T* up = (T*)take();
+  if constexpr (copy) { g.Up = up; g.uside = tmk::NSIDE; }
+  else { g.Up = (const T*)(const void*)g.U; g.Ap = g.A; g.uside = 11; }
+  g.kc.load(c->hp);
+  make_sig_host(c->hp, g.dt / g.dx, g.sig);
+  g.scale3 = (T)(-(1.0 / 3.0) * g.dt / g.dx);
+  g.scale2 = (T)(-(1.0 / 2.0) * g.dt / g.dx);
+  g.sc = -g.dt / g.dx;
   cudaError_t e;
   if constexpr (std::is_same<T, double>::value) e = launch_step_f64(g, c->dp, c->dstatus, s);
   else e = launch_step_f32(g, c->dp, c->dstatus, s);
@@ -148,6 +165,7 @@ tmk_status patch3(tmk_context* c, const tmk_fab3* U, const tmk_fab3* B, const tm
     g.F[d] = Fo[d]->data;
   }
   g.U = U->data;
+  g.Ap = bx_isect(bx_grow(cur, 3), dom);
   g.dx = dx; g.dt = dt; g.time = time;
   return step3<T>(c, g, s);
 }

@@ -26,7 +26,8 @@
 // T = double: the plain FP64 form (built without FMA contraction; equal to the
 // CPU oracle to rounding).  T = float: the mixed form -- predictors, Riemann
 // solves, transverse corrections and fluxes in FP32 with FP32 intermediates;
-// the state U, its update, the friction solves and the boundary data in FP64.
+// the state U, its update, the friction solves (the 2-D mixed form's
+// arrangement for rate and state) and the boundary data in FP64.
 #pragma once
 
 #include "tmk_kernels.cuh"
@@ -76,6 +77,16 @@ struct Step3 {
   double* F[3];         // optional face fluxes (22 comps over flF[d])
   double dx, dt, time;
   int fault;
+  // the predictors' input: U itself (FP64 form; side s at component 11 s) or
+  // its FP32 copy over grow(valid, 3) & domain made once per step (mixed form;
+  // side s at component 9 s), so that no predictor converts FP64 values
+  const T* Up;
+  Bx Ap;
+  int uside;
+  Consts<T> kc;         // the physical constants in T (computed on the host)
+  T sig[NSIDE];         // characteristic Courant numbers lambda dt/dx
+  T scale3, scale2;     // -(1/3) dt/dx and -(1/2) dt/dx
+  double sc;            // -dt/dx
 };
 
 template <int D> TMK_HD double rvs(int s) { return (D == 1 && s == 1) ? -1.0 : 1.0; }
@@ -96,6 +107,30 @@ template <int D> TMK_D void step(int& i, int& j, int& k, int s) {
   if (D == 0) i += s; else if (D == 1) j += s; else k += s;
 }
 template <int D> TMK_D int coord(int i, int j, int k) { return D == 0 ? i : (D == 1 ? j : k); }
+
+// Face t of the y-face box fb with the fault plane (its first y layer) first:
+// the friction solves, long chains of dependent FP64 operations, then start
+// with the grid and run beside the bulk instead of trailing it.
+TMK_D void face_fault_first(const Bx& fb, bool fault, long long t, int& i, int& j, int& k) {
+  const long long nf = (long long)fb.n[0] * fb.n[2];
+  if (!fault) { fb.cell(t, i, j, k); return; }
+  if (t < nf) {
+    i = fb.lo[0] + (int)(t % fb.n[0]);
+    j = fb.lo[1];
+    k = fb.lo[2] + (int)(t / fb.n[0]);
+    return;
+  }
+  t -= nf;
+  const int ny = fb.n[1] - 1;
+  i = fb.lo[0] + (int)(t % fb.n[0]);
+  const long long r = t / fb.n[0];
+  j = fb.lo[1] + 1 + (int)(r % ny);
+  k = fb.lo[2] + (int)(r / ny);
+}
+template <int D> TMK_D void face_at(const Bx& fb, bool fault, long long t, int& i, int& j, int& k) {
+  if (D == 1) face_fault_first(fb, fault, t, i, j, k);
+  else fb.cell(t, i, j, k);
+}
 
 // Predicted lo-face value of a zero-speed component (lambda or gamma) in the
 // arithmetic of ppm_predict / plm_predict: PPM limited delta, PLM traced slope,
@@ -126,15 +161,13 @@ __global__ void __launch_bounds__(128) pred_kernel(const __grid_constant__ Step3
   if (t >= g.S.cells()) return;
   int i, j, k;
   g.S.cell(t, i, j, k);
-  Consts<T> kc;
-  kc.load(P);
-  T sig[NSIDE];
-  make_sig(P, g.dt / g.dx, sig);
+  const Consts<T>& kc = g.kc;
+  const T* sig = g.sig;
   const int q0 = coord<D>(i, j, k);
   bool in[5];
 #pragma unroll
   for (int m = 0; m < 5; ++m) in[m] = q0 - 2 + m >= g.dlo[D] && q0 - 2 + m <= g.dhi[D];
-  const long long acs = g.A.cells();
+  const long long acs = g.A.cells(), pcs = g.Ap.cells();
   T WM[NS], WP[NS];
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
@@ -143,9 +176,9 @@ __global__ void __launch_bounds__(128) pred_kernel(const __grid_constant__ Step3
     for (int m = 0; m < 5; ++m) {
       int ii = i, jj = j, kk = k;
       step<D>(ii, jj, kk, m - 2);
-      const long long o = in[m] ? g.A.at(ii, jj, kk) : 0;
+      const long long o = in[m] ? g.Ap.at(ii, jj, kk) : 0;
 #pragma unroll
-      for (int c = 0; c < NSIDE; ++c) w5[c][m] = in[m] ? (T)g.U[(11 * s + c) * acs + o] : T(0);
+      for (int c = 0; c < NSIDE; ++c) w5[c][m] = in[m] ? g.Up[(g.uside * s + c) * pcs + o] : T(0);
     }
     ppm_predict<D, T>(kc, (T)rvs<D>(s), w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM + NSIDE * s,
                       WP + NSIDE * s, P.order, P.fourth != 0);
@@ -180,12 +213,18 @@ TMK_D double bdry_value(const DevParams& P, const Step3<T>& g, int i, int k, con
   if (!U22) return P.fault_law == 1 ? Bi[10 * bs] : Bi[7 * bs];
   if (P.fault_law == 1) {
     const RSFace fr = rs_face(P, nullptr, 0, 0);
-    return rs_setbnd(P, fr, U22, Bi, (int)bs, dtp, (i + 0.5) * g.dx - P.rs_x0, 0.0, false);
+    const double x = (i + 0.5) * g.dx - P.rs_x0;
+    if constexpr (!kExact<T>) return rs_setbnd_k(P, rs_face_k(P, fr, x), U22, Bi, (int)bs, dtp, 0.0, false);
+    return rs_setbnd(P, fr, U22, Bi, (int)bs, dtp, x, 0.0, false);
   }
   return sw_setbnd(P, U22, Bi, (int)bs, dtp, 0.0, false);
 }
 
-// fault face (i, dom lo, k): 22-comp state Wg from the interior state Wi22
+// fault face (i, dom lo, k): 22-comp state Wg from the interior state Wi22.
+// The mixed form solves the rate-and-state friction equation with the
+// latency-arranged z-space Newton of the 2-D mixed form (rs_fault_k): the
+// 3-D law is the 2-D one (no antiplane characteristic, nucleation in x).
+template <typename T>
 TMK_D void fault_face(const DevParams& P, double dx, int i, int k, const double* Wi, double bval, double* Wg,
                       DevStatus* st) {
 #pragma unroll
@@ -193,7 +232,9 @@ TMK_D void fault_face(const DevParams& P, double dx, int i, int k, const double*
   const double xc = (i + 0.5) * dx;
   if (P.fault_law == 1) {
     const RSFace fr = rs_face(P, nullptr, 0, 0);
-    const int it = rs_fault(P, fr, Wi, bval, xc - P.rs_x0, Wg);
+    int it;
+    if constexpr (!kExact<T>) it = rs_fault_k(P, rs_face_k(P, fr, xc - P.rs_x0), Wi, bval, Wg);
+    else it = rs_fault(P, fr, Wi, bval, xc - P.rs_x0, Wg);
     if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
   } else {
     sw_fault<true>(P, Wi, bval, xc, Wg, (k + 0.5) * dx);
@@ -234,7 +275,7 @@ TMK_D void fault_solve(const DevParams& P, const Step3<T>& g, int i, int k, cons
   for (int c = 0; c < NSIDE; ++c) { Wi[c] = (double)R18[c]; Wi[11 + c] = (double)R18[NSIDE + c]; }
   Wi[9] = g.LG[fo]; Wi[10] = g.LG[fcs + fo];
   Wi[20] = 0.0; Wi[21] = 0.0;
-  fault_face(P, g.dx, i, k, Wi, bval, Wg, st);
+  fault_face<T>(P, g.dx, i, k, Wi, bval, Wg, st);
 #pragma unroll
   for (int c = 0; c < NSIDE; ++c) { G18[c] = (T)Wg[c]; G18[NSIDE + c] = (T)Wg[11 + c]; }
   if (FFk) {
@@ -259,9 +300,8 @@ __global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Step
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= fb.cells()) return;
   int i, j, k;
-  fb.cell(t, i, j, k);
-  Consts<T> kc;
-  kc.load(P);
+  face_at<D>(fb, g.fault != 0, t, i, j, k);
+  const Consts<T>& kc = g.kc;
   const int f = coord<D>(i, j, k);
   T L[NS], R[NS], G[NS];
   int li = i, lj = j, lk = k;
@@ -299,10 +339,9 @@ __global__ void __launch_bounds__(128) riem2_kernel(const __grid_constant__ Step
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= fb.cells()) return;
   int i, j, k;
-  fb.cell(t, i, j, k);
-  Consts<T> kc;
-  kc.load(P);
-  const T scale = (T)(-(1.0 / 3.0) * g.dt / g.dx);
+  face_at<D1>(fb, g.fault != 0, t, i, j, k);
+  const Consts<T>& kc = g.kc;
+  const T scale = g.scale3;
   const int f = coord<D1>(i, j, k);
   T L[NS], R[NS], G[NS];
   int li = i, lj = j, lk = k;
@@ -350,10 +389,9 @@ __global__ void __launch_bounds__(128) final_kernel(const __grid_constant__ Step
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= fb.cells()) return;
   int i, j, k;
-  fb.cell(t, i, j, k);
-  Consts<T> kc;
-  kc.load(P);
-  const T scale = (T)(-(1.0 / 2.0) * g.dt / g.dx);
+  face_at<D1>(fb, g.fault != 0, t, i, j, k);
+  const Consts<T>& kc = g.kc;
+  const T scale = g.scale2;
   const int f = coord<D1>(i, j, k);
   T L[NS], R[NS], G[NS];
   int li = i, lj = j, lk = k;
@@ -393,15 +431,14 @@ __global__ void __launch_bounds__(128) update_kernel(const __grid_constant__ Ste
   if (t >= g.cur.cells()) return;
   int i, j, k;
   g.cur.cell(t, i, j, k);
-  Consts<T> kc;
-  kc.load(P);
+  const Consts<T>& kc = g.kc;
   T dU[NS];
 #pragma unroll
   for (int c = 0; c < NS; ++c) dU[c] = T(0);
   flux_diff<0, T>(g, kc, i, j, k, dU);
   flux_diff<1, T>(g, kc, i, j, k, dU);
   flux_diff<2, T>(g, kc, i, j, k, dU);
-  const double sc = -g.dt / g.dx;
+  const double sc = g.sc;
   const long long acs = g.A.cells(), o = g.A.at(i, j, k);
 #pragma unroll
   for (int s = 0; s < 2; ++s)
@@ -422,8 +459,7 @@ __global__ void __launch_bounds__(128) flux_kernel(const __grid_constant__ Step3
   if (t >= fb.cells()) return;
   int i, j, k;
   fb.cell(t, i, j, k);
-  Consts<T> kc;
-  kc.load(P);
+  const Consts<T>& kc = g.kc;
   T w[NS], F[NS];
   load18(g.WH[D], fb, i, j, k, w);
 #pragma unroll
@@ -455,11 +491,28 @@ __global__ void __launch_bounds__(128) bdry_final_kernel(const __grid_constant__
   const int bs = (int)g.bb.cells();
   if (P.fault_law == 1) {
     const RSFace fr = rs_face(P, nullptr, 0, 0);
-    const double psi = rs_setbnd(P, fr, U22, Bi, bs, g.dt, (i + 0.5) * g.dx - P.rs_x0, g.time + g.dt, true);
+    const double x = (i + 0.5) * g.dx - P.rs_x0;
+    double psi;
+    if constexpr (!kExact<T>) psi = rs_setbnd_k(P, rs_face_k(P, fr, x), U22, Bi, bs, g.dt, g.time + g.dt, true);
+    else psi = rs_setbnd(P, fr, U22, Bi, bs, g.dt, x, g.time + g.dt, true);
     if (isnan(psi)) report(st, ST_NAN, bo);
   } else {
     sw_setbnd(P, U22, Bi, bs, g.dt, g.time + g.dt, true);
   }
+}
+
+// FP32 copy of the evolving components of U over Ap (mixed form)
+template <typename T>
+__global__ void __launch_bounds__(256) to_pred_kernel(const __grid_constant__ Step3<T> g, T* out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= g.Ap.cells()) return;
+  int i, j, k;
+  g.Ap.cell(t, i, j, k);
+  const long long acs = g.A.cells(), o = g.A.at(i, j, k), pcs = g.Ap.cells();
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int c = 0; c < NSIDE; ++c) out[(NSIDE * s + c) * pcs + t] = (T)g.U[(11 * s + c) * acs + o];
 }
 
 inline unsigned blocks(long long n) { return (unsigned)((n + 127) / 128); }
@@ -467,6 +520,8 @@ inline unsigned blocks(long long n) { return (unsigned)((n + 127) / 128); }
 // the whole step on stream s, in the reference's order
 template <typename T>
 cudaError_t launch_step(const Step3<T>& g, const DevParams* P, DevStatus* st, cudaStream_t s) {
+  if (g.Up != (const T*)(const void*)g.U)
+    to_pred_kernel<T><<<(unsigned)((g.Ap.cells() + 255) / 256), 256, 0, s>>>(g, const_cast<T*>(g.Up));
   const unsigned bS = blocks(g.S.cells());
   pred_kernel<0, T><<<bS, 128, 0, s>>>(g, P);
   pred_kernel<1, T><<<bS, 128, 0, s>>>(g, P);

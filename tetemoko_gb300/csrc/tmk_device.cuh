@@ -63,7 +63,7 @@ struct Consts {
   T inv_rho, inv_Zp, inv_Zs, ratio;       // ratio = lam/(2G+lam)
   T half_inv_Zp, half_inv_Zs, lamp2G;     // lamp2G = lam + 2G
   T cs, cp;
-  TMK_D void load(const DevParams& p) {
+  TMK_HD void load(const DevParams& p) {
     lam = (T)p.lam; G = (T)p.G; rho = (T)p.rho; Zp = (T)p.Zp; Zs = (T)p.Zs;
     lam2G = (T)(2.0 * p.G + p.lam);
     lamp2G = (T)(p.lam + 2.0 * p.G);
