@@ -3,6 +3,7 @@
 // rounds as in the reference's Fortran and the CPU oracle.  The kernels are in
 // tmk_3d.cuh; the mixed form's instantiation is in tmk_3d_f32.cu.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -122,6 +123,12 @@ tmk_status step3(tmk_context* c, tmk::d3::Step3<T>& g, cudaStream_t s) {
   g.scale3 = (T)(-(1.0 / 3.0) * g.dt / g.dx);
   g.scale2 = (T)(-(1.0 / 2.0) * g.dt / g.dx);
   g.sc = -g.dt / g.dx;
+  g.fastpred = copy && c->hp.order == 2 && c->hp.prim_lim && !c->hp.char_lim;
+  for (int q = 0; q < tmk::NSIDE; ++q) {
+    const double sv = std::fabs((double)g.sig[q]);
+    g.trA[q] = (T)(0.5 * sv);
+    g.trB[q] = (T)(q < 3 ? 3.0 * (0.5 * sv - sv * sv / 3.0) : 1.5 * sv * (1.0 - (2.0 / 3.0) * sv));
+  }
   cudaError_t e;
   if constexpr (std::is_same<T, double>::value) e = launch_step_f64(g, c->dp, c->dstatus, s);
   else e = launch_step_f32(g, c->dp, c->dstatus, s);
