@@ -401,6 +401,113 @@ def ensemble_measurement(steps, warmup, stream, nscen=ENSEMBLE_SIZE, autotune=Tr
     return out
 
 
+THREE_D = (192, 96, 96)
+# algorithmic bytes per cell of the 3-D step: the 18 evolving FP64 components
+# of the state read and written once (lambda and gamma carry no flux)
+BYTES_PER_CELL_3D = 18 * 8 * 2
+
+
+def three_d_measurement(steps, warmup, stream, fp64_steps=3, cpu_seconds=5.0, size=THREE_D):
+    """One 192x96x96 patch of the rate-and-state workload in 3-D (a
+    CH_SPACEDIM == 3 build: the 3-D corner transport upwind step, the fault the
+    y-lo plane), stepped through tmk_patch_update_state_3d in the mixed form
+    and in the plain FP64 form; the oracle's 3-D step on a 24x12x12 patch for
+    the CPU rate.  Returns the JSON object of the measurement."""
+    import torch
+    import numpy as np
+    from tetemoko_gb300 import _capi as A, scenarios as S
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    nx, ny, nz = size
+    g = A.TMK_NGHOST
+    lo, hi = (0, 0, 0), (nx - 1, ny - 1, nz - 1)
+
+    def state(sc):
+        rng = np.random.default_rng(2024)
+        U = np.empty((22, nz + 2 * g, ny + 2 * g, nx + 2 * g))
+        U[:] = sc.background()[:, None, None, None]
+        U[[0, 11]] += 1e-3 * rng.standard_normal((2,) + U.shape[1:])
+        B1 = sc.initial_B(xlo=0, xhi=nx - 1)
+        B = np.ascontiguousarray(np.repeat(B1[:, None, :], nz + 2 * g, axis=1))
+        return U, B
+
+    out = {}
+    for prec, n in ((A.TMK_PREC_MIXED, steps), (A.TMK_PREC_FP64, fp64_steps)):
+        sc = S.rate_state(nx=nx, ny=ny, dx=0.1, precision=prec)
+        ctx = Context(sc)
+        pg = LinElastPatchGodunov3D(ctx, (lo, hi))
+        pg.set_current_box((lo, hi))
+        U0, B0 = state(sc)
+        Ud = torch.from_numpy(U0).cuda()
+        Bd = torch.from_numpy(B0).cuda()
+        dt = sc.dt() / 3 ** 0.5      # the 3-D CFL bound
+        t = 0.0
+        for _ in range(warmup):
+            pg.set_current_time(t)
+            pg.update_state(Ud, (-g, -g, -g), dt, B=Bd, blo=(-g, -g), stream=stream)
+            t += dt
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            pg.set_current_time(t)
+            pg.update_state(Ud, (-g, -g, -g), dt, B=Bd, blo=(-g, -g), stream=stream)
+            t += dt
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / n
+        out[prec] = {"value": nx * ny * nz / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": n,
+                     "finite": bool(torch.isfinite(Ud).all().item())}
+        ctx.close()
+    mixed, fp64 = out[A.TMK_PREC_MIXED], out[A.TMK_PREC_FP64]
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = BYTES_PER_CELL_3D * nx * ny * nz / (mixed["ms_per_step"] * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "patch_step_3d_mixed_192x96x96.traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("dram_bytes_per_step")
+        except Exception:
+            traffic = None
+    cpu = None
+    if cpu_seconds > 0:
+        import oracle as O
+        sc = S.rate_state(nx=24, ny=12, dx=0.1)
+        cn = (24, 12, 12)
+        U = np.empty((22, cn[2] + 2 * g, cn[1] + 2 * g, cn[0] + 2 * g))
+        U[:] = sc.background()[:, None, None, None]
+        B = np.ascontiguousarray(np.repeat(sc.initial_B(xlo=0, xhi=cn[0] - 1)[:, None, :], cn[2] + 2 * g, axis=1))
+        dt = sc.dt() / 3 ** 0.5
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < cpu_seconds or n == 0:
+            O.patch_update_state_3d(sc, U, (-g, -g, -g), (0, 0, 0), (cn[0] - 1, cn[1] - 1, cn[2] - 1), (0, 0, 0),
+                                    (cn[0] - 1, cn[1] - 1, cn[2] - 1), B, (-g, -g), sc.dx, n * dt, dt)
+            n += 1
+        el = time.perf_counter() - t0
+        cpu = {"value": cn[0] * cn[1] * cn[2] * n / el, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{n} oracle 3-D patch steps of a 24x12x12 patch (the same scenario), one thread"}
+    return {"workload": f"rate-and-state fault plane y=0, one {nx}x{ny}x{nz} patch, dx = 0.1 km, PPM + "
+                        "primitive limiting, dt = CFL 0.9/sqrt(3)",
+            "value": mixed["value"], "unit": UNIT, "ms_per_step": mixed["ms_per_step"], "steps": mixed["steps"],
+            "form": "mixed (FP32 volume arithmetic and intermediates, FP64 state, friction and boundary data)",
+            "fp64_plain": fp64, "mixed_over_fp64": mixed["value"] / fp64["value"],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic,
+                         "algorithmic_bytes_per_step": BYTES_PER_CELL_3D * nx * ny * nz,
+                         "kernel": "the whole 3-D step (19 launches: FP32 copy, 3 predictors, 3 + 6 + 3 face "
+                                   "passes, update, boundary data)",
+                         "timing": f"CUDA events on the launch stream around {mixed['steps']} steps"},
+            "cpu_baseline": cpu,
+            "finite": mixed["finite"] and fp64["finite"],
+            "execution": "one tmk_patch_update_state_3d call per step, device FABs"}
+
+
 def host_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -468,6 +575,9 @@ def main():
     ap.add_argument("--ensemble-only", action="store_true")
     ap.add_argument("--ensemble-max-grid", type=int, default=1024)  # largest patch side (1024: one patch per scenario)
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")   # keep the default tuning
+    ap.add_argument("--three-d-steps", type=int, default=20)   # timed steps of the 3-D measurement
+    ap.add_argument("--three-d-only", action="store_true")
+    ap.add_argument("--three-d-size", default="192x96x96")   # profiling runs use a smaller patch
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     args = ap.parse_args()
@@ -556,6 +666,12 @@ def main():
         amr = amr_measurement(args.amr_steps, args.warmup, stream, args.autotune)
         if rank == 0:
             print(json.dumps({"amr": amr}), flush=True)
+        return 0
+    if args.three_d_only:
+        td = three_d_measurement(args.three_d_steps, 3, stream, cpu_seconds=0.0,
+                                 size=tuple(int(v) for v in args.three_d_size.split("x")))
+        if rank == 0:
+            print(json.dumps({"three_d": td}), flush=True)
         return 0
     if args.ensemble_only:
         ens = ensemble_measurement(args.ensemble_steps, args.warmup, stream, autotune=args.autotune,
@@ -656,6 +772,10 @@ def main():
     ens = ensemble_measurement(args.ensemble_steps, 3, stream, autotune=args.autotune, max_grid=args.ensemble_max_grid) \
         if args.ensemble_steps > 0 else None
 
+    # ---- the 3-D patch step
+    three_d = three_d_measurement(args.three_d_steps, 3, stream, cpu_seconds=min(5.0, args.cpu_seconds)) \
+        if args.three_d_steps > 0 and rank == 0 else None
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and args.cpu_seconds > 0:
@@ -686,6 +806,7 @@ def main():
             "mixed_over_fp64": value / value64,
             "amr": amr,
             "ensemble": ens,
+            "three_d": three_d,
             "device_status": {"mixed": st[1], "fp64": st64[1]},
         }
         print(json.dumps(line), flush=True)
