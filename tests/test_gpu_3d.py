@@ -180,7 +180,7 @@ def test_bad_descriptors_are_refused(cuda_lib):
     ctx.close()
 
 
-MIXED = [n for n in ("rs_slip", "rs_aging", "sw_ref9", "sw_off11", "rs_plm2", "no_fault")]
+MIXED = [n for n in ("rs_slip", "rs_aging", "sw_ref9", "sw_off11", "sw_charlim", "rs_plm2", "rs_ctu", "no_fault")]
 
 
 @pytest.mark.parametrize("name", MIXED)

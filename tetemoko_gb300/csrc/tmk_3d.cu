@@ -86,11 +86,11 @@ tmk_status step3(tmk_context* c, tmk::d3::Step3<T>& g, cudaStream_t s) {
   constexpr bool copy = !std::is_same<T, double>::value;
   std::vector<size_t> sizes;
   for (int d = 0; d < 6; ++d) sizes.push_back(s18);
-  for (int d = 0; d < 3; ++d) sizes.push_back((size_t)NS * g.fl1[d].cells() * sizeof(T));
+  for (int d = 0; d < 3; ++d) sizes.push_back((size_t)NF * g.fl1[d].cells() * sizeof(T));
   for (int d1 = 0; d1 < 3; ++d1)
     for (int d2 = 0; d2 < 3; ++d2)
-      if (d1 != d2) sizes.push_back((size_t)NS * g.fl1[d1].cells() * sizeof(T));
-  for (int d = 0; d < 3; ++d) sizes.push_back((size_t)NS * g.flF[d].cells() * sizeof(T));
+      if (d1 != d2) sizes.push_back((size_t)NF * g.fl1[d1].cells() * sizeof(T));
+  for (int d = 0; d < 3; ++d) sizes.push_back((size_t)NF * g.flF[d].cells() * sizeof(T));
   sizes.push_back(2 * (size_t)g.fplane.cells() * sizeof(double));
   for (int k = 0; k < 3; ++k) sizes.push_back((size_t)TMK_NCOMP * g.fplane.cells() * sizeof(double));
   sizes.push_back(copy ? (size_t)NS * g.Ap.cells() * sizeof(T) : 0);

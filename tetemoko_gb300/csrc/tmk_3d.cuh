@@ -15,6 +15,8 @@
 //                WHalf2[D2][D3] with -(1/2) dt/dx (:422-440)
 //   update       fluxes, their divergence and U += -dt/dx dU in place; then
 //                the fault's boundary data (RSSETBND / SWSETBND, final)
+// Cell states (WM, WP) are stored with 18 components, face states with the 12
+// that the transverse terms and the fluxes read.
 // The fault is the y-lo plane of the domain.  Its boundary data predicted at
 // (1/3) dt from WHalf1[1] and at (1/2) dt from WHalf2[1][2] (the reference's
 // call order leaves those in m_tmpBdryData when WHalf2[1][*] and WHalf[1] are
@@ -107,6 +109,34 @@ TMK_D void store18(T* a, const Bx& b, int i, int j, int k, const T* q) {
 #pragma unroll
   for (int c = 0; c < NS; ++c) a[c * cs + o] = q[c];
 }
+// Face states are stored with the components the transverse term (adwdx_add)
+// and the flux read: the rotated cx, cy, cz, cx+3, cxy, cxz of each side (12 of
+// 18).  The Riemann solves read cell states only; fault faces keep all 22
+// components in FF.
+constexpr int NF = 12;
+template <int D> TMK_D constexpr int face_comp(int m) {
+  using R = Rot<D>;
+  return m == 0 ? R::cx : m == 1 ? R::cy : m == 2 ? R::cz : m == 3 ? R::cx + 3 : m == 4 ? R::cxy : R::cxz;
+}
+template <int D, typename T>
+TMK_D void store_face(T* a, const Bx& b, int i, int j, int k, const T* q) {
+  const long long cs = b.cells(), o = b.at(i, j, k);
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int m = 0; m < 6; ++m) a[(6 * s + m) * cs + o] = q[NSIDE * s + face_comp<D>(m)];
+}
+template <int D, typename T>
+TMK_D void load_face(const T* a, const Bx& b, int i, int j, int k, T* q) {
+  const long long cs = b.cells(), o = b.at(i, j, k);
+#pragma unroll
+  for (int c = 0; c < NS; ++c) q[c] = T(0);
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int m = 0; m < 6; ++m) q[NSIDE * s + face_comp<D>(m)] = a[(6 * s + m) * cs + o];
+}
+
 template <int D> TMK_D void step(int& i, int& j, int& k, int s) {
   if (D == 0) i += s; else if (D == 1) j += s; else k += s;
 }
@@ -368,7 +398,7 @@ __global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Step
   if (f <= g.dhi[D]) load18(g.WM[D], g.S, i, j, k, R);
   if (!face_state<D, T>(P, kc, g, f, L, R, G))
     fault_solve(P, g, i, k, R, bdry_value(P, g, i, k, nullptr, 0.0), g.FF[0], G, st);
-  store18(g.WH1[D], fb, i, j, k, G);
+  store_face<D>(g.WH1[D], fb, i, j, k, G);
 }
 
 // cell state T18 of array A (direction-D1 normal states) at (i, j, k), moved by
@@ -381,8 +411,8 @@ TMK_D void corrected(const Step3<T>& g, const Consts<T>& kc, const T* A, const T
   T h[NS], l[NS];
   int hi = i, hj = j, hk = k;
   step<D2>(hi, hj, hk, 1);
-  load18(H, hb, hi, hj, hk, h);
-  load18(H, hb, i, j, k, l);
+  load_face<D2>(H, hb, hi, hj, hk, h);
+  load_face<D2>(H, hb, i, j, k, l);
 #pragma unroll
   for (int s = 0; s < 2; ++s)
     adwdx_add<D2, T>(kc, (T)rvs<D2>(s), scale, h + NSIDE * s, l + NSIDE * s, T18 + NSIDE * s);
@@ -412,7 +442,7 @@ __global__ void __launch_bounds__(128) riem2_kernel(const __grid_constant__ Step
     const double bval = bdry_value(P, g, i, k, U22, (1.0 / 3.0) * g.dt);
     fault_solve(P, g, i, k, R, bval, (D2 == 2) ? g.FF[1] : nullptr, G, st);
   }
-  store18(g.WH2[D1][D2], fb, i, j, k, G);
+  store_face<D1>(g.WH2[D1][D2], fb, i, j, k, G);
 }
 
 // ------------------------------------------------------------ final pass
@@ -423,8 +453,8 @@ TMK_D void add_final(const Step3<T>& g, const Consts<T>& kc, T scale, int i, int
   T h[NS], l[NS];
   int hi = i, hj = j, hk = k;
   step<Dc>(hi, hj, hk, 1);
-  load18(g.WH2[Dc][D3], g.fl1[Dc], hi, hj, hk, h);
-  load18(g.WH2[Dc][D3], g.fl1[Dc], i, j, k, l);
+  load_face<Dc>(g.WH2[Dc][D3], g.fl1[Dc], hi, hj, hk, h);
+  load_face<Dc>(g.WH2[Dc][D3], g.fl1[Dc], i, j, k, l);
 #pragma unroll
   for (int s = 0; s < 2; ++s)
     adwdx_add<Dc, T>(kc, (T)rvs<Dc>(s), scale, h + NSIDE * s, l + NSIDE * s, T18 + NSIDE * s);
@@ -462,7 +492,7 @@ __global__ void __launch_bounds__(128) final_kernel(const __grid_constant__ Step
     const double bval = bdry_value(P, g, i, k, U22, (1.0 / 2.0) * g.dt);
     fault_solve(P, g, i, k, R, bval, g.FF[2], G, st);
   }
-  store18(g.WH[D1], fb, i, j, k, G);
+  store_face<D1>(g.WH[D1], fb, i, j, k, G);
 }
 
 // ---------------------------------------------------------------- update
@@ -471,8 +501,8 @@ TMK_D void flux_diff(const Step3<T>& g, const Consts<T>& kc, int i, int j, int k
   T h[NS], l[NS], Fh[NS], Fl[NS];
   int hi = i, hj = j, hk = k;
   step<D>(hi, hj, hk, 1);
-  load18(g.WH[D], g.flF[D], hi, hj, hk, h);
-  load18(g.WH[D], g.flF[D], i, j, k, l);
+  load_face<D>(g.WH[D], g.flF[D], hi, hj, hk, h);
+  load_face<D>(g.WH[D], g.flF[D], i, j, k, l);
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     flux<D, T>(kc, (T)rvs<D>(s), h + NSIDE * s, Fh + NSIDE * s);
@@ -519,7 +549,7 @@ __global__ void __launch_bounds__(128) flux_kernel(const __grid_constant__ Step3
   fb.cell(t, i, j, k);
   const Consts<T>& kc = g.kc;
   T w[NS], F[NS];
-  load18(g.WH[D], fb, i, j, k, w);
+  load_face<D>(g.WH[D], fb, i, j, k, w);
 #pragma unroll
   for (int s = 0; s < 2; ++s) flux<D, T>(kc, (T)rvs<D>(s), w + NSIDE * s, F + NSIDE * s);
   const long long cs = fb.cells();
