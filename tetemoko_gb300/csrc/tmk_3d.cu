@@ -82,7 +82,7 @@ template <typename T>
 tmk_status step3(tmk_context* c, tmk::d3::Step3<T>& g, cudaStream_t s) {
   using namespace tmk::d3;
   // scratch: WM, WP (3 each) | WH1 (3) | WH2 (6) | WH (3) | LG | FF (3) | FP32 copy of U
-  const size_t s18 = (size_t)NS * g.S.cells() * sizeof(T);
+  const size_t s18 = (size_t)NF * g.S.cells() * sizeof(T);
   constexpr bool copy = !std::is_same<T, double>::value;
   std::vector<size_t> sizes;
   for (int d = 0; d < 6; ++d) sizes.push_back(s18);

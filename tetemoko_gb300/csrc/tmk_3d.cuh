@@ -97,22 +97,17 @@ struct Step3 {
 
 template <int D> TMK_HD double rvs(int s) { return (D == 1 && s == 1) ? -1.0 : 1.0; }
 
-template <typename T>
-TMK_D void load18(const T* a, const Bx& b, int i, int j, int k, T* q) {
-  const long long cs = b.cells(), o = b.at(i, j, k);
-#pragma unroll
-  for (int c = 0; c < NS; ++c) q[c] = a[c * cs + o];
-}
-template <typename T>
-TMK_D void store18(T* a, const Bx& b, int i, int j, int k, const T* q) {
-  const long long cs = b.cells(), o = b.at(i, j, k);
-#pragma unroll
-  for (int c = 0; c < NS; ++c) a[c * cs + o] = q[c];
-}
-// Face states are stored with the components the transverse term (adwdx_add)
-// and the flux read: the rotated cx, cy, cz, cx+3, cxy, cxz of each side (12 of
-// 18).  The Riemann solves read cell states only; fault faces keep all 22
-// components in FF.
+// States of direction D are stored with the components the transverse terms
+// (adwdx_add) and the fluxes read from its face states: the rotated cx, cy, cz,
+// cx+3, cxy, cxz of each side (12 of 18).  These face components come from the
+// same components of the cell states (RIEMANNF and the edge conditions form
+// them from the waves sxx -/+ Zp vx, sxy -/+ Zs vy, sxz -/+ Zs vz), and the
+// fault laws' outputs that anything reads (the face state's velocities, syy,
+// sxy, syz and the boundary data) depend on those components of the interior
+// state only; so the normal states WM/WP of direction D are stored with the
+// same 12 components, and the predictor's work for the other three (the
+// zero-speed waves wyy, wzz, wyz) is dropped by the compiler.  Fault faces keep
+// all 22 components of their states in FF.
 constexpr int NF = 12;
 template <int D> TMK_D constexpr int face_comp(int m) {
   using R = Rot<D>;
@@ -271,8 +266,8 @@ __global__ void __launch_bounds__(128) pred_kernel(const __grid_constant__ Step3
       ppm_predict<D, T>(kc, (T)rvs<D>(s), w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM + NSIDE * s,
                         WP + NSIDE * s, P.order, P.fourth != 0);
   }
-  store18(g.WM[D], g.S, i, j, k, WM);
-  store18(g.WP[D], g.S, i, j, k, WP);
+  store_face<D>(g.WM[D], g.S, i, j, k, WM);
+  store_face<D>(g.WP[D], g.S, i, j, k, WP);
   if (D == 1 && g.fault && j == g.dlo[1]) {
     // lambda and gamma of side 1 at the fault's lo faces (read by the
     // reference-layout slip-weakening law as side-2 velocities)
@@ -394,8 +389,8 @@ __global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Step
   T L[NS], R[NS], G[NS];
   int li = i, lj = j, lk = k;
   step<D>(li, lj, lk, -1);
-  if (f > g.dlo[D]) load18(g.WP[D], g.S, li, lj, lk, L);
-  if (f <= g.dhi[D]) load18(g.WM[D], g.S, i, j, k, R);
+  if (f > g.dlo[D]) load_face<D>(g.WP[D], g.S, li, lj, lk, L);
+  if (f <= g.dhi[D]) load_face<D>(g.WM[D], g.S, i, j, k, R);
   if (!face_state<D, T>(P, kc, g, f, L, R, G))
     fault_solve(P, g, i, k, R, bdry_value(P, g, i, k, nullptr, 0.0), g.FF[0], G, st);
   store_face<D>(g.WH1[D], fb, i, j, k, G);
@@ -403,10 +398,10 @@ __global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Step
 
 // cell state T18 of array A (direction-D1 normal states) at (i, j, k), moved by
 // -(scale) A dW/dx of the face states H in direction D2 where the cell lies in ccBox[D2]
-template <int D2, typename T>
+template <int D1, int D2, typename T>
 TMK_D void corrected(const Step3<T>& g, const Consts<T>& kc, const T* A, const T* H, const Bx& hb, T scale, int i,
                      int j, int k, T* T18) {
-  load18(A, g.S, i, j, k, T18);
+  load_face<D1>(A, g.S, i, j, k, T18);
   if (!g.cc[D2].has(i, j, k)) return;
   T h[NS], l[NS];
   int hi = i, hj = j, hk = k;
@@ -434,8 +429,8 @@ __global__ void __launch_bounds__(128) riem2_kernel(const __grid_constant__ Step
   T L[NS], R[NS], G[NS];
   int li = i, lj = j, lk = k;
   step<D1>(li, lj, lk, -1);
-  if (f > g.dlo[D1]) corrected<D2, T>(g, kc, g.WP[D1], g.WH1[D2], g.fl1[D2], scale, li, lj, lk, L);
-  if (f <= g.dhi[D1]) corrected<D2, T>(g, kc, g.WM[D1], g.WH1[D2], g.fl1[D2], scale, i, j, k, R);
+  if (f > g.dlo[D1]) corrected<D1, D2, T>(g, kc, g.WP[D1], g.WH1[D2], g.fl1[D2], scale, li, lj, lk, L);
+  if (f <= g.dhi[D1]) corrected<D1, D2, T>(g, kc, g.WM[D1], g.WH1[D2], g.fl1[D2], scale, i, j, k, R);
   if (!face_state<D1, T>(P, kc, g, f, L, R, G)) {
     double U22[NC];
     load_ff(g, g.FF[0], i, k, U22);
@@ -464,7 +459,7 @@ template <int D1, typename T>
 TMK_D void final_state(const Step3<T>& g, const Consts<T>& kc, const T* A, T scale, int i, int j, int k, T* T18) {
   constexpr int Da = (D1 == 0) ? 1 : 0;      // the two other directions, ascending
   constexpr int Db = (D1 == 2) ? 1 : 2;
-  load18(A, g.S, i, j, k, T18);
+  load_face<D1>(A, g.S, i, j, k, T18);
   add_final<D1, Da, T>(g, kc, scale, i, j, k, T18);
   add_final<D1, Db, T>(g, kc, scale, i, j, k, T18);
 }
