@@ -13,8 +13,9 @@
 namespace tmk {
 namespace d3 {
 
-cudaError_t launch_step_f64(const Step3<double>& g, const DevParams* P, DevStatus* st, cudaStream_t s) {
-  return launch_step<double>(g, P, st, s);
+cudaError_t launch_step_f64(const Step3<double>& g, const DevParams* P, DevStatus* st, cudaStream_t s,
+                            const Side* side) {
+  return launch_step<double>(g, P, st, s, side);
 }
 
 __global__ void plastic3_kernel(double* U, Bx A, Bx box, const DevParams* P, double dt) {
@@ -116,8 +117,8 @@ tmk_status step3(tmk_context* c, tmk::d3::Step3<T>& g, cudaStream_t s) {
   g.LG = (double*)take();
   for (int k = 0; k < 3; ++k) g.FF[k] = (double*)take();
   T* up = (T*)take();
-  if constexpr (copy) { g.Up = up; g.uside = tmk::NSIDE; }
-  else { g.Up = (const T*)(const void*)g.U; g.Ap = g.A; g.uside = 11; }
+  if constexpr (copy) { g.Up = up; g.Uc = up; g.uside = tmk::NSIDE; }
+  else { g.Up = (const T*)(const void*)g.U; g.Uc = nullptr; g.Ap = g.A; g.uside = 11; }
   g.kc.load(c->hp);
   make_sig_host(c->hp, g.dt / g.dx, g.sig);
   g.scale3 = (T)(-(1.0 / 3.0) * g.dt / g.dx);
@@ -129,9 +130,22 @@ tmk_status step3(tmk_context* c, tmk::d3::Step3<T>& g, cudaStream_t s) {
     g.trA[q] = (T)(0.5 * sv);
     g.trB[q] = (T)(q < 3 ? 3.0 * (0.5 * sv - sv * sv / 3.0) : 1.5 * sv * (1.0 - (2.0 / 3.0) * sv));
   }
+  // the side stream and events of the overlapped schedule, made once per context
+  Side side;
+  if (g.fault) {
+    if (!c->side) {
+      cudaStream_t ss = nullptr;
+      if (cudaStreamCreateWithFlags(&ss, cudaStreamNonBlocking) != cudaSuccess) return TMK_ERR_CUDA;
+      c->side = ss;
+      for (int q = 0; q < 6; ++q)
+        if (cudaEventCreateWithFlags(&c->side_ev[q], cudaEventDisableTiming) != cudaSuccess) return TMK_ERR_CUDA;
+    }
+    side.s = c->side;
+    for (int q = 0; q < 6; ++q) side.ev[q] = c->side_ev[q];
+  }
   cudaError_t e;
-  if constexpr (std::is_same<T, double>::value) e = launch_step_f64(g, c->dp, c->dstatus, s);
-  else e = launch_step_f32(g, c->dp, c->dstatus, s);
+  if constexpr (std::is_same<T, double>::value) e = launch_step_f64(g, c->dp, c->dstatus, s, &side);
+  else e = launch_step_f32(g, c->dp, c->dstatus, s, &side);
   return e == cudaSuccess ? TMK_OK : TMK_ERR_CUDA;
 }
 

@@ -83,6 +83,7 @@ struct Step3 {
   // its FP32 copy over grow(valid, 3) & domain made once per step (mixed form;
   // side s at component 9 s), so that no predictor converts FP64 values
   const T* Up;
+  T* Uc;                // the FP32 copy (mixed form; Up == Uc), else null
   Bx Ap;
   int uside;
   Consts<T> kc;         // the physical constants in T (computed on the host)
@@ -159,6 +160,22 @@ TMK_D void face_fault_first(const Bx& fb, bool fault, long long t, int& i, int& 
 template <int D> TMK_D void face_at(const Bx& fb, bool fault, long long t, int& i, int& j, int& k) {
   if (D == 1) face_fault_first(fb, fault, t, i, j, k);
   else fb.cell(t, i, j, k);
+}
+
+// Which faces a launch of a face pass covers: all of them, the bulk (the
+// fault plane excluded) or the fault plane alone.  The fault plane's passes
+// run on a second stream beside the bulk (launch_step).
+enum : int { PART_ALL = 0, PART_BULK = 1, PART_FAULT = 2 };
+template <int D>
+TMK_HD long long part_faces(const Bx& fb, bool fault, int part) {
+  const long long nf = (D == 1 && fault) ? (long long)fb.n[0] * fb.n[2] : 0;
+  return part == PART_BULK ? fb.cells() - nf : part == PART_FAULT ? nf : fb.cells();
+}
+// face t of a launch covering `part` (t < part_faces)
+template <int D>
+TMK_D void part_face(const Bx& fb, bool fault, int part, long long t, int& i, int& j, int& k) {
+  if (D == 1 && fault && part == PART_BULK) t += (long long)fb.n[0] * fb.n[2];
+  face_at<D>(fb, fault, t, i, j, k);
 }
 
 // Predicted lo-face value of a zero-speed component (lambda or gamma) in the
@@ -377,13 +394,13 @@ TMK_D void load_ff(const Step3<T>& g, const double* FFk, int i, int k, double* U
 // ------------------------------------------------------------ first pass
 template <int D, typename T>
 __global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
-                                                    DevStatus* st) {
+                                                    DevStatus* st, int part) {
   const DevParams& P = *Pp;
   const Bx& fb = g.fl1[D];
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= fb.cells()) return;
+  if (t >= part_faces<D>(fb, g.fault != 0, part)) return;
   int i, j, k;
-  face_at<D>(fb, g.fault != 0, t, i, j, k);
+  part_face<D>(fb, g.fault != 0, part, t, i, j, k);
   const Consts<T>& kc = g.kc;
   const int f = coord<D>(i, j, k);
   T L[NS], R[NS], G[NS];
@@ -415,14 +432,11 @@ TMK_D void corrected(const Step3<T>& g, const Consts<T>& kc, const T* A, const T
 
 // ----------------------------------------------------------- second pass
 template <int D1, int D2, typename T>
-__global__ void __launch_bounds__(128) riem2_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
-                                                    DevStatus* st) {
-  const DevParams& P = *Pp;
+TMK_D void riem2_face(const Step3<T>& g, const DevParams& P, DevStatus* st, int part, long long t) {
   const Bx& fb = g.fl1[D1];
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= fb.cells()) return;
+  if (t >= part_faces<D1>(fb, g.fault != 0, part)) return;
   int i, j, k;
-  face_at<D1>(fb, g.fault != 0, t, i, j, k);
+  part_face<D1>(fb, g.fault != 0, part, t, i, j, k);
   const Consts<T>& kc = g.kc;
   const T scale = g.scale3;
   const int f = coord<D1>(i, j, k);
@@ -438,6 +452,22 @@ __global__ void __launch_bounds__(128) riem2_kernel(const __grid_constant__ Step
     fault_solve(P, g, i, k, R, bval, (D2 == 2) ? g.FF[1] : nullptr, G, st);
   }
   store_face<D1>(g.WH2[D1][D2], fb, i, j, k, G);
+}
+
+template <int D1, int D2, typename T>
+__global__ void __launch_bounds__(128) riem2_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
+                                                    DevStatus* st, int part) {
+  riem2_face<D1, D2, T>(g, *Pp, st, part, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+}
+
+// WHalf2[1][0] and WHalf2[1][2] on the fault plane in one launch (grid y = 0,
+// 1): the two friction solves of a face run side by side
+template <typename T>
+__global__ void __launch_bounds__(128) riem2_fault_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
+                                                          DevStatus* st) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (blockIdx.y == 0) riem2_face<1, 0, T>(g, *Pp, st, PART_FAULT, t);
+  else riem2_face<1, 2, T>(g, *Pp, st, PART_FAULT, t);
 }
 
 // ------------------------------------------------------------ final pass
@@ -466,13 +496,13 @@ TMK_D void final_state(const Step3<T>& g, const Consts<T>& kc, const T* A, T sca
 
 template <int D1, typename T>
 __global__ void __launch_bounds__(128) final_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
-                                                    DevStatus* st) {
+                                                    DevStatus* st, int part) {
   const DevParams& P = *Pp;
   const Bx& fb = g.flF[D1];
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= fb.cells()) return;
+  if (t >= part_faces<D1>(fb, g.fault != 0, part)) return;
   int i, j, k;
-  face_at<D1>(fb, g.fault != 0, t, i, j, k);
+  part_face<D1>(fb, g.fault != 0, part, t, i, j, k);
   const Consts<T>& kc = g.kc;
   const T scale = g.scale2;
   const int f = coord<D1>(i, j, k);
@@ -600,27 +630,74 @@ __global__ void __launch_bounds__(256) to_pred_kernel(const __grid_constant__ St
 
 inline unsigned blocks(long long n) { return (unsigned)((n + 127) / 128); }
 
-// the whole step on stream s, in the reference's order
+// Streams and events of the overlapped schedule (created with the context's
+// first 3-D step)
+struct Side {
+  cudaStream_t s = nullptr;
+  cudaEvent_t ev[6] = {};
+};
+
+// The whole step on stream s.  When the patch holds fault faces and a side
+// stream is given, the three passes over the fault plane (their friction
+// solves are chains of dependent FP64 operations) run on the side stream
+// beside the bulk passes, forked and joined with events:
+//   side: [pred<1>] F1 = riem1<1> fault | [riem1<0>, riem1<2>] F2 = riem2<1,0> and riem2<1,2> fault (one launch)
+//         | [riem2<0,2>, riem2<2,0>] F3 = final<1> fault
+//   main: pred x3, riem1<0>, riem1<2>, riem1<1> bulk, riem2<0,2>, riem2<2,0>, riem2<1,*> bulk,
+//         [F1] riem2<0,1>, riem2<2,1>, final<1> bulk, [F2] final<0>, final<2>, [F3] update
+// Each pass still reads exactly what the reference's order has written when
+// it runs; the passes on the two streams write disjoint faces.
 template <typename T>
-cudaError_t launch_step(const Step3<T>& g, const DevParams* P, DevStatus* st, cudaStream_t s) {
+cudaError_t launch_step(const Step3<T>& g, const DevParams* P, DevStatus* st, cudaStream_t s, const Side* side) {
   if (g.Up != (const T*)(const void*)g.U)
-    to_pred_kernel<T><<<(unsigned)((g.Ap.cells() + 255) / 256), 256, 0, s>>>(g, const_cast<T*>(g.Up));
+    to_pred_kernel<T><<<(unsigned)((g.Ap.cells() + 255) / 256), 256, 0, s>>>(g, g.Uc);
+  const bool split = g.fault && side && side->s;
+  const bool f = g.fault != 0;
+  const int bulk = split ? PART_BULK : PART_ALL;
+  cudaStream_t fs = split ? side->s : s;
+  auto fork = [&](int e) {
+    if (!split) return;
+    cudaEventRecord(side->ev[e], s);
+    cudaStreamWaitEvent(fs, side->ev[e], 0);
+  };
+  auto join = [&](int e) {
+    if (!split) return;
+    cudaStreamWaitEvent(s, side->ev[e], 0);
+  };
   const unsigned bS = blocks(g.S.cells());
   pred_kernel<0, T><<<bS, 128, 0, s>>>(g, P);
   pred_kernel<1, T><<<bS, 128, 0, s>>>(g, P);
+  fork(0);
+  if (split) {
+    riem1_kernel<1, T><<<blocks(part_faces<1>(g.fl1[1], f, PART_FAULT)), 128, 0, fs>>>(g, P, st, PART_FAULT);
+    cudaEventRecord(side->ev[3], fs);
+  }
   pred_kernel<2, T><<<bS, 128, 0, s>>>(g, P);
-  riem1_kernel<0, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st);
-  riem1_kernel<1, T><<<blocks(g.fl1[1].cells()), 128, 0, s>>>(g, P, st);
-  riem1_kernel<2, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st);
-  riem2_kernel<0, 1, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st);
-  riem2_kernel<0, 2, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st);
-  riem2_kernel<1, 0, T><<<blocks(g.fl1[1].cells()), 128, 0, s>>>(g, P, st);
-  riem2_kernel<1, 2, T><<<blocks(g.fl1[1].cells()), 128, 0, s>>>(g, P, st);
-  riem2_kernel<2, 0, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st);
-  riem2_kernel<2, 1, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st);
-  final_kernel<0, T><<<blocks(g.flF[0].cells()), 128, 0, s>>>(g, P, st);
-  final_kernel<1, T><<<blocks(g.flF[1].cells()), 128, 0, s>>>(g, P, st);
-  final_kernel<2, T><<<blocks(g.flF[2].cells()), 128, 0, s>>>(g, P, st);
+  riem1_kernel<0, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  riem1_kernel<2, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  fork(1);
+  if (split) {
+    riem2_fault_kernel<T><<<dim3(blocks(part_faces<1>(g.fl1[1], f, PART_FAULT)), 2), 128, 0, fs>>>(g, P, st);
+    cudaEventRecord(side->ev[4], fs);
+  }
+  riem1_kernel<1, T><<<blocks(part_faces<1>(g.fl1[1], f, bulk)), 128, 0, s>>>(g, P, st, bulk);
+  riem2_kernel<0, 2, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  riem2_kernel<2, 0, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  fork(2);
+  if (split) {
+    final_kernel<1, T><<<blocks(part_faces<1>(g.flF[1], f, PART_FAULT)), 128, 0, fs>>>(g, P, st, PART_FAULT);
+    cudaEventRecord(side->ev[5], fs);
+  }
+  riem2_kernel<1, 0, T><<<blocks(part_faces<1>(g.fl1[1], f, bulk)), 128, 0, s>>>(g, P, st, bulk);
+  riem2_kernel<1, 2, T><<<blocks(part_faces<1>(g.fl1[1], f, bulk)), 128, 0, s>>>(g, P, st, bulk);
+  join(3);
+  riem2_kernel<0, 1, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  riem2_kernel<2, 1, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  final_kernel<1, T><<<blocks(part_faces<1>(g.flF[1], f, bulk)), 128, 0, s>>>(g, P, st, bulk);
+  join(4);
+  final_kernel<0, T><<<blocks(g.flF[0].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  final_kernel<2, T><<<blocks(g.flF[2].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  join(5);
   if (g.F[0]) flux_kernel<0, T><<<blocks(g.flF[0].cells()), 128, 0, s>>>(g, P);
   if (g.F[1]) flux_kernel<1, T><<<blocks(g.flF[1].cells()), 128, 0, s>>>(g, P);
   if (g.F[2]) flux_kernel<2, T><<<blocks(g.flF[2].cells()), 128, 0, s>>>(g, P);
@@ -631,8 +708,10 @@ cudaError_t launch_step(const Step3<T>& g, const DevParams* P, DevStatus* st, cu
 
 // FP64 instantiation (tmk_3d.cu, built without FMA contraction) and the mixed
 // form (tmk_3d_f32.cu)
-cudaError_t launch_step_f64(const Step3<double>& g, const DevParams* P, DevStatus* st, cudaStream_t s);
-cudaError_t launch_step_f32(const Step3<float>& g, const DevParams* P, DevStatus* st, cudaStream_t s);
+cudaError_t launch_step_f64(const Step3<double>& g, const DevParams* P, DevStatus* st, cudaStream_t s,
+                            const Side* side);
+cudaError_t launch_step_f32(const Step3<float>& g, const DevParams* P, DevStatus* st, cudaStream_t s,
+                            const Side* side);
 
 }  // namespace d3
 }  // namespace tmk

@@ -5,8 +5,9 @@
 namespace tmk {
 namespace d3 {
 
-cudaError_t launch_step_f32(const Step3<float>& g, const DevParams* P, DevStatus* st, cudaStream_t s) {
-  return launch_step<float>(g, P, st, s);
+cudaError_t launch_step_f32(const Step3<float>& g, const DevParams* P, DevStatus* st, cudaStream_t s,
+                            const Side* side) {
+  return launch_step<float>(g, P, st, s, side);
 }
 
 }  // namespace d3

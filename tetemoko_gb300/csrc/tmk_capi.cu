@@ -110,6 +110,9 @@ extern "C" void tmk_context_destroy(tmk_context* c) {
   cudaFree(c->dp);
   cudaFree(c->dstatus);
   cudaFree(c->scratch);
+  for (cudaEvent_t e : c->side_ev)
+    if (e) cudaEventDestroy(e);
+  if (c->side) cudaStreamDestroy(c->side);
   delete c;
 }
 

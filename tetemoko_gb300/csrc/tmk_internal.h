@@ -64,6 +64,10 @@ struct tmk_context_s {
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
   tmk::DevStatus* dstatus = nullptr;
+  // second stream and events of the 3-D step's overlapped schedule (made by
+  // the first 3-D step of a patch with fault faces)
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_ev[6] = {};
 };
 
 struct tmk_level_s {
