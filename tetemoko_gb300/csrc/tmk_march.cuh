@@ -81,6 +81,20 @@ template <> struct Role<1, 0> { static constexpr bool hasP = false, hasZc = fals
 template <> struct Role<1, 1> { static constexpr bool hasP = false, hasZc = false, hasZf = true;
   static constexpr int vP = 0, sP = 0, vS = 0, sS = 2, zc0 = 0, zc1 = 0, zf = 1; };
 
+// Components of a group whose direction-D states feed no flux and no
+// transverse term: the zero-speed components of the direction (the normal
+// stresses tied to the P-wave stress, the uncoupled stress).  RIEMANNF, the
+// edge conditions, GETFLUXF and GETADWDXF read only the P and S wave pairs of
+// a face state, and those are formed from the wave pairs of the cell states
+// alone, so these components of the predicted states, of the face states and
+// of a transverse correction aimed at direction D are never read: the kernels
+// skip them (szz, for instance, is updated from the fluxes of the velocities
+// but feeds no face state in either direction).
+template <int G, int D> TMK_HD constexpr bool live(int c) {
+  using R = Role<G, D>;
+  return !((R::hasZc && (c == R::zc0 || c == R::zc1)) || (R::hasZf && c == R::zf));
+}
+
 // Packed constants of one direction.
 template <typename T>
 struct MK {
@@ -198,7 +212,8 @@ TMK_D void predict(const MK<T>& k, const typename PairOf<T>::P* w, typename Pair
   constexpr int N = Grp<G>::N;
   if (plim) {
 #pragma unroll
-    for (int c = 0; c < N; ++c) limit2(dm[c], dp[c]);
+    for (int c = 0; c < N; ++c)
+      if (live<G, D>(c)) limit2(dm[c], dp[c]);
   }
   // S wave pair
   {
@@ -215,17 +230,7 @@ TMK_D void predict(const MK<T>& k, const typename PairOf<T>::P* w, typename Pair
   if constexpr (R::hasP) {
     P nm = pfma(k.ZpE, dm[R::vP], dm[R::sP]), pm = pfma(k.nZpE, dm[R::vP], dm[R::sP]);
     P np = pfma(k.ZpE, dp[R::vP], dp[R::sP]), pp = pfma(k.nZpE, dp[R::vP], dp[R::sP]);
-    P z0m = dm[R::zc0], z0p = dp[R::zc0], z1m = dm[R::zc1], z1p = dp[R::zc1];
-    if (clim) {
-      limit2(nm, np); limit2(pm, pp);
-      P sPm = dm[R::sP], sPp = dp[R::sP];
-      z0m = pfma(k.nr, sPm, z0m); z0p = pfma(k.nr, sPp, z0p);
-      z1m = pfma(k.nr, sPm, z1m); z1p = pfma(k.nr, sPp, z1p);
-      limit2(z0m, z0p); limit2(z1m, z1p);
-    } else {
-      z0m = pfma(k.nr, dm[R::sP], z0m); z0p = pfma(k.nr, dp[R::sP], z0p);
-      z1m = pfma(k.nr, dm[R::sP], z1m); z1p = pfma(k.nr, dp[R::sP], z1p);
-    }
+    if (clim) { limit2(nm, np); limit2(pm, pp); }
     P nmt = pfma(k.aP, nm, pmul(k.bP, np));
     P ppt = pfma(k.aP, pp, pmul(k.bP, pm));
     P sPm = pmul(k.half, padd(nmt, pm)), sPp = pmul(k.half, padd(np, ppt));
@@ -233,17 +238,11 @@ TMK_D void predict(const MK<T>& k, const typename PairOf<T>::P* w, typename Pair
     WM[R::vP] = padd(w[R::vP], pmul(k.hZpE, psub(nmt, pm)));
     WP[R::sP] = padd(w[R::sP], sPp);
     WP[R::vP] = padd(w[R::vP], pmul(k.hZpE, psub(np, ppt)));
-    WM[R::zc0] = padd(w[R::zc0], pfma(k.r, sPm, z0m));
-    WP[R::zc0] = padd(w[R::zc0], pfma(k.r, sPp, z0p));
-    WM[R::zc1] = padd(w[R::zc1], pfma(k.r, sPm, z1m));
-    WP[R::zc1] = padd(w[R::zc1], pfma(k.r, sPp, z1p));
   }
-  if constexpr (R::hasZf) {
-    P zm = dm[R::zf], zp = dp[R::zf];
-    if (clim) limit2(zm, zp);
-    WM[R::zf] = padd(w[R::zf], zm);
-    WP[R::zf] = padd(w[R::zf], zp);
-  }
+  // the zero-speed components of direction D are not read (live<G, D>)
+#pragma unroll
+  for (int c = 0; c < Grp<G>::N; ++c)
+    if (!live<G, D>(c)) { WM[c] = mk2(T(0), T(0)); WP[c] = mk2(T(0), T(0)); }
 }
 
 // RIEMANNF for a group: L = state left of the face, Rt = right
@@ -264,12 +263,11 @@ TMK_D void riem(const MK<T>& k, const typename PairOf<T>::P* L, const typename P
     P s = pmul(k.half, padd(wneg, wpos));
     g[R::sP] = s;
     g[R::vP] = pmul(k.hZpE, psub(wneg, wpos));
-    P zr0 = pfma(k.nr, Rt[R::sP], Rt[R::zc0]), zl0 = pfma(k.nr, L[R::sP], L[R::zc0]);
-    P zr1 = pfma(k.nr, Rt[R::sP], Rt[R::zc1]), zl1 = pfma(k.nr, L[R::sP], L[R::zc1]);
-    g[R::zc0] = pfma(k.r, s, pmul(k.half, padd(zr0, zl0)));
-    g[R::zc1] = pfma(k.r, s, pmul(k.half, padd(zr1, zl1)));
   }
-  if constexpr (R::hasZf) g[R::zf] = pmul(k.half, padd(Rt[R::zf], L[R::zf]));
+  // zero-speed components of the face state: not read (live<G, D>)
+#pragma unroll
+  for (int c = 0; c < Grp<G>::N; ++c)
+    if (!live<G, D>(c)) g[c] = mk2(decltype(L[0].x)(0), decltype(L[0].x)(0));
 }
 
 // Background state of a group, read from the launch constants by group index.
@@ -310,11 +308,11 @@ TMK_D void edge2(const MK<T>& k, bool lo, bool outflow, const typename PairOf<T>
     P s = pmul(k.half, padd(wneg, wpos));
     g[R::sP] = s;
     g[R::vP] = pmul(k.hZpE, psub(wneg, wpos));
-    P shf = pmul(k.nr, psub(Wi[R::vP], s));
-    g[R::zc0] = padd(Wi[R::zc0], shf);
-    g[R::zc1] = padd(Wi[R::zc1], shf);
   }
-  if constexpr (R::hasZf) g[R::zf] = Wi[R::zf];
+  // zero-speed components (the reference's SHF terms): not read (live<G, D>)
+#pragma unroll
+  for (int c = 0; c < Grp<G>::N; ++c)
+    if (!live<G, D>(c)) g[c] = mk2(T(0), T(0));
 }
 
 // GETFLUXF for a group
@@ -350,9 +348,11 @@ TMK_D void adw2(const MK<T>& k, const typename PairOf<T>::P* h, const typename P
     P dv = psub(h[R::vP], l[R::vP]);
     P b = pmul(k.a_l2g, dv);
     q1[R::sP] = padd(q1[R::sP], b); q2[R::sP] = padd(q2[R::sP], b);
+    // the targets are states of the other direction: their components that
+    // are zero-speed there are not read
     P c = pmul(k.a_lam, dv);
-    q1[R::zc0] = padd(q1[R::zc0], c); q2[R::zc0] = padd(q2[R::zc0], c);
-    q1[R::zc1] = padd(q1[R::zc1], c); q2[R::zc1] = padd(q2[R::zc1], c);
+    if constexpr (live<G, 1 - D>(R::zc0)) { q1[R::zc0] = padd(q1[R::zc0], c); q2[R::zc0] = padd(q2[R::zc0], c); }
+    if constexpr (live<G, 1 - D>(R::zc1)) { q1[R::zc1] = padd(q1[R::zc1], c); q2[R::zc1] = padd(q2[R::zc1], c); }
   }
 }
 
@@ -503,6 +503,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
       P dm[N], dp[N];
 #pragma unroll
       for (int c = 0; c < N; ++c) {
+        if (!live<G, 0>(c)) { dm[c] = mk2(T(0), T(0)); dp[c] = dm[c]; continue; }
         P wl = shfl_up2(w[c], 1), wr = shfl_dn2(w[c], 1);
         P s = slope2(wl, w[c], wr, inL, inR, lim);
         P sl = shfl_up2(s, 1);
@@ -519,12 +520,12 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
     }
     P L[N];
 #pragma unroll
-    for (int c = 0; c < N; ++c) L[c] = shfl_up2(WP[c], 1);
+    for (int c = 0; c < N; ++c) L[c] = live<G, 0>(c) ? shfl_up2(WP[c], 1) : mk2(T(0), T(0));
     if (x == dlo0) edge2<G, 0, T>(kx, true, xout_lo, WM, bg, H1lo);
     else if (x == dhi0 + 1) edge2<G, 0, T>(kx, false, xout_hi, L, bg, H1lo);
     else riem<G, 0, T>(kx, L, WM, H1lo);
 #pragma unroll
-    for (int c = 0; c < N; ++c) H1hi[c] = shfl_dn2(H1lo[c], 1);
+    for (int c = 0; c < N; ++c) H1hi[c] = live<G, 0>(c) ? shfl_dn2(H1lo[c], 1) : mk2(T(0), T(0));
   };
 
   const int q_s = max(it.y0 - 1, dlo1);
@@ -547,6 +548,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
     const bool hl = q_s - 1 >= dlo1, hr = q_s + 1 <= dhi1;
 #pragma unroll
     for (int c = 0; c < N; ++c) {
+      if (!live<G, 1>(c)) { sy0[c] = mk2(T(0), T(0)); Fy0[c] = sy0[c]; continue; }
       sy0[c] = slope2(Wb[c], W0[c], W1[c], hl, hr, lim);
       if (hl) {
         P sm = slope2(Wa[c], Wb[c], W0[c], q_s - 2 >= dlo1, true, lim);
@@ -560,15 +562,20 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
   // q-1 (WMx, WPx), the first-pass face q-1 (H1y) and the final flux q-1 (Fy)
   // in this lane's own shared-memory slots (vector v, component c)
   P WPy_p[N], WPcy_p[N];
+  enum { kWMx = 0, kWPx = 1, kH1y = 2, kFy = 3, kWold = 4 };
+  // components a carried vector needs: x states and y faces only their live ones
+  auto needed = [&](int v, int c) {
+    return (v == kWMx || v == kWPx) ? live<G, 0>(c) : v == kH1y ? live<G, 1>(c) : true;
+  };
   auto cput = [&](int v, const P* a) {
 #pragma unroll
-    for (int c = 0; c < N; ++c) carry[(v * N + c) * 32 + lane] = a[c];
+    for (int c = 0; c < N; ++c)
+      if (needed(v, c)) carry[(v * N + c) * 32 + lane] = a[c];
   };
   auto cget = [&](int v, P* a) {
 #pragma unroll
-    for (int c = 0; c < N; ++c) a[c] = carry[(v * N + c) * 32 + lane];
+    for (int c = 0; c < N; ++c) a[c] = needed(v, c) ? carry[(v * N + c) * 32 + lane] : mk2(T(0), T(0));
   };
-  enum { kWMx = 0, kWPx = 1, kH1y = 2, kFy = 3, kWold = 4 };
 
   for (int q = q_s; q <= q_e; ++q) {
     const bool rowin = q <= dhi1;
@@ -587,6 +594,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
         P dm[N], dp[N];
 #pragma unroll
         for (int c = 0; c < N; ++c) {
+          if (!live<G, 1>(c)) { sy1[c] = mk2(T(0), T(0)); Fy1[c] = sy1[c]; dm[c] = sy1[c]; dp[c] = sy1[c]; continue; }
           sy1[c] = slope2(W0[c], W1[c], W2[c], hl, hr, lim);
           Fy1[c] = (q + 1 <= dhi1) ? face2<T>(W0[c], W1[c], sy0[c], sy1[c])
                                    : pfma(mk2(T(0.5), T(0.5)), sy0[c], W0[c]);
@@ -664,7 +672,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
       }
       P L[N], g[N], Fx[N], Fxh[N];
 #pragma unroll
-      for (int c = 0; c < N; ++c) L[c] = shfl_up2(WPcx[c], 1);
+      for (int c = 0; c < N; ++c) L[c] = live<G, 0>(c) ? shfl_up2(WPcx[c], 1) : mk2(T(0), T(0));
       if (x == dlo0) edge2<G, 0, T>(kx, true, xout_lo, WMcx, bg, g);
       else if (x == dhi0 + 1) edge2<G, 0, T>(kx, false, xout_hi, L, bg, g);
       else riem<G, 0, T>(kx, L, WMcx, g);
@@ -737,7 +745,7 @@ TMK_D void fault_row_finish(const PatchDev<T>& pp, const MarchItem& it, const Ma
   const BgView<G, P> bg{mc.bg};
   P L[N], g[N], Fx[N], Fxh[N];
 #pragma unroll
-  for (int c = 0; c < N; ++c) L[c] = shfl_up2(WPcx[c], 1);
+  for (int c = 0; c < N; ++c) L[c] = live<G, 0>(c) ? shfl_up2(WPcx[c], 1) : mk2(T(0), T(0));
   if (x == dlo0) edge2<G, 0, T>(mc.kx, true, mc.xout_lo != 0, WMcx, bg, g);
   else if (x == dhi0 + 1) edge2<G, 0, T>(mc.kx, false, mc.xout_hi != 0, L, bg, g);
   else riem<G, 0, T>(mc.kx, L, WMcx, g);
