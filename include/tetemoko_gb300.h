@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TMK_ABI_VERSION 2   /* 2: tmk_scheme gained use_fourth_order_slopes */
+#define TMK_ABI_VERSION 3   /* 2: tmk_scheme gained use_fourth_order_slopes; 3: tmk_tuning gained fault_first */
 
 #define TMK_NCOMP      22   /* state components, srcLinElast/LEINDEX.H:12-47 */
 #define TMK_NSIDE_COMP 11   /* IX_OFFSET, srcLinElast/LEINDEX.H:23 */
@@ -136,13 +136,17 @@ typedef struct { int lo[2], hi[2]; } tmk_box;   /* cell-centred, inclusive */
 /* How a level's step is cut into work (an extension: the reference's patch
  * loop has no such choices).  Defaults: the scheme's volume kernel, one wave
  * per marching group, runs of at least 16 rows, one antiplane slot per
- * fault-kernel CTA, 32 fault faces per fault-kernel CTA. */
+ * fault-kernel CTA, 32 fault faces per fault-kernel CTA, the fault kernel
+ * after the in-plane marching kernel. */
 typedef struct {
   int volume_kernel;    /* TMK_VOLUME_MARCH or TMK_VOLUME_TILE (march only if the scheme allows it) */
   int march_waves[2];   /* marching items of the in-plane / antiplane group, in waves of resident CTAs: 1..8 */
   int min_run;          /* fewest rows of a marching item: 4..4096 */
   int fault_displace;   /* antiplane CTA slots left free per fault-kernel CTA: 0..4 */
   int fault_seg;        /* fault faces per fault-kernel CTA: 32 (4 warps) or 16 (2 warps) */
+  int fault_first;      /* 1: the fault kernel first, running beside the in-plane marching kernel
+                           (2-warp CTAs fit in the registers two in-plane CTAs leave free);
+                           0: after it, beside the antiplane kernel */
 } tmk_tuning;
 
 /* Refinement tagging parameters (the comp.* keys of the input deck,

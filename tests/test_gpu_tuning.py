@@ -15,16 +15,17 @@ G = A.TMK_NGHOST
 BOXES = [(0, 0, 20, 9), (21, 0, 63, 9), (0, 10, 31, 31), (32, 10, 63, 31)]
 
 
-def _tuning(volume="march", waves=(1, 1), min_run=16, disp=1, seg=32):
+def _tuning(volume="march", waves=(1, 1), min_run=16, disp=1, seg=32, first=0):
     t = A.Tuning()
     t.volume_kernel = A.TMK_VOLUME_MARCH if volume == "march" else A.TMK_VOLUME_TILE
     t.march_waves[0], t.march_waves[1] = waves
-    t.min_run, t.fault_displace, t.fault_seg = min_run, disp, seg
+    t.min_run, t.fault_displace, t.fault_seg, t.fault_first = min_run, disp, seg, first
     return t
 
 
 VARIANTS = [dict(), dict(waves=(2, 1)), dict(waves=(1, 2), min_run=8), dict(min_run=32, disp=0),
-            dict(seg=16), dict(waves=(2, 2), min_run=8, disp=2, seg=16)]
+            dict(seg=16), dict(waves=(2, 2), min_run=8, disp=2, seg=16), dict(first=1, seg=16, disp=0),
+            dict(first=1, seg=32, waves=(2, 1))]
 
 
 def _run(sc, Ug, Bg, tuning, nsteps=6):
@@ -110,7 +111,7 @@ def test_tuning_is_refused_where_unsafe(cuda_lib):
     ctx = Context(sc)
     lvl = LinElastLevelGodunov(ctx, BOXES)
     lvl.set_level(sc.initial_U(), sc.initial_B())
-    for bad in (dict(waves=(0, 1)), dict(min_run=2), dict(disp=9), dict(seg=8)):
+    for bad in (dict(waves=(0, 1)), dict(min_run=2), dict(disp=9), dict(seg=8), dict(first=2)):
         with pytest.raises(A.TmkError):
             lvl.set_tuning(_tuning(**bad))
     g = lvl.graph(2, 0.0, sc.dt())

@@ -205,6 +205,7 @@ tmk_tuning default_tuning(int march_allowed) {
   t.min_run = kMinRun;
   t.fault_displace = kFaultDisplace;
   t.fault_seg = tmk::FAULT_SEG;
+  t.fault_first = 0;
   return t;
 }
 
@@ -214,6 +215,7 @@ bool tuning_ok(const tmk_level_s* L, const tmk_tuning& t) {
   for (int g = 0; g < 2; ++g)
     if (t.march_waves[g] < 1 || t.march_waves[g] > 8) return false;
   if (t.min_run < 4 || t.min_run > 4096 || t.fault_displace < 0 || t.fault_displace > 4) return false;
+  if (t.fault_first != 0 && t.fault_first != 1) return false;
   return t.fault_seg == tmk::FAULT_SEG || t.fault_seg == tmk::FAULT_SEG_SMALL;
 }
 
@@ -722,7 +724,10 @@ namespace {
 // the in-plane kernel, then the fault kernel (scheduled as in-plane CTAs
 // retire, reading only the step's input state), then the antiplane kernel
 // beside it, then row 0 of the fault patches, which alone needs the fault
-// results.  With per-launch timing the fault kernel runs first and alone.
+// results.  With the tuning's fault_first the fault kernel comes first and the
+// in-plane kernel is its programmatic dependent, so that the fault kernel's
+// CTAs run beside the in-plane ones.  With per-launch timing the fault kernel
+// runs first and alone.
 template <typename Real>
 tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEvent_t* ev, cudaStream_t s) {
   tmk_context* c = L->ctx;
@@ -746,6 +751,10 @@ tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEve
     TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false, L->tune.fault_seg, s));
     TMK_CU(cudaEventRecord(ev[2], s));
     TMK_CU(tmk::Launch<Real>::march(0, pd, L->ditems[0], L->nitems[0], mc, false, s));
+    TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, true, s));
+  } else if (L->tune.fault_first && L->nfault) {
+    TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false, L->tune.fault_seg, s));
+    TMK_CU(tmk::Launch<Real>::march(0, pd, L->ditems[0], L->nitems[0], mc, true, s));
     TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, true, s));
   } else {
     TMK_CU(tmk::Launch<Real>::march(0, pd, L->ditems[0], L->nitems[0], mc, false, s));
@@ -879,8 +888,9 @@ tmk_status time_steps(tmk_level_s* L, double time, double dt, int steps, cudaStr
 }  // namespace
 
 // Candidate tunings of a level for the autotuners: every combination of the
-// marching choices (waves per group, shortest run, fault displacement) and
-// both fault-kernel variants, plus the tile kernel; `reduced` leaves out the
+// marching choices (waves per group, shortest run, fault displacement, the
+// fault kernel's place in the step) and both fault-kernel variants, plus the
+// tile kernel; `reduced` leaves out the
 // shortest runs of 8 rows (the hierarchy autotuner times whole coarse steps).
 std::vector<tmk_tuning> tmk_host::tuning_candidates(const tmk_level_s* L, bool reduced) {
   std::vector<tmk_tuning> out;
@@ -893,10 +903,13 @@ std::vector<tmk_tuning> tmk_host::tuning_candidates(const tmk_level_s* L, bool r
         for (int w1 : {1, 2})
           for (int run : {8, 16, 32}) {
             if (reduced && run == 8) continue;
-            for (int disp : {0, 1, 2}) {
-              t.march_waves[0] = w0; t.march_waves[1] = w1; t.min_run = run; t.fault_displace = disp;
-              out.push_back(t);
-            }
+            for (int disp : {0, 1, 2})
+              for (int first : {0, 1}) {
+                if (first && disp == 2) continue;
+                t.march_waves[0] = w0; t.march_waves[1] = w1; t.min_run = run; t.fault_displace = disp;
+                t.fault_first = first;
+                out.push_back(t);
+              }
           }
     }
     tmk_tuning tt = default_tuning(L->march_allowed);
