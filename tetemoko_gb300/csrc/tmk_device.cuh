@@ -82,6 +82,15 @@ template <> struct Rot<0> { static constexpr int cx = 0, cy = 1, cz = 2, cxy = 6
 template <> struct Rot<1> { static constexpr int cx = 1, cy = 2, cz = 0, cxy = 8, cxz = 6, cyz = 7; };
 template <> struct Rot<2> { static constexpr int cx = 2, cy = 0, cz = 1, cxy = 7, cxz = 8, cyz = 6; };
 
+// Components of one side's state in direction D that a face state's flux and
+// transverse term never read: the zero-speed ones (cy+3, cz+3, cyz).  RIEMANNF
+// and the edge conditions form the components the fluxes read (cx, cy, cz,
+// cx+3, cxy, cxz) from the same components of the states they are given.
+template <int D> TMK_HD constexpr bool live9(int c) {
+  using R = Rot<D>;
+  return c != R::cy + 3 && c != R::cz + 3 && c != R::cyz;
+}
+
 // lambda-ratio product  s*lam/(2G+lam)
 template <typename T> TMK_D T lratio(const Consts<T>& k, T s) {
   if constexpr (kExact<T>) return s * k.lam / k.lam2G; else return s * k.ratio;

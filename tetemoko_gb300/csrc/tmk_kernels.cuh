@@ -79,7 +79,9 @@ TMK_D void fault_ypred_side(const PatchDev<Real>& p, const DevParams& P, const C
   T WM[NSIDE], WP[NSIDE];
   T rv = (s == 1) ? T(-1) : T(1);
   ppm_predict<1, T>(k, rv, w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM, WP, P.order, P.fourth != 0);
-  for (int c = 0; c < NSIDE; ++c) out11[c] = (double)WM[c];
+  // the zero-speed components of the y direction reach no face component that
+  // is read downstream (live9): not predicted
+  for (int c = 0; c < NSIDE; ++c) out11[c] = live9<1>(c) ? (double)WM[c] : 0.0;
   for (int c = 9; c < 11; ++c) {
     T w[5];
     for (int m = 0; m < 5; ++m) w[m] = in[m] ? (T)p.Uin[fab_idx(p, 11 * s + c, i, j0 - 2 + m)] : T(0);
@@ -194,7 +196,11 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
       if (c >= p.dlo0 && c <= p.dhi0 && c <= s1 + 1) {
         T WM[NSIDE], WP[NSIDE];
         fault_xpred_side(p, P, k, s, c, sig, WM, WP);
-        for (int q = 0; q < NSIDE; ++q) { xWM[s][ci][q] = WM[q]; xWP[s][ci][q] = WP[q]; }
+        // the x faces' zero-speed components are never read (live9): not predicted
+        for (int q = 0; q < NSIDE; ++q) {
+          xWM[s][ci][q] = live9<0>(q) ? WM[q] : T(0);
+          xWP[s][ci][q] = live9<0>(q) ? WP[q] : T(0);
+        }
       }
     } else if (c >= fa && c <= fb) {
       fault_ypred_side(p, P, k, s, c, sig, lim, &sWi[ci][11 * s]);
