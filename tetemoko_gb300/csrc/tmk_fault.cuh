@@ -325,6 +325,19 @@ TMK_D double rs_setbnd_k(const DevParams& P, const RSFaceK& fk, const double* U,
   return dPsi;
 }
 
+// Out-of-line copies of the mixed-form solve and boundary update for a kernel
+// that calls each twice (first pass and final): one copy of their code instead
+// of one per call site.  The fault kernel runs few warps per SM along long
+// chains of dependent FP64 operations, where instruction fetch stalls show.
+static __device__ __noinline__ int rs_fault_k_ool(const DevParams& P, const RSFaceK& fk, const double* Wi,
+                                                  double psi, double* Wg) {
+  return rs_fault_k(P, fk, Wi, psi, Wg);
+}
+static __device__ __noinline__ double rs_setbnd_k_ool(const DevParams& P, const RSFaceK& fk, const double* U,
+                                                      double* B, int bstride, double dt, double time, bool final_) {
+  return rs_setbnd_k(P, fk, U, B, bstride, dt, time, final_);
+}
+
 // SWFAULTBCF (ibcLinElast/SWIBCF.ChF:79-267) at one fault face.  Side 2 is read
 // and written at component offset P.sw_off (9 as in the reference source).
 // Components the law does not write keep the values already in Wg.  Z3 (the

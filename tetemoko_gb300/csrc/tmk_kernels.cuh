@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
       int it = 0;
       const RSFace fr = rs_face(P, p.fric, i - p.blo0, bs);
       if (P.fault_law == 1) {
-        if constexpr (kZSolve) it = rs_fault_k(P, sFk[tid], sWi[tid], Bi[10 * bs], Wg);
+        if constexpr (kZSolve) it = rs_fault_k_ool(P, sFk[tid], sWi[tid], Bi[10 * bs], Wg);
         else it = rs_fault(P, fr, sWi[tid], Bi[10 * bs], xc - P.rs_x0, Wg);
       } else {
         sw_fault(P, sWi[tid], Bi[7 * bs], xc, Wg);
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
       for (int c = 0; c < NC; ++c) first[c * p.nfirst] = Wg[c];
       if (i >= s0 && i <= s1) {
         if (P.fault_law == 1) {
-          if constexpr (kZSolve) sTmp[tid] = rs_setbnd_k(P, sFk[tid], Wg, Bi, bs, 0.5 * dt, 0.0, false);
+          if constexpr (kZSolve) sTmp[tid] = rs_setbnd_k_ool(P, sFk[tid], Wg, Bi, bs, 0.5 * dt, 0.0, false);
           else sTmp[tid] = rs_setbnd(P, fr, Wg, Bi, bs, 0.5 * dt, xc - P.rs_x0, 0.0, false);
         } else {
           sTmp[tid] = sw_setbnd(P, Wg, Bi, bs, 0.5 * dt, 0.0, false);
@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
     int it = 0;
     const RSFace fr = rs_face(P, p.fric, i - p.blo0, bs);
     if (P.fault_law == 1) {
-      if constexpr (kZSolve) it = rs_fault_k(P, sFk[ci], Wi, sTmp[ci], Wg);
+      if constexpr (kZSolve) it = rs_fault_k_ool(P, sFk[ci], Wi, sTmp[ci], Wg);
       else it = rs_fault(P, fr, Wi, sTmp[ci], xc - P.rs_x0, Wg);
     } else {
       sw_fault(P, Wi, sTmp[ci], xc, Wg);
@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
     // (G) boundary-data update with the final fault state (final=true, t+dt)
     if (P.fault_law == 1) {
       double np;
-      if constexpr (kZSolve) np = rs_setbnd_k(P, sFk[ci], Wg, Bi, bs, dt, time + dt, true);
+      if constexpr (kZSolve) np = rs_setbnd_k_ool(P, sFk[ci], Wg, Bi, bs, dt, time + dt, true);
       else np = rs_setbnd(P, fr, Wg, Bi, bs, dt, xc - P.rs_x0, time + dt, true);
       if (isnan(np)) report(st, ST_NAN, (long long)i);
     } else {
