@@ -460,6 +460,57 @@ def three_d_measurement(steps, warmup, stream, fp64_steps=3, cpu_seconds=5.0, si
                      "finite": bool(torch.isfinite(Ud).all().item())}
         ctx.close()
     mixed, fp64 = out[A.TMK_PREC_MIXED], out[A.TMK_PREC_FP64]
+    # the same domain as Chombo-sized patches of 32^3: one call per patch, and
+    # the level's patch loop in one batched call (mixed form)
+    tiles = {}
+    tsz = 32
+    if nx % tsz == 0 and ny % tsz == 0 and nz % tsz == 0:
+        sc = S.rate_state(nx=nx, ny=ny, dx=0.1, precision=A.TMK_PREC_MIXED)
+        ctx = Context(sc)
+        pg = LinElastPatchGodunov3D(ctx, (lo, hi))
+        U0, B0 = state(sc)
+        patches = []
+        for k0 in range(0, nz, tsz):
+            for j0 in range(0, ny, tsz):
+                for i0 in range(0, nx, tsz):
+                    v = ((i0, j0, k0), (i0 + tsz - 1, j0 + tsz - 1, k0 + tsz - 1))
+                    U = torch.from_numpy(np.ascontiguousarray(
+                        U0[:, k0:k0 + tsz + 2 * g, j0:j0 + tsz + 2 * g, i0:i0 + tsz + 2 * g])).cuda()
+                    B = None
+                    if j0 == 0:
+                        B = torch.from_numpy(np.ascontiguousarray(B0[:, k0:k0 + tsz + 2 * g, i0:i0 + tsz + 2 * g])).cuda()
+                    patches.append((v, U, (i0 - g, j0 - g, k0 - g), B, (i0 - g, k0 - g)))
+        dt = sc.dt() / 3 ** 0.5
+
+        def per_patch(t):
+            pg.set_current_time(t)
+            for v, U, ulo, B, blo in patches:
+                pg.set_current_box(v)
+                pg.update_state(U, ulo, dt, B=B, blo=blo, stream=stream)
+
+        def batched(t):
+            pg.set_current_time(t)
+            pg.update_states(patches, dt, stream=stream)
+
+        for name, fn in (("per_patch_calls", per_patch), ("batched", batched)):
+            t = 0.0
+            for _ in range(warmup):
+                fn(t)
+                t += dt
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                fn(t)
+                t += dt
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            tiles[name] = {"value": nx * ny * nz / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms}
+        tiles["patches"] = len(patches)
+        tiles["patch"] = f"{tsz}^3 (ghost exchange left out: the caller's)"
+        ctx.close()
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -504,6 +555,7 @@ def three_d_measurement(steps, warmup, stream, fp64_steps=3, cpu_seconds=5.0, si
                                    "passes, update, boundary data)",
                          "timing": f"CUDA events on the launch stream around {mixed['steps']} steps"},
             "cpu_baseline": cpu,
+            "patches_32": tiles,
             "finite": mixed["finite"] and fp64["finite"],
             "execution": "one tmk_patch_update_state_3d call per step, device FABs"}
 

@@ -266,6 +266,21 @@ tmk_status tmk_patch_update_state_3d(tmk_context* ctx, const tmk_fab3* U, const 
                                      double dx, double time, double dt,
                                      double* max_wave_speed, void* stream);
 
+/* The patch loop of LinElastLevelGodunov::step (srcLinElast/LinElastLevelGodunov.cpp:284-333)
+ * in a CH_SPACEDIM == 3 build, batched: tmk_patch_update_state_3d on the npatch patches
+ * of one level, each pass of the step one launch over all of them (Chombo's
+ * 3-D boxes are small: per-patch calls are bound by their launches).  U, valid:
+ * arrays of npatch; B: array of npatch (the entries of patches off the fault plane
+ * are not read) or NULL when no patch starts on it; F0, F1, F2: arrays of npatch
+ * or NULL.  The patches' U must not overlap in their valid boxes (the ghost
+ * exchange is the caller's, before the call).  Same results as npatch calls of
+ * tmk_patch_update_state_3d. */
+tmk_status tmk_patches_update_state_3d(tmk_context* ctx, int npatch, const tmk_fab3* U, const tmk_fab3* B,
+                                       const tmk_fab3* F0, const tmk_fab3* F1, const tmk_fab3* F2,
+                                       const tmk_box3* valid, const tmk_box3* domain,
+                                       double dx, double time, double dt,
+                                       double* max_wave_speed, void* stream);
+
 /* LinElastPhysics::plasticUpdate -> PLASTICCORRECTION on a 3-D device FAB over box. */
 tmk_status tmk_plastic_update_3d(tmk_context* ctx, const tmk_fab3* U, const tmk_box3* box,
                                  double dt, void* stream);

@@ -264,3 +264,75 @@ def test_mixed_3d_tracks_fp64_over_steps(cuda_lib):
     e = rel_err(a, b)
     print("20 steps", e)
     assert 0.0 < e < 1e-4
+
+
+TILES = [((0, 0, 0), (5, 4, 7)), ((6, 0, 0), (11, 4, 3)), ((6, 0, 4), (11, 4, 7)), ((0, 5, 0), (11, 9, 7))]
+
+
+@pytest.mark.parametrize("name", ["rs_aging", "sw_ref9", "no_fault"])
+@pytest.mark.parametrize("prec", [A.TMK_PREC_FP64, A.TMK_PREC_MIXED], ids=["fp64", "mixed"])
+def test_batched_patches_equal_the_whole_domain_step(cuda_lib, name, prec):
+    """tmk_patches_update_state_3d on patches tiling the domain (ghosts taken
+    from the same global state, as an exchange leaves them) gives bit for bit
+    the step of one patch over the whole domain, and the same as one call per
+    patch.  In the mixed form the FP64 boundary-data update is built with FMA
+    contraction, which the compiler may apply differently in the single-patch
+    and batched kernels (a*a + b*b fused either way): there the boundary data
+    agree to 1e-12."""
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    sc = dict(SCEN)[name]
+    rng = np.random.default_rng(99)
+    lo, hi = (0, 0, 0), (NX - 1, NY - 1, NZ - 1)
+    U0 = perturbed_state_3d(sc, rng, lo, hi)
+    fault = sc.scheme.fault_law != A.TMK_FAULT_NONE
+    B0 = random_B_3d(sc, rng, NX + 2 * G, NZ + 2 * G) if fault else None
+    old = sc.scheme.precision
+    sc.scheme.precision = prec
+    try:
+        ctx = Context(sc)
+    finally:
+        sc.scheme.precision = old
+    dt, time = sc.dt(), 0.5
+    pg = LinElastPatchGodunov3D(ctx, DOM)
+    pg.set_current_time(time)
+    # the whole domain as one patch
+    Uw = torch.from_numpy(U0.copy()).cuda()
+    Bw = torch.from_numpy(B0.copy()).cuda() if fault else None
+    pg.set_current_box((lo, hi))
+    pg.update_state(Uw, (-G, -G, -G), dt, B=Bw, blo=(-G, -G))
+
+    def tile_arrays(v):
+        (l0, l1, l2), (h0, h1, h2) = v
+        U = torch.from_numpy(np.ascontiguousarray(U0[:, l2:h2 + 2 * G + 1, l1:h1 + 2 * G + 1, l0:h0 + 2 * G + 1])).cuda()
+        B = None
+        if fault and l1 == 0:
+            B = torch.from_numpy(np.ascontiguousarray(B0[:, l2:h2 + 2 * G + 1, l0:h0 + 2 * G + 1])).cuda()
+        return U, (l0 - G, l1 - G, l2 - G), B, (l0 - G, l2 - G)
+
+    batch = []
+    single = []
+    for v in TILES:
+        U, ulo, B, blo = tile_arrays(v)
+        batch.append((v, U, ulo, B, blo))
+        U2, _, B2, _ = tile_arrays(v)
+        pg.set_current_box(v)
+        pg.update_state(U2, ulo, dt, B=B2, blo=blo)
+        single.append((U2, B2))
+    pg.update_states(batch, dt)
+    torch.cuda.synchronize()
+    Uwh = Uw.cpu().numpy()
+    Bwh = Bw.cpu().numpy() if fault else None
+    for (v, U, ulo, B, blo), (U2, B2) in zip(batch, single):
+        (l0, l1, l2), (h0, h1, h2) = v
+        a = U.cpu().numpy()[:, G:-G, G:-G, G:-G]
+        np.testing.assert_array_equal(a, U2.cpu().numpy()[:, G:-G, G:-G, G:-G])
+        np.testing.assert_array_equal(a, Uwh[:, l2 + G:h2 + G + 1, l1 + G:h1 + G + 1, l0 + G:h0 + G + 1])
+        if B is not None:
+            b = B.cpu().numpy()[:, G:-G, G:-G]
+            for ref in (B2.cpu().numpy()[:, G:-G, G:-G], Bwh[:, l2 + G:h2 + G + 1, l0 + G:h0 + G + 1]):
+                if prec == A.TMK_PREC_FP64:
+                    np.testing.assert_array_equal(b, ref)
+                else:
+                    assert rel_err(b, ref) <= 1e-12
+    ctx.close()

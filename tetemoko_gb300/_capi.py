@@ -170,6 +170,8 @@ def lib() -> C.CDLL:
     L.tmk_patch_update_state_3d.argtypes = [vp, F3, F3, F3, F3, F3, C.POINTER(Box3), C.POINTER(Box3), C.c_double,
                                             C.c_double, C.c_double, dp, vp]
     L.tmk_plastic_update_3d.argtypes = [vp, F3, C.POINTER(Box3), C.c_double, vp]
+    L.tmk_patches_update_state_3d.argtypes = [vp, C.c_int, F3, F3, F3, F3, F3, C.POINTER(Box3), C.POINTER(Box3),
+                                              C.c_double, C.c_double, C.c_double, dp, vp]
     L.tmk_level_create.argtypes = [vp, C.POINTER(Box), C.c_double, C.c_int, C.POINTER(Box), C.POINTER(vp)]
     L.tmk_level_destroy.argtypes = [vp]
     L.tmk_level_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
@@ -228,7 +230,7 @@ def lib() -> C.CDLL:
                  "tmk_level_average_down", "tmk_level_interp_from_coarser", "tmk_level_copy_overlap",
                  "tmk_level_register_size", "tmk_amr_create", "tmk_amr_step", "tmk_amr_time",
                  "tmk_level_graph_create", "tmk_amr_graph_create", "tmk_graph_launch",
-                 "tmk_patch_update_state_3d", "tmk_plastic_update_3d"):
+                 "tmk_patch_update_state_3d", "tmk_plastic_update_3d", "tmk_patches_update_state_3d"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

@@ -13,9 +13,13 @@
 namespace tmk {
 namespace d3 {
 
-cudaError_t launch_step_f64(const Step3<double>& g, const DevParams* P, DevStatus* st, cudaStream_t s,
+cudaError_t launch_one_f64(const PlanOne<double>& pl, const DevParams* P, DevStatus* st, cudaStream_t s,
+                           const Side* side) {
+  return launch_plan<double>(pl, P, st, s, side);
+}
+cudaError_t launch_many_f64(const PlanMany<double>& pl, const DevParams* P, DevStatus* st, cudaStream_t s,
                             const Side* side) {
-  return launch_step<double>(g, P, st, s, side);
+  return launch_plan<double>(pl, P, st, s, side);
 }
 
 __global__ void plastic3_kernel(double* U, Bx A, Bx box, const DevParams* P, double dt) {
@@ -78,87 +82,18 @@ void make_sig_host(const tmk::DevParams& P, double dtbydx, T* sig) {
 
 namespace {
 
-// fill the boxes and scratch pointers of a step in arithmetic T and launch it
-template <typename T>
-tmk_status step3(tmk_context* c, tmk::d3::Step3<T>& g, cudaStream_t s) {
-  using namespace tmk::d3;
-  // scratch: WM, WP (3 each) | WH1 (3) | WH2 (6) | WH (3) | LG | FF (3) | FP32 copy of U
-  const size_t s18 = (size_t)NF * g.S.cells() * sizeof(T);
-  constexpr bool copy = !std::is_same<T, double>::value;
-  std::vector<size_t> sizes;
-  for (int d = 0; d < 6; ++d) sizes.push_back(s18);
-  for (int d = 0; d < 3; ++d) sizes.push_back((size_t)NF * g.fl1[d].cells() * sizeof(T));
-  for (int d1 = 0; d1 < 3; ++d1)
-    for (int d2 = 0; d2 < 3; ++d2)
-      if (d1 != d2) sizes.push_back((size_t)NF * g.fl1[d1].cells() * sizeof(T));
-  for (int d = 0; d < 3; ++d) sizes.push_back((size_t)NF * g.flF[d].cells() * sizeof(T));
-  sizes.push_back(2 * (size_t)g.fplane.cells() * sizeof(double));
-  for (int k = 0; k < 3; ++k) sizes.push_back((size_t)TMK_NCOMP * g.fplane.cells() * sizeof(double));
-  sizes.push_back(copy ? (size_t)NS * g.Ap.cells() * sizeof(T) : 0);
-  size_t total = 0;
-  for (size_t z : sizes) total += align_up3(z);
-  if (total > c->scratch_bytes) {
-    TMK_CU(cudaStreamSynchronize(s));
-    cudaFree(c->scratch);
-    c->scratch = nullptr; c->scratch_bytes = 0;
-    if (cudaMalloc(&c->scratch, total) != cudaSuccess) return TMK_ERR_ALLOC;
-    c->scratch_bytes = total;
-  }
-  char* base = (char*)c->scratch;
-  size_t off = 0, n = 0;
-  auto take = [&]() { char* p = base + off; off += align_up3(sizes[n++]); return p; };
-  for (int d = 0; d < 3; ++d) g.WM[d] = (T*)take();
-  for (int d = 0; d < 3; ++d) g.WP[d] = (T*)take();
-  for (int d = 0; d < 3; ++d) g.WH1[d] = (T*)take();
-  for (int d1 = 0; d1 < 3; ++d1)
-    for (int d2 = 0; d2 < 3; ++d2)
-      if (d1 != d2) g.WH2[d1][d2] = (T*)take();
-  for (int d = 0; d < 3; ++d) g.WH[d] = (T*)take();
-  g.LG = (double*)take();
-  for (int k = 0; k < 3; ++k) g.FF[k] = (double*)take();
-  T* up = (T*)take();
-  if constexpr (copy) { g.Up = up; g.Uc = up; g.uside = tmk::NSIDE; }
-  else { g.Up = (const T*)(const void*)g.U; g.Uc = nullptr; g.Ap = g.A; g.uside = 11; }
-  g.kc.load(c->hp);
-  make_sig_host(c->hp, g.dt / g.dx, g.sig);
-  g.scale3 = (T)(-(1.0 / 3.0) * g.dt / g.dx);
-  g.scale2 = (T)(-(1.0 / 2.0) * g.dt / g.dx);
-  g.sc = -g.dt / g.dx;
-  g.fastpred = copy && c->hp.order == 2 && c->hp.prim_lim && !c->hp.char_lim;
-  for (int q = 0; q < tmk::NSIDE; ++q) {
-    const double sv = std::fabs((double)g.sig[q]);
-    g.trA[q] = (T)(0.5 * sv);
-    g.trB[q] = (T)(q < 3 ? 3.0 * (0.5 * sv - sv * sv / 3.0) : 1.5 * sv * (1.0 - (2.0 / 3.0) * sv));
-  }
-  // the side stream and events of the overlapped schedule, made once per context
-  Side side;
-  if (g.fault) {
-    if (!c->side) {
-      cudaStream_t ss = nullptr;
-      if (cudaStreamCreateWithFlags(&ss, cudaStreamNonBlocking) != cudaSuccess) return TMK_ERR_CUDA;
-      c->side = ss;
-      for (int q = 0; q < 6; ++q)
-        if (cudaEventCreateWithFlags(&c->side_ev[q], cudaEventDisableTiming) != cudaSuccess) return TMK_ERR_CUDA;
-    }
-    side.s = c->side;
-    for (int q = 0; q < 6; ++q) side.ev[q] = c->side_ev[q];
-  }
-  cudaError_t e;
-  if constexpr (std::is_same<T, double>::value) e = launch_step_f64(g, c->dp, c->dstatus, s, &side);
-  else e = launch_step_f32(g, c->dp, c->dstatus, s, &side);
-  return e == cudaSuccess ? TMK_OK : TMK_ERR_CUDA;
-}
+using tmk::d3::Step3;
 
-// validate the descriptors, fill the step's boxes and run it in arithmetic T
+// Validate one patch's descriptors and fill its step's boxes, pointers and
+// launch constants (scratch pointers are laid out by layout3).
 template <typename T>
-tmk_status patch3(tmk_context* c, const tmk_fab3* U, const tmk_fab3* B, const tmk_fab3* const* Fo,
-                  const tmk_box3* valid, const tmk_box3* domain, double dx, double time, double dt,
-                  cudaStream_t s) {
+tmk_status fill3(tmk_context* c, const tmk_fab3* U, const tmk_fab3* B, const tmk_fab3* const* Fo,
+                 const tmk_box3* valid, const tmk_box3* domain, double dx, double time, double dt, Step3<T>& g) {
   using namespace tmk::d3;
+  if (!U || !U->data || !valid || U->ncomp != TMK_NCOMP) return TMK_ERR_BAD_DESC;
   const Bx cur = bx_of(valid->lo, valid->hi), dom = bx_of(domain->lo, domain->hi), A = bx_of(U->lo, U->hi);
   if (!bx_ok(cur) || !bx_ok(dom) || !bx_ok(A) || !bx_contains(dom, cur)) return TMK_ERR_BAD_DESC;
   if (!bx_contains(A, bx_isect(bx_grow(cur, 3), dom))) return TMK_ERR_BAD_DESC;
-  Step3<T> g;
   std::memset(&g, 0, sizeof(g));
   g.A = A; g.cur = cur;
   for (int d = 0; d < 3; ++d) { g.dlo[d] = domain->lo[d]; g.dhi[d] = domain->hi[d]; }
@@ -178,7 +113,7 @@ tmk_status patch3(tmk_context* c, const tmk_fab3* U, const tmk_fab3* B, const tm
     g.B = B->data;
   }
   for (int d = 0; d < 3; ++d) {
-    if (!Fo[d]) continue;
+    if (!Fo || !Fo[d]) continue;
     if (!Fo[d]->data || Fo[d]->ncomp != TMK_NCOMP) return TMK_ERR_BAD_DESC;
     const Bx fb = bx_of(Fo[d]->lo, Fo[d]->hi);
     for (int e = 0; e < 3; ++e)
@@ -188,7 +123,145 @@ tmk_status patch3(tmk_context* c, const tmk_fab3* U, const tmk_fab3* B, const tm
   g.U = U->data;
   g.Ap = bx_isect(bx_grow(cur, 3), dom);
   g.dx = dx; g.dt = dt; g.time = time;
-  return step3<T>(c, g, s);
+  // launch constants (the same FP64 expressions as the device code, on the host)
+  constexpr bool copy = !std::is_same<T, double>::value;
+  g.kc.load(c->hp);
+  make_sig_host(c->hp, g.dt / g.dx, g.sig);
+  g.scale3 = (T)(-(1.0 / 3.0) * g.dt / g.dx);
+  g.scale2 = (T)(-(1.0 / 2.0) * g.dt / g.dx);
+  g.sc = -g.dt / g.dx;
+  g.fastpred = copy && c->hp.order == 2 && c->hp.prim_lim && !c->hp.char_lim;
+  for (int q = 0; q < tmk::NSIDE; ++q) {
+    const double sv = std::fabs((double)g.sig[q]);
+    g.trA[q] = (T)(0.5 * sv);
+    g.trB[q] = (T)(q < 3 ? 3.0 * (0.5 * sv - sv * sv / 3.0) : 1.5 * sv * (1.0 - (2.0 / 3.0) * sv));
+  }
+  return TMK_OK;
+}
+
+// Scratch of one patch's step -- WM, WP (3 each) | WH1 (3) | WH2 (6) | WH (3) |
+// LG | FF (3) | FP32 copy of U (mixed form) -- from `base` (or only its size
+// when base is null).  Returns the bytes used.
+template <typename T>
+size_t layout3(Step3<T>& g, char* base) {
+  using namespace tmk::d3;
+  constexpr bool copy = !std::is_same<T, double>::value;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* p = base ? base + off : nullptr;
+    off += align_up3(bytes);
+    return p;
+  };
+  const size_t cell12 = (size_t)NF * g.S.cells() * sizeof(T);
+  for (int d = 0; d < 3; ++d) g.WM[d] = (T*)take(cell12);
+  for (int d = 0; d < 3; ++d) g.WP[d] = (T*)take(cell12);
+  for (int d = 0; d < 3; ++d) g.WH1[d] = (T*)take((size_t)NF * g.fl1[d].cells() * sizeof(T));
+  for (int d1 = 0; d1 < 3; ++d1)
+    for (int d2 = 0; d2 < 3; ++d2)
+      if (d1 != d2) g.WH2[d1][d2] = (T*)take((size_t)NF * g.fl1[d1].cells() * sizeof(T));
+  for (int d = 0; d < 3; ++d) g.WH[d] = (T*)take((size_t)NF * g.flF[d].cells() * sizeof(T));
+  g.LG = (double*)take(2 * (size_t)g.fplane.cells() * sizeof(double));
+  for (int k = 0; k < 3; ++k) g.FF[k] = (double*)take((size_t)TMK_NCOMP * g.fplane.cells() * sizeof(double));
+  T* up = (T*)take(copy ? (size_t)NS * g.Ap.cells() * sizeof(T) : 0);
+  if constexpr (copy) { g.Up = up; g.Uc = up; g.uside = tmk::NSIDE; }
+  else { g.Up = (const T*)(const void*)g.U; g.Uc = nullptr; g.Ap = g.A; g.uside = 11; }
+  return off;
+}
+
+tmk_status ensure_scratch(tmk_context* c, size_t total, cudaStream_t s) {
+  if (total <= c->scratch_bytes) return TMK_OK;
+  TMK_CU(cudaStreamSynchronize(s));
+  cudaFree(c->scratch);
+  c->scratch = nullptr; c->scratch_bytes = 0;
+  if (cudaMalloc(&c->scratch, total) != cudaSuccess) return TMK_ERR_ALLOC;
+  c->scratch_bytes = total;
+  return TMK_OK;
+}
+
+// the side stream and events of the overlapped schedule, made once per context
+tmk_status ensure_side(tmk_context* c, tmk::d3::Side& side) {
+  if (!c->side) {
+    cudaStream_t ss = nullptr;
+    if (cudaStreamCreateWithFlags(&ss, cudaStreamNonBlocking) != cudaSuccess) return TMK_ERR_CUDA;
+    c->side = ss;
+    for (int q = 0; q < 6; ++q)
+      if (cudaEventCreateWithFlags(&c->side_ev[q], cudaEventDisableTiming) != cudaSuccess) return TMK_ERR_CUDA;
+  }
+  side.s = c->side;
+  for (int q = 0; q < 6; ++q) side.ev[q] = c->side_ev[q];
+  return TMK_OK;
+}
+
+template <typename T>
+tmk_status patch3(tmk_context* c, const tmk_fab3* U, const tmk_fab3* B, const tmk_fab3* const* Fo,
+                  const tmk_box3* valid, const tmk_box3* domain, double dx, double time, double dt,
+                  cudaStream_t s) {
+  using namespace tmk::d3;
+  PlanOne<T> pl;
+  tmk_status r = fill3<T>(c, U, B, Fo, valid, domain, dx, time, dt, pl.g);
+  if (r != TMK_OK) return r;
+  if ((r = ensure_scratch(c, layout3<T>(pl.g, nullptr), s)) != TMK_OK) return r;
+  layout3<T>(pl.g, (char*)c->scratch);
+  Side side;
+  if (pl.g.fault && (r = ensure_side(c, side)) != TMK_OK) return r;
+  cudaError_t e;
+  if constexpr (std::is_same<T, double>::value) e = launch_one_f64(pl, c->dp, c->dstatus, s, &side);
+  else e = launch_one_f32(pl, c->dp, c->dstatus, s, &side);
+  return e == cudaSuccess ? TMK_OK : TMK_ERR_CUDA;
+}
+
+// The patches of a level: their descriptors and each pass's prefix sums in
+// the scratch's head, uploaded with one copy, then one launch per pass over
+// every patch.
+template <typename T>
+tmk_status patches3(tmk_context* c, int np, const tmk_fab3* U, const tmk_fab3* B, const tmk_fab3* const* Fa,
+                    const tmk_box3* valid, const tmk_box3* domain, double dx, double time, double dt,
+                    cudaStream_t s) {
+  using namespace tmk::d3;
+  std::vector<Step3<T>> gs(np);
+  for (int p = 0; p < np; ++p) {
+    const tmk_fab3* Fo[3] = {Fa[0] ? Fa[0] + p : nullptr, Fa[1] ? Fa[1] + p : nullptr, Fa[2] ? Fa[2] + p : nullptr};
+    const tmk_status r = fill3<T>(c, U + p, B ? B + p : nullptr, Fo, valid + p, domain, dx, time, dt, gs[p]);
+    if (r != TMK_OK) return r;
+  }
+  PlanMany<T> pl;
+  pl.np = np;
+  pl.copy_ = !std::is_same<T, double>::value;
+  pl.fault_ = false;
+  for (int d = 0; d < 3; ++d) pl.flux_[d] = false;
+  std::vector<long long> start((size_t)NKIND * (np + 1), 0);
+  for (int k = 0; k < NKIND; ++k) {
+    long long* st = start.data() + (size_t)k * (np + 1);
+    for (int p = 0; p < np; ++p) st[p + 1] = st[p] + kind_count(gs[p], k);
+    pl.tot[k] = st[np];
+  }
+  const size_t head = align_up3(np * sizeof(Step3<T>)) + align_up3(start.size() * sizeof(long long));
+  size_t total = head;
+  std::vector<size_t> offs(np);
+  for (int p = 0; p < np; ++p) {
+    offs[p] = total;
+    total += layout3<T>(gs[p], nullptr);
+    pl.fault_ = pl.fault_ || gs[p].fault;
+    for (int d = 0; d < 3; ++d) pl.flux_[d] = pl.flux_[d] || gs[p].F[d];
+  }
+  tmk_status r = ensure_scratch(c, total, s);
+  if (r != TMK_OK) return r;
+  char* base = (char*)c->scratch;
+  for (int p = 0; p < np; ++p) layout3<T>(gs[p], base + offs[p]);
+  // descriptors and prefix sums: one upload (pageable: staged before the call returns)
+  std::vector<char> hbuf(head);
+  std::memcpy(hbuf.data(), gs.data(), np * sizeof(Step3<T>));
+  const size_t soff = align_up3(np * sizeof(Step3<T>));
+  std::memcpy(hbuf.data() + soff, start.data(), start.size() * sizeof(long long));
+  TMK_CU(cudaMemcpyAsync(base, hbuf.data(), head, cudaMemcpyHostToDevice, s));
+  pl.dgs = (const Step3<T>*)base;
+  pl.dstart = (const long long*)(base + soff);
+  Side side;
+  if (pl.fault_ && (r = ensure_side(c, side)) != TMK_OK) return r;
+  cudaError_t e;
+  if constexpr (std::is_same<T, double>::value) e = launch_many_f64(pl, c->dp, c->dstatus, s, &side);
+  else e = launch_many_f32(pl, c->dp, c->dstatus, s, &side);
+  return e == cudaSuccess ? TMK_OK : TMK_ERR_CUDA;
 }
 
 }  // namespace
@@ -206,6 +279,21 @@ extern "C" tmk_status tmk_patch_update_state_3d(tmk_context* c, const tmk_fab3* 
   const tmk_status r = c->scheme.precision == TMK_PREC_MIXED
                            ? patch3<float>(c, U, B, Fo, valid, domain, dx, time, dt, s)
                            : patch3<double>(c, U, B, Fo, valid, domain, dx, time, dt, s);
+  if (r != TMK_OK) return r;
+  if (max_wave_speed) *max_wave_speed = std::max(c->hp.cs, c->hp.cp);
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_patches_update_state_3d(tmk_context* c, int npatch, const tmk_fab3* U, const tmk_fab3* B,
+                                                  const tmk_fab3* F0, const tmk_fab3* F1, const tmk_fab3* F2,
+                                                  const tmk_box3* valid, const tmk_box3* domain, double dx,
+                                                  double time, double dt, double* max_wave_speed, void* stream) {
+  if (!c || npatch < 1 || !U || !valid || !domain || !(dx > 0) || !(dt > 0)) return TMK_ERR_BAD_DESC;
+  const tmk_fab3* Fa[3] = {F0, F1, F2};
+  cudaStream_t s = (cudaStream_t)stream;
+  const tmk_status r = c->scheme.precision == TMK_PREC_MIXED
+                           ? patches3<float>(c, npatch, U, B, Fa, valid, domain, dx, time, dt, s)
+                           : patches3<double>(c, npatch, U, B, Fa, valid, domain, dx, time, dt, s);
   if (r != TMK_OK) return r;
   if (max_wave_speed) *max_wave_speed = std::max(c->hp.cs, c->hp.cp);
   return TMK_OK;

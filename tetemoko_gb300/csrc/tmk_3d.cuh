@@ -164,7 +164,7 @@ template <int D> TMK_D void face_at(const Bx& fb, bool fault, long long t, int& 
 
 // Which faces a launch of a face pass covers: all of them, the bulk (the
 // fault plane excluded) or the fault plane alone.  The fault plane's passes
-// run on a second stream beside the bulk (launch_step).
+// run on a second stream beside the bulk (launch_plan).
 enum : int { PART_ALL = 0, PART_BULK = 1, PART_FAULT = 2 };
 template <int D>
 TMK_HD long long part_faces(const Bx& fb, bool fault, int part) {
@@ -249,10 +249,38 @@ TMK_D void ppm_predict_prim(const Consts<T>& k, T rv, const T (*w5)[5], const bo
   for (int c = 0; c < NSIDE; ++c) { WM[c] += w5[c][2]; WP[c] += w5[c][2]; }
 }
 
+// ------------------------------------------------------ work of a launch
+// A launch covers one patch (its descriptor passed by value) or the patches of
+// a batch (descriptors in device memory, with the prefix sums of the pass's
+// work per patch): find() gives thread t's patch and its index there.
+template <typename T>
+struct One {
+  Step3<T> g;
+  TMK_D const Step3<T>* find(long long t, long long& lt) const { lt = t; return &g; }
+};
+template <typename T>
+struct Many {
+  const Step3<T>* gs;
+  const long long* start;   // np + 1 prefix sums of the pass's work
+  int np;
+  TMK_D const Step3<T>* find(long long t, long long& lt) const {
+    if (t >= start[np]) return nullptr;
+    int lo = 0, hi = np - 1;            // the last patch whose work starts at or before t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (start[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    lt = t - start[lo];
+    return gs + lo;
+  }
+};
+#define TMK3_FIND(T)                                                                 \
+  long long lt;                                                                      \
+  const Step3<T>* gp = src.find(blockIdx.x * (long long)blockDim.x + threadIdx.x, lt); \
+  if (!gp) return;
+
 template <int D, typename T>
-__global__ void __launch_bounds__(128) pred_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp) {
-  const DevParams& P = *Pp;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+TMK_D void pred_body(const Step3<T>& g, const DevParams& P, long long t) {
   if (t >= g.S.cells()) return;
   int i, j, k;
   g.S.cell(t, i, j, k);
@@ -300,6 +328,11 @@ __global__ void __launch_bounds__(128) pred_kernel(const __grid_constant__ Step3
       g.LG[(c - 9) * g.fplane.cells() + g.fplane.at(i, j, k)] = zero_speed_lo(P, w, in);
     }
   }
+}
+template <int D, typename T, typename Src>
+__global__ void __launch_bounds__(128) pred_kernel(const __grid_constant__ Src src, const DevParams* Pp) {
+  TMK3_FIND(T)
+  pred_body<D, T>(*gp, *Pp, lt);
 }
 
 // -------------------------------------------------------- face conditions
@@ -393,11 +426,8 @@ TMK_D void load_ff(const Step3<T>& g, const double* FFk, int i, int k, double* U
 
 // ------------------------------------------------------------ first pass
 template <int D, typename T>
-__global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
-                                                    DevStatus* st, int part) {
-  const DevParams& P = *Pp;
+TMK_D void riem1_body(const Step3<T>& g, const DevParams& P, DevStatus* st, int part, long long t) {
   const Bx& fb = g.fl1[D];
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= part_faces<D>(fb, g.fault != 0, part)) return;
   int i, j, k;
   part_face<D>(fb, g.fault != 0, part, t, i, j, k);
@@ -411,6 +441,12 @@ __global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Step
   if (!face_state<D, T>(P, kc, g, f, L, R, G))
     fault_solve(P, g, i, k, R, bdry_value(P, g, i, k, nullptr, 0.0), g.FF[0], G, st);
   store_face<D>(g.WH1[D], fb, i, j, k, G);
+}
+template <int D, typename T, typename Src>
+__global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Src src, const DevParams* Pp,
+                                                    DevStatus* st, int part) {
+  TMK3_FIND(T)
+  riem1_body<D, T>(*gp, *Pp, st, part, lt);
 }
 
 // cell state T18 of array A (direction-D1 normal states) at (i, j, k), moved by
@@ -454,20 +490,21 @@ TMK_D void riem2_face(const Step3<T>& g, const DevParams& P, DevStatus* st, int 
   store_face<D1>(g.WH2[D1][D2], fb, i, j, k, G);
 }
 
-template <int D1, int D2, typename T>
-__global__ void __launch_bounds__(128) riem2_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
+template <int D1, int D2, typename T, typename Src>
+__global__ void __launch_bounds__(128) riem2_kernel(const __grid_constant__ Src src, const DevParams* Pp,
                                                     DevStatus* st, int part) {
-  riem2_face<D1, D2, T>(g, *Pp, st, part, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+  TMK3_FIND(T)
+  riem2_face<D1, D2, T>(*gp, *Pp, st, part, lt);
 }
 
 // WHalf2[1][0] and WHalf2[1][2] on the fault plane in one launch (grid y = 0,
 // 1): the two friction solves of a face run side by side
-template <typename T>
-__global__ void __launch_bounds__(128) riem2_fault_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
+template <typename T, typename Src>
+__global__ void __launch_bounds__(128) riem2_fault_kernel(const __grid_constant__ Src src, const DevParams* Pp,
                                                           DevStatus* st) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (blockIdx.y == 0) riem2_face<1, 0, T>(g, *Pp, st, PART_FAULT, t);
-  else riem2_face<1, 2, T>(g, *Pp, st, PART_FAULT, t);
+  TMK3_FIND(T)
+  if (blockIdx.y == 0) riem2_face<1, 0, T>(*gp, *Pp, st, PART_FAULT, lt);
+  else riem2_face<1, 2, T>(*gp, *Pp, st, PART_FAULT, lt);
 }
 
 // ------------------------------------------------------------ final pass
@@ -495,11 +532,8 @@ TMK_D void final_state(const Step3<T>& g, const Consts<T>& kc, const T* A, T sca
 }
 
 template <int D1, typename T>
-__global__ void __launch_bounds__(128) final_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
-                                                    DevStatus* st, int part) {
-  const DevParams& P = *Pp;
+TMK_D void final_body(const Step3<T>& g, const DevParams& P, DevStatus* st, int part, long long t) {
   const Bx& fb = g.flF[D1];
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= part_faces<D1>(fb, g.fault != 0, part)) return;
   int i, j, k;
   part_face<D1>(fb, g.fault != 0, part, t, i, j, k);
@@ -518,6 +552,12 @@ __global__ void __launch_bounds__(128) final_kernel(const __grid_constant__ Step
     fault_solve(P, g, i, k, R, bval, g.FF[2], G, st);
   }
   store_face<D1>(g.WH[D1], fb, i, j, k, G);
+}
+template <int D1, typename T, typename Src>
+__global__ void __launch_bounds__(128) final_kernel(const __grid_constant__ Src src, const DevParams* Pp,
+                                                    DevStatus* st, int part) {
+  TMK3_FIND(T)
+  final_body<D1, T>(*gp, *Pp, st, part, lt);
 }
 
 // ---------------------------------------------------------------- update
@@ -538,9 +578,7 @@ TMK_D void flux_diff(const Step3<T>& g, const Consts<T>& kc, int i, int j, int k
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128) update_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp) {
-  const DevParams& P = *Pp;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+TMK_D void update_body(const Step3<T>& g, long long t) {
   if (t >= g.cur.cells()) return;
   int i, j, k;
   g.cur.cell(t, i, j, k);
@@ -561,15 +599,18 @@ __global__ void __launch_bounds__(128) update_kernel(const __grid_constant__ Ste
       *u = *u + (double)dU[NSIDE * s + c] * sc;
     }
 }
+template <typename T, typename Src>
+__global__ void __launch_bounds__(128) update_kernel(const __grid_constant__ Src src) {
+  TMK3_FIND(T)
+  update_body<T>(*gp, lt);
+}
 
 // the face fluxes of direction D (22 comps; lambda, gamma and the antiplane
 // stress of the face normal carry none)
 template <int D, typename T>
-__global__ void __launch_bounds__(128) flux_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp) {
-  const DevParams& P = *Pp;
+TMK_D void flux_body(const Step3<T>& g, long long t) {
   const Bx& fb = g.flF[D];
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= fb.cells()) return;
+  if (t >= fb.cells() || !g.F[D]) return;
   int i, j, k;
   fb.cell(t, i, j, k);
   const Consts<T>& kc = g.kc;
@@ -587,15 +628,17 @@ __global__ void __launch_bounds__(128) flux_kernel(const __grid_constant__ Step3
     out[(11 * s + 10) * cs] = 0.0;
   }
 }
+template <int D, typename T, typename Src>
+__global__ void __launch_bounds__(128) flux_kernel(const __grid_constant__ Src src) {
+  TMK3_FIND(T)
+  flux_body<D, T>(*gp, lt);
+}
 
 // the fault's boundary data, final (RSSETBND / SWSETBND over the valid x, z)
 template <typename T>
-__global__ void __launch_bounds__(128) bdry_final_kernel(const __grid_constant__ Step3<T> g, const DevParams* Pp,
-                                                         DevStatus* st) {
-  const DevParams& P = *Pp;
+TMK_D void bdry_final_body(const Step3<T>& g, const DevParams& P, DevStatus* st, long long t) {
   const int nx = g.cur.n[0], nz = g.cur.n[2];
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)nx * nz) return;
+  if (!g.fault || t >= (long long)nx * nz) return;
   const int i = g.cur.lo[0] + (int)(t % nx), k = g.cur.lo[2] + (int)(t / nx);
   double U22[NC];
   load_ff(g, g.FF[2], i, k, U22);
@@ -613,12 +656,18 @@ __global__ void __launch_bounds__(128) bdry_final_kernel(const __grid_constant__
     sw_setbnd(P, U22, Bi, bs, g.dt, g.time + g.dt, true);
   }
 }
+template <typename T, typename Src>
+__global__ void __launch_bounds__(128) bdry_final_kernel(const __grid_constant__ Src src, const DevParams* Pp,
+                                                         DevStatus* st) {
+  TMK3_FIND(T)
+  bdry_final_body<T>(*gp, *Pp, st, lt);
+}
 
 // FP32 copy of the evolving components of U over Ap (mixed form)
 template <typename T>
-__global__ void __launch_bounds__(256) to_pred_kernel(const __grid_constant__ Step3<T> g, T* out) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+TMK_D void to_pred_body(const Step3<T>& g, long long t) {
   if (t >= g.Ap.cells()) return;
+  T* out = g.Uc;
   int i, j, k;
   g.Ap.cell(t, i, j, k);
   const long long acs = g.A.cells(), o = g.A.at(i, j, k), pcs = g.Ap.cells();
@@ -627,8 +676,69 @@ __global__ void __launch_bounds__(256) to_pred_kernel(const __grid_constant__ St
 #pragma unroll
     for (int c = 0; c < NSIDE; ++c) out[(NSIDE * s + c) * pcs + t] = (T)g.U[(11 * s + c) * acs + o];
 }
+template <typename T, typename Src>
+__global__ void __launch_bounds__(128) to_pred_kernel(const __grid_constant__ Src src) {
+  TMK3_FIND(T)
+  to_pred_body<T>(*gp, lt);
+}
 
 inline unsigned blocks(long long n) { return (unsigned)((n + 127) / 128); }
+
+// ------------------------------------------------------------ work plans
+// The work of each kind of pass: cells or faces, for the y-direction face
+// passes also split into the bulk and the fault plane.
+enum : int {
+  K_AP = 0, K_S, K_FL1_0, K_FL1_1, K_FL1_1B, K_FL1_1F, K_FL1_2, K_FLF_0, K_FLF_1, K_FLF_1B, K_FLF_1F, K_FLF_2,
+  K_CUR, K_BF, NKIND
+};
+template <typename T>
+TMK_HD long long kind_count(const Step3<T>& g, int kind) {
+  const bool f = g.fault != 0;
+  switch (kind) {
+    case K_AP: return g.Ap.cells();
+    case K_S: return g.S.cells();
+    case K_FL1_0: return g.fl1[0].cells();
+    case K_FL1_1: return part_faces<1>(g.fl1[1], f, PART_ALL);
+    case K_FL1_1B: return part_faces<1>(g.fl1[1], f, PART_BULK);
+    case K_FL1_1F: return part_faces<1>(g.fl1[1], f, PART_FAULT);
+    case K_FL1_2: return g.fl1[2].cells();
+    case K_FLF_0: return g.flF[0].cells();
+    case K_FLF_1: return part_faces<1>(g.flF[1], f, PART_ALL);
+    case K_FLF_1B: return part_faces<1>(g.flF[1], f, PART_BULK);
+    case K_FLF_1F: return part_faces<1>(g.flF[1], f, PART_FAULT);
+    case K_FLF_2: return g.flF[2].cells();
+    case K_CUR: return g.cur.cells();
+    case K_BF: return f ? (long long)g.cur.n[0] * g.cur.n[2] : 0;
+  }
+  return 0;
+}
+
+// one patch: its descriptor by value
+template <typename T>
+struct PlanOne {
+  using Src = One<T>;
+  Step3<T> g;
+  long long n(int kind) const { return kind_count(g, kind); }
+  Src src(int) const { return Src{g}; }
+  bool copy() const { return g.Up != (const T*)(const void*)g.U; }
+  bool fault() const { return g.fault != 0; }
+  bool flux(int d) const { return g.F[d] != nullptr; }
+};
+// a batch: descriptors and prefix sums in device memory, totals on the host
+template <typename T>
+struct PlanMany {
+  using Src = Many<T>;
+  const Step3<T>* dgs;
+  const long long* dstart;     // NKIND x (np + 1)
+  int np;
+  long long tot[NKIND];
+  bool copy_, fault_, flux_[3];
+  long long n(int kind) const { return tot[kind]; }
+  Src src(int kind) const { return Src{dgs, dstart + (size_t)kind * (np + 1), np}; }
+  bool copy() const { return copy_; }
+  bool fault() const { return fault_; }
+  bool flux(int d) const { return flux_[d]; }
+};
 
 // Streams and events of the overlapped schedule (created with the context's
 // first 3-D step)
@@ -637,24 +747,23 @@ struct Side {
   cudaEvent_t ev[6] = {};
 };
 
-// The whole step on stream s.  When the patch holds fault faces and a side
-// stream is given, the three passes over the fault plane (their friction
-// solves are chains of dependent FP64 operations) run on the side stream
-// beside the bulk passes, forked and joined with events:
+// The whole step on stream s, for one patch or a batch.  When the work holds
+// fault faces and a side stream is given, the three passes over the fault
+// plane (their friction solves are chains of dependent FP64 operations) run on
+// the side stream beside the bulk passes, forked and joined with events:
 //   side: [pred<1>] F1 = riem1<1> fault | [riem1<0>, riem1<2>] F2 = riem2<1,0> and riem2<1,2> fault (one launch)
 //         | [riem2<0,2>, riem2<2,0>] F3 = final<1> fault
 //   main: pred x3, riem1<0>, riem1<2>, riem1<1> bulk, riem2<0,2>, riem2<2,0>, riem2<1,*> bulk,
 //         [F1] riem2<0,1>, riem2<2,1>, final<1> bulk, [F2] final<0>, final<2>, [F3] update
 // Each pass still reads exactly what the reference's order has written when
 // it runs; the passes on the two streams write disjoint faces.
-template <typename T>
-cudaError_t launch_step(const Step3<T>& g, const DevParams* P, DevStatus* st, cudaStream_t s, const Side* side) {
-  if (g.Up != (const T*)(const void*)g.U)
-    to_pred_kernel<T><<<(unsigned)((g.Ap.cells() + 255) / 256), 256, 0, s>>>(g, g.Uc);
-  const bool split = g.fault && side && side->s;
-  const bool f = g.fault != 0;
-  const int bulk = split ? PART_BULK : PART_ALL;
+template <typename T, typename Plan>
+cudaError_t launch_plan(const Plan& pl, const DevParams* P, DevStatus* st, cudaStream_t s, const Side* side) {
+  using Src = typename Plan::Src;
+  const bool split = pl.fault() && side && side->s;
   cudaStream_t fs = split ? side->s : s;
+  const int bulk = split ? PART_BULK : PART_ALL;
+  const int k11 = split ? K_FL1_1B : K_FL1_1, kf1 = split ? K_FLF_1B : K_FLF_1;
   auto fork = [&](int e) {
     if (!split) return;
     cudaEventRecord(side->ev[e], s);
@@ -664,53 +773,58 @@ cudaError_t launch_step(const Step3<T>& g, const DevParams* P, DevStatus* st, cu
     if (!split) return;
     cudaStreamWaitEvent(s, side->ev[e], 0);
   };
-  const unsigned bS = blocks(g.S.cells());
-  pred_kernel<0, T><<<bS, 128, 0, s>>>(g, P);
-  pred_kernel<1, T><<<bS, 128, 0, s>>>(g, P);
+  auto nb = [&](int kind) { return blocks(pl.n(kind)); };
+  if (pl.copy() && pl.n(K_AP)) to_pred_kernel<T, Src><<<nb(K_AP), 128, 0, s>>>(pl.src(K_AP));
+  pred_kernel<0, T, Src><<<nb(K_S), 128, 0, s>>>(pl.src(K_S), P);
+  pred_kernel<1, T, Src><<<nb(K_S), 128, 0, s>>>(pl.src(K_S), P);
   fork(0);
   if (split) {
-    riem1_kernel<1, T><<<blocks(part_faces<1>(g.fl1[1], f, PART_FAULT)), 128, 0, fs>>>(g, P, st, PART_FAULT);
+    riem1_kernel<1, T, Src><<<nb(K_FL1_1F), 128, 0, fs>>>(pl.src(K_FL1_1F), P, st, PART_FAULT);
     cudaEventRecord(side->ev[3], fs);
   }
-  pred_kernel<2, T><<<bS, 128, 0, s>>>(g, P);
-  riem1_kernel<0, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
-  riem1_kernel<2, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  pred_kernel<2, T, Src><<<nb(K_S), 128, 0, s>>>(pl.src(K_S), P);
+  riem1_kernel<0, T, Src><<<nb(K_FL1_0), 128, 0, s>>>(pl.src(K_FL1_0), P, st, PART_ALL);
+  riem1_kernel<2, T, Src><<<nb(K_FL1_2), 128, 0, s>>>(pl.src(K_FL1_2), P, st, PART_ALL);
   fork(1);
   if (split) {
-    riem2_fault_kernel<T><<<dim3(blocks(part_faces<1>(g.fl1[1], f, PART_FAULT)), 2), 128, 0, fs>>>(g, P, st);
+    riem2_fault_kernel<T, Src><<<dim3(nb(K_FL1_1F), 2), 128, 0, fs>>>(pl.src(K_FL1_1F), P, st);
     cudaEventRecord(side->ev[4], fs);
   }
-  riem1_kernel<1, T><<<blocks(part_faces<1>(g.fl1[1], f, bulk)), 128, 0, s>>>(g, P, st, bulk);
-  riem2_kernel<0, 2, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
-  riem2_kernel<2, 0, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  riem1_kernel<1, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
+  riem2_kernel<0, 2, T, Src><<<nb(K_FL1_0), 128, 0, s>>>(pl.src(K_FL1_0), P, st, PART_ALL);
+  riem2_kernel<2, 0, T, Src><<<nb(K_FL1_2), 128, 0, s>>>(pl.src(K_FL1_2), P, st, PART_ALL);
   fork(2);
   if (split) {
-    final_kernel<1, T><<<blocks(part_faces<1>(g.flF[1], f, PART_FAULT)), 128, 0, fs>>>(g, P, st, PART_FAULT);
+    final_kernel<1, T, Src><<<nb(K_FLF_1F), 128, 0, fs>>>(pl.src(K_FLF_1F), P, st, PART_FAULT);
     cudaEventRecord(side->ev[5], fs);
   }
-  riem2_kernel<1, 0, T><<<blocks(part_faces<1>(g.fl1[1], f, bulk)), 128, 0, s>>>(g, P, st, bulk);
-  riem2_kernel<1, 2, T><<<blocks(part_faces<1>(g.fl1[1], f, bulk)), 128, 0, s>>>(g, P, st, bulk);
+  riem2_kernel<1, 0, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
+  riem2_kernel<1, 2, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
   join(3);
-  riem2_kernel<0, 1, T><<<blocks(g.fl1[0].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
-  riem2_kernel<2, 1, T><<<blocks(g.fl1[2].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
-  final_kernel<1, T><<<blocks(part_faces<1>(g.flF[1], f, bulk)), 128, 0, s>>>(g, P, st, bulk);
+  riem2_kernel<0, 1, T, Src><<<nb(K_FL1_0), 128, 0, s>>>(pl.src(K_FL1_0), P, st, PART_ALL);
+  riem2_kernel<2, 1, T, Src><<<nb(K_FL1_2), 128, 0, s>>>(pl.src(K_FL1_2), P, st, PART_ALL);
+  final_kernel<1, T, Src><<<nb(kf1), 128, 0, s>>>(pl.src(kf1), P, st, bulk);
   join(4);
-  final_kernel<0, T><<<blocks(g.flF[0].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
-  final_kernel<2, T><<<blocks(g.flF[2].cells()), 128, 0, s>>>(g, P, st, PART_ALL);
+  final_kernel<0, T, Src><<<nb(K_FLF_0), 128, 0, s>>>(pl.src(K_FLF_0), P, st, PART_ALL);
+  final_kernel<2, T, Src><<<nb(K_FLF_2), 128, 0, s>>>(pl.src(K_FLF_2), P, st, PART_ALL);
   join(5);
-  if (g.F[0]) flux_kernel<0, T><<<blocks(g.flF[0].cells()), 128, 0, s>>>(g, P);
-  if (g.F[1]) flux_kernel<1, T><<<blocks(g.flF[1].cells()), 128, 0, s>>>(g, P);
-  if (g.F[2]) flux_kernel<2, T><<<blocks(g.flF[2].cells()), 128, 0, s>>>(g, P);
-  update_kernel<T><<<blocks(g.cur.cells()), 128, 0, s>>>(g, P);
-  if (g.fault) bdry_final_kernel<T><<<blocks((long long)g.cur.n[0] * g.cur.n[2]), 128, 0, s>>>(g, P, st);
+  if (pl.flux(0)) flux_kernel<0, T, Src><<<nb(K_FLF_0), 128, 0, s>>>(pl.src(K_FLF_0));
+  if (pl.flux(1)) flux_kernel<1, T, Src><<<nb(K_FLF_1), 128, 0, s>>>(pl.src(K_FLF_1));
+  if (pl.flux(2)) flux_kernel<2, T, Src><<<nb(K_FLF_2), 128, 0, s>>>(pl.src(K_FLF_2));
+  update_kernel<T, Src><<<nb(K_CUR), 128, 0, s>>>(pl.src(K_CUR));
+  if (pl.fault() && pl.n(K_BF)) bdry_final_kernel<T, Src><<<nb(K_BF), 128, 0, s>>>(pl.src(K_BF), P, st);
   return cudaGetLastError();
 }
 
 // FP64 instantiation (tmk_3d.cu, built without FMA contraction) and the mixed
 // form (tmk_3d_f32.cu)
-cudaError_t launch_step_f64(const Step3<double>& g, const DevParams* P, DevStatus* st, cudaStream_t s,
+cudaError_t launch_one_f64(const PlanOne<double>& pl, const DevParams* P, DevStatus* st, cudaStream_t s,
+                           const Side* side);
+cudaError_t launch_many_f64(const PlanMany<double>& pl, const DevParams* P, DevStatus* st, cudaStream_t s,
                             const Side* side);
-cudaError_t launch_step_f32(const Step3<float>& g, const DevParams* P, DevStatus* st, cudaStream_t s,
+cudaError_t launch_one_f32(const PlanOne<float>& pl, const DevParams* P, DevStatus* st, cudaStream_t s,
+                           const Side* side);
+cudaError_t launch_many_f32(const PlanMany<float>& pl, const DevParams* P, DevStatus* st, cudaStream_t s,
                             const Side* side);
 
 }  // namespace d3

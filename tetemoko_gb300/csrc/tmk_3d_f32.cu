@@ -5,9 +5,13 @@
 namespace tmk {
 namespace d3 {
 
-cudaError_t launch_step_f32(const Step3<float>& g, const DevParams* P, DevStatus* st, cudaStream_t s,
+cudaError_t launch_one_f32(const PlanOne<float>& pl, const DevParams* P, DevStatus* st, cudaStream_t s,
+                           const Side* side) {
+  return launch_plan<float>(pl, P, st, s, side);
+}
+cudaError_t launch_many_f32(const PlanMany<float>& pl, const DevParams* P, DevStatus* st, cudaStream_t s,
                             const Side* side) {
-  return launch_step<float>(g, P, st, s, side);
+  return launch_plan<float>(pl, P, st, s, side);
 }
 
 }  // namespace d3

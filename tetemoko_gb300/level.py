@@ -191,6 +191,33 @@ class LinElastPatchGodunov3D:
             self.dx, self.time, dt, C.byref(mws), _stream_ptr(stream)), "tmk_patch_update_state_3d")
         return mws.value, F
 
+    def update_states(self, patches, dt: float, stream=None):
+        """The level's patch loop in one batched call: `patches` is a list of
+        (valid box, U, ulo, B or None, blo); the patches' passes run as one
+        launch each over all of them.  Returns the max wave speed."""
+        n = len(patches)
+        Ua = (A.Fab3 * n)()
+        Ba = (A.Fab3 * n)()
+        Va = (A.Box3 * n)()
+        anyB = False
+        for p, (valid, U, ulo, B, blo) in enumerate(patches):
+            Ua[p] = _fab3(U, ulo)
+            Va[p] = A.box3(*valid)
+            if B is not None:
+                anyB = True
+                f = A.Fab3()
+                f.data = B.data_ptr()
+                f.lo[0], f.lo[1], f.lo[2] = blo[0], self.domain[0][1], blo[1]
+                f.hi[0], f.hi[1], f.hi[2] = blo[0] + B.shape[2] - 1, self.domain[0][1], blo[1] + B.shape[1] - 1
+                f.ncomp = B.shape[0]
+                Ba[p] = f
+        mws = C.c_double(0.0)
+        d = A.box3(*self.domain)
+        A.check(self.ctx.lib.tmk_patches_update_state_3d(
+            self.ctx.h, n, Ua, Ba if anyB else None, None, None, None, Va, C.byref(d), self.dx, self.time, dt,
+            C.byref(mws), _stream_ptr(stream)), "tmk_patches_update_state_3d")
+        return mws.value
+
     def plastic_update(self, U, ulo, dt: float, box=None, stream=None):
         b = A.box3(*(box or self.box))
         A.check(self.ctx.lib.tmk_plastic_update_3d(self.ctx.h, C.byref(_fab3(U, ulo)), C.byref(b), dt,
