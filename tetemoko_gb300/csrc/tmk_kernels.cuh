@@ -173,10 +173,21 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
   const int fa = (s0 == p.vlo0) ? max(p.vlo0 - 1, p.dlo0) : s0;
   const int fb = (s1 == p.vhi0) ? min(p.vhi0 + 1, p.dhi0) : s1;
   const int tid = threadIdx.x;
-  Consts<T> k; k.load(P);
   const double dt = p.dt, dx = p.dx;
-  T sig[9];
-  make_sig(P, dt / dx, sig);
+  // the constants once per CTA: computed per thread they were hundreds of FP64
+  // divisions and products queued on GB300's narrow FP64 pipe before any face
+  // could start
+  __shared__ Consts<T> sk;
+  __shared__ Consts<double> skd;
+  __shared__ T ssig[9];
+  if (tid == 0) {
+    sk.load(P);
+    skd.load(P);
+    make_sig(P, dt / dx, ssig);
+  }
+  __syncthreads();
+  const Consts<T>& k = sk;
+  const T* sig = ssig;
   const bool lim = P.prim_lim || P.char_lim;
   const int bs = p.bnx;
 
@@ -280,7 +291,7 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
     }
     if (it > RS_IMAX) atomicAdd(&st->newton_maxed, 1ull);
     // (F) y fluxes through the fault face (GETFLUXF, FP64)
-    Consts<double> kd; kd.load(P);
+    const Consts<double>& kd = skd;
     double F[NSIDE];
     double* ff = p.ffault + (i - p.vlo0);
     const int nv = p.vhi0 - p.vlo0 + 1;
