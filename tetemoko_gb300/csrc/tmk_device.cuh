@@ -478,6 +478,55 @@ TMK_D void ppm_predict(const Consts<T>& k, T rv, const T (*w5)[5], const bool* i
   for (int c = 0; c < NSIDE; ++c) { WM[c] += w5[c][2]; WP[c] += w5[c][2]; }
 }
 
+// PPM normal predictor of one side of one cell with primitive limiting, for
+// the mixed forms (the 3-D passes, the fault-row predictors): the stages of ppm_predict with the domain-edge cases as
+// selects instead of branches (a warp along x holds edge and inner cells), and
+// the tracing of each characteristic with the coefficients of its known
+// direction -- the waves (-cp, -cs, -cs) move to the lo face, (cs, cs, cp) to
+// the hi face:
+//   lo-going  m <- m + A (p - m) - B (m + p),  A = s/2, B = 3 (s/2 - s^2/3)
+//   hi-going  p <- p - A (p - m) - B (m + p),  A = s/2, B = (3/2) s (1 - 2s/3)
+// with s = |lambda| dt/dx (Colella & Woodward 1984 eq. 1.12).
+// Van Leer limited slope of w0 with neighbours wm, wp (one-sided next to a
+// domain edge, zero with neither neighbour)
+template <typename T>
+TMK_D T vl_lim(T wm, T w0, T wp, bool hasL, bool hasR) {
+  const T dL = w0 - wm, dR = wp - w0;
+  const T dl = hasL ? dL : dR, dr = hasR ? dR : dL;
+  const T dc = (hasL && hasR) ? T(0.5) * (wp - wm) : dl;
+  const T m = fmin(fabs(dc), T(2) * fmin(fabs(dl), fabs(dr)));
+  return (dl * dr > T(0) && (hasL || hasR)) ? copysign(m, dc) : T(0);
+}
+
+template <int D, typename T>
+TMK_D void ppm_predict_prim(const Consts<T>& k, T rv, const T (*w5)[5], const bool* in, const T* trA, const T* trB,
+                            T* WM, T* WP) {
+  T dm[NSIDE], dp[NSIDE];
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) {
+    const T* w = w5[c];
+    const T sm = in[1] ? vl_lim(w[0], w[1], w[2], in[0], true) : T(0);
+    const T s0 = vl_lim(w[1], w[2], w[3], in[1], in[3]);
+    const T sp = in[3] ? vl_lim(w[2], w[3], w[4], true, in[4]) : T(0);
+    const T flo = in[1] ? T(0.5) * (w[1] + w[2]) - (s0 - sm) * T(1.0 / 6.0) : w[2] - T(0.5) * s0;
+    const T fhi = in[3] ? T(0.5) * (w[2] + w[3]) - (sp - s0) * T(1.0 / 6.0) : w[2] + T(0.5) * s0;
+    T m = flo - w[2], p = fhi - w[2];
+    ppm_limit(m, p);
+    dm[c] = m; dp[c] = p;
+  }
+  T cm[NSIDE], cp[NSIDE];
+  char_analysis<D>(k, rv, dm, cm);
+  char_analysis<D>(k, rv, dp, cp);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) cm[c] = cm[c] + trA[c] * (cp[c] - cm[c]) - trB[c] * (cm[c] + cp[c]);
+#pragma unroll
+  for (int c = 6; c < 9; ++c) cp[c] = cp[c] - trA[c] * (cp[c] - cm[c]) - trB[c] * (cm[c] + cp[c]);
+  char_synthesis<D>(k, rv, cm, WM);
+  char_synthesis<D>(k, rv, cp, WP);
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) { WM[c] += w5[c][2]; WP[c] += w5[c][2]; }
+}
+
 // -------------------------------------------------------- status reporting
 enum : int { ST_OK = 0, ST_NAN = 2, ST_TIMEOUT = 3 };
 struct DevStatus {

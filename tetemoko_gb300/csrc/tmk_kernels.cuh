@@ -68,9 +68,18 @@ TMK_D void make_sig(const DevParams& P, double dtbydx, T* sig) {
 // =============================================================== fault kernel
 // Predicted state of one side's 11 components at (i, j0) in y, in arithmetic T
 // (lambda, gamma carry only their limited PPM delta: zero characteristic speed).
+// `tr` (the tracing coefficients A then B of ppm_predict_prim, mixed form with
+// PPM and primitive limiting) selects the branch-free predictor.
+template <int D, typename T>
+TMK_D void fault_pred(const DevParams& P, const Consts<T>& k, T rv, const T (*w5)[5], const bool* in, const T* sig,
+                      const T* tr, T* WM, T* WP) {
+  if (tr) ppm_predict_prim<D, T>(k, rv, w5, in, tr, tr + NSIDE, WM, WP);
+  else ppm_predict<D, T>(k, rv, w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM, WP, P.order, P.fourth != 0);
+}
+
 template <typename Real, typename T>
 TMK_D void fault_ypred_side(const PatchDev<Real>& p, const DevParams& P, const Consts<T>& k, int s, int i,
-                            const T* sig, bool lim, double* out11) {
+                            const T* sig, const T* tr, bool lim, double* out11) {
   const int j0 = p.dlo1;
   bool in[5] = {false, false, true, j0 + 1 <= p.dhi1, j0 + 2 <= p.dhi1};
   T w5[NSIDE][5];
@@ -78,7 +87,7 @@ TMK_D void fault_ypred_side(const PatchDev<Real>& p, const DevParams& P, const C
     for (int m = 0; m < 5; ++m) w5[c][m] = in[m] ? (T)p.Uin[fab_idx(p, 11 * s + c, i, j0 - 2 + m)] : T(0);
   T WM[NSIDE], WP[NSIDE];
   T rv = (s == 1) ? T(-1) : T(1);
-  ppm_predict<1, T>(k, rv, w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM, WP, P.order, P.fourth != 0);
+  fault_pred<1, T>(P, k, rv, w5, in, sig, tr, WM, WP);
   // the zero-speed components of the y direction reach no face component that
   // is read downstream (live9): not predicted
   for (int c = 0; c < NSIDE; ++c) out11[c] = live9<1>(c) ? (double)WM[c] : 0.0;
@@ -106,14 +115,14 @@ TMK_D void fault_ypred_side(const PatchDev<Real>& p, const DevParams& P, const C
 // x-direction predicted states (WM, WP) of one side at cell (i, j0)
 template <typename Real, typename T>
 TMK_D void fault_xpred_side(const PatchDev<Real>& p, const DevParams& P, const Consts<T>& k, int s, int i,
-                            const T* sig, T* WM, T* WP) {
+                            const T* sig, const T* tr, T* WM, T* WP) {
   const int j0 = p.dlo1;
   bool in[5];
   for (int m = 0; m < 5; ++m) in[m] = (i - 2 + m >= p.dlo0) && (i - 2 + m <= p.dhi0);
   T w5[NSIDE][5];
   for (int c = 0; c < NSIDE; ++c)
     for (int m = 0; m < 5; ++m) w5[c][m] = in[m] ? (T)p.Uin[fab_idx(p, 11 * s + c, i - 2 + m, j0)] : T(0);
-  ppm_predict<0, T>(k, T(1), w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM, WP, P.order, P.fourth != 0);
+  fault_pred<0, T>(P, k, T(1), w5, in, sig, tr, WM, WP);
 }
 
 // x face state (first pass) of one side at face f of row j0 from the cells
@@ -180,14 +189,23 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
   __shared__ Consts<T> sk;
   __shared__ Consts<double> skd;
   __shared__ T ssig[9];
+  __shared__ T str[2 * NSIDE];     // tracing coefficients of the branch-free predictor
+  const bool fastpred = !kExact<T> && P.order == 2 && P.prim_lim && !P.char_lim;
   if (tid == 0) {
     sk.load(P);
     skd.load(P);
     make_sig(P, dt / dx, ssig);
+    if (fastpred)
+      for (int q = 0; q < NSIDE; ++q) {
+        const double sv = fabs((double)ssig[q]);
+        str[q] = (T)(0.5 * sv);
+        str[NSIDE + q] = (T)(q < 3 ? 3.0 * (0.5 * sv - sv * sv / 3.0) : 1.5 * sv * (1.0 - (2.0 / 3.0) * sv));
+      }
   }
   __syncthreads();
   const Consts<T>& k = sk;
   const T* sig = ssig;
+  const T* tr = fastpred ? str : nullptr;
   const bool lim = P.prim_lim || P.char_lim;
   const int bs = p.bnx;
 
@@ -206,7 +224,7 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
     if (kind == 0) {
       if (c >= p.dlo0 && c <= p.dhi0 && c <= s1 + 1) {
         T WM[NSIDE], WP[NSIDE];
-        fault_xpred_side(p, P, k, s, c, sig, WM, WP);
+        fault_xpred_side(p, P, k, s, c, sig, tr, WM, WP);
         // the x faces' zero-speed components are never read (live9): not predicted
         for (int q = 0; q < NSIDE; ++q) {
           xWM[s][ci][q] = live9<0>(q) ? WM[q] : T(0);
@@ -214,7 +232,7 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
         }
       }
     } else if (c >= fa && c <= fb) {
-      fault_ypred_side(p, P, k, s, c, sig, lim, &sWi[ci][11 * s]);
+      fault_ypred_side(p, P, k, s, c, sig, tr, lim, &sWi[ci][11 * s]);
     }
   }
   __syncthreads();
