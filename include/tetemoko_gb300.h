@@ -259,7 +259,12 @@ typedef struct { int lo[3], hi[3]; } tmk_box3;   /* cell-centred, inclusive */
  * boundary data, a device FAB3 with lo[1] = hi[1] = domain lo[1] covering
  * grow(valid, 1) & domain in x and z (nbdry comps); else ignored.  F0, F1, F2:
  * optional device FAB3s over the faces of valid in x, y, z (22 comps) that
- * receive the fluxes (for the flux registers). */
+ * receive the fluxes (for the flux registers).  scheme.precision picks the FP64
+ * form or the mixed one (FP32 volume arithmetic; U, friction and boundary data
+ * stay FP64).  The intermediates live in the context's scratch, so calls on
+ * one context are ordered on one stream; the first call of a context with
+ * fault faces creates its second stream and events (make it before any
+ * stream capture). */
 tmk_status tmk_patch_update_state_3d(tmk_context* ctx, const tmk_fab3* U, const tmk_fab3* B,
                                      const tmk_fab3* F0, const tmk_fab3* F1, const tmk_fab3* F2,
                                      const tmk_box3* valid, const tmk_box3* domain,
