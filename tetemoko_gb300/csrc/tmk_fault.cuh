@@ -433,13 +433,25 @@ TMK_D double sw_setbnd(const DevParams& P, const double* U, double* B, int bstri
   return st;
 }
 
-// PLASTICFLOW (srcLinElast/PlasticPhysicsF.ChF:74-181) on one side's stresses;
-// returns whether the point yielded (else only p_lam, set to 0, changed)
+// The plasticity parameters (PLASTICSETF) and moduli in arithmetic T.
 template <typename T>
-TMK_D bool plastic_flow(const DevParams& P, T& sxx, T& syy, T& szz, T& sxy, T& sxz, T& syz, T& p_lam,
-                        T& p_gam, T dt) {
-  const T mu = (T)P.p_mu, beta = (T)P.p_beta, eta = (T)P.p_eta, pb = (T)P.p_b, ph = (T)P.p_h;
-  const T G = (T)P.G, K = (T)P.K;
+struct PlasticK {
+  T mu, beta, eta, pb, ph, G, K;
+  TMK_HD void load(const DevParams& P) {
+    mu = (T)P.p_mu; beta = (T)P.p_beta; eta = (T)P.p_eta; pb = (T)P.p_b; ph = (T)P.p_h;
+    G = (T)P.G; K = (T)P.K;
+  }
+};
+
+// PLASTICFLOW (srcLinElast/PlasticPhysicsF.ChF:74-181) on one side's stresses;
+// returns whether the point yielded (else only p_lam, set to 0, changed).  The
+// parameters come in T already: a pass over many cells converts them once (on
+// GB300 each FP64-to-FP32 conversion uses the narrow FP64 pipe).
+template <typename T>
+TMK_D bool plastic_flow_k(const PlasticK<T>& c, T& sxx, T& syy, T& szz, T& sxy, T& sxz, T& syz, T& p_lam,
+                          T& p_gam, T dt) {
+  const T mu = c.mu, beta = c.beta, eta = c.eta, pb = c.pb, ph = c.ph;
+  const T G = c.G, K = c.K;
   T sigma = (sxx + syy + szz) / T(3);
   T J2 = ((sxx - syy) * (sxx - syy) + (syy - szz) * (syy - szz) + (szz - sxx) * (szz - sxx)) / T(6) +
          sxy * sxy + sxz * sxz + syz * syz;
@@ -460,6 +472,15 @@ TMK_D bool plastic_flow(const DevParams& P, T& sxx, T& syy, T& szz, T& sxy, T& s
   sxz = factor * sxz;
   syz = factor * syz;
   return true;
+}
+
+// the same from the scenario's parameters
+template <typename T>
+TMK_D bool plastic_flow(const DevParams& P, T& sxx, T& syy, T& szz, T& sxy, T& sxz, T& syz, T& p_lam,
+                        T& p_gam, T dt) {
+  PlasticK<T> c;
+  c.load(P);
+  return plastic_flow_k<T>(c, sxx, syy, szz, sxy, sxz, syz, p_lam, p_gam, dt);
 }
 
 }  // namespace tmk

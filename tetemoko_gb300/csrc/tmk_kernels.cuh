@@ -567,8 +567,16 @@ __global__ void __launch_bounds__(256) plastic_tiles_kernel(const PatchDev<Real>
   using T = Real;
   const TileDev tl = tiles[blockIdx.x];
   const PatchDev<Real>& p = patches[tl.patch];
-  const DevParams& P = params[p.scen];
-  const T dt = (T)p.dt;
+  // the parameters in T once per CTA (FP64-to-FP32 conversions use GB300's
+  // narrow FP64 pipe: per cell they were the pass's bound)
+  __shared__ PlasticK<T> sk;
+  __shared__ T sdt;
+  if (threadIdx.x == 0) {
+    sk.load(params[p.scen]);
+    sdt = (T)p.dt;
+  }
+  __syncthreads();
+  const T dt = sdt;
   for (int idx = threadIdx.x; idx < tl.nx * tl.ny; idx += blockDim.x) {
     const int x = tl.x0 + idx % tl.nx, y = tl.y0 + idx / tl.nx;
 #pragma unroll
@@ -580,7 +588,7 @@ __global__ void __launch_bounds__(256) plastic_tiles_kernel(const PatchDev<Real>
       T lam;                                   // the plastic rate is only written
       T gam = p.Uin[fab_idx(p, O + 10, x, y)];
       // the stresses are stored back only where the point yielded (else unchanged)
-      if (plastic_flow<T>(P, u[0], u[1], u[2], u[3], u[4], u[5], lam, gam, dt)) {
+      if (plastic_flow_k<T>(sk, u[0], u[1], u[2], u[3], u[4], u[5], lam, gam, dt)) {
 #pragma unroll
         for (int c = 0; c < 6; ++c) p.Uout[fab_idx(p, O + 3 + c, x, y)] = u[c];
       }
