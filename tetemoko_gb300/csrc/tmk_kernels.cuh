@@ -579,21 +579,27 @@ __global__ void __launch_bounds__(256) plastic_tiles_kernel(const PatchDev<Real>
   const T dt = sdt;
   for (int idx = threadIdx.x; idx < tl.nx * tl.ny; idx += blockDim.x) {
     const int x = tl.x0 + idx % tl.nx, y = tl.y0 + idx / tl.nx;
+    const size_t o = fab_idx(p, 0, x, y), plane = (size_t)p.anx * p.any;
+    // both sides' stresses and hardening first: the stores below may alias
+    // them for the compiler, which would otherwise wait for one side's stores
+    // before loading the other's
+    T u[2][6], gam[2];
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      const int O = 11 * s;
-      T u[6];
 #pragma unroll
-      for (int c = 0; c < 6; ++c) u[c] = p.Uout[fab_idx(p, O + 3 + c, x, y)];
+      for (int c = 0; c < 6; ++c) u[s][c] = p.Uout[o + (size_t)(11 * s + 3 + c) * plane];
+      gam[s] = p.Uin[o + (size_t)(11 * s + 10) * plane];
+    }
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
       T lam;                                   // the plastic rate is only written
-      T gam = p.Uin[fab_idx(p, O + 10, x, y)];
       // the stresses are stored back only where the point yielded (else unchanged)
-      if (plastic_flow_k<T>(sk, u[0], u[1], u[2], u[3], u[4], u[5], lam, gam, dt)) {
+      if (plastic_flow_k<T>(sk, u[s][0], u[s][1], u[s][2], u[s][3], u[s][4], u[s][5], lam, gam[s], dt)) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) p.Uout[fab_idx(p, O + 3 + c, x, y)] = u[c];
+        for (int c = 0; c < 6; ++c) p.Uout[o + (size_t)(11 * s + 3 + c) * plane] = u[s][c];
       }
-      p.Uout[fab_idx(p, O + 9, x, y)] = lam;
-      p.Uout[fab_idx(p, O + 10, x, y)] = gam;
+      p.Uout[o + (size_t)(11 * s + 9) * plane] = lam;
+      p.Uout[o + (size_t)(11 * s + 10) * plane] = gam[s];
     }
   }
 }
