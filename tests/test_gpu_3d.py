@@ -336,3 +336,68 @@ def test_batched_patches_equal_the_whole_domain_step(cuda_lib, name, prec):
                 else:
                     assert rel_err(b, ref) <= 1e-12
     ctx.close()
+
+
+def _run_rupture_3d(sc, nz, nsteps, stations, kmid):
+    """A z-uniform rate-and-state nucleation on one 3-D patch (outflow z
+    faces): fault slip-rate history at the stations of row kmid, and the final
+    state and fault data."""
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    nx, ny = sc.nx, sc.ny
+    lo, hi = (0, 0, 0), (nx - 1, ny - 1, nz - 1)
+    U0 = np.empty((22, nz + 2 * G, ny + 2 * G, nx + 2 * G))
+    U0[:] = sc.background()[:, None, None, None]
+    B0 = np.ascontiguousarray(np.repeat(sc.initial_B()[:, None, :], nz + 2 * G, axis=1))
+    ctx = Context(sc)
+    pg = LinElastPatchGodunov3D(ctx, (lo, hi))
+    pg.set_current_box((lo, hi))
+    U = torch.from_numpy(U0).cuda()
+    B = torch.from_numpy(B0).cuda()
+    dt, t = sc.dt() / 3 ** 0.5, 0.0
+    idx = torch.tensor([i + G for i in stations], device="cuda")
+    hist, ts = [], []
+    for _ in range(nsteps):
+        pg.set_current_time(t)
+        pg.update_state(U, (-G, -G, -G), dt, B=B, blo=(-G, -G))
+        t += dt
+        hist.append(B[2, kmid + G].index_select(0, idx).clone())
+        ts.append(t)
+    torch.cuda.synchronize()
+    out = (np.array(ts), torch.stack(hist).cpu().numpy(), U.cpu().numpy(), B.cpu().numpy())
+    ctx.close()
+    return out
+
+
+def test_mixed_3d_rupture_metrics_vs_fp64(cuda_lib):
+    """The 3-D mixed form through nucleation and rupture against the 3-D FP64
+    form (equal to the oracle per step): rupture arrival at fault stations 2-6 km
+    either side of the nucleation (0.5 %), final slip (1e-3), peak slip rate
+    (1e-2) and the particle velocities of the volume (1e-2), as the 2-D mixed
+    form's rupture test."""
+    from tests.test_gpu_mixed import _arrival
+    nz, nsteps = 8, 450
+    sc64 = S.rate_state(nx=192, ny=64, dx=0.1)
+    scm = S.rate_state(nx=192, ny=64, dx=0.1, precision=A.TMK_PREC_MIXED)
+    x0 = sc64.rs.x0
+    st = [int(round((x0 + s * d) / sc64.dx - 0.5)) for d in (2.0, 4.0, 6.0) for s in (-1, 1)]
+    kmid = nz // 2
+    tr, Vr, Ur, Br = _run_rupture_3d(sc64, nz, nsteps, st, kmid)
+    tm, Vm, Um, Bm = _run_rupture_3d(scm, nz, nsteps, st, kmid)
+    thr = sc64.rs.rupture_threshold
+    ar, am = _arrival(tr, Vr, thr), _arrival(tm, Vm, thr)
+    assert np.all(np.isfinite(ar)), "every station must rupture within the run"
+    arr_err = np.max(np.abs(am - ar) / ar)
+    sl = [i + G for i in st]
+    slip_r, slip_m = Br[8, kmid + G, sl], Bm[8, kmid + G, sl]
+    slip_err = np.max(np.abs(slip_m - slip_r) / np.abs(slip_r))
+    peak_err = np.max(np.abs(Vm.max(axis=0) - Vr.max(axis=0)) / Vr.max(axis=0))
+    vcomp = [0, 1, 2, 11, 12, 13]
+    vs = (vcomp, slice(G, -G), slice(G, -G), slice(G, -G))
+    vel_err = np.abs(Um[vs] - Ur[vs]).max() / np.abs(Ur[vs]).max()
+    print(f"3-D mixed vs FP64: arrival {arr_err:.2e}, final slip {slip_err:.2e}, "
+          f"peak slip rate {peak_err:.2e}, volume velocity {vel_err:.2e}")
+    assert arr_err < 5e-3
+    assert slip_err < 1e-3
+    assert peak_err < 1e-2
+    assert vel_err < 1e-2
