@@ -51,7 +51,12 @@ Bx bx_of(const int lo[3], const int hi[3]) {
   for (int d = 0; d < 3; ++d) { b.lo[d] = lo[d]; b.n[d] = hi[d] - lo[d] + 1; }
   return b;
 }
-bool bx_ok(const Bx& b) { return b.n[0] > 0 && b.n[1] > 0 && b.n[2] > 0; }
+// a non-empty box whose node box holds fewer than 2^31 points (the kernels
+// index the cells of a box, and of its node boxes, in 32 bits)
+bool bx_ok(const Bx& b) {
+  return b.n[0] > 0 && b.n[1] > 0 && b.n[2] > 0 &&
+         (long long)(b.n[0] + 1) * (b.n[1] + 1) * (b.n[2] + 1) < (1LL << 31);
+}
 int bx_hi(const Bx& b, int d) { return b.lo[d] + b.n[d] - 1; }
 bool bx_contains(const Bx& a, const Bx& b) {
   for (int d = 0; d < 3; ++d)

@@ -10,13 +10,15 @@
 //   riem1<D>     first-pass face states WHalf1[D] (Riemann solve, or the
 //                domain-edge / fault condition)
 //   riem2<D1,D2> WHalf2[D1][D2]: the D1 face states after the normal states
-//                were moved by -(1/3) dt/dx A dW/dx of WHalf1[D2] (:329-381)
+//                were moved by -(1/3) dt/dx A dW/dx of WHalf1[D2] (:329-381);
+//                both D2 of a D1 in one pass (riem2_pair) that reads the
+//                normal states once
 //   final<D1>    the time-centred WHalf[D1], normal states moved by both
 //                WHalf2[D2][D3] with -(1/2) dt/dx (:422-440)
 //   update       fluxes, their divergence and U += -dt/dx dU in place; then
 //                the fault's boundary data (RSSETBND / SWSETBND, final)
-// Cell states (WM, WP) are stored with 18 components, face states with the 12
-// that the transverse terms and the fluxes read.
+// Cell states (WM, WP) and face states are stored with the 12 components that
+// the transverse terms and the fluxes read.
 // The fault is the y-lo plane of the domain.  Its boundary data predicted at
 // (1/3) dt from WHalf1[1] and at (1/2) dt from WHalf2[1][2] (the reference's
 // call order leaves those in m_tmpBdryData when WHalf2[1][*] and WHalf[1] are
@@ -48,11 +50,15 @@ struct Bx {
   TMK_HD long long at(int i, int j, int k) const {
     return ((long long)(k - lo[2]) * n[1] + (j - lo[1])) * n[0] + (i - lo[0]);
   }
+  // t < cells() < 2^31 (every box of a step lies in the nodes of U's box,
+  // whose node count the host keeps below 2^31): 32-bit unsigned division,
+  // several times cheaper on the GPU than the 64-bit one.
   TMK_HD void cell(long long t, int& i, int& j, int& k) const {
-    i = lo[0] + (int)(t % n[0]);
-    long long r = t / n[0];
-    j = lo[1] + (int)(r % n[1]);
-    k = lo[2] + (int)(r / n[1]);
+    const unsigned u = (unsigned)t, n0 = (unsigned)n[0], n1 = (unsigned)n[1];
+    const unsigned r = u / n0, q = r / n1;
+    i = lo[0] + (int)(u - r * n0);
+    j = lo[1] + (int)(r - q * n1);
+    k = lo[2] + (int)q;
   }
 };
 
@@ -142,20 +148,21 @@ template <int D> TMK_D int coord(int i, int j, int k) { return D == 0 ? i : (D =
 // the friction solves, long chains of dependent FP64 operations, then start
 // with the grid and run beside the bulk instead of trailing it.
 TMK_D void face_fault_first(const Bx& fb, bool fault, long long t, int& i, int& j, int& k) {
-  const long long nf = (long long)fb.n[0] * fb.n[2];
   if (!fault) { fb.cell(t, i, j, k); return; }
-  if (t < nf) {
-    i = fb.lo[0] + (int)(t % fb.n[0]);
+  const unsigned nx = (unsigned)fb.n[0], nf = nx * (unsigned)fb.n[2];
+  unsigned u = (unsigned)t;
+  if (u < nf) {
+    const unsigned q = u / nx;
+    i = fb.lo[0] + (int)(u - q * nx);
     j = fb.lo[1];
-    k = fb.lo[2] + (int)(t / fb.n[0]);
+    k = fb.lo[2] + (int)q;
     return;
   }
-  t -= nf;
-  const int ny = fb.n[1] - 1;
-  i = fb.lo[0] + (int)(t % fb.n[0]);
-  const long long r = t / fb.n[0];
-  j = fb.lo[1] + 1 + (int)(r % ny);
-  k = fb.lo[2] + (int)(r / ny);
+  u -= nf;
+  const unsigned ny = (unsigned)fb.n[1] - 1, r = u / nx, q = r / ny;
+  i = fb.lo[0] + (int)(u - r * nx);
+  j = fb.lo[1] + 1 + (int)(r - q * ny);
+  k = fb.lo[2] + (int)q;
 }
 template <int D> TMK_D void face_at(const Bx& fb, bool fault, long long t, int& i, int& j, int& k) {
   if (D == 1) face_fault_first(fb, fault, t, i, j, k);
@@ -400,12 +407,11 @@ __global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Src 
   riem1_body<D, T>(*gp, *Pp, st, part, lt);
 }
 
-// cell state T18 of array A (direction-D1 normal states) at (i, j, k), moved by
-// -(scale) A dW/dx of the face states H in direction D2 where the cell lies in ccBox[D2]
-template <int D1, int D2, typename T>
-TMK_D void corrected(const Step3<T>& g, const Consts<T>& kc, const T* A, const T* H, const Bx& hb, T scale, int i,
-                     int j, int k, T* T18) {
-  load_face<D1>(A, g.S, i, j, k, T18);
+// cell state T18 (direction-D1 normal states) at (i, j, k) moved by -(scale)
+// A dW/dx of the face states H in direction D2 where the cell lies in ccBox[D2]
+template <int D2, typename T>
+TMK_D void add_transverse(const Step3<T>& g, const Consts<T>& kc, const T* H, const Bx& hb, T scale, int i, int j,
+                          int k, T* T18) {
   if (!g.cc[D2].has(i, j, k)) return;
   T h[NS], l[NS];
   int hi = i, hj = j, hk = k;
@@ -418,34 +424,81 @@ TMK_D void corrected(const Step3<T>& g, const Consts<T>& kc, const T* A, const T
 }
 
 // ----------------------------------------------------------- second pass
+// The normal states WP[D1] of the left and WM[D1] of the right cell of the D1
+// face (i, j, k), where those cells lie in the domain.
+template <int D1, typename T>
+TMK_D void riem2_load(const Step3<T>& g, int i, int j, int k, bool hasL, bool hasR, T* L0, T* R0) {
+  int li = i, lj = j, lk = k;
+  step<D1>(li, lj, lk, -1);
+  if (hasL) load_face<D1>(g.WP[D1], g.S, li, lj, lk, L0);
+  if (hasR) load_face<D1>(g.WM[D1], g.S, i, j, k, R0);
+}
+
+// WHalf2[D1][D2] at the D1 face (i, j, k) from the normal states L0, R0 of its
+// two cells: the transverse corrections of WHalf1[D2], then the Riemann solve
+// or the face's condition.
+template <int D1, int D2, typename T>
+TMK_D void riem2_solve(const Step3<T>& g, const DevParams& P, DevStatus* st, int i, int j, int k, bool hasL,
+                       bool hasR, const T* L0, const T* R0) {
+  const Consts<T>& kc = g.kc;
+  const T scale = g.scale3;
+  T L[NS], R[NS], G[NS];
+  if (hasL) {
+    int li = i, lj = j, lk = k;
+    step<D1>(li, lj, lk, -1);
+#pragma unroll
+    for (int c = 0; c < NS; ++c) L[c] = L0[c];
+    add_transverse<D2, T>(g, kc, g.WH1[D2], g.fl1[D2], scale, li, lj, lk, L);
+  }
+  if (hasR) {
+#pragma unroll
+    for (int c = 0; c < NS; ++c) R[c] = R0[c];
+    add_transverse<D2, T>(g, kc, g.WH1[D2], g.fl1[D2], scale, i, j, k, R);
+  }
+  if (!face_state<D1, T>(P, kc, g, coord<D1>(i, j, k), L, R, G)) {
+    double U22[NC];
+    load_ff(g, g.FF[0], i, k, U22);
+    const double bval = bdry_value(P, g, i, k, U22, (1.0 / 3.0) * g.dt);
+    fault_solve(P, g, i, k, R, bval, (D2 == 2) ? g.FF[1] : nullptr, G, st);
+  }
+  store_face<D1>(g.WH2[D1][D2], g.fl1[D1], i, j, k, G);
+}
+
 template <int D1, int D2, typename T>
 TMK_D void riem2_face(const Step3<T>& g, const DevParams& P, DevStatus* st, int part, long long t) {
   const Bx& fb = g.fl1[D1];
   if (t >= part_faces<D1>(fb, g.fault != 0, part)) return;
   int i, j, k;
   part_face<D1>(fb, g.fault != 0, part, t, i, j, k);
-  const Consts<T>& kc = g.kc;
-  const T scale = g.scale3;
   const int f = coord<D1>(i, j, k);
-  T L[NS], R[NS], G[NS];
-  int li = i, lj = j, lk = k;
-  step<D1>(li, lj, lk, -1);
-  if (f > g.dlo[D1]) corrected<D1, D2, T>(g, kc, g.WP[D1], g.WH1[D2], g.fl1[D2], scale, li, lj, lk, L);
-  if (f <= g.dhi[D1]) corrected<D1, D2, T>(g, kc, g.WM[D1], g.WH1[D2], g.fl1[D2], scale, i, j, k, R);
-  if (!face_state<D1, T>(P, kc, g, f, L, R, G)) {
-    double U22[NC];
-    load_ff(g, g.FF[0], i, k, U22);
-    const double bval = bdry_value(P, g, i, k, U22, (1.0 / 3.0) * g.dt);
-    fault_solve(P, g, i, k, R, bval, (D2 == 2) ? g.FF[1] : nullptr, G, st);
-  }
-  store_face<D1>(g.WH2[D1][D2], fb, i, j, k, G);
+  const bool hasL = f > g.dlo[D1], hasR = f <= g.dhi[D1];
+  T L0[NS], R0[NS];
+  riem2_load<D1, T>(g, i, j, k, hasL, hasR, L0, R0);
+  riem2_solve<D1, D2, T>(g, P, st, i, j, k, hasL, hasR, L0, R0);
 }
 
-template <int D1, int D2, typename T, typename Src>
-__global__ void __launch_bounds__(128) riem2_kernel(const __grid_constant__ Src src, const DevParams* Pp,
-                                                    DevStatus* st, int part) {
+// WHalf2[D1][Da] and WHalf2[D1][Db] (Da, Db the other two directions) at a D1
+// face, the normal states read once for both
+template <int D1, typename T>
+TMK_D void riem2_pair_face(const Step3<T>& g, const DevParams& P, DevStatus* st, int part, long long t) {
+  constexpr int Da = D1 == 0 ? 1 : 0, Db = D1 == 2 ? 1 : 2;
+  const Bx& fb = g.fl1[D1];
+  if (t >= part_faces<D1>(fb, g.fault != 0, part)) return;
+  int i, j, k;
+  part_face<D1>(fb, g.fault != 0, part, t, i, j, k);
+  const int f = coord<D1>(i, j, k);
+  const bool hasL = f > g.dlo[D1], hasR = f <= g.dhi[D1];
+  T L0[NS], R0[NS];
+  riem2_load<D1, T>(g, i, j, k, hasL, hasR, L0, R0);
+  riem2_solve<D1, Da, T>(g, P, st, i, j, k, hasL, hasR, L0, R0);
+  riem2_solve<D1, Db, T>(g, P, st, i, j, k, hasL, hasR, L0, R0);
+}
+
+template <int D1, typename T, typename Src>
+__global__ void __launch_bounds__(128) riem2_pair_kernel(const __grid_constant__ Src src, const DevParams* Pp,
+                                                         DevStatus* st, int part) {
   TMK3_FIND(T)
-  riem2_face<D1, D2, T>(*gp, *Pp, st, part, lt);
+  riem2_pair_face<D1, T>(*gp, *Pp, st, part, lt);
 }
 
 // WHalf2[1][0] and WHalf2[1][2] on the fault plane in one launch (grid y = 0,
@@ -703,9 +756,10 @@ struct Side {
 // plane (their friction solves are chains of dependent FP64 operations) run on
 // the side stream beside the bulk passes, forked and joined with events:
 //   side: [pred<1>] F1 = riem1<1> fault | [riem1<0>, riem1<2>] F2 = riem2<1,0> and riem2<1,2> fault (one launch)
-//         | [riem2<0,2>, riem2<2,0>] F3 = final<1> fault
-//   main: pred x3, riem1<0>, riem1<2>, riem1<1> bulk, riem2<0,2>, riem2<2,0>, riem2<1,*> bulk,
-//         [F1] riem2<0,1>, riem2<2,1>, final<1> bulk, [F2] final<0>, final<2>, [F3] update
+//         | [riem2<0,*>, riem2<2,*>] F3 = final<1> fault
+//   main: pred x3, riem1<0>, riem1<2>, riem1<1> bulk, [F1] riem2<0,*>, riem2<2,*>, riem2<1,*> bulk,
+//         final<1> bulk, [F2] final<0>, final<2>, [F3] update
+// (riem2<D1,*>: WHalf2[D1][D2] for both D2 != D1 in one pass.)
 // Each pass still reads exactly what the reference's order has written when
 // it runs; the passes on the two streams write disjoint faces.
 template <typename T, typename Plan>
@@ -742,18 +796,15 @@ cudaError_t launch_plan(const Plan& pl, const DevParams* P, DevStatus* st, cudaS
     cudaEventRecord(side->ev[4], fs);
   }
   riem1_kernel<1, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
-  riem2_kernel<0, 2, T, Src><<<nb(K_FL1_0), 128, 0, s>>>(pl.src(K_FL1_0), P, st, PART_ALL);
-  riem2_kernel<2, 0, T, Src><<<nb(K_FL1_2), 128, 0, s>>>(pl.src(K_FL1_2), P, st, PART_ALL);
+  join(3);
+  riem2_pair_kernel<0, T, Src><<<nb(K_FL1_0), 128, 0, s>>>(pl.src(K_FL1_0), P, st, PART_ALL);
+  riem2_pair_kernel<2, T, Src><<<nb(K_FL1_2), 128, 0, s>>>(pl.src(K_FL1_2), P, st, PART_ALL);
   fork(2);
   if (split) {
     final_kernel<1, T, Src><<<nb(K_FLF_1F), 128, 0, fs>>>(pl.src(K_FLF_1F), P, st, PART_FAULT);
     cudaEventRecord(side->ev[5], fs);
   }
-  riem2_kernel<1, 0, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
-  riem2_kernel<1, 2, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
-  join(3);
-  riem2_kernel<0, 1, T, Src><<<nb(K_FL1_0), 128, 0, s>>>(pl.src(K_FL1_0), P, st, PART_ALL);
-  riem2_kernel<2, 1, T, Src><<<nb(K_FL1_2), 128, 0, s>>>(pl.src(K_FL1_2), P, st, PART_ALL);
+  riem2_pair_kernel<1, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
   final_kernel<1, T, Src><<<nb(kf1), 128, 0, s>>>(pl.src(kf1), P, st, bulk);
   join(4);
   final_kernel<0, T, Src><<<nb(K_FLF_0), 128, 0, s>>>(pl.src(K_FLF_0), P, st, PART_ALL);
