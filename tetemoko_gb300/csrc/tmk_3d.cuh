@@ -383,7 +383,9 @@ TMK_D void load_ff(const Step3<T>& g, const double* FFk, int i, int k, double* U
 }
 
 // ------------------------------------------------------------ first pass
-template <int D, typename T>
+// FC = false: a launch without fault faces (the bulk part), built without the
+// friction solve's code and registers.
+template <int D, typename T, bool FC = true>
 TMK_D void riem1_body(const Step3<T>& g, const DevParams& P, DevStatus* st, int part, long long t) {
   const Bx& fb = g.fl1[D];
   if (t >= part_faces<D>(fb, g.fault != 0, part)) return;
@@ -396,15 +398,16 @@ TMK_D void riem1_body(const Step3<T>& g, const DevParams& P, DevStatus* st, int 
   step<D>(li, lj, lk, -1);
   if (f > g.dlo[D]) load_face<D>(g.WP[D], g.S, li, lj, lk, L);
   if (f <= g.dhi[D]) load_face<D>(g.WM[D], g.S, i, j, k, R);
-  if (!face_state<D, T>(P, kc, g, f, L, R, G))
-    fault_solve(P, g, i, k, R, bdry_value(P, g, i, k, nullptr, 0.0), g.FF[0], G, st);
+  if (!face_state<D, T>(P, kc, g, f, L, R, G)) {
+    if constexpr (FC) fault_solve(P, g, i, k, R, bdry_value(P, g, i, k, nullptr, 0.0), g.FF[0], G, st);
+  }
   store_face<D>(g.WH1[D], fb, i, j, k, G);
 }
-template <int D, typename T, typename Src>
+template <int D, typename T, typename Src, bool FC = true>
 __global__ void __launch_bounds__(128) riem1_kernel(const __grid_constant__ Src src, const DevParams* Pp,
                                                     DevStatus* st, int part) {
   TMK3_FIND(T)
-  riem1_body<D, T>(*gp, *Pp, st, part, lt);
+  riem1_body<D, T, FC>(*gp, *Pp, st, part, lt);
 }
 
 // cell state T18 (direction-D1 normal states) at (i, j, k) moved by -(scale)
@@ -437,7 +440,7 @@ TMK_D void riem2_load(const Step3<T>& g, int i, int j, int k, bool hasL, bool ha
 // WHalf2[D1][D2] at the D1 face (i, j, k) from the normal states L0, R0 of its
 // two cells: the transverse corrections of WHalf1[D2], then the Riemann solve
 // or the face's condition.
-template <int D1, int D2, typename T>
+template <int D1, int D2, typename T, bool FC = true>
 TMK_D void riem2_solve(const Step3<T>& g, const DevParams& P, DevStatus* st, int i, int j, int k, bool hasL,
                        bool hasR, const T* L0, const T* R0) {
   const Consts<T>& kc = g.kc;
@@ -456,6 +459,7 @@ TMK_D void riem2_solve(const Step3<T>& g, const DevParams& P, DevStatus* st, int
     add_transverse<D2, T>(g, kc, g.WH1[D2], g.fl1[D2], scale, i, j, k, R);
   }
   if (!face_state<D1, T>(P, kc, g, coord<D1>(i, j, k), L, R, G)) {
+    if constexpr (!FC) return;
     double U22[NC];
     load_ff(g, g.FF[0], i, k, U22);
     const double bval = bdry_value(P, g, i, k, U22, (1.0 / 3.0) * g.dt);
@@ -479,7 +483,7 @@ TMK_D void riem2_face(const Step3<T>& g, const DevParams& P, DevStatus* st, int 
 
 // WHalf2[D1][Da] and WHalf2[D1][Db] (Da, Db the other two directions) at a D1
 // face, the normal states read once for both
-template <int D1, typename T>
+template <int D1, typename T, bool FC>
 TMK_D void riem2_pair_face(const Step3<T>& g, const DevParams& P, DevStatus* st, int part, long long t) {
   constexpr int Da = D1 == 0 ? 1 : 0, Db = D1 == 2 ? 1 : 2;
   const Bx& fb = g.fl1[D1];
@@ -490,15 +494,15 @@ TMK_D void riem2_pair_face(const Step3<T>& g, const DevParams& P, DevStatus* st,
   const bool hasL = f > g.dlo[D1], hasR = f <= g.dhi[D1];
   T L0[NS], R0[NS];
   riem2_load<D1, T>(g, i, j, k, hasL, hasR, L0, R0);
-  riem2_solve<D1, Da, T>(g, P, st, i, j, k, hasL, hasR, L0, R0);
-  riem2_solve<D1, Db, T>(g, P, st, i, j, k, hasL, hasR, L0, R0);
+  riem2_solve<D1, Da, T, FC>(g, P, st, i, j, k, hasL, hasR, L0, R0);
+  riem2_solve<D1, Db, T, FC>(g, P, st, i, j, k, hasL, hasR, L0, R0);
 }
 
-template <int D1, typename T, typename Src>
+template <int D1, typename T, typename Src, bool FC = true>
 __global__ void __launch_bounds__(128) riem2_pair_kernel(const __grid_constant__ Src src, const DevParams* Pp,
                                                          DevStatus* st, int part) {
   TMK3_FIND(T)
-  riem2_pair_face<D1, T>(*gp, *Pp, st, part, lt);
+  riem2_pair_face<D1, T, FC>(*gp, *Pp, st, part, lt);
 }
 
 // WHalf2[1][0] and WHalf2[1][2] on the fault plane in one launch (grid y = 0,
@@ -535,7 +539,7 @@ TMK_D void final_state(const Step3<T>& g, const Consts<T>& kc, const T* A, T sca
   add_final<D1, Db, T>(g, kc, scale, i, j, k, T18);
 }
 
-template <int D1, typename T>
+template <int D1, typename T, bool FC>
 TMK_D void final_body(const Step3<T>& g, const DevParams& P, DevStatus* st, int part, long long t) {
   const Bx& fb = g.flF[D1];
   if (t >= part_faces<D1>(fb, g.fault != 0, part)) return;
@@ -550,6 +554,7 @@ TMK_D void final_body(const Step3<T>& g, const DevParams& P, DevStatus* st, int 
   if (f > g.dlo[D1]) final_state<D1, T>(g, kc, g.WP[D1], scale, li, lj, lk, L);
   if (f <= g.dhi[D1]) final_state<D1, T>(g, kc, g.WM[D1], scale, i, j, k, R);
   if (!face_state<D1, T>(P, kc, g, f, L, R, G)) {
+    if constexpr (!FC) return;
     double U22[NC];
     load_ff(g, g.FF[1], i, k, U22);
     const double bval = bdry_value(P, g, i, k, U22, (1.0 / 2.0) * g.dt);
@@ -557,11 +562,11 @@ TMK_D void final_body(const Step3<T>& g, const DevParams& P, DevStatus* st, int 
   }
   store_face<D1>(g.WH[D1], fb, i, j, k, G);
 }
-template <int D1, typename T, typename Src>
+template <int D1, typename T, typename Src, bool FC = true>
 __global__ void __launch_bounds__(128) final_kernel(const __grid_constant__ Src src, const DevParams* Pp,
                                                     DevStatus* st, int part) {
   TMK3_FIND(T)
-  final_body<D1, T>(*gp, *Pp, st, part, lt);
+  final_body<D1, T, FC>(*gp, *Pp, st, part, lt);
 }
 
 // ---------------------------------------------------------------- update
@@ -795,7 +800,8 @@ cudaError_t launch_plan(const Plan& pl, const DevParams* P, DevStatus* st, cudaS
     riem2_fault_kernel<T, Src><<<dim3(nb(K_FL1_1F), 2), 128, 0, fs>>>(pl.src(K_FL1_1F), P, st);
     cudaEventRecord(side->ev[4], fs);
   }
-  riem1_kernel<1, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
+  if (split) riem1_kernel<1, T, Src, false><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
+  else riem1_kernel<1, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
   join(3);
   riem2_pair_kernel<0, T, Src><<<nb(K_FL1_0), 128, 0, s>>>(pl.src(K_FL1_0), P, st, PART_ALL);
   riem2_pair_kernel<2, T, Src><<<nb(K_FL1_2), 128, 0, s>>>(pl.src(K_FL1_2), P, st, PART_ALL);
@@ -804,8 +810,10 @@ cudaError_t launch_plan(const Plan& pl, const DevParams* P, DevStatus* st, cudaS
     final_kernel<1, T, Src><<<nb(K_FLF_1F), 128, 0, fs>>>(pl.src(K_FLF_1F), P, st, PART_FAULT);
     cudaEventRecord(side->ev[5], fs);
   }
-  riem2_pair_kernel<1, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
-  final_kernel<1, T, Src><<<nb(kf1), 128, 0, s>>>(pl.src(kf1), P, st, bulk);
+  if (split) riem2_pair_kernel<1, T, Src, false><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
+  else riem2_pair_kernel<1, T, Src><<<nb(k11), 128, 0, s>>>(pl.src(k11), P, st, bulk);
+  if (split) final_kernel<1, T, Src, false><<<nb(kf1), 128, 0, s>>>(pl.src(kf1), P, st, bulk);
+  else final_kernel<1, T, Src><<<nb(kf1), 128, 0, s>>>(pl.src(kf1), P, st, bulk);
   join(4);
   final_kernel<0, T, Src><<<nb(K_FLF_0), 128, 0, s>>>(pl.src(K_FLF_0), P, st, PART_ALL);
   final_kernel<2, T, Src><<<nb(K_FLF_2), 128, 0, s>>>(pl.src(K_FLF_2), P, st, PART_ALL);
