@@ -237,43 +237,82 @@ struct Many {
   const Step3<T>* gp = src.find(blockIdx.x * (long long)blockDim.x + threadIdx.x, lt); \
   if (!gp) return;
 
+// The slope box halved along D: each pred thread takes two neighbouring cells
+// along D (the last one alone where the box has odd length), whose PPM
+// stencils share four of their five points.
+template <int D> TMK_HD Bx pair_box(const Bx& S) {
+  Bx b = S;
+  b.n[D] = (S.n[D] + 1) / 2;
+  return b;
+}
+
 template <int D, typename T>
 TMK_D void pred_body(const Step3<T>& g, const DevParams& P, long long t) {
-  if (t >= g.S.cells()) return;
+  const Bx pb = pair_box<D>(g.S);
+  if (t >= pb.cells()) return;
   int i, j, k;
-  g.S.cell(t, i, j, k);
+  pb.cell(t, i, j, k);
+  if (D == 0) i = g.S.lo[0] + 2 * (i - g.S.lo[0]);
+  else if (D == 1) j = g.S.lo[1] + 2 * (j - g.S.lo[1]);
+  else k = g.S.lo[2] + 2 * (k - g.S.lo[2]);
   const Consts<T>& kc = g.kc;
   const T* sig = g.sig;
   const int q0 = coord<D>(i, j, k);
-  bool in[5];
+  const bool two = q0 + 1 < g.S.lo[D] + g.S.n[D];
+  // window points q0-2 .. q0+3; the last is read only for a second cell (the
+  // predictor input covers the slope box grown by 2 within the domain)
+  bool in[6];
 #pragma unroll
-  for (int m = 0; m < 5; ++m) in[m] = q0 - 2 + m >= g.dlo[D] && q0 - 2 + m <= g.dhi[D];
+  for (int m = 0; m < 6; ++m) in[m] = q0 - 2 + m >= g.dlo[D] && q0 - 2 + m <= g.dhi[D];
+  in[5] = in[5] && two;
   const long long acs = g.A.cells(), pcs = g.Ap.cells();
-  T WM[NS], WP[NS];
+  T WM0[NS], WP0[NS], WM1[NS], WP1[NS];
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
-    T w5[NSIDE][5];
+    T w6[NSIDE][6];
 #pragma unroll
-    for (int m = 0; m < 5; ++m) {
+    for (int m = 0; m < 6; ++m) {
       int ii = i, jj = j, kk = k;
       step<D>(ii, jj, kk, m - 2);
       const long long o = in[m] ? g.Ap.at(ii, jj, kk) : 0;
 #pragma unroll
-      for (int c = 0; c < NSIDE; ++c) w5[c][m] = in[m] ? g.Up[(g.uside * s + c) * pcs + o] : T(0);
+      for (int c = 0; c < NSIDE; ++c) w6[c][m] = in[m] ? g.Up[(g.uside * s + c) * pcs + o] : T(0);
     }
     bool fast = false;
     if constexpr (!kExact<T>) fast = g.fastpred != 0;
-    if (fast)
-      ppm_predict_prim<D, T>(kc, (T)rvs<D>(s), w5, in, g.trA, g.trB, WM + NSIDE * s, WP + NSIDE * s);
-    else
-      ppm_predict<D, T>(kc, (T)rvs<D>(s), w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM + NSIDE * s,
-                        WP + NSIDE * s, P.order, P.fourth != 0);
+    if (fast) {
+      ppm_predict_prim2<D, T>(kc, (T)rvs<D>(s), w6, in, two, g.trA, g.trB, WM0 + NSIDE * s, WP0 + NSIDE * s,
+                              WM1 + NSIDE * s, WP1 + NSIDE * s);
+    } else {
+      T w5[NSIDE][5];
+#pragma unroll
+      for (int c = 0; c < NSIDE; ++c)
+#pragma unroll
+        for (int m = 0; m < 5; ++m) w5[c][m] = w6[c][m];
+      ppm_predict<D, T>(kc, (T)rvs<D>(s), w5, in, P.prim_lim != 0, P.char_lim != 0, sig, WM0 + NSIDE * s,
+                        WP0 + NSIDE * s, P.order, P.fourth != 0);
+      if (two) {
+#pragma unroll
+        for (int c = 0; c < NSIDE; ++c)
+#pragma unroll
+          for (int m = 0; m < 5; ++m) w5[c][m] = w6[c][m + 1];
+        ppm_predict<D, T>(kc, (T)rvs<D>(s), w5, in + 1, P.prim_lim != 0, P.char_lim != 0, sig, WM1 + NSIDE * s,
+                          WP1 + NSIDE * s, P.order, P.fourth != 0);
+      }
+    }
   }
-  store_face<D>(g.WM[D], g.S, i, j, k, WM);
-  store_face<D>(g.WP[D], g.S, i, j, k, WP);
+  store_face<D>(g.WM[D], g.S, i, j, k, WM0);
+  store_face<D>(g.WP[D], g.S, i, j, k, WP0);
+  if (two) {
+    int i1 = i, j1 = j, k1 = k;
+    step<D>(i1, j1, k1, 1);
+    store_face<D>(g.WM[D], g.S, i1, j1, k1, WM1);
+    store_face<D>(g.WP[D], g.S, i1, j1, k1, WP1);
+  }
   if (D == 1 && g.fault && j == g.dlo[1]) {
     // lambda and gamma of side 1 at the fault's lo faces (read by the
-    // reference-layout slip-weakening law as side-2 velocities)
+    // reference-layout slip-weakening law as side-2 velocities); only the
+    // first cell of a pair can lie on the domain's y-lo layer
 #pragma unroll
     for (int c = 9; c < 11; ++c) {
       double w[5];
@@ -697,7 +736,7 @@ inline unsigned blocks(long long n) { return (unsigned)((n + 127) / 128); }
 // The work of each kind of pass: cells or faces, for the y-direction face
 // passes also split into the bulk and the fault plane.
 enum : int {
-  K_AP = 0, K_S, K_FL1_0, K_FL1_1, K_FL1_1B, K_FL1_1F, K_FL1_2, K_FLF_0, K_FLF_1, K_FLF_1B, K_FLF_1F, K_FLF_2,
+  K_AP = 0, K_SP0, K_SP1, K_SP2, K_FL1_0, K_FL1_1, K_FL1_1B, K_FL1_1F, K_FL1_2, K_FLF_0, K_FLF_1, K_FLF_1B, K_FLF_1F, K_FLF_2,
   K_CUR, K_BF, NKIND
 };
 template <typename T>
@@ -705,7 +744,9 @@ TMK_HD long long kind_count(const Step3<T>& g, int kind) {
   const bool f = g.fault != 0;
   switch (kind) {
     case K_AP: return g.Ap.cells();
-    case K_S: return g.S.cells();
+    case K_SP0: return pair_box<0>(g.S).cells();
+    case K_SP1: return pair_box<1>(g.S).cells();
+    case K_SP2: return pair_box<2>(g.S).cells();
     case K_FL1_0: return g.fl1[0].cells();
     case K_FL1_1: return part_faces<1>(g.fl1[1], f, PART_ALL);
     case K_FL1_1B: return part_faces<1>(g.fl1[1], f, PART_BULK);
@@ -785,14 +826,14 @@ cudaError_t launch_plan(const Plan& pl, const DevParams* P, DevStatus* st, cudaS
   };
   auto nb = [&](int kind) { return blocks(pl.n(kind)); };
   if (pl.copy() && pl.n(K_AP)) to_pred_kernel<T, Src><<<nb(K_AP), 128, 0, s>>>(pl.src(K_AP));
-  pred_kernel<0, T, Src><<<nb(K_S), 128, 0, s>>>(pl.src(K_S), P);
-  pred_kernel<1, T, Src><<<nb(K_S), 128, 0, s>>>(pl.src(K_S), P);
+  pred_kernel<0, T, Src><<<nb(K_SP0), 128, 0, s>>>(pl.src(K_SP0), P);
+  pred_kernel<1, T, Src><<<nb(K_SP1), 128, 0, s>>>(pl.src(K_SP1), P);
   fork(0);
   if (split) {
     riem1_kernel<1, T, Src><<<nb(K_FL1_1F), 128, 0, fs>>>(pl.src(K_FL1_1F), P, st, PART_FAULT);
     cudaEventRecord(side->ev[3], fs);
   }
-  pred_kernel<2, T, Src><<<nb(K_S), 128, 0, s>>>(pl.src(K_S), P);
+  pred_kernel<2, T, Src><<<nb(K_SP2), 128, 0, s>>>(pl.src(K_SP2), P);
   riem1_kernel<0, T, Src><<<nb(K_FL1_0), 128, 0, s>>>(pl.src(K_FL1_0), P, st, PART_ALL);
   riem1_kernel<2, T, Src><<<nb(K_FL1_2), 128, 0, s>>>(pl.src(K_FL1_2), P, st, PART_ALL);
   fork(1);

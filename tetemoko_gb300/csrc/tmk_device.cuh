@@ -498,22 +498,11 @@ TMK_D T vl_lim(T wm, T w0, T wp, bool hasL, bool hasR) {
   return (dl * dr > T(0) && (hasL || hasR)) ? copysign(m, dc) : T(0);
 }
 
+// the characteristic stage of ppm_predict_prim: limited deltas dm, dp of the
+// cell with centre values w -> traced face states WM, WP
 template <int D, typename T>
-TMK_D void ppm_predict_prim(const Consts<T>& k, T rv, const T (*w5)[5], const bool* in, const T* trA, const T* trB,
-                            T* WM, T* WP) {
-  T dm[NSIDE], dp[NSIDE];
-#pragma unroll
-  for (int c = 0; c < NSIDE; ++c) {
-    const T* w = w5[c];
-    const T sm = in[1] ? vl_lim(w[0], w[1], w[2], in[0], true) : T(0);
-    const T s0 = vl_lim(w[1], w[2], w[3], in[1], in[3]);
-    const T sp = in[3] ? vl_lim(w[2], w[3], w[4], true, in[4]) : T(0);
-    const T flo = in[1] ? T(0.5) * (w[1] + w[2]) - (s0 - sm) * T(1.0 / 6.0) : w[2] - T(0.5) * s0;
-    const T fhi = in[3] ? T(0.5) * (w[2] + w[3]) - (sp - s0) * T(1.0 / 6.0) : w[2] + T(0.5) * s0;
-    T m = flo - w[2], p = fhi - w[2];
-    ppm_limit(m, p);
-    dm[c] = m; dp[c] = p;
-  }
+TMK_D void prim_trace(const Consts<T>& k, T rv, const T* dm, const T* dp, const T* w, const T* trA, const T* trB,
+                      T* WM, T* WP) {
   T cm[NSIDE], cp[NSIDE];
   char_analysis<D>(k, rv, dm, cm);
   char_analysis<D>(k, rv, dp, cp);
@@ -524,7 +513,55 @@ TMK_D void ppm_predict_prim(const Consts<T>& k, T rv, const T (*w5)[5], const bo
   char_synthesis<D>(k, rv, cm, WM);
   char_synthesis<D>(k, rv, cp, WP);
 #pragma unroll
-  for (int c = 0; c < NSIDE; ++c) { WM[c] += w5[c][2]; WP[c] += w5[c][2]; }
+  for (int c = 0; c < NSIDE; ++c) { WM[c] += w[c]; WP[c] += w[c]; }
+}
+
+template <int D, typename T>
+TMK_D void ppm_predict_prim(const Consts<T>& k, T rv, const T (*w5)[5], const bool* in, const T* trA, const T* trB,
+                            T* WM, T* WP) {
+  T dm[NSIDE], dp[NSIDE], w[NSIDE];
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) {
+    const T* wc = w5[c];
+    const T sm = in[1] ? vl_lim(wc[0], wc[1], wc[2], in[0], true) : T(0);
+    const T s0 = vl_lim(wc[1], wc[2], wc[3], in[1], in[3]);
+    const T sp = in[3] ? vl_lim(wc[2], wc[3], wc[4], true, in[4]) : T(0);
+    const T flo = in[1] ? T(0.5) * (wc[1] + wc[2]) - (s0 - sm) * T(1.0 / 6.0) : wc[2] - T(0.5) * s0;
+    const T fhi = in[3] ? T(0.5) * (wc[2] + wc[3]) - (sp - s0) * T(1.0 / 6.0) : wc[2] + T(0.5) * s0;
+    T m = flo - wc[2], p = fhi - wc[2];
+    ppm_limit(m, p);
+    dm[c] = m; dp[c] = p; w[c] = wc[2];
+  }
+  prim_trace<D, T>(k, rv, dm, dp, w, trA, trB, WM, WP);
+}
+
+// ppm_predict_prim for two neighbouring cells along D (window points 2 and 3 of
+// w6, in[m] whether point m lies in the domain; the second cell only if `two`,
+// which implies in[3]): the slopes at points 2 and 3 and the face value
+// between the cells serve both, with the same arithmetic as two single calls.
+template <int D, typename T>
+TMK_D void ppm_predict_prim2(const Consts<T>& k, T rv, const T (*w6)[6], const bool* in, bool two, const T* trA,
+                             const T* trB, T* WM0, T* WP0, T* WM1, T* WP1) {
+  T dm0[NSIDE], dp0[NSIDE], dm1[NSIDE], dp1[NSIDE], w0[NSIDE], w1[NSIDE];
+#pragma unroll
+  for (int c = 0; c < NSIDE; ++c) {
+    const T* w = w6[c];
+    const T s1 = in[1] ? vl_lim(w[0], w[1], w[2], in[0], true) : T(0);
+    const T s2 = vl_lim(w[1], w[2], w[3], in[1], in[3]);
+    const T s3 = in[3] ? vl_lim(w[2], w[3], w[4], true, in[4]) : T(0);
+    const T f12 = in[1] ? T(0.5) * (w[1] + w[2]) - (s2 - s1) * T(1.0 / 6.0) : w[2] - T(0.5) * s2;
+    const T f23 = in[3] ? T(0.5) * (w[2] + w[3]) - (s3 - s2) * T(1.0 / 6.0) : w[2] + T(0.5) * s2;
+    T m = f12 - w[2], p = f23 - w[2];
+    ppm_limit(m, p);
+    dm0[c] = m; dp0[c] = p; w0[c] = w[2];
+    const T s4 = in[4] ? vl_lim(w[3], w[4], w[5], true, in[5]) : T(0);
+    const T f34 = in[4] ? T(0.5) * (w[3] + w[4]) - (s4 - s3) * T(1.0 / 6.0) : w[3] + T(0.5) * s3;
+    T m1 = f23 - w[3], p1 = f34 - w[3];
+    ppm_limit(m1, p1);
+    dm1[c] = m1; dp1[c] = p1; w1[c] = w[3];
+  }
+  prim_trace<D, T>(k, rv, dm0, dp0, w0, trA, trB, WM0, WP0);
+  if (two) prim_trace<D, T>(k, rv, dm1, dp1, w1, trA, trB, WM1, WP1);
 }
 
 // -------------------------------------------------------- status reporting
