@@ -383,10 +383,15 @@ TMK_D bool face_state(const DevParams& P, const Consts<T>& kc, const Step3<T>& g
     const bool outflow = P.bc[2 * D + (lo ? 0 : 1)] == 0;
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      T bg[NSIDE];
+      // the interior state by element-wise selects (a select of the array
+      // pointer would put both arrays in local memory)
+      T bg[NSIDE], wi[NSIDE];
 #pragma unroll
-      for (int c = 0; c < NSIDE; ++c) bg[c] = (T)P.bg[11 * s + c];
-      edge_bc<D, T>(kc, (T)rvs<D>(s), lo ? -1 : +1, outflow, bg, (lo ? R18 : L18) + NSIDE * s, G18 + NSIDE * s);
+      for (int c = 0; c < NSIDE; ++c) {
+        bg[c] = (T)P.bg[11 * s + c];
+        wi[c] = lo ? R18[NSIDE * s + c] : L18[NSIDE * s + c];
+      }
+      edge_bc<D, T>(kc, (T)rvs<D>(s), lo ? -1 : +1, outflow, bg, wi, G18 + NSIDE * s);
     }
   } else {
 #pragma unroll
