@@ -523,7 +523,8 @@ def three_d_measurement(steps, warmup, stream, fp64_steps=3, cpu_seconds=5.0, si
     tf = os.path.join(ROOT, "profiles", "patch_step_3d_mixed_192x96x96.traffic.json")
     if os.path.exists(tf):
         try:
-            traffic = json.load(open(tf)).get("dram_bytes_per_step")
+            # measured per cell on a 128x64x64 patch; every pass is a pass over the patch
+            traffic = json.load(open(tf))["bytes_per_cell"] * nx * ny * nz
         except Exception:
             traffic = None
     cpu = None
@@ -551,8 +552,9 @@ def three_d_measurement(steps, warmup, stream, fp64_steps=3, cpu_seconds=5.0, si
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
                          "algorithmic_bytes_per_step": BYTES_PER_CELL_3D * nx * ny * nz,
-                         "kernel": "the whole 3-D step (19 launches: FP32 copy, 3 predictors, 3 + 6 + 3 face "
-                                   "passes, update, boundary data)",
+                         "kernel": "the whole 3-D step (18 launches: FP32 copy, 3 predictors, 4 first-pass, "
+                                   "3 paired second-pass + 1 fault-plane and 4 final face passes, update, "
+                                   "boundary data)",
                          "timing": f"CUDA events on the launch stream around {mixed['steps']} steps"},
             "cpu_baseline": cpu,
             "patches_32": tiles,
