@@ -15,6 +15,19 @@ L0_BOXES = [(0, 0, 20, 9), (21, 0, 63, 9), (0, 10, 31, 31), (32, 10, 47, 20), (3
 L1_BOXES = [(40, 0, 71, 15), (72, 0, 87, 23), (40, 16, 71, 23)]
 L2_BOXES = [(96, 0, 127, 31), (128, 0, 143, 31)]
 
+# the reference decks' refinement ratios (4: execLinElast/tpv5_r1:69,
+# input/bssa_flat_amr.input:84; 8: input/labvalues_Psi50_m.input:78): finer
+# boxes of uneven size (8 to 64 cells per side) around the same nucleation,
+# aligned to the ratio and nested at least 8 coarser cells inside their level
+LAYOUTS = {
+    (2, 2): [L1_BOXES, L2_BOXES],
+    (4, 4): [[(96, 0, 159, 31), (160, 0, 167, 47), (168, 0, 175, 47), (96, 32, 159, 47)],
+             [(448, 0, 575, 63), (576, 0, 639, 31)]],
+    (4, 2): [[(96, 0, 159, 31), (160, 0, 167, 47), (168, 0, 175, 47), (96, 32, 159, 47)],
+             [(224, 0, 287, 15), (288, 0, 319, 31)]],
+    (8,): [[(192, 0, 319, 63), (320, 0, 351, 31)]],
+}
+
 
 def level_from_global(domain, dx, boxes, nb, Ug, Bg) -> O.LevelData:
     """Per-patch arrays sliced from a domain-wide state (22, ny+8, nx+8) and fault row (nb, nx+8)."""
@@ -33,13 +46,14 @@ def refine_domain(d, r):
 
 def hierarchy(sc, rng, nlev=2, ratios=(2, 2), fine_noise=0.0):
     """Level data of a hierarchy: level 0 seeded, finer levels prolonged from
-    their coarser level (plus optional seeded noise)."""
+    their coarser level (plus optional seeded noise).  The finer levels' boxes
+    are LAYOUTS[ratios]."""
     nb = sc.nbdry
     dom0 = (0, 0, sc.nx - 1, sc.ny - 1)
     Ug = perturbed_state(sc, rng, amp_v=0.05, amp_s=1.0)
     Bg = sc.initial_B() if nb else np.zeros((0, sc.nx + 2 * G))
     levels = [level_from_global(dom0, sc.dx, L0_BOXES, nb, Ug, Bg)]
-    boxes = [L1_BOXES, L2_BOXES]
+    boxes = LAYOUTS[tuple(ratios)]
     for l in range(1, nlev):
         r = ratios[l - 1]
         c = levels[-1]

@@ -61,6 +61,8 @@ def _scenario(kind="rs", precision=A.TMK_PREC_FP64):
         sc = S.rate_state(nx=64, ny=32, dx=0.1, precision=precision)
     elif kind == "sw":
         sc = S.slip_weakening(nx=64, ny=32, dx=0.1, precision=precision)
+    elif kind == "sw_ref9":                          # the reference's side-2 layout at component 9
+        sc = S.slip_weakening(nx=64, ny=32, dx=0.1, precision=precision, layout=A.TMK_SW_LAYOUT_REFERENCE9)
     elif kind == "sw_plastic":
         sc = S.slip_weakening(nx=64, ny=32, dx=0.1, precision=precision, plasticity=True)
     else:
@@ -68,62 +70,109 @@ def _scenario(kind="rs", precision=A.TMK_PREC_FP64):
     return sc
 
 
-@pytest.mark.parametrize("alpha", [0.0, 0.3, 0.5, 1.0])
-def test_cf_fill_matches_oracle(cuda_lib, alpha):
+# a ratio's hierarchy layout (the reference decks refine by 4 and 8)
+RATIO_LAYOUT = {2: (2, 2), 4: (4, 4), 8: (8,)}
+FILL_CASES = [(r, a) for r in (2, 4, 8) for a in (0.0, 0.25, 0.3, 0.5, 0.75, 1.0)]
+
+
+@pytest.mark.parametrize("r,alpha", FILL_CASES, ids=[f"r{r}_a{a}" for r, a in FILL_CASES])
+def test_cf_fill_matches_oracle(cuda_lib, r, alpha):
     from tetemoko_gb300.level import Context
     sc = _scenario()
     rng = np.random.default_rng(21)
-    d0, d1 = H.hierarchy(sc, rng, nlev=2)
+    d0, d1 = H.hierarchy(sc, rng, nlev=2, ratios=RATIO_LAYOUT[r])
     for u in d1.U:                                   # ghosts the fill must overwrite (or keep)
         u[:, :G, :] = rng.standard_normal(u[:, :G, :].shape)
         u[:, :, -G:] = rng.standard_normal(u[:, :, -G:].shape)
     ctx = Context(sc)
     C, F = _levels_on_gpu(ctx, [d0, d1])
-    F.attach_coarser(C, 2)
+    F.attach_coarser(C, r)
     C.step(0.0, sc.dt())
     cnew = _read(C, d0)
     F.fill_coarse_fine(alpha)
     got = _read(F, d1)
     ref = d1.copy()
-    assert O.cf_fill(2, d0, cnew, alpha, ref) == 0
+    assert O.cf_fill(r, d0, cnew, alpha, ref) == 0
     assert _all_err(got, ref) <= RTOL_FP64
     F.close(); C.close(); ctx.close()
 
 
-def test_average_down_and_prolongation_match_oracle(cuda_lib):
+@pytest.mark.parametrize("r", [2, 4, 8])
+def test_cf_time_coefficient_snaps_to_the_coarse_times(cuda_lib, r):
+    """LinElastLevelGodunov::step's alpha = (t - tCold) / (tCnew - tCold) is
+    snapped to 0 or 1 within 0.04 dt / r (LinElastLevelGodunov.cpp:230-256):
+    a fine step that starts just inside the window equals the step taken at
+    the coarse time itself; alpha outside [0, 1] after snapping is an error."""
+    from tetemoko_gb300.level import Context
+    sc = _scenario()
+    sc.scheme.fault_law = A.TMK_FAULT_NONE          # rupture times would record the shifted start
+    sc.scheme.boundary_type[2] = 0
+    d0, d1 = H.hierarchy(sc, np.random.default_rng(27), nlev=2, ratios=RATIO_LAYOUT[r])
+    ctx = Context(sc)
+    dtc = sc.dt()
+    dtf = dtc / r
+    outs = []
+    eps_t = 0.03 * dtf / r * dtc                 # alpha = 0.03 dt / r: inside the window (0.04 dt / r)
+    for t0, edge in ((0.0, 0), (eps_t, 0), (dtc, 1), (dtc - eps_t, 1)):
+        C, F = _levels_on_gpu(ctx, [d0, d1])
+        F.attach_coarser(C, r)
+        C.step(0.0, dtc)
+        F.step(t0, dtf, t_coarse_old=0.0, t_coarse_new=dtc)
+        outs.append((edge, _read(F, d1)))
+        if edge == 1:
+            with pytest.raises(A.TmkError):           # alpha > 1 + eps
+                F.step(dtc + 0.1 * dtf, dtf, t_coarse_old=0.0, t_coarse_new=dtc)
+        F.close(); C.close()
+    for e in (0, 1):
+        a, b = [o for edge, o in outs if edge == e]
+        for p in range(len(a.boxes)):
+            np.testing.assert_array_equal(a.U[p], b.U[p])
+    # the two ends differ: the test is not vacuous
+    assert max(rel_err(outs[0][1].U[p], outs[2][1].U[p]) for p in range(len(d1.boxes))) > 1e-6
+    ctx.close()
+
+
+@pytest.mark.parametrize("r", [2, 4, 8])
+def test_average_down_and_prolongation_match_oracle(cuda_lib, r):
     from tetemoko_gb300.level import Context
     sc = _scenario()
     rng = np.random.default_rng(22)
-    d0, d1 = H.hierarchy(sc, rng, nlev=2, fine_noise=0.05)
+    d0, d1 = H.hierarchy(sc, rng, nlev=2, ratios=RATIO_LAYOUT[r], fine_noise=0.05)
     ctx = Context(sc)
     C, F = _levels_on_gpu(ctx, [d0, d1])
-    F.attach_coarser(C, 2)
+    F.attach_coarser(C, r)
     C.average_down()
     ref = d0.copy()
-    assert O.average_down(2, ref, d1) == 0
+    assert O.average_down(r, ref, d1) == 0
     assert _valid_err(_read(C, d0), ref) <= RTOL_FP64
     # prolongation of the (averaged) coarse level onto the fine level
     F.interp_from_coarser()
     fref = d1.copy()
-    assert O.fine_interp(2, ref, fref) == 0
+    assert O.fine_interp(r, ref, fref) == 0
     assert _valid_err(_read(F, d1), fref) <= RTOL_FP64
     F.close(); C.close(); ctx.close()
 
 
-def test_regrid_prolongs_then_copies_the_old_level(cuda_lib):
+REGRID_BOXES = {2: [(48, 0, 79, 15), (48, 16, 79, 27)],
+                4: [(128, 0, 191, 31), (128, 32, 159, 55)],
+                8: [(256, 0, 383, 47), (384, 0, 415, 23)]}
+
+
+@pytest.mark.parametrize("r", [2, 4, 8])
+def test_regrid_prolongs_then_copies_the_old_level(cuda_lib, r):
     from tetemoko_gb300.amr import regrid_level
     from tetemoko_gb300.level import Context, LinElastLevelGodunov
     sc = _scenario()
     rng = np.random.default_rng(23)
-    d0, d1 = H.hierarchy(sc, rng, nlev=2, fine_noise=0.05)
+    d0, d1 = H.hierarchy(sc, rng, nlev=2, ratios=RATIO_LAYOUT[r], fine_noise=0.05)
     ctx = Context(sc)
     C, F = _levels_on_gpu(ctx, [d0, d1])
-    F.attach_coarser(C, 2)
-    new_boxes = [(48, 0, 79, 15), (48, 16, 79, 27)]
+    F.attach_coarser(C, r)
+    new_boxes = REGRID_BOXES[r]
     N = LinElastLevelGodunov(ctx, new_boxes, domain=d1.domain, dx=d1.dx)
-    regrid_level(N, F, C, 2)
+    regrid_level(N, F, C, r)
     dn = O.LevelData(d1.domain, d1.dx, new_boxes, d1.nb)
-    assert O.fine_interp(2, d0, dn) == 0
+    assert O.fine_interp(r, d0, dn) == 0
     for p, nb in enumerate(new_boxes):            # copy of the old fine cells
         for q, ob in enumerate(d1.boxes):
             lo0, hi0, lo1, hi1 = max(nb[0], ob[0]), min(nb[2], ob[2]), max(nb[1], ob[1]), min(nb[3], ob[3])
@@ -138,18 +187,22 @@ def test_regrid_prolongs_then_copies_the_old_level(cuda_lib):
     N.close(); F.close(); C.close(); ctx.close()
 
 
-CASES = [("rs", 2, 3), ("rs", 3, 2), ("sw", 2, 3), ("sw_plastic", 2, 2)]
+CASES = [("rs", (2, 2), 2, 3), ("rs", (2, 2), 3, 2), ("sw", (2, 2), 2, 3), ("sw_plastic", (2, 2), 2, 2),
+         ("rs", (4, 4), 2, 2), ("rs", (4, 4), 3, 1), ("sw", (4, 4), 2, 2), ("sw_ref9", (4, 4), 2, 2),
+         ("sw_plastic", (4, 4), 2, 2), ("sw_plastic", (4, 4), 3, 1), ("rs", (4, 2), 3, 2),
+         ("rs", (8,), 2, 1), ("sw_plastic", (8,), 2, 1)]
 
 
-@pytest.mark.parametrize("kind,nlev,nsteps", CASES, ids=[f"{k}_{n}lev" for k, n, _ in CASES])
-def test_amr_hierarchy_matches_oracle(cuda_lib, kind, nlev, nsteps):
+@pytest.mark.parametrize("kind,ratios,nlev,nsteps", CASES,
+                         ids=[f"{k}_r{'x'.join(map(str, r[:n - 1]))}_{n}lev" for k, r, n, _ in CASES])
+def test_amr_hierarchy_matches_oracle(cuda_lib, kind, ratios, nlev, nsteps):
     from tetemoko_gb300.amr import AMRHierarchy
     from tetemoko_gb300.level import Context
     sc = _scenario(kind)
     rng = np.random.default_rng(24)
-    datas = H.hierarchy(sc, rng, nlev=nlev)
+    datas = H.hierarchy(sc, rng, nlev=nlev, ratios=ratios)
     refs = [d.copy() for d in datas]
-    ratios = [2] * (nlev - 1)
+    ratios = list(ratios[:nlev - 1])
     assert O.amr_run(sc, refs, ratios, 0.0, sc.dt(), nsteps) == 0
     ctx = Context(sc)
     lvs = _levels_on_gpu(ctx, datas)
@@ -161,29 +214,35 @@ def test_amr_hierarchy_matches_oracle(cuda_lib, kind, nlev, nsteps):
         rc, info = lv.status()
         assert rc == 0, info
         assert _valid_err(_read(lv, d), r) <= 1e-11
+    sub = np.cumprod([1] + ratios)
     assert h.cell_updates() == sum(
-        sum((b[2] - b[0] + 1) * (b[3] - b[1] + 1) for b in d.boxes) * 2 ** l for l, d in enumerate(datas))
+        sum((b[2] - b[0] + 1) * (b[3] - b[1] + 1) for b in d.boxes) * int(sub[l]) for l, d in enumerate(datas))
     h.close()
     for lv in lvs:
         lv.close()
     ctx.close()
 
 
-def test_amr_mixed_form_within_fp32_rounding(cuda_lib):
+MIXED_CASES = [("rs", (2,)), ("rs", (4,)), ("sw_plastic", (4, 4))]
+
+
+@pytest.mark.parametrize("kind,ratios", MIXED_CASES, ids=[f"{k}_r{'x'.join(map(str, r))}" for k, r in MIXED_CASES])
+def test_amr_mixed_form_within_fp32_rounding(cuda_lib, kind, ratios):
     from tetemoko_gb300.amr import AMRHierarchy
     from tetemoko_gb300.level import Context
-    sc = _scenario("rs")
+    sc = _scenario(kind)
     rng = np.random.default_rng(25)
-    datas = H.hierarchy(sc, rng, nlev=2)
+    datas = H.hierarchy(sc, rng, nlev=len(ratios) + 1, ratios=RATIO_LAYOUT[ratios[0]])
     refs = [d.copy() for d in datas]
-    assert O.amr_run(sc, refs, [2], 0.0, sc.dt(), 3) == 0
+    assert O.amr_run(sc, refs, list(ratios), 0.0, sc.dt(), 3) == 0
     sc.scheme.precision = A.TMK_PREC_MIXED
     ctx = Context(sc)
     lvs = _levels_on_gpu(ctx, datas)
-    h = AMRHierarchy(lvs, [2])
+    h = AMRHierarchy(lvs, list(ratios))
     for _ in range(3):
         h.step(sc.dt())
     for lv, d, r in zip(lvs, datas, refs):
+        assert lv.status()[0] == 0
         got = _read(lv, d)
         for p in range(len(d.boxes)):
             assert rel_err(got.U[p][:, G:-G, G:-G], r.U[p][:, G:-G, G:-G]) <= 1e-4
@@ -195,21 +254,22 @@ def test_amr_mixed_form_within_fp32_rounding(cuda_lib):
     ctx.close()
 
 
-def test_amr_refluxing_conserves_the_composite_sum_on_device(cuda_lib):
+@pytest.mark.parametrize("r", [2, 4])
+def test_amr_refluxing_conserves_the_composite_sum_on_device(cuda_lib, r):
     from tetemoko_gb300.amr import AMRHierarchy
     from tetemoko_gb300.level import Context
     from tests.test_oracle_amr import _bump_level, _no_fault_bump
     sc = _no_fault_bump()
-    fboxes = [(32, 16, 63, 31), (32, 32, 63, 47)]
+    fboxes = [(16 * r, 8 * r, 32 * r - 1, 16 * r - 1), (16 * r, 16 * r, 32 * r - 1, 24 * r - 1)]
     C0 = _bump_level(sc, (0, 0, 47, 31), 0.2, O.tile_boxes(48, 32, 16), 3.2, 3.2, 0.6)
-    F0 = _bump_level(sc, (0, 0, 95, 63), 0.1, fboxes, 3.2, 3.2, 0.6)
+    F0 = _bump_level(sc, (0, 0, 48 * r - 1, 32 * r - 1), 0.2 / r, fboxes, 3.2, 3.2, 0.6)
     ctx = Context(sc)
     C, F = _levels_on_gpu(ctx, [C0, F0])
-    h = AMRHierarchy([C, F], [2])
-    t0 = H.composite_sum([C0, F0], [2])
+    h = AMRHierarchy([C, F], [r])
+    t0 = H.composite_sum([C0, F0], [r])
     for _ in range(2):
         h.step(sc.dt())
-    t1 = H.composite_sum([_read(C, C0), _read(F, F0)], [2])
+    t1 = H.composite_sum([_read(C, C0), _read(F, F0)], [r])
     assert (np.abs(t1 - t0) / np.maximum(np.abs(t0), 1.0)).max() < 1e-14
     h.close(); F.close(); C.close(); ctx.close()
 

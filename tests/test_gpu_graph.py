@@ -57,19 +57,20 @@ def test_level_graph_needs_an_even_step_count(cuda_lib):
     lvl.close(); ctx.close()
 
 
-@pytest.mark.parametrize("kind", ["rs", "sw_plastic"])
-def test_amr_graph_replays_subcycled_steps(cuda_lib, kind):
+@pytest.mark.parametrize("kind,ratios", [("rs", (2, 2)), ("sw_plastic", (2, 2)), ("rs", (4, 4)),
+                                         ("sw_plastic", (4, 2))])
+def test_amr_graph_replays_subcycled_steps(cuda_lib, kind, ratios):
     from tetemoko_gb300.amr import AMRHierarchy
     from tetemoko_gb300.level import Context
     from tests.test_gpu_amr import _fault_err, _levels_on_gpu, _read
     sc = S.rate_state(nx=64, ny=32, dx=0.1) if kind == "rs" else \
         S.slip_weakening(nx=64, ny=32, dx=0.1, plasticity=True)
-    datas = H.hierarchy(sc, np.random.default_rng(32), nlev=3)
+    datas = H.hierarchy(sc, np.random.default_rng(32), nlev=3, ratios=ratios)
     ctx = Context(sc)
     la = _levels_on_gpu(ctx, datas)
     lb = _levels_on_gpu(ctx, datas)
-    ha = AMRHierarchy(la, [2, 2])
-    hb = AMRHierarchy(lb, [2, 2])
+    ha = AMRHierarchy(la, list(ratios))
+    hb = AMRHierarchy(lb, list(ratios))
     for _ in range(4):
         ha.step(sc.dt())
     g = hb.graph(2, sc.dt())

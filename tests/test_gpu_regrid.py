@@ -11,15 +11,16 @@ pytestmark = pytest.mark.gpu
 G = A.TMK_NGHOST
 
 
-def test_regrid_cycle(cuda_lib):
+@pytest.mark.parametrize("r", [2, 4])
+def test_regrid_cycle(cuda_lib, r):
     from tetemoko_gb300.amr import AMRHierarchy, regrid
     from tetemoko_gb300.level import Context
     from tests.test_gpu_amr import _levels_on_gpu
     sc = S.rate_state(nx=64, ny=32, dx=0.1)
-    datas = H.hierarchy(sc, np.random.default_rng(91), nlev=2)
+    datas = H.hierarchy(sc, np.random.default_rng(91), nlev=2, ratios=(r, r))
     ctx = Context(sc)
     lvs = _levels_on_gpu(ctx, datas)
-    h = AMRHierarchy(lvs, [2])
+    h = AMRHierarchy(lvs, [r])
     for _ in range(2):
         h.step(sc.dt())
     t = h.time(0)
@@ -27,13 +28,13 @@ def test_regrid_cycle(cuda_lib):
     tp = A.tag_params(level=0, refine_thresh=0.02, tag_buffer=1)
     mask = lvs[0].tag_cells(tp)
     old = {p: u for p, u in enumerate(lvs[1].get_patches()[0])}
-    new = regrid(lvs, [2], [tp], block_factor=8, max_grid_size=32, fill_ratio=0.7)
+    new = regrid(lvs, [r], [tp], block_factor=8, max_grid_size=32, fill_ratio=0.7)
     assert len(new) == 2 and new[0] is lvs[0]
     fine = new[1]
     # every tag is refined (level 0 nests everything), boxes obey the limits
     ys, xs = np.nonzero(mask)
     for i, j in zip(xs, ys):
-        assert any(b[0] <= 2 * i <= b[2] and b[1] <= 2 * j <= b[3] for b in fine.boxes)
+        assert any(b[0] <= r * i <= b[2] and b[1] <= r * j <= b[3] for b in fine.boxes)
     for b in fine.boxes:
         assert b[2] - b[0] + 1 <= 32 and b[3] - b[1] + 1 <= 32 and b[0] % 8 == 0 and b[1] % 8 == 0
     # cells the old fine level had keep their values
@@ -51,7 +52,7 @@ def test_regrid_cycle(cuda_lib):
             checked += a.size
     assert checked > 0
     lvs[1].close()
-    h2 = AMRHierarchy(new, [2], time=t)
+    h2 = AMRHierarchy(new, [r], time=t)
     for _ in range(2):
         h2.step(sc.dt())
     for lv in new:

@@ -84,7 +84,8 @@ def test_station_records_in_a_graph_and_when_full(cuda_lib):
     ctx.close()
 
 
-def test_stations_in_a_subcycled_hierarchy(cuda_lib):
+@pytest.mark.parametrize("r", [2, 4])
+def test_stations_in_a_subcycled_hierarchy(cuda_lib, r):
     """The coarse level records after its finer level's substeps, reflux and
     average-down (postTimeStep's order); the fine level after each substep."""
     from tetemoko_gb300.amr import AMRHierarchy
@@ -92,10 +93,10 @@ def test_stations_in_a_subcycled_hierarchy(cuda_lib):
     from tetemoko_gb300.stations import Stations
     from tests.test_gpu_amr import _levels_on_gpu, _read
     sc = S.rate_state(nx=64, ny=32, dx=0.1)
-    datas = H.hierarchy(sc, np.random.default_rng(62), nlev=2)
+    datas = H.hierarchy(sc, np.random.default_rng(62), nlev=2, ratios=(r, r))
     ctx = Context(sc)
     lvs = _levels_on_gpu(ctx, datas)
-    h = AMRHierarchy(lvs, [2])
+    h = AMRHierarchy(lvs, [r])
     fx = [3.33]
     sts = [Stations(lv, fx, [(3.21, 0.45)], capacity=8) for lv in lvs]
     for s in sts:
@@ -104,7 +105,7 @@ def test_stations_in_a_subcycled_hierarchy(cuda_lib):
     h.step(dt0)
     rc, rf = sts[0].read(), sts[1].read()
     np.testing.assert_allclose(rc["time"], [dt0], rtol=1e-15)
-    np.testing.assert_allclose(rf["time"], [dt0 / 2, dt0], rtol=1e-15)
+    np.testing.assert_allclose(rf["time"], [dt0 * (k + 1) / r for k in range(r)], rtol=1e-15)
     d0 = _read(lvs[0], datas[0])
     Ug = np.zeros((22, 32 + 2 * G, 64 + 2 * G))
     Bg = np.zeros((sc.nbdry, 64 + 2 * G))
