@@ -54,8 +54,12 @@ def load(path: str):
     """Rebuild the scenario, a context and the levels of a checkpoint (levels
     attached coarse to fine).  Returns (scenario, context, levels, ratios, time);
     build an AMRHierarchy(levels, ratios, time) to continue a hierarchy."""
+    with np.load(path) as z:
+        return _rebuild(z)
+
+
+def _rebuild(z):
     from .level import Context, LinElastLevelGodunov
-    z = np.load(path)
     nx, ny = (int(v) for v in z["grid"])
     dx, cfl = (float(v) for v in z["dx_cfl"])
     sc = Scenario(str(z["name"]), nx, ny, dx, cfl, _struct_from(A.ElasticParams, z["elastic"]),

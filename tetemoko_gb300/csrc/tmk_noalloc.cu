@@ -33,18 +33,51 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[TMK_NOALLOC_SCR
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_addr[kMaxDevices] = {};
+unsigned long long g_ctx[kMaxDevices] = {};   // the context the cached address belongs to
 
-// Device address of the scratch on the current device; the first call on a
-// device looks it up (with that device current) and caches it.
+// Unique id of the calling thread's current CUDA context (cuCtxGetId ids are
+// never reused within a process), or 0 when it cannot be had.  The driver
+// calls are reached through the runtime's entry-point query, so the library
+// does not link libcuda.  Call with g_mu held.
+unsigned long long current_context_id() {
+  typedef int (*GetCurrent)(void**);
+  typedef int (*GetId)(void*, unsigned long long*);
+  static bool queried = false;
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  if (!queried) {
+    queried = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)f;
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, &id) == 0) return id;
+  return 0;
+}
+
+// Device address of the scratch in the current device's context.  The first
+// call in a context looks it up (with that device current) and caches it; a
+// new context on the device (after cudaDeviceReset, the module and its array
+// are loaded again, possibly elsewhere) looks it up again.
 tmk_status scratch_address(void** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) return TMK_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return TMK_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_addr[dev]) {
+  const unsigned long long id = current_context_id();
+  if (!g_addr[dev] || id == 0 || id != g_ctx[dev]) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return TMK_ERR_CUDA;
     g_addr[dev] = p;
+    g_ctx[dev] = current_context_id();   // the lookup made the device's primary context current
   }
   *out = g_addr[dev];
   return TMK_OK;
