@@ -327,6 +327,168 @@ def amr_measurement(steps, warmup, stream, autotune=True):
     return out
 
 
+def rupture_errors(make_scenario, nsteps, offsets_km, stream, graph_steps=0):
+    """The mixed form against the plain FP64 form (the oracle-pinned one) on the
+    same level from the same initial state: both run `nsteps` steps with fault
+    stations at the nucleation centre +- offsets_km; returns the largest
+    relative errors of arrival time, final slip and peak slip rate at the
+    stations, the volume particle-velocity error, the friction solves that hit
+    the bracket edge or the iteration limit in each form (status info[2]), and
+    the mixed form's rate when `graph_steps` > 0 (steps replayed from a graph)."""
+    import numpy as np
+    import torch
+    from tetemoko_gb300 import _capi as A, rupture as R
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    from tetemoko_gb300.stations import Stations
+    res = {}
+    for prec in (A.TMK_PREC_FP64, A.TMK_PREC_MIXED):
+        sc = make_scenario(prec)
+        ctx = Context(sc)
+        lvl = LinElastLevelGodunov(ctx, [(0, 0, sc.nx - 1, sc.ny - 1)])
+        lvl.set_patch(0, sc.initial_U(), sc.initial_B())
+        xc = sc.nx * sc.dx / 2.0
+        fx = [xc + s * d for d in offsets_km for s in (-1.0, 1.0)]
+        st = Stations(lvl, fx, [], capacity=1024)
+        st.attach()
+        dt, t = sc.dt(), 0.0
+        chunks = []
+        for n in range(nsteps):
+            lvl.step(t, dt, stream)
+            t += dt
+            if (n + 1) % 1000 == 0 or n + 1 == nsteps:
+                torch.cuda.synchronize()
+                chunks.append(st.read())
+        rec = {"time": np.concatenate([c["time"] for c in chunks]),
+               "fault": np.concatenate([c["fault"] for c in chunks])}
+        law = sc.scheme.fault_law
+        thr = sc.rs.rupture_threshold if law == A.TMK_FAULT_RS else sc.sw.rupture_threshold
+        U, _ = lvl.get_patch(0)
+        rc, info = lvl.status()
+        res[prec] = (R.station_metrics(rec, law, thr), U, rc, info)
+        st.close()
+        rate = None
+        if prec == A.TMK_PREC_MIXED and graph_steps:
+            graph = lvl.graph(graph_steps, t, dt)
+            graph.launch(t, stream)
+            t += graph_steps * dt
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            nrep = max(1, nsteps // graph_steps)
+            e0.record(stream)
+            for _ in range(nrep):
+                graph.launch(t, stream)
+                t += graph_steps * dt
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / (nrep * graph_steps)
+            rate = {"value": sc.nx * sc.ny / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                    "steps": nrep * graph_steps,
+                    "execution": f"CUDA graph of {graph_steps} level steps, replayed (after the error run)"}
+            graph.close()
+        res["rate"] = rate
+        lvl.close()
+        ctx.close()
+    m64, U64, rc64, info64 = res[A.TMK_PREC_FP64]
+    mm, Um, rcm, infom = res[A.TMK_PREC_MIXED]
+    out = R.compare(mm, m64)
+    out["volume_velocity"] = R.velocity_error(Um, U64)
+    out["bounds"] = {"arrival": 5e-3, "final_slip": 1e-3}
+    out["within_bounds"] = bool(out["arrival"] is not None and out["arrival"] < 5e-3 and out["final_slip"] < 1e-3)
+    out["steps"] = nsteps
+    out["stations_km_from_nucleation"] = [s * d for d in offsets_km for s in (-1, 1)]
+    out["bracket_limited_solves"] = {"fp64": info64[2], "mixed": infom[2]}
+    out["status"] = {"fp64": rc64, "mixed": rcm}
+    out["reference"] = "the plain FP64 GPU form (equal to the FP64 oracle to 1e-11 per step), same initial state"
+    return out, res["rate"]
+
+
+def amr3_measurement(coarse_steps, stream, regrid_interval=2):
+    """Three levels at ratio 4 over the slip-weakening 512x256 base (dx 0.1 km,
+    finest 6.25 m) with Drucker-Prager plasticity (1 MPa cohesion, background
+    normal stresses from plas_Psi = 30 degrees), refined by device tags on the
+    fault row's slip rate (>= 1e-3 m/s) and on velocity gradients, regridded
+    every `regrid_interval` coarse steps with boxes of 8 to 64 cells
+    (blocking factor 8, maximum 64, Berger-Rigoutsos on the host), mixed form.
+    The subcycled steps are timed with CUDA events; each regrid (tags, boxes,
+    new levels, prolongation, copy) by the host clock, reported apart."""
+    import torch
+    from tetemoko_gb300 import _capi as A, scenarios as S
+    from tetemoko_gb300.amr import AMRHierarchy, refine_domain, regrid
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    sc = S.slip_weakening(nx=512, ny=256, precision=A.TMK_PREC_MIXED, plasticity=True, cohesion=1.0, plas_psi=30)
+    ctx = Context(sc)
+    ratios = [4, 4]
+    base = LinElastLevelGodunov(ctx, tile_boxes(0, 0, sc.nx - 1, sc.ny - 1, 64))
+    U, B = sc.initial_U(), sc.initial_B()
+    base.set_level(U, B)
+    box_args = dict(block_factor=8, max_grid_size=64, fill_ratio=0.7)
+
+    def tps(initial):
+        return [A.tag_params(level=l, initial=initial, refine_thresh=0.01, tag_buffer=2, slip_rate_thresh=1e-3)
+                for l in range(2)]
+
+    # initial hierarchy from tagCellsInit's nucleation marks (levels built one at a time)
+    t0 = time.perf_counter()
+    levels = regrid([base], ratios, tps(True), max_level=2, stream=stream, **box_args)
+    torch.cuda.synchronize()
+    init_s = time.perf_counter() - t0
+    dt0 = sc.dt()
+    t = 0.0
+    step_ms, regrid_s, updates, nregrid = 0.0, 0.0, 0, 0
+    sizes = set()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    done = 0
+    while done < coarse_steps:
+        h = AMRHierarchy(levels, ratios[:len(levels) - 1], time=t)
+        n = min(regrid_interval, coarse_steps - done)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(n):
+            h.step(dt0, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        step_ms += e0.elapsed_time(e1)
+        updates += h.cell_updates() * n
+        t = h.time(0)
+        h.close()
+        done += n
+        if done < coarse_steps:
+            r0 = time.perf_counter()
+            old = levels
+            levels = regrid(levels, ratios, tps(False), stream=stream, **box_args)
+            torch.cuda.synchronize()
+            regrid_s += time.perf_counter() - r0
+            nregrid += 1
+            for lv in old[1:]:
+                if all(lv is not n_ for n_ in levels):
+                    lv.close()
+        for lv in levels[1:]:
+            for b in lv.boxes:
+                sizes.add(max(b[2] - b[0] + 1, b[3] - b[1] + 1))
+    status = [lv.status()[1] for lv in levels]
+    cells = [sum((b[2] - b[0] + 1) * (b[3] - b[1] + 1) for b in lv.boxes) for lv in levels]
+    out = {"value": updates / (step_ms * 1e-3), "unit": "cell-updates/s",
+           "ms_per_coarse_step": step_ms / coarse_steps, "coarse_steps": coarse_steps,
+           "regrids": nregrid, "regrid_ms_each": 1e3 * regrid_s / max(1, nregrid),
+           "initial_hierarchy_ms": 1e3 * init_s,
+           "cells_per_level_at_end": cells, "patches_per_level_at_end": [len(lv.boxes) for lv in levels],
+           "patch_side_range": [min(sizes), max(sizes)] if sizes else None,
+           "config": "3 levels, ratio 4, base 512x256 at dx=0.1 km (finest 6.25 m), slip weakening (mu_s 0.677, "
+                     "mu_d 0.525, Dc 0.4 m, side 2 at offset 11), Drucker-Prager plasticity with 1 MPa cohesion "
+                     "(b = c cos(phi), an extension), background from plas_Psi = 30 deg, tags: fault-row slip rate "
+                     ">= 1e-3 m/s (an extension) or velocity gradient >= 0.01, tag buffer 2, boxes: blocking "
+                     "factor 8, max 64, fill ratio 0.7, regrid every 2 coarse steps, FP32 volume / FP64 fault",
+           "execution": "tmk_amr_step per coarse step (levels change every regrid); regrid on the device (tags, "
+                        "prolongation, copy) with host box generation",
+           "device_status": status}
+    for lv in levels:
+        lv.close()
+    ctx.close()
+    return out
+
+
 ENSEMBLE_SIZE = 64
 
 
@@ -632,6 +794,8 @@ def main():
     ap.add_argument("--three-d-steps", type=int, default=20)   # timed steps of the 3-D measurement
     ap.add_argument("--three-d-only", action="store_true")
     ap.add_argument("--three-d-size", default="192x96x96")   # profiling runs use a smaller patch
+    ap.add_argument("--error-steps", type=int, default=4000)   # mixed vs FP64 rupture errors (max_step)
+    ap.add_argument("--sw-steps", type=int, default=1000)      # slip-weakening 512x256 level (its max_step)
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     args = ap.parse_args()
@@ -820,6 +984,23 @@ def main():
     lvl64.close()
     ctx64.close()
 
+    # ---- the slip error of the mixed form at the benchmarked configuration
+    errors = None
+    if args.error_steps > 0:
+        errors, _ = rupture_errors(lambda p: S.rate_state(nx=nx, ny=ny, precision=p), args.error_steps,
+                                   (5.0, 10.0, 20.0, 40.0, 60.0, 80.0), stream)
+    # ---- the slip-weakening 512x256 level (the CPU-runnable workload), mixed
+    # form rate and its rupture errors against the FP64 form
+    sw_level = None
+    if args.sw_steps > 0:
+        sw_err, sw_rate = rupture_errors(lambda p: S.slip_weakening(nx=512, ny=256, precision=p), args.sw_steps,
+                                         (3.0, 6.0, 9.0, 12.0, 15.0, 20.0), stream, graph_steps=100)
+        sw_level = dict(sw_rate or {})
+        sw_level["config"] = ("slip-weakening planar fault, uniform 512x256, dx=0.1 km, mu_s=0.677, mu_d=0.525, "
+                              "Dc=0.4 m, 120 MPa normal / 70 MPa shear, 3 km nucleation window at 81.6 MPa, "
+                              "side-2 components at offset 11, FP32 volume / FP64 fault")
+        sw_level["errors"] = sw_err
+
     # ---- subcycled 4-level AMR hierarchy (rank 0 reports its own)
     amr = amr_measurement(args.amr_steps, 2, stream, args.autotune) if args.amr_steps > 0 else None
     # ---- ensemble of 64 independent scenarios in one level
@@ -858,6 +1039,8 @@ def main():
                            "volume_kernel": args.fp64_kernel, "volume_kernel_ms": vol64,
                            "volume_hbm_gbs": BYTES_PER_CELL_FP64 * cells / (vol64 * 1e-3) / 1e9},
             "mixed_over_fp64": value / value64,
+            "errors": errors,
+            "sw_level": sw_level,
             "amr": amr,
             "ensemble": ens,
             "three_d": three_d,

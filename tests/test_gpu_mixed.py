@@ -160,3 +160,62 @@ def test_mixed_fault_path_tracks_the_fp64_oracle(cuda_lib, variant):
     assert rel_err(Bm[:, g:-g], Br[:, g:-g]) <= 1e-3
     lv.close()
     ctx.close()
+
+
+SW_STEPS = 1000                     # the slip-weakening workload's max_step
+
+
+def test_mixed_slip_weakening_rupture_metrics_vs_fp64_oracle(cuda_lib):
+    """The slip-weakening workload at full size (512x256, dx = 0.1 km, 1000
+    steps, side 2 at offset 11): the mixed form's rupture against the FP64
+    oracle's at fault stations 3-15 km either side of the nucleation, with the
+    station values interpolated on the device (tmk_stations_*) and by the
+    oracle's restatement of the same interpolation."""
+    import os
+    from tetemoko_gb300 import rupture as R
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    from tetemoko_gb300.stations import Stations
+    sc64 = S.slip_weakening(nx=512, ny=256, dx=0.1)
+    scm = S.slip_weakening(nx=512, ny=256, dx=0.1, precision=A.TMK_PREC_MIXED)
+    xc = sc64.nx * sc64.dx / 2.0
+    fx = [xc + s * d for d in (3.0, 6.0, 9.0, 12.0, 15.0) for s in (-1.0, 1.0)]
+    dt = sc64.dt()
+    g = A.TMK_NGHOST
+    dom = (0, 0, sc64.nx - 1, sc64.ny - 1)
+    # FP64 oracle
+    U, B = sc64.initial_U(), sc64.initial_B()
+    boxes = O.tile_boxes(sc64.nx, sc64.ny, 128)
+    nthreads = max(1, len(os.sched_getaffinity(0)))
+    ts, Vf = [], []
+    t = 0.0
+    for _ in range(SW_STEPS):
+        assert O.level_step(sc64, U, B, boxes, t, dt, nthreads=nthreads) == 0
+        t += dt
+        wf, _ = O.station_values(dom, sc64.dx, U, B, fx, [])
+        ts.append(t)
+        Vf.append(np.asarray(wf))
+    ref = {"time": np.array(ts), "fault": np.array(Vf)}
+    # mixed form on the device
+    ctx = Context(scm)
+    lvl = LinElastLevelGodunov(ctx, [dom])
+    lvl.set_patch(0, scm.initial_U(), scm.initial_B())
+    st = Stations(lvl, fx, [], capacity=SW_STEPS + 8)
+    st.attach()
+    t = 0.0
+    for _ in range(SW_STEPS):
+        lvl.step(t, dt)
+        t += dt
+    rec = st.read()
+    Um, _ = lvl.get_patch(0)
+    rc, info = lvl.status()
+    st.close(); lvl.close(); ctx.close()
+    assert rc == 0, info
+    thr = sc64.sw.rupture_threshold
+    e = R.compare(R.station_metrics(rec, A.TMK_FAULT_SW, thr), R.station_metrics(ref, A.TMK_FAULT_SW, thr))
+    vel_err = R.velocity_error(Um, U)
+    print(f"slip weakening, mixed vs FP64 oracle, {SW_STEPS} steps: {e}, volume velocity {vel_err:.2e}")
+    assert e["stations_ruptured"] == len(fx), "every station must rupture within the run"
+    assert e["arrival"] < ARRIVAL_RTOL
+    assert e["final_slip"] < SLIP_RTOL
+    assert e["peak_slip_rate"] < PEAK_RTOL
+    assert vel_err < VEL_RTOL

@@ -151,3 +151,23 @@ def test_station_files_in_the_reference_format(cuda_lib, tmp_path):
     st.close()
     lvl.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("which", ["fault_only", "body_only"])
+def test_stations_of_one_kind_only(cuda_lib, which):
+    """A station set with fault stations alone (or body stations alone) reads
+    back records of the right shapes."""
+    from tetemoko_gb300.stations import Stations
+    sc, ctx, lvl, Ug, Bg = _setup(A.TMK_PREC_FP64)
+    fx, bxy = (FAULT_X, []) if which == "fault_only" else ([], BODY_XY[:2])
+    st = Stations(lvl, fx, bxy, capacity=8)
+    st.attach()
+    for k in range(3):
+        lvl.step(k * sc.dt(), sc.dt())
+    rec = st.read()
+    assert rec["time"].shape == (3,)
+    assert rec["fault"].shape == (3, len(fx), sc.nbdry)
+    assert rec["body"].shape == (3, len(bxy), 22)
+    st.close()
+    lvl.close()
+    ctx.close()

@@ -81,8 +81,9 @@ class Stations:
                                            C.byref(n), C.byref(dropped)), "tmk_stations_read")
         r = buf[:n.value]
         nf = len(self.fault_x)
-        fault = r[:, 1:1 + nf * self.nb].reshape(-1, nf, self.nb)
-        body = r[:, 1 + nf * self.nb:].reshape(-1, len(self.body_xy), 22)
+        nrec = r.shape[0]
+        fault = r[:, 1:1 + nf * self.nb].reshape(nrec, nf, self.nb)
+        body = r[:, 1 + nf * self.nb:].reshape(nrec, len(self.body_xy), 22)
         return {"time": r[:, 0].copy(), "fault": fault.copy(), "body": body.copy(), "dropped": dropped.value}
 
     # ---------------------------------------------------------------- files
