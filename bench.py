@@ -489,6 +489,91 @@ def amr3_measurement(coarse_steps, stream, regrid_interval=2):
     return out
 
 
+def amr3_measurement(coarse_steps, stream, regrid_interval=2):
+    """Three levels at ratio 4 over the slip-weakening 512x256 base (dx 0.1 km,
+    finest 6.25 m) with Drucker-Prager plasticity (1 MPa cohesion, background
+    normal stresses from plas_Psi = 30 degrees), refined by device tags on the
+    fault row's slip rate (>= 1e-3 m/s) and on velocity gradients, regridded
+    every `regrid_interval` coarse steps with boxes of 8 to 64 cells
+    (blocking factor 8, maximum 64, Berger-Rigoutsos on the host), mixed form.
+    The subcycled steps are timed with CUDA events; each regrid (tags, boxes,
+    new levels, prolongation, copy) by the host clock, reported apart."""
+    import torch
+    from tetemoko_gb300 import _capi as A, scenarios as S
+    from tetemoko_gb300.amr import AMRHierarchy, regrid
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    sc = S.slip_weakening(nx=512, ny=256, precision=A.TMK_PREC_MIXED, plasticity=True, cohesion=1.0, plas_psi=30)
+    ctx = Context(sc)
+    ratios = [4, 4]
+    base = LinElastLevelGodunov(ctx, tile_boxes(0, 0, sc.nx - 1, sc.ny - 1, 64))
+    base.set_level(sc.initial_U(), sc.initial_B())
+    box_args = dict(block_factor=8, max_grid_size=64, fill_ratio=0.7)
+
+    def tps(initial):
+        return [A.tag_params(level=l, initial=initial, refine_thresh=0.01, tag_buffer=2, slip_rate_thresh=1e-3)
+                for l in range(2)]
+
+    # the initial hierarchy from tagCellsInit's nucleation marks
+    t0 = time.perf_counter()
+    levels = regrid([base], ratios, tps(True), max_level=2, stream=stream, **box_args)
+    torch.cuda.synchronize()
+    init_s = time.perf_counter() - t0
+    dt0 = sc.dt()
+    t = 0.0
+    step_ms, regrid_s, updates, nregrid = 0.0, 0.0, 0, 0
+    sizes = set()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    done = 0
+    while done < coarse_steps:
+        h = AMRHierarchy(levels, ratios[:len(levels) - 1], time=t)
+        n = min(regrid_interval, coarse_steps - done)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(n):
+            h.step(dt0, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        step_ms += e0.elapsed_time(e1)
+        updates += h.cell_updates() * n
+        t = h.time(0)
+        h.close()
+        done += n
+        if done < coarse_steps:
+            r0 = time.perf_counter()
+            old = levels
+            levels = regrid(levels, ratios, tps(False), stream=stream, **box_args)
+            torch.cuda.synchronize()
+            regrid_s += time.perf_counter() - r0
+            nregrid += 1
+            for lv in old[1:]:
+                if all(lv is not nl for nl in levels):
+                    lv.close()
+        for lv in levels[1:]:
+            for b in lv.boxes:
+                sizes.add(max(b[2] - b[0] + 1, b[3] - b[1] + 1))
+    status = [lv.status()[1] for lv in levels]
+    cells = [sum((b[2] - b[0] + 1) * (b[3] - b[1] + 1) for b in lv.boxes) for lv in levels]
+    out = {"value": updates / (step_ms * 1e-3), "unit": "cell-updates/s",
+           "ms_per_coarse_step": step_ms / coarse_steps, "coarse_steps": coarse_steps,
+           "regrids": nregrid, "regrid_ms_each": 1e3 * regrid_s / max(1, nregrid),
+           "initial_hierarchy_ms": 1e3 * init_s,
+           "cells_per_level_at_end": cells, "patches_per_level_at_end": [len(lv.boxes) for lv in levels],
+           "patch_side_range": [min(sizes), max(sizes)] if sizes else None,
+           "config": "3 levels, ratio 4, base 512x256 at dx=0.1 km (finest 6.25 m), slip weakening (mu_s 0.677, "
+                     "mu_d 0.525, Dc 0.4 m, side 2 at offset 11), Drucker-Prager plasticity with 1 MPa cohesion "
+                     "(b = c cos(phi), an extension), background from plas_Psi = 30 deg, tags: fault-row slip rate "
+                     ">= 1e-3 m/s (an extension) or velocity gradient >= 0.01, tag buffer 2, boxes: blocking "
+                     "factor 8, max 64, fill ratio 0.7, regrid every 2 coarse steps, FP32 volume / FP64 fault",
+           "execution": "tmk_amr_step per coarse step (levels change every regrid); regrid on the device (tags, "
+                        "prolongation, copy) with host box generation",
+           "device_status": status}
+    for lv in levels:
+        lv.close()
+    ctx.close()
+    return out
+
+
 ENSEMBLE_SIZE = 64
 
 
@@ -796,6 +881,8 @@ def main():
     ap.add_argument("--three-d-size", default="192x96x96")   # profiling runs use a smaller patch
     ap.add_argument("--error-steps", type=int, default=4000)   # mixed vs FP64 rupture errors (max_step)
     ap.add_argument("--sw-steps", type=int, default=1000)      # slip-weakening 512x256 level (its max_step)
+    ap.add_argument("--amr3-steps", type=int, default=100)     # coarse steps of the regridded 3-level ratio-4 run
+    ap.add_argument("--amr3-only", action="store_true")
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     args = ap.parse_args()
@@ -890,6 +977,11 @@ def main():
                                  size=tuple(int(v) for v in args.three_d_size.split("x")))
         if rank == 0:
             print(json.dumps({"three_d": td}), flush=True)
+        return 0
+    if args.amr3_only:
+        a3 = amr3_measurement(args.amr3_steps, stream)
+        if rank == 0:
+            print(json.dumps({"amr3": a3}), flush=True)
         return 0
     if args.ensemble_only:
         ens = ensemble_measurement(args.ensemble_steps, args.warmup, stream, autotune=args.autotune,
@@ -1003,6 +1095,8 @@ def main():
 
     # ---- subcycled 4-level AMR hierarchy (rank 0 reports its own)
     amr = amr_measurement(args.amr_steps, 2, stream, args.autotune) if args.amr_steps > 0 else None
+    # ---- 3 levels at ratio 4, slip weakening with plasticity, regridded every 2 coarse steps
+    amr3 = amr3_measurement(args.amr3_steps, stream) if args.amr3_steps > 0 else None
     # ---- ensemble of 64 independent scenarios in one level
     ens = ensemble_measurement(args.ensemble_steps, 3, stream, autotune=args.autotune, max_grid=args.ensemble_max_grid) \
         if args.ensemble_steps > 0 else None
@@ -1042,6 +1136,7 @@ def main():
             "errors": errors,
             "sw_level": sw_level,
             "amr": amr,
+            "amr3": amr3,
             "ensemble": ens,
             "three_d": three_d,
             "device_status": {"mixed": st[1], "fp64": st64[1]},

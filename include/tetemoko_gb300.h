@@ -32,7 +32,8 @@
 extern "C" {
 #endif
 
-#define TMK_ABI_VERSION 3   /* 2: tmk_scheme gained use_fourth_order_slopes; 3: tmk_tuning gained fault_first */
+#define TMK_ABI_VERSION 4   /* 2: tmk_scheme gained use_fourth_order_slopes; 3: tmk_tuning gained fault_first;
+                               4: tmk_tag_params gained slip_rate_thresh */
 
 #define TMK_NCOMP      22   /* state components, srcLinElast/LEINDEX.H:12-47 */
 #define TMK_NSIDE_COMP 11   /* IX_OFFSET, srcLinElast/LEINDEX.H:23 */
@@ -162,6 +163,10 @@ typedef struct {
   double width_coarsen;        /* comp.width_coarsen [1e40] */
   double x_coarsen2[2], y_coarsen2[2];  /* comp.x_coarsen2, y_coarsen2 [-1e40 1e40] */
   int    coarsen2_max_level;   /* comp.coarsen2_max_level [max_level] */
+  double slip_rate_thresh;     /* extension (the reference has no slip-rate tag): > 0 also tags
+                                  every cell of the fault row j = domain.lo[1] whose face's slip
+                                  rate (rate and state: boundary component 2; slip weakening: 4)
+                                  is at least this (m/s), inside the coarsen2 window; <= 0: off */
 } tmk_tag_params;
 
 typedef struct tmk_context_s tmk_context;

@@ -2393,7 +2393,12 @@ void tagLevel(const Phys& P, const OLevel& L, const tmk_tag_params& tp, std::vec
           const bool window = tp.level < tp.coarsen2_max_level ||
                               (x >= tp.x_coarsen2[0] && x <= tp.x_coarsen2[1] && y >= tp.y_coarsen2[0] &&
                                y <= tp.y_coarsen2[1]);
-          tag = window && (gm >= thr || U(i, j, 10) >= tp.plastic_thresh || U(i, j, 21) >= tp.plastic_thresh);
+          // slip-rate tag of the fault row (an extension, absent from the reference): the
+          // face below the cell slips at least slip_rate_thresh (RS component 2, SW 4)
+          bool slip = false;
+          if (tp.slip_rate_thresh > 0 && P.sch.fault_law != TMK_FAULT_NONE && j == D.lo[1] && L.fault((int)p))
+            slip = L.B[p](i, D.lo[1], P.sch.fault_law == TMK_FAULT_SW ? 4 : 2) >= tp.slip_rate_thresh;
+          tag = window && (gm >= thr || U(i, j, 10) >= tp.plastic_thresh || U(i, j, 21) >= tp.plastic_thresh || slip);
         }
         if (tag) raw[(size_t)(j - D.lo[1]) * nx + (i - D.lo[0])] = 1;
       }

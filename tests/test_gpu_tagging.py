@@ -84,3 +84,28 @@ def test_mixed_form_tags_agree_away_from_the_threshold(cuda_lib):
     assert (got != want).mean() <= 0.01
     lvl.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("kind", ["rs", "sw"])
+def test_slip_rate_tags_match_oracle(cuda_lib, kind):
+    """The slip-rate tag of the fault row (an extension the refinement of a
+    rupture front uses): bit for bit with the oracle, alone and with the
+    gradient tags, across the fault row split between patches."""
+    sc = S.rate_state(nx=64, ny=32, dx=0.1) if kind == "rs" else S.slip_weakening(nx=64, ny=32, dx=0.1)
+    rng = np.random.default_rng(54)
+    Ug = perturbed_state(sc, rng, amp_v=0.05, amp_s=1.0)
+    Bg = sc.initial_B()
+    vc = 2 if kind == "rs" else 4
+    x = (np.arange(-G, sc.nx + G) + 0.5) * sc.dx
+    Bg[vc] = np.where((x > 1.5) & (x < 2.6), 2e-3, 1e-9) + np.where((x > 4.0) & (x < 4.3), 5e-4, 0.0)
+    ctx, lvl = _device_level(sc, Ug, Bg)
+    d = H.level_from_global((0, 0, sc.nx - 1, sc.ny - 1), sc.dx, BOXES, sc.nbdry, Ug, Bg)
+    for tp in (A.tag_params(refine_thresh=1e10, tag_buffer=0, slip_rate_thresh=1e-3),
+               A.tag_params(refine_thresh=1e10, tag_buffer=2, slip_rate_thresh=4e-4),
+               A.tag_params(refine_thresh=0.04, tag_buffer=1, slip_rate_thresh=1e-3)):
+        want = O.tag_cells(sc, tp, d.copy())
+        got = lvl.tag_cells(tp)
+        assert want.sum() > 0
+        np.testing.assert_array_equal(got, want)
+    lvl.close()
+    ctx.close()

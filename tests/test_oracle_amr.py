@@ -249,3 +249,25 @@ def test_gradient_tags_follow_getfullgradf():
     x = np.arange(48) * sc.dx
     thr = 0.01 * (1 + np.maximum(0.0, x - 2.0) * 1.0 / 0.1)
     assert np.array_equal(m[0], (0.02 >= thr).astype(np.uint8))
+
+
+def test_slip_rate_tags_by_hand():
+    """The slip-rate tag (an extension): exactly the fault-row cells whose face
+    slips at least the threshold, grown by the tag buffer; off when <= 0."""
+    G = A.TMK_NGHOST
+    boxes = [(0, 0, 20, 9), (21, 0, 63, 9), (0, 10, 31, 31), (32, 10, 63, 31)]
+    for sc, vc in ((S.rate_state(nx=64, ny=32, dx=0.1), 2), (S.slip_weakening(nx=64, ny=32, dx=0.1), 4)):
+        Ug, Bg = sc.initial_U(), sc.initial_B()
+        x = (np.arange(-G, sc.nx + G) + 0.5) * sc.dx
+        Bg[vc] = np.where((x > 1.5) & (x < 2.6), 2e-3, 1e-9)
+        d = H.level_from_global((0, 0, 63, 31), sc.dx, boxes, sc.nbdry, Ug, Bg)
+        m = O.tag_cells(sc, A.tag_params(refine_thresh=1e10, tag_buffer=0, slip_rate_thresh=1e-3), d.copy())
+        want = np.zeros_like(m)
+        want[0, 15:26] = 1                                  # cell centres 1.55 .. 2.55 km
+        np.testing.assert_array_equal(m, want)
+        m = O.tag_cells(sc, A.tag_params(refine_thresh=1e10, tag_buffer=2, slip_rate_thresh=1e-3), d.copy())
+        want = np.zeros_like(m)
+        want[0:3, 13:28] = 1
+        np.testing.assert_array_equal(m, want)
+        m = O.tag_cells(sc, A.tag_params(refine_thresh=1e10, tag_buffer=2, slip_rate_thresh=0.0), d.copy())
+        assert m.sum() == 0

@@ -86,13 +86,16 @@ class TagParams(C.Structure):
     _fields_ = [("level", C.c_int), ("initial", C.c_int), ("refine_thresh", C.c_double),
                 ("plastic_thresh", C.c_double), ("tag_buffer", C.c_int), ("x_coarsen", C.c_double * 2),
                 ("y_coarsen", C.c_double * 2), ("slope_coarsen", C.c_double), ("width_coarsen", C.c_double),
-                ("x_coarsen2", C.c_double * 2), ("y_coarsen2", C.c_double * 2), ("coarsen2_max_level", C.c_int)]
+                ("x_coarsen2", C.c_double * 2), ("y_coarsen2", C.c_double * 2), ("coarsen2_max_level", C.c_int),
+                ("slip_rate_thresh", C.c_double)]
 
 
 def tag_params(level=0, initial=False, refine_thresh=0.01, plastic_thresh=1e-5, tag_buffer=2,
                x_coarsen=(-1e40, 1e40), y_coarsen=(-1e40, 1e40), slope_coarsen=0.0, width_coarsen=1e40,
-               x_coarsen2=(-1e40, 1e40), y_coarsen2=(-1e40, 1e40), coarsen2_max_level=100) -> TagParams:
-    """Tagging parameters with the input deck's defaults (execLinElast/amrGodunov.cpp:274-283, 400-440)."""
+               x_coarsen2=(-1e40, 1e40), y_coarsen2=(-1e40, 1e40), coarsen2_max_level=100,
+               slip_rate_thresh=0.0) -> TagParams:
+    """Tagging parameters with the input deck's defaults (execLinElast/amrGodunov.cpp:274-283, 400-440);
+    slip_rate_thresh > 0 adds the slip-rate tag of the fault row (an extension)."""
     t = TagParams()
     t.level, t.initial, t.refine_thresh, t.plastic_thresh = level, int(initial), refine_thresh, plastic_thresh
     t.tag_buffer, t.slope_coarsen, t.width_coarsen = tag_buffer, slope_coarsen, width_coarsen
@@ -101,6 +104,7 @@ def tag_params(level=0, initial=False, refine_thresh=0.01, plastic_thresh=1e-5, 
     t.x_coarsen2[:] = list(x_coarsen2)
     t.y_coarsen2[:] = list(y_coarsen2)
     t.coarsen2_max_level = coarsen2_max_level
+    t.slip_rate_thresh = slip_rate_thresh
     return t
 
 

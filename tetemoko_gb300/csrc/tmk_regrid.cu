@@ -5,8 +5,9 @@
 // difference of side 1's velocities (GETFULLGRADF + MAXF,
 // srcLinElast/LinElastPhysicsF.ChF:59-82, 199-259), the fault law's nucleation
 // marks (RSIBC/SWIBC::tagCellsInit), the coarsening-scaled threshold, the
-// coarsen2 window and the plastic-strain test; then IntVectSet::grow by the
-// tag buffer as two separable max filters over a byte mask of the domain.
+// coarsen2 window and the plastic-strain test (plus, as an extension, a
+// slip-rate test on the fault row); then IntVectSet::grow by the tag buffer as
+// two separable max filters over a byte mask of the domain.
 // Built with --fmad=false: the FP64 form tags exactly as the oracle does.
 #include <cmath>
 #include <cstring>
@@ -21,6 +22,8 @@ constexpr int kMaxNuc = TMK_SW_MAX_PATCHES;
 
 struct TagConst {
   double dx, thr, pthr, xc0, xc1, yc0, yc1, slope, width, x20, x21, y20, y21;
+  double vthr;           // slip-rate threshold of the fault-row tag (<= 0: off)
+  int vcomp;             // the slip-rate component of the boundary data
   int window_always;     // level < coarsen2_max_level
   int initial, marks;    // tagCellsInit; the fault law marks nucleation cells
   int nnuc;
@@ -73,7 +76,10 @@ __global__ void tag_kernel(const PatchDev<Real>* __restrict__ patches, const Tag
       { const double a = tc.yc0 - y, b = y - tc.yc1; const double m = (a < b) ? b : a; r = (r < m) ? m : r; }
       const double thr = tc.thr * (1 + r * tc.slope / tc.width);
       const bool window = tc.window_always || (x >= tc.x20 && x <= tc.x21 && y >= tc.y20 && y <= tc.y21);
-      tag = window && (gm >= thr || uat(p, 10, i, j) >= tc.pthr || uat(p, 21, i, j) >= tc.pthr);
+      // slip-rate tag of the fault row (an extension): the slip rate of the face below the cell
+      const bool slip = tc.vthr > 0 && p.fault && j == tc.dlo1 &&
+                        p.B[(size_t)tc.vcomp * p.bnx + (i - p.blo0)] >= tc.vthr;
+      tag = window && (gm >= thr || uat(p, 10, i, j) >= tc.pthr || uat(p, 21, i, j) >= tc.pthr || slip);
     }
     if (tag) raw[(size_t)(j - tc.dlo1) * mnx + (i - tc.dlo0)] = 1;
   }
@@ -124,6 +130,8 @@ extern "C" tmk_status tmk_level_tag_cells(tmk_level* L, const tmk_tag_params* tp
   tc.x20 = tp->x_coarsen2[0]; tc.x21 = tp->x_coarsen2[1]; tc.y20 = tp->y_coarsen2[0]; tc.y21 = tp->y_coarsen2[1];
   tc.window_always = tp->level < tp->coarsen2_max_level ? 1 : 0;
   tc.initial = tp->initial ? 1 : 0;
+  tc.vthr = P.fault_law == 0 ? 0.0 : tp->slip_rate_thresh;
+  tc.vcomp = P.fault_law == 2 ? 4 : 2;     // RSSETBND V / SWSETBND V
   tc.dlo0 = L->domain.lo[0]; tc.dlo1 = L->domain.lo[1]; tc.dhi0 = L->domain.hi[0]; tc.dhi1 = L->domain.hi[1];
   // RSIBC::tagCellsInit (ibcLinElast/RSIBC.cpp:351-368) / SWIBC::tagCellsInit (ibcLinElast/SWIBC.cpp:340-372)
   if (P.fault_law == 1) {

@@ -109,6 +109,16 @@ def _elastic(cs=3.464, cp=6.0, rho=2.670, sxx0=0.0, syy0=-120.0, szz0=0.0, sxy0=
     return e
 
 
+def plastic_background(syy0: float, sxy0: float, psi_deg: float) -> tuple[float, float]:
+    """sxx0 and szz0 of a deck with physics.plas_Psi (the angle of the largest
+    compressive stress to the fault): the rule of execLinElast/amrGodunov.cpp:482-495."""
+    if psi_deg == 45:
+        sxx0 = syy0
+    else:
+        sxx0 = (1.0 - 2.0 * sxy0 / (syy0 * math.tan(2.0 * (math.pi * psi_deg / 180.0)))) * syy0
+    return sxx0, (sxx0 + syy0) / 2.0
+
+
 def psi_steady(tau: float, sn: float, V: float, a: float, V0: float, Zs: float) -> float:
     """State psi at which slip rate V is steady under shear tau and normal stress sn:
     tau - Zs/2 V = sn a asinh(V/(2 V0) exp(psi/a))."""
@@ -117,7 +127,7 @@ def psi_steady(tau: float, sn: float, V: float, a: float, V0: float, Zs: float) 
 
 def slip_weakening(nx=512, ny=256, dx=0.1, precision=A.TMK_PREC_FP64,
                    layout=A.TMK_SW_LAYOUT_OFFSET11, cfl=0.9, plasticity=False,
-                   nuc_tau=11.6, nuc_half_width=1.5) -> Scenario:
+                   nuc_tau=11.6, nuc_half_width=1.5, cohesion=0.0, plas_psi=None) -> Scenario:
     """Slip-weakening planar fault at y=0 (the 512x256, dx=0.1 km CPU-runnable workload):
     mu_s=0.677, mu_d=0.525, Dc=0.4 m, sn=120 MPa, tau=70 MPa, a 3 km nucleation
     window at 81.6 MPa (11.6 MPa excess), friction box covering the whole fault."""
@@ -132,8 +142,11 @@ def slip_weakening(nx=512, ny=256, dx=0.1, precision=A.TMK_PREC_FP64,
     sw.layout = layout
     pl = None
     if plasticity:
-        pl = plastic_params()
-    return Scenario("slip_weakening", nx, ny, dx, cfl, _elastic(),
+        pl = plastic_params(cohesion=cohesion)
+    e = _elastic()
+    if plas_psi is not None:       # the deck's plas_Psi sets the background's normal stresses
+        e.sxx0, e.szz0 = plastic_background(e.syy0, e.sxy0, plas_psi)
+    return Scenario("slip_weakening", nx, ny, dx, cfl, e,
                     _scheme(A.TMK_FAULT_SW, precision, int(plasticity)), sw=sw, plastic=pl)
 
 
@@ -159,13 +172,17 @@ def rate_state(nx=2048, ny=1024, dx=0.1, precision=A.TMK_PREC_FP64,
     return sc
 
 
-def plastic_params(mu=math.sin(0.75), eta_time=0.03, G=None) -> A.PlasticParams:
+def plastic_params(mu=math.sin(0.75), eta_time=0.03, G=None, cohesion=0.0) -> A.PlasticParams:
     """Drucker-Prager: plas_mu, plas_beta = plas_mu/2 (execLinElast/amrGodunov.cpp:514),
-    plas_eta = eta_time * G (viscoplastic relaxation time eta/G)."""
+    plas_eta = eta_time * G (viscoplastic relaxation time eta/G).  A cohesion c
+    (MPa) enters as the yield term b = c cos(phi) with mu = sin(phi); the
+    reference hard-wires b = 0 (srcLinElast/PlasticPhysicsF.ChF:19), so c > 0 is
+    an extension."""
     if G is None:
         G = 2.670 * 3.464 ** 2
     p = A.PlasticParams()
-    p.mu, p.beta, p.eta, p.b, p.h = mu, mu / 2.0, eta_time * G, 0.0, 0.0
+    p.mu, p.beta, p.eta, p.h = mu, mu / 2.0, eta_time * G, 0.0
+    p.b = cohesion * math.cos(math.asin(mu))
     return p
 
 
