@@ -370,22 +370,46 @@ constexpr int MARCH_STASH_VECS = 5;
 constexpr int MARCH_COLS = 26;   // updated columns per warp
 constexpr int MARCH_WARPS = 4;   // warps per CTA
 
-// Number of per-row vectors a lane keeps in shared memory instead of registers
-// (the x states of row q-1, the first-pass y face q-1, the final y flux q-1
-// and the old state of row q-1).
-constexpr int MARCH_SMEM_VECS = 5;
+// Per-row vectors a lane carries from row to row in shared memory rather than
+// registers: the x states of row q-1 (WMx, WPx), the first-pass y face q-1
+// (H1y), the final y flux q-1 (Fy), the old state of row q-1 (Wold), the
+// y-predicted and corrected states of row q-1 (WPy, WPcy), and the y slope
+// and lo-face value of row q (Sy, Fyf).  Each keeps only the components that
+// are read: the x states the components live in x, the y states and faces
+// those live in y.  The FP64 form keeps the last four in registers: in shared
+// memory its in-plane CTA would need 131 KB, one CTA per SM.
+enum MarchCarry { kWMx = 0, kWPx, kH1y, kFy, kWold, kWPy, kWPcy, kSy, kFyf, kNumCarry };
+template <int G>
+TMK_HD constexpr bool carry_needed(int v, int c) {
+  return (v == kWMx || v == kWPx) ? live<G, 0>(c) : (v == kFy || v == kWold) ? true : live<G, 1>(c);
+}
+template <typename T>
+TMK_HD constexpr bool carry_in_smem(int v) { return v < kWPy || sizeof(T) == 4; }
+// position of (vector v, component c) among the shared-memory slots of a lane
+template <typename T, int G>
+TMK_HD constexpr int carry_slot(int v, int c) {
+  int k = 0;
+  for (int vv = 0; vv < v; ++vv)
+    for (int cc = 0; cc < Grp<G>::N; ++cc) k += (carry_in_smem<T>(vv) && carry_needed<G>(vv, cc)) ? 1 : 0;
+  for (int cc = 0; cc < c; ++cc) k += carry_needed<G>(v, cc) ? 1 : 0;
+  return k;
+}
+template <typename T, int G>
+TMK_HD constexpr int carry_slots() { return carry_slot<T, G>(kNumCarry, 0); }
 // Rows q..q+2 of the rolling window plus the row in flight live in a per-warp
 // ring of shared memory filled by cp.async; slot = row & 3.
 constexpr int MARCH_RING = 4;
 template <typename T, int G>
 constexpr size_t march_smem_bytes() {
-  return (size_t)MARCH_WARPS * (MARCH_SMEM_VECS + MARCH_RING) * Grp<G>::N * 32 * sizeof(typename PairOf<T>::P);
+  return (size_t)MARCH_WARPS * (carry_slots<T, G>() + MARCH_RING * Grp<G>::N) * 32 * sizeof(typename PairOf<T>::P);
 }
 
-// resident CTAs per SM the register allocation targets: the in-plane kernel at
-// 2 (255 registers, no spills: measured faster than 3 CTAs with spills), the
-// antiplane kernel at 4 (120 registers)
-template <int G> struct MarchMinBlocks { static constexpr int value = (G == 0) ? 2 : 4; };
+// resident CTAs per SM the register allocation targets: FP32 in-plane 3 (164
+// registers, no spills, with the y-direction carries in shared memory),
+// antiplane 5 (94 registers); FP64 in-plane 2, antiplane 4
+template <typename T, int G> struct MarchMinBlocks {
+  static constexpr int value = sizeof(T) == 4 ? ((G == 0) ? 3 : 5) : ((G == 0) ? 2 : 4);
+};
 
 // asynchronous copy of one element into shared memory (completion tracked per thread)
 template <typename T> TMK_D void cp_async_elem(T* dst_smem, const T* src) {
@@ -424,14 +448,15 @@ TMK_D void march_capture(const PatchDev<T>& pp, const MarchItem& it, const March
 }
 
 template <typename T, int G>
-__global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) march_kernel(const PatchDev<T>* __restrict__ patches,
+__global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value) march_kernel(const PatchDev<T>* __restrict__ patches,
                                                                  const MarchItem* __restrict__ items, int nitems,
                                                                  const __grid_constant__ MarchConst<T> mc) {
   using P = typename PairOf<T>::P;
   constexpr int N = Grp<G>::N;
   extern __shared__ __align__(16) unsigned char march_smem[];
-  P* const carry = reinterpret_cast<P*>(march_smem) + (size_t)(threadIdx.x >> 5) * (MARCH_SMEM_VECS + MARCH_RING) * N * 32;
-  P* const ring = carry + MARCH_SMEM_VECS * N * 32;
+  P* const carry = reinterpret_cast<P*>(march_smem) +
+                   (size_t)(threadIdx.x >> 5) * (carry_slots<T, G>() + MARCH_RING * N) * 32;
+  P* const ring = carry + carry_slots<T, G>() * 32;
   const int wid = blockIdx.x * MARCH_WARPS + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   // a later kernel of the step may be scheduled now; every warp waits for the
@@ -531,10 +556,24 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
   const int q_s = max(it.y0 - 1, dlo1);
   const int q_e = it.y1 + 1;
   int cpos = it.cap0;                     // next coarse-fine face to store
-  // rolling window of rows q, q+1, q+2 (ring slots); sy0 = slope(q); Fy0 = lo-face value of row q
-  P sy0[N], Fy0[N];
+  P rcar[kNumCarry - kWPy][N];     // the register-resident carries (FP64 form)
+  auto cput = [&](int v, const P* a) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      if (!carry_needed<G>(v, c)) continue;
+      if (carry_in_smem<T>(v)) carry[carry_slot<T, G>(v, c) * 32 + lane] = a[c];
+      else rcar[v - kWPy][c] = a[c];
+    }
+  };
+  auto cget = [&](int v, P* a) {
+#pragma unroll
+    for (int c = 0; c < N; ++c)
+      a[c] = !carry_needed<G>(v, c) ? mk2(T(0), T(0))
+             : carry_in_smem<T>(v) ? carry[carry_slot<T, G>(v, c) * 32 + lane] : rcar[v - kWPy][c];
+  };
+  // rolling window of rows q, q+1, q+2 (ring slots); slope(q) and the lo-face value of row q carried
   {
-    P Wa[N], Wb[N], W0[N], W1[N], W2[N];
+    P Wa[N], Wb[N], W0[N], W1[N], W2[N], sy0[N], Fy0[N];
     load_row(q_s - 2, Wa);
     load_row(q_s - 1, Wb);
     load_row(q_s, W0);
@@ -557,25 +596,9 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
         Fy0[c] = pfma(mk2(T(-0.5), T(-0.5)), sy0[c], W0[c]);
       }
     }
+    cput(kSy, sy0);
+    cput(kFyf, Fy0);
   }
-  // carried state of row q-1: WPy_p, WPcy_p in registers; the x states of row
-  // q-1 (WMx, WPx), the first-pass face q-1 (H1y) and the final flux q-1 (Fy)
-  // in this lane's own shared-memory slots (vector v, component c)
-  P WPy_p[N], WPcy_p[N];
-  enum { kWMx = 0, kWPx = 1, kH1y = 2, kFy = 3, kWold = 4 };
-  // components a carried vector needs: x states and y faces only their live ones
-  auto needed = [&](int v, int c) {
-    return (v == kWMx || v == kWPx) ? live<G, 0>(c) : v == kH1y ? live<G, 1>(c) : true;
-  };
-  auto cput = [&](int v, const P* a) {
-#pragma unroll
-    for (int c = 0; c < N; ++c)
-      if (needed(v, c)) carry[(v * N + c) * 32 + lane] = a[c];
-  };
-  auto cget = [&](int v, P* a) {
-#pragma unroll
-    for (int c = 0; c < N; ++c) a[c] = needed(v, c) ? carry[(v * N + c) * 32 + lane] : mk2(T(0), T(0));
-  };
 
   for (int q = q_s; q <= q_e; ++q) {
     const bool rowin = q <= dhi1;
@@ -591,7 +614,9 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
       // y predictor of row q
       if (ppm) {
         const bool hl = true, hr = q + 2 <= dhi1;
-        P dm[N], dp[N];
+        P dm[N], dp[N], sy0[N], Fy0[N];
+        cget(kSy, sy0);
+        cget(kFyf, Fy0);
 #pragma unroll
         for (int c = 0; c < N; ++c) {
           if (!live<G, 1>(c)) { sy1[c] = mk2(T(0), T(0)); Fy1[c] = sy1[c]; dm[c] = sy1[c]; dp[c] = sy1[c]; continue; }
@@ -602,9 +627,11 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
           dp[c] = psub(Fy1[c], W0[c]);
         }
         predict<G, 1, T>(ky, W0, dm, dp, plim, clim, WMy, WPy);
+        cput(kSy, sy1);
+        cput(kFyf, Fy1);
       } else {
 #pragma unroll
-        for (int c = 0; c < N; ++c) { WMy[c] = W0[c]; WPy[c] = W0[c]; sy1[c] = sy0[c]; Fy1[c] = Fy0[c]; }
+        for (int c = 0; c < N; ++c) { WMy[c] = W0[c]; WPy[c] = W0[c]; }
       }
       // x predictor of row q, first-pass x faces, corrected y states of row q
       xrow(W0, WMx, WPx, H1lo, H1hi);
@@ -614,6 +641,8 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
     }
     // first-pass y face q (lo face of row q)
     P H1y[N];
+    P WPy_p[N];
+    cget(kWPy, WPy_p);
     const bool need_h1y = (q > q_s) || (q == dlo1);
     if (need_h1y) {
       if (q == dlo1) {
@@ -633,6 +662,8 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
     }
     // final y face q
     P Fy[N];
+    P WPcy_p[N];
+    cget(kWPcy, WPcy_p);
     if (q >= it.y0) {
       if (q == dlo1 && fault) {
 #pragma unroll
@@ -702,11 +733,8 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<G>::value) ma
     cput(kH1y, H1y);
     cput(kFy, Fy);
     cput(kWold, W0);
-#pragma unroll
-    for (int c = 0; c < N; ++c) {
-      WPy_p[c] = WPy[c]; WPcy_p[c] = WPcy[c];
-      sy0[c] = sy1[c]; Fy0[c] = Fy1[c];
-    }
+    cput(kWPy, WPy);
+    cput(kWPcy, WPcy);
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
