@@ -32,8 +32,8 @@
 extern "C" {
 #endif
 
-#define TMK_ABI_VERSION 4   /* 2: tmk_scheme gained use_fourth_order_slopes; 3: tmk_tuning gained fault_first;
-                               4: tmk_tag_params gained slip_rate_thresh */
+#define TMK_ABI_VERSION 5   /* 2: tmk_scheme gained use_fourth_order_slopes; 3: tmk_tuning gained fault_first;
+                               4: tmk_tag_params gained slip_rate_thresh; 5: tmk_tuning gained plastic_fused */
 
 #define TMK_NCOMP      22   /* state components, srcLinElast/LEINDEX.H:12-47 */
 #define TMK_NSIDE_COMP 11   /* IX_OFFSET, srcLinElast/LEINDEX.H:23 */
@@ -138,7 +138,7 @@ typedef struct { int lo[2], hi[2]; } tmk_box;   /* cell-centred, inclusive */
  * loop has no such choices).  Defaults: the scheme's volume kernel, one wave
  * per marching group, runs of at least 16 rows, one antiplane slot per
  * fault-kernel CTA, 32 fault faces per fault-kernel CTA, the fault kernel
- * after the in-plane marching kernel. */
+ * after the in-plane marching kernel, the plastic return as a pass. */
 typedef struct {
   int volume_kernel;    /* TMK_VOLUME_MARCH or TMK_VOLUME_TILE (march only if the scheme allows it) */
   int march_waves[2];   /* marching items of the in-plane / antiplane group, in waves of resident CTAs: 1..8 */
@@ -148,6 +148,10 @@ typedef struct {
   int fault_first;      /* 1: the fault kernel first, running beside the in-plane marching kernel
                            (2-warp CTAs fit in the registers two in-plane CTAs leave free);
                            0: after it, beside the antiplane kernel */
+  int plastic_fused;    /* plastic levels of the marching form: 1: the Drucker-Prager return is
+                           applied by the in-plane marching kernel as it stores each cell (the
+                           antiplane kernel runs first, the fault kernel on a side stream beside
+                           both); 0: a pass over the level after the marching kernels */
 } tmk_tuning;
 
 /* Refinement tagging parameters (the comp.* keys of the input deck,

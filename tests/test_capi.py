@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(cuda_lib):
 
 
 def test_abi_version(cuda_lib):
-    assert cuda_lib.tmk_abi_version() == 4
+    assert cuda_lib.tmk_abi_version() == 5
 
 
 def _create(lib, sc, rs=True, sw=False, pl=False):

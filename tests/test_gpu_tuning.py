@@ -15,11 +15,12 @@ G = A.TMK_NGHOST
 BOXES = [(0, 0, 20, 9), (21, 0, 63, 9), (0, 10, 31, 31), (32, 10, 63, 31)]
 
 
-def _tuning(volume="march", waves=(1, 1), min_run=16, disp=1, seg=32, first=0):
+def _tuning(volume="march", waves=(1, 1), min_run=16, disp=1, seg=32, first=0, fused=0):
     t = A.Tuning()
     t.volume_kernel = A.TMK_VOLUME_MARCH if volume == "march" else A.TMK_VOLUME_TILE
     t.march_waves[0], t.march_waves[1] = waves
     t.min_run, t.fault_displace, t.fault_seg, t.fault_first = min_run, disp, seg, first
+    t.plastic_fused = fused
     return t
 
 
@@ -62,6 +63,59 @@ def test_every_marching_tuning_computes_the_same_step(cuda_lib, prec):
     U, B = _run(sc, Ug, Bg, _tuning(volume="tile", seg=16))
     tol = 1e-12 if prec == A.TMK_PREC_FP64 else 1e-4
     assert rel_err(U[:, G:-G, G:-G], U0[:, G:-G, G:-G]) <= tol
+
+
+@pytest.mark.parametrize("prec", [A.TMK_PREC_FP64, A.TMK_PREC_MIXED], ids=["fp64", "mixed"])
+def test_plastic_return_fused_or_as_a_pass_computes_the_same_step(cuda_lib, prec):
+    """A plastic level: the Drucker-Prager return applied by the in-plane
+    marching kernel's stores (antiplane kernel first, fault kernel on a side
+    stream) equals the return as a pass after the marching kernels -- bit for
+    bit in the FP64 form, to FP32 rounding in the mixed form -- across
+    work-list shapes; the state yields somewhere."""
+    sc = S.slip_weakening(nx=64, ny=32, dx=0.1, precision=prec, plasticity=True)
+    rng = np.random.default_rng(45)
+    Ug = perturbed_state(sc, rng, amp_v=0.05, amp_s=1.0)
+    for side in (0, 11):                         # shear above the yield stress in a band
+        Ug[side + 6, G + 8:G + 14, :] += 60.0
+    Bg = sc.initial_B()
+    U0, B0 = _run(sc, Ug, Bg, _tuning(fused=0))
+    assert U0[9, G:-G, G:-G].max() > 0 and U0[10, G:-G, G:-G].max() > 0, "the state must yield"
+    tol = 0.0 if prec == A.TMK_PREC_FP64 else 1e-5
+    for v in (dict(fused=1), dict(fused=1, waves=(2, 2), min_run=8, seg=16), dict(fused=0, first=1, disp=0)):
+        U, B = _run(sc, Ug, Bg, _tuning(**v))
+        assert rel_err(U[:, G:-G, G:-G], U0[:, G:-G, G:-G]) <= tol, v
+        assert rel_err(B[:, G:-G], B0[:, G:-G]) <= max(tol, 1e-300), v
+
+
+def test_plastic_hierarchy_with_the_fused_return_matches_the_pass(cuda_lib):
+    """A ratio-4 plastic hierarchy whose levels apply the fused return steps as
+    the one with the return as a pass (FP64, bit for bit)."""
+    from tetemoko_gb300.amr import AMRHierarchy
+    from tetemoko_gb300.level import Context
+    from tests.test_gpu_amr import _levels_on_gpu, _read
+    sc = S.slip_weakening(nx=64, ny=32, dx=0.1, plasticity=True)
+    datas = H.hierarchy(sc, np.random.default_rng(46), nlev=3, ratios=(4, 4))
+    ctx = Context(sc)
+    res = []
+    for fused in (0, 1):
+        lvs = _levels_on_gpu(ctx, datas)
+        h = AMRHierarchy(lvs, [4, 4])
+        for lv in lvs:
+            lv.set_tuning(_tuning(fused=fused))
+        for _ in range(2):
+            h.step(sc.dt())
+        res.append([_read(lv, d) for lv, d in zip(lvs, datas)])
+        for lv in lvs:
+            assert lv.status()[0] == 0
+        h.close()
+        for lv in lvs:
+            lv.close()
+    for a, b in zip(*res):
+        for p in range(len(a.boxes)):
+            np.testing.assert_array_equal(a.U[p][:, G:-G, G:-G], b.U[p][:, G:-G, G:-G])
+            if a.B[p] is not None:
+                np.testing.assert_array_equal(a.B[p][:, G:-G], b.B[p][:, G:-G])
+    ctx.close()
 
 
 def test_autotune_keeps_the_state_and_picks_a_valid_tuning(cuda_lib):
@@ -111,7 +165,7 @@ def test_tuning_is_refused_where_unsafe(cuda_lib):
     ctx = Context(sc)
     lvl = LinElastLevelGodunov(ctx, BOXES)
     lvl.set_level(sc.initial_U(), sc.initial_B())
-    for bad in (dict(waves=(0, 1)), dict(min_run=2), dict(disp=9), dict(seg=8), dict(first=2)):
+    for bad in (dict(waves=(0, 1)), dict(min_run=2), dict(disp=9), dict(seg=8), dict(first=2), dict(fused=3)):
         with pytest.raises(A.TmkError):
             lvl.set_tuning(_tuning(**bad))
     g = lvl.graph(2, 0.0, sc.dt())

@@ -73,13 +73,14 @@ TMK_VOLUME_AUTO, TMK_VOLUME_TILE, TMK_VOLUME_MARCH = 0, 1, 2
 
 class Tuning(C.Structure):
     _fields_ = [("volume_kernel", C.c_int), ("march_waves", C.c_int * 2), ("min_run", C.c_int),
-                ("fault_displace", C.c_int), ("fault_seg", C.c_int), ("fault_first", C.c_int)]
+                ("fault_displace", C.c_int), ("fault_seg", C.c_int), ("fault_first", C.c_int),
+                ("plastic_fused", C.c_int)]
 
     def as_dict(self) -> dict:
         return {"volume_kernel": {TMK_VOLUME_MARCH: "march", TMK_VOLUME_TILE: "tile"}.get(self.volume_kernel),
                 "march_waves": list(self.march_waves), "min_run": self.min_run,
                 "fault_displace": self.fault_displace, "fault_seg": self.fault_seg,
-                "fault_first": self.fault_first}
+                "fault_first": self.fault_first, "plastic_fused": self.plastic_fused}
 
 
 class TagParams(C.Structure):

@@ -206,6 +206,7 @@ tmk_tuning default_tuning(int march_allowed) {
   t.fault_displace = kFaultDisplace;
   t.fault_seg = tmk::FAULT_SEG;
   t.fault_first = 0;
+  t.plastic_fused = 0;
   return t;
 }
 
@@ -216,6 +217,7 @@ bool tuning_ok(const tmk_level_s* L, const tmk_tuning& t) {
     if (t.march_waves[g] < 1 || t.march_waves[g] > 8) return false;
   if (t.min_run < 4 || t.min_run > 4096 || t.fault_displace < 0 || t.fault_displace > 4) return false;
   if (t.fault_first != 0 && t.fault_first != 1) return false;
+  if (t.plastic_fused != 0 && t.plastic_fused != 1) return false;
   return t.fault_seg == tmk::FAULT_SEG || t.fault_seg == tmk::FAULT_SEG_SMALL;
 }
 
@@ -254,8 +256,9 @@ tmk_status build_march_lists(tmk_level_s* L) {
     level_free(L, L->ditems[g]);
     level_free(L, L->dfrows[g]);
     level_free(L, L->stash[g]);
-    int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots(g)
-                                          : tmk::Launch<double>::march_slots(g);
+    const int gk = (g == 0 && L->ctx->scheme.plasticity && tu.plastic_fused) ? 2 : g;   // the kernel of group g
+    int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots(gk)
+                                          : tmk::Launch<double>::march_slots(gk);
     slots *= tu.march_waves[g];
     if (g == 1) slots = std::max(warps, slots - tu.fault_displace * warps * fault_ctas);
     std::vector<tmk::MarchItem> items, frows;
@@ -453,6 +456,9 @@ extern "C" void tmk_level_destroy(tmk_level* L) {
   for (void* p : L->allocs) cudaFree(p);
   for (void* p : L->cap_allocs) cudaFree(p);
   for (cudaEvent_t e : L->ev) cudaEventDestroy(e);
+  if (L->fork_ev) cudaEventDestroy(L->fork_ev);
+  if (L->join_ev) cudaEventDestroy(L->join_ev);
+  if (L->side) cudaStreamDestroy(L->side);
   delete L;
 }
 
@@ -747,6 +753,38 @@ tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEve
   mc.stash[1] = L->stash[1];
   mc.caps[0] = L->dmcap[0];
   mc.caps[1] = L->dmcap[1];
+  mc.plastic = c->scheme.plasticity && L->tune.plastic_fused;
+  if (mc.plastic) {
+    // plastic level with the fused return: the in-plane kernel applies the
+    // plastic return to each cell it stores, so it runs after the antiplane
+    // kernel (its programmatic dependent, which waits for it before it
+    // stores).  The fault kernel, which reads only the step's input, runs on a
+    // side stream beside both and is joined before the fault rows are finished
+    // (with per-launch timing it runs first and alone).
+    const bool fork = L->nfault && !ev;
+    if (fork) {
+      if (!L->side) {
+        TMK_CU(cudaStreamCreateWithFlags(&L->side, cudaStreamNonBlocking));
+        TMK_CU(cudaEventCreateWithFlags(&L->fork_ev, cudaEventDisableTiming));
+        TMK_CU(cudaEventCreateWithFlags(&L->join_ev, cudaEventDisableTiming));
+      }
+      TMK_CU(cudaEventRecord(L->fork_ev, s));
+      TMK_CU(cudaStreamWaitEvent(L->side, L->fork_ev, 0));
+      TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false,
+                                      L->tune.fault_seg, L->side));
+      TMK_CU(cudaEventRecord(L->join_ev, L->side));
+    } else {
+      TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false,
+                                      L->tune.fault_seg, s));
+      if (ev) TMK_CU(cudaEventRecord(ev[2], s));
+    }
+    TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, false, s));
+    TMK_CU(tmk::Launch<Real>::march(0, pd, L->ditems[0], L->nitems[0], mc, !ev, s));
+    if (fork) TMK_CU(cudaStreamWaitEvent(s, L->join_ev, 0));
+    TMK_CU(tmk::Launch<Real>::march_fault_rows(pd, nullptr, 0, L->dfrows[1], L->nfrows[1], mc, s));
+    TMK_CU(tmk::Launch<Real>::march_fault_rows(pd, L->dfrows[0], L->nfrows[0], nullptr, 0, mc, s));
+    return TMK_OK;
+  }
   if (ev) {
     TMK_CU(tmk::Launch<Real>::fault(pd, L->dfault, L->nfault, L->max_faces, L->dparams, time, c->dstatus, false, L->tune.fault_seg, s));
     TMK_CU(cudaEventRecord(ev[2], s));
@@ -762,6 +800,7 @@ tmk_status step_kernels(tmk_level_s* L, int par, double time, double dt, cudaEve
     TMK_CU(tmk::Launch<Real>::march(1, pd, L->ditems[1], L->nitems[1], mc, true, s));
   }
   TMK_CU(tmk::Launch<Real>::march_fault_rows(pd, L->dfrows[0], L->nfrows[0], L->dfrows[1], L->nfrows[1], mc, s));
+  // the plastic return as a pass over the level (PLASTICCORRECTION after the update)
   if (c->scheme.plasticity) TMK_CU(tmk::Launch<Real>::plastic(pd, L->dtiles, L->ntiles, L->dparams, s));
   return TMK_OK;
 }
@@ -889,7 +928,8 @@ tmk_status time_steps(tmk_level_s* L, double time, double dt, int steps, cudaStr
 
 // Candidate tunings of a level for the autotuners: every combination of the
 // marching choices (waves per group, shortest run, fault displacement, the
-// fault kernel's place in the step) and both fault-kernel variants, plus the
+// fault kernel's place in the step, on a plastic level the fused or separate
+// plastic return) and both fault-kernel variants, plus the
 // tile kernel; `reduced` leaves out the
 // shortest runs of 8 rows (the hierarchy autotuner times whole coarse steps).
 std::vector<tmk_tuning> tmk_host::tuning_candidates(const tmk_level_s* L, bool reduced) {
@@ -904,12 +944,17 @@ std::vector<tmk_tuning> tmk_host::tuning_candidates(const tmk_level_s* L, bool r
           for (int run : {8, 16, 32}) {
             if (reduced && run == 8) continue;
             for (int disp : {0, 1, 2})
-              for (int first : {0, 1}) {
-                if (first && disp == 2) continue;
-                t.march_waves[0] = w0; t.march_waves[1] = w1; t.min_run = run; t.fault_displace = disp;
-                t.fault_first = first;
-                out.push_back(t);
-              }
+              for (int first : {0, 1})
+                for (int fused : {0, 1}) {
+                  if (first && disp == 2) continue;
+                  // the fused return fixes the kernels' order: fault_first and the
+                  // displacement do not apply
+                  if (fused && (!L->ctx->scheme.plasticity || first || disp)) continue;
+                  t.march_waves[0] = w0; t.march_waves[1] = w1; t.min_run = run; t.fault_displace = disp;
+                  t.fault_first = first;
+                  t.plastic_fused = fused;
+                  out.push_back(t);
+                }
           }
     }
     tmk_tuning tt = default_tuning(L->march_allowed);
@@ -978,8 +1023,12 @@ extern "C" tmk_status tmk_level_autotune(tmk_level* L, double time, double dt, i
 
 extern "C" int tmk_level_launches_per_step(const tmk_level* L) {
   if (!L) return 0;
-  const int vol = L->march ? (L->nitems[0] ? 1 : 0) + (L->nitems[1] ? 1 : 0) + (L->nfrows[0] + L->nfrows[1] ? 1 : 0) +
-                               (L->ctx->scheme.plasticity && L->ntiles ? 1 : 0)
+  // marching form: the two groups' kernels, the fault-row finisher (two
+  // launches with the fused plastic return) and the plastic pass
+  const bool plastic = L->ctx->scheme.plasticity != 0, fused = plastic && L->tune.plastic_fused;
+  const int frows = fused ? (L->nfrows[0] ? 1 : 0) + (L->nfrows[1] ? 1 : 0) : (L->nfrows[0] + L->nfrows[1] ? 1 : 0);
+  const int vol = L->march ? (L->nitems[0] ? 1 : 0) + (L->nitems[1] ? 1 : 0) + frows +
+                                 (plastic && !fused && L->ntiles ? 1 : 0)
                            : (L->ntiles ? 1 : 0);
   return (L->ncopies ? 1 : 0) + (L->nbcopies ? 1 : 0) + (L->nfault ? 1 : 0) + vol + amr_launches(L);
 }

@@ -109,6 +109,10 @@ struct tmk_level_s {
   int parity = 0;
   double cur_dt = -1.0;
   std::vector<void*> allocs;
+  // with the fused plastic return the fault kernel runs on a side stream
+  // forked from the step's stream and joined before the fault rows are finished
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   // per-launch timing (tmk_level_profile)
   std::vector<cudaEvent_t> ev;            // 4 events per recorded step
   int prof_on = 0, prof_max = 0, prof_n = 0;

@@ -42,6 +42,7 @@ struct Launch {
                                       const MarchItem* rows1, int n1, const MarchConst<Real>& mc,
                                       cudaStream_t s);
   // warps of group g's marching kernel resident at once on the current device
+  // (g = 2: the in-plane kernel with the fused plastic return)
   static int march_slots(int g);
   // warps per CTA of the marching kernels
   static int march_warps();

@@ -68,8 +68,12 @@ struct LaunchImpl {
                                             (int)march_smem_bytes<Real, 0>());
       cudaError_t e1 = cudaFuncSetAttribute(march_kernel<Real, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)march_smem_bytes<Real, 1>());
+      cudaError_t e2 = cudaFuncSetAttribute(march_kernel<Real, 0, true>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)march_smem_bytes<Real, 0>());
       if (e0 != cudaSuccess) return e0;
       if (e1 != cudaSuccess) return e1;
+      if (e2 != cudaSuccess) return e2;
       configured = true;
     }
     cudaLaunchAttribute attr[1];
@@ -83,6 +87,7 @@ struct LaunchImpl {
     cfg.numAttrs = pdl ? 1 : 0;
     if (g == 0) {
       cfg.dynamicSmemBytes = march_smem_bytes<Real, 0>();
+      if (mc.plastic) return cudaLaunchKernelEx(&cfg, march_kernel<Real, 0, true>, patches, items, nitems, mc);
       return cudaLaunchKernelEx(&cfg, march_kernel<Real, 0>, patches, items, nitems, mc);
     }
     cfg.dynamicSmemBytes = march_smem_bytes<Real, 1>();
@@ -105,6 +110,11 @@ struct LaunchImpl {
       cudaFuncSetAttribute(march_kernel<Real, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)march_smem_bytes<Real, 0>());
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, march_kernel<Real, 0>, 32 * MARCH_WARPS,
+                                                        march_smem_bytes<Real, 0>());
+    } else if (g == 2) {      // the in-plane kernel with the fused plastic return
+      cudaFuncSetAttribute(march_kernel<Real, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)march_smem_bytes<Real, 0>());
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, march_kernel<Real, 0, true>, 32 * MARCH_WARPS,
                                                         march_smem_bytes<Real, 0>());
     } else {
       cudaFuncSetAttribute(march_kernel<Real, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -146,6 +146,12 @@ struct MarchConst {
   int xout_lo, xout_hi, yout_lo, yout_hi;
   void* stash[2];    // row-0 intermediates of the fault-row items, per component group
   const int4* caps[2];   // coarse-fine faces each group's items store (row, kind, lane, slot)
+  // Drucker-Prager return of a plastic level when it is fused into the
+  // in-plane group's stores (the antiplane group's updated stresses are stored
+  // first); the level's tuning sets `plastic`
+  PlasticK<T> pk;
+  T pdt;
+  int plastic;
   TMK_HD void load(const DevParams& p, double dt, double dx) {
     const double dtdx = dt / dx;
     kx.load(p, 0, dtdx, -(1.0 / 2.0) * dt / dx);
@@ -154,6 +160,9 @@ struct MarchConst {
     sc = mk2((T)(-dt / dx), (T)(-dt / dx));
     plim = p.prim_lim != 0; clim = p.char_lim != 0; lim = plim || clim; ppm = p.order != 0;
     xout_lo = p.bc[0] == 0; xout_hi = p.bc[1] == 0; yout_lo = p.bc[2] == 0; yout_hi = p.bc[3] == 0;
+    plastic = 0;
+    pk.load(p);
+    pdt = (T)dt;
   }
 };
 
@@ -419,6 +428,53 @@ template <typename T> TMK_D void cp_async_elem(T* dst_smem, const T* src) {
 TMK_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 TMK_D void cp_async_wait_all_but_newest() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
+// The inputs of a cell's plastic return the in-plane group does not hold: the
+// antiplane group's updated sxz, syz (stored by the antiplane kernel, which
+// has completed) and the plastic strain of the step's input, both sides.
+template <typename T>
+TMK_D void plastic_inputs(const PatchDev<T>& pp, size_t o, size_t plane, typename PairOf<T>::P* pin) {
+  pin[0] = mk2(pp.Uout[o + 7 * plane], pp.Uout[o + 18 * plane]);
+  pin[1] = mk2(pp.Uout[o + 8 * plane], pp.Uout[o + 19 * plane]);
+  pin[2] = mk2(pp.Uin[o + 10 * plane], pp.Uin[o + 21 * plane]);
+}
+
+// Stores the updated group G of one cell (flat index o of component 0).  With
+// PL (a plastic level whose return is fused) the in-plane group first takes
+// LinElastLevelGodunov::plasticUpdate (PLASTICCORRECTION,
+// srcLinElast/PlasticPhysicsF.ChF:30-133, as the reference applies it after
+// the level's update, LinElastLevelGodunov.cpp:643-667): the cell's six
+// updated stresses and its plastic strain (pin, from plastic_inputs) give the
+// return; the antiplane stresses are rewritten where the point yielded, the
+// plastic rate and strain always.
+template <typename T, int G, bool PL>
+TMK_D void store_cell(const PatchDev<T>& pp, const MarchConst<T>& mc, size_t o, size_t plane,
+                      typename PairOf<T>::P* u, const typename PairOf<T>::P* pin) {
+  constexpr int N = Grp<G>::N;
+  if constexpr (G == 0 && PL) {
+    T sxz[2] = {pin[0].x, pin[0].y}, syz[2] = {pin[1].x, pin[1].y}, gam[2] = {pin[2].x, pin[2].y};
+#pragma unroll
+    for (int sd = 0; sd < 2; ++sd) {
+      T sxx = sd ? u[2].y : u[2].x, syy = sd ? u[3].y : u[3].x;
+      T szz = sd ? u[4].y : u[4].x, sxy = sd ? u[5].y : u[5].x;
+      T lam;
+      if (plastic_flow_k<T>(mc.pk, sxx, syy, szz, sxy, sxz[sd], syz[sd], lam, gam[sd], mc.pdt)) {
+        if (sd) { u[2].y = sxx; u[3].y = syy; u[4].y = szz; u[5].y = sxy; }
+        else { u[2].x = sxx; u[3].x = syy; u[4].x = szz; u[5].x = sxy; }
+        pp.Uout[o + (size_t)(11 * sd + 7) * plane] = sxz[sd];
+        pp.Uout[o + (size_t)(11 * sd + 8) * plane] = syz[sd];
+      }
+      pp.Uout[o + (size_t)(11 * sd + 9) * plane] = lam;
+      pp.Uout[o + (size_t)(11 * sd + 10) * plane] = gam[sd];
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    const int gg = Grp<G>::glob(c);
+    pp.Uout[o + (size_t)gg * plane] = u[c].x;
+    pp.Uout[o + (size_t)(11 + gg) * plane] = u[c].y;
+  }
+}
+
 // Fluxes of the coarse-fine faces of row `row` that this item owns, into the
 // level's flux-register capture buffer (flux registers of the AMR coupling).
 // Entry kinds: 0 the x face below the lane's column, 1 the one above, 2 the
@@ -447,7 +503,10 @@ TMK_D void march_capture(const PatchDev<T>& pp, const MarchItem& it, const March
   }
 }
 
-template <typename T, int G>
+// PL: a plastic level with the fused return (in-plane group only): every
+// stored cell takes the plastic return, and the kernel runs after the
+// antiplane one.
+template <typename T, int G, bool PL = false>
 __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value) march_kernel(const PatchDev<T>* __restrict__ patches,
                                                                  const MarchItem* __restrict__ items, int nitems,
                                                                  const __grid_constant__ MarchConst<T> mc) {
@@ -467,6 +526,8 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
     asm volatile("griddepcontrol.wait;" ::: "memory");
     return;
   }
+  // the fused plastic return reads the antiplane kernel's stresses: wait for it
+  if (PL) asm volatile("griddepcontrol.wait;" ::: "memory");
   const MarchItem it = items[wid];
   const PatchDev<T>& pp = patches[it.patch];
   const int x = it.x0 - 3 + lane;
@@ -603,6 +664,12 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
   for (int q = q_s; q <= q_e; ++q) {
     const bool rowin = q <= dhi1;
     load_row_async(q + 3);            // next row in flight while this one is computed
+    // fused plastic return: its other inputs for row q-1, stored at the end of
+    // this iteration, requested now so that the row's work hides their latency
+    P pin[3];
+    if constexpr (PL) {
+      if (col_valid && q - 1 >= it.y0 && q - 1 <= it.y1) plastic_inputs<T>(pp, fab_idx(pp, 0, x, q - 1), plane, pin);
+    }
     cp_async_wait_all_but_newest();   // rows up to q+2 have landed
     P W0[N], W1[N], W2[N];
     get_row(q, W0);
@@ -715,15 +782,10 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
       cget(kFy, Fy_p);
       cget(kWold, Wold);
       if (col_valid && yr <= it.y1) {
-        const size_t o = fab_idx(pp, 0, x, yr);
+        P u[N];
 #pragma unroll
-        for (int c = 0; c < N; ++c) {
-          const int gg = Grp<G>::glob(c);
-          P du = padd(psub(Fxh[c], Fx[c]), psub(Fy[c], Fy_p[c]));
-          P u = pfma(du, sc, Wold[c]);
-          pp.Uout[o + (size_t)gg * plane] = u.x;
-          pp.Uout[o + (size_t)(11 + gg) * plane] = u.y;
-        }
+        for (int c = 0; c < N; ++c) u[c] = pfma(padd(psub(Fxh[c], Fx[c]), psub(Fy[c], Fy_p[c])), sc, Wold[c]);
+        store_cell<T, G, PL>(pp, mc, fab_idx(pp, 0, x, yr), plane, u, pin);
       }
       if (it.ncap && yr <= it.y1) march_capture<T, G>(pp, it, mc, yr, lane, Fx, Fxh, Fy_p, Fy, cpos);
     }
@@ -786,20 +848,23 @@ TMK_D void fault_row_finish(const PatchDev<T>& pp, const MarchItem& it, const Ma
   }
   const bool col_valid = x >= it.x0 && x < it.x0 + MARCH_COLS && x >= pp.vlo0 && x <= pp.vhi0;
   if (col_valid) {
-    const size_t plane = (size_t)pp.anx * pp.any;
-    const size_t o = fab_idx(pp, 0, x, dlo1);
+    P u[N];
 #pragma unroll
-    for (int c = 0; c < N; ++c) {
-      const int gg = Grp<G>::glob(c);
-      P du = padd(psub(Fxh[c], Fx[c]), psub(Fy1[c], Fy0[c]));
-      P u = pfma(du, mc.sc, Wold[c]);
-      pp.Uout[o + (size_t)gg * plane] = u.x;
-      pp.Uout[o + (size_t)(11 + gg) * plane] = u.y;
+    for (int c = 0; c < N; ++c) u[c] = pfma(padd(psub(Fxh[c], Fx[c]), psub(Fy1[c], Fy0[c])), mc.sc, Wold[c]);
+    const size_t plane = (size_t)pp.anx * pp.any, o = fab_idx(pp, 0, x, dlo1);
+    P pin[3];
+    if (mc.plastic) {
+      plastic_inputs<T>(pp, o, plane, pin);
+      store_cell<T, G, true>(pp, mc, o, plane, u, pin);
+    } else {
+      store_cell<T, G, false>(pp, mc, o, plane, u, pin);
     }
   }
 }
 
-// One warp per fault-row strip: rows0 (in-plane) then rows1 (antiplane).
+// One warp per fault-row strip: rows0 (in-plane) then rows1 (antiplane).  With
+// the fused plastic return the antiplane rows are finished by a launch of
+// their own before the in-plane ones (whose stores apply the return).
 template <typename T>
 __global__ void __launch_bounds__(32 * MARCH_WARPS) march_fault_row_kernel(const PatchDev<T>* __restrict__ patches,
                                                                            const MarchItem* __restrict__ rows0, int n0,
