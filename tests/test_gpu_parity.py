@@ -244,3 +244,36 @@ def test_plm_level_steps_match_oracle(cuda_lib, name):
     assert lvl.status()[0] == 0
     lvl.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("name", ["rs_slip", "sw_ref9"])
+def test_patch_step_staged_by_tma_or_element_wise_is_the_same(cuda_lib, name):
+    """The tile kernel stages each tile and its halo with one TMA tensor copy
+    when the FAB's base and row pitch are 16-byte aligned, else element by
+    element: a FAB one column wider (odd row pitch in FP64) takes the second
+    path, and the step is the same bit for bit."""
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov
+    sc = dict(SCEN)[name]
+    g = A.TMK_NGHOST
+    valid = (5, 0, 40, 13)                      # 36 columns: a row of 44 FP64 values (16-byte pitch)
+    ulo = (valid[0] - g, valid[1] - g)
+    rng = np.random.default_rng(4321)
+    U0 = perturbed_state(sc, rng, lo=valid[:2], hi=valid[2:])
+    B0 = _random_B(sc, rng, valid[2] - valid[0] + 1 + 2 * g)
+    U1 = np.concatenate([U0, U0[:, :, -1:]], axis=2)     # one more ghost column on the right
+    assert U0.shape[2] * 8 % 16 == 0 and U1.shape[2] * 8 % 16 != 0
+    ctx = Context(sc)
+    out = []
+    for U in (U0, U1):
+        pg = LinElastPatchGodunov(ctx)
+        pg.set_current_box(valid)
+        pg.set_current_time(0.5)
+        Ud = torch.from_numpy(np.ascontiguousarray(U)).cuda()
+        Bd = torch.from_numpy(B0.copy()).cuda()
+        _, Fx, Fy = pg.update_state(Ud, ulo, sc.dt(), B=Bd, bxlo=valid[0] - g, with_flux=True)
+        torch.cuda.synchronize()
+        out.append((Ud.cpu().numpy()[:, :, :U0.shape[2]], Bd.cpu().numpy(), Fx.cpu().numpy(), Fy.cpu().numpy()))
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a, b)
+    ctx.close()

@@ -6,6 +6,7 @@
 //   tmk_level    device mirrors of every patch of one level (two state buffers
 //                swapped each step, fault data, fault-face buffers), the tile
 //                work list of the volume kernel and the exchange lists.
+#include <cuda.h>            // CUtensorMap and its enums (the encoder is reached through the runtime)
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
@@ -285,6 +286,36 @@ tmk_status build_march_lists(tmk_level_s* L) {
 
 }  // namespace
 
+bool tmk_host::encode_fab_map(void* map, const void* data, int elem, int anx, int any, int box_x, int box_y) {
+  typedef CUresult (*Encode)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                             const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                             CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static Encode encode = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = (Encode)f;
+  }
+  if (!encode || !data || ((uintptr_t)data % 16) != 0 || ((size_t)anx * elem) % 16 != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)anx, (cuuint64_t)any, (cuuint64_t)TMK_NCOMP};
+  const cuuint64_t strides[2] = {(cuuint64_t)anx * elem, (cuuint64_t)anx * any * elem};
+  const cuuint32_t box[3] = {(cuuint32_t)box_x, (cuuint32_t)box_y, (cuuint32_t)tmk::NSIDE};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUtensorMap m;
+  // cells beyond the tensor read as zero (OOB fill NONE fills zeros)
+  if (encode(&m, elem == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+             const_cast<void*>(data), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+      CUDA_SUCCESS)
+    return false;
+  std::memcpy(map, &m, sizeof(m));
+  return true;
+}
+
 // ---------------------------------------------------------------- patch API
 extern "C" tmk_status tmk_patch_update_state(tmk_context* c, const tmk_fab* U, const tmk_fab* B, const tmk_fab* Fx,
                                              const tmk_fab* Fy, const tmk_box* valid, const tmk_box* domain,
@@ -321,7 +352,8 @@ extern "C" tmk_status tmk_patch_update_state(tmk_context* c, const tmk_fab* U, c
   size_t off_pd = align_up(off_ff + (size_t)TMK_NCOMP * nvx * sizeof(double));
   size_t off_tl = align_up(off_pd + sizeof(PatchDev<double>));
   size_t off_fp = align_up(off_tl + tiles.size() * sizeof(TileDev));
-  size_t total = align_up(off_fp + sizeof(int));
+  size_t off_tm = align_up(off_fp + sizeof(int));
+  size_t total = align_up(off_tm + sizeof(CUtensorMap));
   if (total > c->scratch_bytes) {
     TMK_CU(cudaStreamSynchronize(s));
     cudaFree(c->scratch);
@@ -346,11 +378,18 @@ extern "C" tmk_status tmk_patch_update_state(tmk_context* c, const tmk_fab* U, c
   pd.nfirst = nfirst;
   pd.Fx = Fx ? Fx->data : nullptr;
   pd.Fy = Fy ? Fy->data : nullptr;
+  pd.status = c->dstatus;
+  // the tile kernel stages its tiles with TMA when U's layout allows a tensor map
+  alignas(64) unsigned char tmap[sizeof(CUtensorMap)];
+  const bool use_tma = encode_fab_map(tmap, U->data, (int)sizeof(double), anx, any,
+                                      tmk::Launch<double>::volume_box_x(), tmk::Launch<double>::volume_box_y());
+  pd.tmap = use_tma ? (const void*)(base + off_tm) : nullptr;
   const int zero = 0;
   // descriptors are staged through pageable memory: synchronous with respect to the host
   TMK_CU(cudaMemcpyAsync(base + off_pd, &pd, sizeof(pd), cudaMemcpyHostToDevice, s));
   TMK_CU(cudaMemcpyAsync(base + off_tl, tiles.data(), tiles.size() * sizeof(TileDev), cudaMemcpyHostToDevice, s));
   TMK_CU(cudaMemcpyAsync(base + off_fp, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+  if (use_tma) TMK_CU(cudaMemcpyAsync(base + off_tm, tmap, sizeof(tmap), cudaMemcpyHostToDevice, s));
   if (Fx) TMK_CU(cudaMemsetAsync(Fx->data, 0, (size_t)TMK_NCOMP * (nvx + 1) * nvy * sizeof(double), s));
   if (Fy) TMK_CU(cudaMemsetAsync(Fy->data, 0, (size_t)TMK_NCOMP * nvx * (nvy + 1) * sizeof(double), s));
   const PatchDev<double>* dpd = (const PatchDev<double>*)(base + off_pd);
@@ -404,6 +443,10 @@ void fill_patchdev(tmk_level_s* L, int parity) {
     d.cap = L->cap;
     d.caplist = L->dcaplist;
     d.fric = lp.fric;
+    d.tmap = L->tmap_ok.size() > p && L->tmap_ok[p]
+                 ? (const void*)(L->dtmaps + ((size_t)parity * L->patches.size() + p) * sizeof(CUtensorMap))
+                 : nullptr;
+    d.status = L->ctx->dstatus;
   }
 }
 
@@ -563,6 +606,24 @@ tmk_status level_create_impl(tmk_context* const* ctxs, int nscen, const tmk_box*
   for (int k = 0; k < 2; ++k) {
     if (cudaMalloc(&L->dpatch[k], pds * npatch) != cudaSuccess) return fail(TMK_ERR_ALLOC);
     L->allocs.push_back(L->dpatch[k]);
+  }
+  // TMA tensor maps of every patch's two state buffers, for the tile kernel
+  {
+    const int rs_ = (int)real_size(L->prec);
+    const int bx = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::volume_box_x() : tmk::Launch<double>::volume_box_x();
+    const int by = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::volume_box_y() : tmk::Launch<double>::volume_box_y();
+    std::vector<unsigned char> h((size_t)2 * npatch * sizeof(CUtensorMap), 0);
+    L->tmap_ok.assign(npatch, 1);
+    for (int k = 0; k < 2; ++k)
+      for (int p = 0; p < npatch; ++p) {
+        const LevelPatch& lp = L->patches[p];
+        const int anx = lp.alloc.hi[0] - lp.alloc.lo[0] + 1, any = lp.alloc.hi[1] - lp.alloc.lo[1] + 1;
+        if (!encode_fab_map(h.data() + ((size_t)k * npatch + p) * sizeof(CUtensorMap), lp.U[k], rs_, anx, any, bx, by))
+          L->tmap_ok[p] = 0;
+      }
+    if (cudaMalloc(&L->dtmaps, h.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
+    L->allocs.push_back(L->dtmaps);
+    TMK_CU(cudaMemcpy(L->dtmaps, h.data(), h.size(), cudaMemcpyHostToDevice));
   }
   if (dalloc(&L->dtiles, tiles.size()) != cudaSuccess) return fail(TMK_ERR_ALLOC);
   L->allocs.push_back(L->dtiles);

@@ -53,6 +53,13 @@ struct LevelPatch {
 
 struct CFLink;   // coarse-fine coupling of a level with its coarser level (tmk_amr.cu)
 
+// A TMA tensor map (128 bytes) of a FAB seen as a 3-D tensor (x, y,
+// component) with element size `elem`, for the tile kernel's staged box of
+// box_x x box_y cells of one side's 11 components.  False (map untouched) when
+// the driver's encoder is not available or the FAB's base or row pitch is not
+// 16-byte aligned: the kernel then loads element by element.
+bool encode_fab_map(void* map, const void* data, int elem, int anx, int any, int box_x, int box_y);
+
 }  // namespace tmk_host
 
 struct tmk_context_s {
@@ -82,6 +89,8 @@ struct tmk_level_s {
   int prec = TMK_PREC_FP64;
   std::vector<tmk_host::LevelPatch> patches;
   void* dpatch[2] = {nullptr, nullptr};   // PatchDev arrays, parity 0 (U0->U1) and 1 (U1->U0)
+  unsigned char* dtmaps = nullptr;         // TMA tensor maps of each patch's buffers: [parity][patch], 128 B each
+  std::vector<char> tmap_ok;               // per patch: its buffers have tensor maps
   std::vector<char> hpatch[2];
   std::vector<tmk::TileDev> htiles;        // tile list (host copy; capture ranges rewritten by the AMR links)
   tmk::TileDev* dtiles = nullptr;

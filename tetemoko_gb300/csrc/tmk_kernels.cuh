@@ -43,6 +43,9 @@ struct PatchDev {
   double* cap;              // captured face fluxes of the level (flux registers), 22 per slot
   const int4* caplist;      // (dir, i, j, slot) of the captured faces, grouped by tile
   const double* fric;       // optional per-face rate-and-state a, b, L: 3 planes like B (stride bnx)
+  const void* tmap;         // TMA tensor map of Uin (x, y, component) for the tile kernel's staged
+                            // load, in global memory; null: the tile kernel loads element by element
+  DevStatus* status;        // where the tile kernel reports a staged load that never landed
 };
 
 // A tile of the volume kernel; [cap0, cap0+ncap) are the captured faces it owns.
@@ -334,14 +337,46 @@ __global__ void __launch_bounds__(NT) fault_kernel(const PatchDev<Real>* __restr
 template <typename Real, int TX, int TY>
 struct VolSmem {
   static constexpr int RX = TX + 6, RY = TY + 6, PX = TX + 2, PY = TY + 2;
-  Real W[NSIDE][RY][RX];
+  // staged rows: RXP columns from the 16-byte boundary at or before the
+  // tile's first halo column (a TMA box starts on a 16-byte boundary in x)
+  static constexpr int AX = 16 / (int)sizeof(Real);
+  static constexpr int RXP = (RX + AX - 1 + AX - 1) / AX * AX;
+  Real W[NSIDE][RY][RXP];
   Real WMx[NSIDE][PY][PX], WPx[NSIDE][PY][PX];
   Real WMy[NSIDE][PY][PX], WPy[NSIDE][PY][PX];
   Real H1x[NSIDE][PY][TX + 1];
   Real H1y[NSIDE][TY + 1][PX];
   Real Fx[NSIDE][TY][TX + 1];
   Real Fy[NSIDE][TY + 1][TX];
+  unsigned long long bar;        // mbarrier of the staged load
 };
+
+// ---- TMA: one tensor copy of a box (x, y, component) into shared memory,
+// completion counted on an mbarrier
+TMK_D unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+TMK_D void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // visible to the copy engine
+}
+TMK_D void tma_load_3d(void* dst, const void* tmap, int x, int y, int z, unsigned long long* bar, unsigned bytes) {
+  // the map sits in global memory, written by a copy from the host: order it for the tensormap proxy
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tmap) : "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar)) : "memory");
+}
+// Wait for phase `parity` of the mbarrier, at most `limit` polls; false if it never completed.
+TMK_D bool mbar_wait(unsigned long long* bar, unsigned parity, int limit) {
+  for (int i = 0; i < limit; ++i) {
+    unsigned done;
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+constexpr int TMA_WAIT_POLLS = 1 << 20;
 
 template <typename Real, int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __restrict__ patches,
@@ -349,7 +384,7 @@ __global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __rest
                                                     const DevParams* __restrict__ params) {
   using T = Real;
   using S = VolSmem<Real, TX, TY>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   S& sm = *reinterpret_cast<S*>(smem_raw);
   const TileDev tl = tiles[blockIdx.x];
   const int s = blockIdx.y;                // side
@@ -370,16 +405,45 @@ __global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __rest
   const bool outx_lo = P.bc[0] == 0, outx_hi = P.bc[1] == 0;
   const bool outy_lo = P.bc[2] == 0, outy_hi = P.bc[3] == 0;
 
-  // ---- load W over [x0-3, x0+TX+2] x [y0-3, y0+TY+2]
-  for (int idx = threadIdx.x; idx < NSIDE * S::RY * S::RX; idx += NT) {
-    int c = idx / (S::RY * S::RX), r = (idx / S::RX) % S::RY, q = idx % S::RX;
-    int x = x0 - 3 + q, y = y0 - 3 + r;
-    T v = T(0);
-    if (x >= p.dlo0 && x <= p.dhi0 && y >= p.dlo1 && y <= p.dhi1 && q < tnx + 6 && r < tny + 6)
-      v = p.Uin[fab_idx(p, 11 * s + c, x, y)];
-    sm.W[c][r][q] = v;
+  // ---- stage W over [x0-3, x0+TX+2] x [y0-3, y0+TY+2]; column x0-3+q sits at W[..][q + wo]
+  int wo = 0;
+  if (p.tmap) {
+    // one TMA tensor copy of the side's 11 components over the tile and its halo,
+    // from the 16-byte boundary at or before x0-3 (cells beyond the FAB read 0)
+    const int xr = x0 - 3 - p.alo0;
+    wo = ((xr % S::AX) + S::AX) % S::AX;
+    if (threadIdx.x == 0) mbar_init(&sm.bar);
+    __syncthreads();
+    if (threadIdx.x == 0)
+      tma_load_3d(&sm.W[0][0][0], p.tmap, xr - wo, y0 - 3 - p.alo1, 11 * s, &sm.bar,
+                  (unsigned)(NSIDE * S::RY * S::RXP * sizeof(Real)));
+    const bool landed = mbar_wait(&sm.bar, 0, TMA_WAIT_POLLS);
+    if (__syncthreads_or(!landed)) {     // the whole CTA agrees
+      // the copy never landed: record it, give it one more bounded wait, leave
+      if (threadIdx.x == 0 && p.status) report(p.status, ST_TIMEOUT, (long long)blockIdx.x);
+      mbar_wait(&sm.bar, 0, TMA_WAIT_POLLS);
+      return;
+    }
+    // cells outside the domain stage as zeros, as the element-wise load leaves them
+    if (x0 - 3 < p.dlo0 || x0 + tnx + 2 > p.dhi0 || y0 - 3 < p.dlo1 || y0 + tny + 2 > p.dhi1) {
+      for (int idx = threadIdx.x; idx < NSIDE * S::RY * S::RX; idx += NT) {
+        int c = idx / (S::RY * S::RX), r = (idx / S::RX) % S::RY, q = idx % S::RX;
+        int x = x0 - 3 + q, y = y0 - 3 + r;
+        if (x < p.dlo0 || x > p.dhi0 || y < p.dlo1 || y > p.dhi1) sm.W[c][r][q + wo] = T(0);
+      }
+      __syncthreads();
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < NSIDE * S::RY * S::RX; idx += NT) {
+      int c = idx / (S::RY * S::RX), r = (idx / S::RX) % S::RY, q = idx % S::RX;
+      int x = x0 - 3 + q, y = y0 - 3 + r;
+      T v = T(0);
+      if (x >= p.dlo0 && x <= p.dhi0 && y >= p.dlo1 && y <= p.dhi1 && q < tnx + 6 && r < tny + 6)
+        v = p.Uin[fab_idx(p, 11 * s + c, x, y)];
+      sm.W[c][r][q] = v;
+    }
+    __syncthreads();
   }
-  __syncthreads();
 
   // ---- normal predictors on cells [x0-1, x0+nx] x [y0-1, y0+ny]
   for (int idx = threadIdx.x; idx < (tny + 2) * (tnx + 2); idx += NT) {
@@ -393,7 +457,7 @@ __global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __rest
 #pragma unroll
     for (int c = 0; c < NSIDE; ++c)
 #pragma unroll
-      for (int m = 0; m < 5; ++m) w5[c][m] = sm.W[c][py + 2][px + m];
+      for (int m = 0; m < 5; ++m) w5[c][m] = sm.W[c][py + 2][px + m + wo];
     ppm_predict<0, T>(k, T(1), w5, in, plim, clim, sig, WM, WP, P.order, P.fourth != 0);
 #pragma unroll
     for (int c = 0; c < NSIDE; ++c) { sm.WMx[c][py][px] = WM[c]; sm.WPx[c][py][px] = WP[c]; }
@@ -402,7 +466,7 @@ __global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __rest
 #pragma unroll
     for (int c = 0; c < NSIDE; ++c)
 #pragma unroll
-      for (int m = 0; m < 5; ++m) w5[c][m] = sm.W[c][py + m][px + 2];
+      for (int m = 0; m < 5; ++m) w5[c][m] = sm.W[c][py + m][px + 2 + wo];
     ppm_predict<1, T>(k, rvy, w5, in, plim, clim, sig, WM, WP, P.order, P.fourth != 0);
 #pragma unroll
     for (int c = 0; c < NSIDE; ++c) { sm.WMy[c][py][px] = WM[c]; sm.WPy[c][py][px] = WP[c]; }
@@ -517,7 +581,7 @@ __global__ void __launch_bounds__(NT) volume_kernel(const PatchDev<Real>* __rest
 #pragma unroll
     for (int c = 0; c < NSIDE; ++c) {
       T du = (sm.Fx[c][ry][cx + 1] - sm.Fx[c][ry][cx]) + (sm.Fy[c][ry + 1][cx] - sm.Fy[c][ry][cx]);
-      u[c] = sm.W[c][ry + 3][cx + 3] + du * sc;
+      u[c] = sm.W[c][ry + 3][cx + 3 + wo] + du * sc;
     }
     if (p.plastic) {
       T lam = p.Uin[fab_idx(p, 11 * s + 9, x, y)];

@@ -31,6 +31,10 @@ struct Launch {
   static cudaError_t exchange(const PatchDev<Real>* patches, const CopyDev* copies, int ncopies, int c0,
                               int ncomp, cudaStream_t s);
   static size_t volume_smem();
+  // the tile kernel's staged box (columns, rows) of one component: the TMA
+  // tensor maps of the FABs it reads are encoded with it
+  static int volume_box_x();
+  static int volume_box_y();
   // column-marching volume update of component group g (0 in-plane, 1
   // antiplane): one warp per item.  pdl: the kernel may be scheduled while
   // the kernel before it in the stream still runs (programmatic dependent

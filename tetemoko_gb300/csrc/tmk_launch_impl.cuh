@@ -30,6 +30,8 @@ struct LaunchImpl {
     return cudaLaunchKernelEx(&cfg, fault_kernel<Real, FAULT_SEG, FAULT_THREADS>, patches, fp, params, time, st);
   }
   static size_t smem() { return sizeof(VolSmem<Real, TX_, TY_>); }
+  static int box_x() { return VolSmem<Real, TX_, TY_>::RXP; }
+  static int box_y() { return VolSmem<Real, TX_, TY_>::RY; }
   static cudaError_t volume(const PatchDev<Real>* patches, const TileDev* tiles, int ntiles,
                             const DevParams* params, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
@@ -147,6 +149,8 @@ struct LaunchImpl {
     return LaunchImpl<REAL, TXV, TYV, NTV>::exchange(p, c, n, c0, nc, s);                                    \
   }                                                                                                          \
   template <> size_t Launch<REAL>::volume_smem() { return LaunchImpl<REAL, TXV, TYV, NTV>::smem(); }         \
+  template <> int Launch<REAL>::volume_box_x() { return LaunchImpl<REAL, TXV, TYV, NTV>::box_x(); }          \
+  template <> int Launch<REAL>::volume_box_y() { return LaunchImpl<REAL, TXV, TYV, NTV>::box_y(); }          \
   template <> cudaError_t Launch<REAL>::plastic(const PatchDev<REAL>* p, const TileDev* tl, int nt,         \
                                                 const DevParams* prm, cudaStream_t s) {                     \
     return LaunchImpl<REAL, TXV, TYV, NTV>::plastic(p, tl, nt, prm, s);                                      \
