@@ -547,6 +547,10 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
   const bool defer0 = it.fslot >= 0;      // row 0 is finished by march_fault_row_kernel
   const bool col_valid = x >= it.x0 && x < it.x0 + MARCH_COLS && x >= pp.vlo0 && x <= pp.vhi0;
   const size_t plane = (size_t)pp.anx * pp.any;
+  // a lane of this warp holds a face on a domain x edge: the x Riemann solves
+  // are the interior ones for every lane, overwritten there by the edge
+  // condition; other warps (most) skip the edge code on a uniform branch
+  const bool warp_xedge = __any_sync(0xffffffffu, x == dlo0 || x == dhi0 + 1);
 
   auto load_row = [&](int y, P* w) {
     const bool ok = lane_in && y >= dlo1 && y <= dhi1;
@@ -607,9 +611,11 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
     P L[N];
 #pragma unroll
     for (int c = 0; c < N; ++c) L[c] = live<G, 0>(c) ? shfl_up2(WP[c], 1) : mk2(T(0), T(0));
-    if (x == dlo0) edge2<G, 0, T>(kx, true, xout_lo, WM, bg, H1lo);
-    else if (x == dhi0 + 1) edge2<G, 0, T>(kx, false, xout_hi, L, bg, H1lo);
-    else riem<G, 0, T>(kx, L, WM, H1lo);
+    riem<G, 0, T>(kx, L, WM, H1lo);
+    if (warp_xedge) {                 // the domain-edge conditions, only in warps that reach an x edge
+      if (x == dlo0) edge2<G, 0, T>(kx, true, xout_lo, WM, bg, H1lo);
+      else if (x == dhi0 + 1) edge2<G, 0, T>(kx, false, xout_hi, L, bg, H1lo);
+    }
 #pragma unroll
     for (int c = 0; c < N; ++c) H1hi[c] = live<G, 0>(c) ? shfl_dn2(H1lo[c], 1) : mk2(T(0), T(0));
   };
@@ -771,9 +777,11 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
       P L[N], g[N], Fx[N], Fxh[N];
 #pragma unroll
       for (int c = 0; c < N; ++c) L[c] = live<G, 0>(c) ? shfl_up2(WPcx[c], 1) : mk2(T(0), T(0));
-      if (x == dlo0) edge2<G, 0, T>(kx, true, xout_lo, WMcx, bg, g);
-      else if (x == dhi0 + 1) edge2<G, 0, T>(kx, false, xout_hi, L, bg, g);
-      else riem<G, 0, T>(kx, L, WMcx, g);
+      riem<G, 0, T>(kx, L, WMcx, g);
+      if (warp_xedge) {
+        if (x == dlo0) edge2<G, 0, T>(kx, true, xout_lo, WMcx, bg, g);
+        else if (x == dhi0 + 1) edge2<G, 0, T>(kx, false, xout_hi, L, bg, g);
+      }
       flux2<G, 0, T>(kx, g, Fx);
 #pragma unroll
       for (int c = 0; c < N; ++c) Fxh[c] = shfl_dn2(Fx[c], 1);
