@@ -1123,17 +1123,18 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                     "note": "per step: FP64 state copied host->device (pinned), level step, state copied back"},
             "gpu_launches": launches,
-            "execution": (f"steps replayed from a CUDA graph of {graph_steps} recorded level steps "
-                          "(tmk_level_graph_create / tmk_graph_launch)") if graph_steps else "one call per step",
-            "tuning": {"autotuned": bool(args.autotune), "choice": tuning, "trial_ms_per_step": tune_ms},
-            "per_call": {"value": value_call, "unit": UNIT, "ms_per_step": ms_call / args.steps,
-                         "note": "the same steps, one tmk_level_step call each"},
             "clocks": clocks,
+            # the two forms and the mixed form's errors first: the sub-measurements after them are long
             "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_step": ms64 / n64, "steps": n64,
                            "volume_kernel": args.fp64_kernel, "volume_kernel_ms": vol64,
                            "volume_hbm_gbs": BYTES_PER_CELL_FP64 * cells / (vol64 * 1e-3) / 1e9},
             "mixed_over_fp64": value / value64,
             "errors": errors,
+            "execution": (f"steps replayed from a CUDA graph of {graph_steps} recorded level steps "
+                          "(tmk_level_graph_create / tmk_graph_launch)") if graph_steps else "one call per step",
+            "tuning": {"autotuned": bool(args.autotune), "choice": tuning, "trial_ms_per_step": tune_ms},
+            "per_call": {"value": value_call, "unit": UNIT, "ms_per_step": ms_call / args.steps,
+                         "note": "the same steps, one tmk_level_step call each"},
             "sw_level": sw_level,
             "amr": amr,
             "amr3": amr3,
