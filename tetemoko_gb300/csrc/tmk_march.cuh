@@ -95,7 +95,14 @@ template <int G, int D> TMK_HD constexpr bool live(int c) {
   return !((R::hasZc && (c == R::zc0 || c == R::zc1)) || (R::hasZf && c == R::zf));
 }
 
-// Packed constants of one direction.
+// Packed constants of one direction.  A packed FP32x2 instruction takes a
+// constant operand straight from the parameter bank only when both halves are
+// the same scalar (a broadcast); a pair of two values has to be loaded into
+// registers at each use once the registers are full.  So every constant is
+// also kept as its side-1 scalar (the s* fields): in x, and for the constants
+// that do not change sign with the mirrored y direction of side 2, the
+// kernels build the pair from that scalar (kc, ke); only the y-direction
+// constants with rv (side 2 = -side 1) are used as pairs.
 template <typename T>
 struct MK {
   using P = typename PairOf<T>::P;
@@ -106,6 +113,9 @@ struct MK {
   P aP, bP, aS, bS;    // PPM tracing coefficients of the P and S speeds
   P f_irho, f_l2g, f_lam, f_G;   // GETFLUXF: -rv * {1/rho, lam+2G, lam, G}
   P a_irho, a_l2g, a_lam, a_G;   // GETADWDXF: -rv*scale * {...}
+  // side-1 scalars of the pairs above
+  T sZpE, sZsE, snZpE, snZsE, shZpE, shZsE, saP, sbP, saS, sbS;
+  T sf_irho, sf_l2g, sf_lam, sf_G, sa_irho, sa_l2g, sa_lam, sa_G;
   TMK_HD void load(const DevParams& p, int D, double dtdx, double scale) {
     const T s2 = (D == 1) ? T(-1) : T(1);       // rv of side 2
     ZpE = mk2((T)p.Zp, (T)(s2 * p.Zp)); ZsE = mk2((T)p.Zs, (T)(s2 * p.Zs));
@@ -128,8 +138,24 @@ struct MK {
     a_l2g = mk2((T)(m1 * scale * (p.lam + 2.0 * p.G)), (T)(m2 * scale * (p.lam + 2.0 * p.G)));
     a_lam = mk2((T)(m1 * scale * p.lam), (T)(m2 * scale * p.lam));
     a_G = mk2((T)(m1 * scale * p.G), (T)(m2 * scale * p.G));
+    sZpE = ZpE.x; sZsE = ZsE.x; snZpE = nZpE.x; snZsE = nZsE.x; shZpE = hZpE.x; shZsE = hZsE.x;
+    saP = ap; sbP = bp; saS = as; sbS = bs;
+    sf_irho = f_irho.x; sf_l2g = f_l2g.x; sf_lam = f_lam.x; sf_G = f_G.x;
+    sa_irho = a_irho.x; sa_l2g = a_l2g.x; sa_lam = a_lam.x; sa_G = a_G.x;
   }
 };
+
+// Constant `name` of direction D as a pair: in x a broadcast of its scalar,
+// in y the stored pair (side 2 = -side 1 for the constants carrying rv).
+template <int D, typename T>
+TMK_D typename PairOf<T>::P kc_(const typename PairOf<T>::P& pair, T s) {
+  if constexpr (D == 0) return mk2(s, s);
+  else return pair;
+}
+#define KC(name) kc_<D, T>(k.name, k.s##name)
+// a constant with the same value on both sides in either direction
+#define KE(name) mk2(k.s##name, k.s##name)
+#define KHALF mk2(T(0.5), T(0.5))
 
 // Everything the marching kernel needs that is uniform over a launch (all
 // patches of a level share the scenario, dt and dx).  Built on the host and
@@ -226,27 +252,27 @@ TMK_D void predict(const MK<T>& k, const typename PairOf<T>::P* w, typename Pair
   }
   // S wave pair
   {
-    P nm = pfma(k.ZsE, dm[R::vS], dm[R::sS]), pm = pfma(k.nZsE, dm[R::vS], dm[R::sS]);
-    P np = pfma(k.ZsE, dp[R::vS], dp[R::sS]), pp = pfma(k.nZsE, dp[R::vS], dp[R::sS]);
+    P nm = pfma(KC(ZsE), dm[R::vS], dm[R::sS]), pm = pfma(KC(nZsE), dm[R::vS], dm[R::sS]);
+    P np = pfma(KC(ZsE), dp[R::vS], dp[R::sS]), pp = pfma(KC(nZsE), dp[R::vS], dp[R::sS]);
     if (clim) { limit2(nm, np); limit2(pm, pp); }
-    P nmt = pfma(k.aS, nm, pmul(k.bS, np));       // w- traced to the lo face
-    P ppt = pfma(k.aS, pp, pmul(k.bS, pm));       // w+ traced to the hi face
-    WM[R::sS] = padd(w[R::sS], pmul(k.half, padd(nmt, pm)));
-    WM[R::vS] = padd(w[R::vS], pmul(k.hZsE, psub(nmt, pm)));
-    WP[R::sS] = padd(w[R::sS], pmul(k.half, padd(np, ppt)));
-    WP[R::vS] = padd(w[R::vS], pmul(k.hZsE, psub(np, ppt)));
+    P nmt = pfma(KE(aS), nm, pmul(KE(bS), np));       // w- traced to the lo face
+    P ppt = pfma(KE(aS), pp, pmul(KE(bS), pm));       // w+ traced to the hi face
+    WM[R::sS] = padd(w[R::sS], pmul(KHALF, padd(nmt, pm)));
+    WM[R::vS] = padd(w[R::vS], pmul(KC(hZsE), psub(nmt, pm)));
+    WP[R::sS] = padd(w[R::sS], pmul(KHALF, padd(np, ppt)));
+    WP[R::vS] = padd(w[R::vS], pmul(KC(hZsE), psub(np, ppt)));
   }
   if constexpr (R::hasP) {
-    P nm = pfma(k.ZpE, dm[R::vP], dm[R::sP]), pm = pfma(k.nZpE, dm[R::vP], dm[R::sP]);
-    P np = pfma(k.ZpE, dp[R::vP], dp[R::sP]), pp = pfma(k.nZpE, dp[R::vP], dp[R::sP]);
+    P nm = pfma(KC(ZpE), dm[R::vP], dm[R::sP]), pm = pfma(KC(nZpE), dm[R::vP], dm[R::sP]);
+    P np = pfma(KC(ZpE), dp[R::vP], dp[R::sP]), pp = pfma(KC(nZpE), dp[R::vP], dp[R::sP]);
     if (clim) { limit2(nm, np); limit2(pm, pp); }
-    P nmt = pfma(k.aP, nm, pmul(k.bP, np));
-    P ppt = pfma(k.aP, pp, pmul(k.bP, pm));
-    P sPm = pmul(k.half, padd(nmt, pm)), sPp = pmul(k.half, padd(np, ppt));
+    P nmt = pfma(KE(aP), nm, pmul(KE(bP), np));
+    P ppt = pfma(KE(aP), pp, pmul(KE(bP), pm));
+    P sPm = pmul(KHALF, padd(nmt, pm)), sPp = pmul(KHALF, padd(np, ppt));
     WM[R::sP] = padd(w[R::sP], sPm);
-    WM[R::vP] = padd(w[R::vP], pmul(k.hZpE, psub(nmt, pm)));
+    WM[R::vP] = padd(w[R::vP], pmul(KC(hZpE), psub(nmt, pm)));
     WP[R::sP] = padd(w[R::sP], sPp);
-    WP[R::vP] = padd(w[R::vP], pmul(k.hZpE, psub(np, ppt)));
+    WP[R::vP] = padd(w[R::vP], pmul(KC(hZpE), psub(np, ppt)));
   }
   // the zero-speed components of direction D are not read (live<G, D>)
 #pragma unroll
@@ -261,17 +287,17 @@ TMK_D void riem(const MK<T>& k, const typename PairOf<T>::P* L, const typename P
   using P = typename PairOf<T>::P;
   using R = Role<G, D>;
   {
-    P wpos = pfma(k.nZsE, L[R::vS], L[R::sS]);
-    P wneg = pfma(k.ZsE, Rt[R::vS], Rt[R::sS]);
-    g[R::sS] = pmul(k.half, padd(wneg, wpos));
-    g[R::vS] = pmul(k.hZsE, psub(wneg, wpos));
+    P wpos = pfma(KC(nZsE), L[R::vS], L[R::sS]);
+    P wneg = pfma(KC(ZsE), Rt[R::vS], Rt[R::sS]);
+    g[R::sS] = pmul(KHALF, padd(wneg, wpos));
+    g[R::vS] = pmul(KC(hZsE), psub(wneg, wpos));
   }
   if constexpr (R::hasP) {
-    P wpos = pfma(k.nZpE, L[R::vP], L[R::sP]);
-    P wneg = pfma(k.ZpE, Rt[R::vP], Rt[R::sP]);
-    P s = pmul(k.half, padd(wneg, wpos));
+    P wpos = pfma(KC(nZpE), L[R::vP], L[R::sP]);
+    P wneg = pfma(KC(ZpE), Rt[R::vP], Rt[R::sP]);
+    P s = pmul(KHALF, padd(wneg, wpos));
     g[R::sP] = s;
-    g[R::vP] = pmul(k.hZpE, psub(wneg, wpos));
+    g[R::vP] = pmul(KC(hZpE), psub(wneg, wpos));
   }
   // zero-speed components of the face state: not read (live<G, D>)
 #pragma unroll
@@ -296,27 +322,27 @@ TMK_D void edge2(const MK<T>& k, bool lo, bool outflow, const typename PairOf<T>
   {
     P wneg, wpos;
     if (lo) {
-      wneg = pfma(k.ZsE, Wi[R::vS], Wi[R::sS]);
-      wpos = outflow ? pfma(k.nZsE, bg[R::vS], bg[R::sS]) : pneg(wneg);
+      wneg = pfma(KC(ZsE), Wi[R::vS], Wi[R::sS]);
+      wpos = outflow ? pfma(KC(nZsE), bg[R::vS], bg[R::sS]) : pneg(wneg);
     } else {
-      wpos = pfma(k.nZsE, Wi[R::vS], Wi[R::sS]);
-      wneg = outflow ? pfma(k.ZsE, bg[R::vS], bg[R::sS]) : pneg(wpos);
+      wpos = pfma(KC(nZsE), Wi[R::vS], Wi[R::sS]);
+      wneg = outflow ? pfma(KC(ZsE), bg[R::vS], bg[R::sS]) : pneg(wpos);
     }
-    g[R::sS] = pmul(k.half, padd(wneg, wpos));
-    g[R::vS] = pmul(k.hZsE, psub(wneg, wpos));
+    g[R::sS] = pmul(KHALF, padd(wneg, wpos));
+    g[R::vS] = pmul(KC(hZsE), psub(wneg, wpos));
   }
   if constexpr (R::hasP) {
     P wneg, wpos;
     if (lo) {
-      wneg = pfma(k.ZpE, Wi[R::vP], Wi[R::sP]);
-      wpos = outflow ? pfma(k.nZpE, bg[R::vP], bg[R::sP]) : pneg(wneg);
+      wneg = pfma(KC(ZpE), Wi[R::vP], Wi[R::sP]);
+      wpos = outflow ? pfma(KC(nZpE), bg[R::vP], bg[R::sP]) : pneg(wneg);
     } else {
-      wpos = pfma(k.nZpE, Wi[R::vP], Wi[R::sP]);
-      wneg = outflow ? pfma(k.ZpE, bg[R::vP], bg[R::sP]) : pneg(wpos);
+      wpos = pfma(KC(nZpE), Wi[R::vP], Wi[R::sP]);
+      wneg = outflow ? pfma(KC(ZpE), bg[R::vP], bg[R::sP]) : pneg(wpos);
     }
-    P s = pmul(k.half, padd(wneg, wpos));
+    P s = pmul(KHALF, padd(wneg, wpos));
     g[R::sP] = s;
-    g[R::vP] = pmul(k.hZpE, psub(wneg, wpos));
+    g[R::vP] = pmul(KC(hZpE), psub(wneg, wpos));
   }
   // zero-speed components (the reference's SHF terms): not read (live<G, D>)
 #pragma unroll
@@ -328,13 +354,13 @@ TMK_D void edge2(const MK<T>& k, bool lo, bool outflow, const typename PairOf<T>
 template <int G, int D, typename T>
 TMK_D void flux2(const MK<T>& k, const typename PairOf<T>::P* g, typename PairOf<T>::P* F) {
   using R = Role<G, D>;
-  F[R::vS] = pmul(k.f_irho, g[R::sS]);
-  F[R::sS] = pmul(k.f_G, g[R::vS]);
+  F[R::vS] = pmul(KC(f_irho), g[R::sS]);
+  F[R::sS] = pmul(KC(f_G), g[R::vS]);
   if constexpr (R::hasP) {
-    F[R::vP] = pmul(k.f_irho, g[R::sP]);
-    F[R::sP] = pmul(k.f_l2g, g[R::vP]);
-    F[R::zc0] = pmul(k.f_lam, g[R::vP]);
-    F[R::zc1] = pmul(k.f_lam, g[R::vP]);
+    F[R::vP] = pmul(KC(f_irho), g[R::sP]);
+    F[R::sP] = pmul(KC(f_l2g), g[R::vP]);
+    F[R::zc0] = pmul(KC(f_lam), g[R::vP]);
+    F[R::zc1] = pmul(KC(f_lam), g[R::vP]);
   }
   if constexpr (R::hasZf) F[R::zf] = mk2(decltype(g[0].x)(0), decltype(g[0].x)(0));
 }
@@ -346,20 +372,20 @@ TMK_D void adw2(const MK<T>& k, const typename PairOf<T>::P* h, const typename P
   using P = typename PairOf<T>::P;
   using R = Role<G, D>;
   {
-    P a = pmul(k.a_irho, psub(h[R::sS], l[R::sS]));
+    P a = pmul(KC(a_irho), psub(h[R::sS], l[R::sS]));
     q1[R::vS] = padd(q1[R::vS], a); q2[R::vS] = padd(q2[R::vS], a);
-    P b = pmul(k.a_G, psub(h[R::vS], l[R::vS]));
+    P b = pmul(KC(a_G), psub(h[R::vS], l[R::vS]));
     q1[R::sS] = padd(q1[R::sS], b); q2[R::sS] = padd(q2[R::sS], b);
   }
   if constexpr (R::hasP) {
-    P a = pmul(k.a_irho, psub(h[R::sP], l[R::sP]));
+    P a = pmul(KC(a_irho), psub(h[R::sP], l[R::sP]));
     q1[R::vP] = padd(q1[R::vP], a); q2[R::vP] = padd(q2[R::vP], a);
     P dv = psub(h[R::vP], l[R::vP]);
-    P b = pmul(k.a_l2g, dv);
+    P b = pmul(KC(a_l2g), dv);
     q1[R::sP] = padd(q1[R::sP], b); q2[R::sP] = padd(q2[R::sP], b);
     // the targets are states of the other direction: their components that
     // are zero-speed there are not read
-    P c = pmul(k.a_lam, dv);
+    P c = pmul(KC(a_lam), dv);
     if constexpr (live<G, 1 - D>(R::zc0)) { q1[R::zc0] = padd(q1[R::zc0], c); q2[R::zc0] = padd(q2[R::zc0], c); }
     if constexpr (live<G, 1 - D>(R::zc1)) { q1[R::zc1] = padd(q1[R::zc1], c); q2[R::zc1] = padd(q2[R::zc1], c); }
   }
@@ -888,5 +914,9 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS) march_fault_row_kernel(const
     fault_row_finish<T, 1>(patches[it.patch], it, mc, lane);
   }
 }
+
+#undef KC
+#undef KE
+#undef KHALF
 
 }  // namespace tmk
