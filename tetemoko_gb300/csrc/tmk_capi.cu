@@ -258,8 +258,10 @@ tmk_status build_march_lists(tmk_level_s* L) {
     level_free(L, L->dfrows[g]);
     level_free(L, L->stash[g]);
     const int gk = (g == 0 && L->ctx->scheme.plasticity && tu.plastic_fused) ? 2 : g;   // the kernel of group g
-    int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots(gk)
-                                          : tmk::Launch<double>::march_slots(gk);
+    const tmk::DevParams& hp = L->ctx->hp;
+    const bool fixed = hp.order != 0 && hp.prim_lim && !hp.char_lim;   // march_scheme_fixed of the launches
+    int slots = L->prec == TMK_PREC_MIXED ? tmk::Launch<float>::march_slots(gk, fixed)
+                                          : tmk::Launch<double>::march_slots(gk, fixed);
     slots *= tu.march_waves[g];
     if (g == 1) slots = std::max(warps, slots - tu.fault_displace * warps * fault_ctas);
     std::vector<tmk::MarchItem> items, frows;

@@ -46,8 +46,9 @@ struct Launch {
                                       const MarchItem* rows1, int n1, const MarchConst<Real>& mc,
                                       cudaStream_t s);
   // warps of group g's marching kernel resident at once on the current device
-  // (g = 2: the in-plane kernel with the fused plastic return)
-  static int march_slots(int g);
+  // (g = 2: the in-plane kernel with the fused plastic return); fixed: the
+  // kernel form with the scheme fixed at compile time (PPM, primitive limiting)
+  static int march_slots(int g, bool fixed);
   // warps per CTA of the marching kernels
   static int march_warps();
   // the entry of the fault kernel variant with seg faces per CTA (to find its

@@ -66,18 +66,12 @@ struct LaunchImpl {
     if (nitems <= 0) return cudaSuccess;
     static bool configured = false;
     if (!configured) {
-      cudaError_t e0 = cudaFuncSetAttribute(march_kernel<Real, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)march_smem_bytes<Real, 0>());
-      cudaError_t e1 = cudaFuncSetAttribute(march_kernel<Real, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)march_smem_bytes<Real, 1>());
-      cudaError_t e2 = cudaFuncSetAttribute(march_kernel<Real, 0, true>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)march_smem_bytes<Real, 0>());
-      if (e0 != cudaSuccess) return e0;
-      if (e1 != cudaSuccess) return e1;
-      if (e2 != cudaSuccess) return e2;
+      cudaError_t e = march_configure<MARCH_SCH_RUNTIME>();
+      if (e == cudaSuccess) e = march_configure<MARCH_SCH_PPM_PRIM>();
+      if (e != cudaSuccess) return e;
       configured = true;
     }
+    const bool fx = march_scheme_fixed(mc);
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
@@ -89,11 +83,38 @@ struct LaunchImpl {
     cfg.numAttrs = pdl ? 1 : 0;
     if (g == 0) {
       cfg.dynamicSmemBytes = march_smem_bytes<Real, 0>();
-      if (mc.plastic) return cudaLaunchKernelEx(&cfg, march_kernel<Real, 0, true>, patches, items, nitems, mc);
-      return cudaLaunchKernelEx(&cfg, march_kernel<Real, 0>, patches, items, nitems, mc);
+      if (mc.plastic)
+        return fx ? cudaLaunchKernelEx(&cfg, march_kernel<Real, 0, true, MARCH_SCH_PPM_PRIM>, patches, items, nitems, mc)
+                  : cudaLaunchKernelEx(&cfg, march_kernel<Real, 0, true>, patches, items, nitems, mc);
+      return fx ? cudaLaunchKernelEx(&cfg, march_kernel<Real, 0, false, MARCH_SCH_PPM_PRIM>, patches, items, nitems, mc)
+                : cudaLaunchKernelEx(&cfg, march_kernel<Real, 0>, patches, items, nitems, mc);
     }
     cfg.dynamicSmemBytes = march_smem_bytes<Real, 1>();
-    return cudaLaunchKernelEx(&cfg, march_kernel<Real, 1>, patches, items, nitems, mc);
+    return fx ? cudaLaunchKernelEx(&cfg, march_kernel<Real, 1, false, MARCH_SCH_PPM_PRIM>, patches, items, nitems, mc)
+              : cudaLaunchKernelEx(&cfg, march_kernel<Real, 1>, patches, items, nitems, mc);
+  }
+  // the dynamic shared memory limit of the marching kernels of one scheme form
+  template <int SCH>
+  static cudaError_t march_configure() {
+    cudaError_t e = cudaFuncSetAttribute(march_kernel<Real, 0, false, SCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)march_smem_bytes<Real, 0>());
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(march_kernel<Real, 1, false, SCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)march_smem_bytes<Real, 1>());
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(march_kernel<Real, 0, true, SCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)march_smem_bytes<Real, 0>());
+    return e;
+  }
+  template <int G, bool PL, int SCH>
+  static int march_blocks() {
+    int b = 0;
+    cudaFuncSetAttribute(march_kernel<Real, G, PL, SCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)march_smem_bytes<Real, G>());
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, march_kernel<Real, G, PL, SCH>, 32 * MARCH_WARPS,
+                                                      march_smem_bytes<Real, G>()) != cudaSuccess)
+      return 0;
+    return b;
   }
   static cudaError_t march_fault_rows(const PatchDev<Real>* patches, const MarchItem* rows0, int n0,
                                       const MarchItem* rows1, int n1, const MarchConst<Real>& mc, cudaStream_t s) {
@@ -102,29 +123,18 @@ struct LaunchImpl {
     march_fault_row_kernel<Real><<<blocks, 32 * MARCH_WARPS, 0, s>>>(patches, rows0, n0, rows1, n1, mc);
     return cudaGetLastError();
   }
-  static int march_slots(int g) {
-    int dev = 0, sms = 0, b = 0;
+  // resident warps of marching kernel g (0 in-plane, 1 antiplane, 2 in-plane
+  // with the fused plastic return) over the device, for the scheme form fixed
+  // (march_scheme_fixed) or read at run time
+  static int march_slots(int g, bool fixed) {
+    int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       return 0;
-    cudaError_t e;
-    if (g == 0) {
-      cudaFuncSetAttribute(march_kernel<Real, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)march_smem_bytes<Real, 0>());
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, march_kernel<Real, 0>, 32 * MARCH_WARPS,
-                                                        march_smem_bytes<Real, 0>());
-    } else if (g == 2) {      // the in-plane kernel with the fused plastic return
-      cudaFuncSetAttribute(march_kernel<Real, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)march_smem_bytes<Real, 0>());
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, march_kernel<Real, 0, true>, 32 * MARCH_WARPS,
-                                                        march_smem_bytes<Real, 0>());
-    } else {
-      cudaFuncSetAttribute(march_kernel<Real, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)march_smem_bytes<Real, 1>());
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, march_kernel<Real, 1>, 32 * MARCH_WARPS,
-                                                        march_smem_bytes<Real, 1>());
-    }
-    if (e != cudaSuccess) return 0;
+    int b;
+    if (g == 0) b = fixed ? march_blocks<0, false, MARCH_SCH_PPM_PRIM>() : march_blocks<0, false, MARCH_SCH_RUNTIME>();
+    else if (g == 2) b = fixed ? march_blocks<0, true, MARCH_SCH_PPM_PRIM>() : march_blocks<0, true, MARCH_SCH_RUNTIME>();
+    else b = fixed ? march_blocks<1, false, MARCH_SCH_PPM_PRIM>() : march_blocks<1, false, MARCH_SCH_RUNTIME>();
     return b * sms * MARCH_WARPS;
   }
 };
@@ -164,7 +174,9 @@ struct LaunchImpl {
                                                          const MarchConst<REAL>& mc, cudaStream_t s) {     \
     return LaunchImpl<REAL, TXV, TYV, NTV>::march_fault_rows(p, r0, n0, r1, n1, mc, s);                      \
   }                                                                                                          \
-  template <> int Launch<REAL>::march_slots(int g) { return LaunchImpl<REAL, TXV, TYV, NTV>::march_slots(g); } \
+  template <> int Launch<REAL>::march_slots(int g, bool fx) {                                               \
+    return LaunchImpl<REAL, TXV, TYV, NTV>::march_slots(g, fx);                                              \
+  }                                                                                                          \
   template <> int Launch<REAL>::march_warps() { return MARCH_WARPS; }                                        \
   template <> const void* Launch<REAL>::fault_entry(int seg) {                                               \
     return seg == FAULT_SEG_SMALL ? (const void*)fault_kernel<REAL, FAULT_SEG_SMALL, FAULT_THREADS_SMALL>     \

@@ -529,10 +529,17 @@ TMK_D void march_capture(const PatchDev<T>& pp, const MarchItem& it, const March
   }
 }
 
+// The predictor scheme of every reference deck (PPM, primitive limiting, no
+// characteristic limiting), fixed at compile time: SCH = 1.  SCH = 0 reads the
+// scheme flags from the launch constants.
+constexpr int MARCH_SCH_RUNTIME = 0, MARCH_SCH_PPM_PRIM = 1;
+template <typename T>
+TMK_HD bool march_scheme_fixed(const MarchConst<T>& mc) { return mc.ppm && mc.plim && !mc.clim; }
+
 // PL: a plastic level with the fused return (in-plane group only): every
 // stored cell takes the plastic return, and the kernel runs after the
 // antiplane one.
-template <typename T, int G, bool PL = false>
+template <typename T, int G, bool PL = false, int SCH = MARCH_SCH_RUNTIME>
 __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value) march_kernel(const PatchDev<T>* __restrict__ patches,
                                                                  const MarchItem* __restrict__ items, int nitems,
                                                                  const __grid_constant__ MarchConst<T> mc) {
@@ -561,8 +568,9 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
   const int ahi0 = pp.alo0 + pp.anx - 1;
   const bool lane_in = x >= dlo0 && x <= dhi0 && x >= pp.alo0 && x <= ahi0;
   const bool inL = x - 1 >= dlo0, inR = x + 1 <= dhi0;
-  const bool plim = mc.plim != 0, clim = mc.clim != 0, lim = mc.lim != 0;
-  const bool ppm = mc.ppm != 0;
+  constexpr bool kFixed = SCH == MARCH_SCH_PPM_PRIM;
+  const bool plim = kFixed || mc.plim != 0, clim = !kFixed && mc.clim != 0, lim = kFixed || mc.lim != 0;
+  const bool ppm = kFixed || mc.ppm != 0;
   const MK<T>& kx = mc.kx;
   const MK<T>& ky = mc.ky;
   const P sc = mc.sc;
