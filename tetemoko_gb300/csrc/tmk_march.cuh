@@ -196,25 +196,28 @@ struct MarchConst {
 TMK_D float copysg(float a, float b) { return copysignf(a, b); }
 TMK_D double copysg(double a, double b) { return copysign(a, b); }
 
-// van Leer: sign(dc) min(|dc|, 2|dl|, 2|dr|) when dl dr > 0, else 0
-template <typename T> TMK_D T vl1(T dl, T dr, T dc, T prod) {
-  const T t = fmin(fabs(dc), T(2) * fmin(fabs(dl), fabs(dr)));
+// van Leer: sign(dc) min(|dc|, 2|dl|, 2|dr|) when dl dr > 0, else 0 (dl2, dr2:
+// the doubled differences, exact; one three-input minimum)
+template <typename T> TMK_D T vl1(T dl2, T dr2, T dc, T prod) {
+  const T t = fmin(fmin(fabs(dc), fabs(dl2)), fabs(dr2));
   return prod > T(0) ? copysg(t, dc) : T(0);
 }
 
 // Limited slope of the middle value.  A missing neighbour (outside the
-// domain) is replaced by the reflection 2 w0 - w_other, which turns the
-// centred formula into the one-sided difference the reference uses there.
+// domain) stands for the reflection 2 w0 - w_other, which makes the two
+// one-sided differences equal: the centred formula becomes the one-sided
+// difference the reference uses there.
 template <typename P> TMK_D P slope2(P wm, P w0, P wp, bool hasL, bool hasR, bool limit) {
   using T = decltype(wm.x);
-  const P two = mk2(T(2), T(2)), half = mk2(T(0.5), T(0.5));
-  if (!hasL) wm = psub(pmul(two, w0), wp);
-  if (!hasR) wp = psub(pmul(two, w0), wm);
-  const P dl = psub(w0, wm), dr = psub(wp, w0);
+  const P half = mk2(T(0.5), T(0.5));
+  P dl = psub(w0, wm), dr = psub(wp, w0);
+  if (!hasL) dl = dr;
+  if (!hasR) dr = dl;
   const P dc = pmul(half, padd(dl, dr));
   if (!limit) return dc;
   const P prod = pmul(dl, dr);
-  return mk2(vl1(dl.x, dr.x, dc.x, prod.x), vl1(dl.y, dr.y, dc.y, prod.y));
+  const P dl2 = padd(dl, dl), dr2 = padd(dr, dr);
+  return mk2(vl1(dl2.x, dr2.x, dc.x, prod.x), vl1(dl2.y, dr2.y, dc.y, prod.y));
 }
 
 // PPM limiter (Colella & Woodward 1984 eq. 1.10): both deltas zero at an
