@@ -96,3 +96,40 @@ def test_march_fp32_is_as_accurate_as_tile_fp32(cuda_lib, name, sc):
     assert em <= 1e-4
     assert em <= max(2.0 * et, 5e-6)      # both at FP32 rounding of a ~1e2 MPa state
     assert rel_err(Bm[:, g:-g], Br[:, g:-g]) <= 1e-3
+
+
+WIDE_BOXES = [(0, 0, 299, 11), (0, 12, 130, 23), (131, 12, 299, 23)]
+
+
+@pytest.mark.parametrize("name", ["rs_aging", "sw_ref9", "rs_free_edges"])
+@pytest.mark.parametrize("boxes", [WIDE_BOXES, [(0, 0, 299, 23)]], ids=["three_patches", "one_patch"])
+def test_wide_levels_match_oracle(cuda_lib, name, boxes):
+    """A 300-column level: many marching strips side by side, strips that end
+    short of a patch edge and fault-row strips finished after the fault kernel.
+    FP64 form against the oracle at 1e-11; the mixed form against it at FP32
+    rounding."""
+    if name == "sw_ref9":
+        sc = S.slip_weakening(nx=300, ny=24, dx=0.1, layout=A.TMK_SW_LAYOUT_REFERENCE9)
+    else:
+        sc = S.rate_state(nx=300, ny=24, dx=0.1)
+    if name == "rs_free_edges":
+        for k, v in enumerate((1, 1, 2, 1, 0, 0)):
+            sc.scheme.boundary_type[k] = v
+    sc.scheme.volume_kernel = A.TMK_VOLUME_MARCH
+    rng = np.random.default_rng(7)
+    U0 = perturbed_state(sc, rng, amp_v=0.05, amp_s=1.0)
+    B0 = sc.initial_B()
+    Ur, Br = U0.copy(), B0.copy()
+    t = 0.0
+    for _ in range(4):
+        assert O.level_step(sc, Ur, Br, boxes, t, sc.dt()) == 0
+        t += sc.dt()
+    g = A.TMK_NGHOST
+    vs = (slice(None), slice(g, -g), slice(g, -g))
+    Ug, Bg = _run_level(sc, boxes, U0, B0, 4)
+    assert rel_err(Ug[vs], Ur[vs]) <= 1e-11
+    assert rel_err(Bg[:, g:-g], Br[:, g:-g]) <= 1e-11
+    sc.scheme.precision = A.TMK_PREC_MIXED
+    Um, Bm = _run_level(sc, boxes, U0, B0, 4)
+    assert rel_err(Um[vs], Ur[vs]) <= 1e-4
+    assert rel_err(Bm[:, g:-g], Br[:, g:-g]) <= 1e-3

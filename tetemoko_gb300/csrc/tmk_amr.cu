@@ -495,7 +495,7 @@ tmk_status rebuild_captures_impl(tmk_level_s* L) {
         if (m.patch == p && ci >= m.x0 && ci < m.x0 + tmk::MARCH_COLS && cj >= m.y0 && cj <= m.y1) { owner = (int)k; break; }
       }
       if (owner < 0) return TMK_ERR_BAD_DESC;
-      per[owner].push_back(make_int4(cj, kind, ci - items[owner].x0 + 3, kv.second));
+      per[owner].push_back(make_int4(cj, kind, ci - items[owner].x0 + tmk::MARCH_HALO, kv.second));
     }
     std::vector<int4> caps;
     for (size_t k = 0; k < items.size(); ++k) {

@@ -1,8 +1,11 @@
 // tmk_march.cuh -- column-marching volume kernel.
 //
-// A warp owns 32 adjacent columns of a patch (26 updated columns plus a
-// 3-column halo on each side) and streams up a run of rows.  Per row it
-// computes the x predictor (neighbours by warp shuffles) and the y predictor
+// A warp owns 32 adjacent columns of a patch (28 updated columns plus a
+// 2-column halo on each side) and streams up a run of rows.  Per row it
+// computes the x predictor (each lane's neighbours read from the row's copy in
+// shared memory, which also holds the column one beyond the warp on either
+// side: the outermost slopes need them, and with them a 2-column halo is
+// enough for the 3-cell stencil of one update) and the y predictor
 // (a rolling window of rows in registers), the first-pass Riemann states,
 // the transverse corrections, the final Riemann states, the fluxes and the
 // conservative update -- the CTU sequence of LinElastPatchGodunov::computeWHalf
@@ -405,7 +408,8 @@ struct MarchItem { int patch, x0, y0, y1, fslot, cap0, ncap; };
 // final y flux 1, old state)
 constexpr int MARCH_STASH_VECS = 5;
 
-constexpr int MARCH_COLS = 26;   // updated columns per warp
+constexpr int MARCH_COLS = 28;   // updated columns per warp
+constexpr int MARCH_HALO = 2;    // halo lanes on either side (lane l holds column x0 - 2 + l)
 constexpr int MARCH_WARPS = 4;   // warps per CTA
 
 // Per-row vectors a lane carries from row to row in shared memory rather than
@@ -435,11 +439,18 @@ TMK_HD constexpr int carry_slot(int v, int c) {
 template <typename T, int G>
 TMK_HD constexpr int carry_slots() { return carry_slot<T, G>(kNumCarry, 0); }
 // Rows q..q+2 of the rolling window plus the row in flight live in a per-warp
-// ring of shared memory filled by cp.async; slot = row & 3.
+// ring of shared memory filled by cp.async; slot = row & 3.  A ring row holds
+// MARCH_RW entries per component: the column left of lane 0, the warp's 32
+// columns, the column right of lane 31.
 constexpr int MARCH_RING = 4;
+constexpr int MARCH_RW = 34;
+template <typename T, int G>
+constexpr size_t march_warp_pairs() {
+  return (size_t)carry_slots<T, G>() * 32 + (size_t)MARCH_RING * Grp<G>::N * MARCH_RW;
+}
 template <typename T, int G>
 constexpr size_t march_smem_bytes() {
-  return (size_t)MARCH_WARPS * (carry_slots<T, G>() + MARCH_RING * Grp<G>::N) * 32 * sizeof(typename PairOf<T>::P);
+  return (size_t)MARCH_WARPS * march_warp_pairs<T, G>() * sizeof(typename PairOf<T>::P);
 }
 
 // resident CTAs per SM the register allocation targets: FP32 in-plane 3 (164
@@ -449,10 +460,12 @@ template <typename T, int G> struct MarchMinBlocks {
   static constexpr int value = sizeof(T) == 4 ? ((G == 0) ? 3 : 5) : ((G == 0) ? 2 : 4);
 };
 
-// asynchronous copy of one element into shared memory (completion tracked per thread)
-template <typename T> TMK_D void cp_async_elem(T* dst_smem, const T* src) {
+// asynchronous copy of one element into shared memory (completion tracked per
+// thread); nbytes = sizeof(T), or 0: nothing is read and zeros are written
+template <typename T> TMK_D void cp_async_elem(T* dst_smem, const T* src, unsigned nbytes = sizeof(T)) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(src), "n"(sizeof(T)) : "memory");
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(d), "l"(src), "n"(sizeof(T)), "r"(nbytes)
+               : "memory");
 }
 TMK_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 TMK_D void cp_async_wait_all_but_newest() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
@@ -549,8 +562,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
   using P = typename PairOf<T>::P;
   constexpr int N = Grp<G>::N;
   extern __shared__ __align__(16) unsigned char march_smem[];
-  P* const carry = reinterpret_cast<P*>(march_smem) +
-                   (size_t)(threadIdx.x >> 5) * (carry_slots<T, G>() + MARCH_RING * N) * 32;
+  P* const carry = reinterpret_cast<P*>(march_smem) + (size_t)(threadIdx.x >> 5) * march_warp_pairs<T, G>();
   P* const ring = carry + carry_slots<T, G>() * 32;
   const int wid = blockIdx.x * MARCH_WARPS + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -566,10 +578,16 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
   if (PL) asm volatile("griddepcontrol.wait;" ::: "memory");
   const MarchItem it = items[wid];
   const PatchDev<T>& pp = patches[it.patch];
-  const int x = it.x0 - 3 + lane;
+  const int x = it.x0 - MARCH_HALO + lane;
   const int dlo0 = pp.dlo0, dhi0 = pp.dhi0, dlo1 = pp.dlo1, dhi1 = pp.dhi1;
   const int ahi0 = pp.alo0 + pp.anx - 1;
   const bool lane_in = x >= dlo0 && x <= dhi0 && x >= pp.alo0 && x <= ahi0;
+  // lane 0 also stages the column left of it (ring entry 0), lane 31 the one
+  // right of it (entry 33), each from its own column's address -1 / +1
+  const int dxe = lane == 0 ? -1 : 1;
+  const bool ext_in = (lane == 0 || lane == 31) && x + dxe >= dlo0 && x + dxe <= dhi0 && x + dxe >= pp.alo0 &&
+                      x + dxe <= ahi0;
+  const int ext_pos = lane == 0 ? 0 : 33;
   const bool inL = x - 1 >= dlo0, inR = x + 1 <= dhi0;
   constexpr bool kFixed = SCH == MARCH_SCH_PPM_PRIM;
   const bool plim = kFixed || mc.plim != 0, clim = !kFixed && mc.clim != 0, lim = kFixed || mc.lim != 0;
@@ -598,40 +616,71 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
       w[c] = ok ? mk2(pp.Uin[o + (size_t)g * plane], pp.Uin[o + (size_t)(11 + g) * plane]) : mk2(T(0), T(0));
     }
   };
-  // row y into its ring slot: cp.async for cells in the domain, zeros elsewhere
-  auto ring_row = [&](int y) -> P* { return ring + (size_t)((y & (MARCH_RING - 1)) * N) * 32 + lane; };
+  // row y into its ring slot: cp.async for cells in the domain, zeros
+  // elsewhere; the two outer columns only for the components live in x (the
+  // only ones whose neighbours are read)
+  auto ring_row = [&](int y) -> P* { return ring + (size_t)((y & (MARCH_RING - 1)) * N) * MARCH_RW; };
   auto load_row_async = [&](int y) {
-    const bool ok = lane_in && y >= dlo1 && y <= dhi1;
+    const bool yin = y >= dlo1 && y <= dhi1;
+    const bool ok = lane_in && yin;
     const size_t o = ok ? fab_idx(pp, 0, x, y) : 0;
-    P* dst = ring_row(y);
+    const unsigned nb = ok ? (unsigned)sizeof(T) : 0u;
+    P* const rowp = ring_row(y);
+    P* const dst = rowp + lane + 1;
+    const T* const src = pp.Uin + o;
 #pragma unroll
     for (int c = 0; c < N; ++c) {
       const int g = Grp<G>::glob(c);
-      T* d2 = reinterpret_cast<T*>(dst + c * 32);
-      if (ok) {
-        cp_async_elem(d2, pp.Uin + o + (size_t)g * plane);
-        cp_async_elem(d2 + 1, pp.Uin + o + (size_t)(11 + g) * plane);
-      } else {
-        dst[c * 32] = mk2(T(0), T(0));
+      T* d2 = reinterpret_cast<T*>(dst + c * MARCH_RW);
+      cp_async_elem(d2, src + (size_t)g * plane, nb);
+      cp_async_elem(d2 + 1, src + (size_t)(11 + g) * plane, nb);
+    }
+    if (lane == 0 || lane == 31) {      // the outer columns: own address -1 / +1 (oke implies ok)
+      const bool oke = ext_in && yin;
+      const unsigned nbe = oke ? (unsigned)sizeof(T) : 0u;
+      const T* const srce = oke ? src + dxe : src;
+      P* const dste = rowp + ext_pos;
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        if (!live<G, 0>(c)) continue;
+        const int g = Grp<G>::glob(c);
+        T* d2 = reinterpret_cast<T*>(dste + c * MARCH_RW);
+        cp_async_elem(d2, srce + (size_t)g * plane, nbe);
+        cp_async_elem(d2 + 1, srce + (size_t)(11 + g) * plane, nbe);
       }
     }
     cp_async_commit();
   };
-  auto get_row = [&](int y, P* w) {
-    const P* src = ring_row(y);
+  // the outer columns of row y, loaded directly (the rows staged before the loop)
+  auto store_ext_sync = [&](int y) {
+    if (lane == 0 || lane == 31) {
+      const bool oke = ext_in && y >= dlo1 && y <= dhi1;
+      const size_t oe = oke ? fab_idx(pp, 0, x + dxe, y) : 0;
+      P* de = ring_row(y) + ext_pos;
 #pragma unroll
-    for (int c = 0; c < N; ++c) w[c] = src[c * 32];
+      for (int c = 0; c < N; ++c) {
+        if (!live<G, 0>(c)) continue;
+        const int g = Grp<G>::glob(c);
+        de[c * MARCH_RW] = oke ? mk2(pp.Uin[oe + (size_t)g * plane], pp.Uin[oe + (size_t)(11 + g) * plane])
+                               : mk2(T(0), T(0));
+      }
+    }
+  };
+  auto get_row = [&](int y, P* w) {
+    const P* src = ring_row(y) + lane + 1;
+#pragma unroll
+    for (int c = 0; c < N; ++c) w[c] = src[c * MARCH_RW];
   };
 
-  // x-direction normal predictor of row w and the first-pass x-face state on
-  // the lane's lo face (H1 lo) and hi face (H1 hi)
-  auto xrow = [&](const P* w, P* WM, P* WP, P* H1lo, P* H1hi) {
+  // x-direction normal predictor of row w (its ring row: rw) and the
+  // first-pass x-face state on the lane's lo face (H1 lo) and hi face (H1 hi)
+  auto xrow = [&](const P* w, const P* rw, P* WM, P* WP, P* H1lo, P* H1hi) {
     if (ppm) {
       P dm[N], dp[N];
 #pragma unroll
       for (int c = 0; c < N; ++c) {
         if (!live<G, 0>(c)) { dm[c] = mk2(T(0), T(0)); dp[c] = dm[c]; continue; }
-        P wl = shfl_up2(w[c], 1), wr = shfl_dn2(w[c], 1);
+        const P wl = rw[c * MARCH_RW + lane], wr = rw[c * MARCH_RW + lane + 2];
         P s = slope2(wl, w[c], wr, inL, inR, lim);
         P sl = shfl_up2(s, 1);
         P flo = inL ? face2<T>(wl, w[c], sl, s) : pfma(mk2(T(-0.5), T(-0.5)), s, w[c]);
@@ -684,9 +733,12 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
     load_row(q_s + 1, W1);
     load_row(q_s + 2, W2);
     {
-      P* r0 = ring_row(q_s); P* r1 = ring_row(q_s + 1); P* r2 = ring_row(q_s + 2);
+      P* r0 = ring_row(q_s) + lane + 1; P* r1 = ring_row(q_s + 1) + lane + 1; P* r2 = ring_row(q_s + 2) + lane + 1;
 #pragma unroll
-      for (int c = 0; c < N; ++c) { r0[c * 32] = W0[c]; r1[c * 32] = W1[c]; r2[c * 32] = W2[c]; }
+      for (int c = 0; c < N; ++c) { r0[c * MARCH_RW] = W0[c]; r1[c * MARCH_RW] = W1[c]; r2[c * MARCH_RW] = W2[c]; }
+      store_ext_sync(q_s);
+      store_ext_sync(q_s + 1);
+      store_ext_sync(q_s + 2);
     }
     const bool hl = q_s - 1 >= dlo1, hr = q_s + 1 <= dhi1;
 #pragma unroll
@@ -714,6 +766,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
       if (col_valid && q - 1 >= it.y0 && q - 1 <= it.y1) plastic_inputs<T>(pp, fab_idx(pp, 0, x, q - 1), plane, pin);
     }
     cp_async_wait_all_but_newest();   // rows up to q+2 have landed
+    __syncwarp();                     // ... every lane's copies, whose neighbours read them
     P W0[N], W1[N], W2[N];
     get_row(q, W0);
     get_row(q + 1, W1);
@@ -744,7 +797,7 @@ __global__ void __launch_bounds__(32 * MARCH_WARPS, MarchMinBlocks<T, G>::value)
         for (int c = 0; c < N; ++c) { WMy[c] = W0[c]; WPy[c] = W0[c]; }
       }
       // x predictor of row q, first-pass x faces, corrected y states of row q
-      xrow(W0, WMx, WPx, H1lo, H1hi);
+      xrow(W0, ring_row(q), WMx, WPx, H1lo, H1hi);
 #pragma unroll
       for (int c = 0; c < N; ++c) { WMcy[c] = WMy[c]; WPcy[c] = WPy[c]; }
       adw2<G, 0, T>(kx, H1hi, H1lo, WMcy, WPcy);
@@ -855,7 +908,7 @@ template <typename T, int G>
 TMK_D void fault_row_finish(const PatchDev<T>& pp, const MarchItem& it, const MarchConst<T>& mc, int lane) {
   using P = typename PairOf<T>::P;
   constexpr int N = Grp<G>::N;
-  const int x = it.x0 - 3 + lane;
+  const int x = it.x0 - MARCH_HALO + lane;
   const int dlo0 = pp.dlo0, dhi0 = pp.dhi0, dlo1 = pp.dlo1;
   const P* st = reinterpret_cast<const P*>(mc.stash[G]) + (size_t)it.fslot * MARCH_STASH_VECS * N * 32 + lane;
   P WMcx[N], WPcx[N], H1y1[N], Fy1[N], Wold[N], H1y0[N], Fy0[N];
