@@ -11,8 +11,8 @@ Reported (one JSON line, rank 0):
   fp64_plain   the plain FP64 form on the same workload
   roofline     volume kernel: algorithmic bytes (18 components read + written, 144 B per
                cell in FP32) / average launch time from CUDA events on the launch stream
-  e2e          the same step through the C ABI with host (pinned) FP64 buffers copied in
-               and out every step
+  e2e          the same step through the C ABI with the state in a host (pinned) FP64 FAB:
+               every step copies in what the step reads and copies out what it rewrites
   cpu_baseline the CPU oracle (a port of the reference) on the machine's host cores
 With --gpus N > 1 (torchrun) every rank runs an independent replica ("replicas
 only": the level step has no data-path collective on one GPU per box).
@@ -1039,7 +1039,10 @@ def main():
                 "timing": f"average over a second timed pass of {nprof} steps with CUDA events on the launch "
                           "stream around each launch (serialises the fault/volume overlap of the headline pass)"}
 
-    # ---- e2e through the C ABI with pinned host buffers
+    # ---- e2e through the C ABI with pinned host buffers: the state lives in a
+    # host FAB (as a Chombo FArrayBox does); each step copies in what the step
+    # reads and copies out what it rewrites (tmk_level_put_valid / take_valid:
+    # the 18 evolving components of the valid cells, and the fault data)
     ushape, bshape = lvl.patch_shapes(0)
     Uh = torch.empty(ushape, dtype=torch.float64).pin_memory()
     Bh = torch.empty(bshape, dtype=torch.float64).pin_memory()
@@ -1047,21 +1050,21 @@ def main():
     dt = sc.dt()
     t = 0.0
     for _ in range(2):
-        lvl.set_patch(0, Uh.numpy(), Bh.numpy())
+        lvl.put_valid(0, Uh.numpy(), Bh.numpy())
         lvl.step(t, dt, stream)
-        lvl.get_patch(0, Uh.numpy(), Bh.numpy())
+        lvl.take_valid(0, Uh.numpy(), Bh.numpy())
         t += dt
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        lvl.set_patch(0, Uh.numpy(), Bh.numpy())
+        lvl.put_valid(0, Uh.numpy(), Bh.numpy())
         lvl.step(t, dt, stream)
-        lvl.get_patch(0, Uh.numpy(), Bh.numpy())
+        lvl.take_valid(0, Uh.numpy(), Bh.numpy())
         t += dt
     torch.cuda.synchronize()
     e2e_value, _ = replica_rate(cells, args.e2e_steps, time.perf_counter() - t0, world, device="cuda")
-    h2d = Uh.numel() * 8 + Bh.numel() * 8
+    h2d = 18 * cells * 8 + Bh.numel() * 8
     lvl.close()
     ctx.close()
 
@@ -1121,7 +1124,9 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-                    "note": "per step: FP64 state copied host->device (pinned), level step, state copied back"},
+                    "note": "state in a pinned host FP64 FAB; per step: tmk_level_put_valid (the 18 evolving "
+                            "components of the valid cells and the fault data, host->device), level step, "
+                            "tmk_level_take_valid (the same, device->host)"},
             "gpu_launches": launches,
             "clocks": clocks,
             # the two forms and the mixed form's errors first: the sub-measurements after them are long

@@ -341,6 +341,20 @@ tmk_status tmk_level_set_patch(tmk_level* lvl, int patch, const double* U,
                                const double* B, int host);
 tmk_status tmk_level_get_patch(tmk_level* lvl, int patch, double* U, double* B,
                                int host);
+/* Copy in / out only what a level step reads and rewrites of one patch: the
+ * 18 evolving components (9 per side; on a plastic level also lambda and
+ * gamma of both sides) over the valid box, and the fault data B.  U and B are
+ * laid out as for tmk_level_set_patch (ghost cells and the other components
+ * are neither read nor written); `host` as there.  The counterpart of the
+ * reference's step on FABs that live in host memory
+ * (LinElastLevelGodunov::step, srcLinElast/LinElastLevelGodunov.H:91-105, reads
+ * the valid cells of U and writes them back): put before a step, take after
+ * it.  The level must have been given a whole state once (tmk_level_set_patch)
+ * so that the components these calls leave alone are defined. */
+tmk_status tmk_level_put_valid(tmk_level* lvl, int patch, const double* U,
+                               const double* B, int host);
+tmk_status tmk_level_take_valid(tmk_level* lvl, int patch, double* U, double* B,
+                                int host);
 /* One level step at `time` by `dt`: same-level ghost exchange of U and B,
  * fault solve, volume update of every patch in one launch, and (if the
  * scheme has plasticity) the plastic correction.  *dt_new = dx / max wave

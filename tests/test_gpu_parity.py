@@ -136,6 +136,69 @@ def test_level_steps_match_oracle(cuda_lib, name, sc):
     ctx.close()
 
 
+@pytest.mark.parametrize("prec", [A.TMK_PREC_FP64, A.TMK_PREC_MIXED], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("plastic", [False, True], ids=["elastic", "plastic"])
+def test_steps_through_valid_put_and_take_equal_device_steps(cuda_lib, prec, plastic):
+    """A level whose state goes to host arrays and back every step through
+    tmk_level_put_valid / tmk_level_take_valid (only what a step reads and
+    rewrites) steps exactly as one whose state stays on the device; the
+    components and ghost cells the calls leave alone are untouched."""
+    import torch
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    boxes = [(0, 0, 20, 9), (21, 0, 63, 9), (0, 10, 31, 31), (32, 10, 63, 31)]
+    if plastic:
+        sc = S.slip_weakening(nx=64, ny=32, dx=0.1, precision=prec, plasticity=True)
+    else:
+        sc = S.rate_state(nx=64, ny=32, dx=0.1, precision=prec)
+    rng = np.random.default_rng(17)
+    Ug = perturbed_state(sc, rng, amp_v=0.05, amp_s=1.0)
+    if plastic:
+        for side in (0, 11):
+            Ug[side + 6, 8:14, :] += 60.0
+    Bg = sc.initial_B()
+    dt = sc.dt()
+    ctx = Context(sc)
+    ref = LinElastLevelGodunov(ctx, boxes)
+    ref.set_level(Ug, Bg)
+    lvl = LinElastLevelGodunov(ctx, boxes)
+    lvl.set_level(Ug, Bg)
+    # per-patch host arrays (pinned, read in place, and pageable, staged)
+    Us, Bs = [], []
+    for p in range(len(boxes)):
+        U, B = lvl.get_patch(p)
+        if p % 2 == 0:
+            U = torch.from_numpy(U).pin_memory().numpy()
+        Us.append(U)
+        Bs.append(B)
+    U_before = [u.copy() for u in Us]
+    for n in range(4):
+        ref.step(n * dt, dt)
+        for p in range(len(boxes)):
+            lvl.put_valid(p, Us[p], Bs[p])
+        lvl.step(n * dt, dt)
+        for p in range(len(boxes)):
+            lvl.take_valid(p, Us[p], Bs[p])
+    torch.cuda.synchronize()
+    g = A.TMK_NGHOST
+    evolving = [c for c in range(22) if plastic or c % 11 < 9]
+    other = [c for c in range(22) if c not in evolving]
+    for p in range(len(boxes)):
+        Ur, Br = ref.get_patch(p)
+        vs = (evolving, slice(g, -g), slice(g, -g))
+        np.testing.assert_array_equal(Us[p][:, g:-g, g:-g][evolving], Ur[:, g:-g, g:-g][evolving])
+        if Bs[p] is not None:
+            np.testing.assert_array_equal(Bs[p], Br)
+        # untouched: the other components everywhere, every ghost cell
+        np.testing.assert_array_equal(Us[p][other], U_before[p][other])
+        ghost = np.ones(Us[p].shape[1:], dtype=bool)
+        ghost[g:-g, g:-g] = False
+        np.testing.assert_array_equal(Us[p][:, ghost], U_before[p][:, ghost])
+    assert ref.status()[0] == 0 and lvl.status()[0] == 0
+    ref.close()
+    lvl.close()
+    ctx.close()
+
+
 def test_plastic_update_matches_oracle(cuda_lib):
     import torch
     from tetemoko_gb300.level import Context, LinElastPatchGodunov

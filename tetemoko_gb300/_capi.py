@@ -198,6 +198,8 @@ def lib() -> C.CDLL:
     L.tmk_level_destroy.restype = None
     L.tmk_level_set_patch.argtypes = [vp, C.c_int, vp, vp, C.c_int]
     L.tmk_level_get_patch.argtypes = [vp, C.c_int, vp, vp, C.c_int]
+    L.tmk_level_put_valid.argtypes = [vp, C.c_int, vp, vp, C.c_int]
+    L.tmk_level_take_valid.argtypes = [vp, C.c_int, vp, vp, C.c_int]
     L.tmk_level_step.argtypes = [vp, C.c_double, C.c_double, vp, dp]
     L.tmk_level_status.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.tmk_level_launches_per_step.argtypes = [vp]

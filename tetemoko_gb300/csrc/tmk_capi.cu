@@ -789,6 +789,89 @@ extern "C" tmk_status tmk_level_get_patch(tmk_level* L, int p, double* U, double
 
 namespace {
 
+// The components a step of level L reads and rewrites: the 9 evolving ones of
+// each side, and lambda and gamma where the scheme has plasticity.
+tmk::CompList step_comps(const tmk_level_s* L) {
+  tmk::CompList cl;
+  cl.n = 0;
+  const bool pl = L->ctx->scheme.plasticity != 0;
+  for (int c = 0; c < TMK_NCOMP; ++c)
+    if (pl || (c % TMK_NSIDE_COMP) < tmk::NSIDE) cl.c[cl.n++] = c;
+  return cl;
+}
+
+// U of put/take.  Mixed form: pinned host or device pointers are read or
+// written in place by the copy kernel (one crossing of the host link), other
+// host memory is staged through the level's FP64 staging buffer.  FP64 form:
+// one strided copy per component.
+tmk_status valid_copy(tmk_level_s* L, int p, const double* in, double* out, bool host) {
+  LevelPatch& lp = L->patches[p];
+  const int alo0 = lp.alloc.lo[0], alo1 = lp.alloc.lo[1];
+  const int anx = lp.alloc.hi[0] - alo0 + 1, any = lp.alloc.hi[1] - alo1 + 1;
+  const size_t count = (size_t)TMK_NCOMP * anx * any;
+  const tmk_box& v = lp.valid;
+  const tmk::CompList cl = step_comps(L);
+  if (L->prec != TMK_PREC_MIXED) {
+    const size_t pitch = (size_t)anx * sizeof(double);
+    const size_t o0 = (size_t)(v.lo[1] - alo1) * anx + (v.lo[0] - alo0);
+    for (int k = 0; k < cl.n; ++k) {
+      const size_t o = (size_t)cl.c[k] * anx * any + o0;
+      double* dev = (double*)lp.U[L->parity] + o;
+      if (in) TMK_CU(cudaMemcpy2D(dev, pitch, in + o, pitch, (size_t)(v.hi[0] - v.lo[0] + 1) * sizeof(double),
+                                  v.hi[1] - v.lo[1] + 1, cudaMemcpyDefault));
+      else TMK_CU(cudaMemcpy2D(out + o, pitch, dev, pitch, (size_t)(v.hi[0] - v.lo[0] + 1) * sizeof(double),
+                               v.hi[1] - v.lo[1] + 1, cudaMemcpyDefault));
+    }
+    return TMK_OK;
+  }
+  if (in) {                         // put: into the buffer the next step reads
+    const double* src = host ? (const double*)mapped_host(in) : in;
+    if (!src) {
+      TMK_CU(cudaMemcpy(L->stage, in, count * sizeof(double), cudaMemcpyHostToDevice));
+      src = L->stage;
+    }
+    TMK_CU(tmk::copy_valid_comps(src, (float*)lp.U[L->parity], alo0, alo1, anx, any, v.lo[0], v.lo[1], v.hi[0],
+                                 v.hi[1], cl, 0));
+  } else {                          // take: from the buffer the last step wrote
+    double* dst = host ? (double*)mapped_host(out) : out;
+    if (!dst) TMK_CU(cudaMemcpy(L->stage, out, count * sizeof(double), cudaMemcpyHostToDevice));
+    TMK_CU(tmk::copy_valid_comps((const float*)lp.U[L->parity], dst ? dst : L->stage, alo0, alo1, anx, any, v.lo[0],
+                                 v.lo[1], v.hi[0], v.hi[1], cl, 0));
+    if (!dst) TMK_CU(cudaMemcpy(out, L->stage, count * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  return TMK_OK;
+}
+
+}  // namespace
+
+extern "C" tmk_status tmk_level_put_valid(tmk_level* L, int p, const double* U, const double* B, int host) {
+  if (!L || p < 0 || p >= (int)L->patches.size() || !U) return TMK_ERR_BAD_DESC;
+  LevelPatch& lp = L->patches[p];
+  if (lp.fault && !B) return TMK_ERR_BAD_DESC;
+  tmk_status st = valid_copy(L, p, U, nullptr, host != 0);
+  if (st != TMK_OK) return st;
+  if (lp.fault)
+    TMK_CU(cudaMemcpy(lp.B, B, (size_t)L->ctx->nb * lp.bnx * sizeof(double),
+                      host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice));
+  TMK_CU(cudaDeviceSynchronize());
+  return TMK_OK;
+}
+
+extern "C" tmk_status tmk_level_take_valid(tmk_level* L, int p, double* U, double* B, int host) {
+  if (!L || p < 0 || p >= (int)L->patches.size() || !U) return TMK_ERR_BAD_DESC;
+  LevelPatch& lp = L->patches[p];
+  TMK_CU(cudaDeviceSynchronize());
+  tmk_status st = valid_copy(L, p, nullptr, U, host != 0);
+  if (st != TMK_OK) return st;
+  if (B && lp.fault)
+    TMK_CU(cudaMemcpy(B, lp.B, (size_t)L->ctx->nb * lp.bnx * sizeof(double),
+                      host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice));
+  TMK_CU(cudaDeviceSynchronize());
+  return TMK_OK;
+}
+
+namespace {
+
 // The kernels of one level step after the coarse-fine fill.  Marching form:
 // the in-plane kernel, then the fault kernel (scheduled as in-plane CTAs
 // retire, reading only the step's input state), then the antiplane kernel

@@ -83,6 +83,53 @@ cudaError_t convert_launch(const S* src, D* dst, size_t n, cudaStream_t s) {
   convert_kernel<S, D><<<blocks, 256, 0, s>>>(src, dst, n);
   return cudaGetLastError();
 }
+// One row of one listed component per pass of a CTA (rows of the valid box
+// are contiguous runs of the FAB), four elements per thread in flight: a put
+// or take of a level's state crosses the host link once, inside this kernel.
+template <typename S, typename D>
+__global__ void valid_comps_kernel(const S* __restrict__ a, D* __restrict__ b, int alo0, int alo1, int anx,
+                                   int any, int vlo0, int vlo1, int vnx, int vny, CompList cl) {
+  constexpr int U = 4;
+  const int nrows = cl.n * vny;
+  for (int r = blockIdx.x; r < nrows; r += gridDim.x) {
+    const int c = cl.c[r / vny], j = vlo1 + r % vny;
+    const size_t o = ((size_t)c * any + (j - alo1)) * anx + (vlo0 - alo0);
+    int i = threadIdx.x;
+    for (; i + (U - 1) * (int)blockDim.x < vnx; i += U * blockDim.x) {
+      S v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) v[u] = a[o + i + u * blockDim.x];
+#pragma unroll
+      for (int u = 0; u < U; ++u) b[o + i + u * blockDim.x] = (D)v[u];
+    }
+    for (; i < vnx; i += blockDim.x) b[o + i] = (D)a[o + i];
+  }
+}
+template <typename S, typename D>
+cudaError_t valid_comps_launch(const S* src, D* dst, int alo0, int alo1, int anx, int any, int vlo0, int vlo1,
+                               int vhi0, int vhi1, const CompList& cl, cudaStream_t s) {
+  const int vnx = vhi0 - vlo0 + 1, vny = vhi1 - vlo1 + 1;
+  if (vnx <= 0 || vny <= 0 || cl.n <= 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return cudaErrorUnknown;
+  const unsigned blocks = (unsigned)std::max(1, std::min(cl.n * vny, sms * 8));
+  valid_comps_kernel<S, D><<<blocks, 256, 0, s>>>(src, dst, alo0, alo1, anx, any, vlo0, vlo1, vnx, vny, cl);
+  return cudaGetLastError();
+}
+cudaError_t copy_valid_comps(const double* src, float* dst, int alo0, int alo1, int anx, int any, int vlo0, int vlo1,
+                             int vhi0, int vhi1, const CompList& cl, cudaStream_t s) {
+  return valid_comps_launch(src, dst, alo0, alo1, anx, any, vlo0, vlo1, vhi0, vhi1, cl, s);
+}
+cudaError_t copy_valid_comps(const float* src, double* dst, int alo0, int alo1, int anx, int any, int vlo0, int vlo1,
+                             int vhi0, int vhi1, const CompList& cl, cudaStream_t s) {
+  return valid_comps_launch(src, dst, alo0, alo1, anx, any, vlo0, vlo1, vhi0, vhi1, cl, s);
+}
+cudaError_t copy_valid_comps(const double* src, double* dst, int alo0, int alo1, int anx, int any, int vlo0,
+                             int vlo1, int vhi0, int vhi1, const CompList& cl, cudaStream_t s) {
+  return valid_comps_launch(src, dst, alo0, alo1, anx, any, vlo0, vlo1, vhi0, vhi1, cl, s);
+}
+
 cudaError_t convert_d2f(const double* src, float* dst, size_t n, cudaStream_t s) { return convert_launch(src, dst, n, s); }
 cudaError_t convert_f2d(const float* src, double* dst, size_t n, cudaStream_t s) { return convert_launch(src, dst, n, s); }
 cudaError_t copy_fab(const double* src, double* dst, size_t n, cudaStream_t s) { return convert_launch(src, dst, n, s); }

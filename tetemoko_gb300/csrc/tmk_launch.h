@@ -61,6 +61,16 @@ cudaError_t convert_d2f(const double* src, float* dst, size_t n, cudaStream_t s)
 cudaError_t convert_f2d(const float* src, double* dst, size_t n, cudaStream_t s);
 // copy of n doubles (either side may be mapped pinned host memory)
 cudaError_t copy_fab(const double* src, double* dst, size_t n, cudaStream_t s);
+// The components listed in comps (ncomp of them) over the valid box of two
+// FABs of one shape, converted from S to D (either side may be mapped pinned
+// host memory): the cells and components a level step reads and rewrites.
+struct CompList { int n; int c[22]; };
+cudaError_t copy_valid_comps(const double* src, float* dst, int alo0, int alo1, int anx, int any, int vlo0, int vlo1,
+                             int vhi0, int vhi1, const CompList& comps, cudaStream_t s);
+cudaError_t copy_valid_comps(const float* src, double* dst, int alo0, int alo1, int anx, int any, int vlo0, int vlo1,
+                             int vhi0, int vhi1, const CompList& comps, cudaStream_t s);
+cudaError_t copy_valid_comps(const double* src, double* dst, int alo0, int alo1, int anx, int any, int vlo0,
+                             int vlo1, int vhi0, int vhi1, const CompList& comps, cudaStream_t s);
 // copy components [c0, c0+ncomp) of the valid box of a FAB into another FAB of the same shape
 cudaError_t copy_valid(const double* src, double* dst, int alo0, int alo1, int anx, int any, int vlo0, int vlo1,
                        int vhi0, int vhi1, int c0, int ncomp, cudaStream_t s);

@@ -299,6 +299,24 @@ class LinElastLevelGodunov:
                 "tmk_level_get_fault_friction")
         return F if present.value else None
 
+    def _ptr(self, a):
+        return (a.ctypes.data if isinstance(a, np.ndarray) else a.data_ptr()) if a is not None else None
+
+    def put_valid(self, p, U, B=None):
+        """Copy in what a step reads of patch p: the evolving components (and on a
+        plastic level lambda, gamma) of the valid cells of U (laid out as for
+        set_patch), and B; the level must have had a whole state set once."""
+        host = isinstance(U, np.ndarray)
+        A.check(self.lib.tmk_level_put_valid(self.h, p, self._ptr(U), self._ptr(B), 1 if host else 0),
+                "tmk_level_put_valid")
+
+    def take_valid(self, p, U, B=None):
+        """Copy out what a step rewrites of patch p into U (and B); the other
+        components and the ghost cells of U are left as they are."""
+        host = isinstance(U, np.ndarray)
+        A.check(self.lib.tmk_level_take_valid(self.h, p, self._ptr(U), self._ptr(B), 1 if host else 0),
+                "tmk_level_take_valid")
+
     def set_level_friction(self, Fg: np.ndarray):
         """Scatter a domain-wide per-face friction row (3, nx+8) into the fault patches."""
         g = A.TMK_NGHOST
