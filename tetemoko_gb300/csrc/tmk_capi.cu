@@ -93,6 +93,8 @@ extern "C" tmk_status tmk_context_create(const tmk_elastic_params* e, const tmk_
   if (pl) { P.p_mu = pl->mu; P.p_beta = pl->beta; P.p_eta = pl->eta; P.p_b = pl->b; P.p_h = pl->h; }
   P.inv_Zs = 1.0 / P.Zs; P.inv_Zp = 1.0 / P.Zp; P.lam_r = P.lam / (P.lam + 2.0 * P.G);
   P.two_V0 = 2.0 * P.rs_V0; P.inv_2V0 = P.rs_V0 > 0 ? 1.0 / P.two_V0 : 0.0;
+  P.ln_2V0 = P.rs_V0 > 0 ? std::log(P.two_V0) : 0.0;
+  P.ln_halfZs = P.Zs > 0 ? std::log(0.5 * P.Zs) : 0.0;
   c->scheme = *s;
   c->nb = s->fault_law == TMK_FAULT_RS ? TMK_RS_NBDRY : (s->fault_law == TMK_FAULT_SW ? TMK_SW_NBDRY : 0);
   if (dalloc(&c->dp, 1) != cudaSuccess || dalloc(&c->dstatus, 1) != cudaSuccess) {

@@ -54,6 +54,7 @@ struct DevParams {
   // reciprocals the mixed form's friction solve multiplies by (its chain of
   // FP64 operations is the fault kernel's latency; a division costs several)
   double inv_Zs, inv_Zp, lam_r, two_V0, inv_2V0;   // lam_r = lam/(lam+2G)
+  double ln_2V0, ln_halfZs;                          // log(2 V0), log(Zs / 2)
 };
 
 // Constants of one arithmetic type.

@@ -197,48 +197,89 @@ TMK_D RSFaceK rs_face_k(const DevParams& P, const RSFace& fr, double x) {
 }
 
 // The friction equation of RSNEWTON solved for z = asinh(beta V) instead of V:
-//   f(z) = alpha z + (eta/beta) sinh z - phi = 0,  V = sinh(z)/beta, tau = alpha z.
+//   f(z) = alpha z + c sinh z - phi = 0,  c = eta / beta,  V = sinh(z)/beta,  tau = alpha z.
 // f is smooth and monotone in z on the same bracket (0, asinh(beta phi/Zs)], so
 // Newton converges in a few steps where the iteration in V creeps up through
 // tens of decades; it starts from the guess V0 when that lies inside the
 // bracket.  As in the reference, a root beyond the bracket's upper end
 // V = phi/Zs yields that end.
+//
+// GB300 issues one FP64 warp instruction per 64 cycles on an SM sub-partition,
+// so the iterations run in FP32 (c e^{+-z} as e^{+-z + ln c}, whose exponent
+// stays below log(phi) inside the bracket), and one FP64 Newton step from the
+// FP32 root finishes the solve: from a start within ~1e-5 of the root the step
+// lands within ~1e-10, far below the FP32 volume arithmetic of the mixed form.
+// V is then the FP64 c sinh z of that step's start advanced to its end to
+// second order.  A step that is not small (an FP32 iteration that did not
+// converge) hands the solve to the FP64 iteration from there.
 TMK_D int rs_newton_zk(const DevParams& P, const RSFaceK& fk, double phi, double psi, double sn, double V0,
                        double& V, double& tau) {
   const double atolG = 2.220446049250313e-16 * 1e4;
   const double alpha = sn * fk.a;
-  const double ep = exp(psi * fk.inv_a), em = exp(-psi * fk.inv_a);   // independent: issued together
-  const double beta = ep * P.inv_2V0, inv_beta = em * P.two_V0;
+  const double lb = psi * fk.inv_a - P.ln_2V0;        // ln beta, beta = e^(psi/a) / (2 V0)
   const double eta = 0.5 * P.Zs;
   const double Vmax = phi * P.inv_Zs;
-  if (!(alpha > 0.0) || !(beta > 0.0) || !(beta < 1e300) || !(inv_beta > 0.0) || !(phi > 0.0))
+  if (!(alpha > 0.0) || !(phi > 0.0) || !(lb > -600.0 && lb < 600.0) || !(P.rs_V0 > 0.0))
     return rs_newton(P, phi, psi, sn, fk.a, V, tau);
-  const double zmax = asinh(beta * Vmax);
-  const bool guess = V0 > 0.0 && V0 < Vmax;
-  const double zg = guess ? asinh(beta * V0) : 0.0;                      // independent of zmax
-  if (alpha * zmax + eta * Vmax - phi <= 0.0) {     // root beyond the reference's bracket
+  const double lc = P.ln_halfZs - lb;                 // ln c
+  // bracket end z_max = asinh(beta Vmax) (= ln(2 beta Vmax) to FP64 resolution past e^20)
+  const double lbv = lb + log(Vmax);
+  const double zmax = lbv > 20.0 ? 0.6931471805599453 + lbv : asinh(exp(lbv));
+  if (alpha * zmax + eta * Vmax - phi <= 0.0) {      // root beyond the reference's bracket
     V = Vmax;
     tau = alpha * zmax;
     return RS_IMAX + 1;
   }
-  const double c = eta * inv_beta;
-  double z = guess ? fmin(zg, zmax) : fmin(phi / alpha, zmax);
-  int it;
-  for (it = 1; it <= RS_IMAX; ++it) {
-    const double e = exp(z), ie = z > 20.0 ? 0.0 : recip_nr(e);   // e^-2z below FP64 resolution past 20
-    const double sh = 0.5 * (e - ie), ch = 0.5 * (e + ie);
-    const double f = alpha * z + c * sh - phi;
-    const double dz = -f * (double)__frcp_rn((float)(alpha + c * ch));
-    double zn = z + dz;
-    if (zn < 0.0) zn = 0.5 * z;
-    if (zn > zmax) zn = 0.5 * (z + zmax);
-    z = zn;
-    if (fabs(f) <= atolG || fabs(dz) <= 1e-15 * fmax(1.0, z)) break;
+  // FP32 Newton from the guess
+  const float a32 = (float)alpha, lc32 = (float)lc, phi32 = (float)phi, zmax32 = (float)zmax;
+  float z;
+  if (V0 > 0.0 && V0 < Vmax) {
+    const float lg = (float)lb + logf((float)V0);    // ln(beta V0)
+    z = fminf(lg > 9.f ? 0.6931472f + lg : asinhf(expf(lg)), zmax32);
+  } else {
+    z = fminf(phi32 / a32, zmax32);
   }
-  const double e = exp(z);
-  V = 0.5 * (e - (z > 20.0 ? 0.0 : recip_nr(e))) * inv_beta;
-  tau = alpha * z;
-  return it;
+  int it;
+  for (it = 1; it <= 30; ++it) {
+    const float ep = expf(z + lc32), em = expf(lc32 - z);
+    const float f = a32 * z + 0.5f * (ep - em) - phi32;
+    const float dz = -f / (a32 + 0.5f * (ep + em));
+    float zn = z + dz;
+    if (zn < 0.f) zn = 0.5f * z;
+    if (zn > zmax32) zn = 0.5f * (z + zmax32);
+    z = zn;
+    if (fabsf(dz) <= 2e-6f * fmaxf(1.f, z)) break;
+  }
+  // one FP64 Newton step
+  const double z0 = (double)z;
+  const double ep = exp(z0 + lc), em = exp(lc - z0);  // independent: issued together
+  const double sh = 0.5 * (ep - em), ch = 0.5 * (ep + em);
+  const double f = alpha * z0 + sh - phi;
+  const double dz = -f * recip_nr(alpha + ch);
+  if (fabs(dz) <= 1e-4 * fmax(1.0, z0) && z0 + dz >= 0.0 && z0 + dz <= zmax) {
+    const double z1 = z0 + dz;
+    V = (sh + ch * dz) * (2.0 * P.inv_Zs);            // c sinh(z1) / eta
+    tau = alpha * z1;
+    return it;
+  }
+  // the FP64 iteration from the FP32 result
+  const double c = exp(lc);
+  double zz = fmin(fmax(z0 + dz, 0.0), zmax);
+  int jt;
+  for (jt = 1; jt <= RS_IMAX; ++jt) {
+    const double e = exp(zz), ie = zz > 20.0 ? 0.0 : recip_nr(e);   // e^-2z below FP64 resolution past 20
+    const double f2 = alpha * zz + c * 0.5 * (e - ie) - phi;
+    const double d2 = -f2 * (double)__frcp_rn((float)(alpha + c * 0.5 * (e + ie)));
+    double zn = zz + d2;
+    if (zn < 0.0) zn = 0.5 * zz;
+    if (zn > zmax) zn = 0.5 * (zz + zmax);
+    zz = zn;
+    if (fabs(f2) <= atolG || fabs(d2) <= 1e-15 * fmax(1.0, zz)) break;
+  }
+  const double e = exp(zz + lc), ie = exp(lc - zz);
+  V = 0.5 * (e - ie) * (2.0 * P.inv_Zs);
+  tau = alpha * zz;
+  return it + jt;
 }
 
 // RSFAULTBCF for the mixed form (same states in, same face states out).
