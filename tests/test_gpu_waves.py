@@ -1,0 +1,58 @@
+"""The plane-wave known answers of test_oracle_waves.py on the GPU: the FP64
+form equals the oracle's step on them, and the mixed form (FP32 volume) reaches
+the exact solution at the same second-order rate, its FP32 rounding far below
+the truncation error on these grids."""
+import math
+
+import numpy as np
+import pytest
+
+from tetemoko_gb300 import _capi as A
+from tests import test_oracle_waves as W
+
+pytestmark = pytest.mark.gpu
+G = A.TMK_NGHOST
+
+
+def _gpu_error(n: int, along: str, wave: str, prec: int) -> float:
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    sc = W._scenario(n, along, wave)
+    sc.scheme.precision = prec
+    U = W._wave_state(sc, along, wave, 0.0)
+    speed = sc.elastic.cp if wave == "P" else sc.elastic.cs
+    steps = int(math.ceil(W.TRAVEL / (speed * sc.dt())))
+    dt = W.TRAVEL / (speed * steps)
+    ctx = Context(sc)
+    lvl = LinElastLevelGodunov(ctx, [(0, 0, sc.nx - 1, sc.ny - 1)])
+    lvl.set_level(U, None)
+    t = 0.0
+    for _ in range(steps):
+        lvl.step(t, dt)
+        t += dt
+    out = U.copy()
+    lvl.get_level(out, None)
+    assert lvl.status()[0] == 0
+    lvl.close()
+    ctx.close()
+    exact = W._wave_state(sc, along, wave, t)
+    comp = (3 if along == "x" else 4) if wave == "P" else 6
+    if along == "x":
+        j = G + sc.ny // 2
+        got, ref = out[comp, j, G:-G], exact[comp, j, G:-G]
+    else:
+        i = G + sc.nx // 2
+        got, ref = out[comp, G:-G, i], exact[comp, G:-G, i]
+    return float(np.sum(np.abs(got - ref)) * sc.dx / (W.AMP * W.WIDTH))
+
+
+@pytest.mark.parametrize("along,wave", [("x", "P"), ("y", "S")])
+def test_mixed_form_converges_like_the_oracle(cuda_lib, along, wave):
+    mixed = [_gpu_error(n, along, wave, A.TMK_PREC_MIXED) for n in (64, 128, 256)]
+    fp64 = _gpu_error(256, along, wave, A.TMK_PREC_FP64)
+    ref = W._error(256, along, wave)
+    orders = [math.log2(mixed[k] / mixed[k + 1]) for k in range(2)]
+    print(f"{wave} along {along}: mixed L1 errors {['%.3e' % e for e in mixed]}, orders "
+          f"{['%.2f' % o for o in orders]}; FP64 GPU {fp64:.3e}, oracle {ref:.3e}")
+    assert abs(fp64 - ref) <= 1e-9 * ref + 1e-14
+    assert orders[1] > 1.6
+    assert abs(mixed[2] - ref) <= 0.02 * ref

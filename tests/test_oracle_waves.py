@@ -1,0 +1,105 @@
+"""Known answers of the elastic wave equation for the oracle's level step.
+
+A smooth plane P wave travelling along x and a plane S wave travelling along y
+(no fault, absorbing edges) are advanced by the oracle's LinElastLevelGodunov
+step and compared with the exact solution, the initial pulse translated by the
+wave speed: the error must fall at close to second order as the grid is
+refined (PPM with primitive limiting, corner transport upwind).  The comparison
+row (column) lies outside the region the domain edges reach in the time run.
+The plain FP64 GPU form equals the oracle step for step (test_gpu_march.py,
+test_gpu_parity.py), so these answers pin it as well.
+
+For a wave f travelling in +d along direction d with speed c and impedance
+Z = rho c the equations v_t = (1/rho) div(sigma), sigma_t = C : grad(v) give
+sigma_dd = f(x_d - c t), v_d = -sigma_dd / Z (P wave; sigma of the two other
+normal directions = lam/(lam+2G) sigma_dd), and sigma_de = f, v_e = -f / Zs for
+an S wave polarised along e.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from tetemoko_gb300 import _capi as A, scenarios as S
+
+G = A.TMK_NGHOST
+AMP = 1.0          # MPa
+WIDTH = 0.8        # km, Gaussian half-width of the pulse
+TRAVEL = 2.0       # km the pulse travels
+LEN = 12.8         # km along the wave
+# km across it: the side edges send P waves inward (an S wave's particle
+# velocity crosses them) at cp during the pulse's travel time; the comparison
+# row (column) in the middle must stay beyond their reach
+SIDE = {"P": 6.0, "S": 9.0}
+
+
+def _scenario(n: int, along: str, wave: str):
+    dx = LEN / n
+    m = int(round(SIDE[wave] / dx))
+    nx, ny = (n, m) if along == "x" else (m, n)
+    return S.Scenario(name="plane_wave", nx=nx, ny=ny, dx=dx, cfl=0.9, elastic=S._elastic(),
+                      scheme=S._scheme(A.TMK_FAULT_NONE, bc=(0, 0, 0, 0, 0, 0)))
+
+
+def _pulse(s: np.ndarray) -> np.ndarray:
+    return AMP * np.exp(-(s / WIDTH) ** 2)
+
+
+def _wave_state(sc, along: str, wave: str, t: float) -> np.ndarray:
+    """The state at time t (cell centres), ghosts included."""
+    c = sc.constants()
+    e = sc.elastic
+    U = sc.initial_U()
+    xs = (np.arange(sc.nx + 2 * G) - G + 0.5) * sc.dx
+    ys = (np.arange(sc.ny + 2 * G) - G + 0.5) * sc.dx
+    pos = (xs[None, :] if along == "x" else ys[:, None]) * np.ones_like(U[0])
+    speed = e.cp if wave == "P" else e.cs
+    f = _pulse(pos - (LEN / 2 - TRAVEL / 2) - speed * t)
+    ratio = c["lam"] / (c["lam"] + 2.0 * c["G"])
+    for side in (0, 11):
+        if wave == "P":
+            d = 0 if along == "x" else 1           # vx / vy
+            sdd = 3 if along == "x" else 4         # sxx / syy
+            other = (4, 5) if along == "x" else (3, 5)
+            U[side + sdd] += f
+            U[side + d] += -f / c["Zp"]
+            for o in other:
+                U[side + o] += ratio * f
+        else:                                       # S wave polarised across the direction, in-plane
+            d = 1 if along == "x" else 0           # vy / vx
+            U[side + 6] += f                       # sxy
+            U[side + d] += -f / c["Zs"]
+    return U
+
+
+def _error(n: int, along: str, wave: str) -> float:
+    sc = _scenario(n, along, wave)
+    U = _wave_state(sc, along, wave, 0.0)
+    dt = sc.dt()
+    speed = sc.elastic.cp if wave == "P" else sc.elastic.cs
+    steps = int(math.ceil(TRAVEL / (speed * dt)))
+    dt = TRAVEL / (speed * steps)
+    boxes = [(0, 0, sc.nx - 1, sc.ny - 1)]
+    t = 0.0
+    for _ in range(steps):
+        assert O.level_step(sc, U, None, boxes, t, dt, nthreads=4) == 0
+        t += dt
+    exact = _wave_state(sc, along, wave, t)
+    comp = (3 if along == "x" else 4) if wave == "P" else 6
+    if along == "x":
+        j = G + sc.ny // 2
+        got, ref = U[comp, j, G:-G], exact[comp, j, G:-G]
+    else:
+        i = G + sc.nx // 2
+        got, ref = U[comp, G:-G, i], exact[comp, G:-G, i]
+    return float(np.sum(np.abs(got - ref)) * sc.dx / (AMP * WIDTH))
+
+
+@pytest.mark.parametrize("along,wave", [("x", "P"), ("y", "P"), ("x", "S"), ("y", "S")])
+def test_plane_wave_converges_at_second_order(along, wave):
+    errs = [_error(n, along, wave) for n in (64, 128, 256)]
+    orders = [math.log2(errs[k] / errs[k + 1]) for k in range(2)]
+    print(f"{wave} along {along}: L1 errors {['%.2e' % e for e in errs]}, orders {['%.2f' % o for o in orders]}")
+    assert errs[2] < 2e-3
+    assert orders[1] > 1.6
