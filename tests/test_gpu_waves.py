@@ -59,3 +59,31 @@ def test_mixed_form_converges_like_the_oracle(cuda_lib, along, wave):
     assert orders[1] > 1.6
     # FP32 state rounding of the pulse on that background, ~4e-6 MPa a step
     assert abs(mixed[2] - ref) <= 0.15 * ref
+
+
+@pytest.mark.parametrize("prec", [A.TMK_PREC_FP64, A.TMK_PREC_MIXED], ids=["fp64", "mixed"])
+def test_uniformly_sliding_fault_on_the_gpu(cuda_lib, prec):
+    """The exact slip rate, traction and slip of a uniformly sliding
+    slip-weakening fault (test_oracle_waves.py): the FP64 form to rounding, the
+    mixed form to FP32 rounding of the 80 MPa stresses."""
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    sc = W.uniform_sliding_scenario(prec)
+    V, tau_d = W.uniform_sliding_answer(sc)
+    U, B = sc.initial_U(), sc.initial_B()
+    ctx = Context(sc)
+    lvl = LinElastLevelGodunov(ctx, [(0, 0, 31, 15), (32, 0, 63, 15), (0, 16, 63, 31)])
+    lvl.set_level(U, B)
+    dt = sc.dt()
+    for k in range(12):
+        lvl.step(k * dt, dt)
+    lvl.get_level(U, B)
+    assert lvl.status()[0] == 0
+    lvl.close()
+    ctx.close()
+    t = 12 * dt
+    tol = 1e-12 if prec == A.TMK_PREC_FP64 else 1e-5
+    mid = slice(G + 24, G + 40)
+    np.testing.assert_allclose(B[4, mid], V, rtol=tol)
+    np.testing.assert_allclose(B[2, mid], tau_d, rtol=tol)
+    np.testing.assert_allclose(B[5, mid], V * t, rtol=tol)
+    np.testing.assert_allclose(U[6, G, mid], tau_d, atol=0.01 * (sc.elastic.sxy0 - tau_d))

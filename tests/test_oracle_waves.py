@@ -103,3 +103,47 @@ def test_plane_wave_converges_at_second_order(along, wave):
     print(f"{wave} along {along}: L1 errors {['%.2e' % e for e in errs]}, orders {['%.2f' % o for o in orders]}")
     assert errs[2] < 2e-3
     assert orders[1] > 1.6
+
+
+def uniform_sliding_scenario(prec=A.TMK_PREC_FP64):
+    """A slip-weakening fault loaded above its static strength everywhere
+    (tau0 = 81.6 MPa > mu_s sigma_n = 81.24 MPa, no nucleation patch) with an
+    instant weakening (Dc = 1e-9 m): every face slides from the first step."""
+    sc = S.slip_weakening(nx=64, ny=32, dx=0.1, precision=prec)
+    sc.sw.num_patches = 0
+    sc.sw.dw = 1e-9
+    sc.elastic.sxy0 = 81.6
+    return sc
+
+
+def uniform_sliding_answer(sc):
+    """Exact answer of the 1-D problem the uniform fault poses: shear waves carry
+    the stress drop away at either side, so the traction sits at the dynamic
+    strength mu_d sigma_n and the slip rate is V = 2 (tau0 - mu_d sigma_n) / Zs."""
+    c = sc.constants()
+    sn = -sc.elastic.syy0
+    return 2.0 * (sc.elastic.sxy0 - sc.sw.fd * sn) / c["Zs"], sc.sw.fd * sn
+
+
+def test_uniformly_sliding_fault_radiates_at_the_exact_slip_rate():
+    """Slip-weakening boundary data after 12 steps on the faces away from the
+    domain's x edges: slip rate (component 4, and its x part 0), traction (2) and
+    slip (5, 7) equal the exact answer to rounding; the cells next to the fault
+    carry the dynamic shear stress to within 1 % of the stress drop (the
+    scheme's smearing of the stress front, which the first step's static
+    strength also shapes)."""
+    sc = uniform_sliding_scenario()
+    V, tau_d = uniform_sliding_answer(sc)
+    U, B = sc.initial_U(), sc.initial_B()
+    dt = sc.dt()
+    t = 0.0
+    for _ in range(12):
+        assert O.level_step(sc, U, B, [(0, 0, sc.nx - 1, sc.ny - 1)], t, dt) == 0
+        t += dt
+    mid = slice(G + 24, G + 40)               # faces beyond the x edges' reach (cp t < 1.1 km)
+    np.testing.assert_allclose(B[4, mid], V, rtol=1e-12)
+    np.testing.assert_allclose(B[0, mid], V, rtol=1e-12)
+    np.testing.assert_allclose(B[2, mid], tau_d, rtol=1e-12)
+    np.testing.assert_allclose(B[5, mid], V * t, rtol=1e-12)
+    np.testing.assert_allclose(B[7, mid], V * t, rtol=1e-12)
+    np.testing.assert_allclose(U[6, G, mid], tau_d, atol=0.01 * (sc.elastic.sxy0 - tau_d))
