@@ -453,9 +453,9 @@ constexpr size_t march_smem_bytes() {
   return (size_t)MARCH_WARPS * march_warp_pairs<T, G>() * sizeof(typename PairOf<T>::P);
 }
 
-// resident CTAs per SM the register allocation targets: FP32 in-plane 3 (164
+// resident CTAs per SM the register allocation targets: FP32 in-plane 3 (168
 // registers, no spills, with the y-direction carries in shared memory),
-// antiplane 5 (94 registers); FP64 in-plane 2, antiplane 4
+// antiplane 5 (96 registers); FP64 in-plane 2, antiplane 4
 template <typename T, int G> struct MarchMinBlocks {
   static constexpr int value = sizeof(T) == 4 ? ((G == 0) ? 3 : 5) : ((G == 0) ? 2 : 4);
 };
