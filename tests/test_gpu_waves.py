@@ -87,3 +87,33 @@ def test_uniformly_sliding_fault_on_the_gpu(cuda_lib, prec):
     np.testing.assert_allclose(B[2, mid], tau_d, rtol=tol)
     np.testing.assert_allclose(B[5, mid], V * t, rtol=tol)
     np.testing.assert_allclose(U[6, G, mid], tau_d, atol=0.01 * (sc.elastic.sxy0 - tau_d))
+
+
+@pytest.mark.parametrize("prec", [A.TMK_PREC_FP64, A.TMK_PREC_MIXED], ids=["fp64", "mixed"])
+def test_uniformly_sliding_rate_and_state_fault_on_the_gpu(cuda_lib, prec):
+    """The uniformly sliding rate-and-state fault of test_oracle_waves.py on
+    three patches: slip rate (component 2) against its ODE at the step's
+    midpoint and state (10) at the step's end after 20, 40 and 60 steps; the
+    FP64 form to the oracle's 1e-5 / 1e-6, the mixed form (FP32 volume
+    stresses near 70 MPa) to 1e-4 / 1e-5."""
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    sc = W.uniform_rs_scenario(prec)
+    U, B = sc.initial_U(), sc.initial_B()
+    dt = sc.dt()
+    V_ode, psi_ode = W.uniform_rs_answer(sc, 61 * dt)
+    ctx = Context(sc)
+    lvl = LinElastLevelGodunov(ctx, [(0, 0, 63, 31), (64, 0, 127, 31), (0, 32, 127, 63)])
+    lvl.set_level(U, B)
+    c = G + sc.nx // 2
+    tv, tp = (1e-5, 1e-6) if prec == A.TMK_PREC_FP64 else (1e-4, 1e-5)
+    for k in range(60):
+        lvl.step(k * dt, dt)
+        if (k + 1) % 20 == 0:
+            t = (k + 1) * dt
+            lvl.get_level(U, B)
+            assert lvl.status()[0] == 0
+            V = V_ode(t - 0.5 * dt)
+            assert abs(B[2, c] - V) <= tv * V, (t, B[2, c], V)
+            assert abs(B[10, c] - psi_ode(t)) <= tp, (t, B[10, c], psi_ode(t))
+    lvl.close()
+    ctx.close()

@@ -147,3 +147,68 @@ def test_uniformly_sliding_fault_radiates_at_the_exact_slip_rate():
     np.testing.assert_allclose(B[5, mid], V * t, rtol=1e-12)
     np.testing.assert_allclose(B[7, mid], V * t, rtol=1e-12)
     np.testing.assert_allclose(U[6, G, mid], tau_d, atol=0.01 * (sc.elastic.sxy0 - tau_d))
+
+
+def uniform_rs_scenario(prec=A.TMK_PREC_FP64):
+    """A rate-and-state fault (aging law, velocity strengthening a=0.012,
+    b=0.008, L=0.2 m, no nucleation) in steady sliding at 0.5 m/s whose shear
+    load is then 2 MPa above that state's: every face speeds up and relaxes
+    together, the 1-D problem of a uniformly sliding fault."""
+    sc = S.rate_state(nx=128, ny=64, dx=0.05, precision=prec)
+    rs = sc.rs
+    rs.nsig = 0.0
+    rs.a, rs.b, rs.L = 0.012, 0.008, 0.2
+    sn = -sc.elastic.syy0
+    Zs = sc.constants()["Zs"]
+    Vi = 0.5
+    rs.psi_init = rs.f0 - rs.b * math.log(Vi / rs.V0)            # aging-law steady state at Vi
+    tau_f = sn * rs.a * math.asinh(Vi / (2 * rs.V0) * math.exp(rs.psi_init / rs.a))
+    sc.elastic.sxy0 = tau_f + 0.5 * Zs * Vi + 2.0
+    return sc
+
+
+def uniform_rs_answer(sc, t_end):
+    """The 1-D problem's exact evolution: the traction is tau0 - (Zs/2) V
+    (radiation damping) = sn a asinh(V e^(psi/a) / (2 V0)), and the aging law
+    d psi/dt = (b/L) (V0 e^(-(psi - f0)/b) - V), integrated to 1e-12.
+    Returns (V(t), psi(t))."""
+    from scipy.integrate import solve_ivp
+    from scipy.optimize import brentq
+    rs = sc.rs
+    sn = -sc.elastic.syy0
+    tau0 = sc.elastic.sxy0
+    Zs = sc.constants()["Zs"]
+
+    def V_of(psi):
+        f = lambda V: tau0 - 0.5 * Zs * V - sn * rs.a * math.asinh(V / (2 * rs.V0) * math.exp(psi / rs.a))
+        return brentq(f, 0.0, 2.0 * tau0 / Zs, xtol=1e-15, rtol=1e-15)
+
+    def rhs(t, y):
+        return [rs.b / rs.L * (rs.V0 * math.exp(-(y[0] - rs.f0) / rs.b) - V_of(y[0]))]
+
+    sol = solve_ivp(rhs, (0.0, t_end), [rs.psi_init], rtol=1e-12, atol=1e-14, dense_output=True, method="DOP853")
+    return (lambda t: V_of(float(sol.sol(t)[0]))), (lambda t: float(sol.sol(t)[0]))
+
+
+def test_uniformly_sliding_rate_and_state_fault_follows_its_ode():
+    """60 steps (until the domain's x edges' disturbances could reach the centre
+    faces): the slip rate the level step stores (boundary component 2) is the
+    ODE's at the step's midpoint, where the scheme's time-centred face state
+    sits, to 1e-5, and the state variable (component 10) the ODE's at the step's
+    end to 1e-6; the slip rate changes by 8 % over the run."""
+    sc = uniform_rs_scenario()
+    U, B = sc.initial_U(), sc.initial_B()
+    dt = sc.dt()
+    V_ode, psi_ode = uniform_rs_answer(sc, 61 * dt)
+    c = G + sc.nx // 2
+    t = 0.0
+    Vs = []
+    for _ in range(60):
+        assert O.level_step(sc, U, B, [(0, 0, sc.nx - 1, sc.ny - 1)], t, dt) == 0
+        t += dt
+        V = V_ode(t - 0.5 * dt)
+        assert abs(B[2, c] - V) <= 1e-5 * V, (t, B[2, c], V)
+        assert abs(B[10, c] - psi_ode(t)) <= 1e-6, (t, B[10, c], psi_ode(t))
+        np.testing.assert_allclose(B[2, c - 4:c + 4], B[2, c], rtol=1e-7)      # uniform along the fault
+        Vs.append(B[2, c])
+    assert Vs[-1] / Vs[0] > 1.05
