@@ -1,7 +1,9 @@
-"""The plane-wave known answers of test_oracle_waves.py on the GPU: the FP64
-form equals the oracle's step on them, and the mixed form (FP32 volume) reaches
-the exact solution at the same second-order rate, its FP32 rounding below the
-truncation error on these grids."""
+"""The known answers of test_oracle_waves.py on the GPU: on the plane waves
+(axis-aligned and oblique, 2-D levels and the 3-D patch step) the FP64 form
+equals the oracle's step, and the mixed form (FP32 volume) reaches the exact
+solution at the same second-order rate, its FP32 rounding below the truncation
+error on these grids; on the uniformly sliding faults both forms reach the
+1-D answers."""
 import math
 
 import numpy as np
@@ -9,6 +11,7 @@ import pytest
 
 from tetemoko_gb300 import _capi as A
 from tests import test_oracle_waves as W
+from tests.helpers import rel_err
 
 pytestmark = pytest.mark.gpu
 G = A.TMK_NGHOST
@@ -117,3 +120,144 @@ def test_uniformly_sliding_rate_and_state_fault_on_the_gpu(cuda_lib, prec):
             assert abs(B[10, c] - psi_ode(t)) <= tp, (t, B[10, c], psi_ode(t))
     lvl.close()
     ctx.close()
+
+
+def _gpu_oblique(n: int, wave: str, prec: int):
+    """The oblique plane wave of test_oracle_waves.py advanced by a GPU level
+    tiled into 32x32 patches: (state, per-component L1 errors on the disc)."""
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    from oracle import tile_boxes
+    sc = W.oblique_scenario(n, wave)
+    sc.scheme.precision = prec
+    U, _ = W.oblique_state(sc, wave, 0.0)
+    steps, dt = W.oblique_steps(sc, wave)
+    ctx = Context(sc)
+    lvl = LinElastLevelGodunov(ctx, tile_boxes(n, n, 32))
+    lvl.set_level(U, None)
+    for k in range(steps):
+        lvl.step(k * dt, dt)
+    lvl.get_level(U, None)
+    assert lvl.status()[0] == 0
+    lvl.close()
+    ctx.close()
+    return U, W.oblique_error(sc, wave, U, steps * dt)
+
+
+@pytest.mark.parametrize("wave", ["P", "S"])
+def test_oblique_wave_on_the_gpu(cuda_lib, wave):
+    """The FP64 form reaches the oracle's state at n = 128 to 1e-11 relative
+    per component (the parity bound of the FP64 form); the mixed form converges at the oracle's second order and
+    its error at n = 256 lies within 5 % of the FP64 form's (FP32 rounding of
+    the pulse on the 70 MPa background stays below the truncation error)."""
+    import oracle as O
+    sc = W.oblique_scenario(128, wave)
+    Ur, _ = W.oblique_state(sc, wave, 0.0)
+    steps, dt = W.oblique_steps(sc, wave)
+    for k in range(steps):
+        assert O.level_step(sc, Ur, None, O.tile_boxes(128, 128, 32), k * dt, dt, nthreads=8) == 0
+    U64, _ = _gpu_oblique(128, wave, A.TMK_PREC_FP64)
+    v = (slice(None), slice(G, -G), slice(G, -G))
+    assert rel_err(U64[v], Ur[v]) <= 1e-11
+    mixed = [_gpu_oblique(n, wave, A.TMK_PREC_MIXED)[1] for n in (64, 128, 256)]
+    fp64 = _gpu_oblique(256, wave, A.TMK_PREC_FP64)[1]
+    orders = np.log2(mixed[1] / mixed[2])
+    print(f"oblique {wave}: mixed errors at 256 {mixed[2]}, FP64 {fp64}, orders 128->256 {orders}")
+    assert np.all(orders > 1.8)
+    np.testing.assert_allclose(mixed[2], fp64, rtol=0.05)
+
+
+def _gpu_oblique3(n: int, wave: str, prec: int):
+    """The 3-D oblique plane wave of test_oracle_waves.py advanced on the GPU
+    by tmk_patch_update_state_3d on one patch covering the cube: (state,
+    per-component L1 errors on the ball)."""
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    sc = W.oblique3_scenario(n, wave)
+    sc.scheme.precision = prec
+    U, _ = W.oblique3_state(sc, wave, 0.0)
+    steps, dt = W.oblique3_steps(sc, wave)
+    ctx = Context(sc)
+    box = ((0, 0, 0), (n - 1,) * 3)
+    pg = LinElastPatchGodunov3D(ctx, box)
+    pg.set_current_box(box)
+    Ud = torch.from_numpy(U).cuda()
+    for k in range(steps):
+        pg.set_current_time(k * dt)
+        pg.update_state(Ud, (-G, -G, -G), dt)
+    torch.cuda.synchronize()
+    U = Ud.cpu().numpy()
+    ctx.close()
+    return U, W.oblique3_error(sc, wave, U, steps * dt)
+
+
+@pytest.mark.parametrize("wave", ["P", "S"])
+def test_oblique_wave_3d_on_the_gpu(cuda_lib, wave):
+    """3-D: the FP64 form reaches the oracle's state at n = 48 to 1e-11
+    relative per component; the mixed form converges at the oracle's order
+    from 48 to 64 cells a side, its errors within 5 % of the FP64 form's."""
+    sc = W.oblique3_scenario(48, wave)
+    Ur, _ = W.oblique3_state(sc, wave, 0.0)
+    steps, dt = W.oblique3_steps(sc, wave)
+    W.oracle_steps_3d(sc, Ur, steps, dt)
+    U64, _ = _gpu_oblique3(48, wave, A.TMK_PREC_FP64)
+    v = (slice(None), slice(G, -G), slice(G, -G), slice(G, -G))
+    assert rel_err(U64[v], Ur[v]) <= 1e-11
+    mixed = [_gpu_oblique3(n, wave, A.TMK_PREC_MIXED)[1] for n in (48, 64)]
+    fp64 = _gpu_oblique3(64, wave, A.TMK_PREC_FP64)[1]
+    orders = np.log(mixed[0] / mixed[1]) / math.log(64 / 48)
+    print(f"3-D oblique {wave}: mixed errors at 64 {mixed[1]}, FP64 {fp64}, orders {orders}")
+    assert np.all(orders > 1.6)
+    np.testing.assert_allclose(mixed[1], fp64, rtol=0.05)
+
+
+def _gpu_amr_wave(nc: int, r: int, wave: str, prec: int):
+    """The hierarchy of test_oracle_waves.amr_wave_hierarchy stepped by the
+    device AMR driver: (levels read back as LevelData, [fine, coarse] errors)."""
+    import oracle as O
+    from tetemoko_gb300.amr import AMRHierarchy
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    sc, datas, covered, steps, dt = W.amr_wave_hierarchy(nc, r, wave)
+    sc.scheme.precision = prec
+    ctx = Context(sc)
+    lvs = []
+    for d in datas:
+        lv = LinElastLevelGodunov(ctx, d.boxes, domain=d.domain, dx=d.dx)
+        lv.set_patches(d.U, d.B)
+        lvs.append(lv)
+    h = AMRHierarchy(lvs, [r])
+    for _ in range(steps):
+        h.step(dt)
+    got = []
+    for lv, d in zip(lvs, datas):
+        assert lv.status()[0] == 0
+        Us, Bs = lv.get_patches()
+        got.append(O.LevelData(d.domain, d.dx, d.boxes, d.nb, Us, Bs))
+    h.close()
+    for lv in lvs:
+        lv.close()
+    ctx.close()
+    return got, W.amr_wave_errors(sc, wave, got, covered, steps * dt)
+
+
+@pytest.mark.parametrize("wave", ["P", "S"])
+@pytest.mark.parametrize("r", [2, 4])
+def test_oblique_wave_through_amr_on_the_gpu(cuda_lib, wave, r):
+    """The device hierarchy in the FP64 form ends where the oracle's does
+    (coarse grid of 64 cells: 1e-11 relative per patch and component); in the
+    mixed form its fine- and coarse-level errors converge at the oracle's
+    second order and lie within 5 % of the FP64 form's at 128 cells."""
+    import oracle as O
+    sc, refs, _, steps, dt = W.amr_wave_hierarchy(64, r, wave)
+    assert O.amr_run(sc, refs, [r], 0.0, dt, steps, nthreads=8) == 0
+    got, _ = _gpu_amr_wave(64, r, wave, A.TMK_PREC_FP64)
+    for g, ref in zip(got, refs):
+        for p in range(len(ref.boxes)):
+            assert rel_err(g.U[p][:, G:-G, G:-G], ref.U[p][:, G:-G, G:-G]) <= 1e-11
+    mixed = [_gpu_amr_wave(nc, r, wave, A.TMK_PREC_MIXED)[1] for nc in (64, 128)]
+    fp64 = _gpu_amr_wave(128, r, wave, A.TMK_PREC_FP64)[1]
+    for lvl in range(2):
+        orders = np.log2(mixed[0][lvl] / mixed[1][lvl])
+        print(f"AMR r={r} {wave} level {'fine' if lvl == 0 else 'coarse'}: mixed {mixed[1][lvl]}, "
+              f"FP64 {fp64[lvl]}, orders {orders}")
+        assert np.all(orders > 1.8)
+        np.testing.assert_allclose(mixed[1][lvl], fp64[lvl], rtol=0.05)

@@ -6,8 +6,12 @@ step and compared with the exact solution, the initial pulse translated by the
 wave speed: the error must fall at close to second order as the grid is
 refined (PPM with primitive limiting, corner transport upwind).  The comparison
 row (column) lies outside the region the domain edges reach in the time run.
+Oblique plane waves, in 2-D and in 3-D (the CH_SPACEDIM == 3 step), add the
+transverse corrections, which an axis-aligned wave leaves at zero.  Two fault
+problems with a 1-D exact answer close the set: a uniformly sliding
+slip-weakening fault and a uniformly sliding rate-and-state fault.
 The plain FP64 GPU form equals the oracle step for step (test_gpu_march.py,
-test_gpu_parity.py), so these answers pin it as well.
+test_gpu_parity.py, test_gpu_3d.py), so these answers pin it as well.
 
 For a wave f travelling in +d along direction d with speed c and impedance
 Z = rho c the equations v_t = (1/rho) div(sigma), sigma_t = C : grad(v) give
@@ -80,7 +84,7 @@ def _error(n: int, along: str, wave: str) -> float:
     speed = sc.elastic.cp if wave == "P" else sc.elastic.cs
     steps = int(math.ceil(TRAVEL / (speed * dt)))
     dt = TRAVEL / (speed * steps)
-    boxes = [(0, 0, sc.nx - 1, sc.ny - 1)]
+    boxes = O.tile_boxes(sc.nx, sc.ny, 64)    # patches for the oracle's threads; the exchange makes them one
     t = 0.0
     for _ in range(steps):
         assert O.level_step(sc, U, None, boxes, t, dt, nthreads=4) == 0
@@ -212,3 +216,268 @@ def test_uniformly_sliding_rate_and_state_fault_follows_its_ode():
         np.testing.assert_allclose(B[2, c - 4:c + 4], B[2, c], rtol=1e-7)      # uniform along the fault
         Vs.append(B[2, c])
     assert Vs[-1] / Vs[0] > 1.05
+
+
+# Oblique plane waves: the pulse travels along n = (cos th, sin th), so every
+# direction's transverse correction of the corner transport upwind scheme
+# carries it (an axis-aligned wave has zero transverse differences).  The
+# square domain's edges send waves inward from the first step; the error is
+# measured on the central disc of radius R, which they do not reach in the
+# pulse's travel time (cp t + R + stencil spread below the half-width).
+OBLIQUE_TH = math.radians(30.0)
+OBLIQUE_R = 1.5                       # km
+OBLIQUE_LEN = {"P": 8.0, "S": 11.0}   # km, side of the square domain
+
+
+def oblique_scenario(n: int, wave: str):
+    return S.Scenario(name="oblique_wave", nx=n, ny=n, dx=OBLIQUE_LEN[wave] / n, cfl=0.9,
+                      elastic=S._elastic(), scheme=S._scheme(A.TMK_FAULT_NONE, bc=(0, 0, 0, 0, 0, 0)))
+
+
+def wave_at(sc, wave: str, x: np.ndarray, y: np.ndarray, t: float) -> np.ndarray:
+    """The oblique wave at time t at cell centres (x, y), measured from the
+    domain's centre, on the scenario's background.  A P wave along n carries
+    v = -f/Zp n, sigma = f (r I + (1 - r) n n^T), r = lam/(lam + 2G); an S wave
+    polarised in-plane along m = (-n_y, n_x) carries v = -f/Zs m,
+    sigma = f (n m^T + m n^T)."""
+    c = sc.constants()
+    n = (math.cos(OBLIQUE_TH), math.sin(OBLIQUE_TH))
+    m = (-n[1], n[0])
+    speed = sc.elastic.cp if wave == "P" else sc.elastic.cs
+    f = _pulse(x * n[0] + y * n[1] + 0.5 * TRAVEL - speed * t)
+    r = c["lam"] / (c["lam"] + 2.0 * c["G"])
+    U = np.empty((22,) + x.shape)
+    U[:] = sc.background()[:, None, None]
+    for side in (0, 11):
+        if wave == "P":
+            for d in range(2):
+                U[side + d] += -f / c["Zp"] * n[d]
+                U[side + 3 + d] += f * (r + (1.0 - r) * n[d] * n[d])
+            U[side + 5] += r * f
+            U[side + 6] += f * (1.0 - r) * n[0] * n[1]
+        else:
+            for d in range(2):
+                U[side + d] += -f / c["Zs"] * m[d]
+                U[side + 3 + d] += 2.0 * f * n[d] * m[d]
+            U[side + 6] += f * (n[0] * m[1] + n[1] * m[0])
+    return U
+
+
+def _centres(sc, b, dx: float, ghost: int):
+    """Cell-centre coordinates, from the domain's centre, of box b grown by
+    `ghost` cells on a level of cell size dx."""
+    yy, xx = np.mgrid[b[1] - ghost:b[3] + ghost + 1, b[0] - ghost:b[2] + ghost + 1]
+    return (xx + 0.5) * dx - 0.5 * sc.nx * sc.dx, (yy + 0.5) * dx - 0.5 * sc.ny * sc.dx
+
+
+def oblique_state(sc, wave: str, t: float):
+    """(U, r2): the state of the whole level at time t, ghosts included, and
+    the squared distance of each cell centre from the domain's centre."""
+    x, y = _centres(sc, (0, 0, sc.nx - 1, sc.ny - 1), sc.dx, G)
+    return wave_at(sc, wave, x, y, t), x * x + y * y
+
+
+OBLIQUE_COMPS = (0, 1, 3, 4, 6)       # vx, vy, sxx, syy, sxy
+
+
+def oblique_steps(sc, wave: str):
+    speed = sc.elastic.cp if wave == "P" else sc.elastic.cs
+    steps = int(math.ceil(TRAVEL / (speed * sc.dt())))
+    return steps, TRAVEL / (speed * steps)
+
+
+def oblique_error(sc, wave: str, U: np.ndarray, t: float) -> np.ndarray:
+    """L1 error over the central disc per component of OBLIQUE_COMPS,
+    normalised by the pulse's amplitude and width."""
+    exact, r2 = oblique_state(sc, wave, t)
+    disc = r2 <= OBLIQUE_R ** 2
+    return np.array([np.sum(np.abs(U[c] - exact[c])[disc]) * sc.dx ** 2 / (AMP * WIDTH) for c in OBLIQUE_COMPS])
+
+
+@pytest.mark.parametrize("wave", ["P", "S"])
+def test_oblique_plane_wave_converges_at_second_order(wave):
+    """Every component's error falls at order 2.0-2.1 from 64 to 256 cells a
+    side (the level tiled into 32x32 patches, which the exchange makes
+    equivalent to one patch)."""
+    errs = []
+    for n in (64, 128, 256):
+        sc = oblique_scenario(n, wave)
+        U, _ = oblique_state(sc, wave, 0.0)
+        steps, dt = oblique_steps(sc, wave)
+        t = 0.0
+        for _ in range(steps):
+            assert O.level_step(sc, U, None, O.tile_boxes(n, n, 32), t, dt, nthreads=4) == 0
+            t += dt
+        errs.append(oblique_error(sc, wave, U, t))
+    orders = np.log2(errs[1] / errs[2])
+    print(f"oblique {wave}: errors at 256 {errs[2]}, orders 64->128 {np.log2(errs[0] / errs[1])}, 128->256 {orders}")
+    assert np.all(errs[2] < 4e-3)
+    assert np.all(orders > 1.8)
+
+
+# The same in 3-D (CH_SPACEDIM == 3): a plane wave along a direction with no
+# zero component, so that all six transverse corrections of the 3-D corner
+# transport upwind step carry it; the S wave is polarised along the unit
+# vector of the z axis' part normal to n, so that all nine components carry a
+# pulse.  Error on the central ball of radius 1 km; the S pulse travels 1 km
+# (the edges' P waves must stay out of the ball for its travel time).
+N3 = np.array([1.0, 0.7, 0.5]) / np.linalg.norm([1.0, 0.7, 0.5])
+M3 = np.array([0.0, 0.0, 1.0]) - N3[2] * N3
+M3 /= np.linalg.norm(M3)
+OBLIQUE3_LEN = {"P": 7.0, "S": 6.5}      # km, side of the cube
+OBLIQUE3_TRAVEL = {"P": 2.0, "S": 1.0}   # km
+OBLIQUE3_R = 1.0                         # km
+_SYM = {(0, 0): 3, (1, 1): 4, (2, 2): 5, (0, 1): 6, (0, 2): 7, (1, 2): 8}
+
+
+def oblique3_scenario(n: int, wave: str):
+    return S.Scenario(name="oblique_wave_3d", nx=n, ny=n, dx=OBLIQUE3_LEN[wave] / n, cfl=0.9,
+                      elastic=S._elastic(), scheme=S._scheme(A.TMK_FAULT_NONE, bc=(0, 0, 0, 0, 0, 0)))
+
+
+def oblique3_state(sc, wave: str, t: float):
+    """(U (22, n+8, n+8, n+8), r2) at time t, as oblique_state in 3-D."""
+    c = sc.constants()
+    n = sc.nx
+    U = np.empty((22,) + (n + 2 * G,) * 3)
+    U[:] = sc.background()[:, None, None, None]
+    xs = (np.arange(n + 2 * G) - G + 0.5) * sc.dx - 0.5 * n * sc.dx
+    Z, Y, X = np.meshgrid(xs, xs, xs, indexing="ij")
+    speed = sc.elastic.cp if wave == "P" else sc.elastic.cs
+    f = _pulse(X * N3[0] + Y * N3[1] + Z * N3[2] + 0.5 * OBLIQUE3_TRAVEL[wave] - speed * t)
+    r = c["lam"] / (c["lam"] + 2.0 * c["G"])
+    for side in (0, 11):
+        for d in range(3):
+            U[side + d] += -f / c["Zp"] * N3[d] if wave == "P" else -f / c["Zs"] * M3[d]
+        for (i, j), q in _SYM.items():
+            if wave == "P":
+                U[side + q] += f * ((r if i == j else 0.0) + (1.0 - r) * N3[i] * N3[j])
+            else:
+                U[side + q] += f * (N3[i] * M3[j] + M3[i] * N3[j])
+    return U, X * X + Y * Y + Z * Z
+
+
+def oblique3_steps(sc, wave: str):
+    speed = sc.elastic.cp if wave == "P" else sc.elastic.cs
+    dt = sc.dt() / math.sqrt(3.0)          # the 3-D CFL bound
+    steps = int(math.ceil(OBLIQUE3_TRAVEL[wave] / (speed * dt)))
+    return steps, OBLIQUE3_TRAVEL[wave] / (speed * steps)
+
+
+def oblique3_error(sc, wave: str, U: np.ndarray, t: float) -> np.ndarray:
+    exact, r2 = oblique3_state(sc, wave, t)
+    ball = r2 <= OBLIQUE3_R ** 2
+    return np.array([np.sum(np.abs(U[c] - exact[c])[ball]) * sc.dx ** 3 / (AMP * WIDTH) for c in range(9)])
+
+
+def oracle_steps_3d(sc, U: np.ndarray, steps: int, dt: float, nthreads: int = 8) -> None:
+    """Advance the cube U (no fault) by the oracle's 3-D patch step, the domain
+    tiled into 2x2x2 patches stepped on threads (the oracle's calls release
+    the interpreter lock), each patch's ghost cells refilled from the level
+    between steps as an exchange does."""
+    from concurrent.futures import ThreadPoolExecutor
+    n = sc.nx
+    h = n // 2
+    boxes = [((x0, y0, z0), (x0 + h - 1, y0 + h - 1, z0 + h - 1))
+             for z0 in (0, h) for y0 in (0, h) for x0 in (0, h)]
+    cut = lambda lo, hi, g: (slice(None),) + tuple(slice(lo[d] + G - g, hi[d] + G + g + 1) for d in (2, 1, 0))
+
+    def one(box, t):
+        lo, hi = box
+        sub = np.ascontiguousarray(U[cut(lo, hi, G)])
+        rc, _ = O.patch_update_state_3d(sc, sub, tuple(v - G for v in lo), lo, hi, (0, 0, 0), (n - 1,) * 3,
+                                        None, (0, 0), sc.dx, t, dt)
+        assert rc == 0
+        return sub
+
+    with ThreadPoolExecutor(nthreads) as pool:
+        for k in range(steps):
+            subs = list(pool.map(lambda b: one(b, k * dt), boxes))
+            for (lo, hi), sub in zip(boxes, subs):
+                U[cut(lo, hi, 0)] = sub[:, G:-G, G:-G, G:-G]
+
+
+@pytest.mark.parametrize("wave", ["P", "S"])
+def test_oblique_plane_wave_3d_converges_at_second_order(wave):
+    """Every one of the nine components converges at order 1.8-2.2 from 48 to
+    64 cells a side (the step ratio is 4/3: order = log(e48/e64) / log(4/3))."""
+    errs = []
+    for n in (48, 64):
+        sc = oblique3_scenario(n, wave)
+        U, _ = oblique3_state(sc, wave, 0.0)
+        steps, dt = oblique3_steps(sc, wave)
+        oracle_steps_3d(sc, U, steps, dt)
+        errs.append(oblique3_error(sc, wave, U, steps * dt))
+    orders = np.log(errs[0] / errs[1]) / math.log(64 / 48)
+    print(f"3-D oblique {wave}: errors at 64 {errs[1]}, orders {orders}")
+    assert np.all(errs[1] < 1e-2)
+    assert np.all(orders > 1.6)
+
+
+# Through a refined hierarchy: the 2-D oblique wave crosses the coarse-fine
+# interface of a centred fine square (2 km a side) at ratios 2 and 4, subcycled
+# (AMRLevelLinElast::advance order: the coarse step, r fine steps with the
+# coarse-fine ghost fill interpolated in time, refluxing, average-down).  Its
+# error converges at second order on the fine level and on the coarse cells
+# around it that it does not cover (within 1.5 km of the centre), so the
+# fill, the flux registers and the average-down carry the wave to the
+# scheme's accuracy.
+AMR_FINE_HALF = 1.0     # km
+
+
+def amr_wave_hierarchy(nc: int, r: int, wave: str):
+    """(sc, [coarse, fine] LevelData at t = 0, covered coarse cell range, steps, dt)."""
+    sc = oblique_scenario(nc, wave)
+    k = int(round(AMR_FINE_HALF / sc.dx))
+    c0, c1 = nc // 2 - k, nc // 2 + k - 1
+    fb = (c0 * r, c0 * r, (c1 + 1) * r - 1, (c1 + 1) * r - 1)
+    fboxes = [(i0, j0, min(i0 + 31, fb[2]), min(j0 + 31, fb[3]))
+              for j0 in range(fb[1], fb[3] + 1, 32) for i0 in range(fb[0], fb[2] + 1, 32)]
+    levels = []
+    for dom, dx, boxes in (((0, 0, nc - 1, nc - 1), sc.dx, O.tile_boxes(nc, nc, 32)),
+                           ((0, 0, nc * r - 1, nc * r - 1), sc.dx / r, fboxes)):
+        lv = O.LevelData(dom, dx, boxes, 0)
+        for p, b in enumerate(boxes):
+            lv.U[p][:] = wave_at(sc, wave, *_centres(sc, b, dx, G), 0.0)
+        levels.append(lv)
+    steps, dt = oblique_steps(sc, wave)
+    return sc, levels, (c0, c1), steps, dt
+
+
+def amr_wave_errors(sc, wave: str, levels, covered, t: float, R: float = 1.5):
+    """L1 errors (per component of OBLIQUE_COMPS) of the fine level's valid
+    cells and of the coarse level's uncovered cells within R of the centre."""
+    C, F = levels
+    out = []
+    for lv, coarse in ((F, False), (C, True)):
+        e = np.zeros(len(OBLIQUE_COMPS))
+        for p, b in enumerate(lv.boxes):
+            x, y = _centres(sc, b, lv.dx, 0)
+            exact = wave_at(sc, wave, x, y, t)
+            mask = np.ones(x.shape, dtype=bool)
+            if coarse:
+                ii = np.arange(b[0], b[2] + 1)[None, :]
+                jj = np.arange(b[1], b[3] + 1)[:, None]
+                cov = (ii >= covered[0]) & (ii <= covered[1]) & (jj >= covered[0]) & (jj <= covered[1])
+                mask = (x * x + y * y <= R * R) & ~cov
+            u = lv.U[p][:, G:-G, G:-G]
+            e += [np.sum(np.abs(u[c] - exact[c])[mask]) * lv.dx ** 2 for c in OBLIQUE_COMPS]
+        out.append(e / (AMP * WIDTH))
+    return out
+
+
+@pytest.mark.parametrize("wave", ["P", "S"])
+@pytest.mark.parametrize("r", [2, 4])
+def test_oblique_wave_through_amr_converges_at_second_order(wave, r):
+    """Coarse grids of 32, 64 and 128 cells a side: fine-level and coarse-level
+    errors fall at order 1.9-2.2 from 64 to 128 in every component."""
+    errs = []
+    for nc in (32, 64, 128):
+        sc, levels, covered, steps, dt = amr_wave_hierarchy(nc, r, wave)
+        assert O.amr_run(sc, levels, [r], 0.0, dt, steps, nthreads=4) == 0
+        errs.append(amr_wave_errors(sc, wave, levels, covered, steps * dt))
+    fine = np.log2(errs[1][0] / errs[2][0])
+    coarse = np.log2(errs[1][1] / errs[2][1])
+    print(f"AMR r={r} {wave}: fine errors {errs[2][0]} orders {fine}; coarse errors {errs[2][1]} orders {coarse}")
+    assert np.all(errs[2][0] < 5e-3) and np.all(errs[2][1] < 5e-3)
+    assert np.all(fine > 1.8) and np.all(coarse > 1.8)
