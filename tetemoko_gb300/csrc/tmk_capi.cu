@@ -506,6 +506,9 @@ extern "C" void tmk_level_destroy(tmk_level* L) {
   if (L->fork_ev) cudaEventDestroy(L->fork_ev);
   if (L->join_ev) cudaEventDestroy(L->join_ev);
   if (L->side) cudaStreamDestroy(L->side);
+  for (cudaEvent_t e : L->xfer_ev)
+    if (e) cudaEventDestroy(e);
+  if (L->xfer) cudaStreamDestroy(L->xfer);
   delete L;
 }
 
@@ -802,10 +805,63 @@ tmk::CompList step_comps(const tmk_level_s* L) {
   return cl;
 }
 
-// U of put/take.  Mixed form: pinned host or device pointers are read or
-// written in place by the copy kernel (one crossing of the host link), other
-// host memory is staged through the level's FP64 staging buffer.  FP64 form:
-// one strided copy per component.
+// Mixed form, pinned host FAB: the copy engines move the valid rows of one
+// group of components between the host FAB and the FP64 staging buffer (the
+// same layout) while the conversion kernel works on the group before it (put:
+// copy, then convert into the state; take: convert out of the state, then
+// copy).  The host link bounds both (about 210 GB/s to the device and 190 GB/s
+// back on GB300, whatever the number of copy streams); the conversion kernel
+// reading or writing the mapped host FAB itself reached 88-91 % of that.  The
+// transfer stream starts after the work the legacy stream is ordered after.
+tmk_status valid_copy_pinned(tmk_level_s* L, LevelPatch& lp, const double* in, double* out,
+                             const tmk::CompList& cl) {
+  constexpr int kGroups = (int)(sizeof(L->xfer_ev) / sizeof(L->xfer_ev[0]));
+  if (!L->xfer) TMK_CU(cudaStreamCreateWithFlags(&L->xfer, cudaStreamNonBlocking));
+  for (cudaEvent_t& e : L->xfer_ev)
+    if (!e) TMK_CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  const int alo0 = lp.alloc.lo[0], alo1 = lp.alloc.lo[1];
+  const int anx = lp.alloc.hi[0] - alo0 + 1, any = lp.alloc.hi[1] - alo1 + 1;
+  const tmk_box& v = lp.valid;
+  const size_t pitch = (size_t)anx * sizeof(double);
+  const size_t width = (size_t)(v.hi[0] - v.lo[0] + 1) * sizeof(double);
+  const size_t rows = (size_t)(v.hi[1] - v.lo[1] + 1);
+  const size_t o0 = (size_t)(v.lo[1] - alo1) * anx + (v.lo[0] - alo0);
+  const int per = (cl.n + kGroups - 1) / kGroups;
+  TMK_CU(cudaEventRecord(L->xfer_ev[0], 0));
+  TMK_CU(cudaStreamWaitEvent(L->xfer, L->xfer_ev[0], 0));
+  for (int g = 0, k0 = 0; k0 < cl.n; ++g, k0 += per) {
+    tmk::CompList part{0, {}};
+    for (int k = k0; k < cl.n && k < k0 + per; ++k) part.c[part.n++] = cl.c[k];
+    if (in) {
+      // whole rows, ghost columns included, as one contiguous block per
+      // component (the staging buffer is scratch; strided copies ran slower)
+      for (int k = 0; k < part.n; ++k) {
+        const size_t o = (size_t)part.c[k] * anx * any + (size_t)(v.lo[1] - alo1) * anx;
+        TMK_CU(cudaMemcpyAsync(L->stage + o, in + o, rows * pitch, cudaMemcpyHostToDevice, L->xfer));
+      }
+      TMK_CU(cudaEventRecord(L->xfer_ev[g], L->xfer));
+      TMK_CU(cudaStreamWaitEvent(0, L->xfer_ev[g], 0));
+      TMK_CU(tmk::copy_valid_comps(L->stage, (float*)lp.U[L->parity], alo0, alo1, anx, any, v.lo[0], v.lo[1],
+                                   v.hi[0], v.hi[1], part, 0));
+    } else {
+      TMK_CU(tmk::copy_valid_comps((const float*)lp.U[L->parity], L->stage, alo0, alo1, anx, any, v.lo[0],
+                                   v.lo[1], v.hi[0], v.hi[1], part, 0));
+      TMK_CU(cudaEventRecord(L->xfer_ev[g], 0));
+      TMK_CU(cudaStreamWaitEvent(L->xfer, L->xfer_ev[g], 0));
+      for (int k = 0; k < part.n; ++k) {
+        const size_t o = (size_t)part.c[k] * anx * any + o0;
+        TMK_CU(cudaMemcpy2DAsync(out + o, pitch, L->stage + o, pitch, width, rows, cudaMemcpyDeviceToHost, L->xfer));
+      }
+    }
+  }
+  return TMK_OK;
+}
+
+// U of put/take.  Mixed form: a pinned host FAB moves through the staging
+// buffer by the copy engines (valid_copy_pinned), a device FAB is read or
+// written in place by the copy kernel, other host memory is staged through
+// the level's FP64 staging buffer whole.  FP64 form: one strided copy per
+// component.
 tmk_status valid_copy(tmk_level_s* L, int p, const double* in, double* out, bool host) {
   LevelPatch& lp = L->patches[p];
   const int alo0 = lp.alloc.lo[0], alo1 = lp.alloc.lo[1];
@@ -813,6 +869,8 @@ tmk_status valid_copy(tmk_level_s* L, int p, const double* in, double* out, bool
   const size_t count = (size_t)TMK_NCOMP * anx * any;
   const tmk_box& v = lp.valid;
   const tmk::CompList cl = step_comps(L);
+  if (L->prec == TMK_PREC_MIXED && host && mapped_host(in ? (const void*)in : (const void*)out))
+    return valid_copy_pinned(L, lp, in, out, cl);
   if (L->prec != TMK_PREC_MIXED) {
     const size_t pitch = (size_t)anx * sizeof(double);
     const size_t o0 = (size_t)(v.lo[1] - alo1) * anx + (v.lo[0] - alo0);

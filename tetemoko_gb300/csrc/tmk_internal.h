@@ -115,6 +115,10 @@ struct tmk_level_s {
   int* dbnx = nullptr;
   double* stage = nullptr;                 // FP64 staging for set/get of the mixed form
   size_t stage_count = 0;
+  // put/take of a pinned host FAB in the mixed form: the copy-engine stream
+  // and one event per group of components (created on first use)
+  cudaStream_t xfer = nullptr;
+  cudaEvent_t xfer_ev[6] = {};
   int parity = 0;
   double cur_dt = -1.0;
   std::vector<void*> allocs;
