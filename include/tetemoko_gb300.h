@@ -345,8 +345,8 @@ tmk_status tmk_level_get_patch(tmk_level* lvl, int patch, double* U, double* B,
  * 18 evolving components (9 per side; on a plastic level also lambda and
  * gamma of both sides) over the valid box, and the fault data B.  U and B are
  * laid out as for tmk_level_set_patch (ghost cells and the other components
- * are neither read nor written); `host` as there.  The counterpart of the
- * reference's step on FABs that live in host memory
+ * are not written and their values do not matter); `host` as there.  The
+ * counterpart of the reference's step on FABs that live in host memory
  * (LinElastLevelGodunov::step, srcLinElast/LinElastLevelGodunov.H:91-105, reads
  * the valid cells of U and writes them back): put before a step, take after
  * it.  The level must have been given a whole state once (tmk_level_set_patch)
