@@ -263,3 +263,56 @@ def test_oblique_wave_through_amr_on_the_gpu(cuda_lib, wave, r):
               f"FP64 {fp64[lvl]}, orders {orders}")
         assert np.all(orders > 1.8)
         np.testing.assert_allclose(mixed[1][lvl], fp64[lvl], rtol=0.05)
+
+
+def _gpu_fault_3d(sc, U, B, steps: int, dt: float, prec: int, t0: float = 0.0):
+    """Advance the cube (U, B) of test_oracle_waves.uniform_fault_3d on the GPU
+    by tmk_patch_update_state_3d (one patch); U and B updated in place."""
+    import torch
+    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    sc.scheme.precision = prec
+    ctx = Context(sc)
+    n, ny = sc.nx, sc.ny
+    box = ((0, 0, 0), (n - 1, ny - 1, n - 1))
+    pg = LinElastPatchGodunov3D(ctx, box)
+    pg.set_current_box(box)
+    Ud = torch.from_numpy(U).cuda()
+    Bd = torch.from_numpy(B).cuda()
+    for k in range(steps):
+        pg.set_current_time(t0 + k * dt)
+        pg.update_state(Ud, (-G, -G, -G), dt, B=Bd, blo=(-G, -G))
+    torch.cuda.synchronize()
+    U[:] = Ud.cpu().numpy()
+    B[:] = Bd.cpu().numpy()
+    ctx.close()
+
+
+@pytest.mark.parametrize("prec", [A.TMK_PREC_FP64, A.TMK_PREC_MIXED], ids=["fp64", "mixed"])
+def test_uniformly_sliding_faults_3d_on_the_gpu(cuda_lib, prec):
+    """The 3-D uniformly sliding faults of test_oracle_waves.py through the 3-D
+    patch step: slip weakening to 1e-12 (FP64) / 1e-5 (mixed) on the central
+    faces; rate and state against its ODE to 1e-6 / 1e-8 (FP64) and 1e-4 /
+    1e-5 (mixed) after 10, 20 and 30 steps."""
+    sc = W.uniform_sliding_scenario()
+    V, tau_d = W.uniform_sliding_answer(sc)
+    U, B = W.uniform_fault_3d(sc, 32, 16)
+    dt = sc.dt() / math.sqrt(3.0)
+    _gpu_fault_3d(sc, U, B, 12, dt, prec)
+    tol = 1e-12 if prec == A.TMK_PREC_FP64 else 1e-5
+    mid = (slice(G + 12, G + 20), slice(G + 12, G + 20))
+    for comp, want in ((4, V), (0, V), (2, tau_d), (5, V * 12 * dt), (7, V * 12 * dt)):
+        np.testing.assert_allclose(B[(comp,) + mid], want, rtol=tol, err_msg=f"component {comp}")
+
+    sc = W.uniform_rs_scenario()
+    U, B = W.uniform_fault_3d(sc, 48, 16)
+    dt = sc.dt() / math.sqrt(3.0)
+    V_ode, psi_ode = W.uniform_rs_answer(sc, 31 * dt)
+    tv, tp = (1e-6, 1e-8) if prec == A.TMK_PREC_FP64 else (1e-4, 1e-5)
+    c = G + 24
+    for k in range(3):
+        _gpu_fault_3d(sc, U, B, 10, dt, prec, t0=10 * k * dt)
+        t = 10 * (k + 1) * dt
+        V = V_ode(t - 0.5 * dt)
+        face = (slice(c - 3, c + 3), slice(c - 3, c + 3))
+        assert np.max(np.abs(B[(2,) + face] - V)) <= tv * V, (t, B[2, c, c], V)
+        assert np.max(np.abs(B[(10,) + face] - psi_ode(t))) <= tp, (t, B[10, c, c], psi_ode(t))
