@@ -663,7 +663,7 @@ def three_d_measurement(steps, warmup, stream, fp64_steps=3, cpu_seconds=5.0, si
     import torch
     import numpy as np
     from tetemoko_gb300 import _capi as A, scenarios as S
-    from tetemoko_gb300.level import Context, LinElastPatchGodunov3D
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov3D, LinElastPatchGodunov3D
     nx, ny, nz = size
     g = A.TMK_NGHOST
     lo, hi = (0, 0, 0), (nx - 1, ny - 1, nz - 1)
@@ -739,7 +739,19 @@ def three_d_measurement(steps, warmup, stream, fp64_steps=3, cpu_seconds=5.0, si
             pg.set_current_time(t)
             pg.update_states(patches, dt, stream=stream)
 
-        for name, fn in (("per_patch_calls", per_patch), ("batched", batched)):
+        # the device level over the same patches: its step exchanges the
+        # ghost cells on the device before the batched patch loop
+        lvl = LinElastLevelGodunov3D(ctx, [v for v, *_ in patches], (lo, hi))
+        for p, (v, U, ulo, B, blo) in enumerate(patches):
+            lvl.set_patch(p, U, B)
+
+        def level_step(t):
+            lvl.step(t, dt, stream)
+
+        def level_exchange(t):
+            lvl.exchange(stream)
+
+        def run(fn):
             t = 0.0
             for _ in range(warmup):
                 fn(t)
@@ -753,10 +765,17 @@ def three_d_measurement(steps, warmup, stream, fp64_steps=3, cpu_seconds=5.0, si
                 t += dt
             e1.record(stream)
             torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / steps
+            return e0.elapsed_time(e1) / steps
+
+        for name, fn in (("per_patch_calls", per_patch), ("batched", batched), ("level", level_step)):
+            ms = run(fn)
             tiles[name] = {"value": nx * ny * nz / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms}
+        tiles["level"]["exchange_ms"] = run(level_exchange)
+        tiles["level"]["note"] = ("tmk_level3d_step: the ghost exchange between the patches on the device, then the "
+                                  "batched patch loop")
         tiles["patches"] = len(patches)
-        tiles["patch"] = f"{tsz}^3 (ghost exchange left out: the caller's)"
+        tiles["patch"] = f"{tsz}^3 (per_patch_calls and batched: ghost exchange left out, the caller's)"
+        lvl.close()
         ctx.close()
     peaks = {}
     try:

@@ -175,6 +175,7 @@ typedef struct {
 
 typedef struct tmk_context_s tmk_context;
 typedef struct tmk_level_s   tmk_level;
+typedef struct tmk_level3d_s tmk_level3d;
 typedef struct tmk_amr_s     tmk_amr;
 typedef struct tmk_stations_s tmk_stations;
 typedef struct tmk_graph_s   tmk_graph;
@@ -298,6 +299,35 @@ tmk_status tmk_patches_update_state_3d(tmk_context* ctx, int npatch, const tmk_f
 /* LinElastPhysics::plasticUpdate -> PLASTICCORRECTION on a 3-D device FAB over box. */
 tmk_status tmk_plastic_update_3d(tmk_context* ctx, const tmk_fab3* U, const tmk_box3* box,
                                  double dt, void* stream);
+
+/* Device-resident level of a CH_SPACEDIM == 3 build (LinElastLevelGodunov::
+ * define/step/plasticUpdate, srcLinElast/LinElastLevelGodunov.cpp:45-398,
+ * 643-667, with 3-D boxes).  The level owns every patch's FP64 state FAB over
+ * its valid box grown by TMK_NGHOST (22 components) and, for the patches that
+ * start on the domain's y-lo plane when the scheme has a fault law, the fault
+ * data FAB over that box's x-z range on the plane (nbdry components; lo[1] =
+ * hi[1] = domain lo[1]).  The valid boxes must lie in the domain and must not
+ * overlap (TMK_ERR_BAD_DESC). */
+tmk_status tmk_level3d_create(tmk_context* ctx, const tmk_box3* domain, double dx, int npatch,
+                              const tmk_box3* patches, tmk_level3d** out);
+void       tmk_level3d_destroy(tmk_level3d* lvl);
+/* Copy one patch's whole FABs in / out (`host` as for tmk_level_set_patch;
+ * B is required on set for a fault patch, ignored for the others). */
+tmk_status tmk_level3d_set_patch(tmk_level3d* lvl, int patch, const double* U, const double* B,
+                                 int host);
+tmk_status tmk_level3d_get_patch(tmk_level3d* lvl, int patch, double* U, double* B, int host);
+/* The device FABs of one patch (B zeroed off the fault plane), for callers that
+ * read or write them in place on the level's stream. */
+tmk_status tmk_level3d_patch_fabs(const tmk_level3d* lvl, int patch, tmk_fab3* U, tmk_fab3* B);
+/* Same-level ghost exchange (LevelData::exchange): every ghost cell inside the
+ * domain that another patch's valid box covers takes that patch's value, all
+ * components; likewise the fault data's ghost faces on the plane. */
+tmk_status tmk_level3d_exchange(tmk_level3d* lvl, void* stream);
+/* One level step: the exchange, the patch loop as tmk_patches_update_state_3d
+ * (one launch per pass over every patch) and, when the scheme has plasticity,
+ * tmk_plastic_update_3d on every patch; the kernels are queued on `stream`. */
+tmk_status tmk_level3d_step(tmk_level3d* lvl, double time, double dt, double* max_wave_speed,
+                            void* stream);
 
 /* ---------------------------------------------------------------------------
  * Device-resident level (LinElastLevelGodunov::define/step/plasticUpdate,

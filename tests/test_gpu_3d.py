@@ -401,3 +401,111 @@ def test_mixed_3d_rupture_metrics_vs_fp64(cuda_lib):
     assert slip_err < 1e-3
     assert peak_err < 1e-2
     assert vel_err < 1e-2
+
+
+# The device 3-D level (tmk_level3d): its step (device ghost exchange, the
+# batched patch loop, the plastic correction on plastic schemes) over patches
+# tiling the domain, from ghosts set as any values, equals steps of one patch
+# over the whole domain.
+LEVEL_TILINGS = {
+    "regular": [((x0, y0, z0), (x0 + 5, y0 + 4, z0 + 3)) for z0 in (0, 4) for y0 in (0, 5) for x0 in (0, 6)],
+    "uneven": [((0, 0, 0), (4, 9, 7)), ((5, 0, 0), (11, 2, 7)), ((5, 3, 0), (11, 9, 2)), ((5, 3, 3), (11, 9, 7))],
+}
+
+
+def _level3d_vs_whole(sc, tiles, prec, nsteps, amp_s=5.0):
+    """(whole-domain U, B; level U, B per patch) after nsteps from one perturbed
+    state; the level's patches start with their ghost cells set to NaN, which
+    the exchange must overwrite inside the domain (the step reads no ghost
+    outside it)."""
+    import torch
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov3D, LinElastPatchGodunov3D
+    rng = np.random.default_rng(123)
+    lo, hi = DOM
+    U0 = perturbed_state_3d(sc, rng, lo, hi, amp_s=amp_s)
+    fault = sc.scheme.fault_law != A.TMK_FAULT_NONE
+    B0 = random_B_3d(sc, rng, NX + 2 * G, NZ + 2 * G) if fault else None
+    old = sc.scheme.precision
+    sc.scheme.precision = prec
+    try:
+        ctx = Context(sc)
+    finally:
+        sc.scheme.precision = old
+    dt, t0 = sc.dt() / 3 ** 0.5, 0.5
+    pg = LinElastPatchGodunov3D(ctx, DOM)
+    pg.set_current_box(DOM)
+    Uw = torch.from_numpy(U0.copy()).cuda()
+    Bw = torch.from_numpy(B0.copy()).cuda() if fault else None
+    for k in range(nsteps):
+        pg.set_current_time(t0 + k * dt)
+        pg.update_state(Uw, (-G, -G, -G), dt, B=Bw, blo=(-G, -G))
+        if sc.scheme.plasticity:
+            pg.plastic_update(Uw, (-G, -G, -G), dt, box=DOM)
+    lvl = LinElastLevelGodunov3D(ctx, tiles, DOM)
+    for p, ((l0, l1, l2), (h0, h1, h2)) in enumerate(tiles):
+        U = np.full(lvl.patch_shapes(p)[0], np.nan)
+        U[:, G:-G, G:-G, G:-G] = U0[:, l2 + G:h2 + G + 1, l1 + G:h1 + G + 1, l0 + G:h0 + G + 1]
+        B = None
+        if lvl.touches_fault(p):
+            B = np.full(lvl.patch_shapes(p)[1], np.nan)
+            B[:, G:-G, G:-G] = B0[:, l2 + G:h2 + G + 1, l0 + G:h0 + G + 1]
+        lvl.set_patch(p, U, B)
+    for k in range(nsteps):
+        lvl.step(t0 + k * dt, dt)
+    got = [lvl.get_patch(p) for p in range(len(tiles))]
+    torch.cuda.synchronize()
+    out = (Uw.cpu().numpy(), Bw.cpu().numpy() if fault else None, got)
+    lvl.close()
+    ctx.close()
+    return out
+
+
+@pytest.mark.parametrize("name", ["rs_aging", "sw_off11", "no_fault"])
+@pytest.mark.parametrize("tiling", list(LEVEL_TILINGS))
+@pytest.mark.parametrize("prec", [A.TMK_PREC_FP64, A.TMK_PREC_MIXED], ids=["fp64", "mixed"])
+def test_level3d_steps_equal_whole_domain_steps(cuda_lib, name, tiling, prec):
+    """Three level steps: the FP64 form bit for bit; the mixed form to 1e-10
+    (its boundary-data update may contract a product differently in the
+    single-patch and batched kernels, and the fault data feed the state)."""
+    sc = dict(SCEN)[name]
+    tiles = LEVEL_TILINGS[tiling]
+    Uw, Bw, got = _level3d_vs_whole(sc, tiles, prec, 3)
+    for ((l0, l1, l2), (h0, h1, h2)), (U, B) in zip(tiles, got):
+        a = U[:, G:-G, G:-G, G:-G]
+        ref = Uw[:, l2 + G:h2 + G + 1, l1 + G:h1 + G + 1, l0 + G:h0 + G + 1]
+        if prec == A.TMK_PREC_FP64:
+            np.testing.assert_array_equal(a, ref)
+        else:
+            assert rel_err(a, ref) <= 1e-10
+        if B is not None:
+            b, bref = B[:, G:-G, G:-G], Bw[:, l2 + G:h2 + G + 1, l0 + G:h0 + G + 1]
+            if prec == A.TMK_PREC_FP64:
+                np.testing.assert_array_equal(b, bref)
+            else:
+                assert rel_err(b, bref) <= 1e-10
+
+
+def test_level3d_plastic_steps_equal_whole_domain_steps(cuda_lib):
+    """A plastic slip-weakening level (stresses large enough to yield): the
+    level applies the plastic correction after each step, as one patch over
+    the whole domain does (FP64, bit for bit)."""
+    sc = S.slip_weakening(nx=NX, ny=NY, dx=DX, plasticity=True)
+    tiles = LEVEL_TILINGS["uneven"]
+    Uw, Bw, got = _level3d_vs_whole(sc, tiles, A.TMK_PREC_FP64, 3, amp_s=60.0)
+    yielded = 0
+    for ((l0, l1, l2), (h0, h1, h2)), (U, B) in zip(tiles, got):
+        ref = Uw[:, l2 + G:h2 + G + 1, l1 + G:h1 + G + 1, l0 + G:h0 + G + 1]
+        np.testing.assert_array_equal(U[:, G:-G, G:-G, G:-G], ref)
+        yielded += int(np.count_nonzero(ref[9]))
+    assert yielded > 0, "no cell yielded: the plastic correction was not exercised"
+
+
+def test_level3d_rejects_overlapping_or_outside_boxes(cuda_lib):
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov3D
+    sc = dict(SCEN)["rs_aging"]
+    ctx = Context(sc)
+    for boxes in ([((0, 0, 0), (6, 9, 7)), ((6, 0, 0), (11, 9, 7))],       # overlap at x = 6
+                  [((0, 0, 0), (12, 9, 7))]):                               # beyond the domain in x
+        with pytest.raises(RuntimeError):
+            LinElastLevelGodunov3D(ctx, boxes, DOM)
+    ctx.close()

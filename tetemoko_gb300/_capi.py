@@ -177,6 +177,14 @@ def lib() -> C.CDLL:
     L.tmk_plastic_update_3d.argtypes = [vp, F3, C.POINTER(Box3), C.c_double, vp]
     L.tmk_patches_update_state_3d.argtypes = [vp, C.c_int, F3, F3, F3, F3, F3, C.POINTER(Box3), C.POINTER(Box3),
                                               C.c_double, C.c_double, C.c_double, dp, vp]
+    L.tmk_level3d_create.argtypes = [vp, C.POINTER(Box3), C.c_double, C.c_int, C.POINTER(Box3), C.POINTER(vp)]
+    L.tmk_level3d_destroy.argtypes = [vp]
+    L.tmk_level3d_destroy.restype = None
+    L.tmk_level3d_set_patch.argtypes = [vp, C.c_int, vp, vp, C.c_int]
+    L.tmk_level3d_get_patch.argtypes = [vp, C.c_int, vp, vp, C.c_int]
+    L.tmk_level3d_patch_fabs.argtypes = [vp, C.c_int, F3, F3]
+    L.tmk_level3d_exchange.argtypes = [vp, vp]
+    L.tmk_level3d_step.argtypes = [vp, C.c_double, C.c_double, dp, vp]
     L.tmk_level_create.argtypes = [vp, C.POINTER(Box), C.c_double, C.c_int, C.POINTER(Box), C.POINTER(vp)]
     L.tmk_level_destroy.argtypes = [vp]
     L.tmk_level_get_tuning.argtypes = [vp, C.POINTER(Tuning)]

@@ -1,6 +1,6 @@
 """In-tree build of libtetemoko_gb300.so for sm_103a with nvcc.
 
-Eight translation units, compiled in parallel:
+Nine translation units, compiled in parallel:
   tmk_fp64.cu  plain FP64 kernels, --fmad=false (parity with the CPU oracle)
   tmk_fp32.cu  mixed-form kernels (FP32 volume, FP64 friction)
   tmk_capi.cu  the C ABI (host code)
@@ -9,6 +9,7 @@ Eight translation units, compiled in parallel:
   tmk_regrid.cu  refinement tagging, --fmad=false
   tmk_3d.cu    the 3-D patch step (CH_SPACEDIM == 3), FP64 form, --fmad=false
   tmk_3d_f32.cu  its mixed form (FP32 volume arithmetic)
+  tmk_level3d.cu  the 3-D device level (ghost exchange, batched step)
 """
 from __future__ import annotations
 
@@ -34,6 +35,7 @@ UNITS = {
     "tmk_regrid.cu": ["--fmad=false"],
     "tmk_3d.cu": ["--fmad=false"],
     "tmk_3d_f32.cu": [],
+    "tmk_level3d.cu": [],
 }
 
 

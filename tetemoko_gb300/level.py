@@ -224,6 +224,72 @@ class LinElastPatchGodunov3D:
                                                    _stream_ptr(stream)), "tmk_plastic_update_3d")
 
 
+class LinElastLevelGodunov3D:
+    """Device-resident level of a CH_SPACEDIM == 3 build (tmk_level3d): the
+    level owns each patch's FP64 state FAB (22, nz+8, ny+8, nx+8) over the
+    valid box grown by 4 ghosts and, on the fault plane, its fault data
+    (nbdry, nz+8, nx+8); a step exchanges ghost cells on the device and runs
+    the batched 3-D patch loop (and the plastic correction on plastic
+    schemes).  Boxes are ((lo0, lo1, lo2), (hi0, hi1, hi2))."""
+
+    def __init__(self, ctx: Context, boxes, domain, dx: float | None = None):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.boxes = [(tuple(b[0]), tuple(b[1])) for b in boxes]
+        self.domain = (tuple(domain[0]), tuple(domain[1]))
+        self.dx = ctx.sc.dx if dx is None else dx
+        arr = (A.Box3 * len(self.boxes))(*[A.box3(*b) for b in self.boxes])
+        h = C.c_void_p()
+        A.check(self.lib.tmk_level3d_create(ctx.h, C.byref(A.box3(*self.domain)), self.dx, len(self.boxes), arr,
+                                            C.byref(h)), "tmk_level3d_create")
+        self.h = h
+
+    def touches_fault(self, p) -> bool:
+        return self.ctx.sc.scheme.fault_law != A.TMK_FAULT_NONE and self.boxes[p][0][1] == self.domain[0][1]
+
+    def patch_shapes(self, p):
+        (lo, hi), g = self.boxes[p], A.TMK_NGHOST
+        n = [hi[d] - lo[d] + 1 + 2 * g for d in range(3)]
+        return (22, n[2], n[1], n[0]), (self.ctx.sc.nbdry, n[2], n[0])
+
+    def set_patch(self, p, U, B=None):
+        """U (and B on the fault plane): numpy arrays (host) or CUDA tensors
+        (device) of patch_shapes(p)."""
+        host = isinstance(U, np.ndarray)
+        if host:
+            U = np.ascontiguousarray(U, dtype=np.float64)
+            B = np.ascontiguousarray(B, dtype=np.float64) if B is not None else None
+        ptr = (lambda x: x.ctypes.data) if host else (lambda x: x.data_ptr())
+        A.check(self.lib.tmk_level3d_set_patch(self.h, p, ptr(U), ptr(B) if B is not None else None, int(host)),
+                "tmk_level3d_set_patch")
+
+    def get_patch(self, p, U=None, B=None):
+        """Copy out one patch (into numpy arrays allocated here if not given)."""
+        ushape, bshape = self.patch_shapes(p)
+        if U is None:
+            U = np.empty(ushape)
+        if B is None and self.touches_fault(p):
+            B = np.empty(bshape)
+        host = isinstance(U, np.ndarray)
+        ptr = (lambda x: x.ctypes.data) if host else (lambda x: x.data_ptr())
+        A.check(self.lib.tmk_level3d_get_patch(self.h, p, ptr(U), ptr(B) if B is not None else None, int(host)),
+                "tmk_level3d_get_patch")
+        return U, B
+
+    def exchange(self, stream=None):
+        A.check(self.lib.tmk_level3d_exchange(self.h, _stream_ptr(stream)), "tmk_level3d_exchange")
+
+    def step(self, t: float, dt: float, stream=None) -> float:
+        mws = C.c_double(0.0)
+        A.check(self.lib.tmk_level3d_step(self.h, t, dt, C.byref(mws), _stream_ptr(stream)), "tmk_level3d_step")
+        return mws.value
+
+    def close(self):
+        if self.h:
+            self.lib.tmk_level3d_destroy(self.h)
+            self.h = None
+
+
 class LinElastLevelGodunov:
     """Device-resident single level (all patches of the level in one launch)."""
 
