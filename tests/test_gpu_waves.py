@@ -316,3 +316,44 @@ def test_uniformly_sliding_faults_3d_on_the_gpu(cuda_lib, prec):
         face = (slice(c - 3, c + 3), slice(c - 3, c + 3))
         assert np.max(np.abs(B[(2,) + face] - V)) <= tv * V, (t, B[2, c, c], V)
         assert np.max(np.abs(B[(10,) + face] - psi_ode(t))) <= tp, (t, B[10, c, c], psi_ode(t))
+
+
+@pytest.mark.parametrize("prec", [A.TMK_PREC_FP64, A.TMK_PREC_MIXED], ids=["fp64", "mixed"])
+def test_slip_law_fault_on_the_gpu_converges_at_first_order(cuda_lib, prec):
+    """The reference's slip law on the uniformly sliding fault through a GPU
+    level of three patches.  FP64 form: first order in dt (dt, dt/2, dt/4)
+    with the oracle's errors to 1e-6 of themselves.  Mixed form, at dt and
+    dt/2: slip-rate and state errors within 15 % of the oracle's.  (At dt/4,
+    Courant number 0.225, the mixed form's slip rate departs from the FP64
+    form's by 1e-3 after 160 steps: five rows from the fault the outgoing
+    wave's second differences, ~1e-5 MPa, are an FP32 ulp of the 70 MPa
+    shear stress; the reference's decks and the AMR levels step at 0.9.)"""
+    import oracle as O
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+
+    def steps(sc, U, B, n, dt):
+        sc.scheme.precision = prec
+        ctx = Context(sc)
+        lvl = LinElastLevelGodunov(ctx, [(0, 0, 63, 31), (64, 0, 127, 31), (0, 32, 127, 63)])
+        lvl.set_level(U, B)
+        for k in range(n):
+            lvl.step(k * dt, dt)
+        lvl.get_level(U, B)
+        assert lvl.status()[0] == 0
+        lvl.close()
+        ctx.close()
+
+    def oracle_steps(sc, U, B, n, dt):
+        for k in range(n):
+            assert O.level_step(sc, U, B, O.tile_boxes(sc.nx, sc.ny, 64), k * dt, dt, nthreads=8) == 0
+
+    ks = (1, 2, 4) if prec == A.TMK_PREC_FP64 else (1, 2)
+    e = W.slip_law_errors(steps, ks)
+    ref = W.slip_law_errors(oracle_steps, ks)
+    print("slip law on the GPU: errors", e.tolist(), "oracle", ref.tolist())
+    if prec == A.TMK_PREC_FP64:
+        orders = np.log2(np.abs(e[:-1] / e[1:]))
+        assert np.all(np.abs(orders - 1.0) < 0.1)
+        np.testing.assert_allclose(e, ref, rtol=1e-6)
+    else:
+        np.testing.assert_allclose(e, ref, rtol=0.15)

@@ -153,12 +153,13 @@ def test_uniformly_sliding_fault_radiates_at_the_exact_slip_rate():
     np.testing.assert_allclose(U[6, G, mid], tau_d, atol=0.01 * (sc.elastic.sxy0 - tau_d))
 
 
-def uniform_rs_scenario(prec=A.TMK_PREC_FP64):
-    """A rate-and-state fault (aging law, velocity strengthening a=0.012,
-    b=0.008, L=0.2 m, no nucleation) in steady sliding at 0.5 m/s whose shear
-    load is then 2 MPa above that state's: every face speeds up and relaxes
-    together, the 1-D problem of a uniformly sliding fault."""
-    sc = S.rate_state(nx=128, ny=64, dx=0.05, precision=prec)
+def uniform_rs_scenario(prec=A.TMK_PREC_FP64, law=A.TMK_RS_AGING_LAW):
+    """A rate-and-state fault (aging law, or the reference's slip law;
+    velocity strengthening a=0.012, b=0.008, L=0.2 m, no nucleation) in steady
+    sliding at 0.5 m/s whose shear load is then 2 MPa above that state's:
+    every face speeds up and relaxes together, the 1-D problem of a uniformly
+    sliding fault.  Both laws share the steady state."""
+    sc = S.rate_state(nx=128, ny=64, dx=0.05, precision=prec, state_law=law)
     rs = sc.rs
     rs.nsig = 0.0
     rs.a, rs.b, rs.L = 0.012, 0.008, 0.2
@@ -173,8 +174,9 @@ def uniform_rs_scenario(prec=A.TMK_PREC_FP64):
 
 def uniform_rs_answer(sc, t_end):
     """The 1-D problem's exact evolution: the traction is tau0 - (Zs/2) V
-    (radiation damping) = sn a asinh(V e^(psi/a) / (2 V0)), and the aging law
-    d psi/dt = (b/L) (V0 e^(-(psi - f0)/b) - V), integrated to 1e-12.
+    (radiation damping) = sn a asinh(V e^(psi/a) / (2 V0)) = sn f, and the
+    aging law d psi/dt = (b/L) (V0 e^(-(psi - f0)/b) - V) or the slip law
+    d psi/dt = -(V/L) (f - f0 + (b - a) ln(V/V0)), integrated to 1e-12.
     Returns (V(t), psi(t))."""
     from scipy.integrate import solve_ivp
     from scipy.optimize import brentq
@@ -188,7 +190,11 @@ def uniform_rs_answer(sc, t_end):
         return brentq(f, 0.0, 2.0 * tau0 / Zs, xtol=1e-15, rtol=1e-15)
 
     def rhs(t, y):
-        return [rs.b / rs.L * (rs.V0 * math.exp(-(y[0] - rs.f0) / rs.b) - V_of(y[0]))]
+        V = V_of(y[0])
+        if rs.state_law == A.TMK_RS_SLIP_LAW:
+            f = rs.a * math.asinh(V / (2 * rs.V0) * math.exp(y[0] / rs.a))
+            return [-(V / rs.L) * (f - rs.f0 + (rs.b - rs.a) * math.log(V / rs.V0))]
+        return [rs.b / rs.L * (rs.V0 * math.exp(-(y[0] - rs.f0) / rs.b) - V)]
 
     sol = solve_ivp(rhs, (0.0, t_end), [rs.psi_init], rtol=1e-12, atol=1e-14, dense_output=True, method="DOP853")
     return (lambda t: V_of(float(sol.sol(t)[0]))), (lambda t: float(sol.sol(t)[0]))
@@ -216,6 +222,40 @@ def test_uniformly_sliding_rate_and_state_fault_follows_its_ode():
         np.testing.assert_allclose(B[2, c - 4:c + 4], B[2, c], rtol=1e-7)      # uniform along the fault
         Vs.append(B[2, c])
     assert Vs[-1] / Vs[0] > 1.05
+
+
+def slip_law_errors(level_steps, ks=(1, 2, 4), nbase: int = 40):
+    """The slip-law fault of uniform_rs_scenario stepped nbase * k times by
+    dt / k with level_steps(sc, U, B, n, dt) (the state updated in place):
+    per k, the relative error of the slip rate (component 2) against the ODE
+    at the last step's midpoint and the error of the state (10) at its end."""
+    out = []
+    for k in ks:
+        sc = uniform_rs_scenario(law=A.TMK_RS_SLIP_LAW)
+        U, B = sc.initial_U(), sc.initial_B()
+        dt = sc.dt() / k
+        n = nbase * k
+        V_ode, psi_ode = uniform_rs_answer(sc, (n + 1) * dt)
+        level_steps(sc, U, B, n, dt)
+        c = G + sc.nx // 2
+        t = n * dt
+        out.append((B[2, c] / V_ode(t - 0.5 * dt) - 1.0, B[10, c] - psi_ode(t)))
+    return np.array(out)
+
+
+def test_uniformly_sliding_slip_law_fault_converges_at_first_order():
+    """The reference's slip law (ibcLinElast/RSIBCF.ChF:127-132) advances the
+    state by one explicit step psi -= dt (V/L)(f - fss): the uniformly sliding
+    fault reaches its ODE at first order in dt (40, 80, 160 steps of dt, dt/2,
+    dt/4 over the same time: slip-rate and state errors halve with dt)."""
+    def steps(sc, U, B, n, dt):
+        for k in range(n):
+            assert O.level_step(sc, U, B, O.tile_boxes(sc.nx, sc.ny, 64), k * dt, dt, nthreads=4) == 0
+    e = slip_law_errors(steps)
+    orders = np.log2(np.abs(e[:-1] / e[1:]))
+    print("slip law: errors (V, psi)", e.tolist(), "orders", orders.tolist())
+    assert np.all(np.abs(orders - 1.0) < 0.1)
+    assert abs(e[-1, 0]) < 2e-4 and abs(e[-1, 1]) < 1e-5
 
 
 # Oblique plane waves: the pulse travels along n = (cos th, sin th), so every
