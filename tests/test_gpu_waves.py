@@ -325,9 +325,11 @@ def test_slip_law_fault_on_the_gpu_converges_at_first_order(cuda_lib, prec):
     with the oracle's errors to 1e-6 of themselves.  Mixed form, at dt and
     dt/2: slip-rate and state errors within 15 % of the oracle's.  (At dt/4,
     Courant number 0.225, the mixed form's slip rate departs from the FP64
-    form's by 1e-3 after 160 steps: five rows from the fault the outgoing
-    wave's second differences, ~1e-5 MPa, are an FP32 ulp of the 70 MPa
-    shear stress; the reference's decks and the AMR levels step at 0.9.)"""
+    form's by 1e-3 after 160 steps: at that Courant number the scheme
+    amplifies rounding differences about a million-fold in ~100 steps -- the
+    two FP64 volume kernels, equal to 1e-14 at first, differ by 3e-8 by then
+    -- and FP32 rounding starts 1e8 times larger; the reference's decks and
+    the AMR levels step at 0.9.)"""
     import oracle as O
     from tetemoko_gb300.level import Context, LinElastLevelGodunov
 
