@@ -88,5 +88,17 @@ def test_null_handles_are_rejected(cuda_lib):
                                               None) == 1
     out = (C.c_double * 5)()
     assert lib.tmk_context_constants(None, out) == 1
+    # the 3-D level: no context, no handle
+    dom = A.box3((0, 0, 0), (7, 7, 7))
+    boxes = (A.Box3 * 1)(A.box3((0, 0, 0), (7, 7, 7)))
+    h = C.c_void_p()
+    assert lib.tmk_level3d_create(None, C.byref(dom), 0.1, 1, boxes, C.byref(h)) == 1
+    assert not h.value
+    assert lib.tmk_level3d_step(None, 0.0, 0.1, None, None) == 1
+    assert lib.tmk_level3d_exchange(None, None) == 1
+    assert lib.tmk_level3d_set_patch(None, 0, None, None, 1) == 1
+    assert lib.tmk_level3d_get_patch(None, 0, None, None, 1) == 1
+    assert lib.tmk_level3d_patch_fabs(None, 0, None, None) == 1
     lib.tmk_context_destroy(None)
     lib.tmk_level_destroy(None)
+    lib.tmk_level3d_destroy(None)
