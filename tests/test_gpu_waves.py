@@ -359,3 +359,50 @@ def test_slip_law_fault_on_the_gpu_converges_at_first_order(cuda_lib, prec):
         np.testing.assert_allclose(e, ref, rtol=1e-6)
     else:
         np.testing.assert_allclose(e, ref, rtol=0.15)
+
+
+def _gpu_edge(n: int, free: bool, prec: int):
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    from oracle import tile_boxes
+    sc = W.edge_scenario(n, free)
+    sc.scheme.precision = prec
+    U = W.edge_state(sc, free, 0.0)
+    steps = int(math.ceil(W.EDGE_TRAVEL / (sc.elastic.cp * sc.dt())))
+    dt = W.EDGE_TRAVEL / (sc.elastic.cp * steps)
+    ctx = Context(sc)
+    lvl = LinElastLevelGodunov(ctx, tile_boxes(sc.nx, sc.ny, 64))
+    lvl.set_level(U, None)
+    for k in range(steps):
+        lvl.step(k * dt, dt)
+    lvl.get_level(U, None)
+    assert lvl.status()[0] == 0
+    lvl.close()
+    ctx.close()
+    exact = W.edge_state(sc, free, steps * dt)
+    j = G + sc.ny // 2
+    err = np.array([np.sum(np.abs(U[q, j, G:-G] - exact[q, j, G:-G])) * sc.dx / (W.AMP * W.WIDTH) for q in (0, 3, 4)])
+    return U, err, sc, steps, dt
+
+
+@pytest.mark.parametrize("free", [True, False], ids=["free_surface", "absorbing"])
+def test_pulse_at_a_domain_edge_on_the_gpu(cuda_lib, free):
+    """The FP64 form equals the oracle's level steps at n = 128 (1e-11
+    relative per component).  With the free surface the mixed form's vx and
+    sxx converge at the oracle's order, within 5 % of the FP64 form's errors
+    at n = 256; its syy carries the -120 MPa background in FP32 (an ulp of
+    7.6e-6 MPa per cell), a rounding floor near this grid's truncation error,
+    so it is held to 30 %."""
+    import oracle as O
+    U64, _, sc, steps, dt = _gpu_edge(128, free, A.TMK_PREC_FP64)
+    Ur = W.edge_state(sc, free, 0.0)
+    for k in range(steps):
+        assert O.level_step(sc, Ur, None, O.tile_boxes(sc.nx, sc.ny, 64), k * dt, dt, nthreads=8) == 0
+    v = (slice(None), slice(G, -G), slice(G, -G))
+    assert rel_err(U64[v], Ur[v]) <= 1e-11
+    if free:
+        mixed = [_gpu_edge(n, True, A.TMK_PREC_MIXED)[1] for n in (128, 256)]
+        fp64 = _gpu_edge(256, True, A.TMK_PREC_FP64)[1]
+        print("free surface: mixed errors", mixed[1], "FP64", fp64)
+        assert np.all(np.log2(mixed[0][:2] / mixed[1][:2]) > 1.8)
+        np.testing.assert_allclose(mixed[1][:2], fp64[:2], rtol=0.05)
+        np.testing.assert_allclose(mixed[1][2], fp64[2], rtol=0.3)

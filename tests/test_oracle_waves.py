@@ -109,6 +109,71 @@ def test_plane_wave_converges_at_second_order(along, wave):
     assert orders[1] > 1.6
 
 
+# A P pulse meeting the x-hi domain edge head-on: a free surface (zero
+# traction) reflects it with the stress reversed, sigma_xx = f(x - ct) -
+# f(2X - x - ct), v_x = -(f(x - ct) + f(2X - x - ct)) / Zp (no mode conversion
+# at normal incidence); an absorbing edge lets it leave, sigma_xx =
+# f(x - ct).  The pulse starts 1.5 km from the edge and travels 3 km; the
+# side edges are 4.5 km from the compared row (beyond cp t + the stencil's
+# spread).
+EDGE_TRAVEL = 3.0      # km
+EDGE_SIDE = 9.0        # km
+
+
+def edge_scenario(n: int, free: bool):
+    """No background shear: a free surface would release it as an S wave."""
+    dx = LEN / n
+    e = S._elastic()
+    e.sxy0 = 0.0
+    return S.Scenario(name="edge_wave", nx=n, ny=int(round(EDGE_SIDE / dx)), dx=dx, cfl=0.9, elastic=e,
+                      scheme=S._scheme(A.TMK_FAULT_NONE, bc=(0, 1 if free else 0, 0, 0, 0, 0)))
+
+
+def edge_state(sc, free: bool, t: float) -> np.ndarray:
+    c = sc.constants()
+    U = sc.initial_U()
+    xs = (np.arange(sc.nx + 2 * G) - G + 0.5) * sc.dx
+    X = xs[None, :] * np.ones_like(U[0])
+    x0 = LEN - EDGE_TRAVEL / 2
+    f_in = _pulse(X - x0 - sc.elastic.cp * t)
+    f_re = -_pulse(2 * LEN - X - x0 - sc.elastic.cp * t) if free else 0.0 * X
+    r = c["lam"] / (c["lam"] + 2.0 * c["G"])
+    for side in (0, 11):
+        U[side + 3] += f_in + f_re
+        U[side + 0] += (-f_in + f_re) / c["Zp"]
+        U[side + 4] += r * (f_in + f_re)
+        U[side + 5] += r * (f_in + f_re)
+    return U
+
+
+@pytest.mark.parametrize("free", [True, False], ids=["free_surface", "absorbing"])
+def test_pulse_at_a_domain_edge_converges_at_second_order(free):
+    """vx, sxx, syy along the middle row converge to the reflected (free
+    surface) or departed (absorbing) pulse at order 1.9-2.5 from 64 to 256
+    cells; there syy - r sxx, the zero-speed characteristic of x, stays as it
+    was to rounding."""
+    errs = []
+    for n in (64, 128, 256):
+        sc = edge_scenario(n, free)
+        U = edge_state(sc, free, 0.0)
+        c = sc.constants()
+        r = c["lam"] / (c["lam"] + 2.0 * c["G"])
+        w0 = U[4] - r * U[3]
+        steps = int(math.ceil(EDGE_TRAVEL / (sc.elastic.cp * sc.dt())))
+        dt = EDGE_TRAVEL / (sc.elastic.cp * steps)
+        for k in range(steps):
+            assert O.level_step(sc, U, None, O.tile_boxes(sc.nx, sc.ny, 64), k * dt, dt, nthreads=4) == 0
+        exact = edge_state(sc, free, steps * dt)
+        j = G + sc.ny // 2
+        errs.append(np.array([np.sum(np.abs(U[q, j, G:-G] - exact[q, j, G:-G])) * sc.dx / (AMP * WIDTH)
+                              for q in (0, 3, 4)]))
+        assert np.max(np.abs((U[4] - r * U[3] - w0)[j, G:-G])) < 1e-12
+    orders = np.log2(errs[1] / errs[2])
+    print(f"{'free surface' if free else 'absorbing'}: errors at 256 {errs[2]}, orders {orders}")
+    assert np.all(errs[2] < 2e-3)
+    assert np.all(orders > 1.8)
+
+
 def uniform_sliding_scenario(prec=A.TMK_PREC_FP64):
     """A slip-weakening fault loaded above its static strength everywhere
     (tau0 = 81.6 MPa > mu_s sigma_n = 81.24 MPa, no nucleation patch) with an
