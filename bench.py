@@ -1148,12 +1148,6 @@ def main():
                             "tmk_level_take_valid (the same, device->host)"},
             "gpu_launches": launches,
             "clocks": clocks,
-            # the two forms and the mixed form's errors first: the sub-measurements after them are long
-            "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_step": ms64 / n64, "steps": n64,
-                           "volume_kernel": args.fp64_kernel, "volume_kernel_ms": vol64,
-                           "volume_hbm_gbs": BYTES_PER_CELL_FP64 * cells / (vol64 * 1e-3) / 1e9},
-            "mixed_over_fp64": value / value64,
-            "errors": errors,
             "execution": (f"steps replayed from a CUDA graph of {graph_steps} recorded level steps "
                           "(tmk_level_graph_create / tmk_graph_launch)") if graph_steps else "one call per step",
             "tuning": {"autotuned": bool(args.autotune), "choice": tuning, "trial_ms_per_step": tune_ms},
@@ -1164,7 +1158,14 @@ def main():
             "amr3": amr3,
             "ensemble": ens,
             "three_d": three_d,
+            # the two forms side by side and the mixed form's errors last, where
+            # the end of a truncated log still shows them
             "device_status": {"mixed": st[1], "fp64": st64[1]},
+            "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_step": ms64 / n64, "steps": n64,
+                           "volume_kernel": args.fp64_kernel, "volume_kernel_ms": vol64,
+                           "volume_hbm_gbs": BYTES_PER_CELL_FP64 * cells / (vol64 * 1e-3) / 1e9},
+            "mixed_over_fp64": value / value64,
+            "errors": errors,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
