@@ -14,7 +14,8 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 
 
 def declared_functions():
-    src = open(HEADER).read()
+    with open(HEADER) as f:
+        src = f.read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(tmk_[a-z0-9_]+)\s*\(", src)))
 
