@@ -7,9 +7,13 @@ patch/level call order; its header lists the files it follows.
 
 Parity status: the reference kernels themselves (srcLinElast/*.ChF,
 ibcLinElast/*.ChF) cannot be compiled here (no Fortran compiler, no Chombo),
-and the reference ships no tests or golden vectors, so this restatement is
-pinned only by known-answer properties of the reference formulas
-(tests/test_oracle_kat.py) -- parity unpinned.
+and the reference ships no tests or golden vectors, so parity with the
+reference is unpinned.  The restatement is pinned instead by known-answer
+properties of the reference formulas (tests/test_oracle_kat.py) and by exact
+solutions of the equations it discretises (tests/test_oracle_waves.py: plane
+waves in 2-D and 3-D, also through a refined hierarchy and at free and
+absorbing edges, converging at the scheme's order; uniformly sliding
+slip-weakening and rate-and-state faults meeting their 1-D answers).
 """
 from __future__ import annotations
 

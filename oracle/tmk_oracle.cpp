@@ -17,6 +17,9 @@
 // (Colella & Woodward 1984, J. Comput. Phys. 54:174) and the Chombo design
 // description of the unsplit Godunov integrator.  Parity against Chombo itself
 // is therefore UNPINNED: no reference test or golden vector fixes those stages.
+// The tests pin the restatement instead to exact solutions of the equations
+// (plane waves converging at the scheme's order, uniformly sliding faults
+// meeting their 1-D answers) and to known-answer properties of each formula.
 //
 // Where the reference reads memory it never initialised (face states the
 // slip-weakening law leaves unwritten, slip-weakening boundary components 7
