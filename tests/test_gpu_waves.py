@@ -406,3 +406,42 @@ def test_pulse_at_a_domain_edge_on_the_gpu(cuda_lib, free):
         assert np.all(np.log2(mixed[0][:2] / mixed[1][:2]) > 1.8)
         np.testing.assert_allclose(mixed[1][:2], fp64[:2], rtol=0.05)
         np.testing.assert_allclose(mixed[1][2], fp64[2], rtol=0.3)
+
+
+@pytest.mark.parametrize("prec,fused", [(A.TMK_PREC_FP64, 0), (A.TMK_PREC_FP64, 1), (A.TMK_PREC_MIXED, 0)],
+                         ids=["fp64_pass", "fp64_fused", "mixed_pass"])
+def test_viscoplastic_relaxation_on_the_gpu(cuda_lib, prec, fused):
+    """The uniform over-stressed state of test_oracle_waves.py through 16 GPU
+    level steps, with the Drucker-Prager return as a pass after the marching
+    kernels or fused into the in-plane kernel's stores: the overstress equals
+    the backward-Euler closed form to 1e-12 of Y0 (FP64) or 1e-6 of Y0 (mixed:
+    FP32 stresses of 120 MPa), and the plastic strain (Y0 - Y)/k likewise."""
+    from tetemoko_gb300.level import Context, LinElastLevelGodunov
+    sc = W.plastic_scenario(h=5.0)
+    sc.scheme.precision = prec
+    sc.scheme.volume_kernel = A.TMK_VOLUME_MARCH
+    k = W.plastic_k(sc)
+    eta = sc.plastic.eta
+    U = sc.initial_U()
+    c = G + 32
+    Y0 = W.overstress(sc, U[:11, c, c])
+    from oracle import tile_boxes
+    ctx = Context(sc)
+    lvl = LinElastLevelGodunov(ctx, tile_boxes(64, 64, 32))
+    t = lvl.tuning()
+    t.plastic_fused = fused
+    lvl.set_tuning(t)
+    lvl.set_level(U, None)
+    dt = sc.dt()
+    for n in range(16):
+        lvl.step(n * dt, dt)
+    lvl.get_level(U, None)
+    assert lvl.status()[0] == 0
+    lvl.close()
+    ctx.close()
+    Yd = Y0 * (eta / (eta + k * dt)) ** 16
+    tol = 1e-12 if prec == A.TMK_PREC_FP64 else 1e-6
+    for side in (0, 11):
+        u = U[side:side + 11, c, c]
+        assert abs(W.overstress(sc, u) - Yd) <= tol * Y0, (W.overstress(sc, u), Yd)
+        assert abs(u[10] - (Y0 - Yd) / k) <= tol * Y0 / k

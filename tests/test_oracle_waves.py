@@ -323,6 +323,75 @@ def test_uniformly_sliding_slip_law_fault_converges_at_first_order():
     assert abs(e[-1, 0]) < 2e-4 and abs(e[-1, 1]) < 1e-5
 
 
+# Viscoplastic relaxation (srcLinElast/PlasticPhysicsF.ChF:74-181): a uniform
+# state above the Drucker-Prager yield surface feels no flux, so each level
+# step changes it only by the plastic correction, whose lambda =
+# Y / (dt (h + G + mu beta K) + eta) makes it one backward-Euler step of
+# dY/dt = -k Y / eta, k = G + mu beta K + h: after n steps the overstress is
+# exactly Y0 (eta / (eta + k dt))^n and the plastic strain (Y0 - Y) / k.
+def plastic_scenario(h: float = 0.0):
+    """No fault, absorbing edges, the 120 MPa / 70 MPa background (Y0 = 71 MPa
+    above yield) with the decks' Drucker-Prager parameters and hardening h."""
+    sc = S.Scenario(name="plastic_relaxation", nx=64, ny=64, dx=0.1, cfl=0.9, elastic=S._elastic(),
+                    scheme=S._scheme(A.TMK_FAULT_NONE, plasticity=1, bc=(0, 0, 0, 0, 0, 0)),
+                    plastic=S.plastic_params())
+    sc.plastic.h = h
+    return sc
+
+
+def overstress(sc, u) -> float:
+    """Y = sqrt(J2) - max(b + h gamma - mu sigma_mean, 0) of one side's cell state u (11 comps)."""
+    p = sc.plastic
+    sxx, syy, szz, sxy, sxz, syz = u[3:9]
+    sig = (sxx + syy + szz) / 3.0
+    J2 = ((sxx - syy) ** 2 + (syy - szz) ** 2 + (szz - sxx) ** 2) / 6.0 + sxy ** 2 + sxz ** 2 + syz ** 2
+    return math.sqrt(J2) - max(-p.mu * sig + p.b + u[10] * p.h, 0.0)
+
+
+def plastic_k(sc) -> float:
+    c = sc.constants()
+    return c["G"] + sc.plastic.mu * sc.plastic.beta * (c["lam"] + 2.0 * c["G"] / 3.0) + sc.plastic.h
+
+
+@pytest.mark.parametrize("h", [0.0, 5.0], ids=["no_hardening", "hardening"])
+def test_viscoplastic_relaxation_of_a_uniform_state(h):
+    """16 level steps at the CFL step: the centre cell's overstress equals the
+    backward-Euler closed form to 1e-12 of Y0 and its plastic strain (Y0 - Y)/k
+    to rounding, both sides, the state uniform around it.  Over two relaxation
+    times eta/k with 4, 8, 16, 32 steps the overstress reaches the ODE's
+    Y0 exp(-k t / eta) at first order (orders within 0.15 of 1)."""
+    sc = plastic_scenario(h)
+    k = plastic_k(sc)
+    eta = sc.plastic.eta
+    U = sc.initial_U()
+    c = G + 32
+    Y0 = overstress(sc, U[:11, c, c])
+    assert Y0 > 50.0
+    dt = sc.dt()
+    for n in range(16):
+        assert O.level_step(sc, U, None, O.tile_boxes(64, 64, 32), n * dt, dt, nthreads=4) == 0
+    Yd = Y0 * (eta / (eta + k * dt)) ** 16
+    for side in (0, 11):
+        u = U[side:side + 11, c, c]
+        assert abs(overstress(sc, u) - Yd) <= 1e-12 * Y0
+        assert abs(u[10] - (Y0 - Yd) / k) <= 1e-14 * Y0 / k
+    assert np.ptp(U[3:9, c - 4:c + 4, c - 4:c + 4], axis=(1, 2)).max() == 0.0
+
+    T = 2.0 * eta / k
+    errs = []
+    for n in (4, 8, 16, 32):
+        sc = plastic_scenario(h)
+        U = sc.initial_U()
+        dt = T / n
+        assert dt <= sc.dt()
+        for s in range(n):
+            assert O.level_step(sc, U, None, O.tile_boxes(64, 64, 32), s * dt, dt, nthreads=4) == 0
+        errs.append(overstress(sc, U[:11, c, c]) / (Y0 * math.exp(-k * T / eta)) - 1.0)
+    orders = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+    print(f"plastic relaxation h={h}: ODE errors {errs}, orders {orders}")
+    assert np.all(np.abs(orders - 1.0) < 0.15)
+
+
 # Oblique plane waves: the pulse travels along n = (cos th, sin th), so every
 # direction's transverse correction of the corner transport upwind scheme
 # carries it (an axis-aligned wave has zero transverse differences).  The
