@@ -13,7 +13,8 @@ properties of the reference formulas (tests/test_oracle_kat.py) and by exact
 solutions of the equations it discretises (tests/test_oracle_waves.py: plane
 waves in 2-D and 3-D, also through a refined hierarchy and at free and
 absorbing edges, converging at the scheme's order; uniformly sliding
-slip-weakening and rate-and-state faults meeting their 1-D answers).
+slip-weakening and rate-and-state faults meeting their 1-D answers; a uniform
+over-stressed state relaxing by the closed form of the plastic return).
 """
 from __future__ import annotations
 
