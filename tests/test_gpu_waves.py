@@ -143,7 +143,7 @@ def _gpu_oblique(n: int, wave: str, prec: int):
     return U, W.oblique_error(sc, wave, U, steps * dt)
 
 
-@pytest.mark.parametrize("wave", ["P", "S"])
+@pytest.mark.parametrize("wave", ["P", "S", "SH"])
 def test_oblique_wave_on_the_gpu(cuda_lib, wave):
     """The FP64 form reaches the oracle's state at n = 128 to 1e-11 relative
     per component (the parity bound of the FP64 form); the mixed form converges at the oracle's second order and
@@ -239,13 +239,14 @@ def _gpu_amr_wave(nc: int, r: int, wave: str, prec: int):
     return got, W.amr_wave_errors(sc, wave, got, covered, steps * dt)
 
 
-@pytest.mark.parametrize("wave", ["P", "S"])
+@pytest.mark.parametrize("wave", ["P", "S", "SH"])
 @pytest.mark.parametrize("r", [2, 4])
 def test_oblique_wave_through_amr_on_the_gpu(cuda_lib, wave, r):
     """The device hierarchy in the FP64 form ends where the oracle's does
-    (coarse grid of 64 cells: 2e-10 relative per patch and component, the
+    (coarse grid of 64 cells: 1e-9 relative per patch and component, the
     rounding of 18-23 coarse and up to 92 fine steps against the single step's
-    1e-12; the S wave on the 70 MPa background reaches 6e-11); in the
+    1e-12; the S wave on the 70 MPa background reaches 6e-11, the SH wave's
+    velocity, a component of 0.1 m/s, 6e-10); in the
     mixed form its fine- and coarse-level errors converge at the oracle's
     second order and lie within 5 % of the FP64 form's at 128 cells."""
     import oracle as O
@@ -254,7 +255,7 @@ def test_oblique_wave_through_amr_on_the_gpu(cuda_lib, wave, r):
     got, _ = _gpu_amr_wave(64, r, wave, A.TMK_PREC_FP64)
     for g, ref in zip(got, refs):
         for p in range(len(ref.boxes)):
-            assert rel_err(g.U[p][:, G:-G, G:-G], ref.U[p][:, G:-G, G:-G]) <= 2e-10
+            assert rel_err(g.U[p][:, G:-G, G:-G], ref.U[p][:, G:-G, G:-G]) <= 1e-9
     mixed = [_gpu_amr_wave(nc, r, wave, A.TMK_PREC_MIXED)[1] for nc in (64, 128)]
     fp64 = _gpu_amr_wave(128, r, wave, A.TMK_PREC_FP64)[1]
     for lvl in range(2):

@@ -400,7 +400,7 @@ def test_viscoplastic_relaxation_of_a_uniform_state(h):
 # pulse's travel time (cp t + R + stencil spread below the half-width).
 OBLIQUE_TH = math.radians(30.0)
 OBLIQUE_R = 1.5                       # km
-OBLIQUE_LEN = {"P": 8.0, "S": 11.0}   # km, side of the square domain
+OBLIQUE_LEN = {"P": 8.0, "S": 11.0, "SH": 11.0}   # km, side of the square domain
 
 
 def oblique_scenario(n: int, wave: str):
@@ -413,7 +413,8 @@ def wave_at(sc, wave: str, x: np.ndarray, y: np.ndarray, t: float) -> np.ndarray
     domain's centre, on the scenario's background.  A P wave along n carries
     v = -f/Zp n, sigma = f (r I + (1 - r) n n^T), r = lam/(lam + 2G); an S wave
     polarised in-plane along m = (-n_y, n_x) carries v = -f/Zs m,
-    sigma = f (n m^T + m n^T)."""
+    sigma = f (n m^T + m n^T); the antiplane (SH) wave, polarised along z,
+    carries v_z = -f/Zs, sigma_xz = f n_x, sigma_yz = f n_y."""
     c = sc.constants()
     n = (math.cos(OBLIQUE_TH), math.sin(OBLIQUE_TH))
     m = (-n[1], n[0])
@@ -429,11 +430,15 @@ def wave_at(sc, wave: str, x: np.ndarray, y: np.ndarray, t: float) -> np.ndarray
                 U[side + 3 + d] += f * (r + (1.0 - r) * n[d] * n[d])
             U[side + 5] += r * f
             U[side + 6] += f * (1.0 - r) * n[0] * n[1]
-        else:
+        elif wave == "S":
             for d in range(2):
                 U[side + d] += -f / c["Zs"] * m[d]
                 U[side + 3 + d] += 2.0 * f * n[d] * m[d]
             U[side + 6] += f * (n[0] * m[1] + n[1] * m[0])
+        else:
+            U[side + 2] += -f / c["Zs"]
+            U[side + 7] += f * n[0]
+            U[side + 8] += f * n[1]
     return U
 
 
@@ -451,7 +456,8 @@ def oblique_state(sc, wave: str, t: float):
     return wave_at(sc, wave, x, y, t), x * x + y * y
 
 
-OBLIQUE_COMPS = (0, 1, 3, 4, 6)       # vx, vy, sxx, syy, sxy
+# the components each wave carries: vx, vy, sxx, syy, sxy (in-plane); vz, sxz, syz (antiplane)
+OBLIQUE_COMPS = {"P": (0, 1, 3, 4, 6), "S": (0, 1, 3, 4, 6), "SH": (2, 7, 8)}
 
 
 def oblique_steps(sc, wave: str):
@@ -461,14 +467,15 @@ def oblique_steps(sc, wave: str):
 
 
 def oblique_error(sc, wave: str, U: np.ndarray, t: float) -> np.ndarray:
-    """L1 error over the central disc per component of OBLIQUE_COMPS,
+    """L1 error over the central disc per component the wave carries,
     normalised by the pulse's amplitude and width."""
     exact, r2 = oblique_state(sc, wave, t)
     disc = r2 <= OBLIQUE_R ** 2
-    return np.array([np.sum(np.abs(U[c] - exact[c])[disc]) * sc.dx ** 2 / (AMP * WIDTH) for c in OBLIQUE_COMPS])
+    return np.array([np.sum(np.abs(U[c] - exact[c])[disc]) * sc.dx ** 2 / (AMP * WIDTH)
+                     for c in OBLIQUE_COMPS[wave]])
 
 
-@pytest.mark.parametrize("wave", ["P", "S"])
+@pytest.mark.parametrize("wave", ["P", "S", "SH"])
 def test_oblique_plane_wave_converges_at_second_order(wave):
     """Every component's error falls at order 2.0-2.1 from 64 to 256 cells a
     side (the level tiled into 32x32 patches, which the exchange makes
@@ -627,12 +634,12 @@ def amr_wave_hierarchy(nc: int, r: int, wave: str):
 
 
 def amr_wave_errors(sc, wave: str, levels, covered, t: float, R: float = 1.5):
-    """L1 errors (per component of OBLIQUE_COMPS) of the fine level's valid
+    """L1 errors (per component the wave carries) of the fine level's valid
     cells and of the coarse level's uncovered cells within R of the centre."""
     C, F = levels
     out = []
     for lv, coarse in ((F, False), (C, True)):
-        e = np.zeros(len(OBLIQUE_COMPS))
+        e = np.zeros(len(OBLIQUE_COMPS[wave]))
         for p, b in enumerate(lv.boxes):
             x, y = _centres(sc, b, lv.dx, 0)
             exact = wave_at(sc, wave, x, y, t)
@@ -643,12 +650,12 @@ def amr_wave_errors(sc, wave: str, levels, covered, t: float, R: float = 1.5):
                 cov = (ii >= covered[0]) & (ii <= covered[1]) & (jj >= covered[0]) & (jj <= covered[1])
                 mask = (x * x + y * y <= R * R) & ~cov
             u = lv.U[p][:, G:-G, G:-G]
-            e += [np.sum(np.abs(u[c] - exact[c])[mask]) * lv.dx ** 2 for c in OBLIQUE_COMPS]
+            e += [np.sum(np.abs(u[c] - exact[c])[mask]) * lv.dx ** 2 for c in OBLIQUE_COMPS[wave]]
         out.append(e / (AMP * WIDTH))
     return out
 
 
-@pytest.mark.parametrize("wave", ["P", "S"])
+@pytest.mark.parametrize("wave", ["P", "S", "SH"])
 @pytest.mark.parametrize("r", [2, 4])
 def test_oblique_wave_through_amr_converges_at_second_order(wave, r):
     """Coarse grids of 32, 64 and 128 cells a side: fine-level and coarse-level
