@@ -218,6 +218,45 @@ def test_uniformly_sliding_fault_radiates_at_the_exact_slip_rate():
     np.testing.assert_allclose(U[6, G, mid], tau_d, atol=0.01 * (sc.elastic.sxy0 - tau_d))
 
 
+def test_uniformly_sliding_fault_with_linear_weakening():
+    """Slip weakening over Dc = 0.4 m (ibcLinElast/SWIBCF.ChF:208, f = fs -
+    (fs - fd) slip / Dc) on the uniformly loaded fault: while slip D < Dc the
+    1-D problem gives D' = a + b D, a = 2 (tau0 - fs sn) / Zs, b = 2 (fs - fd)
+    sn / (Zs Dc), so V = a e^(bt) and D = (a/b)(e^(bt) - 1).  After 0.36 s (24,
+    48, 96 steps of dt, dt/2, dt/4) the slip rate converges at first order
+    (friction takes the slip of the step before) and the slip at second
+    order; the state stays uniform along the fault."""
+    def scenario():
+        sc = S.slip_weakening(nx=128, ny=32, dx=0.1)
+        sc.sw.num_patches = 0
+        sc.sw.dw = 0.4
+        sc.elastic.sxy0 = 81.6
+        return sc
+    sc = scenario()
+    Zs, sn = sc.constants()["Zs"], -sc.elastic.syy0
+    a = 2.0 * (sc.elastic.sxy0 - sc.sw.fs * sn) / Zs
+    b = 2.0 * (sc.sw.fs - sc.sw.fd) * sn / (Zs * sc.sw.dw)
+    T = 24 * sc.dt()
+    V_ex, D_ex = a * math.exp(b * T), a / b * (math.exp(b * T) - 1.0)
+    assert D_ex < sc.sw.dw
+    errs = []
+    for k in (1, 2, 4):
+        sc = scenario()
+        U, B = sc.initial_U(), sc.initial_B()
+        dt = sc.dt() / k
+        for n in range(24 * k):
+            assert O.level_step(sc, U, B, O.tile_boxes(sc.nx, sc.ny, 64), n * dt, dt, nthreads=4) == 0
+        c = G + sc.nx // 2
+        errs.append([B[4, c] / V_ex - 1.0, B[7, c] / D_ex - 1.0])
+        assert np.ptp(B[4, c - 8:c + 8]) == 0.0
+    errs = np.array(errs)
+    orders = np.log2(np.abs(errs[:-1] / errs[1:]))
+    print("linear weakening: errors (V, D)", errs.tolist(), "orders", orders.tolist())
+    assert np.all((orders[:, 0] > 0.9) & (orders[:, 0] < 1.2))
+    assert np.all((orders[:, 1] > 1.8) & (orders[:, 1] < 2.1))
+    assert abs(errs[-1, 0]) < 0.03 and abs(errs[-1, 1]) < 1e-3
+
+
 def uniform_rs_scenario(prec=A.TMK_PREC_FP64, law=A.TMK_RS_AGING_LAW):
     """A rate-and-state fault (aging law, or the reference's slip law;
     velocity strengthening a=0.012, b=0.008, L=0.2 m, no nucleation) in steady
