@@ -257,16 +257,18 @@ def test_uniformly_sliding_fault_with_linear_weakening():
     assert abs(errs[-1, 0]) < 0.03 and abs(errs[-1, 1]) < 1e-3
 
 
-def uniform_rs_scenario(prec=A.TMK_PREC_FP64, law=A.TMK_RS_AGING_LAW):
+def uniform_rs_scenario(prec=A.TMK_PREC_FP64, law=A.TMK_RS_AGING_LAW, ab=(0.012, 0.008)):
     """A rate-and-state fault (aging law, or the reference's slip law;
-    velocity strengthening a=0.012, b=0.008, L=0.2 m, no nucleation) in steady
+    velocity strengthening a=0.012, b=0.008 by default, or weakening with
+    the benchmarked a=0.008, b=0.012; L=0.2 m, no nucleation) in steady
     sliding at 0.5 m/s whose shear load is then 2 MPa above that state's:
-    every face speeds up and relaxes together, the 1-D problem of a uniformly
-    sliding fault.  Both laws share the steady state."""
+    every face speeds up together, the 1-D problem of a uniformly sliding
+    fault.  Both laws share the steady state."""
     sc = S.rate_state(nx=128, ny=64, dx=0.05, precision=prec, state_law=law)
     rs = sc.rs
     rs.nsig = 0.0
-    rs.a, rs.b, rs.L = 0.012, 0.008, 0.2
+    rs.a, rs.b = ab
+    rs.L = 0.2
     sn = -sc.elastic.syy0
     Zs = sc.constants()["Zs"]
     Vi = 0.5
@@ -304,13 +306,14 @@ def uniform_rs_answer(sc, t_end):
     return (lambda t: V_of(float(sol.sol(t)[0]))), (lambda t: float(sol.sol(t)[0]))
 
 
-def test_uniformly_sliding_rate_and_state_fault_follows_its_ode():
+@pytest.mark.parametrize("ab", [(0.012, 0.008), (0.008, 0.012)], ids=["strengthening", "weakening"])
+def test_uniformly_sliding_rate_and_state_fault_follows_its_ode(ab):
     """60 steps (until the domain's x edges' disturbances could reach the centre
     faces): the slip rate the level step stores (boundary component 2) is the
     ODE's at the step's midpoint, where the scheme's time-centred face state
     sits, to 1e-5, and the state variable (component 10) the ODE's at the step's
-    end to 1e-6; the slip rate changes by 8 % over the run."""
-    sc = uniform_rs_scenario()
+    end to 1e-6; the slip rate grows by over 5 % in the run."""
+    sc = uniform_rs_scenario(ab=ab)
     U, B = sc.initial_U(), sc.initial_B()
     dt = sc.dt()
     V_ode, psi_ode = uniform_rs_answer(sc, 61 * dt)
