@@ -218,6 +218,39 @@ def test_uniformly_sliding_fault_radiates_at_the_exact_slip_rate():
     np.testing.assert_allclose(U[6, G, mid], tau_d, atol=0.01 * (sc.elastic.sxy0 - tau_d))
 
 
+@pytest.mark.parametrize("r", [2, 4])
+def test_uniformly_sliding_fault_through_amr(r):
+    """The uniformly sliding slip-weakening fault (instant weakening) under a
+    subcycled two-level hierarchy whose fine level covers the fault row from
+    x = 0.8 to 5.6 km (rows 0-7 of the coarse grid): after 10 coarse steps the
+    fine faces at the box's centre and the coarse faces there (the fine fault
+    data averaged down) carry the exact slip rate, traction and slip to
+    rounding.  (Within cp t of the fine box's x edges the coarse state's linear
+    interpolation in time across the radiated front moves V by a few percent.)"""
+    sc = uniform_sliding_scenario()          # 64 x 32 cells of 0.1 km
+    V, tau_d = uniform_sliding_answer(sc)
+    nb = sc.nbdry
+    levels = []
+    for dom, dx, boxes in (((0, 0, 63, 31), sc.dx, O.tile_boxes(64, 32, 16)),
+                           ((0, 0, 64 * r - 1, 32 * r - 1), sc.dx / r, [(8 * r, 0, 56 * r - 1, 8 * r - 1)])):
+        lv = O.LevelData(dom, dx, boxes, nb)
+        for p, b in enumerate(lv.boxes):
+            lv.U[p][:] = sc.background()[:, None, None]
+            if lv.B[p] is not None:
+                lv.B[p][:] = sc.initial_B(xlo=b[0], xhi=b[2])
+        levels.append(lv)
+    dt = sc.dt()
+    assert O.amr_run(sc, levels, [r], 0.0, dt, 10, nthreads=4) == 0
+    t = 10 * dt
+    C, F = levels
+    fine = F.B[0][:, G:-G][:, 24 * r - 4 * r:24 * r + 4 * r]        # fine faces of coarse x 28..35
+    coarse = np.concatenate([C.B[p][:, G:-G] for p in range(len(C.boxes)) if C.B[p] is not None], axis=1)[:, 28:36]
+    for B in (fine, coarse):
+        np.testing.assert_allclose(B[4], V, rtol=1e-13)
+        np.testing.assert_allclose(B[2], tau_d, rtol=1e-13)
+        np.testing.assert_allclose(B[7], V * t, rtol=1e-13)
+
+
 def test_uniformly_sliding_fault_with_linear_weakening():
     """Slip weakening over Dc = 0.4 m (ibcLinElast/SWIBCF.ChF:208, f = fs -
     (fs - fd) slip / Dc) on the uniformly loaded fault: while slip D < Dc the
