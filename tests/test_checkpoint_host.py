@@ -32,3 +32,23 @@ def test_scenario_round_trips_through_an_archive(name, tmp_path):
     np.testing.assert_array_equal(back.initial_U(), sc.initial_U())
     if sc.scheme.fault_law != A.TMK_FAULT_NONE:
         np.testing.assert_array_equal(back.initial_B(), sc.initial_B())
+
+
+def test_3d_level_refuses_fabs_of_another_shape_or_type():
+    """LinElastLevelGodunov3D copies whole FABs of patch_shapes(p) through the
+    library: arrays of another shape, type or layout are refused on the host
+    before any copy (checked here without a device level)."""
+    from tetemoko_gb300.level import LinElastLevelGodunov3D
+
+    class _Ctx:
+        sc = S.rate_state(nx=12, ny=10, dx=0.1)
+
+    lv = LinElastLevelGodunov3D.__new__(LinElastLevelGodunov3D)
+    lv.ctx, lv.boxes, lv.domain = _Ctx(), [((0, 0, 0), (5, 4, 3))], ((0, 0, 0), (11, 9, 7))
+    ushape, bshape = lv.patch_shapes(0)
+    assert ushape == (22, 12, 13, 14) and bshape == (_Ctx.sc.nbdry, 12, 14)
+    lv._checked(0, np.zeros(ushape), np.zeros(bshape), True)
+    for U, B in ((np.zeros((22, 12, 13, 13)), None), (np.zeros(ushape, dtype=np.float32), None),
+                 (np.zeros(ushape[::-1]).T, None), (np.zeros(ushape), np.zeros((11, 12, 13)))):
+        with pytest.raises(ValueError):
+            lv._checked(0, U, B, True)

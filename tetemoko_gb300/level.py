@@ -252,6 +252,21 @@ class LinElastLevelGodunov3D:
         n = [hi[d] - lo[d] + 1 + 2 * g for d in range(3)]
         return (22, n[2], n[1], n[0]), (self.ctx.sc.nbdry, n[2], n[0])
 
+    def _checked(self, p, U, B, host: bool):
+        """The library copies whole FABs of patch_shapes(p): refuse arrays of
+        another shape, type or layout before any copy."""
+        ushape, bshape = self.patch_shapes(p)
+        for x, shape, what in ((U, ushape, "U"), (B, bshape, "B")):
+            if x is None:
+                continue
+            if tuple(x.shape) != shape:
+                raise ValueError(f"patch {p}: {what} has shape {tuple(x.shape)}, expected {shape}")
+            if host:
+                if not isinstance(x, np.ndarray) or x.dtype != np.float64 or not x.flags.c_contiguous:
+                    raise ValueError(f"patch {p}: {what} must be a C-contiguous float64 numpy array")
+            elif x.dtype != _torch().float64 or not x.is_cuda or not x.is_contiguous():
+                raise ValueError(f"patch {p}: {what} must be a contiguous float64 CUDA tensor")
+
     def set_patch(self, p, U, B=None):
         """U (and B on the fault plane): numpy arrays (host) or CUDA tensors
         (device) of patch_shapes(p)."""
@@ -259,6 +274,7 @@ class LinElastLevelGodunov3D:
         if host:
             U = np.ascontiguousarray(U, dtype=np.float64)
             B = np.ascontiguousarray(B, dtype=np.float64) if B is not None else None
+        self._checked(p, U, B, host)
         ptr = (lambda x: x.ctypes.data) if host else (lambda x: x.data_ptr())
         A.check(self.lib.tmk_level3d_set_patch(self.h, p, ptr(U), ptr(B) if B is not None else None, int(host)),
                 "tmk_level3d_set_patch")
@@ -271,6 +287,7 @@ class LinElastLevelGodunov3D:
         if B is None and self.touches_fault(p):
             B = np.empty(bshape)
         host = isinstance(U, np.ndarray)
+        self._checked(p, U, B, host)
         ptr = (lambda x: x.ctypes.data) if host else (lambda x: x.data_ptr())
         A.check(self.lib.tmk_level3d_get_patch(self.h, p, ptr(U), ptr(B) if B is not None else None, int(host)),
                 "tmk_level3d_get_patch")
