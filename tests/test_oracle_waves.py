@@ -571,6 +571,26 @@ def test_oblique_plane_wave_converges_at_second_order(wave):
     assert np.all(orders > 1.8)
 
 
+@pytest.mark.parametrize("wave", ["P", "SH"])
+@pytest.mark.parametrize("order,expect", [(1, (1.8, 2.2)), (0, (0.85, 1.1))], ids=["plm", "first_order"])
+def test_oblique_wave_with_the_other_normal_predictors(wave, order, expect):
+    """The decks' other normal predictors (LinElastPatchGodunov::PLMNormalPred
+    with fourth-order slopes, and the piecewise-constant one of
+    normal_pred_order 0) on the oblique wave: PLM converges at second order,
+    the piecewise-constant predictor at first order (64 -> 256 cells)."""
+    errs = []
+    for n in (64, 128, 256):
+        sc = oblique_scenario(n, wave)
+        sc.scheme.normal_pred_order = order
+        U, _ = oblique_state(sc, wave, 0.0)
+        steps, dt = oblique_steps(sc, wave)
+        for k in range(steps):
+            assert O.level_step(sc, U, None, O.tile_boxes(n, n, 32), k * dt, dt, nthreads=4) == 0
+        errs.append(oblique_error(sc, wave, U, steps * dt))
+    orders = np.log2(errs[1] / errs[2])
+    assert np.all((orders > expect[0]) & (orders < expect[1])), orders
+
+
 # The same in 3-D (CH_SPACEDIM == 3): a plane wave along a direction with no
 # zero component, so that all six transverse corrections of the 3-D corner
 # transport upwind step carry it; the S wave is polarised along the unit
