@@ -572,16 +572,20 @@ def test_oblique_plane_wave_converges_at_second_order(wave):
 
 
 @pytest.mark.parametrize("wave", ["P", "SH"])
-@pytest.mark.parametrize("order,expect", [(1, (1.8, 2.2)), (0, (0.85, 1.1))], ids=["plm", "first_order"])
-def test_oblique_wave_with_the_other_normal_predictors(wave, order, expect):
+@pytest.mark.parametrize("order,charlim,expect", [(1, 0, (1.8, 2.2)), (0, 0, (0.85, 1.1)), (2, 1, (1.8, 2.2))],
+                         ids=["plm", "first_order", "ppm_char_limiting"])
+def test_oblique_wave_with_the_other_normal_predictors(wave, order, charlim, expect):
     """The decks' other normal predictors (LinElastPatchGodunov::PLMNormalPred
-    with fourth-order slopes, and the piecewise-constant one of
-    normal_pred_order 0) on the oblique wave: PLM converges at second order,
-    the piecewise-constant predictor at first order (64 -> 256 cells)."""
+    with fourth-order slopes, the piecewise-constant one of normal_pred_order
+    0, and PPM limited in characteristic instead of primitive variables) on
+    the oblique wave: PLM and characteristic limiting converge at second
+    order, the piecewise-constant predictor at first order (64 -> 256 cells)."""
     errs = []
     for n in (64, 128, 256):
         sc = oblique_scenario(n, wave)
         sc.scheme.normal_pred_order = order
+        if charlim:
+            sc.scheme.use_prim_limiting, sc.scheme.use_char_limiting = 0, 1
         U, _ = oblique_state(sc, wave, 0.0)
         steps, dt = oblique_steps(sc, wave)
         for k in range(steps):
