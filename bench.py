@@ -414,92 +414,6 @@ def amr3_measurement(coarse_steps, stream, regrid_interval=2):
     new levels, prolongation, copy) by the host clock, reported apart."""
     import torch
     from tetemoko_gb300 import _capi as A, scenarios as S
-    from tetemoko_gb300.amr import AMRHierarchy, refine_domain, regrid
-    from tetemoko_gb300.level import Context, LinElastLevelGodunov
-    sc = S.slip_weakening(nx=512, ny=256, precision=A.TMK_PREC_MIXED, plasticity=True, cohesion=1.0, plas_psi=30)
-    ctx = Context(sc)
-    ratios = [4, 4]
-    base = LinElastLevelGodunov(ctx, tile_boxes(0, 0, sc.nx - 1, sc.ny - 1, 64))
-    U, B = sc.initial_U(), sc.initial_B()
-    base.set_level(U, B)
-    box_args = dict(block_factor=8, max_grid_size=64, fill_ratio=0.7)
-
-    def tps(initial):
-        return [A.tag_params(level=l, initial=initial, refine_thresh=0.01, tag_buffer=2, slip_rate_thresh=1e-3)
-                for l in range(2)]
-
-    # initial hierarchy from tagCellsInit's nucleation marks (levels built one at a time)
-    t0 = time.perf_counter()
-    levels = regrid([base], ratios, tps(True), max_level=2, stream=stream, **box_args)
-    torch.cuda.synchronize()
-    init_s = time.perf_counter() - t0
-    dt0 = sc.dt()
-    t = 0.0
-    step_ms, regrid_s, updates, nregrid = 0.0, 0.0, 0, 0
-    sizes = set()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    done = 0
-    while done < coarse_steps:
-        h = AMRHierarchy(levels, ratios[:len(levels) - 1], time=t)
-        n = min(regrid_interval, coarse_steps - done)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(n):
-            h.step(dt0, stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        step_ms += e0.elapsed_time(e1)
-        updates += h.cell_updates() * n
-        t = h.time(0)
-        h.close()
-        done += n
-        if done < coarse_steps:
-            r0 = time.perf_counter()
-            old = levels
-            levels = regrid(levels, ratios, tps(False), stream=stream, **box_args)
-            torch.cuda.synchronize()
-            regrid_s += time.perf_counter() - r0
-            nregrid += 1
-            for lv in old[1:]:
-                if all(lv is not n_ for n_ in levels):
-                    lv.close()
-        for lv in levels[1:]:
-            for b in lv.boxes:
-                sizes.add(max(b[2] - b[0] + 1, b[3] - b[1] + 1))
-    status = [lv.status()[1] for lv in levels]
-    cells = [sum((b[2] - b[0] + 1) * (b[3] - b[1] + 1) for b in lv.boxes) for lv in levels]
-    out = {"value": updates / (step_ms * 1e-3), "unit": "cell-updates/s",
-           "ms_per_coarse_step": step_ms / coarse_steps, "coarse_steps": coarse_steps,
-           "regrids": nregrid, "regrid_ms_each": 1e3 * regrid_s / max(1, nregrid),
-           "initial_hierarchy_ms": 1e3 * init_s,
-           "cells_per_level_at_end": cells, "patches_per_level_at_end": [len(lv.boxes) for lv in levels],
-           "patch_side_range": [min(sizes), max(sizes)] if sizes else None,
-           "config": "3 levels, ratio 4, base 512x256 at dx=0.1 km (finest 6.25 m), slip weakening (mu_s 0.677, "
-                     "mu_d 0.525, Dc 0.4 m, side 2 at offset 11), Drucker-Prager plasticity with 1 MPa cohesion "
-                     "(b = c cos(phi), an extension), background from plas_Psi = 30 deg, tags: fault-row slip rate "
-                     ">= 1e-3 m/s (an extension) or velocity gradient >= 0.01, tag buffer 2, boxes: blocking "
-                     "factor 8, max 64, fill ratio 0.7, regrid every 2 coarse steps, FP32 volume / FP64 fault",
-           "execution": "tmk_amr_step per coarse step (levels change every regrid); regrid on the device (tags, "
-                        "prolongation, copy) with host box generation",
-           "device_status": status}
-    for lv in levels:
-        lv.close()
-    ctx.close()
-    return out
-
-
-def amr3_measurement(coarse_steps, stream, regrid_interval=2):
-    """Three levels at ratio 4 over the slip-weakening 512x256 base (dx 0.1 km,
-    finest 6.25 m) with Drucker-Prager plasticity (1 MPa cohesion, background
-    normal stresses from plas_Psi = 30 degrees), refined by device tags on the
-    fault row's slip rate (>= 1e-3 m/s) and on velocity gradients, regridded
-    every `regrid_interval` coarse steps with boxes of 8 to 64 cells
-    (blocking factor 8, maximum 64, Berger-Rigoutsos on the host), mixed form.
-    The subcycled steps are timed with CUDA events; each regrid (tags, boxes,
-    new levels, prolongation, copy) by the host clock, reported apart."""
-    import torch
-    from tetemoko_gb300 import _capi as A, scenarios as S
     from tetemoko_gb300.amr import AMRHierarchy, regrid
     from tetemoko_gb300.level import Context, LinElastLevelGodunov
     sc = S.slip_weakening(nx=512, ny=256, precision=A.TMK_PREC_MIXED, plasticity=True, cohesion=1.0, plas_psi=30)
