@@ -174,6 +174,59 @@ def test_pulse_at_a_domain_edge_converges_at_second_order(free):
     assert np.all(orders > 1.8)
 
 
+# An antiplane (SH) pulse reflected by the free surface at x-hi: no mode
+# conversion, the reflected pulse mirrors the incident one with the same
+# amplitude, so sigma_xz vanishes and v_z doubles at the wall.  Compared in the
+# strip within 2.5 km of the wall and 1 km of the centre line.
+def sh_reflection_errors(theta_deg: float, ns=(64, 128, 256)):
+    L, d0, travel = 11.0, 1.2, 2.4
+    th = math.radians(theta_deg)
+    n0, n1 = math.cos(th), math.sin(th)
+    out = []
+    for n in ns:
+        e = S._elastic()
+        e.sxy0 = 0.0
+        sc = S.Scenario(name="sh_reflection", nx=n, ny=n, dx=L / n, cfl=0.9, elastic=e,
+                        scheme=S._scheme(A.TMK_FAULT_NONE, bc=(0, 1, 0, 0, 0, 0)))
+        x, y = _centres(sc, (0, 0, n - 1, n - 1), sc.dx, G)
+
+        def state(t):
+            cs, X = sc.elastic.cs, 0.5 * L
+            f = _pulse(x * n0 + y * n1 - (X * n0 - d0) - cs * t)
+            g = _pulse(-x * n0 + y * n1 + X * n0 + d0 - cs * t)       # the mirror image in x = X
+            U = np.empty((22,) + x.shape)
+            U[:] = sc.background()[:, None, None]
+            for side in (0, 11):
+                U[side + 2] += -(f + g) / sc.constants()["Zs"]
+                U[side + 7] += (f - g) * n0
+                U[side + 8] += (f + g) * n1
+            return U
+
+        U = state(0.0)
+        steps = int(math.ceil(travel / (sc.elastic.cs * sc.dt())))
+        dt = travel / (sc.elastic.cs * steps)
+        for k in range(steps):
+            assert O.level_step(sc, U, None, O.tile_boxes(n, n, 32), k * dt, dt, nthreads=4) == 0
+        exact = state(steps * dt)
+        strip = (x > 0.5 * L - 2.5) & (np.abs(y) < 1.0)
+        out.append(np.array([np.sum(np.abs(U[q] - exact[q])[strip]) * sc.dx ** 2 / (AMP * WIDTH) for q in (2, 7, 8)]))
+    return np.array(out)
+
+
+def test_sh_pulse_reflected_by_a_free_surface():
+    """Normal incidence: v_z and sigma_xz converge at second order (64 -> 256
+    cells).  At 30 degrees sigma_xz still converges at second order, and v_z
+    and sigma_yz at least at first order (the scheme's edge cells take
+    one-sided differences)."""
+    e0 = sh_reflection_errors(0.0)
+    o0 = np.log2(e0[1, :2] / e0[2, :2])
+    assert np.all(o0 > 1.8), o0
+    e30 = sh_reflection_errors(30.0)
+    o30 = np.log2(e30[1] / e30[2])
+    assert o30[1] > 1.8 and o30[0] > 0.9 and o30[2] > 0.9, o30
+    assert np.all(e30[2] < 0.1)
+
+
 def uniform_sliding_scenario(prec=A.TMK_PREC_FP64):
     """A slip-weakening fault loaded above its static strength everywhere
     (tau0 = 81.6 MPa > mu_s sigma_n = 81.24 MPa, no nucleation patch) with an
